@@ -1,0 +1,210 @@
+"""Test infrastructure only: ctypes access to the CPU oracle (liboracle.so,
+built from oracle/transport_oracle.c by ``make -C oracle``).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, as the checker.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    return os.path.join(HERE, "liboracle.so")
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        path = os.path.join(HERE, "liboracle.so")
+        src = os.path.join(HERE, "transport_oracle.c")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            build()
+        L = ctypes.CDLL(path)
+        L.orc_transport_run.restype = ctypes.c_int
+        L.orc_transport_run.argtypes = [
+            ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_double, ctypes.c_double,
+            _dp, _dp, _dp,
+            ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+            ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+            ctypes.c_double, _ip, _ip, _ip, _ip, _ip, _ip, _ip,
+            _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
+        L.orc_fill_lm.restype = ctypes.c_int
+        L.orc_fill_lm.argtypes = [ctypes.c_int, _ip, ctypes.c_int, _ip, _ip, _ip]
+        L.orc_csr_pattern.restype = ctypes.c_int
+        L.orc_csr_pattern.argtypes = [ctypes.c_int, ctypes.c_int, _ip, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_symrcm.restype = None
+        L.orc_symrcm.argtypes = [ctypes.c_int, _ip, _ip, _ip]
+        L.orc_reorder_csr.restype = ctypes.c_int
+        L.orc_reorder_csr.argtypes = [ctypes.c_int, ctypes.c_int, _ip, _ip, _ip, ctypes.c_int,
+                                      _ip, ctypes.c_int, _ip]
+        L.orc_ede_pattern.restype = ctypes.c_int
+        L.orc_ede_pattern.argtypes = [ctypes.c_int, ctypes.c_int, _ip, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_csrmv.restype = None
+        L.orc_csrmv.argtypes = [ctypes.c_int, _ip, _ip, _dp, _dp, _dp]
+        L.orc_ebemv.restype = None
+        L.orc_ebemv.argtypes = [ctypes.c_int, ctypes.c_int, _ip, _dp, _dp, _dp]
+        L.orc_edemv.restype = None
+        L.orc_edemv.argtypes = [ctypes.c_int, ctypes.c_int, _ip, _dp, _dp, _dp]
+        L.orc_ilu0_factor.restype = ctypes.c_int
+        L.orc_ilu0_factor.argtypes = [ctypes.c_int, _ip, _ip, _dp, _dp, _dp]
+        L.orc_ilu0_apply.restype = None
+        L.orc_ilu0_apply.argtypes = [ctypes.c_int, _ip, _ip, _dp, _dp, _dp, _dp]
+        L.orc_csr_gmres.restype = ctypes.c_int
+        L.orc_csr_gmres.argtypes = [ctypes.c_int, _ip, _ip, _dp, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_double, _dp, _dp]
+        L.orc_ddot.restype = ctypes.c_double
+        L.orc_ddot.argtypes = [ctypes.c_int, _dp, _dp]
+        _lib = L
+    return _lib
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def run_transport(x, y, node_type, vert, k, gamma, beta, fsrc, upresc, scheme="CSR",
+                  reord="NOT", precond="ILU0", shock="CAU", hshock="2sqrtArea", outflow="NOT",
+                  kmax=30, lmax=1000, tol=1e-8, npicard=3, nonlin_tol=0.0, Pin=None):
+    """Full steady-transport run; same outputs as the reference harness."""
+    L = lib()
+    nn, ne = len(x), len(vert)
+    node_type = _c(node_type, np.int32)
+    neq_ub = int((node_type >= 1).sum())
+    nnz_ub = 9 * ne + 1
+    info = np.zeros(4, np.int32)
+    node_id = np.zeros(nn, np.int32)
+    etype = np.zeros(ne, np.int32)
+    IA = np.zeros(neq_ub + 1, np.int32)
+    JA = np.zeros(max(nnz_ub, 6 * ne + 2), np.int32)
+    sbe = np.zeros(9 * ne, np.int32)
+    order = np.zeros(3 * ne, np.int32)
+    Afirst = np.zeros(max(9 * ne, 4 * (3 * ne + 1), nnz_ub))
+    Ffirst = np.zeros(neq_ub + 1)
+    Fprec = np.zeros(neq_ub + 1)
+    if Pin is None:
+        Pin = np.random.default_rng(7).uniform(-1.0, 1.0, neq_ub + 1)
+    Pin = _c(Pin, np.float64)
+    Qmv = np.zeros(neq_ub + 1)
+    Zpc = np.zeros(neq_ub + 1)
+    uhist = np.zeros(npicard * (neq_ub + 1))
+    iters = np.zeros(npicard, np.int32)
+    nit = L.orc_transport_run(
+        nn, _c(x, np.float64), _c(y, np.float64), node_type, ne, _c(vert, np.int32).reshape(-1),
+        float(k), float(gamma), _c(beta, np.float64).reshape(-1), _c(fsrc, np.float64).reshape(-1),
+        _c(upresc, np.float64), scheme.encode(), reord.encode(), precond.encode(), shock.encode(),
+        hshock.encode(), outflow.encode(), kmax, lmax, tol, npicard, nonlin_tol,
+        info, node_id, etype, IA, JA, sbe, order, Afirst, Ffirst, Fprec, Pin, Qmv, Zpc,
+        uhist, iters)
+    if nit < 0:
+        raise RuntimeError(f"oracle run failed ({nit})")
+    neq, nnz, nedge, bw = (int(v) for v in info)
+    out = dict(neq=neq, nnzero=nnz, nedge=nedge, bandwidth=bw, npicard_run=nit,
+               node_id=node_id, etype=etype, Ffirst=Ffirst, Fprec=Fprec, Pin=Pin, Qmv=Qmv,
+               Zpc=Zpc, uhist=uhist[: nit * (neq + 1)].reshape(nit, neq + 1), iters=iters[:nit])
+    if scheme.upper() == "CSR":
+        out.update(IA=IA[: neq + 1], JA=JA[:nnz], sbe=sbe.reshape(ne, 9), Afirst=Afirst[: nnz + 1])
+    elif scheme.upper() == "EDE":
+        out.update(lm2=JA[: 2 * nedge].reshape(nedge, 2), sbe=sbe[: 3 * ne].reshape(ne, 3),
+                   order=order.reshape(ne, 3), Afirst=Afirst[: 4 * (nedge + 1)].reshape(nedge + 1, 4))
+    else:
+        out.update(Afirst=Afirst[: 9 * ne].reshape(ne, 9))
+    return out
+
+
+def csr_pattern(neq, lm):
+    """(IA, JA, sbe) of csr_Initialization for an lm array [nel, 3]."""
+    L = lib()
+    lm = _c(lm, np.int32).reshape(-1)
+    nel = lm.size // 3
+    nnz = L.orc_csr_pattern(neq, nel, lm, None, None, None)
+    IA = np.zeros(neq + 1, np.int32)
+    JA = np.zeros(max(nnz, 1), np.int32)
+    sbe = np.zeros(9 * nel, np.int32)
+    L.orc_csr_pattern(neq, nel, lm, IA.ctypes.data, JA.ctypes.data, sbe.ctypes.data)
+    return IA, JA[:nnz], sbe.reshape(nel, 9)
+
+
+def fill_lm(node_type, vert):
+    L = lib()
+    node_type = _c(node_type, np.int32)
+    vert = _c(vert, np.int32).reshape(-1)
+    node_id = np.zeros(node_type.size, np.int32)
+    lm = np.zeros(vert.size, np.int32)
+    neq = L.orc_fill_lm(node_type.size, node_type, vert.size // 3, vert, node_id, lm)
+    return neq, node_id, lm.reshape(-1, 3)
+
+
+def symrcm(IA, JA):
+    L = lib()
+    n = IA.size - 1
+    perm = np.zeros(n, np.int32)
+    L.orc_symrcm(n, _c(IA, np.int32), _c(JA, np.int32), perm)
+    return perm
+
+
+def csrmv(IA, JA, AA, P):
+    L = lib()
+    n = IA.size - 1
+    Q = np.zeros(n + 1)
+    L.orc_csrmv(n, _c(IA, np.int32), _c(JA, np.int32), _c(AA, np.float64), _c(P, np.float64), Q)
+    return Q
+
+
+def ebemv(neq, lm, A, P):
+    L = lib()
+    Q = np.zeros(neq + 1)
+    P = np.array(P, dtype=np.float64, copy=True)
+    L.orc_ebemv(neq, len(lm), _c(lm, np.int32).reshape(-1), _c(A, np.float64).reshape(-1), P, Q)
+    return Q
+
+
+def edemv(neq, lm2, A, P):
+    L = lib()
+    Q = np.zeros(neq + 1)
+    P = np.array(P, dtype=np.float64, copy=True)
+    L.orc_edemv(neq, len(lm2), _c(lm2, np.int32).reshape(-1), _c(A, np.float64).reshape(-1), P, Q)
+    return Q
+
+
+def ilu0(IA, JA, AA):
+    L = lib()
+    n = IA.size - 1
+    LU = np.zeros(IA[-1] + 1)
+    Dinv = np.zeros(n + 1)
+    rc = L.orc_ilu0_factor(n, _c(IA, np.int32), _c(JA, np.int32), _c(AA, np.float64), LU, Dinv)
+    if rc:
+        raise ZeroDivisionError(f"zero pivot in row {rc - 1}")
+    return LU, Dinv
+
+
+def ilu0_apply(IA, JA, LU, Dinv, p):
+    L = lib()
+    n = IA.size - 1
+    z = np.zeros(n + 1)
+    L.orc_ilu0_apply(n, _c(IA, np.int32), _c(JA, np.int32), _c(LU, np.float64),
+                     _c(Dinv, np.float64), _c(p, np.float64), z)
+    return z
+
+
+def csr_gmres(IA, JA, AA, B, use_ilu0=True, kmax=30, lmax=1000, tol=1e-8):
+    """pgmres on an assembled CSR system; returns (X, iterations, M^-1 B)."""
+    L = lib()
+    n = IA.size - 1
+    B = np.array(B, dtype=np.float64, copy=True)
+    X = np.zeros(n + 1)
+    it = L.orc_csr_gmres(n, _c(IA, np.int32), _c(JA, np.int32), _c(AA, np.float64),
+                         1 if use_ilu0 else 0, kmax, lmax, tol, B, X)
+    return X, it, B

@@ -1,0 +1,150 @@
+"""Generate golden vectors by running the reference's own steady-transport C
+path (compiled from its sources by ``make -C oracle ref`` into
+oracle/_ref/libfemref.so, driven by oracle/ref_harness.c).
+
+Usage:  python tests/golden/make_golden.py        (writes tests/golden/*.npz)
+
+The fixtures hold the inputs (mesh, node types, coefficient arrays evaluated by
+the reference's plug-in callbacks) and every output the harness dumps: CSR
+pattern, CSR_by_Element, node renumbering, EDE edge list, the first Build's
+matrix storage and RHS, F after precond_setup, one matvec and one precond
+application on a seeded vector, u after each Picard solve and the GMRES
+iteration counts.  Only this script reads the reference library; the tests
+read the committed .npz files.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from fem_codes_gb300.mesh import structured_mesh  # noqa: E402
+
+PROBLEMS = {"SKEW": 0, "CONVECTION": 1, "REACTION": 2, "HEMKER": 3, "VALIDACAO": 4}
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def load_ref(fast: bool = False) -> ctypes.CDLL:
+    name = "libfemref_fast.so" if fast else "libfemref.so"
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", name))
+    f = lib.ref_transport_run
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int,
+                  ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                  ctypes.c_char_p, ctypes.c_char_p,
+                  ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                  _ip, _ip, _ip, _dp, _dp, _dp,
+                  _ip, _ip, _ip, _ip,
+                  _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
+    return lib
+
+
+def node_types(mesh, rule: str) -> np.ndarray:
+    if rule == "inflow":      # x == 0 or y == 0 prescribed
+        presc = (mesh.x == 0.0) | (mesh.y == 0.0)
+    elif rule == "all":       # whole boundary prescribed
+        presc = (mesh.x == 0.0) | (mesh.y == 0.0) | (mesh.x == 1.0) | (mesh.y == 1.0)
+    else:
+        raise ValueError(rule)
+    return np.where(presc, 0, 1).astype(np.int32)
+
+
+def run_ref(lib, mesh, ntype, problem="SKEW", scheme="CSR", reord="NOT", precond="ILU0",
+            shock="CAU", hshock="2sqrtArea", outflow="NOT", kmax=30, lmax=1000,
+            tol=1e-8, npicard=3, nonlin_tol=0.0, seed=7):
+    nn, ne = mesh.nnodes, mesh.nel
+    neq_ub = int((ntype >= 1).sum())
+    nnz_ub = 9 * ne + 1
+    info = np.zeros(4, np.int32)
+    node_id = np.zeros(nn, np.int32)
+    etype = np.zeros(ne, np.int32)
+    beta = np.zeros(2 * ne)
+    fsrc = np.zeros(3 * ne)
+    upresc = np.zeros(nn)
+    IA = np.zeros(neq_ub + 1, np.int32)
+    JA = np.zeros(max(nnz_ub, 6 * ne + 2), np.int32)
+    sbe = np.zeros(9 * ne, np.int32)
+    order = np.zeros(3 * ne, np.int32)
+    Afirst = np.zeros(max(9 * ne, 4 * (3 * ne + 1), nnz_ub))
+    Ffirst = np.zeros(neq_ub + 1)
+    Fprec = np.zeros(neq_ub + 1)
+    rng = np.random.default_rng(seed)
+    Pin = rng.uniform(-1.0, 1.0, neq_ub + 1)
+    Qmv = np.zeros(neq_ub + 1)
+    Zpc = np.zeros(neq_ub + 1)
+    uhist = np.zeros(npicard * (neq_ub + 1))
+    iters = np.zeros(npicard, np.int32)
+    nit = lib.ref_transport_run(
+        nn, np.ascontiguousarray(mesh.x), np.ascontiguousarray(mesh.y), ntype, ne,
+        np.ascontiguousarray(mesh.vert.reshape(-1)), PROBLEMS[problem],
+        scheme.encode(), reord.encode(), precond.encode(), shock.encode(), hshock.encode(),
+        outflow.encode(), kmax, lmax, tol, npicard, nonlin_tol,
+        info, node_id, etype, beta, fsrc, upresc, IA, JA, sbe, order,
+        Afirst, Ffirst, Fprec, Pin, Qmv, Zpc, uhist, iters)
+    neq, nnz, nedge, bw = (int(v) for v in info)
+    out = dict(neq=neq, nnzero=nnz, nedge=nedge, bandwidth=bw, npicard_run=nit,
+               node_id=node_id, etype=etype, beta=beta.reshape(ne, 2),
+               fsrc=fsrc.reshape(ne, 3), upresc=upresc,
+               Ffirst=Ffirst, Fprec=Fprec, Pin=Pin, Qmv=Qmv, Zpc=Zpc,
+               uhist=uhist[: nit * (neq + 1)].reshape(nit, neq + 1), iters=iters[:nit])
+    if scheme == "CSR":
+        out.update(IA=IA[: neq + 1], JA=JA[:nnz], sbe=sbe.reshape(ne, 9), Afirst=Afirst[: nnz + 1])
+    elif scheme == "EDE":
+        out.update(lm2=JA[: 2 * nedge].reshape(nedge, 2), sbe=sbe[: 3 * ne].reshape(ne, 3),
+                   order=order.reshape(ne, 3), Afirst=Afirst[: 4 * (nedge + 1)].reshape(nedge + 1, 4))
+    else:
+        out.update(Afirst=Afirst[: 9 * ne].reshape(ne, 9))
+    return out
+
+
+# name -> (nx, ny, perturb, node rule, run kwargs)
+CASES = {
+    "skew16_csr_ilu0_not": (16, 16, 0.0, "inflow", dict(scheme="CSR", reord="NOT", precond="ILU0")),
+    "skew16_csr_ilu0_rcm": (16, 16, 0.2, "inflow", dict(scheme="CSR", reord="SYMRCM", precond="ILU0")),
+    "skew16_ebe_none": (16, 16, 0.2, "inflow", dict(scheme="EBE", precond="NOT", npicard=2)),
+    "skew16_ede_none": (16, 16, 0.2, "inflow", dict(scheme="EDE", precond="NOT", npicard=2)),
+    "skew16_ebe_diag": (16, 16, 0.0, "inflow", dict(scheme="EBE", precond="Diag", npicard=2)),
+    "skew24x12_csr_diag_yz": (24, 12, 0.2, "inflow", dict(scheme="CSR", precond="Diag", shock="YZBeta",
+                                                          hshock="Option1", npicard=2)),
+    "skew64_csr_ilu0_rcm": (64, 64, 0.0, "inflow", dict(scheme="CSR", reord="SYMRCM", precond="ILU0",
+                                                       npicard=4)),
+    "skew64_csr_ilu0_not": (64, 64, 0.0, "inflow", dict(scheme="CSR", reord="NOT", precond="ILU0",
+                                                       npicard=2)),
+    "reaction16_csr_ilu0": (16, 16, 0.1, "all", dict(problem="REACTION", scheme="CSR", precond="ILU0",
+                                                     hshock="Option2", npicard=2)),
+    "convection20_csr_rcm": (20, 20, 0.0, "inflow", dict(problem="CONVECTION", scheme="CSR", reord="SYMRCM",
+                                                         precond="ILU0", hshock="sqrtArea",
+                                                         outflow="YES", npicard=2)),
+    "validacao16_ebe_diag": (16, 16, 0.15, "all", dict(problem="VALIDACAO", scheme="EBE", precond="Diag",
+                                                       npicard=1)),
+    "hemker12_ede_diag": (12, 12, 0.0, "inflow", dict(problem="HEMKER", scheme="EDE", precond="Diag",
+                                                      npicard=1)),
+}
+
+
+def main():
+    lib = load_ref()
+    for name, (nx, ny, pert, rule, kw) in CASES.items():
+        mesh = structured_mesh(nx, ny, perturb=pert, seed=1234)
+        ntype = node_types(mesh, rule)
+        out = run_ref(lib, mesh, ntype, **kw)
+        meta = dict(kw)
+        meta.setdefault("problem", "SKEW")
+        np.savez_compressed(
+            os.path.join(HERE, f"{name}.npz"),
+            nx=nx, ny=ny, x=mesh.x, y=mesh.y, vert=mesh.vert, node_type=ntype,
+            meta=np.array(repr(meta)), **out)
+        print(f"{name}: neq={out['neq']} nnz={out['nnzero']} nedge={out['nedge']} "
+              f"picard={out['npicard_run']} iters={list(out['iters'])}")
+
+
+if __name__ == "__main__":
+    main()
