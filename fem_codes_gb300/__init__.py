@@ -1,0 +1,312 @@
+"""fem_codes_gb300 -- GB300-native steady 2D stabilised-FEM solve loop.
+
+Python access to libfemgpu.so (C ABI, include/femgpu.h).  The class
+:class:`SSTransport` mirrors the reference's steady-transport driver
+(01_SS_Transport_Equation/2D/01_CommonFiles): ``Preprocess`` is the
+constructor, and ``Build``, ``precond_setup``, ``precond``,
+``ProductMatrixVector``, ``solver`` and ``Process`` carry the names of the
+function pointers they replace (SSTranspEquation.h:97-121), with the same
+argument meaning: vectors of length neq+1, slot neq the dump of prescribed
+dofs.  There is no CPU fallback: every call runs the CUDA kernels, and a
+missing library or GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .build import LIB, build as _build
+
+__all__ = ["SSTransport", "FemGpuError", "load", "OPTS"]
+
+_lib = None
+
+ERRORS = {
+    -1: "bad argument", -2: "CUDA error", -3: "device allocation failed",
+    -4: "zero pivot", -5: "not converged", -6: "GMRES breakdown", -7: "device wait timeout",
+    -8: "mesh/structure unsupported", -9: "call order",
+}
+
+# Parameter-deck strings (Preprocess.c:44-62) -> ABI enums.
+OPTS = {
+    "scheme": {"EBE": 0, "EDE": 1, "CSR": 2},
+    "reorder": {"NOT": 0, "SYMRCM": 1},
+    "precond": {"NOT": 0, "ILU0": 1, "DIAG": 2},
+    "shock": {"CAU": 0, "YZBETA": 1},
+    "hshock": {"2SQRTAREA": 0, "SQRTAREA": 1, "OPTION1": 2, "OPTION2": 3},
+    "precision": {"FP64": 0, "MIXED": 1},
+}
+
+
+class FemGpuError(RuntimeError):
+    def __init__(self, code, where=""):
+        msg = ERRORS.get(code, f"error {code}")
+        detail = _lib.femgpu_last_error().decode() if _lib is not None else ""
+        super().__init__(f"{where}: {msg} ({code}) {detail}".strip())
+        self.code = code
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("scheme", ctypes.c_int), ("reorder", ctypes.c_int), ("precond", ctypes.c_int),
+                ("shock", ctypes.c_int), ("hshock", ctypes.c_int), ("outflow", ctypes.c_int),
+                ("kmax", ctypes.c_int), ("lmax", ctypes.c_int), ("tol", ctypes.c_double),
+                ("nonlin_tol", ctypes.c_double), ("precision", ctypes.c_int), ("ir_max", ctypes.c_int)]
+
+
+_vp = ctypes.c_void_p
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def load(build_if_needed: bool = True) -> ctypes.CDLL:
+    """Load libfemgpu.so (building it first if sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_needed:
+        _build()
+    if not os.path.exists(LIB):
+        raise FemGpuError(-2, f"libfemgpu.so missing at {LIB}")
+    L = ctypes.CDLL(LIB)
+    L.femgpu_last_error.restype = ctypes.c_char_p
+    L.femgpu_transport_default_opts.argtypes = [ctypes.POINTER(Opts)]
+    L.femgpu_transport_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(Opts), ctypes.c_int,
+                                          _vp, _vp, _vp, ctypes.c_int, _vp, ctypes.c_double,
+                                          ctypes.c_double, _vp, _vp, _vp, _vp]
+    L.femgpu_transport_destroy.argtypes = [_vp]
+    L.femgpu_transport_destroy.restype = None
+    for name, args in {
+        "femgpu_transport_set_stream": [_vp, _vp],
+        "femgpu_transport_info": [_vp, _vp],
+        "femgpu_transport_get_pattern": [_vp, _vp, _vp, _vp, _vp, _vp],
+        "femgpu_transport_build": [_vp, _vp, _vp, _vp],
+        "femgpu_transport_precond_setup": [_vp, ctypes.c_int, _vp],
+        "femgpu_transport_precond": [_vp, _vp, _vp],
+        "femgpu_transport_matvec": [_vp, _vp, _vp],
+        "femgpu_transport_solve": [_vp, _vp, _ip],
+        "femgpu_transport_solve_bx": [_vp, _vp, _vp, _ip],
+        "femgpu_transport_process": [_vp, ctypes.c_int, _vp, _vp],
+        "femgpu_transport_build_dev": [_vp],
+        "femgpu_transport_precond_setup_dev": [_vp, ctypes.c_int],
+        "femgpu_transport_matvec_dev": [_vp, _vp, _vp],
+        "femgpu_transport_precond_dev": [_vp, _vp, _vp],
+        "femgpu_transport_solve_dev": [_vp, _ip],
+        "femgpu_transport_true_residual": [_vp, ctypes.POINTER(ctypes.c_double)],
+        "femgpu_transport_last_times": [_vp, _vp],
+        "femgpu_csrmv_f64": [ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp],
+        "femgpu_csrmv_f32": [ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp],
+    }.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    for name in ("femgpu_transport_u_dev", "femgpu_transport_F_dev"):
+        getattr(L, name).argtypes = [_vp]
+        getattr(L, name).restype = _vp
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_vp)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class SSTransport:
+    """Steady scalar transport on one GPU (the reference's Preprocess ->
+    Process -> pgmres path), built from arrays instead of a mesh file."""
+
+    def __init__(self, x, y, node_type, vert, k, gamma, upresc, beta=None, const_beta=None,
+                 fsrc=None, scheme="CSR", reorder="NOT", precond="ILU0", shock="CAU",
+                 hshock="2sqrtArea", outflow=False, kmax=30, lmax=1000, tol=1e-8,
+                 nonlin_tol=0.0, precision="FP64", ir_max=30):
+        L = load()
+        o = Opts()
+        L.femgpu_transport_default_opts(ctypes.byref(o))
+        o.scheme = OPTS["scheme"][scheme.upper()]
+        o.reorder = OPTS["reorder"][reorder.upper()]
+        o.precond = OPTS["precond"][precond.upper()]
+        o.shock = OPTS["shock"][shock.upper()]
+        o.hshock = OPTS["hshock"][hshock.upper()]
+        o.outflow = 1 if outflow else 0
+        o.kmax, o.lmax, o.tol, o.nonlin_tol = kmax, lmax, tol, nonlin_tol
+        o.precision = OPTS["precision"][precision.upper()]
+        o.ir_max = ir_max
+        self.opts = o
+        self._keep = [_f64(x), _f64(y), _i32(node_type), _i32(np.asarray(vert).reshape(-1)),
+                      _f64(upresc)]
+        self.nnodes = len(x)
+        self.nel = self._keep[3].size // 3
+        b = None if beta is None else _f64(np.asarray(beta).reshape(-1))
+        cb = None if const_beta is None else _f64(const_beta)
+        f = None if fsrc is None else _f64(np.asarray(fsrc).reshape(-1))
+        self._keep += [b, cb, f]
+        h = _vp()
+        rc = L.femgpu_transport_create(ctypes.byref(h), ctypes.byref(o), self.nnodes,
+                                       _ptr(self._keep[0]), _ptr(self._keep[1]), _ptr(self._keep[2]),
+                                       self.nel, _ptr(self._keep[3]), float(k), float(gamma),
+                                       _ptr(b), _ptr(cb), _ptr(f), _ptr(self._keep[4]))
+        if rc:
+            raise FemGpuError(rc, "Preprocess")
+        self._h = h
+        self._L = L
+        info = np.zeros(6, np.int32)
+        self._check(L.femgpu_transport_info(h, _ptr(info)), "info")
+        self.neq, self.nnzero, self.nedge, self.bandwidth, self.ilu_levels_L, self.ilu_levels_U = \
+            (int(v) for v in info)
+        self.scheme = scheme.upper()
+
+    @classmethod
+    def from_problem(cls, mesh, prob, **kw):
+        return cls(mesh.x, mesh.y, prob.node_type, mesh.vert, prob.k, prob.gamma, prob.upresc,
+                   beta=prob.beta, fsrc=prob.fsrc, **kw)
+
+    # -- helpers -----------------------------------------------------------
+    def _check(self, rc, where):
+        if rc:
+            raise FemGpuError(rc, where)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.femgpu_transport_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr):
+        self._check(self._L.femgpu_transport_set_stream(self._h, _vp(stream_ptr)), "set_stream")
+
+    # -- structure ---------------------------------------------------------
+    def pattern(self):
+        """Device-built storage structure, as the reference holds it."""
+        node_id = np.zeros(self.nnodes, np.int32)
+        if self.scheme == "CSR":
+            IA = np.zeros(self.neq + 1, np.int32)
+            JA = np.zeros(max(self.nnzero, 1), np.int32)
+            sbe = np.zeros(9 * self.nel, np.int32)
+            self._check(self._L.femgpu_transport_get_pattern(self._h, _ptr(IA), _ptr(JA), _ptr(sbe),
+                                                             None, _ptr(node_id)), "pattern")
+            return dict(IA=IA, JA=JA[: self.nnzero], sbe=sbe.reshape(-1, 9), node_id=node_id)
+        if self.scheme == "EDE":
+            lm2 = np.zeros(2 * max(self.nedge, 1), np.int32)
+            sbe = np.zeros(3 * self.nel, np.int32)
+            order = np.zeros(3 * self.nel, np.int32)
+            self._check(self._L.femgpu_transport_get_pattern(self._h, None, _ptr(lm2), _ptr(sbe),
+                                                             _ptr(order), _ptr(node_id)), "pattern")
+            return dict(lm2=lm2[: 2 * self.nedge].reshape(-1, 2), sbe=sbe.reshape(-1, 3),
+                        order=order.reshape(-1, 3), node_id=node_id)
+        self._check(self._L.femgpu_transport_get_pattern(self._h, None, None, None, None,
+                                                         _ptr(node_id)), "pattern")
+        return dict(node_id=node_id)
+
+    def storage_len(self):
+        if self.scheme == "CSR":
+            return self.nnzero + 1
+        if self.scheme == "EDE":
+            return 4 * (self.nedge + 1)
+        return 9 * self.nel
+
+    # -- the reference's function pointers --------------------------------
+    def Build(self, u=None, want_matrix=False):
+        """FemOtherFunctions->Build: element loop + assembly. Returns (F, A)."""
+        F = np.zeros(self.neq + 1)
+        A = np.zeros(self.storage_len()) if want_matrix else None
+        uu = None if u is None else _f64(u)
+        self._check(self._L.femgpu_transport_build(self._h, _ptr(uu), _ptr(F), _ptr(A)), "Build")
+        return F, A
+
+    def precond_setup(self, tag=1):
+        """FemFunctions->precond_setup: factor, then F := M^-1 F. Returns F."""
+        F = np.zeros(self.neq + 1)
+        self._check(self._L.femgpu_transport_precond_setup(self._h, int(tag), _ptr(F)), "precond_setup")
+        return F
+
+    def precond(self, p):
+        """FemFunctions->precond: z = M^-1 p (entries 0..neq-1)."""
+        p = _f64(p)
+        z = p.copy()
+        self._check(self._L.femgpu_transport_precond(self._h, _ptr(p), _ptr(z)), "precond")
+        return z
+
+    def ProductMatrixVector(self, P, Q=None):
+        """FemFunctions->ProductMatrixVector: Q = A P."""
+        P = np.array(P, dtype=np.float64, copy=True)
+        Q = np.zeros(self.neq + 1) if Q is None else Q
+        self._check(self._L.femgpu_transport_matvec(self._h, _ptr(P), _ptr(Q)), "ProductMatrixVector")
+        return Q
+
+    def solver(self, raise_on_nonconvergence=True):
+        """FemOtherFunctions->solver (pgmres, 4-argument form): B = F, X = u.
+        Returns (u, iterations)."""
+        X = np.zeros(self.neq + 1)
+        it = ctypes.c_int(0)
+        rc = self._L.femgpu_transport_solve(self._h, _ptr(X), ctypes.byref(it))
+        if rc and (rc != -5 or raise_on_nonconvergence):
+            raise FemGpuError(rc, "solver")
+        return X, it.value
+
+    def solver_bx(self, B):
+        """6-argument pgmres form: X = solve(B). Returns (X, iterations)."""
+        B = _f64(B)
+        X = np.zeros(self.neq + 1)
+        it = ctypes.c_int(0)
+        self._check(self._L.femgpu_transport_solve_bx(self._h, _ptr(B), _ptr(X), ctypes.byref(it)),
+                    "solver")
+        return X, it.value
+
+    def Process(self, npicard):
+        """Picard loop of Process.c. Returns (u history [n, neq+1], iterations)."""
+        uh = np.zeros((npicard, self.neq + 1))
+        its = np.zeros(npicard, np.int32)
+        n = self._L.femgpu_transport_process(self._h, int(npicard), _ptr(uh), _ptr(its))
+        if n < 0:
+            raise FemGpuError(n, "Process")
+        return uh[:n], its[:n]
+
+    def true_residual(self):
+        r = ctypes.c_double(0.0)
+        self._check(self._L.femgpu_transport_true_residual(self._h, ctypes.byref(r)), "true_residual")
+        return r.value
+
+    def last_times(self):
+        t = np.zeros(3, np.float32)
+        self._check(self._L.femgpu_transport_last_times(self._h, _ptr(t)), "last_times")
+        return t
+
+    # device-resident path (no host copies)
+    def build_dev(self):
+        self._check(self._L.femgpu_transport_build_dev(self._h), "build_dev")
+
+    def precond_setup_dev(self, tag=1):
+        self._check(self._L.femgpu_transport_precond_setup_dev(self._h, int(tag)), "precond_setup_dev")
+
+    def solve_dev(self):
+        it = ctypes.c_int(0)
+        rc = self._L.femgpu_transport_solve_dev(self._h, ctypes.byref(it))
+        if rc:
+            raise FemGpuError(rc, "solve_dev")
+        return it.value
+
+    def u_dev(self):
+        return self._L.femgpu_transport_u_dev(self._h)

@@ -1,0 +1,249 @@
+// Element build of the steady scalar transport equation -- SUPG with
+// CAU/YZBeta shock capturing on linear triangles (Build_K_F_SUPG.c:35-157,
+// CAU_ShockCapture.c, YZBeta_ShockCapture.c, h_shock_*.c) -- and the
+// deterministic assembly of its element matrices into EDE/CSR storage and of
+// the load vector (F_assembly.c, ede_assembly.c, csr_assembly.c).
+//
+// One thread per element computes ke (3x3) and Fe (3) in FP64 and stores them
+// element-major.  Assembly then gathers, for every CSR row / edge, the
+// contributions of its incident elements in ascending element order: the same
+// sequence of additions the reference's serial element loop performs, so the
+// assembled values and F are reproducible run to run (no atomics).
+//
+// This translation unit is compiled with --fmad=false: every product and sum
+// is rounded separately, as in the reference compiled without contraction.
+#include "fg_common.cuh"
+
+struct BuildArgs {
+	const double *x, *y, *u, *upresc, *beta, *fsrc;
+	const int *vert, *node_id;
+	double k, gamma, cbx, cby;
+	int nel, shock, hshock, beta_const, fsrc_zero;
+	double *ke, *fe;
+};
+
+// Shock length scale: h_shock_2sqrtArea.c:3-8, h_shock_sqrtArea.c:3-61 (every
+// branch yields 2*sqrt|A|), h_shock_Option1.c:3-19, h_shock_Option2.c:3-19.
+__device__ __forceinline__ double h_shock(int opt, double bx, double by, double u1, double u2,
+                                          double u3, double y23, double y31, double y12,
+                                          double x32, double x13, double x21, double Area)
+{
+	if (opt == FEMGPU_H_SQRTAREA) return 2 * sqrt(fabs(Area));
+	if (opt == FEMGPU_H_OPTION1) {
+		double P1 = fabs(u1*y23*y23 + u2*y31*y23 + u3*y12*y23 + u1*x32*x32 + u2*x13*x32 + u3*x21*x32);
+		double P2 = fabs(u1*y23*y31 + u2*y31*y31 + u3*y12*y31 + u1*x32*x13 + u2*x13*x13 + u3*x21*x13);
+		double P3 = fabs(u1*y23*y12 + u2*y31*y12 + u3*y12*y12 + u1*x32*x21 + u2*x13*x21 + u3*x21*x21);
+		double a1 = y23*u1 + y31*u2 + y12*u3, a2 = x32*u1 + x13*u2 + x21*u3;
+		double ng = sqrt(a1*a1 + a2*a2);
+		return (P1 + P2 + P3 >= 1e-12) ? 4*Area*ng/(P1 + P2 + P3) : 0.0;
+	}
+	if (opt == FEMGPU_H_OPTION2) {
+		double P1 = fabs(bx*y23 + by*x32), P2 = fabs(bx*y31 + by*x13), P3 = fabs(bx*y12 + by*x21);
+		double nb = sqrt(bx*bx + by*by);
+		return (P1 + P2 + P3 >= 1e-12) ? 4*Area*nb/(P1 + P2 + P3) : 0.0;
+	}
+	return sqrt(fabs(2*Area));
+}
+
+// CAU_ShockCapture.c:3-30 (the division by |grad u|^2 is only evaluated when
+// |grad u| > 0; the reference computes it first and discards a NaN) and
+// YZBeta_ShockCapture.c:3-27.
+__device__ __forceinline__ double shock_capture(int kind, double kx, double ky, double bx, double by,
+                                                double g, double ue1, double ue2, double ue3,
+                                                double ueb, double feb, double y23, double y31,
+                                                double y12, double x32, double x13, double x21,
+                                                double invArea, double h)
+{
+	double BetaGradu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+	double Ru = BetaGradu + g*ueb - feb;
+	double G0 = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+	double G1 = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+	double nG = sqrt(G0*G0 + G1*G1);
+	if (kind == FEMGPU_SHOCK_YZBETA) {
+		double nRu = fabs(Ru), nu = fabs(ueb);
+		return (nu >= 1e-12 && nG >= 1e-12) ? 0.25*h*nRu/nG + 0.125*h*h*nRu/nu : 0.0;
+	}
+	if (!(nG > 0)) return 0.0;
+	const double third = 1./3.;
+	double bxp = BetaGradu*G0/(nG*nG), byp = BetaGradu*G1/(nG*nG);
+	double kp = bxp*bxp*kx + byp*byp*ky;
+	double nbp = sqrt(bxp*bxp + byp*byp);
+	double Pee = 0.5*h*nbp*nbp*nbp/kp;
+	if (third*Pee < 0.7) return 0.5*h*third*Pee*fabs(Ru)/nG;
+	return 0.5*h*0.7*fabs(Ru)/nG;
+}
+
+__global__ void __launch_bounds__(128) k_build_supg(BuildArgs a)
+{
+	const double third = 1.0/3.0, sixth = 1.0/6.0, twelfth = 1.0/12.0;
+	const double kx = a.k, ky = a.k, gamma = a.gamma;
+	for (int E = blockIdx.x * blockDim.x + threadIdx.x; E < a.nel; E += gridDim.x * blockDim.x) {
+		int J1 = __ldg(&a.vert[3*E]), J2 = __ldg(&a.vert[3*E+1]), J3 = __ldg(&a.vert[3*E+2]);
+		double X0 = __ldg(&a.x[J1]), X1 = __ldg(&a.x[J2]), X2 = __ldg(&a.x[J3]);
+		double Y0 = __ldg(&a.y[J1]), Y1 = __ldg(&a.y[J2]), Y2 = __ldg(&a.y[J3]);
+		double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
+		double x32 = X2 - X1, x13 = X0 - X2, x21 = X1 - X0;
+		double TwoA = x21*y31 - x13*y12, Area = 0.5*TwoA, invArea = 1.0/Area;
+		double h = sqrt(fabs(TwoA));
+		double bx, by;
+		if (a.beta_const) { bx = a.cbx; by = a.cby; }
+		else { bx = __ldg(&a.beta[2*E]); by = __ldg(&a.beta[2*E+1]); }
+		double norm = sqrt(bx*bx + by*by), tau = (norm > 0) ? 0.5*h/norm : 0.0;
+		double fe1 = 0.0, fe2 = 0.0, fe3 = 0.0;
+		if (!a.fsrc_zero) { fe1 = __ldg(&a.fsrc[3*E]); fe2 = __ldg(&a.fsrc[3*E+1]); fe3 = __ldg(&a.fsrc[3*E+2]); }
+		double feb = third*(fe1+fe2+fe3);
+		// eval_U.c:12-22
+		int i1 = __ldg(&a.node_id[J1]), i2 = __ldg(&a.node_id[J2]), i3 = __ldg(&a.node_id[J3]);
+		double ue1 = (i1 >= 0) ? a.u[i1] : __ldg(&a.upresc[J1]);
+		double ue2 = (i2 >= 0) ? a.u[i2] : __ldg(&a.upresc[J2]);
+		double ue3 = (i3 >= 0) ? a.u[i3] : __ldg(&a.upresc[J3]);
+		double ueb = third * (ue1 + ue2 + ue3);
+
+		double D12 = 0.25*invArea*((kx * y23 * y31) + (ky * x32 * x13));
+		double D13 = 0.25*invArea*((kx * y23 * y12) + (ky * x32 * x21));
+		double D23 = 0.25*invArea*((kx * y31 * y12) + (ky * x13 * x21));
+		double C11 = sixth*(bx*y23 + by*x32);
+		double C12 = sixth*(bx*y31 + by*x13);
+		double C13 = sixth*(bx*y12 + by*x21);
+		double R11 = sixth*(gamma*Area);
+		double R12 = twelfth*(gamma * Area);
+		double Cpg12 = 0.25*invArea*tau * (y23*(bx*bx*y31 + bx*by*x13) + x32*(bx*by*y31 + by*by*x13));
+		double Cpg13 = 0.25*invArea*tau * (y23*(bx*bx*y12 + bx*by*x21) + x32*(bx*by*y12 + by*by*x21));
+		double Cpg23 = 0.25*invArea*tau * (y31*(bx*bx*y12 + bx*by*x21) + x13*(bx*by*y12 + by*by*x21));
+		double Rpg11 = sixth*tau*gamma * (bx*y23 + by*x32);
+		double Rpg21 = sixth*tau*gamma * (bx*y31 + by*x13);
+		double Rpg31 = sixth*tau*gamma * (bx*y12 + by*x21);
+
+		double hs = h_shock(a.hshock, bx, by, ue1, ue2, ue3, y23, y31, y12, x32, x13, x21, Area);
+		double Eu = shock_capture(a.shock, kx, ky, bx, by, gamma, ue1, ue2, ue3, ueb, feb,
+		                          y23, y31, y12, x32, x13, x21, invArea, hs);
+		double Csc12 = Eu*0.25*invArea*(y23*y31 + x32*x13);
+		double Csc13 = Eu*0.25*invArea*(y23*y12 + x32*x21);
+		double Csc23 = Eu*0.25*invArea*(y31*y12 + x13*x21);
+
+		double *ke = a.ke + 9LL*E;
+		ke[0] = -(D12 + D13) + C11 - (Cpg12 + Cpg13) + R11 + Rpg11 - (Csc12 + Csc13);
+		ke[1] = D12 + C12 + Cpg12 + R12 + Rpg11 + Csc12;
+		ke[2] = D13 + C13 + Cpg13 + R12 + Rpg11 + Csc13;
+		ke[3] = D12 + C11 + Cpg12 + R12 + Rpg21 + Csc12;
+		ke[4] = -(D12 + D23) + C12 - (Cpg12 + Cpg23) + R11 + Rpg21 - (Csc12 + Csc23);
+		ke[5] = D23 + C13 + Cpg23 + R12 + Rpg21 + Csc23;
+		ke[6] = D13 + C11 + Cpg13 + R12 + Rpg31 + Csc13;
+		ke[7] = D23 + C12 + Cpg23 + R12 + Rpg31 + Csc23;
+		ke[8] = -(D13 + D23) + C13 - (Cpg13 + Cpg23) + R11 + Rpg31 - (Csc13 + Csc23);
+
+		double *fe = a.fe + 3LL*E;
+		fe[0] = Area*twelfth*(2*fe1 +  fe2  +  fe3 ) + sixth*tau*(fe1+fe2+fe3)*(bx*y23 + by*x32);
+		fe[1] = Area*twelfth*(  fe1 + 2*fe2 +  fe3 ) + sixth*tau*(fe1+fe2+fe3)*(bx*y31 + by*x13);
+		fe[2] = Area*twelfth*(  fe1 +  fe2  + 2*fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y12 + by*x21);
+	}
+}
+
+extern "C" int fg_build_elements(femgpu_transport *t)
+{
+	BuildArgs a;
+	a.x = t->x; a.y = t->y; a.u = t->u; a.upresc = t->upresc; a.beta = t->beta; a.fsrc = t->fsrc;
+	a.vert = t->vert; a.node_id = t->node_id;
+	a.k = t->k; a.gamma = t->gamma; a.cbx = t->cbx; a.cby = t->cby;
+	a.nel = t->nel; a.shock = t->o.shock; a.hshock = t->o.hshock;
+	a.beta_const = t->beta_const; a.fsrc_zero = t->fsrc_zero;
+	a.ke = (t->o.scheme == FEMGPU_EBE) ? t->A : t->ke;
+	a.fe = t->fe;
+	k_build_supg<<<fg_grid(t->nel, 128, 32), 128, 0, t->stream>>>(a);
+	return (int)cudaGetLastError();
+}
+
+// ------------------------------------------------------------ assembly ---
+#define FG_ROWCAP 32
+
+// F_assembly.c:5-27 for row I: for each incident element (ascending), add Fe
+// then subtract the Dirichlet lift of every other vertex with Type == 0.
+__device__ __forceinline__ double gather_F(int I, const int *ri_ptr, const int *ri, const double *ke,
+                                           const double *fe, const int *vert, const int *node_type,
+                                           const double *upresc)
+{
+	double F = 0.0;
+	for (int q = ri_ptr[I]; q < ri_ptr[I + 1]; q++) {
+		int code = __ldg(&ri[q]), e = code / 3, aa = code - 3 * e;
+		F += __ldg(&fe[3LL * e + aa]);
+		for (int b = 0; b < 3; b++) {
+			if (b == aa) continue;
+			int v = __ldg(&vert[3 * e + b]);
+			if (__ldg(&node_type[v]) == 0) F -= __ldg(&ke[9LL * e + 3 * aa + b]) * __ldg(&upresc[v]);
+		}
+	}
+	return F;
+}
+
+// CSR rows: csr_assembly.c:9-22 gathered per row, plus F.
+__global__ void k_assemble_csr(int neq, int nnz, const int *IA, const int *sbe, const int *ri_ptr,
+                               const int *ri, const double *ke, const double *fe, const int *vert,
+                               const int *node_type, const double *upresc, double *AA, double *F,
+                               int *err)
+{
+	double acc[FG_ROWCAP];
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < neq; I += gridDim.x * blockDim.x) {
+		int base = IA[I], len = IA[I + 1] - base;
+		if (len > FG_ROWCAP) { fg_set_err(err, FEMGPU_E_MESH); continue; }
+		for (int q = 0; q < len; q++) acc[q] = 0.0;
+		for (int q = ri_ptr[I]; q < ri_ptr[I + 1]; q++) {
+			int code = __ldg(&ri[q]), e = code / 3, aa = code - 3 * e;
+			for (int b = 0; b < 3; b++) {
+				int pos = __ldg(&sbe[9 * e + 3 * aa + b]);
+				if (pos < nnz) acc[pos - base] += __ldg(&ke[9LL * e + 3 * aa + b]);
+			}
+		}
+		for (int q = 0; q < len; q++) AA[base + q] = acc[q];
+		F[I] = gather_F(I, ri_ptr, ri, ke, fe, vert, node_type, upresc);
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) AA[nnz] = 0.0;
+}
+
+// EDE edges: ede_assembly.c:21-36 gathered per edge.
+__global__ void k_assemble_ede(int nedge, const int *ec_ptr, const int *ec, const int *order,
+                               const double *ke, double *A)
+{
+	for (int E = blockIdx.x * blockDim.x + threadIdx.x; E <= nedge; E += gridDim.x * blockDim.x) {
+		double K0 = 0.0, K1 = 0.0, K2 = 0.0, K3 = 0.0;
+		if (E < nedge) {
+			for (int q = ec_ptr[E]; q < ec_ptr[E + 1]; q++) {
+				int code = __ldg(&ec[q]), e = code / 3, s = code - 3 * e;
+				int o0 = __ldg(&order[3 * e]), o1 = __ldg(&order[3 * e + 1]), o2 = __ldg(&order[3 * e + 2]);
+				int Ia = (s == 2) ? o1 : o0, Ib = (s == 0) ? o1 : o2;
+				const double *k = ke + 9LL * e;
+				K0 += 0.5*__ldg(&k[3 * Ia + Ia]);
+				K1 += __ldg(&k[3 * Ia + Ib]);
+				K2 += __ldg(&k[3 * Ib + Ia]);
+				K3 += 0.5*__ldg(&k[3 * Ib + Ib]);
+			}
+		}
+		A[4LL * E] = K0; A[4LL * E + 1] = K1; A[4LL * E + 2] = K2; A[4LL * E + 3] = K3;
+	}
+}
+
+__global__ void k_assemble_F(int neq, const int *ri_ptr, const int *ri, const double *ke,
+                             const double *fe, const int *vert, const int *node_type,
+                             const double *upresc, double *F)
+{
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < neq; I += gridDim.x * blockDim.x)
+		F[I] = gather_F(I, ri_ptr, ri, ke, fe, vert, node_type, upresc);
+}
+
+extern "C" int fg_assemble(femgpu_transport *t)
+{
+	cudaStream_t s = t->stream;
+	int neq = t->neq;
+	if (t->o.scheme == FEMGPU_CSR) {
+		k_assemble_csr<<<fg_grid(neq, 128, 32), 128, 0, s>>>(neq, t->nnz, t->IA, t->sbe, t->ri_ptr,
+			t->ri, t->ke, t->fe, t->vert, t->node_type, t->upresc, t->A, t->F, &t->st->err);
+	} else if (t->o.scheme == FEMGPU_EDE) {
+		k_assemble_ede<<<fg_grid(t->nedge + 1LL), FG_TPB, 0, s>>>(t->nedge, t->ec_ptr, t->ec, t->order,
+			t->ke, t->A);
+		k_assemble_F<<<fg_grid(neq), FG_TPB, 0, s>>>(neq, t->ri_ptr, t->ri, t->ke, t->fe, t->vert,
+			t->node_type, t->upresc, t->F);
+	} else {
+		k_assemble_F<<<fg_grid(neq), FG_TPB, 0, s>>>(neq, t->ri_ptr, t->ri, t->A, t->fe, t->vert,
+			t->node_type, t->upresc, t->F);
+	}
+	return (int)cudaGetLastError();
+}

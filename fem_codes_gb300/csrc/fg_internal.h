@@ -1,0 +1,127 @@
+/*
+ * Internal state and kernel-launch entry points of libfemgpu.
+ * Shared by the CUDA translation units (*.cu) and the host C driver
+ * (host/*.c); plain C, no CUDA-only types beyond cuda_runtime_api.h.
+ *
+ * Device layout (all device memory, allocated once per context):
+ *   mesh      x, y [nnodes] f64; node_type, node_id [nnodes] i32;
+ *             vert, lm [3*nel] i32 (lm = equation of each vertex, neq = dump)
+ *   incidence ri_ptr [neq+1], ri [..] = 3*e + a for every unknown vertex a of
+ *             element e, rows sorted by e (drives the deterministic gathers)
+ *   CSR       IA [neq+1], JA [nnz], sbe [9*nel] (CSR_by_Element), diag [neq]
+ *   EDE       lm2 [2*nedge], sbe [3*nel] (EDGE_by_Element), order [3*nel],
+ *             edge contributor lists ec_ptr/ec, row "second endpoint" lists
+ *   values    A: EBE 9*nel | EDE 4*(nedge+1) | CSR nnz+1 (f64, plus an f32
+ *             copy in mixed precision); ke [9*nel], fe [3*nel] element temps
+ *   vectors   u, F, F0 [neq+1]; Krylov basis V [(kmax+1) x ldv]
+ */
+#ifndef FG_INTERNAL_H
+#define FG_INTERNAL_H
+
+#include <cuda_runtime_api.h>
+#include "femgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Level-scheduled sparse triangular structure (ILU(0) factor and sweeps). */
+typedef struct fg_levels {
+	int nlev;          /* number of dependency levels                        */
+	int ntask;         /* level-aligned tasks of <= 32 rows                  */
+	int *rows;         /* [n] rows in (level, row) order                     */
+	int *task;         /* [ntask+1] start offsets into rows                  */
+} fg_levels;
+
+typedef struct fg_ilu {
+	int n, nnz;
+	double *LU;        /* [nnz] L (col<row) and U (col>row) in A's positions */
+	double *Dinv;      /* [n] inverted pivots                                */
+	float *LU32, *Dinv32;
+	fg_levels lo, up;  /* forward (also the factor) and backward schedules   */
+	unsigned *flags;   /* [n] completion epochs                              */
+	unsigned epoch;
+	int *counter;      /* task claim counter                                 */
+} fg_ilu;
+
+/* Device status block (one per context, device memory). */
+typedef struct fg_status {
+	int err;           /* first device-side error code (FEMGPU_E_*)          */
+	int active;        /* GMRES inner loop still running                     */
+	int inner;         /* inner iterations done in the current cycle         */
+	int total;         /* total inner iterations of the solve                */
+	double rho, eps;
+	double hdiag;      /* scratch                                            */
+	unsigned ticket;   /* last-block reduction ticket                        */
+	int pad;
+} fg_status;
+
+struct femgpu_transport {
+	femgpu_transport_opts o;
+	int nnodes, nel, neq, nnz, nedge, bandwidth;
+	cudaStream_t stream, own_stream;
+	int built, factored;
+
+	/* mesh / problem */
+	double *x, *y, *upresc, *beta, *fsrc;
+	int *node_type, *node_id, *vert, *lm;
+	double k, gamma, cbx, cby;
+	int beta_const, fsrc_zero;
+	int *h_node_id;                 /* host copy of the numbering            */
+
+	/* incidence */
+	int *ri_ptr, *ri;
+
+	/* storage patterns */
+	int *IA, *JA, *sbe, *diag;
+	int *lm2, *order, *ec_ptr, *ec, *e2_ptr, *e2;
+
+	/* values */
+	double *A, *ke, *fe;
+	float *A32;
+	double *u, *F, *F0, *invDiag;
+	fg_ilu ilu;
+
+	/* Krylov workspace */
+	int kmax;
+	size_t ldv;
+	double *V, *H, *cs, *sn, *ge, *gy, *w2;
+	double *partials;               /* reduction partials                    */
+	int nblk_red;
+	fg_status *st;                  /* device status                         */
+	fg_status *st_host;             /* pinned mirror                         */
+
+	/* timing */
+	cudaEvent_t ev[4];
+	float times[3];
+};
+
+/* ---- kernels (stream-ordered launchers, return cudaError_t as int) ---- */
+/* pattern.cu */
+int fg_build_incidence(femgpu_transport *t);                 /* ri_ptr / ri   */
+int fg_build_csr(femgpu_transport *t);                       /* IA, JA, sbe   */
+int fg_build_ede(femgpu_transport *t);                       /* lm2, sbe, ... */
+int fg_compute_lm(femgpu_transport *t);                      /* lm from ids   */
+
+/* build.cu */
+int fg_build_elements(femgpu_transport *t);                  /* ke / A, fe    */
+int fg_assemble(femgpu_transport *t);                        /* A (CSR/EDE), F */
+
+/* linalg.cu */
+int fg_matvec(femgpu_transport *t, const double *P, double *Q, const int *active);
+int fg_csrmv64(int n, const int *IA, const int *JA, const double *AA, const double *P,
+               double *Q, const int *active, cudaStream_t s);
+int fg_csrmv32(int n, const int *IA, const int *JA, const float *AA, const float *P,
+               float *Q, const int *active, cudaStream_t s);
+int fg_diag_setup(femgpu_transport *t);
+int fg_levels_build(const int *h_IA, const int *h_JA, int n, int lower, fg_levels *lv);
+int fg_ilu0_factor(femgpu_transport *t);
+int fg_precond(femgpu_transport *t, const double *p, double *z, const int *active);
+int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, int first);
+int fg_dot(femgpu_transport *t, const double *a, const double *b, int n, double *out_dev);
+int fg_residual_norm(femgpu_transport *t, const double *B, const double *X, double *out_dev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

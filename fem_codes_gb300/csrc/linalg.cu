@@ -1,0 +1,645 @@
+// Linear algebra of the solve loop on the device:
+//   * matvecs csrmv.c / ebemv.c / edemv.c as per-row gathers (no atomics; the
+//     additions of each row happen in the reference's order);
+//   * diagonal preconditioner (Diag_precond*_setup.c, Diag_precond.c);
+//   * ILU(0) (ILUp_precond_setup.c:66-167 at p = 0, ILUp_precond.c:26-46):
+//     factorisation and triangular sweeps in level order by a sync-free
+//     kernel -- one lane per row, warps claim level-aligned tasks of 32 rows
+//     in order, every row waits (bounded) for the completion flags of the rows
+//     it depends on;
+//   * the restarted GMRES of pgmres.c:4-211 with its Arnoldi, Givens and
+//     back-substitution on the device; the inner loop is predicated on a
+//     device flag so a whole restart cycle is enqueued without host syncs.
+// Products and sums in the FP64 parity kernels use __dmul_rn/__dadd_rn so
+// they are rounded exactly like the reference compiled without contraction.
+#include "fg_common.cuh"
+#include <math.h>
+
+#define FG_SPIN_LIMIT (1 << 22)   // bounded waits (~0.4 s with the sleep below)
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
+{
+	unsigned v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v)
+{
+	asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+// Wait until flags[j] == epoch; on timeout record FEMGPU_E_TIMEOUT and give up.
+__device__ __forceinline__ void wait_flag(const unsigned *flags, int j, unsigned epoch, int *err)
+{
+	int spins = 0;
+	while (ld_acquire(flags + j) != epoch) {
+		if (++spins > FG_SPIN_LIMIT) { fg_set_err(err, FEMGPU_E_TIMEOUT); return; }
+		__nanosleep(100);
+	}
+}
+
+// ============================================================= matvecs ====
+// csrmv.c:15-20: Q[i] = sum_j AA[j] P[JA[j]] in column order.
+__global__ void k_csrmv64(int n, const int *__restrict__ IA, const int *__restrict__ JA,
+                          const double *__restrict__ AA, const double *__restrict__ P,
+                          double *__restrict__ Q, const int *active)
+{
+	if (active && !*active) return;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		double q = 0.0;
+		int e = __ldg(&IA[i + 1]);
+		for (int j = __ldg(&IA[i]); j < e; j++)
+			q = __dadd_rn(q, __dmul_rn(__ldg(&AA[j]), __ldg(&P[__ldg(&JA[j])])));
+		Q[i] = q;
+	}
+}
+
+// FP32 values: G lanes per row, coalesced loads, shuffle reduction.
+template <int G>
+__global__ void k_csrmv32(int n, const int *__restrict__ IA, const int *__restrict__ JA,
+                          const float *__restrict__ AA, const float *__restrict__ P,
+                          float *__restrict__ Q, const int *active)
+{
+	if (active && !*active) return;
+	int lane = threadIdx.x % G;
+	long long gstride = (long long)gridDim.x * blockDim.x / G;
+	for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += gstride) {
+		int b = __ldg(&IA[r]), e = __ldg(&IA[r + 1]);
+		float q = 0.f;
+		for (int j = b + lane; j < e; j += G) q += __ldg(&AA[j]) * __ldg(&P[__ldg(&JA[j])]);
+		#pragma unroll
+		for (int o = G / 2; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o, G);
+		if (lane == 0) Q[r] = q;
+	}
+}
+
+extern "C" int fg_csrmv64(int n, const int *IA, const int *JA, const double *AA, const double *P,
+                          double *Q, const int *active, cudaStream_t s)
+{
+	k_csrmv64<<<fg_grid(n, 128, 32), 128, 0, s>>>(n, IA, JA, AA, P, Q, active);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_csrmv32(int n, const int *IA, const int *JA, const float *AA, const float *P,
+                          float *Q, const int *active, cudaStream_t s)
+{
+	k_csrmv32<4><<<fg_grid(4LL * n, 256, 32), 256, 0, s>>>(n, IA, JA, AA, P, Q, active);
+	return (int)cudaGetLastError();
+}
+
+// ebemv.c:42-63 gathered per row: for each incident element (ascending),
+// Q += A[3a]*p1 + A[3a+1]*p2 + A[3a+2]*p3 with P[neq] read as 0.
+__global__ void k_ebemv(int neq, const int *__restrict__ ri_ptr, const int *__restrict__ ri,
+                        const int *__restrict__ lm, const double *__restrict__ A,
+                        const double *__restrict__ P, double *__restrict__ Q, const int *active)
+{
+	if (active && !*active) return;
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I <= neq; I += gridDim.x * blockDim.x) {
+		double q = 0.0;
+		if (I < neq) {
+			for (int k = __ldg(&ri_ptr[I]); k < __ldg(&ri_ptr[I + 1]); k++) {
+				int code = __ldg(&ri[k]), e = code / 3, a = code - 3 * e;
+				int l0 = __ldg(&lm[3 * e]), l1 = __ldg(&lm[3 * e + 1]), l2 = __ldg(&lm[3 * e + 2]);
+				double p0 = (l0 == neq) ? 0.0 : __ldg(&P[l0]);
+				double p1 = (l1 == neq) ? 0.0 : __ldg(&P[l1]);
+				double p2 = (l2 == neq) ? 0.0 : __ldg(&P[l2]);
+				const double *r = A + 9LL * e + 3 * a;
+				double t = __dadd_rn(__dadd_rn(__dmul_rn(__ldg(&r[0]), p0), __dmul_rn(__ldg(&r[1]), p1)),
+				                     __dmul_rn(__ldg(&r[2]), p2));
+				q = __dadd_rn(q, t);
+			}
+		}
+		Q[I] = q;
+	}
+}
+
+// edemv.c:90-103 gathered per row: edges (J, I) with J < I (ascending edge
+// index) contribute A2*pJ + A3*pI, then edges (I, J) contribute A0*pI + A1*pJ.
+__global__ void k_edemv(int neq, const int *__restrict__ first, const int *__restrict__ e2_ptr,
+                        const int *__restrict__ e2, const int *__restrict__ lm2,
+                        const double *__restrict__ A, const double *__restrict__ P,
+                        double *__restrict__ Q, const int *active)
+{
+	if (active && !*active) return;
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I <= neq; I += gridDim.x * blockDim.x) {
+		double q = 0.0;
+		if (I < neq) {
+			double pI = __ldg(&P[I]);
+			for (int k = __ldg(&e2_ptr[I]); k < __ldg(&e2_ptr[I + 1]); k++) {
+				int E = __ldg(&e2[k]), J = __ldg(&lm2[2 * E]);
+				double t = __dadd_rn(__dmul_rn(__ldg(&A[4LL * E + 2]), __ldg(&P[J])),
+				                     __dmul_rn(__ldg(&A[4LL * E + 3]), pI));
+				q = __dadd_rn(q, t);
+			}
+			for (int E = __ldg(&first[I]); E < __ldg(&first[I + 1]); E++) {
+				int J = __ldg(&lm2[2 * E + 1]);
+				double pJ = (J == neq) ? 0.0 : __ldg(&P[J]);
+				double t = __dadd_rn(__dmul_rn(__ldg(&A[4LL * E]), pI), __dmul_rn(__ldg(&A[4LL * E + 1]), pJ));
+				q = __dadd_rn(q, t);
+			}
+		}
+		Q[I] = q;
+	}
+}
+
+extern "C" int fg_matvec(femgpu_transport *t, const double *P, double *Q, const int *active)
+{
+	cudaStream_t s = t->stream;
+	if (t->o.scheme == FEMGPU_CSR) return fg_csrmv64(t->neq, t->IA, t->JA, t->A, P, Q, active, s);
+	if (t->o.scheme == FEMGPU_EBE)
+		k_ebemv<<<fg_grid(t->neq + 1LL, 128, 32), 128, 0, s>>>(t->neq, t->ri_ptr, t->ri, t->lm, t->A, P, Q,
+		                                                      active);
+	else
+		k_edemv<<<fg_grid(t->neq + 1LL, 128, 32), 128, 0, s>>>(t->neq, t->IA, t->e2_ptr, t->e2, t->lm2,
+		                                                      t->A, P, Q, active);
+	return (int)cudaGetLastError();
+}
+
+// ============================================================ diagonal ====
+// Diag_precond_CSR_setup.c:13-26, Diag_precond_EBE_setup.c:15-33,
+// Diag_precond_EDE_setup.c:14-31: diagonal (summed in the reference's
+// order), inverted, then F := F / D.
+__global__ void k_diag_setup(int scheme, int neq, const int *diag, const int *ri_ptr, const int *ri,
+                             const int *first, const int *e2_ptr, const int *e2, const double *A,
+                             double *invDiag, double *F)
+{
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < neq; I += gridDim.x * blockDim.x) {
+		double d = 0.0;
+		if (scheme == FEMGPU_CSR) d = A[diag[I]];
+		else if (scheme == FEMGPU_EBE) {
+			for (int k = ri_ptr[I]; k < ri_ptr[I + 1]; k++) {
+				int code = ri[k], e = code / 3, a = code - 3 * e;
+				d = __dadd_rn(d, A[9LL * e + 4 * a]);
+			}
+		} else {
+			for (int k = e2_ptr[I]; k < e2_ptr[I + 1]; k++) d = __dadd_rn(d, A[4LL * e2[k] + 3]);
+			for (int E = first[I]; E < first[I + 1]; E++) d = __dadd_rn(d, A[4LL * E]);
+		}
+		double inv = 1.0 / d;
+		invDiag[I] = inv;
+		F[I] = __dmul_rn(F[I], inv);
+	}
+}
+
+__global__ void k_diag_apply(int n, const double *invDiag, const double *p, double *z, const int *active)
+{
+	if (active && !*active) return;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		z[i] = __dmul_rn(p[i], invDiag[i]);
+}
+
+extern "C" int fg_diag_setup(femgpu_transport *t)
+{
+	k_diag_setup<<<fg_grid(t->neq), FG_TPB, 0, t->stream>>>(t->o.scheme, t->neq, t->diag, t->ri_ptr, t->ri,
+		t->IA, t->e2_ptr, t->e2, t->A, t->invDiag, t->F);
+	return (int)cudaGetLastError();
+}
+
+// =============================================================== ILU(0) ===
+struct IluArgs {
+	int n;
+	const int *IA, *JA, *diag;
+	const int *rows, *task;
+	int ntask;
+	unsigned *flags;
+	unsigned epoch;
+	int *counter, *err;
+};
+
+// Claim the next task for this warp (lane 0 increments, broadcast).
+__device__ __forceinline__ int claim(int *counter)
+{
+	int t = 0;
+	if ((threadIdx.x & 31) == 0) t = atomicAdd(counter, 1);
+	return __shfl_sync(0xffffffffu, t, 0);
+}
+
+#define FG_ILU_ROWCAP 32
+
+// IKJ ILU(0) of one row (ILUp_precond_setup.c:83-164): copy the row, then for
+// each lower entry in ascending column order scale by the inverted pivot of
+// that row and eliminate with its U part; store 1/pivot.
+__device__ __forceinline__ void ilu_factor_row(const IluArgs &g, int r, const double *__restrict__ AA,
+                                               double *LU, double *Dinv)
+{
+	int cols[FG_ILU_ROWCAP];
+	double vals[FG_ILU_ROWCAP];
+	{
+		int rb = g.IA[r], len = g.IA[r + 1] - rb;
+		if (len > FG_ILU_ROWCAP) { fg_set_err(g.err, FEMGPU_E_MESH); st_release(&g.flags[r], g.epoch); return; }
+		int dpos = -1;
+		for (int q = 0; q < len; q++) {
+			cols[q] = g.JA[rb + q];
+			vals[q] = AA[rb + q];
+			if (cols[q] == r) dpos = q;
+		}
+		double d = (dpos >= 0) ? vals[dpos] : 0.0;
+		for (int q = 0; q < len && cols[q] < r; q++) wait_flag(g.flags, cols[q], g.epoch, g.err);
+		for (int q = 0; q < len && cols[q] < r; q++) {
+			int jrow = cols[q];
+			vals[q] = __dmul_rn(vals[q], __ldcg(&Dinv[jrow]));
+			int kb = g.IA[jrow], ke = g.IA[jrow + 1];
+			for (int k = kb; k < ke; k++) {
+				int col = g.JA[k];
+				if (col <= jrow) continue;
+				int pos = -1;
+				for (int m = 0; m < len; m++) if (cols[m] == col) { pos = m; break; }
+				if (pos < 0) continue;
+				double prod = __dmul_rn(vals[q], __ldcg(&LU[k]));
+				if (col == r) d = __dsub_rn(d, prod);
+				else vals[pos] = __dsub_rn(vals[pos], prod);
+			}
+		}
+		for (int q = 0; q < len; q++) LU[rb + q] = (q == dpos) ? d : vals[q];
+		if (d == 0.0) { fg_set_err(g.err, FEMGPU_E_ZERO_PIVOT); Dinv[r] = 0.0; }
+		else Dinv[r] = 1.0 / d;
+		st_release(&g.flags[r], g.epoch);
+	}
+}
+
+__global__ void __launch_bounds__(128) k_ilu0_factor(IluArgs g, const double *__restrict__ AA,
+                                                     double *LU, double *Dinv)
+{
+	const int lane = threadIdx.x & 31;
+	for (;;) {
+		int t = claim(g.counter);
+		if (t >= g.ntask) break;
+		int b = g.task[t], c = g.task[t + 1] - b;
+		if (lane < c) ilu_factor_row(g, g.rows[b + lane], AA, LU, Dinv);
+	}
+}
+
+// Forward sweep (ILUp_precond.c:35-43): z[i] = p[i] - sum L(i,j) z[j].
+__device__ __forceinline__ void ilu_lower_row(const IluArgs &g, int r, const double *__restrict__ LU,
+                                              const double *p, double *z)
+{
+	int rb = g.IA[r], re = g.IA[r + 1];
+	double x = p[r];
+	for (int j = rb; j < re; j++) {
+		int col = g.JA[j];
+		if (col >= r) break;
+		wait_flag(g.flags, col, g.epoch, g.err);
+		x = __dsub_rn(x, __dmul_rn(__ldcg(&z[col]), LU[j]));
+	}
+	z[r] = x;
+	st_release(&g.flags[r], g.epoch);
+}
+
+__global__ void __launch_bounds__(128) k_ilu0_lower(IluArgs g, const double *__restrict__ LU,
+                                                    const double *p, double *z, const int *active)
+{
+	if (active && !*active) return;
+	const int lane = threadIdx.x & 31;
+	for (;;) {
+		int t = claim(g.counter);
+		if (t >= g.ntask) break;
+		int b = g.task[t], c = g.task[t + 1] - b;
+		if (lane < c) ilu_lower_row(g, g.rows[b + lane], LU, p, z);
+	}
+}
+
+// Backward sweep (ILUp_precond.c:45-53): z[i] = (z[i] - sum U(i,j) z[j]) / pivot.
+__device__ __forceinline__ void ilu_upper_row(const IluArgs &g, int r, const double *__restrict__ LU,
+                                              const double *__restrict__ Dinv, double *z)
+{
+	int rb = g.IA[r], re = g.IA[r + 1];
+	double x = z[r];
+	for (int j = rb; j < re; j++) {
+		int col = g.JA[j];
+		if (col <= r) continue;
+		wait_flag(g.flags, col, g.epoch, g.err);
+		x = __dsub_rn(x, __dmul_rn(__ldcg(&z[col]), LU[j]));
+	}
+	z[r] = __dmul_rn(x, Dinv[r]);
+	st_release(&g.flags[r], g.epoch);
+}
+
+__global__ void __launch_bounds__(128) k_ilu0_upper(IluArgs g, const double *__restrict__ LU,
+                                                    const double *__restrict__ Dinv, double *z,
+                                                    const int *active)
+{
+	if (active && !*active) return;
+	const int lane = threadIdx.x & 31;
+	for (;;) {
+		int t = claim(g.counter);
+		if (t >= g.ntask) break;
+		int b = g.task[t], c = g.task[t + 1] - b;
+		if (lane < c) ilu_upper_row(g, g.rows[b + lane], LU, Dinv, z);
+	}
+}
+
+static int ilu_grid(void) { return FG_SMS * 4; }
+
+static IluArgs ilu_args(femgpu_transport *t, const fg_levels *lv)
+{
+	IluArgs g;
+	g.n = t->neq; g.IA = t->IA; g.JA = t->JA; g.diag = t->diag;
+	g.rows = lv->rows; g.task = lv->task; g.ntask = lv->ntask;
+	g.flags = t->ilu.flags; g.epoch = ++t->ilu.epoch; g.counter = t->ilu.counter; g.err = &t->st->err;
+	return g;
+}
+
+extern "C" int fg_ilu0_factor(femgpu_transport *t)
+{
+	IluArgs g = ilu_args(t, &t->ilu.lo);
+	FG_TRY(cudaMemsetAsync(t->ilu.counter, 0, sizeof(int), t->stream));
+	k_ilu0_factor<<<ilu_grid(), 128, 0, t->stream>>>(g, t->A, t->ilu.LU, t->ilu.Dinv);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_precond(femgpu_transport *t, const double *p, double *z, const int *active)
+{
+	cudaStream_t s = t->stream;
+	if (t->o.precond == FEMGPU_PREC_NOT) {
+		if (p != z) FG_TRY(cudaMemcpyAsync(z, p, sizeof(double) * t->neq, cudaMemcpyDeviceToDevice, s));
+		return 0;
+	}
+	if (t->o.precond == FEMGPU_PREC_DIAG) {
+		k_diag_apply<<<fg_grid(t->neq), FG_TPB, 0, s>>>(t->neq, t->invDiag, p, z, active);
+		return (int)cudaGetLastError();
+	}
+	IluArgs gl = ilu_args(t, &t->ilu.lo);
+	FG_TRY(cudaMemsetAsync(t->ilu.counter, 0, sizeof(int), s));
+	k_ilu0_lower<<<ilu_grid(), 128, 0, s>>>(gl, t->ilu.LU, p, z, active);
+	IluArgs gu = ilu_args(t, &t->ilu.up);
+	FG_TRY(cudaMemsetAsync(t->ilu.counter, 0, sizeof(int), s));
+	k_ilu0_upper<<<ilu_grid(), 128, 0, s>>>(gu, t->ilu.LU, t->ilu.Dinv, z, active);
+	return (int)cudaGetLastError();
+}
+
+// ========================================================== reductions ====
+// Deterministic reduction: block partials, then the last block (by ticket)
+// sums them in block order.
+#define RED_TPB 256
+
+__device__ __forceinline__ double block_sum(double v, double *sh)
+{
+	v = fg_warp_sum(v);
+	int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	if (lane == 0) sh[wid] = v;
+	__syncthreads();
+	double r = 0.0;
+	if (wid == 0) {
+		r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+		r = fg_warp_sum(r);
+	}
+	__syncthreads();
+	return r;   // valid in thread 0
+}
+
+// Returns true in thread 0 of the last block, with *total the ordered sum.
+__device__ __forceinline__ bool last_block_total(double part, double *partials, unsigned *ticket,
+                                                 double *total, double *sh)
+{
+	__shared__ bool last;
+	if (threadIdx.x == 0) {
+		partials[blockIdx.x] = part;
+		__threadfence();
+		unsigned tk = atomicAdd(ticket, 1u);
+		last = (tk == gridDim.x - 1);
+	}
+	__syncthreads();
+	if (!last) return false;
+	double v = 0.0;
+	for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(&partials[b]);
+	v = block_sum(v, sh);
+	if (threadIdx.x == 0) { *total = v; *ticket = 0u; }
+	return threadIdx.x == 0;
+}
+
+__device__ __forceinline__ bool gmres_live(const fg_status *st) { return st->active != 0; }
+
+// MGS step j of iteration i (pgmres.c:107-121), fused:
+//   j == 0:       h(0,i) = u0 . w
+//   0 < j <= i:   w -= h(j-1,i) u_{j-1};  h(j,i) = u_j . w
+//   j == i+1:     w -= h(i,i) u_i;        h(i+1,i) = ||w||
+__global__ void __launch_bounds__(RED_TPB) k_mgs(const double *V, size_t ldv, int n, int i, int j,
+                                                 double *H, int ldh, double *partials, fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	__shared__ double sh[32];
+	double *w = (double *)V + (size_t)(i + 1) * ldv;
+	const double *uj = V + (size_t)j * ldv;
+	const double *um = (j > 0) ? V + (size_t)(j - 1) * ldv : nullptr;
+	double hm = (j > 0) ? H[(j - 1) * ldh + i] : 0.0;
+	double part = 0.0;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		double wk = w[k];
+		if (j > 0) { wk = __dadd_rn(wk, __dmul_rn(-hm, um[k])); w[k] = wk; }
+		part += (j <= i) ? uj[k] * wk : wk * wk;
+	}
+	part = block_sum(part, sh);
+	double tot;
+	if (last_block_total(part, partials, &st->ticket, &tot, sh))
+		H[j * ldh + i] = (j <= i) ? tot : sqrt(tot);
+}
+
+// u = u * (1/h), dscal of pgmres.c:85 / :121.
+__global__ void k_scale(double *u, int n, const double *h, fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	double sc = 1.0 / *h;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+		u[k] = __dmul_rn(sc, u[k]);
+}
+
+// Start of a restart cycle (pgmres.c:77-87): u0 = B - u0, e0 = ||u0||.
+__global__ void __launch_bounds__(RED_TPB) k_residual_start(double *u0, const double *B, int n,
+                                                            double *ge, double *partials, fg_status *st)
+{
+	__shared__ double sh[32];
+	double part = 0.0;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		double r = -__dadd_rn(u0[k], -B[k]);
+		u0[k] = r;
+		part += r * r;
+	}
+	part = block_sum(part, sh);
+	double tot;
+	if (last_block_total(part, partials, &st->ticket, &tot, sh)) {
+		ge[0] = sqrt(tot);
+		st->rho = ge[0];
+		st->inner = 0;
+		st->active = 1;
+	}
+}
+
+// ||B|| and eps = tol ||B|| (pgmres.c:49-53).
+__global__ void __launch_bounds__(RED_TPB) k_norm_eps(const double *B, int n, double tol,
+                                                      double *partials, fg_status *st)
+{
+	__shared__ double sh[32];
+	double part = 0.0;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+		part += B[k] * B[k];
+	part = block_sum(part, sh);
+	double tot;
+	if (last_block_total(part, partials, &st->ticket, &tot, sh)) {
+		st->eps = tol * sqrt(tot);
+		st->total = 0;
+		st->hdiag = sqrt(tot);
+	}
+}
+
+// Givens QR update of column i (pgmres.c:123-163), single thread.
+__global__ void k_givens(double *H, int ldh, double *cs, double *sn, double *ge, int i, int kmax,
+                         fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	for (int j = 0; j <= i - 1; j++) {
+		double hj = H[j * ldh + i], hj1 = H[(j + 1) * ldh + i];
+		double h1 = __dadd_rn(__dmul_rn(cs[j], hj), __dmul_rn(sn[j], hj1));
+		double h2 = __dadd_rn(__dmul_rn(-sn[j], hj), __dmul_rn(cs[j], hj1));
+		H[j * ldh + i] = h1;
+		H[(j + 1) * ldh + i] = h2;
+	}
+	double hii = H[i * ldh + i], hi1 = H[(i + 1) * ldh + i];
+	double r = sqrt(__dadd_rn(__dmul_rn(hii, hii), __dmul_rn(hi1, hi1)));
+	cs[i] = hii / r;
+	sn[i] = hi1 / r;
+	H[i * ldh + i] = r;
+	H[(i + 1) * ldh + i] = 0.0;
+	ge[i + 1] = __dmul_rn(-sn[i], ge[i]);
+	ge[i] = __dmul_rn(cs[i], ge[i]);
+	double rho = fabs(ge[i + 1]);
+	st->rho = rho;
+	st->inner = i + 1;
+	st->total += 1;
+	if (!(rho > st->eps) || i + 1 >= kmax) st->active = 0;
+	if (!(rho == rho)) { st->active = 0; fg_set_err(&st->err, FEMGPU_E_BREAKDOWN); }
+}
+
+// Back substitution (pgmres.c:165-175), single thread; i = inner - 1.
+__global__ void k_backsolve(const double *H, int ldh, const double *ge, double *gy, fg_status *st)
+{
+	int i = st->inner - 1;
+	if (i < 0) return;
+	gy[i] = ge[i] / H[i * ldh + i];
+	for (int j = i - 1; j >= 0; j--) {
+		double soma = 0.0;
+		for (int k = j + 1; k <= i; k++) soma = __dadd_rn(soma, __dmul_rn(H[j * ldh + k], gy[k]));
+		gy[j] = __dadd_rn(ge[j], -soma) / H[j * ldh + j];
+	}
+}
+
+// X += sum_j u_j y_j (pgmres.c:177-181), j ascending per entry.
+__global__ void k_update_x(double *X, const double *V, size_t ldv, int n, const double *gy,
+                           const fg_status *st)
+{
+	int m = st->inner;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		double x = X[k];
+		for (int j = 0; j < m; j++) x = __dadd_rn(x, __dmul_rn(V[(size_t)j * ldv + k], gy[j]));
+		X[k] = x;
+	}
+}
+
+static int red_grid(femgpu_transport *t) { return t->nblk_red; }
+
+// One restart cycle of pgmres.c:58-184, entirely stream-ordered; the status
+// block tells the host afterwards whether to restart.
+extern "C" int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, int first)
+{
+	cudaStream_t s = t->stream;
+	int n = t->neq, kmax = t->kmax, ldh = kmax + 1, G = red_grid(t), rc;
+	size_t ldv = t->ldv;
+	double *V = t->V;
+	int *active = &t->st->active;
+	if (first)
+		k_norm_eps<<<G, RED_TPB, 0, s>>>(B, n, t->o.tol, t->partials, t->st);
+	// u0 = M^-1 A X  (precondR is the identity in the transport drivers)
+	if ((rc = fg_matvec(t, X, V, nullptr))) return rc;
+	if ((rc = fg_precond(t, V, V, nullptr))) return rc;
+	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, t->ge, t->partials, t->st);
+	k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, t->ge, t->st);
+	for (int i = 0; i < kmax; i++) {
+		double *w = V + (size_t)(i + 1) * ldv;
+		if ((rc = fg_matvec(t, V + (size_t)i * ldv, w, active))) return rc;
+		if ((rc = fg_precond(t, w, w, active))) return rc;
+		for (int j = 0; j <= i + 1; j++)
+			k_mgs<<<G, RED_TPB, 0, s>>>(V, ldv, n, i, j, t->H, ldh, t->partials, t->st);
+		k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(w, n, t->H + (i + 1) * ldh + i, t->st);
+		k_givens<<<1, 1, 0, s>>>(t->H, ldh, t->cs, t->sn, t->ge, i, kmax, t->st);
+	}
+	k_backsolve<<<1, 1, 0, s>>>(t->H, ldh, t->ge, t->gy, t->st);
+	k_update_x<<<fg_grid(n), FG_TPB, 0, s>>>(X, V, ldv, n, t->gy, t->st);
+	return (int)cudaGetLastError();
+}
+
+// out = a . b (deterministic), device scalar.
+__global__ void __launch_bounds__(RED_TPB) k_dot(const double *a, const double *b, int n,
+                                                 double *partials, unsigned *ticket, double *out)
+{
+	__shared__ double sh[32];
+	double part = 0.0;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+		part += a[k] * b[k];
+	part = block_sum(part, sh);
+	double tot;
+	if (last_block_total(part, partials, ticket, &tot, sh)) *out = tot;
+}
+
+extern "C" int fg_dot(femgpu_transport *t, const double *a, const double *b, int n, double *out_dev)
+{
+	k_dot<<<red_grid(t), RED_TPB, 0, t->stream>>>(a, b, n, t->partials, &t->st->ticket, out_dev);
+	return (int)cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(RED_TPB) k_resid2(const double *B, const double *Q, int n,
+                                                    double *partials, unsigned *ticket, double *out)
+{
+	__shared__ double sh[32];
+	double part = 0.0;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		double r = B[k] - Q[k];
+		part += r * r;
+	}
+	part = block_sum(part, sh);
+	double tot;
+	if (last_block_total(part, partials, ticket, &tot, sh)) *out = tot;
+}
+
+// max_k |a[k] - b[k]| (the Picard stop test, Process.c:325-328).
+__global__ void __launch_bounds__(RED_TPB) k_maxabsdiff(const double *a, const double *b, int n,
+                                                        double *partials, unsigned *ticket, double *out)
+{
+	__shared__ double sh[32];
+	__shared__ bool last;
+	double m = 0.0;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+		m = fmax(m, fabs(a[k] - b[k]));
+	#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+	if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmax(m, sh[w]);
+		partials[blockIdx.x] = m;
+		__threadfence();
+		last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+	}
+	__syncthreads();
+	if (last && threadIdx.x == 0) {
+		double r = 0.0;
+		for (int q = 0; q < (int)gridDim.x; q++) r = fmax(r, __ldcg(&partials[q]));
+		*out = r;
+		*ticket = 0u;
+	}
+}
+
+extern "C" int fg_maxabsdiff(femgpu_transport *t, const double *a, const double *b, int n, double *out_dev)
+{
+	k_maxabsdiff<<<red_grid(t), RED_TPB, 0, t->stream>>>(a, b, n, t->partials, &t->st->ticket, out_dev);
+	return (int)cudaGetLastError();
+}
+
+// ||B - A X||^2 -> out_dev (A X goes to the scratch vector w2).
+extern "C" int fg_residual_norm(femgpu_transport *t, const double *B, const double *X, double *out_dev)
+{
+	int rc = fg_matvec(t, X, t->w2, nullptr);
+	if (rc) return rc;
+	k_resid2<<<red_grid(t), RED_TPB, 0, t->stream>>>(B, t->w2, t->neq, t->partials, &t->st->ticket,
+	                                                 out_dev);
+	return (int)cudaGetLastError();
+}

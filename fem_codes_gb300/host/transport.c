@@ -1,0 +1,612 @@
+/*
+ * Host driver of the steady-transport solve loop: the control flow of the
+ * reference's Preprocess (storage set-up, Preprocess.c:160-237), Process
+ * (Picard loop, Process.c:276-335) and pgmres (restart loop, pgmres.c:55-184),
+ * calling device kernels for every data-parallel step.  Plain C.
+ */
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime_api.h>
+
+#include "femgpu.h"
+#include "femgpu_host.h"
+#include "../csrc/fg_internal.h"
+
+int fg_maxabsdiff(femgpu_transport *t, const double *a, const double *b, int n, double *out_dev);
+
+static __thread char g_err[512];
+
+void fgh_set_error(const char *fmt, ...)
+{
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(g_err, sizeof g_err, fmt, ap);
+	va_end(ap);
+}
+
+const char *femgpu_last_error(void) { return g_err; }
+
+#define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) {                   \
+	fgh_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));     \
+	return FEMGPU_E_CUDA; } } while (0)
+#define KR(call) do { int r_ = (call); if (r_ > 0) {                                        \
+	fgh_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString((cudaError_t)r_)); \
+	return FEMGPU_E_CUDA; }                                                                 \
+	if (r_ < 0) { fgh_set_error("%s:%d %s: error %d", __FILE__, __LINE__, #call, r_); return r_; } \
+	} while (0)
+
+void femgpu_transport_default_opts(femgpu_transport_opts *o)
+{
+	memset(o, 0, sizeof *o);
+	o->scheme = FEMGPU_CSR;
+	o->reorder = FEMGPU_REORDER_NOT;
+	o->precond = FEMGPU_PREC_ILU0;
+	o->shock = FEMGPU_SHOCK_CAU;
+	o->hshock = FEMGPU_H_2SQRTAREA;
+	o->kmax = 30;
+	o->lmax = 1000;
+	o->tol = 1e-8;
+	o->nonlin_tol = 0.0;
+	o->precision = FEMGPU_FP64;
+	o->ir_max = 30;
+}
+
+static int dmalloc(void **p, size_t bytes)
+{
+	cudaError_t e = cudaMalloc(p, bytes ? bytes : 8);
+	if (e != cudaSuccess) {
+		fgh_set_error("cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+		return FEMGPU_E_NOMEM;
+	}
+	return 0;
+}
+
+#define DM(ptr, bytes) do { int r_ = dmalloc((void **)&(ptr), (bytes)); if (r_) return r_; } while (0)
+
+static int upload(void **dst, const void *src, size_t bytes)
+{
+	int rc = dmalloc(dst, bytes);
+	if (rc) return rc;
+	CK(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+	return 0;
+}
+
+#define UP(ptr, src, bytes) do { int r_ = upload((void **)&(ptr), (src), (bytes)); if (r_) return r_; } while (0)
+
+static int sync_err(femgpu_transport *t)
+{
+	CK(cudaMemcpyAsync(t->st_host, t->st, sizeof(fg_status), cudaMemcpyDeviceToHost, t->stream));
+	CK(cudaStreamSynchronize(t->stream));
+	if (t->st_host->err) {
+		fgh_set_error("device reported error %d", t->st_host->err);
+		return t->st_host->err;
+	}
+	return 0;
+}
+
+/* Download the CSR pattern and rebuild the device structures under a new
+ * equation numbering (reverse Cuthill-McKee, csr_Initialization.c:144-179). */
+static int reorder_symrcm(femgpu_transport *t, int *hIA, int *hJA)
+{
+	int n = t->neq, i, rc;
+	int *perm = malloc(sizeof(int) * (size_t)n), *inv = malloc(sizeof(int) * (size_t)n);
+	if (!perm || !inv) return FEMGPU_E_NOMEM;
+	rc = fgh_symrcm(n, hIA, hJA, perm);
+	if (rc) return rc;
+	for (i = 0; i < n; i++) inv[perm[i]] = i;
+	for (i = 0; i < t->nnodes; i++)
+		if (t->h_node_id[i] != -1) t->h_node_id[i] = inv[t->h_node_id[i]];
+	free(perm);
+	free(inv);
+	CK(cudaMemcpy(t->node_id, t->h_node_id, sizeof(int) * (size_t)t->nnodes, cudaMemcpyHostToDevice));
+	KR(fg_compute_lm(t));
+	KR(fg_build_incidence(t));
+	KR(fg_build_csr(t));
+	return 0;
+}
+
+static int setup_levels(femgpu_transport *t, const int *hIA, const int *hJA, int lower, fg_levels *lv)
+{
+	int *rows = malloc(sizeof(int) * ((size_t)t->neq + 1)), *task = NULL, rc;
+	if (!rows) return FEMGPU_E_NOMEM;
+	rc = fgh_levels(t->neq, hIA, hJA, lower, rows, &task, &lv->ntask, &lv->nlev);
+	if (rc) { free(rows); return rc; }
+	UP(lv->rows, rows, sizeof(int) * (size_t)t->neq);
+	UP(lv->task, task, sizeof(int) * ((size_t)lv->ntask + 1));
+	free(rows);
+	free(task);
+	return 0;
+}
+
+int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts *opts,
+		int nnodes, const double *x, const double *y, const int *node_type,
+		int nel, const int *vert, double k, double gamma,
+		const double *beta, const double *const_beta, const double *fsrc,
+		const double *upresc)
+{
+	femgpu_transport *t;
+	int i, neq = 0, rc;
+	size_t nA = 0;
+	int *hIA = NULL, *hJA = NULL;
+
+	if (!out || nnodes <= 0 || nel <= 0 || !x || !y || !node_type || !vert || !upresc ||
+	    (!beta && !const_beta)) {
+		fgh_set_error("femgpu_transport_create: missing argument");
+		return FEMGPU_E_ARG;
+	}
+	for (i = 0; i < 3 * nel; i++)
+		if (vert[i] < 0 || vert[i] >= nnodes) {
+			fgh_set_error("element vertex %d out of range", vert[i]);
+			return FEMGPU_E_MESH;
+		}
+	t = calloc(1, sizeof *t);
+	if (!t) return FEMGPU_E_NOMEM;
+	if (opts) t->o = *opts; else femgpu_transport_default_opts(&t->o);
+	if (t->o.scheme < 0 || t->o.scheme > 2 || t->o.precond < 0 || t->o.precond > 2 ||
+	    t->o.kmax < 1 || t->o.lmax < 1 || t->o.hshock < 0 || t->o.hshock > 3 ||
+	    (t->o.precond == FEMGPU_PREC_ILU0 && t->o.scheme != FEMGPU_CSR) ||
+	    (t->o.reorder == FEMGPU_REORDER_SYMRCM && t->o.scheme != FEMGPU_CSR)) {
+		/* setPreconditioner.c:84-93: ILU is defined for CSR only */
+		fgh_set_error("unsupported option combination");
+		free(t);
+		return FEMGPU_E_ARG;
+	}
+	*out = NULL;
+	t->nnodes = nnodes;
+	t->nel = nel;
+	t->k = k;
+	t->gamma = gamma;
+	t->kmax = t->o.kmax;
+	CK(cudaStreamCreateWithFlags(&t->own_stream, cudaStreamNonBlocking));
+	t->stream = t->own_stream;
+
+	/* Preprocess.c:73-81 numbering */
+	t->h_node_id = malloc(sizeof(int) * (size_t)nnodes);
+	for (i = 0; i < nnodes; i++) t->h_node_id[i] = (node_type[i] >= 1) ? neq++ : -1;
+	t->neq = neq;
+	if (neq == 0) { fgh_set_error("no unknowns"); free(t); return FEMGPU_E_MESH; }
+
+	UP(t->x, x, sizeof(double) * (size_t)nnodes);
+	UP(t->y, y, sizeof(double) * (size_t)nnodes);
+	UP(t->node_type, node_type, sizeof(int) * (size_t)nnodes);
+	UP(t->node_id, t->h_node_id, sizeof(int) * (size_t)nnodes);
+	UP(t->vert, vert, sizeof(int) * 3 * (size_t)nel);
+	UP(t->upresc, upresc, sizeof(double) * (size_t)nnodes);
+
+	/* Coefficients: constant velocity / zero source need no per-element data. */
+	t->beta_const = 1;
+	if (beta) {
+		t->cbx = beta[0]; t->cby = beta[1];
+		for (i = 1; i < nel; i++)
+			if (beta[2 * i] != t->cbx || beta[2 * i + 1] != t->cby) { t->beta_const = 0; break; }
+		if (!t->beta_const) UP(t->beta, beta, sizeof(double) * 2 * (size_t)nel);
+	} else {
+		t->cbx = const_beta[0]; t->cby = const_beta[1];
+	}
+	t->fsrc_zero = 1;
+	if (fsrc) {
+		for (i = 0; i < 3 * nel; i++) if (fsrc[i] != 0.0) { t->fsrc_zero = 0; break; }
+		if (!t->fsrc_zero) UP(t->fsrc, fsrc, sizeof(double) * 3 * (size_t)nel);
+	}
+
+	DM(t->st, sizeof(fg_status));
+	CK(cudaMemsetAsync(t->st, 0, sizeof(fg_status), t->stream));
+	CK(cudaMallocHost((void **)&t->st_host, sizeof(fg_status)));
+	memset(t->st_host, 0, sizeof(fg_status));
+	DM(t->lm, sizeof(int) * 3 * (size_t)nel);
+	KR(fg_compute_lm(t));
+	KR(fg_build_incidence(t));
+
+	if (t->o.scheme == FEMGPU_CSR) {
+		KR(fg_build_csr(t));
+		hIA = malloc(sizeof(int) * ((size_t)neq + 1));
+		hJA = malloc(sizeof(int) * ((size_t)t->nnz + 1));
+		CK(cudaMemcpy(hIA, t->IA, sizeof(int) * ((size_t)neq + 1), cudaMemcpyDeviceToHost));
+		CK(cudaMemcpy(hJA, t->JA, sizeof(int) * (size_t)t->nnz, cudaMemcpyDeviceToHost));
+		if (t->o.reorder == FEMGPU_REORDER_SYMRCM) {
+			rc = reorder_symrcm(t, hIA, hJA);
+			if (rc) return rc;
+			CK(cudaMemcpy(hIA, t->IA, sizeof(int) * ((size_t)neq + 1), cudaMemcpyDeviceToHost));
+			CK(cudaMemcpy(hJA, t->JA, sizeof(int) * (size_t)t->nnz, cudaMemcpyDeviceToHost));
+		}
+		t->bandwidth = fgh_bandwidth(neq, hIA, hJA);
+		nA = (size_t)t->nnz + 1;
+		DM(t->ke, sizeof(double) * 9 * (size_t)nel);
+	} else if (t->o.scheme == FEMGPU_EDE) {
+		KR(fg_build_ede(t));
+		nA = 4 * ((size_t)t->nedge + 1);
+		DM(t->ke, sizeof(double) * 9 * (size_t)nel);
+	} else {
+		nA = 9 * (size_t)nel;
+	}
+	DM(t->A, sizeof(double) * nA);
+	CK(cudaMemsetAsync(t->A, 0, sizeof(double) * nA, t->stream));
+	DM(t->fe, sizeof(double) * 3 * (size_t)nel);
+	DM(t->u, sizeof(double) * ((size_t)neq + 1));
+	DM(t->F, sizeof(double) * ((size_t)neq + 1));
+	DM(t->F0, sizeof(double) * ((size_t)neq + 1));
+	DM(t->w2, sizeof(double) * ((size_t)neq + 1));
+	DM(t->invDiag, sizeof(double) * ((size_t)neq + 1));
+	CK(cudaMemsetAsync(t->u, 0, sizeof(double) * ((size_t)neq + 1), t->stream));
+	CK(cudaMemsetAsync(t->F, 0, sizeof(double) * ((size_t)neq + 1), t->stream));
+	CK(cudaMemsetAsync(t->F0, 0, sizeof(double) * ((size_t)neq + 1), t->stream));
+
+	if (t->o.precond == FEMGPU_PREC_ILU0) {
+		t->ilu.n = neq;
+		t->ilu.nnz = t->nnz;
+		rc = setup_levels(t, hIA, hJA, 1, &t->ilu.lo);
+		if (rc) return rc;
+		rc = setup_levels(t, hIA, hJA, 0, &t->ilu.up);
+		if (rc) return rc;
+		DM(t->ilu.LU, sizeof(double) * nA);
+		DM(t->ilu.Dinv, sizeof(double) * ((size_t)neq + 1));
+		DM(t->ilu.flags, sizeof(unsigned) * ((size_t)neq + 1));
+		DM(t->ilu.counter, sizeof(int));
+		CK(cudaMemsetAsync(t->ilu.flags, 0, sizeof(unsigned) * ((size_t)neq + 1), t->stream));
+	}
+	free(hIA);
+	free(hJA);
+
+	/* Krylov workspace (pgmres.c:27-42), allocated once. */
+	t->ldv = (((size_t)neq + 1) + 31) & ~(size_t)31;
+	DM(t->V, sizeof(double) * t->ldv * ((size_t)t->kmax + 1));
+	DM(t->H, sizeof(double) * ((size_t)t->kmax + 1) * ((size_t)t->kmax + 1));
+	DM(t->cs, sizeof(double) * ((size_t)t->kmax + 1));
+	DM(t->sn, sizeof(double) * ((size_t)t->kmax + 1));
+	DM(t->ge, sizeof(double) * ((size_t)t->kmax + 2));
+	DM(t->gy, sizeof(double) * ((size_t)t->kmax + 1));
+	CK(cudaMemsetAsync(t->V, 0, sizeof(double) * t->ldv * ((size_t)t->kmax + 1), t->stream));
+	t->nblk_red = 2 * 152;
+	DM(t->partials, sizeof(double) * (size_t)t->nblk_red);
+	for (i = 0; i < 4; i++) CK(cudaEventCreate(&t->ev[i]));
+	CK(cudaDeviceSynchronize());
+	rc = sync_err(t);
+	if (rc) return rc;
+	*out = t;
+	return 0;
+}
+
+void femgpu_transport_destroy(femgpu_transport *t)
+{
+	int i;
+	if (!t) return;
+	cudaStreamSynchronize(t->stream);
+	void *ptrs[] = { t->x, t->y, t->upresc, t->beta, t->fsrc, t->node_type, t->node_id, t->vert,
+		t->lm, t->ri_ptr, t->ri, t->IA, t->JA, t->sbe, t->diag, t->lm2, t->order, t->ec_ptr,
+		t->ec, t->e2_ptr, t->e2, t->A, t->ke, t->fe, t->A32, t->u, t->F, t->F0, t->invDiag,
+		t->ilu.LU, t->ilu.Dinv, t->ilu.LU32, t->ilu.Dinv32, t->ilu.lo.rows, t->ilu.lo.task,
+		t->ilu.up.rows, t->ilu.up.task, t->ilu.flags, t->ilu.counter, t->V, t->H, t->cs,
+		t->sn, t->ge, t->gy, t->w2, t->partials, t->st };
+	for (i = 0; i < (int)(sizeof ptrs / sizeof ptrs[0]); i++) if (ptrs[i]) cudaFree(ptrs[i]);
+	if (t->st_host) cudaFreeHost(t->st_host);
+	for (i = 0; i < 4; i++) if (t->ev[i]) cudaEventDestroy(t->ev[i]);
+	if (t->own_stream) cudaStreamDestroy(t->own_stream);
+	free(t->h_node_id);
+	free(t);
+}
+
+int femgpu_transport_set_stream(femgpu_transport *t, void *stream)
+{
+	if (!t) return FEMGPU_E_ARG;
+	CK(cudaStreamSynchronize(t->stream));
+	t->stream = stream ? (cudaStream_t)stream : t->own_stream;
+	return 0;
+}
+
+int femgpu_transport_info(const femgpu_transport *t, int *info)
+{
+	if (!t || !info) return FEMGPU_E_ARG;
+	info[0] = t->neq; info[1] = t->nnz; info[2] = t->nedge; info[3] = t->bandwidth;
+	info[4] = t->ilu.lo.nlev; info[5] = t->ilu.up.nlev;
+	return 0;
+}
+
+int femgpu_transport_get_pattern(const femgpu_transport *t, int *IA, int *JA, int *sbe, int *order,
+		int *node_id)
+{
+	if (!t) return FEMGPU_E_ARG;
+	if (node_id) memcpy(node_id, t->h_node_id, sizeof(int) * (size_t)t->nnodes);
+	if (t->o.scheme == FEMGPU_CSR) {
+		if (IA) CK(cudaMemcpy(IA, t->IA, sizeof(int) * ((size_t)t->neq + 1), cudaMemcpyDeviceToHost));
+		if (JA) CK(cudaMemcpy(JA, t->JA, sizeof(int) * (size_t)t->nnz, cudaMemcpyDeviceToHost));
+		if (sbe) CK(cudaMemcpy(sbe, t->sbe, sizeof(int) * 9 * (size_t)t->nel, cudaMemcpyDeviceToHost));
+	} else if (t->o.scheme == FEMGPU_EDE) {
+		if (JA) CK(cudaMemcpy(JA, t->lm2, sizeof(int) * 2 * (size_t)t->nedge, cudaMemcpyDeviceToHost));
+		if (sbe) CK(cudaMemcpy(sbe, t->sbe, sizeof(int) * 3 * (size_t)t->nel, cudaMemcpyDeviceToHost));
+		if (order) CK(cudaMemcpy(order, t->order, sizeof(int) * 3 * (size_t)t->nel, cudaMemcpyDeviceToHost));
+	}
+	return 0;
+}
+
+static size_t storage_len(const femgpu_transport *t)
+{
+	if (t->o.scheme == FEMGPU_CSR) return (size_t)t->nnz + 1;
+	if (t->o.scheme == FEMGPU_EDE) return 4 * ((size_t)t->nedge + 1);
+	return 9 * (size_t)t->nel;
+}
+
+/* ---------------------------------------------------------------- build */
+int femgpu_transport_build_dev(femgpu_transport *t)
+{
+	if (!t) return FEMGPU_E_ARG;
+	CK(cudaEventRecord(t->ev[0], t->stream));
+	KR(fg_build_elements(t));
+	KR(fg_assemble(t));
+	CK(cudaEventRecord(t->ev[1], t->stream));
+	t->built = 1;
+	t->factored = 0;
+	return 0;
+}
+
+int femgpu_transport_build(femgpu_transport *t, const double *u_host, double *F_host, double *A_host)
+{
+	int rc;
+	if (!t) return FEMGPU_E_ARG;
+	if (u_host)
+		CK(cudaMemcpyAsync(t->u, u_host, sizeof(double) * ((size_t)t->neq + 1), cudaMemcpyHostToDevice,
+		                   t->stream));
+	rc = femgpu_transport_build_dev(t);
+	if (rc) return rc;
+	if (F_host)
+		CK(cudaMemcpyAsync(F_host, t->F, sizeof(double) * ((size_t)t->neq + 1), cudaMemcpyDeviceToHost,
+		                   t->stream));
+	if (A_host)
+		CK(cudaMemcpyAsync(A_host, t->A, sizeof(double) * storage_len(t), cudaMemcpyDeviceToHost, t->stream));
+	return sync_err(t);
+}
+
+/* ------------------------------------------------------- preconditioner */
+int femgpu_transport_precond_setup_dev(femgpu_transport *t, int tag)
+{
+	(void)tag;   /* the symbolic phase of tag == 1 is done once at create */
+	if (!t) return FEMGPU_E_ARG;
+	if (!t->built) { fgh_set_error("precond_setup before Build"); return FEMGPU_E_NOT_BUILT; }
+	CK(cudaMemcpyAsync(t->F0, t->F, sizeof(double) * ((size_t)t->neq + 1), cudaMemcpyDeviceToDevice,
+	                   t->stream));
+	if (t->o.precond == FEMGPU_PREC_ILU0) {
+		KR(fg_ilu0_factor(t));
+		KR(fg_precond(t, t->F, t->F, NULL));
+	} else if (t->o.precond == FEMGPU_PREC_DIAG) {
+		KR(fg_diag_setup(t));
+	}
+	CK(cudaEventRecord(t->ev[2], t->stream));
+	t->factored = 1;
+	return 0;
+}
+
+int femgpu_transport_precond_setup(femgpu_transport *t, int tag, double *F_host)
+{
+	int rc = femgpu_transport_precond_setup_dev(t, tag);
+	if (rc) return rc;
+	if (F_host)
+		CK(cudaMemcpyAsync(F_host, t->F, sizeof(double) * ((size_t)t->neq + 1), cudaMemcpyDeviceToHost,
+		                   t->stream));
+	return sync_err(t);
+}
+
+int femgpu_transport_precond_dev(femgpu_transport *t, const double *p, double *z)
+{
+	if (!t || !p || !z) return FEMGPU_E_ARG;
+	if (!t->factored && t->o.precond != FEMGPU_PREC_NOT) {
+		fgh_set_error("precond before precond_setup");
+		return FEMGPU_E_NOT_BUILT;
+	}
+	KR(fg_precond(t, p, z, NULL));
+	return 0;
+}
+
+int femgpu_transport_precond(femgpu_transport *t, const double *p_host, double *z_host)
+{
+	int rc;
+	size_t n1;
+	if (!t || !p_host || !z_host) return FEMGPU_E_ARG;
+	n1 = (size_t)t->neq + 1;
+	CK(cudaMemcpyAsync(t->w2, p_host, sizeof(double) * n1, cudaMemcpyHostToDevice, t->stream));
+	rc = femgpu_transport_precond_dev(t, t->w2, t->w2);
+	if (rc) return rc;
+	CK(cudaMemcpyAsync(z_host, t->w2, sizeof(double) * t->neq, cudaMemcpyDeviceToHost, t->stream));
+	return sync_err(t);
+}
+
+/* --------------------------------------------------------------- matvec */
+int femgpu_transport_matvec_dev(femgpu_transport *t, const double *P, double *Q)
+{
+	if (!t || !P || !Q) return FEMGPU_E_ARG;
+	KR(fg_matvec(t, P, Q, NULL));
+	return 0;
+}
+
+int femgpu_transport_matvec(femgpu_transport *t, const double *P_host, double *Q_host)
+{
+	int rc;
+	size_t n1;
+	double *P, *Q;
+	if (!t || !P_host || !Q_host) return FEMGPU_E_ARG;
+	n1 = (size_t)t->neq + 1;
+	P = t->V;
+	Q = t->V + t->ldv;
+	CK(cudaMemcpyAsync(P, P_host, sizeof(double) * n1, cudaMemcpyHostToDevice, t->stream));
+	rc = femgpu_transport_matvec_dev(t, P, Q);
+	if (rc) return rc;
+	/* csrmv.c leaves Q[neq] alone; ebemv.c / edemv.c zero P[neq] and Q[neq] */
+	CK(cudaMemcpyAsync(Q_host, Q, sizeof(double) * (t->o.scheme == FEMGPU_CSR ? n1 - 1 : n1),
+	                   cudaMemcpyDeviceToHost, t->stream));
+	rc = sync_err(t);
+	if (rc) return rc;
+	if (t->o.scheme != FEMGPU_CSR) { ((double *)P_host)[t->neq] = 0.0; Q_host[t->neq] = 0.0; }
+	return 0;
+}
+
+/* ---------------------------------------------------------------- GMRES */
+static int gmres(femgpu_transport *t, const double *B, double *X, int *iters)
+{
+	int l = 0, n = t->neq;
+	double normb2;
+	if (!t->factored && t->o.precond != FEMGPU_PREC_NOT) {
+		fgh_set_error("solve before precond_setup");
+		return FEMGPU_E_NOT_BUILT;
+	}
+	CK(cudaMemsetAsync(X, 0, sizeof(double) * (size_t)n, t->stream));          /* pgmres.c:46 */
+	KR(fg_dot(t, B, B, n, &t->st->hdiag));
+	CK(cudaMemcpyAsync(&t->st_host->hdiag, &t->st->hdiag, sizeof(double), cudaMemcpyDeviceToHost,
+	                   t->stream));
+	CK(cudaStreamSynchronize(t->stream));
+	normb2 = t->st_host->hdiag;
+	if (!(normb2 > 0.0)) {
+		/* B == 0: X = 0 is the solution (pgmres.c would divide 0 by 0). */
+		if (iters) *iters = 0;
+		return (normb2 == 0.0) ? 0 : FEMGPU_E_BREAKDOWN;
+	}
+	t->st_host->eps = t->o.tol * sqrt(normb2);
+	t->st_host->total = 0;
+	t->st_host->err = 0;
+	t->st_host->ticket = 0;
+	CK(cudaMemcpyAsync(t->st, t->st_host, sizeof(fg_status), cudaMemcpyHostToDevice, t->stream));
+	do {
+		int rc;
+		KR(fg_gmres_cycle(t, B, X, 0));
+		rc = sync_err(t);
+		if (rc) return rc;
+		l++;
+	} while (t->st_host->rho > t->st_host->eps && l < t->o.lmax);
+	if (iters) *iters = t->st_host->total;
+	if (t->st_host->rho > t->st_host->eps) {
+		fgh_set_error("GMRES: %d restarts, rho %.3e > eps %.3e", l, t->st_host->rho, t->st_host->eps);
+		return FEMGPU_E_NOT_CONVERGED;
+	}
+	return 0;
+}
+
+int femgpu_transport_solve_dev(femgpu_transport *t, int *iters)
+{
+	int rc;
+	if (!t) return FEMGPU_E_ARG;
+	rc = gmres(t, t->F, t->u, iters);
+	CK(cudaEventRecord(t->ev[3], t->stream));
+	return rc;
+}
+
+int femgpu_transport_solve(femgpu_transport *t, double *X_host, int *iters)
+{
+	int rc = femgpu_transport_solve_dev(t, iters);
+	if (rc && rc != FEMGPU_E_NOT_CONVERGED) return rc;
+	if (X_host)
+		CK(cudaMemcpyAsync(X_host, t->u, sizeof(double) * (size_t)t->neq, cudaMemcpyDeviceToHost, t->stream));
+	CK(cudaStreamSynchronize(t->stream));
+	return rc;
+}
+
+int femgpu_transport_solve_bx(femgpu_transport *t, const double *B_host, double *X_host, int *iters)
+{
+	int rc;
+	if (!t || !B_host || !X_host) return FEMGPU_E_ARG;
+	CK(cudaMemcpyAsync(t->w2, B_host, sizeof(double) * (size_t)t->neq, cudaMemcpyHostToDevice, t->stream));
+	rc = gmres(t, t->w2, t->u, iters);
+	if (rc && rc != FEMGPU_E_NOT_CONVERGED) return rc;
+	CK(cudaMemcpyAsync(X_host, t->u, sizeof(double) * (size_t)t->neq, cudaMemcpyDeviceToHost, t->stream));
+	CK(cudaStreamSynchronize(t->stream));
+	return rc;
+}
+
+double *femgpu_transport_u_dev(femgpu_transport *t) { return t ? t->u : NULL; }
+double *femgpu_transport_F_dev(femgpu_transport *t) { return t ? t->F : NULL; }
+
+/* -------------------------------------------------------------- Process */
+int femgpu_transport_process(femgpu_transport *t, int npicard, double *u_hist, int *iters)
+{
+	int it = 0, rc;
+	size_t n1;
+	double *uold;
+	if (!t || npicard < 1) return FEMGPU_E_ARG;
+	n1 = (size_t)t->neq + 1;
+	uold = t->w2;
+	CK(cudaMemsetAsync(t->u, 0, sizeof(double) * n1, t->stream));                  /* Process.c:289 */
+	while (it < npicard) {
+		int nit = 0;
+		it++;
+		CK(cudaMemcpyAsync(uold, t->u, sizeof(double) * (size_t)t->neq, cudaMemcpyDeviceToDevice, t->stream));
+		rc = femgpu_transport_build_dev(t);
+		if (rc) return rc;
+		rc = femgpu_transport_precond_setup_dev(t, it);
+		if (rc) return rc;
+		rc = femgpu_transport_solve_dev(t, &nit);
+		if (rc && rc != FEMGPU_E_NOT_CONVERGED) return rc;
+		if (iters) iters[it - 1] = nit;
+		if (u_hist)
+			CK(cudaMemcpyAsync(u_hist + (size_t)(it - 1) * n1, t->u, sizeof(double) * n1,
+			                   cudaMemcpyDeviceToHost, t->stream));
+		if (t->o.nonlin_tol > 0.0) {
+			KR(fg_maxabsdiff(t, t->u, uold, t->neq, &t->st->hdiag));
+			CK(cudaMemcpyAsync(&t->st_host->hdiag, &t->st->hdiag, sizeof(double), cudaMemcpyDeviceToHost,
+			                   t->stream));
+			CK(cudaStreamSynchronize(t->stream));
+			if (!(t->st_host->hdiag > t->o.nonlin_tol)) break;
+		}
+	}
+	CK(cudaStreamSynchronize(t->stream));
+	return it;
+}
+
+int femgpu_transport_true_residual(femgpu_transport *t, double *relres)
+{
+	double r2, b2;
+	if (!t || !relres) return FEMGPU_E_ARG;
+	KR(fg_residual_norm(t, t->F0, t->u, &t->st->hdiag));
+	KR(fg_dot(t, t->F0, t->F0, t->neq, &t->st->rho));
+	CK(cudaMemcpyAsync(t->st_host, t->st, sizeof(fg_status), cudaMemcpyDeviceToHost, t->stream));
+	CK(cudaStreamSynchronize(t->stream));
+	r2 = t->st_host->hdiag;
+	b2 = t->st_host->rho;
+	*relres = (b2 > 0) ? sqrt(r2 / b2) : sqrt(r2);
+	return 0;
+}
+
+int femgpu_transport_last_times(const femgpu_transport *t, float *tm)
+{
+	if (!t || !tm) return FEMGPU_E_ARG;
+	CK(cudaEventSynchronize(t->ev[3]));
+	CK(cudaEventElapsedTime(&tm[0], t->ev[0], t->ev[1]));
+	CK(cudaEventElapsedTime(&tm[1], t->ev[1], t->ev[2]));
+	CK(cudaEventElapsedTime(&tm[2], t->ev[2], t->ev[3]));
+	return 0;
+}
+
+/* ------------------------------------------------------- host utilities */
+int femgpu_symrcm(int n, const int *IA, const int *JA, int *perm)
+{
+	if (n <= 0 || !IA || !JA || !perm) return FEMGPU_E_ARG;
+	return fgh_symrcm(n, IA, JA, perm);
+}
+
+int femgpu_ilu_levels(int n, const int *IA, const int *JA, int lower)
+{
+	int *rows, *task = NULL, ntask = 0, nlev = 0, rc;
+	if (n <= 0 || !IA || !JA) return FEMGPU_E_ARG;
+	rows = malloc(sizeof(int) * (size_t)n);
+	if (!rows) return FEMGPU_E_NOMEM;
+	rc = fgh_levels(n, IA, JA, lower, rows, &task, &ntask, &nlev);
+	free(rows);
+	free(task);
+	return rc ? rc : nlev;
+}
+
+/* -------------------------------------------------- stateless kernels */
+int femgpu_csrmv_f64(int n, const int *IA, const int *JA, const double *AA, const double *P, double *Q,
+		void *stream)
+{
+	if (n < 0 || !IA || !JA || !AA || !P || !Q) return FEMGPU_E_ARG;
+	KR(fg_csrmv64(n, IA, JA, AA, P, Q, NULL, (cudaStream_t)stream));
+	return 0;
+}
+
+int femgpu_csrmv_f32(int n, const int *IA, const int *JA, const float *AA, const float *P, float *Q,
+		void *stream)
+{
+	if (n < 0 || !IA || !JA || !AA || !P || !Q) return FEMGPU_E_ARG;
+	KR(fg_csrmv32(n, IA, JA, AA, P, Q, NULL, (cudaStream_t)stream));
+	return 0;
+}

@@ -1,0 +1,182 @@
+/*
+ * femgpu.h -- C ABI of the GB300 (sm_103a) steady 2D stabilised-FEM solve loop.
+ *
+ * Drop-in for the hot path of mod-comp-ufes/FEM_CODES: the element build, the
+ * EBE/EDE/CSR storage and matvecs, ILU(0)/diagonal preconditioning and the
+ * restarted GMRES of 00_CommonFiles.  The reference binds these through
+ * function pointers with struct arguments (FemFunctionsType /
+ * FemOtherFunctionsType, 01_SS_Transport_Equation/2D/01_CommonFiles/
+ * SSTranspEquation.h:97-121); this ABI exposes the same operations with plain
+ * pointers and sizes, so a thin shim assigns them to those pointers (see
+ * INTEGRATION.md).  Every entry point returns 0 or a negative FEMGPU_E* code;
+ * none aborts the process and none traps the GPU.
+ *
+ * Host-buffer entry points (no suffix) take arrays in host memory laid out
+ * exactly as the reference holds them (length neq+1 vectors, slot neq being the
+ * dump for prescribed dofs) and copy across the boundary.  *_dev entry points
+ * take device pointers and run on the context's stream without host
+ * synchronisation.
+ */
+#ifndef FEMGPU_H
+#define FEMGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ------------------------------------------------------- */
+#define FEMGPU_OK                 0
+#define FEMGPU_E_ARG             -1   /* bad argument / option                 */
+#define FEMGPU_E_CUDA            -2   /* CUDA runtime error                    */
+#define FEMGPU_E_NOMEM           -3   /* device allocation failed              */
+#define FEMGPU_E_ZERO_PIVOT      -4   /* ILU zero pivot (ILUp_precond_setup.c:154-163) */
+#define FEMGPU_E_NOT_CONVERGED   -5   /* GMRES hit its restart limit           */
+#define FEMGPU_E_BREAKDOWN       -6   /* GMRES zero/NaN norm (pgmres.c:85,121) */
+#define FEMGPU_E_TIMEOUT         -7   /* a device wait exceeded its bound      */
+#define FEMGPU_E_MESH            -8   /* mesh/structure unsupported            */
+#define FEMGPU_E_NOT_BUILT       -9   /* call order (Build before solve, ...)  */
+
+/* ---- options (the reference's parameter-deck strings, Preprocess.c:44-62) */
+enum femgpu_scheme   { FEMGPU_EBE = 0, FEMGPU_EDE = 1, FEMGPU_CSR = 2 };
+enum femgpu_reorder  { FEMGPU_REORDER_NOT = 0, FEMGPU_REORDER_SYMRCM = 1 };
+enum femgpu_precond  { FEMGPU_PREC_NOT = 0, FEMGPU_PREC_ILU0 = 1, FEMGPU_PREC_DIAG = 2 };
+enum femgpu_shock    { FEMGPU_SHOCK_CAU = 0, FEMGPU_SHOCK_YZBETA = 1 };
+enum femgpu_hshock   { FEMGPU_H_2SQRTAREA = 0, FEMGPU_H_SQRTAREA = 1,
+                       FEMGPU_H_OPTION1 = 2, FEMGPU_H_OPTION2 = 3 };
+/* Arithmetic of the solve: FP64 throughout (the reference's), or FP32
+ * storage/matvec/preconditioner inside FP64 iterative refinement. */
+enum femgpu_precision { FEMGPU_FP64 = 0, FEMGPU_MIXED = 1 };
+
+typedef struct femgpu_transport_opts {
+	int scheme;          /* femgpu_scheme        (MatrixVectorProductScheme) */
+	int reorder;         /* femgpu_reorder       (reordering)                */
+	int precond;         /* femgpu_precond       (Preconditioner)            */
+	int shock;           /* femgpu_shock         (ShockCapture)              */
+	int hshock;          /* femgpu_hshock        (h_Shock)                   */
+	int outflow;         /* OutputFlow == YES                                */
+	int kmax;            /* KrylovBasisVectorsQuantity                       */
+	int lmax;            /* SolverMaxIter (restart cycles, pgmres.c:15)      */
+	double tol;          /* SolverTolerance                                  */
+	double nonlin_tol;   /* NonLinearTolerance                               */
+	int precision;       /* femgpu_precision                                 */
+	int ir_max;          /* mixed precision: max refinement sweeps           */
+} femgpu_transport_opts;
+
+void femgpu_transport_default_opts(femgpu_transport_opts *o);
+
+/* Opaque device-resident problem: mesh, numbering, storage pattern, matrix,
+ * preconditioner and Krylov workspace.  Replaces the storage the reference
+ * keeps in MatrixDataType / FemStructsType (SSTranspEquation.h:64-95). */
+typedef struct femgpu_transport femgpu_transport;
+
+/* Preprocess (Preprocess.c:160-237): numbering (id = neq++ for Type >= 1),
+ * Fill_LM, and the storage pattern -- csr_Initialization (+ SYMRCM
+ * reordering), ede_Initialization or EBE allocation -- built on the device.
+ *   x, y       [nnodes]   node coordinates
+ *   node_type  [nnodes]   reference node Type (>= 1 unknown, 0 prescribed)
+ *   vert       [3*nel]    element vertices (0-based)
+ *   k, gamma              conductivity and reaction (Condutivity(), Reaction())
+ *   beta       [2*nel]    velocity at each element centroid (Velocity(XB,YB))
+ *   fsrc       [3*nel]    source at the element's vertices (Font(...))
+ *   upresc     [nnodes]   prescribed value at each node (upresc(x,y))
+ * beta/fsrc may be NULL when const_beta/fsrc-zero apply: pass beta == NULL with
+ * const_beta non-NULL (2 doubles) for a constant velocity, fsrc == NULL for f=0. */
+int femgpu_transport_create(femgpu_transport **ctx, const femgpu_transport_opts *opts,
+		int nnodes, const double *x, const double *y, const int *node_type,
+		int nel, const int *vert, double k, double gamma,
+		const double *beta, const double *const_beta, const double *fsrc,
+		const double *upresc);
+void femgpu_transport_destroy(femgpu_transport *ctx);
+
+/* Bind the context to a CUDA stream (cudaStream_t passed as void*; NULL = the
+ * context's own stream). */
+int femgpu_transport_set_stream(femgpu_transport *ctx, void *stream);
+
+/* Sizes: info[0]=neq, [1]=nnzero, [2]=nedge, [3]=bandwidth after reordering,
+ * [4]=ILU levels (L), [5]=ILU levels (U). */
+int femgpu_transport_info(const femgpu_transport *ctx, int *info);
+
+/* Copies of the device-built structure, for parity checks against the
+ * reference (IA [neq+1], JA [nnz], CSR_by_Element [9*nel]; EDE: lm2 [2*nedge],
+ * EDGE_by_Element [3*nel], order [3*nel]; node ids [nnodes]). NULL skips. */
+int femgpu_transport_get_pattern(const femgpu_transport *ctx, int *IA, int *JA, int *sbe,
+		int *order, int *node_id);
+
+/* Build (Build_K_F_SUPG.c:5-163 through FemOtherFunctions->Build): element
+ * matrices + RHS from the current u.  u_host [neq+1] (NULL = use the device
+ * copy, i.e. the last solution), F_host [neq+1] receives F (NULL skips).
+ * A_host receives the matrix storage when non-NULL (EBE 9*nel, EDE
+ * 4*(nedge+1), CSR nnz+1). */
+int femgpu_transport_build(femgpu_transport *ctx, const double *u_host, double *F_host,
+		double *A_host);
+
+/* precond_setup (e.g. ILUp_precond_setup.c:8-60): factor, then F := M^-1 F
+ * in place on the device copy of F; F_host [neq+1] receives it when non-NULL. */
+int femgpu_transport_precond_setup(femgpu_transport *ctx, int tag, double *F_host);
+
+/* precond (ILUp_precond.c, Diag_precond.c): z = M^-1 p; p may equal z. */
+int femgpu_transport_precond(femgpu_transport *ctx, const double *p_host, double *z_host);
+
+/* ProductMatrixVector (csrmv.c / ebemv.c / edemv.c): Q = A P, P[neq] and
+ * Q[neq] set to 0 as the EBE/EDE products do. */
+int femgpu_transport_matvec(femgpu_transport *ctx, const double *P_host, double *Q_host);
+
+/* solver (pgmres.c:4-211, 4-argument steady-transport form): B = the device
+ * F (already preconditioned by precond_setup), X = the device u.  X_host
+ * [neq+1] receives u when non-NULL; iters receives the inner iterations. */
+int femgpu_transport_solve(femgpu_transport *ctx, double *X_host, int *iters);
+
+/* 6-argument pgmres form (Euler/NS solver pointer, EulerEquations.h:168):
+ * B_host, X_host [neq+1] in host memory. B is not modified. */
+int femgpu_transport_solve_bx(femgpu_transport *ctx, const double *B_host, double *X_host,
+		int *iters);
+
+/* Process (Process.c:276-335): Picard iterations Build -> precond_setup ->
+ * solver until max|u - u_old| <= NonLinearTolerance or npicard iterations.
+ * u_hist [npicard*(neq+1)] and iters [npicard] receive each iterate (NULL
+ * skips). Returns the number of Picard iterations run (> 0) or an error. */
+int femgpu_transport_process(femgpu_transport *ctx, int npicard, double *u_hist, int *iters);
+
+/* Device-pointer forms (stream-ordered, no synchronisation). */
+int femgpu_transport_build_dev(femgpu_transport *ctx);
+int femgpu_transport_precond_setup_dev(femgpu_transport *ctx, int tag);
+int femgpu_transport_matvec_dev(femgpu_transport *ctx, const double *P, double *Q);
+int femgpu_transport_precond_dev(femgpu_transport *ctx, const double *p, double *z);
+int femgpu_transport_solve_dev(femgpu_transport *ctx, int *iters);
+/* Device pointers of the context's u and F (length neq+1). */
+double *femgpu_transport_u_dev(femgpu_transport *ctx);
+double *femgpu_transport_F_dev(femgpu_transport *ctx);
+
+/* True residual ||F_orig - A u|| / ||F_orig|| of the last solve in FP64
+ * (F_orig = the RHS before precond_setup). */
+int femgpu_transport_true_residual(femgpu_transport *ctx, double *relres);
+
+/* Timing of the last solve's phases in milliseconds (CUDA events):
+ * t[0] build, t[1] precond_setup, t[2] solve. */
+int femgpu_transport_last_times(const femgpu_transport *ctx, float *t);
+
+/* ---- stateless device kernels (device pointers, stream as void*) -------- */
+/* csrmv.c:3-24 in FP64 / FP32 values. */
+int femgpu_csrmv_f64(int n, const int *IA, const int *JA, const double *AA,
+		const double *P, double *Q, void *stream);
+int femgpu_csrmv_f32(int n, const int *IA, const int *JA, const float *AA,
+		const float *P, float *Q, void *stream);
+
+/* ---- host utilities (no GPU needed) ------------------------------------- */
+/* REORDERING_SYMRCM (00_CommonFiles/Reordering/symrcm.c:4-242): reverse
+ * Cuthill-McKee permutation perm[new] = old of a structurally symmetric CSR
+ * pattern, with the reference's tie-breaking. */
+int femgpu_symrcm(int n, const int *IA, const int *JA, int *perm);
+/* Dependency levels of the ILU(0) forward (lower != 0) or backward sweep:
+ * returns the number of levels. */
+int femgpu_ilu_levels(int n, const int *IA, const int *JA, int lower);
+
+/* Last CUDA/device error text of this thread (static buffer). */
+const char *femgpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
