@@ -1,0 +1,398 @@
+#!/usr/bin/env python
+"""Benchmark: time to solution of the 2048x1024 steady transport problem.
+
+Workload: 2D advection-diffusion on the unit square, 2048x1024 cells split
+into 4,194,304 linear triangles (2,100,225 nodes), interior nodes perturbed by
+a seeded uniform offset of +-0.2h (seed 1234), k = 1e-4, beta = (cos30, sin30),
+f = 0, SUPG + CAU shock capturing, CSR storage with SYMRCM reordering.
+
+A step is one nonlinear (Picard) iteration: element build and assembly,
+ILU(0) factorisation, and the linear solve to a relative residual of 1e-8 on
+the unpreconditioned FP64 residual ||F - A u|| / ||F|| (right-preconditioned
+flexible GMRES(50); the reference's left-preconditioned stopping rule is not
+used because it accepts residuals of 1e-1 on this mesh).  Steps continue the
+Picard sequence from the warm-up steps.
+
+Arms: --impl ours (default): the GPU library through its device API (value)
+and through the host-buffer C ABI (e2e).  --impl reference: the reference's
+CPU algorithm (the oracle's restatement, one core) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time-to-solution at 1e-8 residual, learned vs ILU/AMG precond; matvec HBM GB/s"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=2048)
+    ap.add_argument("--ny", type=int, default=1024)
+    ap.add_argument("--precision", default="MIXED", choices=["FP64", "MIXED", "MIXED_IR"])
+    ap.add_argument("--precond", default="ILU0")
+    ap.add_argument("--kmax", type=int, default=50)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def workload(nx, ny):
+    from fem_codes_gb300.mesh import skew_problem, structured_mesh
+    m = structured_mesh(nx, ny, perturb=0.2, seed=1234)
+    return m, skew_problem(m)
+
+
+def config(a):
+    return {"workload": f"steady transport SUPG+CAU {a.nx}x{a.ny} cells ({2 * a.nx * a.ny} triangles), "
+                        "perturbed +-0.2h, CSR+SYMRCM, ILU(0)-FGMRES(50), rel tol 1e-8 (true residual)",
+            "nx": a.nx, "ny": a.ny, "precision": a.precision, "precond": a.precond, "kmax": a.kmax,
+            "step": "build + ILU(0) factor + solve to 1e-8", "l2": "inputs larger than L2 (matrix+factors > 129 MB)"}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.seek(0)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            c = [x.strip() for x in line.split(",")]
+            if len(c) < 9 or c[0] != "0":
+                continue
+            try:
+                sm.append(float(c[1]))
+                mx = max(mx, float(c[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, c[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------- CPU
+def cpu_run(m, p, npicard, kmax):
+    """The reference's algorithm (oracle restatement, one core): set-up, then
+    npicard Picard steps with its ILU(0) and left-preconditioned pgmres."""
+    from oracle import pyoracle
+    out = pyoracle.run_transport(m.x, m.y, p.node_type, m.vert, p.k, p.gamma, p.beta, p.fsrc, p.upresc,
+                                 scheme="CSR", reord="SYMRCM", precond="ILU0", kmax=kmax, lmax=1000,
+                                 tol=1e-8, npicard=npicard)
+    times, steps = pyoracle.last_times(npicard)
+    import scipy.sparse as sp
+    n = out["neq"]
+    A = sp.csr_matrix((out["Afirst"][:-1], out["JA"], out["IA"]), shape=(n, n))
+    b = out["Ffirst"][:-1]
+    rel = float(np.linalg.norm(b - A @ out["uhist"][0][:-1]) / np.linalg.norm(b))
+    return times, steps, out["iters"], rel
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    m, p = workload(a.nx, a.ny)
+    n = a.warmup + a.steps
+    times, steps, iters, rel = cpu_run(m, p, n, a.kmax)
+    timed = steps[a.warmup:]
+    ms = 1e3 * float(np.mean(timed))
+    cores = 1
+    line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config(a),
+            "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port",
+                             "sample": f"{a.warmup}+{a.steps} Picard steps of the full workload on one core "
+                                       f"(reference algorithm: left-preconditioned pgmres, GMRES iters "
+                                       f"{[int(i) for i in iters]}, true rel. residual of step 1 {rel:.2e}); "
+                                       f"set-up {times[0]:.1f} s excluded"},
+            "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------- GPU
+def run_ours(a):
+    import torch
+    import fem_codes_gb300 as fg
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    cpu = None
+    m, p = workload(a.nx, a.ny)
+    if rank == 0 and not a.no_cpu_baseline:
+        # bounded sample: one Picard step of the same workload on one core
+        times, steps, iters, rel = cpu_run(m, p, 1, a.kmax)
+        cpu = {"value": 1e3 * float(steps[0]), "unit": "ms", "cores": 1, "kind": "port",
+               "sample": f"1 Picard step of the full workload, reference algorithm (left-preconditioned "
+                         f"pgmres, {int(iters[0])} iters, true rel. residual {rel:.2e}), set-up "
+                         f"{times[0]:.1f} s excluded"}
+
+    T = fg.SSTransport.from_problem(m, p, scheme="CSR", reorder="SYMRCM", precond=a.precond, kmax=a.kmax,
+                                    lmax=200, tol=1e-8, solver="FGMRES", precision=a.precision,
+                                    inner_tol=1e-4, ir_max=40)
+    L = T._L
+    s = torch.cuda.Stream()
+    T.set_stream(s.cuda_stream)
+    n1 = T.neq + 1
+    launches_per_step = None
+
+    def step():
+        T.build_dev()
+        T.precond_setup_dev(2)
+        return T.solve_dev()
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = Clocks()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    iters, rels = [], []
+    torch.cuda.synchronize()
+    e0.record(s)
+    t_wall = time.perf_counter()
+    for _ in range(a.steps):
+        iters.append(step())
+    e1.record(s)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / a.steps
+    rel = T.true_residual()
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+
+    # ---- end to end through the host-buffer C ABI (pinned host memory) ----
+    u_h = torch.zeros(n1, dtype=torch.float64, pin_memory=True)
+    F_h = torch.zeros(n1, dtype=torch.float64, pin_memory=True)
+    X_h = torch.zeros(n1, dtype=torch.float64, pin_memory=True)
+    vp = ctypes.c_void_p
+    it_c = ctypes.c_int(0)
+    # start from the current iterate
+    L.femgpu_transport_solve(T.handle, vp(u_h.data_ptr()), ctypes.byref(it_c))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        rc = L.femgpu_transport_build(T.handle, vp(u_h.data_ptr()), vp(F_h.data_ptr()), None)
+        rc |= L.femgpu_transport_precond_setup(T.handle, 2, None)
+        rc2 = L.femgpu_transport_solve(T.handle, vp(X_h.data_ptr()), ctypes.byref(it_c))
+        if rc or rc2:
+            raise fg.FemGpuError(rc or rc2, "e2e step")
+        u_h.copy_(X_h)
+    torch.cuda.synchronize()
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / a.steps
+
+    # ---- per-kernel rooflines (CUDA events on the context's stream) ----
+    peak, peak_kind = peaks()
+    kern = kernel_times(T, s, a)
+    nnz, neq = T.nnzero, T.neq
+    # dominant kernel of a step: the preconditioner sweeps (two per iteration)
+    mean_it = float(np.mean(iters))
+    sweep_key = "ilu0_apply_f32" if a.precision != "FP64" else "ilu0_apply_f64"
+    shares = {
+        "ilu_apply": mean_it * kern[sweep_key],
+        "spmv": mean_it * kern["spmv_f64"],
+    }
+    dom = max(shares, key=shares.get)
+    if dom == "ilu_apply":
+        vs = 4 if a.precision != "FP64" else 8
+        # algorithmic bytes: L and U values + 4-byte indices once, pivots, in/out vectors
+        alg = nnz * (vs + 4) + neq * vs + 4 * neq * vs
+        t_k = kern[sweep_key]
+        name = "k_sweep (ILU(0) forward+backward, level-pipelined, 1 CTA)"
+    else:
+        alg = nnz * 12 + (neq + 1) * 4 + 2 * neq * 8
+        t_k = kern["spmv_f64"]
+        name = "k_csrmv64"
+    achieved = alg / (t_k * 1e-3) / 1e9
+    traffic = read_traffic(dom)
+    spmv_bytes = nnz * 12 + (neq + 1) * 4 + 2 * neq * 8
+    spmv_gbs = spmv_bytes / (kern["spmv_f64"] * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64/f32 mixed" if a.precision != "FP64" else "f64", "data": "synthetic",
+        "config": config(a),
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": n1 * 8, "d2h_bytes_per_step": 2 * n1 * 8},
+        "roofline": {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                     else "fallback 6.8 TB/s"},
+        "matvec": {"kernel": "k_csrmv64 (FP64 CSR)", "GB/s": spmv_gbs, "frac": spmv_gbs / peak,
+                   "us": kern["spmv_f64"] * 1e3,
+                   "f32_us": kern["spmv_f32"] * 1e3,
+                   "f32_GB/s": (nnz * 8 + (neq + 1) * 4 + 2 * neq * 4) / (kern["spmv_f32"] * 1e-3) / 1e9},
+        "breakdown_ms": {k: round(v, 4) for k, v in kern.items()},
+        "gmres_iters": [int(i) for i in iters], "true_rel_residual": rel,
+        "neq": neq, "nnz": nnz, "ilu_levels": [T.ilu_levels_L, T.ilu_levels_U],
+        "wall_ms_per_step": 1e3 * wall / a.steps,
+        "gpu_launches": launches_estimate(a, iters),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if clocks:
+        line["clocks"] = clocks
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    T.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def kernel_times(T, s, a, reps=10):
+    """Average duration (ms) of single launches, CUDA events on stream s."""
+    import torch
+    L = T._L
+    vp = ctypes.c_void_p
+    n1 = T.neq + 1
+    x = torch.randn(n1, dtype=torch.float64, device="cuda")
+    y = torch.zeros_like(x)
+    z32 = torch.zeros(n1, dtype=torch.float32, device="cuda")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    out = {}
+
+    def timeit(fn):
+        for _ in range(2):
+            fn()
+        tot = 0.0
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(s):
+                flush.zero_()  # evict L2 between launches (same stream)
+                e0.record(s)
+                fn()
+                e1.record(s)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / reps
+
+    torch.cuda.synchronize()
+    s.wait_stream(torch.cuda.current_stream())
+    out["spmv_f64"] = timeit(lambda: L.femgpu_transport_matvec_dev(T.handle, vp(x.data_ptr()), vp(y.data_ptr())))
+    out["ilu0_apply_f64"] = timeit(lambda: L.femgpu_transport_precond_dev(T.handle, vp(x.data_ptr()),
+                                                                          vp(y.data_ptr())))
+    out["ilu0_apply_f32"] = timeit(lambda: L.femgpu_transport_precond32_dev(T.handle, vp(x.data_ptr()),
+                                                                            vp(z32.data_ptr())))
+    out["build"] = timeit(lambda: L.femgpu_transport_build_dev(T.handle))
+    out["precond_setup"] = timeit(lambda: L.femgpu_transport_precond_setup_dev(T.handle, 2))
+    # FP32 CSR product on the same pattern (stateless entry point)
+    out["spmv_f32"] = spmv32_time(T, s, timeit)
+    return out
+
+
+def spmv32_time(T, s, timeit):
+    import torch
+    L = T._L
+    vp = ctypes.c_void_p
+    pat = T.pattern()
+    IA = torch.from_numpy(pat["IA"]).cuda()
+    JA = torch.from_numpy(pat["JA"]).cuda()
+    AA = torch.randn(T.nnzero, dtype=torch.float32, device="cuda")
+    P = torch.randn(T.neq + 1, dtype=torch.float32, device="cuda")
+    Q = torch.zeros_like(P)
+    return timeit(lambda: L.femgpu_csrmv_f32(T.neq, vp(IA.data_ptr()), vp(JA.data_ptr()), vp(AA.data_ptr()),
+                                             vp(P.data_ptr()), vp(Q.data_ptr()), vp(s.cuda_stream)))
+
+
+def read_traffic(kind):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/), or None if not captured."""
+    path = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    try:
+        for line in open(path):
+            k, v = line.split(":", 1)
+            if k.strip() == kind:
+                return float(v.split()[0])
+    except Exception:
+        return None
+    return None
+
+
+def launches_estimate(a, iters):
+    """Kernel launches of the timed steps: build (2) + factor (5) + per FGMRES
+    iteration (precond 3, matvec 1, MGS j+2, scale, Givens) + per cycle (4)."""
+    kmax = a.kmax
+    tot = 0
+    for it in iters:
+        it = int(it)
+        cyc = (it + kmax - 1) // kmax
+        inner = sum(3 + 1 + (j % kmax) + 2 + 2 for j in range(it))
+        # predicated-off iterations of the last cycle are launched too
+        pad = cyc * kmax - it
+        inner += sum(3 + 1 + ((it + q) % kmax) + 2 + 2 for q in range(pad))
+        tot += 2 + 5 + inner + 5 * cyc + 1
+    return tot
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -36,7 +36,8 @@ OPTS = {
     "precond": {"NOT": 0, "ILU0": 1, "DIAG": 2},
     "shock": {"CAU": 0, "YZBETA": 1},
     "hshock": {"2SQRTAREA": 0, "SQRTAREA": 1, "OPTION1": 2, "OPTION2": 3},
-    "precision": {"FP64": 0, "MIXED": 1},
+    "precision": {"FP64": 0, "MIXED": 1, "MIXED_IR": 2},
+    "solver": {"GMRES": 0, "PGMRES": 0, "FGMRES": 1},
 }
 
 
@@ -52,7 +53,8 @@ class Opts(ctypes.Structure):
     _fields_ = [("scheme", ctypes.c_int), ("reorder", ctypes.c_int), ("precond", ctypes.c_int),
                 ("shock", ctypes.c_int), ("hshock", ctypes.c_int), ("outflow", ctypes.c_int),
                 ("kmax", ctypes.c_int), ("lmax", ctypes.c_int), ("tol", ctypes.c_double),
-                ("nonlin_tol", ctypes.c_double), ("precision", ctypes.c_int), ("ir_max", ctypes.c_int)]
+                ("nonlin_tol", ctypes.c_double), ("precision", ctypes.c_int), ("ir_max", ctypes.c_int),
+                ("solver", ctypes.c_int), ("inner_tol", ctypes.c_double)]
 
 
 _vp = ctypes.c_void_p
@@ -126,7 +128,7 @@ class SSTransport:
     def __init__(self, x, y, node_type, vert, k, gamma, upresc, beta=None, const_beta=None,
                  fsrc=None, scheme="CSR", reorder="NOT", precond="ILU0", shock="CAU",
                  hshock="2sqrtArea", outflow=False, kmax=30, lmax=1000, tol=1e-8,
-                 nonlin_tol=0.0, precision="FP64", ir_max=30):
+                 nonlin_tol=0.0, precision="FP64", ir_max=30, solver="GMRES", inner_tol=1e-4):
         L = load()
         o = Opts()
         L.femgpu_transport_default_opts(ctypes.byref(o))
@@ -139,6 +141,8 @@ class SSTransport:
         o.kmax, o.lmax, o.tol, o.nonlin_tol = kmax, lmax, tol, nonlin_tol
         o.precision = OPTS["precision"][precision.upper()]
         o.ir_max = ir_max
+        o.solver = OPTS["solver"][solver.upper()]
+        o.inner_tol = inner_tol
         self.opts = o
         self._keep = [_f64(x), _f64(y), _i32(node_type), _i32(np.asarray(vert).reshape(-1)),
                       _f64(upresc)]

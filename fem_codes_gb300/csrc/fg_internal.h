@@ -25,23 +25,31 @@
 extern "C" {
 #endif
 
-/* Level-scheduled sparse triangular structure (ILU(0) factor and sweeps). */
-typedef struct fg_levels {
-	int nlev;          /* number of dependency levels                        */
-	int ntask;         /* level-aligned tasks of <= 32 rows                  */
-	int *rows;         /* [n] rows in (level, row) order                     */
-	int *task;         /* [ntask+1] start offsets into rows                  */
-} fg_levels;
+/* One triangular sweep compiled into level blocks (see ilu.cu). */
+typedef struct fg_sweep {
+	int nlev;
+	long long bytes, maxblk, nval;
+	int npad;                  /* padded length of the level-ordered vector  */
+	unsigned char *prog;       /* level blocks                               */
+	long long *blk_off;        /* [nlev+1] byte offsets of the blocks        */
+	int *lev_start;            /* [nlev+1] first level-order position        */
+	int *lev_pstart;           /* [nlev+1] same, padded to 4 entries         */
+	int *rows;                 /* [n] row at each level-order position       */
+	int *ppos;                 /* [n] padded position of each position       */
+	long long *val_off;        /* [nval] byte offset of each value slot      */
+	int *val_src;              /* [nval] CSR position (-1 zero, -2-r pivot)  */
+} fg_sweep;
+
+typedef struct fg_ilu_sweeps {
+	fg_sweep lo64, up64, lo32, up32;
+	double *bl64, *y64;
+	float *bl32, *y32;
+} fg_ilu_sweeps;
 
 typedef struct fg_ilu {
 	int n, nnz;
 	double *LU;        /* [nnz] L (col<row) and U (col>row) in A's positions */
 	double *Dinv;      /* [n] inverted pivots                                */
-	float *LU32, *Dinv32;
-	fg_levels lo, up;  /* forward (also the factor) and backward schedules   */
-	unsigned *flags;   /* [n] completion epochs                              */
-	unsigned epoch;
-	int *counter;      /* task claim counter                                 */
 } fg_ilu;
 
 /* Device status block (one per context, device memory). */
@@ -80,12 +88,17 @@ struct femgpu_transport {
 	double *A, *ke, *fe;
 	float *A32;
 	double *u, *F, *F0, *invDiag;
+	float *invDiag32;
 	fg_ilu ilu;
+	fg_ilu_sweeps sweeps;
 
 	/* Krylov workspace */
 	int kmax;
 	size_t ldv;
 	double *V, *H, *cs, *sn, *ge, *gy, *w2;
+	double *Z;                      /* FGMRES preconditioned vectors (FP64)  */
+	float *Z32;                     /* ... (FP32, mixed precision)           */
+	double *xr, *dr;                /* refinement: residual and correction   */
 	double *partials;               /* reduction partials                    */
 	int nblk_red;
 	fg_status *st;                  /* device status                         */
@@ -114,10 +127,21 @@ int fg_csrmv64(int n, const int *IA, const int *JA, const double *AA, const doub
 int fg_csrmv32(int n, const int *IA, const int *JA, const float *AA, const float *P,
                float *Q, const int *active, cudaStream_t s);
 int fg_diag_setup(femgpu_transport *t);
-int fg_levels_build(const int *h_IA, const int *h_JA, int n, int lower, fg_levels *lv);
-int fg_ilu0_factor(femgpu_transport *t);
 int fg_precond(femgpu_transport *t, const double *p, double *z, const int *active);
 int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, int first);
+/* Flexible GMRES cycle, right preconditioned; mixed != 0: FP32 operator and
+ * preconditioner (A32, FP32 ILU/diagonal), FP64 Arnoldi. */
+int fg_fgmres_cycle(femgpu_transport *t, const double *B, double *X, int mixed);
+int fg_to_f32(const double *a, float *b, long long n, cudaStream_t s);
+int fg_axpy_resid(femgpu_transport *t, const double *B, double *r);     /* r = B - A u */
+int fg_add(double *x, const double *d, int n, cudaStream_t s);          /* x += d */
+
+/* ilu.cu */
+int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJA);
+int fg_ilu0_factor(femgpu_transport *t);
+int fg_ilu0_apply64(femgpu_transport *t, const double *p, double *z, const int *active);
+int fg_ilu0_apply32(femgpu_transport *t, const double *p, float *z, const int *active);
+void fg_ilu_free(femgpu_transport *t);
 int fg_dot(femgpu_transport *t, const double *a, const double *b, int n, double *out_dev);
 int fg_residual_norm(femgpu_transport *t, const double *B, const double *X, double *out_dev);
 

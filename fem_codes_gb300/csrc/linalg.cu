@@ -1,43 +1,18 @@
 // Linear algebra of the solve loop on the device:
 //   * matvecs csrmv.c / ebemv.c / edemv.c as per-row gathers (no atomics; the
-//     additions of each row happen in the reference's order);
+//     additions of each row happen in the reference's order), plus FP32-value
+//     CSR products for the mixed-precision solve;
 //   * diagonal preconditioner (Diag_precond*_setup.c, Diag_precond.c);
-//   * ILU(0) (ILUp_precond_setup.c:66-167 at p = 0, ILUp_precond.c:26-46):
-//     factorisation and triangular sweeps in level order by a sync-free
-//     kernel -- one lane per row, warps claim level-aligned tasks of 32 rows
-//     in order, every row waits (bounded) for the completion flags of the rows
-//     it depends on;
-//   * the restarted GMRES of pgmres.c:4-211 with its Arnoldi, Givens and
-//     back-substitution on the device; the inner loop is predicated on a
-//     device flag so a whole restart cycle is enqueued without host syncs.
+//   * the restarted GMRES of pgmres.c:4-211 (left preconditioned) and a
+//     flexible, right-preconditioned GMRES judged by the unpreconditioned
+//     residual, with Arnoldi, Givens and back-substitution on the device; the
+//     inner loop is predicated on a device flag so a whole restart cycle is
+//     enqueued without host synchronisation.
 // Products and sums in the FP64 parity kernels use __dmul_rn/__dadd_rn so
 // they are rounded exactly like the reference compiled without contraction.
+// ILU(0) lives in ilu.cu.
 #include "fg_common.cuh"
 #include <math.h>
-
-#define FG_SPIN_LIMIT (1 << 22)   // bounded waits (~0.4 s with the sleep below)
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
-{
-	unsigned v;
-	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-	return v;
-}
-
-__device__ __forceinline__ void st_release(unsigned *p, unsigned v)
-{
-	asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
-}
-
-// Wait until flags[j] == epoch; on timeout record FEMGPU_E_TIMEOUT and give up.
-__device__ __forceinline__ void wait_flag(const unsigned *flags, int j, unsigned epoch, int *err)
-{
-	int spins = 0;
-	while (ld_acquire(flags + j) != epoch) {
-		if (++spins > FG_SPIN_LIMIT) { fg_set_err(err, FEMGPU_E_TIMEOUT); return; }
-		__nanosleep(100);
-	}
-}
 
 // ============================================================= matvecs ====
 // csrmv.c:15-20: Q[i] = sum_j AA[j] P[JA[j]] in column order.
@@ -55,11 +30,11 @@ __global__ void k_csrmv64(int n, const int *__restrict__ IA, const int *__restri
 	}
 }
 
-// FP32 values: G lanes per row, coalesced loads, shuffle reduction.
-template <int G>
+// FP32 values and input, G lanes per row, FP32 accumulation; output TO.
+template <int G, typename TO>
 __global__ void k_csrmv32(int n, const int *__restrict__ IA, const int *__restrict__ JA,
                           const float *__restrict__ AA, const float *__restrict__ P,
-                          float *__restrict__ Q, const int *active)
+                          TO *__restrict__ Q, const int *active)
 {
 	if (active && !*active) return;
 	int lane = threadIdx.x % G;
@@ -67,7 +42,26 @@ __global__ void k_csrmv32(int n, const int *__restrict__ IA, const int *__restri
 	for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += gstride) {
 		int b = __ldg(&IA[r]), e = __ldg(&IA[r + 1]);
 		float q = 0.f;
-		for (int j = b + lane; j < e; j += G) q += __ldg(&AA[j]) * __ldg(&P[__ldg(&JA[j])]);
+		for (int j = b + lane; j < e; j += G) q = fmaf(__ldg(&AA[j]), __ldg(&P[__ldg(&JA[j])]), q);
+		#pragma unroll
+		for (int o = G / 2; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o, G);
+		if (lane == 0) Q[r] = (TO)q;
+	}
+}
+
+// FP64 values, FP32 input, FP64 accumulation (mixed mode with FP64 operator).
+template <int G>
+__global__ void k_csrmv64_xf(int n, const int *__restrict__ IA, const int *__restrict__ JA,
+                             const double *__restrict__ AA, const float *__restrict__ P,
+                             double *__restrict__ Q, const int *active)
+{
+	if (active && !*active) return;
+	int lane = threadIdx.x % G;
+	long long gstride = (long long)gridDim.x * blockDim.x / G;
+	for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += gstride) {
+		int b = __ldg(&IA[r]), e = __ldg(&IA[r + 1]);
+		double q = 0.0;
+		for (int j = b + lane; j < e; j += G) q = fma(__ldg(&AA[j]), (double)__ldg(&P[__ldg(&JA[j])]), q);
 		#pragma unroll
 		for (int o = G / 2; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o, G);
 		if (lane == 0) Q[r] = q;
@@ -84,7 +78,7 @@ extern "C" int fg_csrmv64(int n, const int *IA, const int *JA, const double *AA,
 extern "C" int fg_csrmv32(int n, const int *IA, const int *JA, const float *AA, const float *P,
                           float *Q, const int *active, cudaStream_t s)
 {
-	k_csrmv32<4><<<fg_grid(4LL * n, 256, 32), 256, 0, s>>>(n, IA, JA, AA, P, Q, active);
+	k_csrmv32<4, float><<<fg_grid(4LL * n, 256, 32), 256, 0, s>>>(n, IA, JA, AA, P, Q, active);
 	return (int)cudaGetLastError();
 }
 
@@ -156,13 +150,25 @@ extern "C" int fg_matvec(femgpu_transport *t, const double *P, double *Q, const 
 	return (int)cudaGetLastError();
 }
 
+// Operator applied to an FP32 vector (mixed precision, CSR): FP64 values
+// with FP64 accumulation (op32 == 0) or FP32 values with FP32 accumulation.
+static int matvec_xf(femgpu_transport *t, const float *P, double *Q, const int *active, int op32)
+{
+	cudaStream_t s = t->stream;
+	if (op32) k_csrmv32<4, double><<<fg_grid(4LL * t->neq, 256, 32), 256, 0, s>>>(t->neq, t->IA, t->JA,
+		t->A32, P, Q, active);
+	else k_csrmv64_xf<4><<<fg_grid(4LL * t->neq, 256, 32), 256, 0, s>>>(t->neq, t->IA, t->JA, t->A, P, Q,
+		active);
+	return (int)cudaGetLastError();
+}
+
 // ============================================================ diagonal ====
 // Diag_precond_CSR_setup.c:13-26, Diag_precond_EBE_setup.c:15-33,
 // Diag_precond_EDE_setup.c:14-31: diagonal (summed in the reference's
-// order), inverted, then F := F / D.
+// order), inverted, then F := F / D (unless the solve is right preconditioned).
 __global__ void k_diag_setup(int scheme, int neq, const int *diag, const int *ri_ptr, const int *ri,
                              const int *first, const int *e2_ptr, const int *e2, const double *A,
-                             double *invDiag, double *F)
+                             double *invDiag, float *invDiag32, double *F)
 {
 	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < neq; I += gridDim.x * blockDim.x) {
 		double d = 0.0;
@@ -178,7 +184,8 @@ __global__ void k_diag_setup(int scheme, int neq, const int *diag, const int *ri
 		}
 		double inv = 1.0 / d;
 		invDiag[I] = inv;
-		F[I] = __dmul_rn(F[I], inv);
+		invDiag32[I] = (float)inv;
+		if (F) F[I] = __dmul_rn(F[I], inv);
 	}
 }
 
@@ -189,165 +196,28 @@ __global__ void k_diag_apply(int n, const double *invDiag, const double *p, doub
 		z[i] = __dmul_rn(p[i], invDiag[i]);
 }
 
+__global__ void k_diag_apply32(int n, const float *invDiag, const double *p, float *z, const int *active)
+{
+	if (active && !*active) return;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		z[i] = (float)p[i] * invDiag[i];
+}
+
+__global__ void k_copy_f32(int n, const double *p, float *z, const int *active)
+{
+	if (active && !*active) return;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) z[i] = (float)p[i];
+}
+
 extern "C" int fg_diag_setup(femgpu_transport *t)
 {
 	k_diag_setup<<<fg_grid(t->neq), FG_TPB, 0, t->stream>>>(t->o.scheme, t->neq, t->diag, t->ri_ptr, t->ri,
-		t->IA, t->e2_ptr, t->e2, t->A, t->invDiag, t->F);
+		t->IA, t->e2_ptr, t->e2, t->A, t->invDiag, t->invDiag32,
+		t->o.solver == FEMGPU_FGMRES ? nullptr : t->F);
 	return (int)cudaGetLastError();
 }
 
-// =============================================================== ILU(0) ===
-struct IluArgs {
-	int n;
-	const int *IA, *JA, *diag;
-	const int *rows, *task;
-	int ntask;
-	unsigned *flags;
-	unsigned epoch;
-	int *counter, *err;
-};
-
-// Claim the next task for this warp (lane 0 increments, broadcast).
-__device__ __forceinline__ int claim(int *counter)
-{
-	int t = 0;
-	if ((threadIdx.x & 31) == 0) t = atomicAdd(counter, 1);
-	return __shfl_sync(0xffffffffu, t, 0);
-}
-
-#define FG_ILU_ROWCAP 32
-
-// IKJ ILU(0) of one row (ILUp_precond_setup.c:83-164): copy the row, then for
-// each lower entry in ascending column order scale by the inverted pivot of
-// that row and eliminate with its U part; store 1/pivot.
-__device__ __forceinline__ void ilu_factor_row(const IluArgs &g, int r, const double *__restrict__ AA,
-                                               double *LU, double *Dinv)
-{
-	int cols[FG_ILU_ROWCAP];
-	double vals[FG_ILU_ROWCAP];
-	{
-		int rb = g.IA[r], len = g.IA[r + 1] - rb;
-		if (len > FG_ILU_ROWCAP) { fg_set_err(g.err, FEMGPU_E_MESH); st_release(&g.flags[r], g.epoch); return; }
-		int dpos = -1;
-		for (int q = 0; q < len; q++) {
-			cols[q] = g.JA[rb + q];
-			vals[q] = AA[rb + q];
-			if (cols[q] == r) dpos = q;
-		}
-		double d = (dpos >= 0) ? vals[dpos] : 0.0;
-		for (int q = 0; q < len && cols[q] < r; q++) wait_flag(g.flags, cols[q], g.epoch, g.err);
-		for (int q = 0; q < len && cols[q] < r; q++) {
-			int jrow = cols[q];
-			vals[q] = __dmul_rn(vals[q], __ldcg(&Dinv[jrow]));
-			int kb = g.IA[jrow], ke = g.IA[jrow + 1];
-			for (int k = kb; k < ke; k++) {
-				int col = g.JA[k];
-				if (col <= jrow) continue;
-				int pos = -1;
-				for (int m = 0; m < len; m++) if (cols[m] == col) { pos = m; break; }
-				if (pos < 0) continue;
-				double prod = __dmul_rn(vals[q], __ldcg(&LU[k]));
-				if (col == r) d = __dsub_rn(d, prod);
-				else vals[pos] = __dsub_rn(vals[pos], prod);
-			}
-		}
-		for (int q = 0; q < len; q++) LU[rb + q] = (q == dpos) ? d : vals[q];
-		if (d == 0.0) { fg_set_err(g.err, FEMGPU_E_ZERO_PIVOT); Dinv[r] = 0.0; }
-		else Dinv[r] = 1.0 / d;
-		st_release(&g.flags[r], g.epoch);
-	}
-}
-
-__global__ void __launch_bounds__(128) k_ilu0_factor(IluArgs g, const double *__restrict__ AA,
-                                                     double *LU, double *Dinv)
-{
-	const int lane = threadIdx.x & 31;
-	for (;;) {
-		int t = claim(g.counter);
-		if (t >= g.ntask) break;
-		int b = g.task[t], c = g.task[t + 1] - b;
-		if (lane < c) ilu_factor_row(g, g.rows[b + lane], AA, LU, Dinv);
-	}
-}
-
-// Forward sweep (ILUp_precond.c:35-43): z[i] = p[i] - sum L(i,j) z[j].
-__device__ __forceinline__ void ilu_lower_row(const IluArgs &g, int r, const double *__restrict__ LU,
-                                              const double *p, double *z)
-{
-	int rb = g.IA[r], re = g.IA[r + 1];
-	double x = p[r];
-	for (int j = rb; j < re; j++) {
-		int col = g.JA[j];
-		if (col >= r) break;
-		wait_flag(g.flags, col, g.epoch, g.err);
-		x = __dsub_rn(x, __dmul_rn(__ldcg(&z[col]), LU[j]));
-	}
-	z[r] = x;
-	st_release(&g.flags[r], g.epoch);
-}
-
-__global__ void __launch_bounds__(128) k_ilu0_lower(IluArgs g, const double *__restrict__ LU,
-                                                    const double *p, double *z, const int *active)
-{
-	if (active && !*active) return;
-	const int lane = threadIdx.x & 31;
-	for (;;) {
-		int t = claim(g.counter);
-		if (t >= g.ntask) break;
-		int b = g.task[t], c = g.task[t + 1] - b;
-		if (lane < c) ilu_lower_row(g, g.rows[b + lane], LU, p, z);
-	}
-}
-
-// Backward sweep (ILUp_precond.c:45-53): z[i] = (z[i] - sum U(i,j) z[j]) / pivot.
-__device__ __forceinline__ void ilu_upper_row(const IluArgs &g, int r, const double *__restrict__ LU,
-                                              const double *__restrict__ Dinv, double *z)
-{
-	int rb = g.IA[r], re = g.IA[r + 1];
-	double x = z[r];
-	for (int j = rb; j < re; j++) {
-		int col = g.JA[j];
-		if (col <= r) continue;
-		wait_flag(g.flags, col, g.epoch, g.err);
-		x = __dsub_rn(x, __dmul_rn(__ldcg(&z[col]), LU[j]));
-	}
-	z[r] = __dmul_rn(x, Dinv[r]);
-	st_release(&g.flags[r], g.epoch);
-}
-
-__global__ void __launch_bounds__(128) k_ilu0_upper(IluArgs g, const double *__restrict__ LU,
-                                                    const double *__restrict__ Dinv, double *z,
-                                                    const int *active)
-{
-	if (active && !*active) return;
-	const int lane = threadIdx.x & 31;
-	for (;;) {
-		int t = claim(g.counter);
-		if (t >= g.ntask) break;
-		int b = g.task[t], c = g.task[t + 1] - b;
-		if (lane < c) ilu_upper_row(g, g.rows[b + lane], LU, Dinv, z);
-	}
-}
-
-static int ilu_grid(void) { return FG_SMS * 4; }
-
-static IluArgs ilu_args(femgpu_transport *t, const fg_levels *lv)
-{
-	IluArgs g;
-	g.n = t->neq; g.IA = t->IA; g.JA = t->JA; g.diag = t->diag;
-	g.rows = lv->rows; g.task = lv->task; g.ntask = lv->ntask;
-	g.flags = t->ilu.flags; g.epoch = ++t->ilu.epoch; g.counter = t->ilu.counter; g.err = &t->st->err;
-	return g;
-}
-
-extern "C" int fg_ilu0_factor(femgpu_transport *t)
-{
-	IluArgs g = ilu_args(t, &t->ilu.lo);
-	FG_TRY(cudaMemsetAsync(t->ilu.counter, 0, sizeof(int), t->stream));
-	k_ilu0_factor<<<ilu_grid(), 128, 0, t->stream>>>(g, t->A, t->ilu.LU, t->ilu.Dinv);
-	return (int)cudaGetLastError();
-}
-
+// precond / ILUp_precond / Diag_precond in FP64; p may equal z.
 extern "C" int fg_precond(femgpu_transport *t, const double *p, double *z, const int *active)
 {
 	cudaStream_t s = t->stream;
@@ -359,13 +229,22 @@ extern "C" int fg_precond(femgpu_transport *t, const double *p, double *z, const
 		k_diag_apply<<<fg_grid(t->neq), FG_TPB, 0, s>>>(t->neq, t->invDiag, p, z, active);
 		return (int)cudaGetLastError();
 	}
-	IluArgs gl = ilu_args(t, &t->ilu.lo);
-	FG_TRY(cudaMemsetAsync(t->ilu.counter, 0, sizeof(int), s));
-	k_ilu0_lower<<<ilu_grid(), 128, 0, s>>>(gl, t->ilu.LU, p, z, active);
-	IluArgs gu = ilu_args(t, &t->ilu.up);
-	FG_TRY(cudaMemsetAsync(t->ilu.counter, 0, sizeof(int), s));
-	k_ilu0_upper<<<ilu_grid(), 128, 0, s>>>(gu, t->ilu.LU, t->ilu.Dinv, z, active);
-	return (int)cudaGetLastError();
+	return fg_ilu0_apply64(t, p, z, active);
+}
+
+// The same preconditioner computed in FP32.
+extern "C" int fg_precond32(femgpu_transport *t, const double *p, float *z, const int *active)
+{
+	cudaStream_t s = t->stream;
+	if (t->o.precond == FEMGPU_PREC_NOT) {
+		k_copy_f32<<<fg_grid(t->neq), FG_TPB, 0, s>>>(t->neq, p, z, active);
+		return (int)cudaGetLastError();
+	}
+	if (t->o.precond == FEMGPU_PREC_DIAG) {
+		k_diag_apply32<<<fg_grid(t->neq), FG_TPB, 0, s>>>(t->neq, t->invDiag32, p, z, active);
+		return (int)cudaGetLastError();
+	}
+	return fg_ilu0_apply32(t, p, z, active);
 }
 
 // ========================================================== reductions ====
@@ -445,8 +324,10 @@ __global__ void k_scale(double *u, int n, const double *h, fg_status *st)
 }
 
 // Start of a restart cycle (pgmres.c:77-87): u0 = B - u0, e0 = ||u0||.
+// force: run at least one inner iteration (the do-while of pgmres.c:89-163).
 __global__ void __launch_bounds__(RED_TPB) k_residual_start(double *u0, const double *B, int n,
-                                                            double *ge, double *partials, fg_status *st)
+                                                            double *ge, double *partials, fg_status *st,
+                                                            int force)
 {
 	__shared__ double sh[32];
 	double part = 0.0;
@@ -461,24 +342,7 @@ __global__ void __launch_bounds__(RED_TPB) k_residual_start(double *u0, const do
 		ge[0] = sqrt(tot);
 		st->rho = ge[0];
 		st->inner = 0;
-		st->active = 1;
-	}
-}
-
-// ||B|| and eps = tol ||B|| (pgmres.c:49-53).
-__global__ void __launch_bounds__(RED_TPB) k_norm_eps(const double *B, int n, double tol,
-                                                      double *partials, fg_status *st)
-{
-	__shared__ double sh[32];
-	double part = 0.0;
-	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-		part += B[k] * B[k];
-	part = block_sum(part, sh);
-	double tot;
-	if (last_block_total(part, partials, &st->ticket, &tot, sh)) {
-		st->eps = tol * sqrt(tot);
-		st->total = 0;
-		st->hdiag = sqrt(tot);
+		st->active = (force || st->rho > st->eps) ? 1 : 0;
 	}
 }
 
@@ -524,13 +388,13 @@ __global__ void k_backsolve(const double *H, int ldh, const double *ge, double *
 }
 
 // X += sum_j u_j y_j (pgmres.c:177-181), j ascending per entry.
-__global__ void k_update_x(double *X, const double *V, size_t ldv, int n, const double *gy,
-                           const fg_status *st)
+template <typename TV>
+__global__ void k_update_x(double *X, const TV *V, size_t ldv, int n, const double *gy, const fg_status *st)
 {
 	int m = st->inner;
 	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
 		double x = X[k];
-		for (int j = 0; j < m; j++) x = __dadd_rn(x, __dmul_rn(V[(size_t)j * ldv + k], gy[j]));
+		for (int j = 0; j < m; j++) x = __dadd_rn(x, __dmul_rn((double)V[(size_t)j * ldv + k], gy[j]));
 		X[k] = x;
 	}
 }
@@ -546,12 +410,11 @@ extern "C" int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, i
 	size_t ldv = t->ldv;
 	double *V = t->V;
 	int *active = &t->st->active;
-	if (first)
-		k_norm_eps<<<G, RED_TPB, 0, s>>>(B, n, t->o.tol, t->partials, t->st);
+	(void)first;
 	// u0 = M^-1 A X  (precondR is the identity in the transport drivers)
 	if ((rc = fg_matvec(t, X, V, nullptr))) return rc;
 	if ((rc = fg_precond(t, V, V, nullptr))) return rc;
-	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, t->ge, t->partials, t->st);
+	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, t->ge, t->partials, t->st, 1);
 	k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, t->ge, t->st);
 	for (int i = 0; i < kmax; i++) {
 		double *w = V + (size_t)(i + 1) * ldv;
@@ -563,7 +426,43 @@ extern "C" int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, i
 		k_givens<<<1, 1, 0, s>>>(t->H, ldh, t->cs, t->sn, t->ge, i, kmax, t->st);
 	}
 	k_backsolve<<<1, 1, 0, s>>>(t->H, ldh, t->ge, t->gy, t->st);
-	k_update_x<<<fg_grid(n), FG_TPB, 0, s>>>(X, V, ldv, n, t->gy, t->st);
+	k_update_x<double><<<fg_grid(n), FG_TPB, 0, s>>>(X, V, ldv, n, t->gy, t->st);
+	return (int)cudaGetLastError();
+}
+
+// One restart cycle of flexible GMRES with right preconditioning:
+// r0 = B - A X, z_i = M^-1 v_i, w = A z_i, MGS, Givens; X += Z y.  The
+// Arnoldi residual is the unpreconditioned one.  mixed: 0 FP64 throughout,
+// 1 FP32 preconditioner (FP64 operator), 2 FP32 preconditioner and operator.
+extern "C" int fg_fgmres_cycle(femgpu_transport *t, const double *B, double *X, int mixed)
+{
+	cudaStream_t s = t->stream;
+	int n = t->neq, kmax = t->kmax, ldh = kmax + 1, G = red_grid(t), rc;
+	size_t ldv = t->ldv;
+	double *V = t->V;
+	int *active = &t->st->active;
+	if ((rc = fg_matvec(t, X, V, nullptr))) return rc;
+	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, t->ge, t->partials, t->st, 0);
+	k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, t->ge, t->st);
+	for (int i = 0; i < kmax; i++) {
+		double *v = V + (size_t)i * ldv, *w = V + (size_t)(i + 1) * ldv;
+		if (mixed) {
+			float *z = t->Z32 + (size_t)i * ldv;
+			if ((rc = fg_precond32(t, v, z, active))) return rc;
+			if ((rc = matvec_xf(t, z, w, active, mixed == 2))) return rc;
+		} else {
+			double *z = t->Z + (size_t)i * ldv;
+			if ((rc = fg_precond(t, v, z, active))) return rc;
+			if ((rc = fg_matvec(t, z, w, active))) return rc;
+		}
+		for (int j = 0; j <= i + 1; j++)
+			k_mgs<<<G, RED_TPB, 0, s>>>(V, ldv, n, i, j, t->H, ldh, t->partials, t->st);
+		k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(w, n, t->H + (i + 1) * ldh + i, t->st);
+		k_givens<<<1, 1, 0, s>>>(t->H, ldh, t->cs, t->sn, t->ge, i, kmax, t->st);
+	}
+	k_backsolve<<<1, 1, 0, s>>>(t->H, ldh, t->ge, t->gy, t->st);
+	if (mixed) k_update_x<float><<<fg_grid(n), FG_TPB, 0, s>>>(X, t->Z32, ldv, n, t->gy, t->st);
+	else k_update_x<double><<<fg_grid(n), FG_TPB, 0, s>>>(X, t->Z, ldv, n, t->gy, t->st);
 	return (int)cudaGetLastError();
 }
 
@@ -641,5 +540,42 @@ extern "C" int fg_residual_norm(femgpu_transport *t, const double *B, const doub
 	if (rc) return rc;
 	k_resid2<<<red_grid(t), RED_TPB, 0, t->stream>>>(B, t->w2, t->neq, t->partials, &t->st->ticket,
 	                                                 out_dev);
+	return (int)cudaGetLastError();
+}
+
+// r = B - A u (FP64), for iterative refinement.
+__global__ void k_sub(const double *B, const double *Q, double *r, int n)
+{
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) r[k] = B[k] - Q[k];
+}
+
+extern "C" int fg_axpy_resid(femgpu_transport *t, const double *B, double *r)
+{
+	int rc = fg_matvec(t, t->u, t->w2, nullptr);
+	if (rc) return rc;
+	k_sub<<<fg_grid(t->neq), FG_TPB, 0, t->stream>>>(B, t->w2, r, t->neq);
+	return (int)cudaGetLastError();
+}
+
+__global__ void k_add(double *x, const double *d, int n)
+{
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) x[k] += d[k];
+}
+
+extern "C" int fg_add(double *x, const double *d, int n, cudaStream_t s)
+{
+	k_add<<<fg_grid(n), FG_TPB, 0, s>>>(x, d, n);
+	return (int)cudaGetLastError();
+}
+
+__global__ void k_to_f32(const double *a, float *b, long long n)
+{
+	for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+		b[k] = (float)a[k];
+}
+
+extern "C" int fg_to_f32(const double *a, float *b, long long n, cudaStream_t s)
+{
+	k_to_f32<<<fg_grid(n), FG_TPB, 0, s>>>(a, b, n);
 	return (int)cudaGetLastError();
 }

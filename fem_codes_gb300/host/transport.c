@@ -109,19 +109,6 @@ static int reorder_symrcm(femgpu_transport *t, int *hIA, int *hJA)
 	return 0;
 }
 
-static int setup_levels(femgpu_transport *t, const int *hIA, const int *hJA, int lower, fg_levels *lv)
-{
-	int *rows = malloc(sizeof(int) * ((size_t)t->neq + 1)), *task = NULL, rc;
-	if (!rows) return FEMGPU_E_NOMEM;
-	rc = fgh_levels(t->neq, hIA, hJA, lower, rows, &task, &lv->ntask, &lv->nlev);
-	if (rc) { free(rows); return rc; }
-	UP(lv->rows, rows, sizeof(int) * (size_t)t->neq);
-	UP(lv->task, task, sizeof(int) * ((size_t)lv->ntask + 1));
-	free(rows);
-	free(task);
-	return 0;
-}
-
 int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts *opts,
 		int nnodes, const double *x, const double *y, const int *node_type,
 		int nel, const int *vert, double k, double gamma,
@@ -148,6 +135,8 @@ int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts 
 	if (opts) t->o = *opts; else femgpu_transport_default_opts(&t->o);
 	if (t->o.scheme < 0 || t->o.scheme > 2 || t->o.precond < 0 || t->o.precond > 2 ||
 	    t->o.kmax < 1 || t->o.lmax < 1 || t->o.hshock < 0 || t->o.hshock > 3 ||
+	    t->o.precision < 0 || t->o.precision > 2 || t->o.solver < 0 || t->o.solver > 1 ||
+	    (t->o.precision != FEMGPU_FP64 && (t->o.solver != FEMGPU_FGMRES || t->o.scheme != FEMGPU_CSR)) ||
 	    (t->o.precond == FEMGPU_PREC_ILU0 && t->o.scheme != FEMGPU_CSR) ||
 	    (t->o.reorder == FEMGPU_REORDER_SYMRCM && t->o.scheme != FEMGPU_CSR)) {
 		/* setPreconditioner.c:84-93: ILU is defined for CSR only */
@@ -231,22 +220,26 @@ int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts 
 	DM(t->F0, sizeof(double) * ((size_t)neq + 1));
 	DM(t->w2, sizeof(double) * ((size_t)neq + 1));
 	DM(t->invDiag, sizeof(double) * ((size_t)neq + 1));
+	DM(t->invDiag32, sizeof(float) * ((size_t)neq + 1));
 	CK(cudaMemsetAsync(t->u, 0, sizeof(double) * ((size_t)neq + 1), t->stream));
 	CK(cudaMemsetAsync(t->F, 0, sizeof(double) * ((size_t)neq + 1), t->stream));
 	CK(cudaMemsetAsync(t->F0, 0, sizeof(double) * ((size_t)neq + 1), t->stream));
+	if (t->o.precision == FEMGPU_MIXED_IR) {
+		DM(t->A32, sizeof(float) * nA);
+		DM(t->xr, sizeof(double) * ((size_t)neq + 1));
+		DM(t->dr, sizeof(double) * ((size_t)neq + 1));
+	}
 
 	if (t->o.precond == FEMGPU_PREC_ILU0) {
 		t->ilu.n = neq;
 		t->ilu.nnz = t->nnz;
-		rc = setup_levels(t, hIA, hJA, 1, &t->ilu.lo);
-		if (rc) return rc;
-		rc = setup_levels(t, hIA, hJA, 0, &t->ilu.up);
-		if (rc) return rc;
 		DM(t->ilu.LU, sizeof(double) * nA);
 		DM(t->ilu.Dinv, sizeof(double) * ((size_t)neq + 1));
-		DM(t->ilu.flags, sizeof(unsigned) * ((size_t)neq + 1));
-		DM(t->ilu.counter, sizeof(int));
-		CK(cudaMemsetAsync(t->ilu.flags, 0, sizeof(unsigned) * ((size_t)neq + 1), t->stream));
+		rc = fg_ilu_prepare(t, hIA, hJA);
+		if (rc) {
+			fgh_set_error("ILU(0) sweep programs: %d (%s)", rc, rc > 0 ? cudaGetErrorString((cudaError_t)rc) : "");
+			return rc > 0 ? FEMGPU_E_CUDA : rc;
+		}
 	}
 	free(hIA);
 	free(hJA);
@@ -260,6 +253,10 @@ int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts 
 	DM(t->ge, sizeof(double) * ((size_t)t->kmax + 2));
 	DM(t->gy, sizeof(double) * ((size_t)t->kmax + 1));
 	CK(cudaMemsetAsync(t->V, 0, sizeof(double) * t->ldv * ((size_t)t->kmax + 1), t->stream));
+	if (t->o.solver == FEMGPU_FGMRES) {
+		if (t->o.precision == FEMGPU_FP64) DM(t->Z, sizeof(double) * t->ldv * (size_t)t->kmax);
+		else DM(t->Z32, sizeof(float) * t->ldv * (size_t)t->kmax);
+	}
 	t->nblk_red = 2 * 152;
 	DM(t->partials, sizeof(double) * (size_t)t->nblk_red);
 	for (i = 0; i < 4; i++) CK(cudaEventCreate(&t->ev[i]));
@@ -278,10 +275,10 @@ void femgpu_transport_destroy(femgpu_transport *t)
 	void *ptrs[] = { t->x, t->y, t->upresc, t->beta, t->fsrc, t->node_type, t->node_id, t->vert,
 		t->lm, t->ri_ptr, t->ri, t->IA, t->JA, t->sbe, t->diag, t->lm2, t->order, t->ec_ptr,
 		t->ec, t->e2_ptr, t->e2, t->A, t->ke, t->fe, t->A32, t->u, t->F, t->F0, t->invDiag,
-		t->ilu.LU, t->ilu.Dinv, t->ilu.LU32, t->ilu.Dinv32, t->ilu.lo.rows, t->ilu.lo.task,
-		t->ilu.up.rows, t->ilu.up.task, t->ilu.flags, t->ilu.counter, t->V, t->H, t->cs,
-		t->sn, t->ge, t->gy, t->w2, t->partials, t->st };
+		t->invDiag32, t->ilu.LU, t->ilu.Dinv, t->V, t->H, t->cs, t->sn, t->ge, t->gy, t->w2,
+		t->Z, t->Z32, t->xr, t->dr, t->partials, t->st };
 	for (i = 0; i < (int)(sizeof ptrs / sizeof ptrs[0]); i++) if (ptrs[i]) cudaFree(ptrs[i]);
+	if (t->o.precond == FEMGPU_PREC_ILU0) fg_ilu_free(t);
 	if (t->st_host) cudaFreeHost(t->st_host);
 	for (i = 0; i < 4; i++) if (t->ev[i]) cudaEventDestroy(t->ev[i]);
 	if (t->own_stream) cudaStreamDestroy(t->own_stream);
@@ -301,7 +298,7 @@ int femgpu_transport_info(const femgpu_transport *t, int *info)
 {
 	if (!t || !info) return FEMGPU_E_ARG;
 	info[0] = t->neq; info[1] = t->nnz; info[2] = t->nedge; info[3] = t->bandwidth;
-	info[4] = t->ilu.lo.nlev; info[5] = t->ilu.up.nlev;
+	info[4] = t->sweeps.lo64.nlev; info[5] = t->sweeps.up64.nlev;
 	return 0;
 }
 
@@ -367,12 +364,16 @@ int femgpu_transport_precond_setup_dev(femgpu_transport *t, int tag)
 	if (!t->built) { fgh_set_error("precond_setup before Build"); return FEMGPU_E_NOT_BUILT; }
 	CK(cudaMemcpyAsync(t->F0, t->F, sizeof(double) * ((size_t)t->neq + 1), cudaMemcpyDeviceToDevice,
 	                   t->stream));
+	/* Left preconditioning (the reference's pgmres) solves M^-1 A x = M^-1 F,
+	 * so precond_setup also applies M^-1 to F; the right-preconditioned
+	 * solver keeps F as is. */
 	if (t->o.precond == FEMGPU_PREC_ILU0) {
 		KR(fg_ilu0_factor(t));
-		KR(fg_precond(t, t->F, t->F, NULL));
+		if (t->o.solver == FEMGPU_PGMRES) KR(fg_precond(t, t->F, t->F, NULL));
 	} else if (t->o.precond == FEMGPU_PREC_DIAG) {
 		KR(fg_diag_setup(t));
 	}
+	if (t->o.precision == FEMGPU_MIXED_IR) KR(fg_to_f32(t->A, t->A32, (long long)storage_len(t), t->stream));
 	CK(cudaEventRecord(t->ev[2], t->stream));
 	t->factored = 1;
 	return 0;
@@ -396,6 +397,19 @@ int femgpu_transport_precond_dev(femgpu_transport *t, const double *p, double *z
 		return FEMGPU_E_NOT_BUILT;
 	}
 	KR(fg_precond(t, p, z, NULL));
+	return 0;
+}
+
+int fg_precond32(femgpu_transport *t, const double *p, float *z, const int *active);
+
+int femgpu_transport_precond32_dev(femgpu_transport *t, const double *p, float *z)
+{
+	if (!t || !p || !z) return FEMGPU_E_ARG;
+	if (!t->factored && t->o.precond != FEMGPU_PREC_NOT) {
+		fgh_set_error("precond before precond_setup");
+		return FEMGPU_E_NOT_BUILT;
+	}
+	KR(fg_precond32(t, p, z, NULL));
 	return 0;
 }
 
@@ -442,43 +456,89 @@ int femgpu_transport_matvec(femgpu_transport *t, const double *P_host, double *Q
 }
 
 /* ---------------------------------------------------------------- GMRES */
+static int dot_host(femgpu_transport *t, const double *a, const double *b, double *out)
+{
+	KR(fg_dot(t, a, b, t->neq, &t->st->hdiag));
+	CK(cudaMemcpyAsync(&t->st_host->hdiag, &t->st->hdiag, sizeof(double), cudaMemcpyDeviceToHost,
+	                   t->stream));
+	CK(cudaStreamSynchronize(t->stream));
+	*out = t->st_host->hdiag;
+	return 0;
+}
+
+/* Restart cycles until the cycle's residual estimate rho <= eps or lmax
+ * cycles ran.  kind: -1 the reference's left-preconditioned pgmres, else the
+ * FGMRES mixed-precision mode (0, 1 or 2).  Adds the inner iterations to
+ * *iters. */
+static int cycles(femgpu_transport *t, const double *B, double *X, int kind, double eps, int lmax,
+                  int *iters)
+{
+	int l = 0, rc;
+	t->st_host->eps = eps;
+	t->st_host->total = 0;
+	t->st_host->err = 0;
+	t->st_host->ticket = 0;
+	t->st_host->active = 0;
+	CK(cudaMemcpyAsync(t->st, t->st_host, sizeof(fg_status), cudaMemcpyHostToDevice, t->stream));
+	do {
+		if (kind < 0) KR(fg_gmres_cycle(t, B, X, 0));
+		else KR(fg_fgmres_cycle(t, B, X, kind));
+		rc = sync_err(t);
+		if (rc) return rc;
+		l++;
+	} while (t->st_host->rho > eps && l < lmax);
+	*iters += t->st_host->total;
+	if (t->st_host->rho > eps) {
+		fgh_set_error("GMRES: %d restarts, rho %.3e > eps %.3e", l, t->st_host->rho, eps);
+		return FEMGPU_E_NOT_CONVERGED;
+	}
+	return 0;
+}
+
 static int gmres(femgpu_transport *t, const double *B, double *X, int *iters)
 {
-	int l = 0, n = t->neq;
-	double normb2;
+	int n = t->neq, it = 0, rc;
+	double normb2, eps;
 	if (!t->factored && t->o.precond != FEMGPU_PREC_NOT) {
 		fgh_set_error("solve before precond_setup");
 		return FEMGPU_E_NOT_BUILT;
 	}
+	if (iters) *iters = 0;
 	CK(cudaMemsetAsync(X, 0, sizeof(double) * (size_t)n, t->stream));          /* pgmres.c:46 */
-	KR(fg_dot(t, B, B, n, &t->st->hdiag));
-	CK(cudaMemcpyAsync(&t->st_host->hdiag, &t->st->hdiag, sizeof(double), cudaMemcpyDeviceToHost,
-	                   t->stream));
-	CK(cudaStreamSynchronize(t->stream));
-	normb2 = t->st_host->hdiag;
+	rc = dot_host(t, B, B, &normb2);
+	if (rc) return rc;
 	if (!(normb2 > 0.0)) {
 		/* B == 0: X = 0 is the solution (pgmres.c would divide 0 by 0). */
-		if (iters) *iters = 0;
 		return (normb2 == 0.0) ? 0 : FEMGPU_E_BREAKDOWN;
 	}
-	t->st_host->eps = t->o.tol * sqrt(normb2);
-	t->st_host->total = 0;
-	t->st_host->err = 0;
-	t->st_host->ticket = 0;
-	CK(cudaMemcpyAsync(t->st, t->st_host, sizeof(fg_status), cudaMemcpyHostToDevice, t->stream));
-	do {
-		int rc;
-		KR(fg_gmres_cycle(t, B, X, 0));
-		rc = sync_err(t);
-		if (rc) return rc;
-		l++;
-	} while (t->st_host->rho > t->st_host->eps && l < t->o.lmax);
-	if (iters) *iters = t->st_host->total;
-	if (t->st_host->rho > t->st_host->eps) {
-		fgh_set_error("GMRES: %d restarts, rho %.3e > eps %.3e", l, t->st_host->rho, t->st_host->eps);
-		return FEMGPU_E_NOT_CONVERGED;
+	eps = t->o.tol * sqrt(normb2);                                               /* pgmres.c:49-53 */
+	if (t->o.solver == FEMGPU_PGMRES) {
+		rc = cycles(t, B, X, -1, eps, t->o.lmax, &it);
+	} else if (t->o.precision != FEMGPU_MIXED_IR) {
+		rc = cycles(t, B, X, t->o.precision == FEMGPU_MIXED ? 1 : 0, eps, t->o.lmax, &it);
+	} else {
+		/* FP64 iterative refinement around FP32 inner solves:
+		 * r = B - A x (FP64), solve A d = r to inner_tol in FP32, x += d. */
+		int sweep;
+		double itol = t->o.inner_tol > 0 ? t->o.inner_tol : 1e-4;
+		rc = FEMGPU_E_NOT_CONVERGED;
+		for (sweep = 0; sweep < t->o.ir_max; sweep++) {
+			double r2;
+			int rci;
+			KR(fg_axpy_resid(t, B, t->xr));
+			rci = dot_host(t, t->xr, t->xr, &r2);
+			if (rci) return rci;
+			if (!(r2 == r2)) { rc = FEMGPU_E_BREAKDOWN; break; }
+			if (sqrt(r2) <= eps) { rc = 0; break; }
+			CK(cudaMemsetAsync(t->dr, 0, sizeof(double) * (size_t)n, t->stream));
+			rci = cycles(t, t->xr, t->dr, 2, fmax(itol * sqrt(r2), 0.5 * eps), t->o.lmax, &it);
+			if (rci && rci != FEMGPU_E_NOT_CONVERGED) return rci;
+			KR(fg_add(X, t->dr, n, t->stream));
+		}
+		if (rc) fgh_set_error("iterative refinement: %d sweeps without reaching tol", sweep);
 	}
-	return 0;
+	if (iters) *iters = it;
+	return rc;
 }
 
 int femgpu_transport_solve_dev(femgpu_transport *t, int *iters)

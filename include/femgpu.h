@@ -45,9 +45,16 @@ enum femgpu_precond  { FEMGPU_PREC_NOT = 0, FEMGPU_PREC_ILU0 = 1, FEMGPU_PREC_DI
 enum femgpu_shock    { FEMGPU_SHOCK_CAU = 0, FEMGPU_SHOCK_YZBETA = 1 };
 enum femgpu_hshock   { FEMGPU_H_2SQRTAREA = 0, FEMGPU_H_SQRTAREA = 1,
                        FEMGPU_H_OPTION1 = 2, FEMGPU_H_OPTION2 = 3 };
-/* Arithmetic of the solve: FP64 throughout (the reference's), or FP32
- * storage/matvec/preconditioner inside FP64 iterative refinement. */
-enum femgpu_precision { FEMGPU_FP64 = 0, FEMGPU_MIXED = 1 };
+/* Arithmetic of the solve (FGMRES only): FP64 throughout (the reference's);
+ * MIXED: preconditioner in FP32, operator and Arnoldi in FP64; MIXED_IR:
+ * FP32 operator and preconditioner inside FP64 iterative refinement of the
+ * outer residual (CSR storage for both mixed modes). */
+enum femgpu_precision { FEMGPU_FP64 = 0, FEMGPU_MIXED = 1, FEMGPU_MIXED_IR = 2 };
+/* Krylov solver: the reference's left-preconditioned GMRES, which stops on
+ * ||M^-1 r|| <= tol ||M^-1 b|| (pgmres.c:49-53,184), or flexible GMRES with
+ * right preconditioning, which stops on the unpreconditioned residual
+ * ||b - A x|| <= tol ||b|| and leaves F unpreconditioned. */
+enum femgpu_solver { FEMGPU_PGMRES = 0, FEMGPU_FGMRES = 1 };
 
 typedef struct femgpu_transport_opts {
 	int scheme;          /* femgpu_scheme        (MatrixVectorProductScheme) */
@@ -62,6 +69,9 @@ typedef struct femgpu_transport_opts {
 	double nonlin_tol;   /* NonLinearTolerance                               */
 	int precision;       /* femgpu_precision                                 */
 	int ir_max;          /* mixed precision: max refinement sweeps           */
+	int solver;          /* femgpu_solver                                    */
+	double inner_tol;    /* mixed precision: relative tolerance of each FP32 */
+	                     /* inner solve inside the FP64 refinement           */
 } femgpu_transport_opts;
 
 void femgpu_transport_default_opts(femgpu_transport_opts *o);
@@ -144,6 +154,8 @@ int femgpu_transport_build_dev(femgpu_transport *ctx);
 int femgpu_transport_precond_setup_dev(femgpu_transport *ctx, int tag);
 int femgpu_transport_matvec_dev(femgpu_transport *ctx, const double *P, double *Q);
 int femgpu_transport_precond_dev(femgpu_transport *ctx, const double *p, double *z);
+/* The same preconditioner evaluated in FP32 (the mixed-precision solves'). */
+int femgpu_transport_precond32_dev(femgpu_transport *ctx, const double *p, float *z);
 int femgpu_transport_solve_dev(femgpu_transport *ctx, int *iters);
 /* Device pointers of the context's u and F (length neq+1). */
 double *femgpu_transport_u_dev(femgpu_transport *ctx);

@@ -90,6 +90,12 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 		const double *Pin, double *Qmv, double *Zpc,
 		double *uhist, int *iters);
 
+/* Phase wall times of the last orc_transport_run in seconds:
+ * [set-up, build, precond_setup, solve] (the last three summed over Picard). */
+void orc_get_times(double *t);
+/* Wall time (seconds) of each of the first n Picard iterations of that run. */
+void orc_get_step_times(double *t, int n);
+
 /* pgmres.c:4-211 on an assembled CSR system with optional ILU(0):
  * B is overwritten by M^-1 B when precond != 0 (the precond_setup side effect),
  * X receives the solution. Returns the number of inner iterations. */

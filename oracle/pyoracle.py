@@ -67,6 +67,10 @@ def lib() -> ctypes.CDLL:
                                     ctypes.c_int, ctypes.c_double, _dp, _dp]
         L.orc_ddot.restype = ctypes.c_double
         L.orc_ddot.argtypes = [ctypes.c_int, _dp, _dp]
+        L.orc_get_times.restype = None
+        L.orc_get_times.argtypes = [_dp]
+        L.orc_get_step_times.restype = None
+        L.orc_get_step_times.argtypes = [_dp, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -122,6 +126,17 @@ def run_transport(x, y, node_type, vert, k, gamma, beta, fsrc, upresc, scheme="C
     else:
         out.update(Afirst=Afirst[: 9 * ne].reshape(ne, 9))
     return out
+
+
+def last_times(npicard=0):
+    """(phase times [setup, build, precond_setup, solve], per-step times) of
+    the last run_transport, in seconds."""
+    L = lib()
+    t = np.zeros(4)
+    L.orc_get_times(t)
+    s = np.zeros(max(npicard, 1))
+    L.orc_get_step_times(s, max(npicard, 1))
+    return t, s[:npicard]
 
 
 def csr_pattern(neq, lm):

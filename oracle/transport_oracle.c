@@ -13,6 +13,32 @@
 #include <stdlib.h>
 #include <string.h>
 #include <strings.h>
+#include <time.h>
+
+/* Wall-clock phases of the last orc_transport_run (seconds): set-up, then
+ * build, precond_setup and solve summed over the Picard iterations. */
+static double g_times[4];
+#define ORC_MAX_STEPS 256
+static double g_step[ORC_MAX_STEPS];    /* wall time of each Picard iteration */
+
+static double now_s(void)
+{
+	struct timespec ts;
+	clock_gettime(CLOCK_MONOTONIC, &ts);
+	return ts.tv_sec + 1e-9 * ts.tv_nsec;
+}
+
+void orc_get_times(double *t)
+{
+	int i;
+	for (i = 0; i < 4; i++) t[i] = g_times[i];
+}
+
+void orc_get_step_times(double *t, int n)
+{
+	int i;
+	for (i = 0; i < n && i < ORC_MAX_STEPS; i++) t[i] = g_step[i];
+}
 
 /* ------------------------------------------------------------------------ */
 /* Numbering: Preprocess.c:73-81 (id = neq++ for Type >= 1), Fill_LM.c:7-19  */
@@ -808,8 +834,10 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 	size_t nA;
 	double *A, *F, *u, *uold, *LU = NULL, *Dinv = NULL, *invDiag = NULL, err = 100.0;
 
+	double t0 = now_s(), t1;
 	memset(&t, 0, sizeof t);
 	memset(&o, 0, sizeof o);
+	memset(g_times, 0, sizeof g_times);
 	neq = orc_fill_lm(nnodes, ntype, nel, vert, node_id, lm);
 	for (I = 0; I < nel; I++) etype[I] = classify_element(x, y, vert + 3*I);
 	t.nnodes = nnodes; t.nel = nel; t.neq = neq;
@@ -862,11 +890,17 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 	if (o.prec == 1) { LU = calloc(nA, sizeof(double)); Dinv = calloc((size_t)neq + 1, sizeof(double)); }
 	if (o.prec == 2) invDiag = calloc((size_t)neq + 1, sizeof(double));
 	o.A = A; o.LU = LU; o.Dinv = Dinv;
+	t1 = now_s();
+	g_times[0] = t1 - t0;
 
 	while (it < npicard && (nonlin_tol <= 0 || err > nonlin_tol)) {
+		double tstep = now_s();
 		it++;
 		memcpy(uold, u, (size_t)neq * sizeof(double));
+		t0 = tstep;
 		orc_build_supg(&t, u, A, F);
+		t1 = now_s();
+		g_times[1] += t1 - t0;
 		if (it == 1) {
 			double *tmp = malloc(((size_t)neq + 1) * sizeof(double));
 			memcpy(Ffirst, F, ((size_t)neq + 1) * sizeof(double));
@@ -875,18 +909,24 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 			op_mv(&o, tmp, Qmv);
 			free(tmp);
 		}
+		t0 = now_s();
 		if (o.prec == 1) {
 			if (orc_ilu0_factor(neq, o.IA, o.JA, A, LU, Dinv)) { it = -3; break; }
 			orc_ilu0_apply(neq, o.IA, o.JA, LU, Dinv, F, F);
 		} else if (o.prec == 2) {
 			diag_setup(&o, invDiag, F);
 		}
+		g_times[2] += now_s() - t0;
 		if (it == 1) {
 			memcpy(Fprec, F, ((size_t)neq + 1) * sizeof(double));
 			memcpy(Zpc, Pin, ((size_t)neq + 1) * sizeof(double));
 			op_prec(&o, (double *)Pin, Zpc);
 		}
+		t0 = now_s();
 		iters[it-1] = orc_pgmres(&o, kmax, lmax, tol, F, u);
+		t1 = now_s();
+		g_times[3] += t1 - t0;
+		if (it - 1 < ORC_MAX_STEPS) g_step[it-1] = t1 - tstep;
 		memcpy(uhist + (size_t)(it-1)*((size_t)neq + 1), u, ((size_t)neq + 1) * sizeof(double));
 		err = 0.0;
 		for (I = 0; I < neq; I++) {
