@@ -176,6 +176,21 @@ int femgpu_csrmv_f64(int n, const int *IA, const int *JA, const double *AA,
 int femgpu_csrmv_f32(int n, const int *IA, const int *JA, const float *AA,
 		const float *P, float *Q, void *stream);
 
+/* Allocation-free residual norm.  No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc -- code running inside a CUDA graph
+ * capture or a memory-pool-restricted host application, or a driver that
+ * must not grow device memory between steps.  Computes, for a CSR system in
+ * device memory, out2[0] = ||F - A u||^2 and out2[1] = ||F||^2 (out2: two
+ * doubles of device memory), the quantity femgpu_transport_true_residual
+ * reports.  Its block partial sums live in a fixed static device array
+ * (32 KB, held by every GPU that loads the library until exit), so
+ * n <= 4,194,304 rows; larger n returns FEMGPU_E_ARG.  The first call on a
+ * device looks up that array's device address (make it before any stream
+ * capture).  All calls share the array: calls that overlap on the GPU race,
+ * so serialise them. */
+int femgpu_csr_resnorm_noalloc(int n, const int *IA, const int *JA, const double *AA,
+		const double *u, const double *F, double *out2, void *stream);
+
 /* ---- host utilities (no GPU needed) ------------------------------------- */
 /* REORDERING_SYMRCM (00_CommonFiles/Reordering/symrcm.c:4-242): reverse
  * Cuthill-McKee permutation perm[new] = old of a structurally symmetric CSR
