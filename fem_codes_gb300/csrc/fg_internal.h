@@ -27,13 +27,13 @@ extern "C" {
 
 /* One triangular sweep compiled into level blocks (see ilu.cu). */
 typedef struct fg_sweep {
-	int nlev;
+	int nlev, nsb;             /* levels, sub-blocks (<= 512 rows each)      */
 	long long bytes, maxblk, nval;
 	int npad;                  /* padded length of the level-ordered vector  */
-	unsigned char *prog;       /* level blocks                               */
-	long long *blk_off;        /* [nlev+1] byte offsets of the blocks        */
+	unsigned char *prog;       /* sub-blocks                                 */
+	long long *blk_off;        /* [nsb+1] byte offsets of the sub-blocks     */
+	int *sb_in, *sb_inb;       /* [nsb] input slice start (padded), bytes    */
 	int *lev_start;            /* [nlev+1] first level-order position        */
-	int *lev_pstart;           /* [nlev+1] same, padded to 4 entries         */
 	int *rows;                 /* [n] row at each level-order position       */
 	int *ppos;                 /* [n] padded position of each position       */
 	long long *val_off;        /* [nval] byte offset of each value slot      */
@@ -44,6 +44,7 @@ typedef struct fg_ilu_sweeps {
 	fg_sweep lo64, up64, lo32, up32;
 	double *bl64, *y64;
 	float *bl32, *y32;
+	int *fac_ptr, *fac_prog;   /* precompiled elimination of each row        */
 } fg_ilu_sweeps;
 
 typedef struct fg_ilu {

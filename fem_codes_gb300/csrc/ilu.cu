@@ -4,33 +4,40 @@
 // The triangular sweeps have ~2.5*nx dependency levels after SYMRCM (5118
 // for a 2048x1024 grid) of a few hundred rows each, so they are bound by
 // per-level latency, not bandwidth.  They run in ONE thread block:
-//   * at set-up, each sweep is compiled into a "program": for every level a
-//     16-byte aligned block holding the level's rows in ELL layout --
-//     dependency codes, factor values (refreshed after every factorisation),
-//     output slots and, for the backward sweep, inverted pivots;
-//   * the block streams level programs (and the level's slice of the input
-//     vector) into shared memory with TMA bulk copies (cp.async.bulk +
-//     mbarrier) several levels ahead;
-//   * solution values of the most recent levels live in a shared-memory ring
-//     indexed by level-order position; older dependencies are read back from
-//     global memory (written by the same block, ordered by __syncthreads);
-//   * one __syncthreads per level.
+//   * at set-up, each sweep is compiled into a "program": every level is cut
+//     into sub-blocks of at most SW_SUB rows, each a 16-byte aligned block in
+//     ELL layout -- dependency codes, factor values (refreshed after every
+//     factorisation), output slots and, for the backward sweep, inverted
+//     pivots;
+//   * one producer warp streams sub-blocks (and their slice of the input
+//     vector) into a ring of shared-memory stages with TMA bulk copies
+//     (cp.async.bulk, completion on a "full" mbarrier; stage reuse gated by an
+//     "empty" mbarrier the consumer warps arrive on);
+//   * consumer warps compute a level, publish its values in a shared-memory
+//     ring indexed by level-order position (older dependencies are re-read
+//     from global memory) and synchronise among themselves with one named
+//     barrier per level.
 // Rows are computed in the reference's order (ascending columns) and the
 // FP64 variant rounds each operation separately, so its results are
-// bit-identical to the reference's sweeps.  Every mbarrier wait is bounded:
-// on timeout the block records FEMGPU_E_TIMEOUT, waits (bounded) for the
-// copies it has in flight and returns.
+// bit-identical to the reference's sweeps.  Every wait is bounded: on timeout
+// the block records FEMGPU_E_TIMEOUT, waits (bounded) for the copies it has in
+// flight and returns.
 #include "fg_common.cuh"
 #include <string.h>
 #include <vector>
 #include <algorithm>
 
-#define SW_THREADS 1024
+#define SW_SUB 512                    // max rows of a sub-block
+#define SW_MAXW 8                     // dependencies per row on the unrolled path
+#define SW_RPT 4                      // rows per consumer thread per pass
+#define FAC_THREADS 1024
 #define SW_RING 4096                  // ring slots (power of two)
 #define SW_NEAR 0x80000000u           // dependency code: ring slot
 #define SW_WAIT_LIMIT (1 << 24)
-#define SW_BAR_BYTES 64               // up to 8 mbarriers
+#define SW_MAXD 12                    // max stages
+#define SW_BAR_BYTES (2 * SW_MAXD * 8)
 #define SW_SMEM_CAP (220 * 1024)
+#define SW_HDR 32
 
 // ------------------------------------------------------------ PTX helpers
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -47,6 +54,11 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned
 {
 	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
 	             :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
+{
+	asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar)
@@ -72,6 +84,16 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned pari
 	return false;
 }
 
+// Wait for a phase, giving up when the bound is hit or another warp failed.
+__device__ __forceinline__ bool mbar_wait_or_fail(unsigned long long *bar, unsigned parity, volatile int *failed)
+{
+	for (int i = 0; i < SW_WAIT_LIMIT; i++) {
+		if (mbar_try_wait(bar, parity)) return true;
+		if (*failed) return false;
+	}
+	return false;
+}
+
 __device__ __forceinline__ void fence_proxy_async()
 {
 	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -80,6 +102,14 @@ __device__ __forceinline__ void fence_proxy_async()
 __device__ __forceinline__ void fence_mbar_init()
 {
 	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Synchronise the CW consumer warps (shared-memory ordering included).
+template <int CW>
+__device__ __forceinline__ void consumer_sync()
+{
+	if (CW == 1) __syncwarp();
+	else asm volatile("bar.sync 1, %0;" :: "r"(CW * 32) : "memory");
 }
 
 template <typename T> __device__ __forceinline__ T fms(T x, T a, T b);   // x - a*b
@@ -92,92 +122,159 @@ template <typename T> __device__ __forceinline__ T mul(T a, T b);
 template <> __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 template <> __device__ __forceinline__ float mul(float a, float b) { return a * b; }
 
-// Level block: header, dep[w*cp] (int), out[cp] (int), pad to 16,
-// val[w*cp] (T), and for the backward sweep dinv[cp] (T).
-struct LevHdr { int c, w, start, cp; };
+// x - a*b: separately rounded (bit-identical to the reference) or fused.
+template <typename T, bool FMA> __device__ __forceinline__ T fmsub(T x, T a, T b)
+{
+	if (FMA) return fma(-a, b, x);
+	return fms(x, a, b);
+}
+
+// Sub-block: 32-byte header, dep[w*cp] (int), out[cp] (int), pad to 16,
+// val[w*cp] (T), and for the backward sweep dinv[cp] (T); the stage then
+// holds the sub-block's slice of the input vector.  Header: rows c, ELL
+// width w, level-order position of the first row, padded rows cp, number of
+// sub-blocks of the level, a flag set when some dependency is older than the
+// ring holds (read from global memory instead), and the byte offsets of the
+// values and of the input slice.
+struct LevHdr { int c, w, start, cp, nsub, hasfar, voff, boff; };
 
 static inline __host__ __device__ long long al16(long long x) { return (x + 15) & ~15LL; }
 
+template <typename T, bool UPPER>
+__host__ __device__ __forceinline__ long long blk_bytes(int w, int cp)
+{
+	long long voff = al16(SW_HDR + (long long)(w + 1) * cp * 4);
+	return al16(voff + (long long)w * cp * (long long)sizeof(T) + (UPPER ? (long long)cp * sizeof(T) : 0));
+}
+
 struct SweepArgs {
 	const unsigned char *prog;
-	const long long *blk_off;     // [nlev+1]
-	const int *lev_pstart;        // [nlev+1] padded start of each level in the input vector
-	int nlev, D, stage_bytes;
+	const long long *blk_off;     // [nsb+1] byte offset of each sub-block
+	const int *sb_in;             // [nsb] padded start of the sub-block's input slice
+	const int *sb_inb;            // [nsb] bytes of that slice
+	int nlev, nsb, D, stage_bytes;
 	int *err;
 	const int *active;
 };
 
-// Issue the copies of level l into stage s (thread 0 only).
-template <typename T>
-__device__ __forceinline__ void issue_level(const SweepArgs &a, const T *in, unsigned char *stages,
-                                            unsigned long long *bar, int l, int s)
-{
-	unsigned char *dst = stages + (size_t)s * a.stage_bytes;
-	long long b0 = a.blk_off[l];
-	unsigned bb = (unsigned)(a.blk_off[l + 1] - b0);
-	int p0 = a.lev_pstart[l];
-	unsigned vb = (unsigned)al16((long long)(a.lev_pstart[l + 1] - p0) * (long long)sizeof(T));
-	mbar_expect_tx(&bar[s], bb + vb);
-	bulk_g2s(dst, a.prog + b0, bb, &bar[s]);
-	if (vb) bulk_g2s(dst + bb, in + p0, vb, &bar[s]);
-}
-
-template <typename T, bool UPPER>
-__global__ void __launch_bounds__(SW_THREADS, 1)
+// CW consumer warps (warps 0..CW-1) and one producer warp (warp CW).
+template <typename T, bool UPPER, int CW, bool FMA>
+__global__ void __launch_bounds__((CW + 1) * 32, 1)
 k_sweep(SweepArgs a, const T *__restrict__ in, T *out)
 {
 	if (a.active && !*a.active) return;
 	extern __shared__ __align__(128) unsigned char sm[];
-	const size_t ring_b = al16((SW_RING + 1) * sizeof(T));
+	const unsigned ring_b = (unsigned)al16((SW_RING + 1) * sizeof(T));
 	T *ring = (T *)sm;
-	unsigned long long *bar = (unsigned long long *)(sm + ring_b);
-	unsigned char *stages = sm + ((ring_b + SW_BAR_BYTES + 127) & ~(size_t)127);
-	__shared__ int failed;
-	const int tid = threadIdx.x, D = a.D;
+	unsigned long long *full = (unsigned long long *)(sm + ring_b);
+	unsigned long long *empty = full + SW_MAXD;
+	unsigned char *stages = sm + ((ring_b + SW_BAR_BYTES + 127) & ~127u);
+	__shared__ int failed, issued, pdone;
+	volatile int *vfailed = &failed;
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, D = a.D;
+	const unsigned sbytes = (unsigned)a.stage_bytes;
 
 	if (tid == 0) {
-		failed = 0;
+		failed = 0; issued = 0; pdone = 0;
 		ring[SW_RING] = T(0);
-		for (int s = 0; s < D; s++) mbar_init(&bar[s], 1);
+		for (int s = 0; s < D; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
 		fence_mbar_init();
-		fence_proxy_async();
-		for (int l = 0; l < D && l < a.nlev; l++) issue_level<T>(a, in, stages, bar, l, l);
 	}
 	__syncthreads();
-	int l = 0;
-	for (; l < a.nlev; l++) {
-		const int s = l % D;
-		if (!mbar_wait(&bar[s], (unsigned)((l / D) & 1))) failed = 1;
-		__syncthreads();
-		if (failed) break;
-		const unsigned char *st = stages + (size_t)s * a.stage_bytes;
-		const LevHdr h = *(const LevHdr *)st;
-		const int *dep = (const int *)(st + 16);
-		const int *outp = dep + h.w * h.cp;
-		const T *val = (const T *)(st + al16(16 + (long long)(h.w + 1) * h.cp * 4));
-		const T *dinv = val + h.w * h.cp;
-		const T *bv = (const T *)(st + (a.blk_off[l + 1] - a.blk_off[l]));
-		for (int r = tid; r < h.c; r += SW_THREADS) {
-			T x = bv[r];
-			for (int k = 0; k < h.w; k++) {
-				unsigned d = (unsigned)dep[k * h.cp + r];
-				T xd = (d & SW_NEAR) ? ring[d & ~SW_NEAR] : __ldcg(&out[d]);
-				x = fms(x, xd, val[k * h.cp + r]);
+
+	if (warp == CW) {                                     // ---- producer warp
+		bool stop = false;
+		int s = 0;
+		unsigned ph = 0;                                  // phase of empty[s] to wait for
+		for (int base = 0; base < a.nsb && !stop; base += 32) {
+			// each lane fetches the offsets of one upcoming sub-block
+			int i = base + lane;
+			long long b0 = 0, b1 = 0;
+			int p0 = 0, vb = 0;
+			if (i < a.nsb) { b0 = a.blk_off[i]; b1 = a.blk_off[i + 1]; p0 = a.sb_in[i]; vb = a.sb_inb[i]; }
+			for (int j = 0; j < 32 && base + j < a.nsb; j++) {
+				long long B0 = __shfl_sync(0xffffffffu, b0, j), B1 = __shfl_sync(0xffffffffu, b1, j);
+				int P0 = __shfl_sync(0xffffffffu, p0, j), VB = __shfl_sync(0xffffffffu, vb, j);
+				int sb = base + j;
+				int go = 1;
+				if (lane == 0) {
+					if (sb >= D && !mbar_wait_or_fail(&empty[s], ph, vfailed)) go = 0;
+					if (*vfailed) go = 0;
+					if (go) {
+						unsigned bb = (unsigned)(B1 - B0);
+						unsigned char *dst = stages + (unsigned)s * sbytes;
+						fence_proxy_async();
+						mbar_expect_tx(&full[s], bb + (unsigned)VB);
+						bulk_g2s(dst, a.prog + B0, bb, &full[s]);
+						if (VB) bulk_g2s(dst + bb, in + P0, (unsigned)VB, &full[s]);
+						*(volatile int *)&issued = sb + 1;
+					}
+				}
+				go = __shfl_sync(0xffffffffu, go, 0);
+				if (!go) { stop = true; break; }
+				if (++s == D) { s = 0; if (sb >= D) ph ^= 1u; else if (sb == D - 1) ph = 0; }
 			}
-			if (UPPER) x = mul(x, dinv[r]);
-			ring[(h.start + r) & (SW_RING - 1)] = x;
-			out[outp[r]] = x;
 		}
-		__syncthreads();
-		if (tid == 0 && l + D < a.nlev) {
-			fence_proxy_async();
-			issue_level<T>(a, in, stages, bar, l + D, s);
-		}
+		if (lane == 0) *(volatile int *)&pdone = 1;
+		return;
 	}
-	if (failed && tid == 0) {
+
+	const int ctid = tid;                                 // ---- consumer warps
+	int sb = 0, s = 0;
+	unsigned ph = 0;                                      // phase of full[s] to wait for
+	for (int l = 0; l < a.nlev; l++) {
+		int nsub = 1, j = 0, s0 = s;
+		for (; j < nsub; j++) {
+			bool ok = mbar_wait_or_fail(&full[s], ph, vfailed);
+			if (!ok) { *vfailed = 1; break; }
+			const unsigned char *st = stages + (unsigned)s * sbytes;
+			const LevHdr h = *(const LevHdr *)st;
+			if (j == 0) nsub = h.nsub;
+			const int *dep = (const int *)(st + SW_HDR);
+			const int *outp = dep + h.w * h.cp;
+			const T *val = (const T *)(st + h.voff);
+			const T *dinv = val + h.w * h.cp;
+			const T *bv = (const T *)(st + h.boff);
+			if (!h.hasfar) {
+				// every dependency is in the ring
+				for (int r = ctid; r < h.c; r += CW * 32) {
+					T x = bv[r];
+					for (int k = 0; k < h.w; k++)
+						x = fmsub<T, FMA>(x, ring[(unsigned)dep[k * h.cp + r] & ~SW_NEAR], val[k * h.cp + r]);
+					if (UPPER) x = mul(x, dinv[r]);
+					ring[(h.start + r) & (SW_RING - 1)] = x;
+					out[outp[r]] = x;
+				}
+			} else {
+				for (int r = ctid; r < h.c; r += CW * 32) {
+					T x = bv[r];
+					for (int k = 0; k < h.w; k++) {
+						unsigned d = (unsigned)dep[k * h.cp + r];
+						T xd = (d & SW_NEAR) ? ring[d & ~SW_NEAR] : __ldcg(&out[d]);
+						x = fmsub<T, FMA>(x, xd, val[k * h.cp + r]);
+					}
+					if (UPPER) x = mul(x, dinv[r]);
+					ring[(h.start + r) & (SW_RING - 1)] = x;
+					out[outp[r]] = x;
+				}
+			}
+			if (++s == D) { s = 0; ph ^= 1u; }
+		}
+		consumer_sync<CW>();
+		// every consumer is done with the level's stages: release them
+		if (ctid == 0) {
+			int q = s0;
+			for (int c = 0; c < j; c++) { mbar_arrive(&empty[q]); if (++q == D) q = 0; }
+		}
+		sb += j;
+		if (*vfailed) break;
+	}
+	if (*vfailed && ctid == 0) {
 		fg_set_err(a.err, FEMGPU_E_TIMEOUT);
-		// copies in flight: levels l .. l+D-1 (bounded waits)
-		for (int q = l; q < l + D && q < a.nlev; q++) (void)mbar_wait(&bar[q % D], (unsigned)((q / D) & 1));
+		// let the producer stop, then wait (bounded) for the copies it issued
+		for (int i = 0; i < SW_WAIT_LIMIT && !*(volatile int *)&pdone; i++) __nanosleep(64);
+		int last = *(volatile int *)&issued;
+		for (int q = sb; q < last; q++) (void)mbar_wait(&full[q % D], (unsigned)((q / D) & 1));
 	}
 }
 
@@ -206,41 +303,38 @@ __global__ void k_refresh(unsigned char *prog, const long long *val_off, const i
 // ---------------------------------------------------------- factor ------
 // IKJ ILU(0) in level order in one block: rows of a level in parallel, one
 // __syncthreads per level; U parts and pivots of earlier levels were written
-// by this block before a barrier, so plain loads see them.
+// by this block before a barrier, so plain loads see them.  The elimination
+// structure of each row is precompiled (fac_prog): [dpos, ngroups] then per
+// lower entry, in ascending column order, [q, jrow, cnt, (dst, src) x cnt]
+// -- dst the position in row r updated by U(jrow, src) (-1: the pivot) --
+// so a row needs no pattern searches, only independent loads.
 #define FAC_CAP 32
-__global__ void __launch_bounds__(SW_THREADS, 1)
-k_ilu0_factor_cta(const int *__restrict__ IA, const int *__restrict__ JA, const double *__restrict__ AA,
+__global__ void __launch_bounds__(FAC_THREADS, 1)
+k_ilu0_factor_cta(const int *__restrict__ IA, const double *__restrict__ AA,
                   const int *__restrict__ rows, const int *__restrict__ lev_start, int nlev,
+                  const int *__restrict__ fac_ptr, const int *__restrict__ fac_prog,
                   double *LU, double *Dinv, int *err)
 {
 	for (int l = 0; l < nlev; l++) {
 		int b = lev_start[l], e = lev_start[l + 1];
-		for (int q0 = b + threadIdx.x; q0 < e; q0 += SW_THREADS) {
-			int r = rows[q0];
+		for (int p = b + threadIdx.x; p < e; p += FAC_THREADS) {
+			int r = rows[p];
 			int rb = IA[r], len = IA[r + 1] - rb;
-			if (len > FAC_CAP) { fg_set_err(err, FEMGPU_E_MESH); continue; }
-			int cols[FAC_CAP];
 			double vals[FAC_CAP];
-			int dpos = -1;
-			for (int q = 0; q < len; q++) {
-				cols[q] = JA[rb + q];
-				vals[q] = AA[rb + q];
-				if (cols[q] == r) dpos = q;
-			}
-			double d = (dpos >= 0) ? vals[dpos] : 0.0;
-			for (int q = 0; q < len && cols[q] < r; q++) {
-				int jrow = cols[q];
-				vals[q] = __dmul_rn(vals[q], Dinv[jrow]);
-				int kb = IA[jrow], ke = IA[jrow + 1];
-				for (int k = kb; k < ke; k++) {
-					int col = JA[k];
-					if (col <= jrow) continue;
-					int pos = -1;
-					for (int m = 0; m < len; m++) if (cols[m] == col) { pos = m; break; }
-					if (pos < 0) continue;
-					double prod = __dmul_rn(vals[q], LU[k]);
-					if (col == r) d = __dsub_rn(d, prod);
-					else vals[pos] = __dsub_rn(vals[pos], prod);
+			for (int q = 0; q < len; q++) vals[q] = AA[rb + q];
+			const int *pr = fac_prog + fac_ptr[p];
+			int dpos = pr[0], ng = pr[1];
+			pr += 2;
+			double d = vals[dpos];
+			for (int g = 0; g < ng; g++) {
+				int q = pr[0], jrow = pr[1], cnt = pr[2];
+				pr += 3;
+				double lq = __dmul_rn(vals[q], Dinv[jrow]);
+				vals[q] = lq;
+				for (int c = 0; c < cnt; c++, pr += 2) {
+					double prod = __dmul_rn(lq, LU[pr[1]]);
+					if (pr[0] < 0) d = __dsub_rn(d, prod);
+					else vals[pr[0]] = __dsub_rn(vals[pr[0]], prod);
 				}
 			}
 			for (int q = 0; q < len; q++) LU[rb + q] = (q == dpos) ? d : vals[q];
@@ -308,40 +402,65 @@ static int up_vec(X **d, const std::vector<X> &h)
 // One sweep program.  Forward (lower): L part, outputs to the backward
 // sweep's padded level order (target = the U levels' ppos).  Backward: U part
 // and pivots, outputs in natural order.
-static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, bool lower,
-                      const HostLevels *target, size_t tsize, fg_sweep &sw)
+template <typename T, bool UPPER>
+static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, const HostLevels *target,
+                      fg_sweep &sw)
 {
+	const bool lower = !UPPER;
+	const long long tsize = sizeof(T);
 	int nlev = H.nlev;
-	std::vector<long long> off(nlev + 1, 0);
-	std::vector<int> width(nlev, 0);
-	long long maxblk = 0;
+	// sub-blocks: (level, first row within the level, rows, width)
+	struct Sub { int l, j0, c, w; };
+	std::vector<Sub> subs;
+	subs.reserve(nlev + 16);
 	for (int l = 0; l < nlev; l++) {
-		int c = H.start[l + 1] - H.start[l], w = 0;
-		for (int p = H.start[l]; p < H.start[l + 1]; p++) {
-			int r = H.rows[p], cnt = 0;
-			for (int k = IA[r]; k < IA[r + 1]; k++) if (lower ? JA[k] < r : JA[k] > r) cnt++;
-			w = std::max(w, cnt);
+		int c = H.start[l + 1] - H.start[l];
+		for (int j0 = 0; j0 < c; j0 += SW_SUB) {
+			int cc = std::min(SW_SUB, c - j0), w = 0;
+			for (int p = H.start[l] + j0; p < H.start[l] + j0 + cc; p++) {
+				int r = H.rows[p], cnt = 0;
+				for (int k = IA[r]; k < IA[r + 1]; k++) if (lower ? JA[k] < r : JA[k] > r) cnt++;
+				w = std::max(w, cnt);
+			}
+			subs.push_back({ l, j0, cc, w });
 		}
-		width[l] = w;
-		int cp = (c + 3) & ~3;
-		long long sz = al16(16 + (long long)(w + 1) * cp * 4) + (long long)w * cp * (long long)tsize
-		               + (lower ? 0 : (long long)cp * (long long)tsize);
-		off[l + 1] = off[l] + al16(sz);
-		maxblk = std::max(maxblk, al16(sz) + al16((long long)cp * (long long)tsize));
 	}
-	std::vector<unsigned char> prog((size_t)off[nlev] + 16, 0);
+	int nsb = (int)subs.size();
+	std::vector<long long> off(nsb + 1, 0);
+	std::vector<int> sb_in(nsb), sb_inb(nsb);
+	long long maxblk = 0;
+	for (int i = 0; i < nsb; i++) {
+		int cp = (subs[i].c + 3) & ~3;
+		long long bb = blk_bytes<T, UPPER>(subs[i].w, cp);
+		off[i + 1] = off[i] + bb;
+		sb_in[i] = H.pstart[subs[i].l] + subs[i].j0;                 // j0 is a multiple of 4
+		sb_inb[i] = (int)al16((long long)cp * tsize);
+		maxblk = std::max(maxblk, bb + sb_inb[i]);
+	}
+	std::vector<unsigned char> prog((size_t)off[nsb] + 16, 0);
 	std::vector<long long> val_off;
 	std::vector<int> val_src;
 	val_off.reserve((size_t)IA[n] + n);
 	val_src.reserve((size_t)IA[n] + n);
-	for (int l = 0; l < nlev; l++) {
-		int c = H.start[l + 1] - H.start[l], w = width[l], cp = (c + 3) & ~3, start = H.start[l];
+	for (int i = 0; i < nsb; i++) {
+		const Sub &S = subs[i];
+		int l = S.l, c = S.c, w = S.w, cp = (c + 3) & ~3, start = H.start[l] + S.j0;
 		int end = H.start[l + 1];
-		unsigned char *b = prog.data() + off[l];
-		LevHdr h = { c, w, start, cp };
+		int nsub = (H.start[l + 1] - H.start[l] + SW_SUB - 1) / SW_SUB;
+		unsigned char *b = prog.data() + off[i];
+		int hasfar = 0;
+		for (int j = 0; j < c; j++) {
+			int r = H.rows[start + j];
+			for (int q = IA[r]; q < IA[r + 1]; q++) {
+				int col = JA[q];
+				if ((lower ? col < r : col > r) && end - H.pos[col] > SW_RING) hasfar = 1;
+			}
+		}
+		LevHdr h = { c, w, start, cp, nsub, hasfar, (int)al16(SW_HDR + (long long)(w + 1) * cp * 4),
+		             (int)blk_bytes<T, UPPER>(w, cp) };
 		memcpy(b, &h, sizeof h);
-		int *dep = (int *)(b + 16), *outp = dep + (size_t)w * cp;
-		long long voff = al16(16 + (long long)(w + 1) * cp * 4);
+		int *dep = (int *)(b + SW_HDR), *outp = dep + (size_t)w * cp;
+		long long voff = al16(SW_HDR + (long long)(w + 1) * cp * 4);
 		for (int k = 0; k < w * cp; k++) dep[k] = (int)(SW_NEAR | SW_RING);       // the zero slot
 		for (int j = 0; j < c; j++) {
 			int r = H.rows[start + j], k = 0;
@@ -353,22 +472,23 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 				unsigned code = (end - p <= SW_RING) ? (SW_NEAR | (unsigned)(p & (SW_RING - 1)))
 				                                     : (unsigned)(lower ? target->ppos[col] : col);
 				dep[(size_t)k * cp + j] = (int)code;
-				val_off.push_back(off[l] + voff + ((long long)k * cp + j) * (long long)tsize);
+				val_off.push_back(off[i] + voff + ((long long)k * cp + j) * tsize);
 				val_src.push_back(q);
 				k++;
 			}
 			for (; k < w; k++) {
-				val_off.push_back(off[l] + voff + ((long long)k * cp + j) * (long long)tsize);
+				val_off.push_back(off[i] + voff + ((long long)k * cp + j) * tsize);
 				val_src.push_back(-1);
 			}
 			if (!lower) {
-				val_off.push_back(off[l] + voff + ((long long)w * cp + j) * (long long)tsize);
+				val_off.push_back(off[i] + voff + ((long long)w * cp + j) * tsize);
 				val_src.push_back(-2 - r);
 			}
 		}
 	}
 	sw.nlev = nlev;
-	sw.bytes = off[nlev];
+	sw.nsb = nsb;
+	sw.bytes = off[nsb];
 	sw.maxblk = maxblk;
 	sw.nval = (long long)val_off.size();
 	sw.npad = H.pstart[nlev];
@@ -376,8 +496,9 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 	FG_TRY(cudaMalloc((void **)&sw.prog, prog.size()));
 	FG_TRY(cudaMemcpy(sw.prog, prog.data(), prog.size(), cudaMemcpyHostToDevice));
 	if ((rc = up_vec(&sw.blk_off, off))) return rc;
+	if ((rc = up_vec(&sw.sb_in, sb_in))) return rc;
+	if ((rc = up_vec(&sw.sb_inb, sb_inb))) return rc;
 	if ((rc = up_vec(&sw.lev_start, H.start))) return rc;
-	if ((rc = up_vec(&sw.lev_pstart, H.pstart))) return rc;
 	if ((rc = up_vec(&sw.rows, H.rows))) return rc;
 	std::vector<int> ppos_by_pos(n);
 	for (int p = 0; p < n; p++) ppos_by_pos[p] = H.ppos[H.rows[p]];
@@ -387,13 +508,97 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 	return 0;
 }
 
+// Elimination program of every row, in forward level order (the layout
+// k_ilu0_factor_cta reads): the same sequence of updates as
+// ILUp_precond_setup.c:119-139, resolved against the pattern once.
+static int build_factor_prog(const int *IA, const int *JA, int n, const HostLevels &Lo, fg_ilu_sweeps &S)
+{
+	std::vector<int> ptr(n + 1, 0), prog;
+	prog.reserve((size_t)n * 24);
+	for (int p = 0; p < n; p++) {
+		int r = Lo.rows[p], rb = IA[r], len = IA[r + 1] - rb, dpos = -1, ng = 0;
+		if (len > FAC_CAP) return FEMGPU_E_MESH;
+		for (int q = 0; q < len; q++) if (JA[rb + q] == r) dpos = q;
+		if (dpos < 0) return FEMGPU_E_ZERO_PIVOT;           // no diagonal entry
+		ptr[p] = (int)prog.size();
+		size_t hdr = prog.size();
+		prog.push_back(dpos);
+		prog.push_back(0);
+		for (int q = 0; q < len && JA[rb + q] < r; q++) {
+			int jrow = JA[rb + q], cnt = 0;
+			size_t g = prog.size();
+			prog.push_back(q);
+			prog.push_back(jrow);
+			prog.push_back(0);
+			for (int k = IA[jrow]; k < IA[jrow + 1]; k++) {
+				int col = JA[k], pos = -1;
+				if (col <= jrow) continue;
+				for (int m = 0; m < len; m++) if (JA[rb + m] == col) { pos = m; break; }
+				if (pos < 0) continue;
+				prog.push_back(col == r ? -1 : pos);
+				prog.push_back(k);
+				cnt++;
+			}
+			prog[g + 2] = cnt;
+			ng++;
+		}
+		prog[hdr + 1] = ng;
+	}
+	ptr[n] = (int)prog.size();
+	int rc;
+	if ((rc = up_vec(&S.fac_ptr, ptr))) return rc;
+	return up_vec(&S.fac_prog, prog);
+}
+
+#define SW_SET(T, U, CW, F) FG_TRY(cudaFuncSetAttribute(k_sweep<T, U, CW, F>, \
+	cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP))
+#define SW_SET_CW(CW) SW_SET(double, false, CW, false); SW_SET(double, true, CW, false); \
+	SW_SET(double, false, CW, true); SW_SET(double, true, CW, true); \
+	SW_SET(float, false, CW, false); SW_SET(float, true, CW, false)
+static int sweep_attrs(void)
+{
+	SW_SET_CW(4);
+	SW_SET_CW(8);
+	SW_SET_CW(16);
+	return 0;
+}
+
+// Consumer warps per sweep (4, 8 or 16; FEMGPU_SWEEP_WARPS overrides).
+static int sweep_cw(void)
+{
+	static int cw = 0;
+	if (!cw) {
+		const char *e = getenv("FEMGPU_SWEEP_WARPS");
+		int v = e ? atoi(e) : 16;
+		cw = (v == 4 || v == 8 || v == 16) ? v : 16;
+	}
+	return cw;
+}
+
+// fma: fused multiply-subtract in the FP64 sweeps (the FGMRES solves); the
+// separately rounded form reproduces the reference bit for bit.
+template <typename T, bool UPPER>
+static void launch_sweep(const SweepArgs &a, int bytes, cudaStream_t s, const T *in, T *out, bool fma)
+{
+	int cw = sweep_cw();
+	if (fma && sizeof(T) == 8) {
+		if (cw == 4) k_sweep<T, UPPER, 4, true><<<1, 160, bytes, s>>>(a, in, out);
+		else if (cw == 8) k_sweep<T, UPPER, 8, true><<<1, 288, bytes, s>>>(a, in, out);
+		else k_sweep<T, UPPER, 16, true><<<1, 544, bytes, s>>>(a, in, out);
+	} else {
+		if (cw == 4) k_sweep<T, UPPER, 4, false><<<1, 160, bytes, s>>>(a, in, out);
+		else if (cw == 8) k_sweep<T, UPPER, 8, false><<<1, 288, bytes, s>>>(a, in, out);
+		else k_sweep<T, UPPER, 16, false><<<1, 544, bytes, s>>>(a, in, out);
+	}
+}
+
 static int sweep_smem(const fg_sweep &sw, size_t tsize, int *D, int *stage_bytes)
 {
 	size_t fixed = ((al16((SW_RING + 1) * tsize) + SW_BAR_BYTES + 127) & ~(size_t)127);
 	size_t sb = (size_t)((sw.maxblk + 127) & ~127LL);
-	if (fixed + 2 * sb > SW_SMEM_CAP) return FEMGPU_E_MESH;   // a level too wide to stage
+	if (fixed + 2 * sb > SW_SMEM_CAP) return FEMGPU_E_MESH;   // a sub-block too wide to stage
 	int d = (int)((SW_SMEM_CAP - fixed) / sb);
-	if (d > 6) d = 6;
+	if (d > SW_MAXD) d = SW_MAXD;
 	*D = d;
 	*stage_bytes = (int)sb;
 	return (int)(fixed + (size_t)d * sb);
@@ -404,10 +609,11 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 	int n = t->neq, rc, D, sb;
 	fg_ilu_sweeps &S = t->sweeps;
 	HostLevels Lo = host_levels(hIA, hJA, n, true), Up = host_levels(hIA, hJA, n, false);
-	if ((rc = build_prog(hIA, hJA, n, Up, false, nullptr, sizeof(double), S.up64))) return rc;
-	if ((rc = build_prog(hIA, hJA, n, Lo, true, &Up, sizeof(double), S.lo64))) return rc;
-	if ((rc = build_prog(hIA, hJA, n, Up, false, nullptr, sizeof(float), S.up32))) return rc;
-	if ((rc = build_prog(hIA, hJA, n, Lo, true, &Up, sizeof(float), S.lo32))) return rc;
+	if ((rc = build_prog<double, true>(hIA, hJA, n, Up, nullptr, S.up64))) return rc;
+	if ((rc = build_prog<double, false>(hIA, hJA, n, Lo, &Up, S.lo64))) return rc;
+	if ((rc = build_prog<float, true>(hIA, hJA, n, Up, nullptr, S.up32))) return rc;
+	if ((rc = build_prog<float, false>(hIA, hJA, n, Lo, &Up, S.lo32))) return rc;
+	if ((rc = build_factor_prog(hIA, hJA, n, Lo, S))) return rc;
 	size_t nb = (size_t)std::max(Lo.pstart[Lo.nlev], Up.pstart[Up.nlev]) + 64;
 	FG_TRY(cudaMalloc((void **)&S.bl64, sizeof(double) * nb));
 	FG_TRY(cudaMalloc((void **)&S.y64, sizeof(double) * nb));
@@ -422,19 +628,15 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 		rc = sweep_smem(*all[i], i < 2 ? sizeof(double) : sizeof(float), &D, &sb);
 		if (rc < 0) return rc;
 	}
-	FG_TRY(cudaFuncSetAttribute(k_sweep<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP));
-	FG_TRY(cudaFuncSetAttribute(k_sweep<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP));
-	FG_TRY(cudaFuncSetAttribute(k_sweep<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP));
-	FG_TRY(cudaFuncSetAttribute(k_sweep<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP));
-	return 0;
+	return sweep_attrs();
 }
 
 extern "C" int fg_ilu0_factor(femgpu_transport *t)
 {
 	cudaStream_t s = t->stream;
 	fg_ilu_sweeps &S = t->sweeps;
-	k_ilu0_factor_cta<<<1, SW_THREADS, 0, s>>>(t->IA, t->JA, t->A, S.lo64.rows, S.lo64.lev_start, S.lo64.nlev,
-	                                           t->ilu.LU, t->ilu.Dinv, &t->st->err);
+	k_ilu0_factor_cta<<<1, FAC_THREADS, 0, s>>>(t->IA, t->A, S.lo64.rows, S.lo64.lev_start, S.lo64.nlev,
+	                                            S.fac_ptr, S.fac_prog, t->ilu.LU, t->ilu.Dinv, &t->st->err);
 	fg_sweep *pr[4] = { &S.lo64, &S.up64, &S.lo32, &S.up32 };
 	for (int i = 0; i < 4; i++) {
 		int g = fg_grid(pr[i]->nval);
@@ -448,7 +650,7 @@ extern "C" int fg_ilu0_factor(femgpu_transport *t)
 
 template <typename T, typename TI, typename TO>
 static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, T *bl, T *y,
-                   const TI *p, TO *z, const int *active)
+                   const TI *p, TO *z, const int *active, bool fma)
 {
 	cudaStream_t s = t->stream;
 	int n = t->neq, D, sb, bytes;
@@ -458,27 +660,28 @@ static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, 
 	a.active = active;
 	bytes = sweep_smem(lo, sizeof(T), &D, &sb);
 	if (bytes < 0) return bytes;
-	a.prog = lo.prog; a.blk_off = lo.blk_off; a.lev_pstart = lo.lev_pstart; a.nlev = lo.nlev;
-	a.D = D; a.stage_bytes = sb;
-	k_sweep<T, false><<<1, SW_THREADS, bytes, s>>>(a, bl, y);
+	a.prog = lo.prog; a.blk_off = lo.blk_off; a.sb_in = lo.sb_in; a.sb_inb = lo.sb_inb;
+	a.nlev = lo.nlev; a.nsb = lo.nsb; a.D = D; a.stage_bytes = sb;
+	launch_sweep<T, false>(a, bytes, s, bl, y, fma);
 	bytes = sweep_smem(up, sizeof(T), &D, &sb);
 	if (bytes < 0) return bytes;
-	a.prog = up.prog; a.blk_off = up.blk_off; a.lev_pstart = up.lev_pstart; a.nlev = up.nlev;
-	a.D = D; a.stage_bytes = sb;
-	k_sweep<T, true><<<1, SW_THREADS, bytes, s>>>(a, y, (T *)z);
+	a.prog = up.prog; a.blk_off = up.blk_off; a.sb_in = up.sb_in; a.sb_inb = up.sb_inb;
+	a.nlev = up.nlev; a.nsb = up.nsb; a.D = D; a.stage_bytes = sb;
+	launch_sweep<T, true>(a, bytes, s, y, (T *)z, fma);
 	return (int)cudaGetLastError();
 }
 
 extern "C" int fg_ilu0_apply64(femgpu_transport *t, const double *p, double *z, const int *active)
 {
 	fg_ilu_sweeps &S = t->sweeps;
-	return apply_t<double, double, double>(t, S.lo64, S.up64, S.bl64, S.y64, p, z, active);
+	return apply_t<double, double, double>(t, S.lo64, S.up64, S.bl64, S.y64, p, z, active,
+	                                       t->o.solver == FEMGPU_FGMRES);
 }
 
 extern "C" int fg_ilu0_apply32(femgpu_transport *t, const double *p, float *z, const int *active)
 {
 	fg_ilu_sweeps &S = t->sweeps;
-	return apply_t<float, double, float>(t, S.lo32, S.up32, S.bl32, S.y32, p, z, active);
+	return apply_t<float, double, float>(t, S.lo32, S.up32, S.bl32, S.y32, p, z, active, false);
 }
 
 extern "C" void fg_ilu_free(femgpu_transport *t)
@@ -486,10 +689,10 @@ extern "C" void fg_ilu_free(femgpu_transport *t)
 	fg_ilu_sweeps &S = t->sweeps;
 	fg_sweep *all[4] = { &S.lo64, &S.up64, &S.lo32, &S.up32 };
 	for (int i = 0; i < 4; i++) {
-		void *p[] = { all[i]->prog, all[i]->blk_off, all[i]->lev_start, all[i]->lev_pstart, all[i]->rows,
-		              all[i]->ppos, all[i]->val_off, all[i]->val_src };
+		void *p[] = { all[i]->prog, all[i]->blk_off, all[i]->sb_in, all[i]->sb_inb, all[i]->lev_start,
+		              all[i]->rows, all[i]->ppos, all[i]->val_off, all[i]->val_src };
 		for (void *q : p) if (q) cudaFree(q);
 	}
-	void *v[] = { S.bl64, S.y64, S.bl32, S.y32 };
+	void *v[] = { S.bl64, S.y64, S.bl32, S.y32, S.fac_ptr, S.fac_prog };
 	for (void *q : v) if (q) cudaFree(q);
 }
