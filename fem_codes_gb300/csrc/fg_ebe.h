@@ -1,0 +1,34 @@
+/* State of a multi-dof element-by-element operator (Euler ndof 4, Navier-
+ * Stokes ndof 3).  Plain C; shared by ebe_block.cu and host/ebe.c.
+ * Device layout: lm [nel*m] (m = 3*ndof), element matrices A [nel*m*m]
+ * row-major as the reference stores them, dof-row incidence lists ri
+ * (code e*m + a, ascending e), node incidence lists ni (code e*3 + a),
+ * nodal blocks BD / invBD [nnodes*ndof*ndof]. */
+#ifndef FG_EBE_H
+#define FG_EBE_H
+#include <cuda_runtime_api.h>
+#include "femgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+struct femgpu_ebe {
+	int ndof, m, nnodes, nel, neq;
+	cudaStream_t stream, own_stream;
+	int *vert, *node_id, *lm;
+	int *ri_ptr, *ri, *ni_ptr, *ni;
+	double *A, *BD, *invBD;
+	double *P, *Q;          /* scratch for the host-buffer entry points */
+	int have_bd;
+};
+
+int fg_ebe_lm(femgpu_ebe *c);
+int fg_ebe_matvec(femgpu_ebe *c, const double *P, double *Q, int offdiag);
+int fg_ebe_blockdiag_setup(femgpu_ebe *c);
+int fg_ebe_blockdiag_apply(femgpu_ebe *c, const double *p, double *z, int mode);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -169,6 +169,40 @@ int femgpu_transport_true_residual(femgpu_transport *ctx, double *relres);
  * t[0] build, t[1] precond_setup, t[2] solve. */
 int femgpu_transport_last_times(const femgpu_transport *ctx, float *t);
 
+/* ---- multi-dof element-by-element operators ------------------------------
+ * The Euler (ndof 4: rho, rho u, rho v, rho E; 12x12 element blocks) and
+ * steady Navier-Stokes (ndof 3: u, v, p; 9x9) storage of
+ * 03_Euler_Equations/2D/01_CommonFiles/EulerEquations.h:87-126 and
+ * 04_SS_NavierStokes_Equations/2D/01_CommonFiles/SSNavierStokesEquations.h.
+ * node_id [nnodes*ndof]: Node[].id[] of Fill_ID.c (-1 prescribed), so
+ * lm[e][ndof*a+k] follows Fill_LM.c (neq for prescribed).  Element matrices
+ * A [nel*(3ndof)^2] row-major, the reference's A[e][...] layout. */
+typedef struct femgpu_ebe femgpu_ebe;
+int femgpu_ebe_create(femgpu_ebe **ctx, int ndof, int nnodes, int nel, const int *vert,
+		const int *node_id, int neq);
+void femgpu_ebe_destroy(femgpu_ebe *ctx);
+int femgpu_ebe_set_stream(femgpu_ebe *ctx, void *stream);
+/* Upload element matrices from host memory (the device copy is also
+ * reachable through femgpu_ebe_A_dev for matrices built on the device). */
+int femgpu_ebe_set_matrix(femgpu_ebe *ctx, const double *A_host);
+double *femgpu_ebe_A_dev(femgpu_ebe *ctx);
+/* ebemvNDOF4 (EBE/ebemvNDOF4.c:3-112) / ebemvNDOF3 (EBE/ebemvNDOF3.c:3-86):
+ * Q = A P; P[neq] read as 0, Q[neq] = 0. */
+int femgpu_ebe_matvec(femgpu_ebe *ctx, const double *P_host, double *Q_host);
+int femgpu_ebe_matvec_dev(femgpu_ebe *ctx, const double *P, double *Q);
+/* ebe2mvNDOF4 (EBE/ebe2mvNDOF4.c:4-79, ndof 4): off-diagonal node blocks of
+ * every element, then with_inverse ? Q = P + D^-1 Q (BlockDiag2_precond.c)
+ * : Q += D P (NOBlockDiag2_precond.c).  Needs femgpu_ebe_blockdiag_setup. */
+int femgpu_ebe_matvec2(femgpu_ebe *ctx, const double *P_host, double *Q_host, int with_inverse);
+int femgpu_ebe_matvec2_dev(femgpu_ebe *ctx, const double *P, double *Q, int with_inverse);
+/* BlockDiag_precond_EBE_setup.c:6-86 / BlockDiagDOF3_precond_EBE_setup.c:
+ * nodal diagonal blocks D, their inverses, then F := D^-1 F (F_host may be
+ * NULL).  BD_host / invBD_host [nnodes*ndof^2] receive the blocks (NULL skips). */
+int femgpu_ebe_blockdiag_setup(femgpu_ebe *ctx, double *F_host, double *BD_host, double *invBD_host);
+/* BlockDiag_precond.c / BlockDiagDOF3_precond.c: z = D^-1 p; p may equal z. */
+int femgpu_ebe_blockdiag_apply(femgpu_ebe *ctx, const double *p_host, double *z_host);
+int femgpu_ebe_blockdiag_apply_dev(femgpu_ebe *ctx, const double *p, double *z);
+
 /* ---- stateless device kernels (device pointers, stream as void*) -------- */
 /* csrmv.c:3-24 in FP64 / FP32 values. */
 int femgpu_csrmv_f64(int n, const int *IA, const int *JA, const double *AA,

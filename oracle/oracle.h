@@ -102,6 +102,19 @@ void orc_get_step_times(double *t, int n);
 int orc_csr_gmres(int neq, const int *IA, const int *JA, const double *AA, int use_ilu0,
                   int kmax, int lmax, double tol, double *B, double *X);
 
+/* ---- multi-dof EBE operators (Euler ndof 4, Navier-Stokes ndof 3) ------- */
+void orc_fill_lm_blk(int ndof, int nel, const int *vert, const int *node_id, int neq, int *lm);
+void orc_ebemv_blk(int ndof, int neq, int nel, const int *lm, const double *A, double *P, double *Q);
+void orc_blockdiag_assemble(int ndof, int nnodes, int nel, const int *vert, const double *A, double *BD);
+void orc_inverse4(const double *B, double *V);
+void orc_inverse3(const double *B, double *V);
+void orc_blockdiag_apply(int ndof, int nnodes, int neq, const int *node_id, const double *invBD,
+                         const double *p, double *z);
+void orc_blockdiag_setup(int ndof, int nnodes, int nel, int neq, const int *vert, const int *node_id,
+                         const double *A, double *BD, double *invBD, double *F);
+void orc_ebe2mv4(int nnodes, int neq, int nel, const int *lm, const int *node_id, const double *A,
+                 const double *BD, const double *invBD, int with_inverse, double *P, double *Q);
+
 #ifdef __cplusplus
 }
 #endif

@@ -128,6 +128,53 @@ def run_transport(x, y, node_type, vert, k, gamma, beta, fsrc, upresc, scheme="C
     return out
 
 
+def _blk_lib():
+    L = lib()
+    if not hasattr(L, "_blk_ready"):
+        L.orc_fill_lm_blk.restype = None
+        L.orc_fill_lm_blk.argtypes = [ctypes.c_int, ctypes.c_int, _ip, _ip, ctypes.c_int, _ip]
+        L.orc_ebemv_blk.restype = None
+        L.orc_ebemv_blk.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _dp, _dp, _dp]
+        L.orc_blockdiag_setup.restype = None
+        L.orc_blockdiag_setup.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _ip,
+                                          _dp, _dp, _dp, ctypes.c_void_p]
+        L.orc_blockdiag_apply.restype = None
+        L.orc_blockdiag_apply.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _dp, _dp, _dp]
+        L.orc_ebe2mv4.restype = None
+        L.orc_ebe2mv4.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _ip, _ip, _dp, _dp, _dp,
+                                  ctypes.c_int, _dp, _dp]
+        L._blk_ready = True
+    return L
+
+
+def block_ops(ndof, nnodes, vert, node_id, neq, A, P, p, F):
+    """Every multi-dof EBE operator of the oracle on one input set."""
+    L = _blk_lib()
+    vert = _c(vert, np.int32).reshape(-1)
+    node_id = _c(node_id, np.int32).reshape(-1)
+    nel = vert.size // 3
+    m = 3 * ndof
+    A = _c(A, np.float64).reshape(-1)
+    lm = np.zeros(nel * m, np.int32)
+    L.orc_fill_lm_blk(ndof, nel, vert, node_id, neq, lm)
+    Q = np.zeros(neq + 1)
+    L.orc_ebemv_blk(ndof, neq, nel, lm, A, np.array(P, dtype=np.float64), Q)
+    d2 = ndof * ndof
+    BD = np.zeros(nnodes * d2)
+    invBD = np.zeros(nnodes * d2)
+    Fo = np.array(F, dtype=np.float64)
+    L.orc_blockdiag_setup(ndof, nnodes, nel, neq, vert, node_id, A, BD, invBD, Fo.ctypes.data)
+    Z = np.array(p, dtype=np.float64)
+    L.orc_blockdiag_apply(ndof, nnodes, neq, node_id, invBD, np.array(p, dtype=np.float64), Z)
+    out = dict(lm=lm.reshape(nel, m), Q=Q, BD=BD.reshape(nnodes, d2), invBD=invBD.reshape(nnodes, d2), F=Fo, Z=Z)
+    if ndof == 4:
+        for key, inv in (("Q2", 1), ("Q2no", 0)):
+            Qx = np.zeros(neq + 1)
+            L.orc_ebe2mv4(nnodes, neq, nel, lm, node_id, A, BD, invBD, inv, np.array(P, dtype=np.float64), Qx)
+            out[key] = Qx
+    return out
+
+
 def last_times(npicard=0):
     """(phase times [setup, build, precond_setup, solve], per-step times) of
     the last run_transport, in seconds."""

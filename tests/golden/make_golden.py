@@ -130,7 +130,72 @@ CASES = {
 }
 
 
+def block_node_ids(mesh, ndof, seed):
+    """Node numbering of Fill_ID.c (03_Euler_Equations/2D): dofs numbered node
+    by node; inflow (x = 0) nodes have every dof prescribed, wall (y = 0) nodes
+    their normal velocity (dof 2), a few random interior dofs are prescribed
+    too so that mixed nodes occur."""
+    rng = np.random.default_rng(seed)
+    presc = np.zeros((mesh.nnodes, ndof), bool)
+    presc[mesh.x == 0.0, :] = True
+    presc[mesh.y == 0.0, 2 % ndof] = True
+    presc |= rng.random((mesh.nnodes, ndof)) < 0.03
+    node_id = np.full((mesh.nnodes, ndof), -1, np.int32)
+    neq = 0
+    for i in range(mesh.nnodes):
+        for k in range(ndof):
+            if not presc[i, k]:
+                node_id[i, k] = neq
+                neq += 1
+    return node_id, neq
+
+
+def run_ref_block(ndof, mesh, seed):
+    name = "libfemref_euler_blk.so" if ndof == 4 else "libfemref_ns_blk.so"
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", name))
+    f = lib.ref_block_run
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int, ctypes.c_int, _ip, _ip, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp,
+                  _dp, _dp, _dp, _dp]
+    node_id, neq = block_node_ids(mesh, ndof, seed)
+    m = 3 * ndof
+    rng = np.random.default_rng(seed + 1)
+    # diagonally weighted random element matrices keep the nodal blocks invertible
+    A = rng.uniform(-1.0, 1.0, (mesh.nel, m, m)) + np.eye(m)[None] * 4.0
+    P = rng.uniform(-1.0, 1.0, neq + 1)
+    P[neq] = 0.0
+    p = rng.uniform(-1.0, 1.0, neq + 1)
+    p[neq] = 0.0
+    F = rng.uniform(-1.0, 1.0, neq + 1)
+    F[neq] = 0.0
+    F0 = F.copy()
+    d2 = ndof * ndof
+    Q = np.zeros(neq + 1)
+    Q2 = np.zeros(neq + 1)
+    Q2no = np.zeros(neq + 1)
+    BD = np.zeros(mesh.nnodes * d2)
+    invBD = np.zeros(mesh.nnodes * d2)
+    Z = np.zeros(neq + 1)
+    f(mesh.nnodes, mesh.nel, np.ascontiguousarray(mesh.vert.reshape(-1)), node_id.reshape(-1), neq,
+      np.ascontiguousarray(A.reshape(-1)), P, Q, Q2, Q2no, F, BD, invBD, p, Z)
+    return dict(ndof=ndof, neq=neq, node_id=node_id, A=A.reshape(mesh.nel, m * m), P=P, Q=Q, Q2=Q2,
+                Q2no=Q2no, F0=F0, F=F, BD=BD.reshape(mesh.nnodes, d2),
+                invBD=invBD.reshape(mesh.nnodes, d2), p=p, Z=Z)
+
+
+BLOCK_CASES = {"blk_euler_10x6": (4, 10, 6, 0.1, 11), "blk_ns_9x7": (3, 9, 7, 0.1, 12)}
+
+
+def main_blocks():
+    for name, (ndof, nx, ny, pert, seed) in BLOCK_CASES.items():
+        mesh = structured_mesh(nx, ny, perturb=pert, seed=seed)
+        out = run_ref_block(ndof, mesh, seed)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, **out)
+        print(f"{name}: neq={out['neq']}")
+
+
 def main():
+    main_blocks()
     lib = load_ref()
     for name, (nx, ny, pert, rule, kw) in CASES.items():
         mesh = structured_mesh(nx, ny, perturb=pert, seed=1234)
