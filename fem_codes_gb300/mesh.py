@@ -138,3 +138,53 @@ def element_types(mesh: Mesh) -> np.ndarray:
     m1 = c1 == 2
     t[m1] = np.where((c1 == c2)[m1], 5, np.where((c1 == c4)[m1], 8, 1))
     return t
+
+
+@dataclasses.dataclass
+class EulerProblem:
+    """A 2D Euler problem on a mesh: equation numbering node_id [nnodes, 4]
+    (-1 prescribed; Fill_ID.c:3-39 numbers node by node, dof by dof), the
+    prescribed conservative values upresc [nnodes, 4] (rho, rho u, rho v,
+    rho E), the initial solution u0 [neq+1] and gamma."""
+    name: str
+    node_id: np.ndarray
+    neq: int
+    upresc: np.ndarray
+    u0: np.ndarray
+    gamma: float
+
+
+def refletido_problem(mesh: Mesh) -> EulerProblem:
+    """Reflected oblique shock (03_Euler_Equations/2D/REFLETIDO): inflow x = 0
+    with (1, 2.9, 0, 5.990715) and top y = ymax with (1.7, 4.452878,
+    -0.860744, 9.870181681) fully prescribed, rho v = 0 on the bottom wall
+    y = 0, free outflow; initial state the inflow state
+    (REFLETIDO_InitialSolution.c, REFLETIDO_*presc.c: the left boundary
+    wins at shared corners)."""
+    x, y = mesh.x, mesh.y
+    left = np.abs(x) <= 1e-15
+    top = y == y.max()
+    bottom = np.abs(y) <= 1e-15
+    presc = np.zeros((mesh.nnodes, 4), dtype=bool)
+    presc[left | top, :] = True
+    presc[bottom, 2] = True
+    node_id = np.full((mesh.nnodes, 4), -1, np.int32)
+    neq = int((~presc).sum())
+    node_id[~presc] = np.arange(neq, dtype=np.int32)
+    upresc = np.empty((mesh.nnodes, 4))
+    upresc[:, 0] = np.where(left, 1.0, 1.7)
+    upresc[:, 1] = np.where(left, 2.9, 4.452878)
+    upresc[:, 2] = np.where(left | bottom, 0.0, -0.860744)
+    upresc[:, 3] = np.where(left, 5.990715, 9.870181681)
+    init = np.array([1.0, 2.9, 0.0, 5.990715])
+    u0 = np.zeros(neq + 1)
+    free = node_id >= 0
+    u0[node_id[free]] = np.broadcast_to(init, node_id.shape)[free]
+    return EulerProblem("REFLETIDO", node_id, neq, upresc, u0, 1.4)
+
+
+def euler_cfl_dt(mesh: Mesh, cfl: float = 5.0, speed: float = 2.9, sound: float = 1.0) -> float:
+    """Time step from a CFL number, dt = CFL * h / (|v| + c), h the smaller
+    cell size (the reference's decks give dt directly)."""
+    h = min(float(mesh.x.max() - mesh.x.min()) / mesh.nx, float(mesh.y.max() - mesh.y.min()) / mesh.ny)
+    return cfl * h / (speed + sound)

@@ -96,6 +96,14 @@ void orc_get_times(double *t);
 /* Wall time (seconds) of each of the first n Picard iterations of that run. */
 void orc_get_step_times(double *t, int n);
 
+/* Operator application out = Op(in) on vectors of neq+1 entries. */
+typedef void (*orc_apply_fn)(const void *ctx, double *in, double *out);
+
+/* pgmres.c:4-211 over caller-supplied operator and preconditioner (prec may
+ * be NULL for none).  Returns the number of inner iterations. */
+int orc_pgmres_cb(int neq, orc_apply_fn mv, orc_apply_fn prec, const void *ctx, int kmax, int lmax,
+                  double tol, const double *B, double *X);
+
 /* pgmres.c:4-211 on an assembled CSR system with optional ILU(0):
  * B is overwritten by M^-1 B when precond != 0 (the precond_setup side effect),
  * X receives the solution. Returns the number of inner iterations. */
@@ -114,6 +122,29 @@ void orc_blockdiag_setup(int ndof, int nnodes, int nel, int neq, const int *vert
                          const double *A, double *BD, double *invBD, double *F);
 void orc_ebe2mv4(int nnodes, int neq, int nel, const int *lm, const int *node_id, const double *A,
                  const double *BD, const double *invBD, int with_inverse, double *P, double *Q);
+
+/* ---- 2D Euler (03_Euler_Equations/2D) ---------------------------------- */
+typedef struct {
+	int nnodes, nel, neq;
+	const double *x, *y;          /* [nnodes]                                   */
+	const int *vert;              /* [3*nel]                                    */
+	const int *node_id;           /* [4*nnodes] equation of (node, dof) or -1   */
+	const double *upresc;         /* [4*nnodes] prescribed (rho, rho u, rho v, rho E) */
+	double gamma, mach;           /* mach used only when dimensionless != 0     */
+	int dimensionless;
+	double alpha, dt, stab_tol;
+} orc_euler;
+
+/* Build_M_K_F_SUPG.c:6-1072 (no slip-wall rotation): element matrices
+ * Ae [nel*144] (row-major 12x12) and residual R [neq+1]. */
+void orc_euler_build(const orc_euler *p, const double *u, const double *du, double *Ae, double *R);
+
+/* Predictor_Old.c:46-132 with StopByIterations (ncorr correctors per step),
+ * BlockDiag_precond_EBE_setup + ebemvNDOF4 + pgmres.  u [neq+1] in/out;
+ * uhist [nsteps*(neq+1)] (may be NULL), iters [nsteps*ncorr] (may be NULL).
+ * Returns the total GMRES iterations. */
+int orc_euler_predictor(const orc_euler *p, int kmax, int lmax, double tol, int nsteps, int ncorr,
+                        double *u, double *uhist, int *iters);
 
 #ifdef __cplusplus
 }

@@ -1,5 +1,5 @@
 """Test infrastructure only: ctypes access to the CPU oracle (liboracle.so,
-built from oracle/transport_oracle.c by ``make -C oracle``).
+built from oracle/*_oracle.c by ``make -C oracle``).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
 module, as the checker.
@@ -27,8 +27,9 @@ def lib() -> ctypes.CDLL:
     global _lib
     if _lib is None:
         path = os.path.join(HERE, "liboracle.so")
-        src = os.path.join(HERE, "transport_oracle.c")
-        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        srcs = [os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith((".c", ".h"))
+                and not f.startswith("ref_")]
+        if not os.path.exists(path) or any(os.path.getmtime(path) < os.path.getmtime(f) for f in srcs):
             build()
         L = ctypes.CDLL(path)
         L.orc_transport_run.restype = ctypes.c_int
@@ -270,3 +271,50 @@ def csr_gmres(IA, JA, AA, B, use_ilu0=True, kmax=30, lmax=1000, tol=1e-8):
     it = L.orc_csr_gmres(n, _c(IA, np.int32), _c(JA, np.int32), _c(AA, np.float64),
                          1 if use_ilu0 else 0, kmax, lmax, tol, B, X)
     return X, it, B
+
+
+class EulerParams(ctypes.Structure):
+    """orc_euler of oracle.h."""
+    _fields_ = [("nnodes", ctypes.c_int), ("nel", ctypes.c_int), ("neq", ctypes.c_int),
+                ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("vert", ctypes.c_void_p),
+                ("node_id", ctypes.c_void_p), ("upresc", ctypes.c_void_p),
+                ("gamma", ctypes.c_double), ("mach", ctypes.c_double), ("dimensionless", ctypes.c_int),
+                ("alpha", ctypes.c_double), ("dt", ctypes.c_double), ("stab_tol", ctypes.c_double)]
+
+
+def _euler(x, y, vert, node_id, neq, upresc, gamma, alpha, dt, stab_tol, mach=1.0, dimensionless=False):
+    keep = [_c(x, np.float64), _c(y, np.float64), _c(vert, np.int32).reshape(-1),
+            _c(node_id, np.int32).reshape(-1), _c(upresc, np.float64).reshape(-1)]
+    p = EulerParams(len(keep[0]), len(keep[2]) // 3, int(neq), *(k.ctypes.data for k in keep),
+                    float(gamma), float(mach), int(bool(dimensionless)), float(alpha), float(dt),
+                    float(stab_tol))
+    return p, keep
+
+
+def euler_build(x, y, vert, node_id, neq, upresc, u, du, gamma=1.4, alpha=0.5, dt=1e-3,
+                stab_tol=1e-6, mach=1.0, dimensionless=False):
+    """Build_M_K_F_SUPG: (Ae [nel,144], R [neq+1])."""
+    L = lib()
+    p, keep = _euler(x, y, vert, node_id, neq, upresc, gamma, alpha, dt, stab_tol, mach, dimensionless)
+    Ae = np.zeros((p.nel, 144))
+    R = np.zeros(neq + 1)
+    L.orc_euler_build.restype = None
+    L.orc_euler_build.argtypes = [ctypes.POINTER(EulerParams), _dp, _dp, _dp, _dp]
+    L.orc_euler_build(ctypes.byref(p), _c(u, np.float64), _c(du, np.float64), Ae, R)
+    return Ae, R
+
+
+def euler_predictor(x, y, vert, node_id, neq, upresc, u0, nsteps, ncorr=2, gamma=1.4, alpha=0.5,
+                    dt=1e-3, stab_tol=1e-6, kmax=30, lmax=100, tol=1e-8, mach=1.0, dimensionless=False):
+    """Predictor_Old with StopByIterations: (u after each step [nsteps, neq+1],
+    GMRES iterations [nsteps, ncorr])."""
+    L = lib()
+    p, keep = _euler(x, y, vert, node_id, neq, upresc, gamma, alpha, dt, stab_tol, mach, dimensionless)
+    u = np.array(u0, dtype=np.float64)
+    uhist = np.zeros((nsteps, neq + 1))
+    iters = np.zeros((nsteps, ncorr), np.int32)
+    L.orc_euler_predictor.restype = ctypes.c_int
+    L.orc_euler_predictor.argtypes = [ctypes.POINTER(EulerParams), ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp, _ip]
+    L.orc_euler_predictor(ctypes.byref(p), kmax, lmax, tol, nsteps, ncorr, u, uhist, iters)
+    return uhist, iters

@@ -1,0 +1,193 @@
+/*
+ * Test infrastructure only: drives the reference's 2D Euler SUPG+CAU element
+ * build (03_Euler_Equations/2D/01_CommonFiles/Build_M_K_F_SUPG.c with
+ * Delta_CAU.c, Ax_Ay_calculations.c, eval_U_dU.c, ebe_assembly.c, the
+ * REFLETIDO plug-in) and its predictor-multicorrector (Predictor_Old.c:46-132
+ * control flow) on in-memory arrays, compiled from the reference's sources by
+ * oracle/Makefile with -DEulerEquations2D.
+ *
+ * The shipped 00_CommonFiles/.../pgmres.c only has the steady-transport
+ * 4-argument form, so the Euler driver does not link as shipped; the 6-argument
+ * GMRES below is the documented adapter: the same algorithm (pgmres.c:4-211,
+ * left preconditioned, modified Gram-Schmidt, Givens) taking B and X as
+ * arguments and FemFunctions->mv as the product.
+ */
+#include "EulerEquations.h"
+
+void *mycalloc(char *, int, int);
+void myfree(void *);
+int ebemvNDOF4(ParametersType *, MatrixDataType *, FemStructsType *, double *, double *);
+int BlockDiag_precond_EBE_setup(ParametersType *, MatrixDataType *, FemStructsType *, int, double *);
+int BlockDiag_precond(ParametersType *, MatrixDataType *, FemStructsType *, double *, double *);
+int Build_M_K_F_SUPG(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *);
+double Delta_CAU(double, double *, double *, double *, double (*)[4], double (*)[4], double (*)[4],
+                 double *, double, double, double, double, double, double, double, int, double *, double *);
+void dimensional_Ax_Ay_calculations(double, double, double *, double (*)[4], double (*)[4]);
+double REFLETIDO_gamma(double, double);
+double REFLETIDO_rhopresc(double, double);
+double REFLETIDO_v1presc(double, double);
+double REFLETIDO_v2presc(double, double);
+double REFLETIDO_epresc(double, double);
+double ddot(int, double *, double *);
+
+static double zero_theta(double x, double y) { return 0.0; }
+
+/* pgmres.c:4-211 in the 6-argument form (B, X given). */
+static int gmres6(ParametersType *P, MatrixDataType *M, FemStructsType *FS, FemFunctionsType *FF,
+                  double *B, double *X)
+{
+	int i, j, k, l, cont, kmax = P->KrylovBasisVectorsQuantity, lmax = P->LinearMaxIter, neq = P->neq;
+	double normb, eps, rho, r, h1, h2, soma;
+	double **u = calloc(kmax + 1, sizeof(double *)), **h = calloc(kmax + 1, sizeof(double *));
+	double *e = calloc(kmax + 1, sizeof(double)), *c = calloc(kmax, sizeof(double));
+	double *s = calloc(kmax, sizeof(double)), *y = calloc(kmax, sizeof(double));
+	double *v = calloc(neq + 1, sizeof(double));
+	for (i = 0; i <= kmax; i++) { u[i] = calloc(neq + 1, sizeof(double)); h[i] = calloc(kmax + 1, sizeof(double)); }
+	for (k = 0; k < neq; k++) X[k] = 0;
+	normb = sqrt(ddot(neq, B, B));
+	eps = P->SolverTolerance * normb;
+	l = 0; cont = 0;
+	do {
+		i = 0;
+		for (j = 0; j < kmax; j++) memset(u[j], 0, sizeof(double) * neq);
+		memcpy(v, X, sizeof(double) * neq);
+		FF->mv(P, M, FS, v, u[0]);
+		FF->precond(P, M, FS, u[0], u[0]);
+		for (k = 0; k < neq; k++) u[0][k] += -1.0 * B[k];
+		for (k = 0; k < neq; k++) u[0][k] = -1.0 * u[0][k];
+		e[0] = sqrt(ddot(neq, u[0], u[0]));
+		{ double sc = 1.0 / e[0]; for (k = 0; k < neq; k++) u[0][k] = sc * u[0][k]; }
+		rho = e[0];
+		do {
+			cont++;
+			memcpy(v, u[i], sizeof(double) * neq);
+			FF->mv(P, M, FS, v, u[i+1]);
+			FF->precond(P, M, FS, u[i+1], u[i+1]);
+			for (j = 0; j <= i; j++) {
+				h[j][i] = ddot(neq, u[j], u[i+1]);
+				for (k = 0; k < neq; k++) u[i+1][k] += -h[j][i] * u[j][k];
+			}
+			h[i+1][i] = sqrt(ddot(neq, u[i+1], u[i+1]));
+			{ double sc = 1.0 / h[i+1][i]; for (k = 0; k < neq; k++) u[i+1][k] = sc * u[i+1][k]; }
+			for (j = 0; j <= i - 1; j++) {
+				h1 = c[j]*h[j][i] + s[j]*h[j+1][i];
+				h2 = -s[j]*h[j][i] + c[j]*h[j+1][i];
+				h[j][i] = h1; h[j+1][i] = h2;
+			}
+			r = sqrt(h[i][i]*h[i][i] + h[i+1][i]*h[i+1][i]);
+			c[i] = h[i][i] / r; s[i] = h[i+1][i] / r;
+			h[i][i] = r; h[i+1][i] = 0.0;
+			e[i+1] = -s[i]*e[i]; e[i] = c[i]*e[i];
+			rho = fabs(e[i+1]);
+			i++;
+		} while (rho > eps && i < kmax);
+		i--;
+		y[i] = e[i] / h[i][i];
+		for (j = i - 1; j >= 0; j--) {
+			soma = 0.0;
+			for (k = j + 1; k <= i; k++) soma = soma + h[j][k]*y[k];
+			y[j] = (e[j] - soma) / h[j][j];
+		}
+		for (j = 0; j <= i; j++) for (k = 0; k < neq; k++) X[k] = X[k] + u[j][k]*y[j];
+		l++;
+	} while (rho > eps && l < lmax);
+	P->iterations += cont;
+	for (i = 0; i <= kmax; i++) { free(u[i]); free(h[i]); }
+	free(u); free(h); free(e); free(c); free(s); free(y); free(v);
+	return 0;
+}
+
+static void setup(int nnodes, const double *x, const double *y, const int *node_id, int nel, const int *vert,
+                  int neq, double alpha, double dt, double stab_tol,
+                  ParametersType **Po, MatrixDataType **Mo, FemStructsType **FSo, FemFunctionsType **FFo)
+{
+	int I, k;
+	ParametersType *P = mycalloc("P", 1, sizeof(ParametersType));
+	MatrixDataType *M = mycalloc("M", 1, sizeof(MatrixDataType));
+	FemStructsType *FS = mycalloc("FS", 1, sizeof(FemStructsType));
+	FemFunctionsType *FF = mycalloc("FF", 1, sizeof(FemFunctionsType));
+	NodeType *Node = mycalloc("Node", nnodes, sizeof(NodeType));
+	ElementType *El = mycalloc("El", nel, sizeof(ElementType));
+	int **lm = mycalloc("lm", nel, sizeof(int *));
+	double **A = mycalloc("A", nel, sizeof(double *)), *Aaux = mycalloc("Aaux", nel * 144, sizeof(double));
+	AuxBuildStructuresType *aux = mycalloc("aux", 1, sizeof(AuxBuildStructuresType));
+	P->nnodes = nnodes; P->nel = nel; P->neq = neq;
+	P->Alpha = alpha; P->Alpha_Build = alpha; P->DeltaT = dt; P->DeltaT_Build = dt;
+	P->StabilizationTolerance = stab_tol;
+	strcpy(P->MatrixVectorProductScheme, "EBE");
+	strcpy(P->Preconditioner, "BlockDiag");
+	for (I = 0; I < nnodes; I++) {
+		Node[I].x = x[I]; Node[I].y = y[I];
+		Node[I].rhoType = Node[I].v1Type = Node[I].v2Type = Node[I].eType = 1;
+		for (k = 0; k < 4; k++) Node[I].id[k] = node_id[4 * I + k];
+	}
+	for (I = 0; I < nel; I++) {
+		for (k = 0; k < 3; k++) El[I].Vertex[k] = vert[3 * I + k];
+		lm[I] = mycalloc("lm", 12, sizeof(int));
+		A[I] = Aaux + 144 * I;
+	}
+	Fill_LM(neq, nel, lm, Node, El);
+	M->A = A; M->Aaux = Aaux;
+	aux->tolerance = stab_tol;
+	FS->lm = lm; FS->Node = Node; FS->Element = El; FS->AuxBuild = aux;
+	FS->F = mycalloc("F", neq + 1, sizeof(double));
+	FS->u = mycalloc("u", neq + 1, sizeof(double));
+	FS->du = mycalloc("du", neq + 1, sizeof(double));
+	FS->delta_old = mycalloc("delta_old", nel, sizeof(double));
+	FF->gamma = REFLETIDO_gamma;
+	FF->rhopresc = REFLETIDO_rhopresc; FF->v1presc = REFLETIDO_v1presc;
+	FF->v2presc = REFLETIDO_v2presc; FF->epresc = REFLETIDO_epresc;
+	FF->Ax_Ay_calculations = dimensional_Ax_Ay_calculations;
+	FF->ShockCapture = Delta_CAU;
+	FF->BC_theta = zero_theta;
+	FF->assembly = ebe_assembly;
+	FF->mv = ebemvNDOF4;
+	FF->precond = BlockDiag_precond;
+	*Po = P; *Mo = M; *FSo = FS; *FFo = FF;
+}
+
+/* One Build on the state (u, du): element matrices Ae [nel*144] and R. */
+int ref_euler_build(int nnodes, const double *x, const double *y, const int *node_id, int nel, const int *vert,
+                    int neq, double alpha, double dt, double stab_tol, const double *u, const double *du,
+                    double *Ae, double *R)
+{
+	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF;
+	setup(nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
+	memcpy(FS->u, u, sizeof(double) * (neq + 1));
+	memcpy(FS->du, du, sizeof(double) * (neq + 1));
+	Build_M_K_F_SUPG(P, M, FS, FF);
+	memcpy(Ae, M->Aaux, sizeof(double) * nel * 144);
+	memcpy(R, FS->F, sizeof(double) * (neq + 1));
+	return 0;
+}
+
+/* Predictor_Old.c:46-132 with ncorr correctors per step (StopByIterations,
+ * Criteria.c:25-31) and nsteps steps, BlockDiag + EBE + the GMRES above.
+ * u in/out; ahist [nsteps*(neq+1)], uhist likewise; iters [nsteps*ncorr]. */
+int ref_euler_predictor(int nnodes, const double *x, const double *y, const int *node_id, int nel,
+                        const int *vert, int neq, double alpha, double dt, double stab_tol, int kmax,
+                        int lmax, double tol, int nsteps, int ncorr, double *u_io, double *uhist, int *iters)
+{
+	int I, step, i, tag = 1;
+	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF;
+	setup(nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
+	P->KrylovBasisVectorsQuantity = kmax; P->LinearMaxIter = lmax; P->SolverTolerance = tol;
+	double *u = FS->u, *a = FS->du, *R = FS->F, *Da = calloc(neq + 1, sizeof(double));
+	memcpy(u, u_io, sizeof(double) * (neq + 1));
+	for (step = 0; step < nsteps; step++) {
+		for (I = 0; I < neq; I++) { u[I] += (1.0 - alpha)*dt*a[I]; a[I] = 0.0; }
+		for (i = 0; i < ncorr; i++) {
+			int before = P->iterations;
+			Build_M_K_F_SUPG(P, M, FS, FF);
+			BlockDiag_precond_EBE_setup(P, M, FS, tag++, R);
+			gmres6(P, M, FS, FF, R, Da);
+			iters[step * ncorr + i] = P->iterations - before;
+			for (I = 0; I < neq; I++) a[I] += 1 * Da[I];
+			for (I = 0; I < neq; I++) u[I] += alpha*dt * Da[I];
+		}
+		memcpy(uhist + (size_t)step * (neq + 1), u, sizeof(double) * (neq + 1));
+	}
+	memcpy(u_io, u, sizeof(double) * (neq + 1));
+	free(Da);
+	return 0;
+}

@@ -675,16 +675,20 @@ double orc_ddot(int n, const double *x, const double *y)
 	return s;
 }
 
-/* Operator bundle for the solver. */
+/* Operator bundle for the solver; mvf/pcf (with ctx) replace the built-in
+ * schemes when set. */
 typedef struct {
 	int scheme, neq, nel, nedge, prec;       /* prec: 0 none, 1 ILU0, 2 Diag */
 	const int *IA, *JA, *lm, *lm2;
 	const double *A, *LU, *Dinv, *invDiag;
+	orc_apply_fn mvf, pcf;
+	const void *ctx;
 } orc_op;
 
 static void op_mv(const orc_op *o, double *P, double *Q)
 {
-	if (o->scheme == ORC_CSR) orc_csrmv(o->neq, o->IA, o->JA, o->A, P, Q);
+	if (o->mvf) o->mvf(o->ctx, P, Q);
+	else if (o->scheme == ORC_CSR) orc_csrmv(o->neq, o->IA, o->JA, o->A, P, Q);
 	else if (o->scheme == ORC_EBE) orc_ebemv(o->neq, o->nel, o->lm, o->A, P, Q);
 	else orc_edemv(o->neq, o->nedge, o->lm2, o->A, P, Q);
 }
@@ -692,7 +696,8 @@ static void op_mv(const orc_op *o, double *P, double *Q)
 static void op_prec(const orc_op *o, double *p, double *z)
 {
 	int i;
-	if (o->prec == 1) orc_ilu0_apply(o->neq, o->IA, o->JA, o->LU, o->Dinv, p, z);
+	if (o->pcf) o->pcf(o->ctx, p, z);
+	else if (o->prec == 1) orc_ilu0_apply(o->neq, o->IA, o->JA, o->LU, o->Dinv, p, z);
 	else if (o->prec == 2) for (i = 0; i < o->neq; i++) z[i] = p[i]*o->invDiag[i];  /* Diag_precond.c:3-14 */
 }
 
@@ -768,6 +773,15 @@ static int orc_pgmres(const orc_op *o, int kmax, int lmax, double tol, const dou
 	for (i = 0; i <= kmax; i++) free(u[i]);
 	free(u); free(h); free(e); free(c); free(s); free(y); free(v);
 	return cont;
+}
+
+int orc_pgmres_cb(int neq, orc_apply_fn mv, orc_apply_fn prec, const void *ctx, int kmax, int lmax,
+                  double tol, const double *B, double *X)
+{
+	orc_op o;
+	memset(&o, 0, sizeof o);
+	o.neq = neq; o.mvf = mv; o.pcf = prec; o.ctx = ctx;
+	return orc_pgmres(&o, kmax, lmax, tol, B, X);
 }
 
 /* Diag_precond_{CSR,EBE,EDE}_setup.c: extract the diagonal, invert, F *= 1/D. */

@@ -22,9 +22,10 @@ def pytest_configure(config):
 
 
 def golden_names():
-    """Steady-transport golden cases (the blk_* files hold block operators)."""
+    """Steady-transport golden cases (blk_* hold block operators, eul_* the
+    Euler build and predictor)."""
     return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(f).startswith("blk_"))
+                  if not os.path.basename(f).startswith(("blk_", "eul_")))
 
 
 def load_golden(name):

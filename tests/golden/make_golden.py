@@ -1,6 +1,8 @@
-"""Generate golden vectors by running the reference's own steady-transport C
-path (compiled from its sources by ``make -C oracle ref`` into
-oracle/_ref/libfemref.so, driven by oracle/ref_harness.c).
+"""Generate golden vectors by running the reference's own C paths, compiled
+from its sources by ``make -C oracle ref`` into oracle/_ref/: the steady-
+transport solve (libfemref.so, oracle/ref_harness.c), the multi-dof EBE
+operators (libfemref_*_blk.so, oracle/ref_block_harness.c) and the 2D Euler
+build and predictor (libfemref_euler.so, oracle/ref_euler_harness.c).
 
 Usage:  python tests/golden/make_golden.py        (writes tests/golden/*.npz)
 
@@ -194,7 +196,57 @@ def main_blocks():
         print(f"{name}: neq={out['neq']}")
 
 
+# 2D Euler (REFLETIDO) cases: name -> (nx, ny, perturb, seed, alpha, CFL, stab_tol, nsteps, ncorr)
+EULER_CASES = {
+    "eul_refletido_16x4": (16, 4, 0.2, 3, 0.5, 5.0, 1e-6, 3, 2),
+    "eul_refletido_12x6": (12, 6, 0.0, 4, 0.7, 2.0, 1e-3, 2, 3),
+}
+
+
+def main_euler():
+    """Euler SUPG+CAU Build on a perturbed state (element matrices and
+    residual) and a short predictor-multicorrector run, through the
+    reference's sources (oracle/ref_euler_harness.c)."""
+    from fem_codes_gb300.mesh import euler_cfl_dt, refletido_problem
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libfemref_euler.so"))
+    lib.ref_euler_build.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int,
+                                    ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp]
+    lib.ref_euler_predictor.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                        _ip]
+    for name, (nx, ny, pert, seed, alpha, cfl, stol, nsteps, ncorr) in EULER_CASES.items():
+        mesh = structured_mesh(nx, ny, lx=4.0, ly=1.0, perturb=pert, seed=seed)
+        pb = refletido_problem(mesh)
+        neq = pb.neq
+        rng = np.random.default_rng(seed)
+        u = pb.u0 * (1.0 + 0.05 * rng.uniform(-1.0, 1.0, neq + 1))
+        du = 0.1 * rng.uniform(-1.0, 1.0, neq + 1)
+        u[neq] = du[neq] = 0.0
+        dt = euler_cfl_dt(mesh, cfl)
+        vert = np.ascontiguousarray(mesh.vert.reshape(-1), np.int32)
+        nid = np.ascontiguousarray(pb.node_id.reshape(-1), np.int32)
+        Ae = np.zeros(mesh.nel * 144)
+        R = np.zeros(neq + 1)
+        lib.ref_euler_build(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol, u, du,
+                            Ae, R)
+        kmax, lmax, tol = 30, 100, 1e-8
+        up = pb.u0.copy()
+        uhist = np.zeros(nsteps * (neq + 1))
+        iters = np.zeros(nsteps * ncorr, np.int32)
+        lib.ref_euler_predictor(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol,
+                                kmax, lmax, tol, nsteps, ncorr, up, uhist, iters)
+        np.savez_compressed(
+            os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id,
+            neq=neq, upresc=pb.upresc, u0=pb.u0, gamma=pb.gamma, alpha=alpha, dt=dt, stab_tol=stol,
+            u=u, du=du, Ae=Ae.reshape(mesh.nel, 144), R=R, kmax=kmax, lmax=lmax, tol=tol,
+            nsteps=nsteps, ncorr=ncorr, uhist=uhist.reshape(nsteps, neq + 1),
+            iters=iters.reshape(nsteps, ncorr))
+        print(f"{name}: neq={neq} nel={mesh.nel} dt={dt:.4g} iters={list(iters)}")
+
+
 def main():
+    main_euler()
     main_blocks()
     lib = load_ref()
     for name, (nx, ny, pert, rule, kw) in CASES.items():
