@@ -19,7 +19,7 @@ import numpy as np
 
 from .build import LIB, build as _build
 
-__all__ = ["SSTransport", "FemGpuError", "load", "OPTS"]
+__all__ = ["SSTransport", "Euler", "FemGpuError", "load", "OPTS"]
 
 _lib = None
 
@@ -33,7 +33,7 @@ ERRORS = {
 OPTS = {
     "scheme": {"EBE": 0, "EDE": 1, "CSR": 2},
     "reorder": {"NOT": 0, "SYMRCM": 1},
-    "precond": {"NOT": 0, "ILU0": 1, "DIAG": 2},
+    "precond": {"NOT": 0, "ILU0": 1, "DIAG": 2, "BLOCKDIAG": 3},
     "shock": {"CAU": 0, "YZBETA": 1},
     "hshock": {"2SQRTAREA": 0, "SQRTAREA": 1, "OPTION1": 2, "OPTION2": 3},
     "precision": {"FP64": 0, "MIXED": 1, "MIXED_IR": 2},
@@ -55,6 +55,14 @@ class Opts(ctypes.Structure):
                 ("kmax", ctypes.c_int), ("lmax", ctypes.c_int), ("tol", ctypes.c_double),
                 ("nonlin_tol", ctypes.c_double), ("precision", ctypes.c_int), ("ir_max", ctypes.c_int),
                 ("solver", ctypes.c_int), ("inner_tol", ctypes.c_double)]
+
+
+class EulerOpts(ctypes.Structure):
+    """femgpu_euler_opts of femgpu.h."""
+    _fields_ = [("gamma", ctypes.c_double), ("mach", ctypes.c_double), ("dimensionless", ctypes.c_int),
+                ("alpha", ctypes.c_double), ("dt", ctypes.c_double), ("stab_tol", ctypes.c_double),
+                ("precond", ctypes.c_int), ("solver", ctypes.c_int), ("kmax", ctypes.c_int),
+                ("lmax", ctypes.c_int), ("tol", ctypes.c_double), ("ncorr", ctypes.c_int)]
 
 
 _vp = ctypes.c_void_p
@@ -102,6 +110,31 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         f = getattr(L, name)
         f.argtypes = args
         f.restype = ctypes.c_int
+    L.femgpu_euler_default_opts.argtypes = [ctypes.POINTER(EulerOpts)]
+    L.femgpu_euler_default_opts.restype = None
+    L.femgpu_euler_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(EulerOpts), ctypes.c_int, _vp, _vp,
+                                      ctypes.c_int, _vp, _vp, ctypes.c_int, _vp]
+    L.femgpu_euler_create.restype = ctypes.c_int
+    L.femgpu_euler_destroy.argtypes = [_vp]
+    L.femgpu_euler_destroy.restype = None
+    for name, args in {
+        "femgpu_euler_set_stream": [_vp, _vp],
+        "femgpu_euler_build": [_vp, _vp, _vp, _vp, _vp],
+        "femgpu_euler_build_dev": [_vp],
+        "femgpu_euler_precond_setup": [_vp, _vp],
+        "femgpu_euler_precond_setup_dev": [_vp],
+        "femgpu_euler_solve": [_vp, _vp, _vp, _ip],
+        "femgpu_euler_solve_dev": [_vp, _ip],
+        "femgpu_euler_predictor": [_vp, _vp, ctypes.c_int, _vp, _vp],
+        "femgpu_euler_predictor_dev": [_vp, ctypes.c_int, _vp],
+        "femgpu_euler_last_times": [_vp, _vp],
+    }.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    for name in ("femgpu_euler_u_dev", "femgpu_euler_ebe"):
+        getattr(L, name).argtypes = [_vp]
+        getattr(L, name).restype = _vp
     for name in ("femgpu_transport_u_dev", "femgpu_transport_F_dev"):
         getattr(L, name).argtypes = [_vp]
         getattr(L, name).restype = _vp
@@ -314,3 +347,123 @@ class SSTransport:
 
     def u_dev(self):
         return self._L.femgpu_transport_u_dev(self._h)
+
+
+class Euler:
+    """2D Euler equations on one GPU: SUPG+CAU element build, block EBE
+    storage with the nodal block-diagonal preconditioner, GMRES and the
+    predictor-multicorrector (03_Euler_Equations/2D with SUPG, CAU, EBE,
+    Predictor1, StopMulticorrection ITERATION).  ``Build``,
+    ``precond_setup``, ``solver`` and ``Predictor`` carry the names of the
+    functions they replace (EulerEquations.h:136-170, Predictor_Old.c);
+    vectors have length neq+1 with slot neq the dump of prescribed dofs."""
+
+    def __init__(self, x, y, vert, node_id, neq, upresc, gamma=1.4, mach=1.0, dimensionless=False,
+                 alpha=0.5, dt=1e-3, stab_tol=1e-6, precond="BlockDiag", solver="GMRES", kmax=30,
+                 lmax=100, tol=1e-8, ncorr=2):
+        L = load()
+        o = EulerOpts()
+        L.femgpu_euler_default_opts(ctypes.byref(o))
+        o.gamma, o.mach, o.dimensionless = float(gamma), float(mach), int(bool(dimensionless))
+        o.alpha, o.dt, o.stab_tol = float(alpha), float(dt), float(stab_tol)
+        o.precond = OPTS["precond"][precond.upper()]
+        o.solver = OPTS["solver"][solver.upper()]
+        o.kmax, o.lmax, o.tol, o.ncorr = int(kmax), int(lmax), float(tol), int(ncorr)
+        self.opts = o
+        self._keep = [_f64(x), _f64(y), _i32(np.asarray(vert).reshape(-1)),
+                      _i32(np.asarray(node_id).reshape(-1)), _f64(np.asarray(upresc).reshape(-1))]
+        self.nnodes = len(self._keep[0])
+        self.nel = self._keep[2].size // 3
+        self.neq = int(neq)
+        h = _vp()
+        rc = L.femgpu_euler_create(ctypes.byref(h), ctypes.byref(o), self.nnodes, _ptr(self._keep[0]),
+                                   _ptr(self._keep[1]), self.nel, _ptr(self._keep[2]), _ptr(self._keep[3]),
+                                   self.neq, _ptr(self._keep[4]))
+        if rc:
+            raise FemGpuError(rc, "Preprocess")
+        self._h = h
+        self._L = L
+
+    @classmethod
+    def from_problem(cls, mesh, prob, **kw):
+        return cls(mesh.x, mesh.y, mesh.vert, prob.node_id, prob.neq, prob.upresc, gamma=prob.gamma, **kw)
+
+    def _check(self, rc, where):
+        if rc:
+            raise FemGpuError(rc, where)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.femgpu_euler_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr):
+        self._check(self._L.femgpu_euler_set_stream(self._h, _vp(stream_ptr)), "set_stream")
+
+    def Build(self, u=None, du=None, want_matrix=False):
+        """Build_M_K_F_SUPG from (u, du). Returns (R, Ae [nel, 144] or None)."""
+        R = np.zeros(self.neq + 1)
+        Ae = np.zeros((self.nel, 144)) if want_matrix else None
+        uu = None if u is None else _f64(u)
+        dd = None if du is None else _f64(du)
+        self._check(self._L.femgpu_euler_build(self._h, _ptr(uu), _ptr(dd), _ptr(Ae), _ptr(R)), "Build")
+        return R, Ae
+
+    def precond_setup(self):
+        """BlockDiag_precond_EBE_setup: blocks, inverses, R := D^-1 R. Returns R."""
+        R = np.zeros(self.neq + 1)
+        self._check(self._L.femgpu_euler_precond_setup(self._h, _ptr(R)), "precond_setup")
+        return R
+
+    def solver(self, B=None, raise_on_nonconvergence=True):
+        """pgmres (6-argument form) on the block EBE operator: X = A^-1 B
+        (B None: the context's R). Returns (X, iterations)."""
+        BB = None if B is None else _f64(B)
+        X = np.zeros(self.neq + 1)
+        it = ctypes.c_int(0)
+        rc = self._L.femgpu_euler_solve(self._h, _ptr(BB), _ptr(X), ctypes.byref(it))
+        if rc and (rc != -5 or raise_on_nonconvergence):
+            raise FemGpuError(rc, "solver")
+        return X, it.value
+
+    def Predictor(self, u0, nsteps):
+        """Predictor_Old for nsteps steps from u0. Returns (u after each step
+        [nsteps, neq+1], GMRES iterations [nsteps, ncorr])."""
+        u = np.array(u0, dtype=np.float64, copy=True)
+        uh = np.zeros((nsteps, self.neq + 1))
+        its = np.zeros((nsteps, self.opts.ncorr), np.int32)
+        self._check(self._L.femgpu_euler_predictor(self._h, _ptr(u), int(nsteps), _ptr(uh), _ptr(its)),
+                    "Predictor")
+        return uh, its
+
+    def predictor_dev(self, nsteps):
+        """Predictor_Old continuing from the device state; returns the GMRES
+        iterations [nsteps, ncorr]."""
+        its = np.zeros((nsteps, self.opts.ncorr), np.int32)
+        self._check(self._L.femgpu_euler_predictor_dev(self._h, int(nsteps), _ptr(its)), "predictor_dev")
+        return its
+
+    def last_times(self):
+        """Seconds in (build, precond_setup, solve) of the last Predictor."""
+        t = np.zeros(3)
+        self._check(self._L.femgpu_euler_last_times(self._h, _ptr(t)), "last_times")
+        return t
+
+    def u_dev(self):
+        return self._L.femgpu_euler_u_dev(self._h)

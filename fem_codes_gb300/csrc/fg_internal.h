@@ -65,6 +65,34 @@ typedef struct fg_status {
 	int pad;
 } fg_status;
 
+/* Krylov workspace (device memory unless noted); one per context.  A view
+ * of a context's buffers is enough to run the cycles below. */
+typedef struct fg_krylov {
+	int n, kmax, nblk;              /* unknowns, basis size, reduction blocks */
+	size_t ldv;                     /* leading dimension of V / Z (>= n+1)   */
+	cudaStream_t stream;
+	double *V;                      /* [(kmax+1) x ldv] Arnoldi basis         */
+	double *H, *cs, *sn, *ge, *gy;  /* Hessenberg (kmax+1)^2, Givens, rhs, y  */
+	double *Z;                      /* [kmax x ldv] FGMRES M^-1 v (FP64)      */
+	float *Z32;                     /* [kmax x ldv] FGMRES M^-1 v (FP32)      */
+	double *partials;               /* [nblk] reduction partials              */
+	fg_status *st;                  /* device status                          */
+	fg_status *st_host;             /* pinned host mirror                     */
+} fg_krylov;
+
+/* Operator callbacks, stream-ordered, returning cudaError_t (> 0) or a
+ * FEMGPU_E* code (< 0).  active (device flag, may be NULL) predicates the
+ * work of an inner iteration after convergence.  precond NULL: identity. */
+typedef struct fg_linop {
+	void *ctx;
+	int (*matvec)(void *ctx, const double *p, double *q, const int *active);
+	int (*precond)(void *ctx, const double *p, double *z, const int *active);
+	/* mixed precision (FGMRES): z = M^-1 p in FP32, and q = A z from an FP32
+	 * vector with FP64 (op32 == 0) or FP32 (op32 != 0) matrix values. */
+	int (*precond32)(void *ctx, const double *p, float *z, const int *active);
+	int (*matvec_xf)(void *ctx, const float *p, double *q, const int *active, int op32);
+} fg_linop;
+
 struct femgpu_transport {
 	femgpu_transport_opts o;
 	int nnodes, nel, neq, nnz, nedge, bandwidth;
@@ -129,6 +157,14 @@ int fg_csrmv32(int n, const int *IA, const int *JA, const float *AA, const float
                float *Q, const int *active, cudaStream_t s);
 int fg_diag_setup(femgpu_transport *t);
 int fg_precond(femgpu_transport *t, const double *p, double *z, const int *active);
+/* One restart cycle of the reference's left-preconditioned GMRES
+ * (pgmres.c:58-184) / of flexible right-preconditioned GMRES (mixed 0: FP64,
+ * 1: FP32 preconditioner, 2: FP32 preconditioner and operator). */
+int fg_kry_pgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X);
+int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int mixed);
+int fg_kry_dot(const fg_krylov *k, const double *a, const double *b, int n, double *out_dev);
+/* The transport context's Krylov buffers and operator as a view. */
+void fg_transport_krylov(femgpu_transport *t, fg_krylov *k, fg_linop *op);
 int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, int first);
 /* Flexible GMRES cycle, right preconditioned; mixed != 0: FP32 operator and
  * preconditioner (A32, FP32 ILU/diagonal), FP64 Arnoldi. */

@@ -403,30 +403,29 @@ static int red_grid(femgpu_transport *t) { return t->nblk_red; }
 
 // One restart cycle of pgmres.c:58-184, entirely stream-ordered; the status
 // block tells the host afterwards whether to restart.
-extern "C" int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, int first)
+extern "C" int fg_kry_pgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X)
 {
-	cudaStream_t s = t->stream;
-	int n = t->neq, kmax = t->kmax, ldh = kmax + 1, G = red_grid(t), rc;
-	size_t ldv = t->ldv;
-	double *V = t->V;
-	int *active = &t->st->active;
-	(void)first;
-	// u0 = M^-1 A X  (precondR is the identity in the transport drivers)
-	if ((rc = fg_matvec(t, X, V, nullptr))) return rc;
-	if ((rc = fg_precond(t, V, V, nullptr))) return rc;
-	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, t->ge, t->partials, t->st, 1);
-	k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, t->ge, t->st);
+	cudaStream_t s = k->stream;
+	int n = k->n, kmax = k->kmax, ldh = kmax + 1, G = k->nblk, rc;
+	size_t ldv = k->ldv;
+	double *V = k->V;
+	int *active = &k->st->active;
+	// u0 = M^-1 A X  (precondR is the identity in the drivers using pgmres)
+	if ((rc = op->matvec(op->ctx, X, V, nullptr))) return rc;
+	if (op->precond && (rc = op->precond(op->ctx, V, V, nullptr))) return rc;
+	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, k->ge, k->partials, k->st, 1);
+	k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, k->ge, k->st);
 	for (int i = 0; i < kmax; i++) {
 		double *w = V + (size_t)(i + 1) * ldv;
-		if ((rc = fg_matvec(t, V + (size_t)i * ldv, w, active))) return rc;
-		if ((rc = fg_precond(t, w, w, active))) return rc;
+		if ((rc = op->matvec(op->ctx, V + (size_t)i * ldv, w, active))) return rc;
+		if (op->precond && (rc = op->precond(op->ctx, w, w, active))) return rc;
 		for (int j = 0; j <= i + 1; j++)
-			k_mgs<<<G, RED_TPB, 0, s>>>(V, ldv, n, i, j, t->H, ldh, t->partials, t->st);
-		k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(w, n, t->H + (i + 1) * ldh + i, t->st);
-		k_givens<<<1, 1, 0, s>>>(t->H, ldh, t->cs, t->sn, t->ge, i, kmax, t->st);
+			k_mgs<<<G, RED_TPB, 0, s>>>(V, ldv, n, i, j, k->H, ldh, k->partials, k->st);
+		k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(w, n, k->H + (i + 1) * ldh + i, k->st);
+		k_givens<<<1, 1, 0, s>>>(k->H, ldh, k->cs, k->sn, k->ge, i, kmax, k->st);
 	}
-	k_backsolve<<<1, 1, 0, s>>>(t->H, ldh, t->ge, t->gy, t->st);
-	k_update_x<double><<<fg_grid(n), FG_TPB, 0, s>>>(X, V, ldv, n, t->gy, t->st);
+	k_backsolve<<<1, 1, 0, s>>>(k->H, ldh, k->ge, k->gy, k->st);
+	k_update_x<double><<<fg_grid(n), FG_TPB, 0, s>>>(X, V, ldv, n, k->gy, k->st);
 	return (int)cudaGetLastError();
 }
 
@@ -434,36 +433,90 @@ extern "C" int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, i
 // r0 = B - A X, z_i = M^-1 v_i, w = A z_i, MGS, Givens; X += Z y.  The
 // Arnoldi residual is the unpreconditioned one.  mixed: 0 FP64 throughout,
 // 1 FP32 preconditioner (FP64 operator), 2 FP32 preconditioner and operator.
-extern "C" int fg_fgmres_cycle(femgpu_transport *t, const double *B, double *X, int mixed)
+extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X,
+                                   int mixed)
 {
-	cudaStream_t s = t->stream;
-	int n = t->neq, kmax = t->kmax, ldh = kmax + 1, G = red_grid(t), rc;
-	size_t ldv = t->ldv;
-	double *V = t->V;
-	int *active = &t->st->active;
-	if ((rc = fg_matvec(t, X, V, nullptr))) return rc;
-	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, t->ge, t->partials, t->st, 0);
-	k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, t->ge, t->st);
+	cudaStream_t s = k->stream;
+	int n = k->n, kmax = k->kmax, ldh = kmax + 1, G = k->nblk, rc;
+	size_t ldv = k->ldv;
+	double *V = k->V;
+	int *active = &k->st->active;
+	if (mixed && (!op->precond32 || !op->matvec_xf || !k->Z32)) return FEMGPU_E_ARG;
+	if (!mixed && !k->Z) return FEMGPU_E_ARG;
+	if ((rc = op->matvec(op->ctx, X, V, nullptr))) return rc;
+	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, k->ge, k->partials, k->st, 0);
+	k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, k->ge, k->st);
 	for (int i = 0; i < kmax; i++) {
 		double *v = V + (size_t)i * ldv, *w = V + (size_t)(i + 1) * ldv;
 		if (mixed) {
-			float *z = t->Z32 + (size_t)i * ldv;
-			if ((rc = fg_precond32(t, v, z, active))) return rc;
-			if ((rc = matvec_xf(t, z, w, active, mixed == 2))) return rc;
+			float *z = k->Z32 + (size_t)i * ldv;
+			if ((rc = op->precond32(op->ctx, v, z, active))) return rc;
+			if ((rc = op->matvec_xf(op->ctx, z, w, active, mixed == 2))) return rc;
 		} else {
-			double *z = t->Z + (size_t)i * ldv;
-			if ((rc = fg_precond(t, v, z, active))) return rc;
-			if ((rc = fg_matvec(t, z, w, active))) return rc;
+			double *z = k->Z + (size_t)i * ldv;
+			if (op->precond) {
+				if ((rc = op->precond(op->ctx, v, z, active))) return rc;
+			} else {
+				FG_TRY(cudaMemcpyAsync(z, v, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+			}
+			if ((rc = op->matvec(op->ctx, z, w, active))) return rc;
 		}
 		for (int j = 0; j <= i + 1; j++)
-			k_mgs<<<G, RED_TPB, 0, s>>>(V, ldv, n, i, j, t->H, ldh, t->partials, t->st);
-		k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(w, n, t->H + (i + 1) * ldh + i, t->st);
-		k_givens<<<1, 1, 0, s>>>(t->H, ldh, t->cs, t->sn, t->ge, i, kmax, t->st);
+			k_mgs<<<G, RED_TPB, 0, s>>>(V, ldv, n, i, j, k->H, ldh, k->partials, k->st);
+		k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(w, n, k->H + (i + 1) * ldh + i, k->st);
+		k_givens<<<1, 1, 0, s>>>(k->H, ldh, k->cs, k->sn, k->ge, i, kmax, k->st);
 	}
-	k_backsolve<<<1, 1, 0, s>>>(t->H, ldh, t->ge, t->gy, t->st);
-	if (mixed) k_update_x<float><<<fg_grid(n), FG_TPB, 0, s>>>(X, t->Z32, ldv, n, t->gy, t->st);
-	else k_update_x<double><<<fg_grid(n), FG_TPB, 0, s>>>(X, t->Z, ldv, n, t->gy, t->st);
+	k_backsolve<<<1, 1, 0, s>>>(k->H, ldh, k->ge, k->gy, k->st);
+	if (mixed) k_update_x<float><<<fg_grid(n), FG_TPB, 0, s>>>(X, k->Z32, ldv, n, k->gy, k->st);
+	else k_update_x<double><<<fg_grid(n), FG_TPB, 0, s>>>(X, k->Z, ldv, n, k->gy, k->st);
 	return (int)cudaGetLastError();
+}
+
+// ------------------------------------------- the transport context's view
+static int tr_matvec(void *c, const double *p, double *q, const int *a)
+{
+	return fg_matvec((femgpu_transport *)c, p, q, a);
+}
+static int tr_precond(void *c, const double *p, double *z, const int *a)
+{
+	return fg_precond((femgpu_transport *)c, p, z, a);
+}
+static int tr_precond32(void *c, const double *p, float *z, const int *a)
+{
+	return fg_precond32((femgpu_transport *)c, p, z, a);
+}
+static int tr_matvec_xf(void *c, const float *p, double *q, const int *a, int op32)
+{
+	return matvec_xf((femgpu_transport *)c, p, q, a, op32);
+}
+
+extern "C" void fg_transport_krylov(femgpu_transport *t, fg_krylov *k, fg_linop *op)
+{
+	k->n = t->neq; k->kmax = t->kmax; k->nblk = red_grid(t); k->ldv = t->ldv; k->stream = t->stream;
+	k->V = t->V; k->H = t->H; k->cs = t->cs; k->sn = t->sn; k->ge = t->ge; k->gy = t->gy;
+	k->Z = t->Z; k->Z32 = t->Z32; k->partials = t->partials; k->st = t->st; k->st_host = t->st_host;
+	op->ctx = t;
+	op->matvec = tr_matvec;
+	op->precond = tr_precond;
+	op->precond32 = tr_precond32;
+	op->matvec_xf = tr_matvec_xf;
+}
+
+extern "C" int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, int first)
+{
+	fg_krylov k;
+	fg_linop op;
+	(void)first;
+	fg_transport_krylov(t, &k, &op);
+	return fg_kry_pgmres_cycle(&k, &op, B, X);
+}
+
+extern "C" int fg_fgmres_cycle(femgpu_transport *t, const double *B, double *X, int mixed)
+{
+	fg_krylov k;
+	fg_linop op;
+	fg_transport_krylov(t, &k, &op);
+	return fg_kry_fgmres_cycle(&k, &op, B, X, mixed);
 }
 
 // out = a . b (deterministic), device scalar.
@@ -477,6 +530,12 @@ __global__ void __launch_bounds__(RED_TPB) k_dot(const double *a, const double *
 	part = block_sum(part, sh);
 	double tot;
 	if (last_block_total(part, partials, ticket, &tot, sh)) *out = tot;
+}
+
+extern "C" int fg_kry_dot(const fg_krylov *k, const double *a, const double *b, int n, double *out_dev)
+{
+	k_dot<<<k->nblk, RED_TPB, 0, k->stream>>>(a, b, n, k->partials, &k->st->ticket, out_dev);
+	return (int)cudaGetLastError();
 }
 
 extern "C" int fg_dot(femgpu_transport *t, const double *a, const double *b, int n, double *out_dev)

@@ -12,14 +12,6 @@
 #include "femgpu_host.h"
 #include "../csrc/fg_ebe.h"
 
-#define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) {                   \
-	fgh_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));     \
-	return FEMGPU_E_CUDA; } } while (0)
-#define KR(call) do { int r_ = (call); if (r_ > 0) {                                        \
-	fgh_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString((cudaError_t)r_)); \
-	return FEMGPU_E_CUDA; }                                                                 \
-	if (r_ < 0) { fgh_set_error("%s:%d %s: error %d", __FILE__, __LINE__, #call, r_); return r_; } \
-	} while (0)
 
 int femgpu_ebe_create(femgpu_ebe **out, int ndof, int nnodes, int nel, const int *vert,
 		const int *node_id, int neq)

@@ -1,0 +1,311 @@
+/*
+ * Host driver of the 2D Euler path: the control flow of Predictor_Old
+ * (00_CommonFiles/Time_Integration/Predictor_Old.c:46-132, multicorrector
+ * stopped after NonLinearMaxIter correctors as StopByIterations does,
+ * Criteria.c:25-31) around device kernels for the build
+ * (Build_M_K_F_SUPG), the nodal block-diagonal preconditioner, the block-EBE
+ * matvec and GMRES.  Plain C.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime_api.h>
+
+#include "femgpu.h"
+#include "femgpu_host.h"
+#include "../csrc/fg_euler.h"
+
+#define DM(ptr, bytes) do { int r_ = fgh_dmalloc((void **)&(ptr), (bytes)); if (r_) return r_; } while (0)
+
+void femgpu_euler_default_opts(femgpu_euler_opts *o)
+{
+	memset(o, 0, sizeof *o);
+	o->gamma = 1.4;
+	o->mach = 1.0;
+	o->alpha = 0.5;
+	o->dt = 1e-3;
+	o->stab_tol = 1e-6;
+	o->precond = FEMGPU_PREC_BLOCKDIAG;
+	o->solver = FEMGPU_PGMRES;
+	o->kmax = 30;
+	o->lmax = 100;
+	o->tol = 1e-8;
+	o->ncorr = 2;
+}
+
+/* ---- operator callbacks of the Krylov solver ---------------------------- */
+static int op_matvec(void *ctx, const double *p, double *q, const int *active)
+{
+	(void)active;
+	return fg_ebe_matvec(((femgpu_euler *)ctx)->ebe, p, q, 0);
+}
+
+static int op_precond(void *ctx, const double *p, double *z, const int *active)
+{
+	(void)active;
+	return fg_ebe_blockdiag_apply(((femgpu_euler *)ctx)->ebe, p, z, 0);
+}
+
+static void linop(femgpu_euler *c, fg_linop *op)
+{
+	memset(op, 0, sizeof *op);
+	op->ctx = c;
+	op->matvec = op_matvec;
+	op->precond = c->o.precond == FEMGPU_PREC_BLOCKDIAG ? op_precond : NULL;
+}
+
+static int uploadd(double **dst, const double *src, size_t n)
+{
+	int rc = fgh_dmalloc((void **)dst, sizeof(double) * n);
+	if (rc) return rc;
+	CK(cudaMemcpy(*dst, src, sizeof(double) * n, cudaMemcpyHostToDevice));
+	return 0;
+}
+
+static int create(femgpu_euler *c, const femgpu_euler_opts *o, int nnodes, const double *x, const double *y,
+                  int nel, const int *vert, const int *node_id, int neq, const double *upresc)
+{
+	size_t n1 = (size_t)neq + 1;
+	int i, rc;
+	c->o = *o;
+	c->nnodes = nnodes; c->nel = nel; c->neq = neq;
+	rc = femgpu_ebe_create(&c->ebe, 4, nnodes, nel, vert, node_id, neq);
+	if (rc) return rc;
+	CK(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking));
+	c->stream = c->own_stream;
+	KR(femgpu_ebe_set_stream(c->ebe, c->stream));
+	rc = uploadd(&c->x, x, (size_t)nnodes);
+	if (!rc) rc = uploadd(&c->y, y, (size_t)nnodes);
+	if (!rc) rc = uploadd(&c->upresc, upresc, 4 * (size_t)nnodes);
+	if (rc) return rc;
+	DM(c->u, sizeof(double) * n1);
+	DM(c->a, sizeof(double) * n1);
+	DM(c->R, sizeof(double) * n1);
+	DM(c->Da, sizeof(double) * n1);
+	DM(c->Re, sizeof(double) * 12 * (size_t)nel);
+	CK(cudaMemsetAsync(c->u, 0, sizeof(double) * n1, c->stream));
+	CK(cudaMemsetAsync(c->a, 0, sizeof(double) * n1, c->stream));
+	CK(cudaMemsetAsync(c->R, 0, sizeof(double) * n1, c->stream));
+	CK(cudaMemsetAsync(c->Da, 0, sizeof(double) * n1, c->stream));
+	rc = fgh_kry_alloc(&c->kry, neq, o->kmax, o->solver == FEMGPU_FGMRES ? 1 : 0, c->stream);
+	if (rc) return rc;
+	for (i = 0; i < 4; i++) CK(cudaEventCreate(&c->ev[i]));
+	CK(cudaStreamSynchronize(c->stream));
+	return 0;
+}
+
+int femgpu_euler_create(femgpu_euler **out, const femgpu_euler_opts *opts, int nnodes, const double *x,
+                        const double *y, int nel, const int *vert, const int *node_id, int neq,
+                        const double *upresc)
+{
+	femgpu_euler_opts o;
+	femgpu_euler *c;
+	int rc;
+	if (!out) return FEMGPU_E_ARG;
+	*out = NULL;
+	if (opts) o = *opts; else femgpu_euler_default_opts(&o);
+	if (nnodes <= 0 || nel <= 0 || neq <= 0 || !x || !y || !vert || !node_id || !upresc ||
+	    o.kmax < 1 || o.lmax < 1 || o.ncorr < 1 || !(o.dt > 0.0) || !(o.tol > 0.0) ||
+	    (o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_BLOCKDIAG) ||
+	    (o.solver != FEMGPU_PGMRES && o.solver != FEMGPU_FGMRES)) {
+		fgh_set_error("femgpu_euler_create: bad argument or option");
+		return FEMGPU_E_ARG;
+	}
+	c = calloc(1, sizeof *c);
+	if (!c) return FEMGPU_E_NOMEM;
+	rc = create(c, &o, nnodes, x, y, nel, vert, node_id, neq, upresc);
+	if (rc) { femgpu_euler_destroy(c); return rc; }
+	*out = c;
+	return 0;
+}
+
+void femgpu_euler_destroy(femgpu_euler *c)
+{
+	int i;
+	if (!c) return;
+	if (c->stream) cudaStreamSynchronize(c->stream);
+	if (c->ebe) femgpu_ebe_destroy(c->ebe);
+	{
+		void *p[] = { c->x, c->y, c->upresc, c->u, c->a, c->R, c->Da, c->Re };
+		for (i = 0; i < (int)(sizeof p / sizeof p[0]); i++) if (p[i]) cudaFree(p[i]);
+	}
+	fgh_kry_free(&c->kry);
+	for (i = 0; i < 4; i++) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+	if (c->own_stream) cudaStreamDestroy(c->own_stream);
+	free(c);
+}
+
+int femgpu_euler_set_stream(femgpu_euler *c, void *stream)
+{
+	if (!c) return FEMGPU_E_ARG;
+	CK(cudaStreamSynchronize(c->stream));
+	c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+	c->kry.stream = c->stream;
+	KR(femgpu_ebe_set_stream(c->ebe, c->stream));
+	return 0;
+}
+
+double *femgpu_euler_u_dev(femgpu_euler *c) { return c ? c->u : NULL; }
+femgpu_ebe *femgpu_euler_ebe(femgpu_euler *c) { return c ? c->ebe : NULL; }
+
+int femgpu_euler_last_times(const femgpu_euler *c, double *t)
+{
+	if (!c || !t) return FEMGPU_E_ARG;
+	memcpy(t, c->times, sizeof c->times);
+	return 0;
+}
+
+/* ---- Build / precond_setup / solver ------------------------------------- */
+int femgpu_euler_build_dev(femgpu_euler *c)
+{
+	if (!c) return FEMGPU_E_ARG;
+	KR(fg_euler_build(c, c->u, c->a));
+	c->built = 1;
+	c->have_bd = 0;
+	return 0;
+}
+
+int femgpu_euler_build(femgpu_euler *c, const double *u, const double *du, double *Ae_host, double *R_host)
+{
+	size_t n1;
+	if (!c) return FEMGPU_E_ARG;
+	n1 = (size_t)c->neq + 1;
+	if (u) CK(cudaMemcpyAsync(c->u, u, sizeof(double) * n1, cudaMemcpyHostToDevice, c->stream));
+	if (du) CK(cudaMemcpyAsync(c->a, du, sizeof(double) * n1, cudaMemcpyHostToDevice, c->stream));
+	KR(femgpu_euler_build_dev(c));
+	if (Ae_host)
+		CK(cudaMemcpyAsync(Ae_host, c->ebe->A, sizeof(double) * 144 * (size_t)c->nel, cudaMemcpyDeviceToHost,
+		                   c->stream));
+	if (R_host) CK(cudaMemcpyAsync(R_host, c->R, sizeof(double) * n1, cudaMemcpyDeviceToHost, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	return 0;
+}
+
+int femgpu_euler_precond_setup_dev(femgpu_euler *c)
+{
+	if (!c) return FEMGPU_E_ARG;
+	if (!c->built) { fgh_set_error("precond_setup before build"); return FEMGPU_E_NOT_BUILT; }
+	if (c->o.precond != FEMGPU_PREC_BLOCKDIAG) return 0;     /* NO_precond_setup */
+	KR(fg_ebe_blockdiag_setup(c->ebe));
+	c->ebe->have_bd = 1;
+	c->have_bd = 1;
+	if (c->o.solver == FEMGPU_PGMRES) KR(fg_ebe_blockdiag_apply(c->ebe, c->R, c->R, 0));
+	return 0;
+}
+
+int femgpu_euler_precond_setup(femgpu_euler *c, double *R_host)
+{
+	if (!c) return FEMGPU_E_ARG;
+	KR(femgpu_euler_precond_setup_dev(c));
+	if (R_host)
+		CK(cudaMemcpyAsync(R_host, c->R, sizeof(double) * ((size_t)c->neq + 1), cudaMemcpyDeviceToHost,
+		                   c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	return 0;
+}
+
+static int solve(femgpu_euler *c, const double *B, double *X, int *iters)
+{
+	fg_linop op;
+	double normb2;
+	int it = 0, rc;
+	if (c->o.precond == FEMGPU_PREC_BLOCKDIAG && !c->have_bd) {
+		fgh_set_error("solve before precond_setup");
+		return FEMGPU_E_NOT_BUILT;
+	}
+	if (iters) *iters = 0;
+	CK(cudaMemsetAsync(X, 0, sizeof(double) * ((size_t)c->neq + 1), c->stream));      /* pgmres.c:46 */
+	rc = fgh_kry_dot_host(&c->kry, B, B, c->neq, &normb2);
+	if (rc) return rc;
+	if (!(normb2 > 0.0)) return normb2 == 0.0 ? 0 : FEMGPU_E_BREAKDOWN;
+	linop(c, &op);
+	rc = fgh_kry_cycles(&c->kry, &op, B, X, c->o.solver == FEMGPU_PGMRES ? -1 : 0, c->o.tol * sqrt(normb2),
+	                    c->o.lmax, &it);
+	if (iters) *iters = it;
+	return rc;
+}
+
+int femgpu_euler_solve_dev(femgpu_euler *c, int *iters)
+{
+	if (!c) return FEMGPU_E_ARG;
+	return solve(c, c->R, c->Da, iters);
+}
+
+int femgpu_euler_solve(femgpu_euler *c, const double *B_host, double *X_host, int *iters)
+{
+	int rc;
+	if (!c) return FEMGPU_E_ARG;
+	if (B_host)
+		CK(cudaMemcpyAsync(c->R, B_host, sizeof(double) * ((size_t)c->neq + 1), cudaMemcpyHostToDevice,
+		                   c->stream));
+	rc = femgpu_euler_solve_dev(c, iters);
+	if (rc && rc != FEMGPU_E_NOT_CONVERGED) return rc;
+	if (X_host)
+		CK(cudaMemcpyAsync(X_host, c->Da, sizeof(double) * ((size_t)c->neq + 1), cudaMemcpyDeviceToHost,
+		                   c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	return rc;
+}
+
+/* ---- Predictor_Old ------------------------------------------------------- */
+static double elapsed(cudaEvent_t a, cudaEvent_t b)
+{
+	float ms = 0.0f;
+	cudaEventElapsedTime(&ms, a, b);
+	return 1e-3 * ms;
+}
+
+static int predictor(femgpu_euler *c, int nsteps, double *uhist, int *iters)
+{
+	const double c_pred = (1.0 - c->o.alpha) * c->o.dt, c_corr = c->o.alpha * c->o.dt;
+	size_t n1 = (size_t)c->neq + 1;
+	int step, i, rc;
+	memset(c->times, 0, sizeof c->times);
+	for (step = 0; step < nsteps; step++) {
+		KR(fg_euler_predict(c, c_pred));                                    /* :57-62   */
+		for (i = 0; i < c->o.ncorr; i++) {                                  /* :68-126  */
+			int it = 0;
+			CK(cudaEventRecord(c->ev[0], c->stream));
+			KR(femgpu_euler_build_dev(c));                                  /* :71      */
+			CK(cudaEventRecord(c->ev[1], c->stream));
+			KR(femgpu_euler_precond_setup_dev(c));                          /* :75      */
+			CK(cudaEventRecord(c->ev[2], c->stream));
+			rc = solve(c, c->R, c->Da, &it);                                /* :111     */
+			if (rc) return rc;
+			CK(cudaEventRecord(c->ev[3], c->stream));
+			KR(fg_euler_correct(c, c_corr));                                /* :115-116 */
+			CK(cudaEventSynchronize(c->ev[3]));
+			c->times[0] += elapsed(c->ev[0], c->ev[1]);
+			c->times[1] += elapsed(c->ev[1], c->ev[2]);
+			c->times[2] += elapsed(c->ev[2], c->ev[3]);
+			if (iters) iters[step * c->o.ncorr + i] = it;
+		}
+		if (uhist)
+			CK(cudaMemcpyAsync(uhist + (size_t)step * n1, c->u, sizeof(double) * n1, cudaMemcpyDeviceToHost,
+			                   c->stream));
+	}
+	CK(cudaStreamSynchronize(c->stream));
+	return 0;
+}
+
+int femgpu_euler_predictor_dev(femgpu_euler *c, int nsteps, int *iters)
+{
+	if (!c || nsteps < 0) return FEMGPU_E_ARG;
+	return predictor(c, nsteps, NULL, iters);
+}
+
+int femgpu_euler_predictor(femgpu_euler *c, double *u, int nsteps, double *uhist, int *iters)
+{
+	size_t n1;
+	int rc;
+	if (!c || nsteps < 0) return FEMGPU_E_ARG;
+	n1 = (size_t)c->neq + 1;
+	if (u) CK(cudaMemcpyAsync(c->u, u, sizeof(double) * n1, cudaMemcpyHostToDevice, c->stream));
+	CK(cudaMemsetAsync(c->a, 0, sizeof(double) * n1, c->stream));          /* a = 0 (mycalloc, :18) */
+	rc = predictor(c, nsteps, uhist, iters);
+	if (rc) return rc;
+	if (u) CK(cudaMemcpyAsync(u, c->u, sizeof(double) * n1, cudaMemcpyDeviceToHost, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	return 0;
+}

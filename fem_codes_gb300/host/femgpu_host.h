@@ -2,11 +2,25 @@
 #ifndef FEMGPU_HOST_H
 #define FEMGPU_HOST_H
 
+#include <cuda_runtime_api.h>
+
 #include "femgpu.h"
 
 #ifdef __cplusplus
 extern "C" {
 #endif
+
+/* Return FEMGPU_E_CUDA from the enclosing function on a CUDA runtime error
+ * (CK), or on a launcher's cudaError_t > 0 / pass its FEMGPU_E* < 0 (KR);
+ * the message goes to femgpu_last_error(). */
+#define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) {                   \
+	fgh_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));     \
+	return FEMGPU_E_CUDA; } } while (0)
+#define KR(call) do { int r_ = (call); if (r_ > 0) {                                        \
+	fgh_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString((cudaError_t)r_)); \
+	return FEMGPU_E_CUDA; }                                                                 \
+	if (r_ < 0) { fgh_set_error("%s:%d %s: error %d", __FILE__, __LINE__, #call, r_); return r_; } \
+	} while (0)
 
 /* Reverse Cuthill-McKee permutation, perm[new] = old. */
 int fgh_symrcm(int n, const int *IA, const int *JA, int *perm);
@@ -15,6 +29,21 @@ int fgh_bandwidth(int n, const int *IA, const int *JA);
 int fgh_levels(int n, const int *IA, const int *JA, int lower, int *rows, int **task,
                int *ntask, int *nlev);
 void fgh_set_error(const char *fmt, ...);
+int fgh_dmalloc(void **p, size_t bytes);
+
+/* Krylov workspace (fg_internal.h fg_krylov) for n unknowns and kmax basis
+ * vectors; zmode 0: no FGMRES Z, 1: FP64 Z, 2: FP32 Z. */
+struct fg_krylov;
+struct fg_linop;
+int fgh_kry_alloc(struct fg_krylov *k, int n, int kmax, int zmode, void *stream);
+void fgh_kry_free(struct fg_krylov *k);
+/* Restart cycles until rho <= eps or lmax cycles; kind -1: left-
+ * preconditioned pgmres, 0/1/2: FGMRES mixed mode.  Adds the inner
+ * iterations to *iters; FEMGPU_E_NOT_CONVERGED when lmax is reached. */
+int fgh_kry_cycles(const struct fg_krylov *k, const struct fg_linop *op, const double *B, double *X,
+                   int kind, double eps, int lmax, int *iters);
+/* ||B||^2 on the device, returned to the host (synchronises the stream). */
+int fgh_kry_dot_host(const struct fg_krylov *k, const double *a, const double *b, int n, double *out);
 
 #ifdef __cplusplus
 }

@@ -30,14 +30,6 @@ void fgh_set_error(const char *fmt, ...)
 
 const char *femgpu_last_error(void) { return g_err; }
 
-#define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) {                   \
-	fgh_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));     \
-	return FEMGPU_E_CUDA; } } while (0)
-#define KR(call) do { int r_ = (call); if (r_ > 0) {                                        \
-	fgh_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString((cudaError_t)r_)); \
-	return FEMGPU_E_CUDA; }                                                                 \
-	if (r_ < 0) { fgh_set_error("%s:%d %s: error %d", __FILE__, __LINE__, #call, r_); return r_; } \
-	} while (0)
 
 void femgpu_transport_default_opts(femgpu_transport_opts *o)
 {
@@ -55,7 +47,7 @@ void femgpu_transport_default_opts(femgpu_transport_opts *o)
 	o->ir_max = 30;
 }
 
-static int dmalloc(void **p, size_t bytes)
+int fgh_dmalloc(void **p, size_t bytes)
 {
 	cudaError_t e = cudaMalloc(p, bytes ? bytes : 8);
 	if (e != cudaSuccess) {
@@ -65,11 +57,11 @@ static int dmalloc(void **p, size_t bytes)
 	return 0;
 }
 
-#define DM(ptr, bytes) do { int r_ = dmalloc((void **)&(ptr), (bytes)); if (r_) return r_; } while (0)
+#define DM(ptr, bytes) do { int r_ = fgh_dmalloc((void **)&(ptr), (bytes)); if (r_) return r_; } while (0)
 
 static int upload(void **dst, const void *src, size_t bytes)
 {
-	int rc = dmalloc(dst, bytes);
+	int rc = fgh_dmalloc(dst, bytes);
 	if (rc) return rc;
 	CK(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
 	return 0;
@@ -466,33 +458,14 @@ static int dot_host(femgpu_transport *t, const double *a, const double *b, doubl
 	return 0;
 }
 
-/* Restart cycles until the cycle's residual estimate rho <= eps or lmax
- * cycles ran.  kind: -1 the reference's left-preconditioned pgmres, else the
- * FGMRES mixed-precision mode (0, 1 or 2).  Adds the inner iterations to
- * *iters. */
+/* Restart cycles of the context's solver (fgh_kry_cycles). */
 static int cycles(femgpu_transport *t, const double *B, double *X, int kind, double eps, int lmax,
                   int *iters)
 {
-	int l = 0, rc;
-	t->st_host->eps = eps;
-	t->st_host->total = 0;
-	t->st_host->err = 0;
-	t->st_host->ticket = 0;
-	t->st_host->active = 0;
-	CK(cudaMemcpyAsync(t->st, t->st_host, sizeof(fg_status), cudaMemcpyHostToDevice, t->stream));
-	do {
-		if (kind < 0) KR(fg_gmres_cycle(t, B, X, 0));
-		else KR(fg_fgmres_cycle(t, B, X, kind));
-		rc = sync_err(t);
-		if (rc) return rc;
-		l++;
-	} while (t->st_host->rho > eps && l < lmax);
-	*iters += t->st_host->total;
-	if (t->st_host->rho > eps) {
-		fgh_set_error("GMRES: %d restarts, rho %.3e > eps %.3e", l, t->st_host->rho, eps);
-		return FEMGPU_E_NOT_CONVERGED;
-	}
-	return 0;
+	fg_krylov k;
+	fg_linop op;
+	fg_transport_krylov(t, &k, &op);
+	return fgh_kry_cycles(&k, &op, B, X, kind, eps, lmax, iters);
 }
 
 static int gmres(femgpu_transport *t, const double *B, double *X, int *iters)

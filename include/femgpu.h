@@ -41,7 +41,8 @@ extern "C" {
 /* ---- options (the reference's parameter-deck strings, Preprocess.c:44-62) */
 enum femgpu_scheme   { FEMGPU_EBE = 0, FEMGPU_EDE = 1, FEMGPU_CSR = 2 };
 enum femgpu_reorder  { FEMGPU_REORDER_NOT = 0, FEMGPU_REORDER_SYMRCM = 1 };
-enum femgpu_precond  { FEMGPU_PREC_NOT = 0, FEMGPU_PREC_ILU0 = 1, FEMGPU_PREC_DIAG = 2 };
+enum femgpu_precond  { FEMGPU_PREC_NOT = 0, FEMGPU_PREC_ILU0 = 1, FEMGPU_PREC_DIAG = 2,
+                       FEMGPU_PREC_BLOCKDIAG = 3 /* Euler: nodal 4x4 blocks */ };
 enum femgpu_shock    { FEMGPU_SHOCK_CAU = 0, FEMGPU_SHOCK_YZBETA = 1 };
 enum femgpu_hshock   { FEMGPU_H_2SQRTAREA = 0, FEMGPU_H_SQRTAREA = 1,
                        FEMGPU_H_OPTION1 = 2, FEMGPU_H_OPTION2 = 3 };
@@ -202,6 +203,74 @@ int femgpu_ebe_blockdiag_setup(femgpu_ebe *ctx, double *F_host, double *BD_host,
 /* BlockDiag_precond.c / BlockDiagDOF3_precond.c: z = D^-1 p; p may equal z. */
 int femgpu_ebe_blockdiag_apply(femgpu_ebe *ctx, const double *p_host, double *z_host);
 int femgpu_ebe_blockdiag_apply_dev(femgpu_ebe *ctx, const double *p, double *z);
+
+/* ---- 2D Euler: SUPG+CAU build and predictor-multicorrector -------------
+ * 03_Euler_Equations/2D with StabilizationForm SUPG, ShockCapture CAU,
+ * MatrixVectorProductScheme EBE, TimeIntegration Predictor1 (Predictor_Old)
+ * and StopMulticorrection ITERATION.  Conservative unknowns per node in the
+ * order (rho, rho u, rho v, rho E).  Slip walls (v1Type == -1, rotation.c)
+ * are not supported: prescribe the wall-normal momentum instead. */
+typedef struct femgpu_euler_opts {
+	double gamma;        /* ratio of specific heats (gamma(), constant)     */
+	double mach;         /* reference Mach number (dimensionless only)       */
+	int dimensionless;   /* Dimensionless: 0 NO, 1 YES (Ax_Ay_calculations.c) */
+	double alpha;        /* Alpha of the predictor                           */
+	double dt;           /* DeltaT                                           */
+	double stab_tol;     /* StabilizationTolerance (CAU switch, Delta_CAU.c:71) */
+	int precond;         /* FEMGPU_PREC_NOT or FEMGPU_PREC_BLOCKDIAG         */
+	int solver;          /* femgpu_solver: PGMRES (reference) or FGMRES      */
+	int kmax, lmax;      /* KrylovBasisVectorsQuantity, SolverMaxIter        */
+	double tol;          /* SolverTolerance                                  */
+	int ncorr;           /* NonLinearMaxIter correctors per step (ITERATION) */
+} femgpu_euler_opts;
+
+void femgpu_euler_default_opts(femgpu_euler_opts *o);
+
+/* Device-resident Euler problem (replaces MatrixDataType / FemStructsType of
+ * EulerEquations.h:84-134 for the EBE scheme). */
+typedef struct femgpu_euler femgpu_euler;
+
+/* Preprocess for the EBE scheme (Preprocess.c, Fill_ID.c, Fill_LM.c):
+ *   x, y      [nnodes]     node coordinates
+ *   vert      [3*nel]      element vertices (0-based)
+ *   node_id   [4*nnodes]   equation of each (node, dof), -1 prescribed
+ *   neq                    number of equations
+ *   upresc    [4*nnodes]   prescribed values (rhopresc, v1presc, v2presc,
+ *                          epresc evaluated at the node; eval_U_dU.c:27-90) */
+int femgpu_euler_create(femgpu_euler **ctx, const femgpu_euler_opts *opts, int nnodes, const double *x,
+		const double *y, int nel, const int *vert, const int *node_id, int neq, const double *upresc);
+void femgpu_euler_destroy(femgpu_euler *ctx);
+int femgpu_euler_set_stream(femgpu_euler *ctx, void *stream);
+
+/* Build_M_K_F_SUPG (Build_M_K_F_SUPG.c:6-1072): element matrices
+ * Ae = Me + alpha dt Ke and residual R = -(Me dU + Ke U) assembled by lm, from
+ * u and du [neq+1] (host; NULL = the context's device u / a).  Ae_host
+ * [144*nel] and R_host [neq+1] receive copies (NULL skips). */
+int femgpu_euler_build(femgpu_euler *ctx, const double *u, const double *du, double *Ae_host,
+		double *R_host);
+int femgpu_euler_build_dev(femgpu_euler *ctx);
+/* precond_setup (BlockDiag_precond_EBE_setup.c:6-86 with PGMRES: R := D^-1 R;
+ * FGMRES leaves R unpreconditioned).  R_host [neq+1] receives R (NULL skips). */
+int femgpu_euler_precond_setup(femgpu_euler *ctx, double *R_host);
+int femgpu_euler_precond_setup_dev(femgpu_euler *ctx);
+/* solver (pgmres.c:4-211 with FemFunctions->mv = ebemvNDOF4): Da solves
+ * A Da = R.  B_host [neq+1] replaces R when non-NULL; X_host receives Da. */
+int femgpu_euler_solve(femgpu_euler *ctx, const double *B_host, double *X_host, int *iters);
+int femgpu_euler_solve_dev(femgpu_euler *ctx, int *iters);
+/* Predictor_Old (Time_Integration/Predictor_Old.c:46-132) for nsteps time
+ * steps of ncorr correctors from u (host [neq+1], in/out; NULL = the device
+ * state) with a = 0 at the start of every step.  uhist [nsteps*(neq+1)]
+ * receives u after each step and iters [nsteps*ncorr] the GMRES iterations
+ * of each corrector (NULL skips). */
+int femgpu_euler_predictor(femgpu_euler *ctx, double *u, int nsteps, double *uhist, int *iters);
+int femgpu_euler_predictor_dev(femgpu_euler *ctx, int nsteps, int *iters);
+/* Device pointers of the state vectors u, a, R, Da [neq+1] and the block
+ * EBE operator holding the element matrices. */
+double *femgpu_euler_u_dev(femgpu_euler *ctx);
+femgpu_ebe *femgpu_euler_ebe(femgpu_euler *ctx);
+/* Seconds spent in build, precond_setup and solve by the last
+ * femgpu_euler_predictor(_dev) call (t[3]). */
+int femgpu_euler_last_times(const femgpu_euler *ctx, double *t);
 
 /* ---- stateless device kernels (device pointers, stream as void*) -------- */
 /* csrmv.c:3-24 in FP64 / FP32 values. */

@@ -37,6 +37,29 @@ def test_build_targets_sm103a_only():
     assert b.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
+def test_element_builds_compiled_without_contraction():
+    """Translation units whose results must be bit-identical to the
+    reference (element builds and block operators) are compiled with
+    --fmad=false."""
+    from fem_codes_gb300 import build as b
+    assert {"build.cu", "ebe_block.cu", "euler_build.cu"} <= b.NO_FMA
+
+
+def test_euler_bad_options_rejected_without_gpu(lib):
+    import fem_codes_gb300 as fg
+    o = fg.EulerOpts()
+    lib.femgpu_euler_default_opts(ctypes.byref(o))
+    assert (o.gamma, o.alpha, o.precond, o.solver, o.ncorr) == (1.4, 0.5, 3, 0, 2)
+    o.ncorr = 0
+    h = ctypes.c_void_p()
+    x = np.zeros(3)
+    v = np.zeros(3, np.int32)
+    nid = np.zeros(12, np.int32)
+    rc = lib.femgpu_euler_create(ctypes.byref(h), ctypes.byref(o), 3, x.ctypes.data, x.ctypes.data, 1,
+                                 v.ctypes.data, nid.ctypes.data, 4, np.zeros(12).ctypes.data)
+    assert rc == -1 and not h.value
+
+
 def _pattern(nx, ny, perturb=0.0):
     m = structured_mesh(nx, ny, perturb=perturb)
     p = skew_problem(m)

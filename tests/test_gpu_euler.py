@@ -1,0 +1,139 @@
+"""GPU parity of the 2D Euler path (Build_M_K_F_SUPG + Delta_CAU element
+build, BlockDiag precond_setup, pgmres on the block EBE operator,
+Predictor_Old) against the reference's own outputs (tests/golden/eul_*.npz)
+and against the oracle on larger meshes.
+
+Bars: element matrices, residuals and the preconditioned residual are
+bit-identical (same operation order, no FMA contraction).  Solutions after
+GMRES agree to a relative 1e-8: the device reductions sum dot products in a
+different order than the reference's ddot, so the Krylov iterates differ in
+the last bits."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import pyoracle
+from fem_codes_gb300.mesh import euler_cfl_dt, refletido_problem, structured_mesh
+
+pytestmark = pytest.mark.gpu
+
+CASES = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "eul_*.npz")))
+SOL_RTOL = 1e-8
+
+
+def _load(name):
+    return dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+
+
+def _euler(g, **kw):
+    import fem_codes_gb300 as fg
+    args = dict(gamma=float(g["gamma"]), alpha=float(g["alpha"]), dt=float(g["dt"]),
+                stab_tol=float(g["stab_tol"]), kmax=int(g["kmax"]), lmax=int(g["lmax"]), tol=float(g["tol"]),
+                ncorr=int(g["ncorr"]))
+    args.update(kw)
+    return fg.Euler(g["x"], g["y"], g["vert"], g["node_id"], int(g["neq"]), g["upresc"], **args)
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_euler_build_bitexact_vs_reference(gpu_lib, name):
+    g = _load(name)
+    with _euler(g) as eu:
+        R, Ae = eu.Build(g["u"], g["du"], want_matrix=True)
+    assert np.array_equal(Ae, g["Ae"])
+    assert np.array_equal(R, g["R"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_euler_precond_setup_bitexact(gpu_lib, name):
+    """R := D^-1 R after the build (BlockDiag_precond_EBE_setup.c:82)."""
+    g = _load(name)
+    neq = int(g["neq"])
+    ref = pyoracle.block_ops(4, len(g["x"]), g["vert"], g["node_id"], neq, g["Ae"], np.zeros(neq + 1),
+                             np.zeros(neq + 1), g["R"])
+    with _euler(g) as eu:
+        eu.Build(g["u"], g["du"])
+        Rp = eu.precond_setup()
+    assert np.array_equal(Rp[:neq], ref["F"][:neq])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_euler_predictor_vs_reference(gpu_lib, name):
+    g = _load(name)
+    with _euler(g) as eu:
+        uh, its = eu.Predictor(g["u0"], int(g["nsteps"]))
+    assert _rel(uh, g["uhist"]) < SOL_RTOL
+    assert np.abs(its.astype(int) - g["iters"].astype(int)).max() <= 1
+
+
+def test_euler_build_large_vs_oracle(gpu_lib):
+    import fem_codes_gb300 as fg
+    m = structured_mesh(96, 24, lx=4.0, ly=1.0, perturb=0.25, seed=11)
+    pb = refletido_problem(m)
+    rng = np.random.default_rng(5)
+    u = pb.u0 * (1.0 + 0.08 * rng.uniform(-1, 1, pb.neq + 1))
+    du = 0.2 * rng.uniform(-1, 1, pb.neq + 1)
+    u[pb.neq] = du[pb.neq] = 0.0
+    dt = euler_cfl_dt(m, 5.0)
+    Ao, Ro = pyoracle.euler_build(m.x, m.y, m.vert, pb.node_id, pb.neq, pb.upresc, u, du, alpha=0.5, dt=dt,
+                                  stab_tol=1e-6)
+    with fg.Euler.from_problem(m, pb, alpha=0.5, dt=dt, stab_tol=1e-6) as eu:
+        R, Ae = eu.Build(u, du, want_matrix=True)
+    assert np.array_equal(Ae, Ao)
+    assert np.array_equal(R, Ro)
+
+
+def test_euler_dimensionless_vs_oracle(gpu_lib):
+    """dimensionless_Ax_Ay_calculations (Ax_Ay_calculations.c:3-52)."""
+    import fem_codes_gb300 as fg
+    m = structured_mesh(20, 6, lx=4.0, ly=1.0, perturb=0.2, seed=2)
+    pb = refletido_problem(m)
+    rng = np.random.default_rng(9)
+    u = pb.u0 * (1.0 + 0.05 * rng.uniform(-1, 1, pb.neq + 1))
+    du = 0.1 * rng.uniform(-1, 1, pb.neq + 1)
+    u[pb.neq] = du[pb.neq] = 0.0
+    Ao, Ro = pyoracle.euler_build(m.x, m.y, m.vert, pb.node_id, pb.neq, pb.upresc, u, du, alpha=0.5, dt=0.01,
+                                  stab_tol=1e-6, mach=0.8, dimensionless=True)
+    with fg.Euler.from_problem(m, pb, alpha=0.5, dt=0.01, stab_tol=1e-6, mach=0.8, dimensionless=True) as eu:
+        R, Ae = eu.Build(u, du, want_matrix=True)
+    assert np.array_equal(Ae, Ao)
+    assert np.array_equal(R, Ro)
+
+
+def test_euler_predictor_large_vs_oracle(gpu_lib):
+    import fem_codes_gb300 as fg
+    m = structured_mesh(64, 16, lx=4.0, ly=1.0)
+    pb = refletido_problem(m)
+    dt = euler_cfl_dt(m, 5.0)
+    uo, ito = pyoracle.euler_predictor(m.x, m.y, m.vert, pb.node_id, pb.neq, pb.upresc, pb.u0, 3, 2, dt=dt,
+                                       kmax=30, lmax=100, tol=1e-8)
+    with fg.Euler.from_problem(m, pb, dt=dt, kmax=30, lmax=100, tol=1e-8, ncorr=2) as eu:
+        uh, its = eu.Predictor(pb.u0, 3)
+    assert _rel(uh, uo) < SOL_RTOL
+    assert np.abs(its.astype(int) - ito.astype(int)).max() <= 1
+
+
+def test_euler_fgmres_matches_pgmres(gpu_lib):
+    """Right-preconditioned FGMRES (stops on the true residual) reaches the
+    same corrector solutions as the reference's left-preconditioned GMRES
+    when both solve tightly."""
+    g = _load(CASES[0])
+    with _euler(g, tol=1e-12, lmax=200) as a, _euler(g, tol=1e-12, lmax=200, solver="FGMRES") as b:
+        ua, _ = a.Predictor(g["u0"], 2)
+        ub, _ = b.Predictor(g["u0"], 2)
+    assert _rel(ub, ua) < 1e-7
+
+
+def test_euler_call_order(gpu_lib):
+    import fem_codes_gb300 as fg
+    g = _load(CASES[0])
+    with _euler(g) as eu:
+        with pytest.raises(fg.FemGpuError) as ei:
+            eu.precond_setup()
+        assert ei.value.code == -9
