@@ -33,7 +33,7 @@ ERRORS = {
 OPTS = {
     "scheme": {"EBE": 0, "EDE": 1, "CSR": 2},
     "reorder": {"NOT": 0, "SYMRCM": 1},
-    "precond": {"NOT": 0, "ILU0": 1, "DIAG": 2, "BLOCKDIAG": 3},
+    "precond": {"NOT": 0, "ILU0": 1, "DIAG": 2, "BLOCKDIAG": 3, "LEARNED": 4},
     "shock": {"CAU": 0, "YZBETA": 1},
     "hshock": {"2SQRTAREA": 0, "SQRTAREA": 1, "OPTION1": 2, "OPTION2": 3},
     "precision": {"FP64": 0, "MIXED": 1, "MIXED_IR": 2},
@@ -54,7 +54,7 @@ class Opts(ctypes.Structure):
                 ("shock", ctypes.c_int), ("hshock", ctypes.c_int), ("outflow", ctypes.c_int),
                 ("kmax", ctypes.c_int), ("lmax", ctypes.c_int), ("tol", ctypes.c_double),
                 ("nonlin_tol", ctypes.c_double), ("precision", ctypes.c_int), ("ir_max", ctypes.c_int),
-                ("solver", ctypes.c_int), ("inner_tol", ctypes.c_double)]
+                ("solver", ctypes.c_int), ("inner_tol", ctypes.c_double), ("stall_ratio", ctypes.c_double)]
 
 
 class EulerOpts(ctypes.Structure):
@@ -132,6 +132,31 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         f = getattr(L, name)
         f.argtypes = args
         f.restype = ctypes.c_int
+    L.femgpu_gnn_nparams.restype = ctypes.c_int
+    L.femgpu_gnn_nparams.argtypes = []
+    L.femgpu_gnn_destroy.argtypes = [_vp]
+    L.femgpu_gnn_destroy.restype = None
+    for name, args in {
+        "femgpu_gnn_create": [ctypes.POINTER(_vp), ctypes.c_int, _vp],
+        "femgpu_gnn_set_stream": [_vp, _vp],
+        "femgpu_gnn_set_params": [_vp, _vp],
+        "femgpu_gnn_get_params": [_vp, _vp],
+        "femgpu_gnn_get_grad": [_vp, _vp],
+        "femgpu_gnn_attach_csr": [_vp, ctypes.c_int, _vp, _vp, _vp],
+        "femgpu_gnn_attach_csr_dev": [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp],
+        "femgpu_gnn_apply": [_vp, _vp, _vp],
+        "femgpu_gnn_apply_dev": [_vp, _vp, _vp],
+        "femgpu_gnn_loss_grad_dev": [_vp, _vp, _vp, _vp, ctypes.c_int, _vp],
+        "femgpu_gnn_loss_grad": [_vp, _vp, _vp, _vp, _vp, _vp],
+        "femgpu_gnn_adam_step": [_vp, ctypes.c_float, ctypes.c_float],
+        "femgpu_gnn_set_loss": [_vp, ctypes.c_int],
+        "femgpu_transport_set_learned": [_vp, _vp],
+        "femgpu_transport_krylov_pairs": [_vp, ctypes.c_int, _vp, _vp, ctypes.c_int],
+        "femgpu_transport_csr_dev": [_vp, _vp, _vp, _vp],
+    }.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
     for name in ("femgpu_euler_u_dev", "femgpu_euler_ebe"):
         getattr(L, name).argtypes = [_vp]
         getattr(L, name).restype = _vp
@@ -161,7 +186,8 @@ class SSTransport:
     def __init__(self, x, y, node_type, vert, k, gamma, upresc, beta=None, const_beta=None,
                  fsrc=None, scheme="CSR", reorder="NOT", precond="ILU0", shock="CAU",
                  hshock="2sqrtArea", outflow=False, kmax=30, lmax=1000, tol=1e-8,
-                 nonlin_tol=0.0, precision="FP64", ir_max=30, solver="GMRES", inner_tol=1e-4):
+                 nonlin_tol=0.0, precision="FP64", ir_max=30, solver="GMRES", inner_tol=1e-4,
+                 stall_ratio=0.9):
         L = load()
         o = Opts()
         L.femgpu_transport_default_opts(ctypes.byref(o))
@@ -176,6 +202,7 @@ class SSTransport:
         o.ir_max = ir_max
         o.solver = OPTS["solver"][solver.upper()]
         o.inner_tol = inner_tol
+        o.stall_ratio = stall_ratio
         self.opts = o
         self._keep = [_f64(x), _f64(y), _i32(node_type), _i32(np.asarray(vert).reshape(-1)),
                       _f64(upresc)]
@@ -194,10 +221,10 @@ class SSTransport:
             raise FemGpuError(rc, "Preprocess")
         self._h = h
         self._L = L
-        info = np.zeros(6, np.int32)
+        info = np.zeros(7, np.int32)
         self._check(L.femgpu_transport_info(h, _ptr(info)), "info")
         self.neq, self.nnzero, self.nedge, self.bandwidth, self.ilu_levels_L, self.ilu_levels_U = \
-            (int(v) for v in info)
+            (int(v) for v in info[:6])
         self.scheme = scheme.upper()
 
     @classmethod
@@ -338,15 +365,41 @@ class SSTransport:
     def precond_setup_dev(self, tag=1):
         self._check(self._L.femgpu_transport_precond_setup_dev(self._h, int(tag)), "precond_setup_dev")
 
-    def solve_dev(self):
+    def solve_dev(self, raise_on_nonconvergence=True):
         it = ctypes.c_int(0)
         rc = self._L.femgpu_transport_solve_dev(self._h, ctypes.byref(it))
-        if rc:
+        if rc and (rc != -5 or raise_on_nonconvergence):
             raise FemGpuError(rc, "solve_dev")
         return it.value
 
+    def fell_back(self):
+        """True when the last learned-preconditioned solve switched to ILU(0)."""
+        info = np.zeros(7, np.int32)
+        self._check(self._L.femgpu_transport_info(self._h, _ptr(info)), "info")
+        return bool(info[6])
+
     def u_dev(self):
         return self._L.femgpu_transport_u_dev(self._h)
+
+    def set_learned(self, gnn):
+        """Use a :class:`fem_codes_gb300.learned.MeshGNN` as the
+        FEMGPU_PREC_LEARNED right preconditioner."""
+        self._gnn = gnn
+        self._check(self._L.femgpu_transport_set_learned(self._h, gnn.handle), "set_learned")
+
+    def csr_dev(self):
+        """(IA, JA, AA) device pointers of the CSR matrix."""
+        p = [_vp(), _vp(), _vp()]
+        self._check(self._L.femgpu_transport_csr_dev(self._h, *(ctypes.byref(q) for q in p)), "csr_dev")
+        return tuple(q.value for q in p)
+
+    def krylov_pairs(self, V_dev, Z_dev, ld, max_pairs):
+        """Copy the last FGMRES cycle's (v_i, M^-1 v_i) pairs into device
+        arrays; returns the count."""
+        n = self._L.femgpu_transport_krylov_pairs(self._h, int(max_pairs), _vp(V_dev), _vp(Z_dev), int(ld))
+        if n < 0:
+            raise FemGpuError(n, "krylov_pairs")
+        return n
 
 
 class Euler:

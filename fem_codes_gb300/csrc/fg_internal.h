@@ -1,7 +1,7 @@
 /*
  * Internal state and kernel-launch entry points of libfemgpu.
  * Shared by the CUDA translation units (*.cu) and the host C driver
- * (host/*.c); plain C, no CUDA-only types beyond cuda_runtime_api.h.
+ * (the C files under host/); plain C, no CUDA-only types beyond cuda_runtime_api.h.
  *
  * Device layout (all device memory, allocated once per context):
  *   mesh      x, y [nnodes] f64; node_type, node_id [nnodes] i32;
@@ -132,6 +132,10 @@ struct femgpu_transport {
 	int nblk_red;
 	fg_status *st;                  /* device status                         */
 	fg_status *st_host;             /* pinned mirror                         */
+
+	/* learned preconditioner (FEMGPU_PREC_LEARNED) */
+	struct femgpu_gnn *gnn;
+	int fell_back;                  /* this solve switched to ILU(0)         */
 
 	/* timing */
 	cudaEvent_t ev[4];

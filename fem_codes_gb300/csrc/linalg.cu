@@ -12,6 +12,7 @@
 // they are rounded exactly like the reference compiled without contraction.
 // ILU(0) lives in ilu.cu.
 #include "fg_common.cuh"
+#include "fg_gnn.h"
 #include <math.h>
 
 // ============================================================= matvecs ====
@@ -221,6 +222,7 @@ extern "C" int fg_diag_setup(femgpu_transport *t)
 extern "C" int fg_precond(femgpu_transport *t, const double *p, double *z, const int *active)
 {
 	cudaStream_t s = t->stream;
+	if (t->o.precond == FEMGPU_PREC_LEARNED && !t->fell_back) return fg_gnn_forward(t->gnn, p, z, 0, active);
 	if (t->o.precond == FEMGPU_PREC_NOT) {
 		if (p != z) FG_TRY(cudaMemcpyAsync(z, p, sizeof(double) * t->neq, cudaMemcpyDeviceToDevice, s));
 		return 0;

@@ -42,6 +42,10 @@ void fgh_kry_free(struct fg_krylov *k);
  * iterations to *iters; FEMGPU_E_NOT_CONVERGED when lmax is reached. */
 int fgh_kry_cycles(const struct fg_krylov *k, const struct fg_linop *op, const double *B, double *X,
                    int kind, double eps, int lmax, int *iters);
+/* The pieces of fgh_kry_cycles: reset the status for a solve to eps, then
+ * run one restart cycle and read the status back (k->st_host). */
+int fgh_kry_begin(const struct fg_krylov *k, double eps);
+int fgh_kry_cycle(const struct fg_krylov *k, const struct fg_linop *op, const double *B, double *X, int kind);
 /* ||B||^2 on the device, returned to the host (synchronises the stream). */
 int fgh_kry_dot_host(const struct fg_krylov *k, const double *a, const double *b, int n, double *out);
 

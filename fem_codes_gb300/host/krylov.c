@@ -63,21 +63,31 @@ static int sync_status(const fg_krylov *k)
 	return 0;
 }
 
-int fgh_kry_cycles(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int kind, double eps,
-                   int lmax, int *iters)
+int fgh_kry_begin(const fg_krylov *k, double eps)
 {
-	int l = 0, rc;
 	k->st_host->eps = eps;
 	k->st_host->total = 0;
 	k->st_host->err = 0;
 	k->st_host->ticket = 0;
 	k->st_host->active = 0;
 	CK(cudaMemcpyAsync(k->st, k->st_host, sizeof(fg_status), cudaMemcpyHostToDevice, k->stream));
+	return 0;
+}
+
+int fgh_kry_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int kind)
+{
+	if (kind < 0) KR(fg_kry_pgmres_cycle(k, op, B, X));
+	else KR(fg_kry_fgmres_cycle(k, op, B, X, kind));
+	return sync_status(k);
+}
+
+int fgh_kry_cycles(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int kind, double eps,
+                   int lmax, int *iters)
+{
+	int l = 0, rc;
+	if ((rc = fgh_kry_begin(k, eps))) return rc;
 	do {
-		if (kind < 0) KR(fg_kry_pgmres_cycle(k, op, B, X));
-		else KR(fg_kry_fgmres_cycle(k, op, B, X, kind));
-		rc = sync_status(k);
-		if (rc) return rc;
+		if ((rc = fgh_kry_cycle(k, op, B, X, kind))) return rc;
 		l++;
 	} while (k->st_host->rho > eps && l < lmax);
 	*iters += k->st_host->total;

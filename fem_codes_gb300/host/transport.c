@@ -45,6 +45,7 @@ void femgpu_transport_default_opts(femgpu_transport_opts *o)
 	o->nonlin_tol = 0.0;
 	o->precision = FEMGPU_FP64;
 	o->ir_max = 30;
+	o->stall_ratio = 0.9;
 }
 
 int fgh_dmalloc(void **p, size_t bytes)
@@ -125,7 +126,10 @@ int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts 
 	t = calloc(1, sizeof *t);
 	if (!t) return FEMGPU_E_NOMEM;
 	if (opts) t->o = *opts; else femgpu_transport_default_opts(&t->o);
-	if (t->o.scheme < 0 || t->o.scheme > 2 || t->o.precond < 0 || t->o.precond > 2 ||
+	if (t->o.scheme < 0 || t->o.scheme > 2 || t->o.precond < 0 || t->o.precond > 4 ||
+	    t->o.precond == FEMGPU_PREC_BLOCKDIAG ||
+	    (t->o.precond == FEMGPU_PREC_LEARNED && (t->o.scheme != FEMGPU_CSR || t->o.solver != FEMGPU_FGMRES ||
+	                                            t->o.precision != FEMGPU_FP64)) ||
 	    t->o.kmax < 1 || t->o.lmax < 1 || t->o.hshock < 0 || t->o.hshock > 3 ||
 	    t->o.precision < 0 || t->o.precision > 2 || t->o.solver < 0 || t->o.solver > 1 ||
 	    (t->o.precision != FEMGPU_FP64 && (t->o.solver != FEMGPU_FGMRES || t->o.scheme != FEMGPU_CSR)) ||
@@ -222,7 +226,7 @@ int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts 
 		DM(t->dr, sizeof(double) * ((size_t)neq + 1));
 	}
 
-	if (t->o.precond == FEMGPU_PREC_ILU0) {
+	if (t->o.precond == FEMGPU_PREC_ILU0 || t->o.precond == FEMGPU_PREC_LEARNED) {
 		t->ilu.n = neq;
 		t->ilu.nnz = t->nnz;
 		DM(t->ilu.LU, sizeof(double) * nA);
@@ -264,13 +268,15 @@ void femgpu_transport_destroy(femgpu_transport *t)
 	int i;
 	if (!t) return;
 	cudaStreamSynchronize(t->stream);
+	/* the network outlives this context: give it back its own stream */
+	if (t->gnn) femgpu_gnn_set_stream(t->gnn, NULL);
 	void *ptrs[] = { t->x, t->y, t->upresc, t->beta, t->fsrc, t->node_type, t->node_id, t->vert,
 		t->lm, t->ri_ptr, t->ri, t->IA, t->JA, t->sbe, t->diag, t->lm2, t->order, t->ec_ptr,
 		t->ec, t->e2_ptr, t->e2, t->A, t->ke, t->fe, t->A32, t->u, t->F, t->F0, t->invDiag,
 		t->invDiag32, t->ilu.LU, t->ilu.Dinv, t->V, t->H, t->cs, t->sn, t->ge, t->gy, t->w2,
 		t->Z, t->Z32, t->xr, t->dr, t->partials, t->st };
 	for (i = 0; i < (int)(sizeof ptrs / sizeof ptrs[0]); i++) if (ptrs[i]) cudaFree(ptrs[i]);
-	if (t->o.precond == FEMGPU_PREC_ILU0) fg_ilu_free(t);
+	if (t->o.precond == FEMGPU_PREC_ILU0 || t->o.precond == FEMGPU_PREC_LEARNED) fg_ilu_free(t);
 	if (t->st_host) cudaFreeHost(t->st_host);
 	for (i = 0; i < 4; i++) if (t->ev[i]) cudaEventDestroy(t->ev[i]);
 	if (t->own_stream) cudaStreamDestroy(t->own_stream);
@@ -283,6 +289,7 @@ int femgpu_transport_set_stream(femgpu_transport *t, void *stream)
 	if (!t) return FEMGPU_E_ARG;
 	CK(cudaStreamSynchronize(t->stream));
 	t->stream = stream ? (cudaStream_t)stream : t->own_stream;
+	if (t->gnn) KR(femgpu_gnn_set_stream(t->gnn, t->stream));
 	return 0;
 }
 
@@ -291,6 +298,7 @@ int femgpu_transport_info(const femgpu_transport *t, int *info)
 	if (!t || !info) return FEMGPU_E_ARG;
 	info[0] = t->neq; info[1] = t->nnz; info[2] = t->nedge; info[3] = t->bandwidth;
 	info[4] = t->sweeps.lo64.nlev; info[5] = t->sweeps.up64.nlev;
+	info[6] = t->fell_back;
 	return 0;
 }
 
@@ -362,6 +370,12 @@ int femgpu_transport_precond_setup_dev(femgpu_transport *t, int tag)
 	if (t->o.precond == FEMGPU_PREC_ILU0) {
 		KR(fg_ilu0_factor(t));
 		if (t->o.solver == FEMGPU_PGMRES) KR(fg_precond(t, t->F, t->F, NULL));
+	} else if (t->o.precond == FEMGPU_PREC_LEARNED) {
+		/* re-attach the network to the new matrix; ILU(0) is factored only
+		 * if a solve falls back to it */
+		if (!t->gnn) { fgh_set_error("learned preconditioner not set"); return FEMGPU_E_NOT_BUILT; }
+		KR(femgpu_gnn_attach_csr_dev(t->gnn, t->neq, t->nnz, t->IA, t->JA, t->A));
+		t->fell_back = 0;
 	} else if (t->o.precond == FEMGPU_PREC_DIAG) {
 		KR(fg_diag_setup(t));
 	}
@@ -468,6 +482,81 @@ static int cycles(femgpu_transport *t, const double *B, double *X, int kind, dou
 	return fgh_kry_cycles(&k, &op, B, X, kind, eps, lmax, iters);
 }
 
+/* FGMRES with the learned right preconditioner: a restart cycle that leaves
+ * the residual above stall_ratio times its value at the cycle's start
+ * switches the rest of the solve to ILU(0) (factored then), continuing from
+ * the current iterate; a breakdown (zero or NaN Arnoldi norm) restarts the
+ * solve from X = 0 with ILU(0). */
+static int learned_cycles(femgpu_transport *t, const double *B, double *X, double eps, double rho0,
+                          int *iters)
+{
+	fg_krylov k;
+	fg_linop op;
+	int l = 0, rc, done = 0;
+	double prev = rho0;
+	fg_transport_krylov(t, &k, &op);
+	if ((rc = fgh_kry_begin(&k, eps))) return rc;
+	do {
+		rc = fgh_kry_cycle(&k, &op, B, X, 0);
+		l++;
+		if (rc == FEMGPU_E_BREAKDOWN && !t->fell_back) {
+			done += k.st_host->total;
+			CK(cudaMemsetAsync(X, 0, sizeof(double) * (size_t)t->neq, t->stream));
+			KR(fg_ilu0_factor(t));
+			t->fell_back = 1;
+			prev = rho0;
+			if ((rc = fgh_kry_begin(&k, eps))) return rc;
+			continue;
+		}
+		if (rc) return rc;
+		if (k.st_host->rho <= eps) break;
+		if (!t->fell_back && !(k.st_host->rho <= t->o.stall_ratio * prev)) {
+			KR(fg_ilu0_factor(t));
+			t->fell_back = 1;
+		}
+		prev = k.st_host->rho;
+	} while (l < t->o.lmax);
+	*iters += done + k.st_host->total;
+	if (k.st_host->rho > eps) {
+		fgh_set_error("FGMRES (learned): %d restarts, rho %.3e > eps %.3e", l, k.st_host->rho, eps);
+		return FEMGPU_E_NOT_CONVERGED;
+	}
+	return 0;
+}
+
+int femgpu_transport_set_learned(femgpu_transport *t, femgpu_gnn *g)
+{
+	if (!t || !g || t->o.precond != FEMGPU_PREC_LEARNED) return FEMGPU_E_ARG;
+	KR(femgpu_gnn_set_stream(g, t->stream));
+	t->gnn = g;
+	t->factored = 0;
+	return 0;
+}
+
+int femgpu_transport_csr_dev(femgpu_transport *t, const int **IA, const int **JA, const double **AA)
+{
+	if (!t || t->o.scheme != FEMGPU_CSR || !IA || !JA || !AA) return FEMGPU_E_ARG;
+	*IA = t->IA;
+	*JA = t->JA;
+	*AA = t->A;
+	return 0;
+}
+
+int femgpu_transport_krylov_pairs(femgpu_transport *t, int max, double *V, double *Z, int ld)
+{
+	int i, m;
+	if (!t || max < 0 || !V || !Z || ld < t->neq || !t->Z) return FEMGPU_E_ARG;
+	m = t->st_host->inner < max ? t->st_host->inner : max;
+	for (i = 0; i < m; i++) {
+		CK(cudaMemcpyAsync(V + (size_t)i * ld, t->V + (size_t)i * t->ldv, sizeof(double) * (size_t)t->neq,
+		                   cudaMemcpyDeviceToDevice, t->stream));
+		CK(cudaMemcpyAsync(Z + (size_t)i * ld, t->Z + (size_t)i * t->ldv, sizeof(double) * (size_t)t->neq,
+		                   cudaMemcpyDeviceToDevice, t->stream));
+	}
+	CK(cudaStreamSynchronize(t->stream));
+	return m;
+}
+
 static int gmres(femgpu_transport *t, const double *B, double *X, int *iters)
 {
 	int n = t->neq, it = 0, rc;
@@ -487,6 +576,8 @@ static int gmres(femgpu_transport *t, const double *B, double *X, int *iters)
 	eps = t->o.tol * sqrt(normb2);                                               /* pgmres.c:49-53 */
 	if (t->o.solver == FEMGPU_PGMRES) {
 		rc = cycles(t, B, X, -1, eps, t->o.lmax, &it);
+	} else if (t->o.precond == FEMGPU_PREC_LEARNED) {
+		rc = learned_cycles(t, B, X, eps, sqrt(normb2), &it);
 	} else if (t->o.precision != FEMGPU_MIXED_IR) {
 		rc = cycles(t, B, X, t->o.precision == FEMGPU_MIXED ? 1 : 0, eps, t->o.lmax, &it);
 	} else {

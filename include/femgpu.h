@@ -42,7 +42,8 @@ extern "C" {
 enum femgpu_scheme   { FEMGPU_EBE = 0, FEMGPU_EDE = 1, FEMGPU_CSR = 2 };
 enum femgpu_reorder  { FEMGPU_REORDER_NOT = 0, FEMGPU_REORDER_SYMRCM = 1 };
 enum femgpu_precond  { FEMGPU_PREC_NOT = 0, FEMGPU_PREC_ILU0 = 1, FEMGPU_PREC_DIAG = 2,
-                       FEMGPU_PREC_BLOCKDIAG = 3 /* Euler: nodal 4x4 blocks */ };
+                       FEMGPU_PREC_BLOCKDIAG = 3, /* Euler: nodal 4x4 blocks            */
+                       FEMGPU_PREC_LEARNED = 4    /* graph network, ILU(0) fallback    */ };
 enum femgpu_shock    { FEMGPU_SHOCK_CAU = 0, FEMGPU_SHOCK_YZBETA = 1 };
 enum femgpu_hshock   { FEMGPU_H_2SQRTAREA = 0, FEMGPU_H_SQRTAREA = 1,
                        FEMGPU_H_OPTION1 = 2, FEMGPU_H_OPTION2 = 3 };
@@ -73,6 +74,8 @@ typedef struct femgpu_transport_opts {
 	int solver;          /* femgpu_solver                                    */
 	double inner_tol;    /* mixed precision: relative tolerance of each FP32 */
 	                     /* inner solve inside the FP64 refinement           */
+	double stall_ratio;  /* learned preconditioner: fall back to ILU(0) when */
+	                     /* a restart cycle leaves rho > stall_ratio * rho0  */
 } femgpu_transport_opts;
 
 void femgpu_transport_default_opts(femgpu_transport_opts *o);
@@ -106,7 +109,8 @@ void femgpu_transport_destroy(femgpu_transport *ctx);
 int femgpu_transport_set_stream(femgpu_transport *ctx, void *stream);
 
 /* Sizes: info[0]=neq, [1]=nnzero, [2]=nedge, [3]=bandwidth after reordering,
- * [4]=ILU levels (L), [5]=ILU levels (U). */
+ * [4]=ILU levels (L), [5]=ILU levels (U), [6]=1 when the last learned-
+ * preconditioned solve fell back to ILU(0) (7 ints). */
 int femgpu_transport_info(const femgpu_transport *ctx, int *info);
 
 /* Copies of the device-built structure, for parity checks against the
@@ -271,6 +275,57 @@ femgpu_ebe *femgpu_euler_ebe(femgpu_euler *ctx);
 /* Seconds spent in build, precond_setup and solve by the last
  * femgpu_euler_predictor(_dev) call (t[3]). */
 int femgpu_euler_last_times(const femgpu_euler *ctx, double *t);
+
+/* ---- learned preconditioner ----------------------------------------------
+ * No counterpart in the reference.  A mesh graph network (3 message-passing
+ * layers of width 32, FP32 weights, bf16 or FP32 activations) on the graph of
+ * a CSR matrix maps a residual r to a correction z ~ M^-1 r; it is trained on
+ * the GPU on (r, ILU(0) correction) pairs by hand-written forward and
+ * backward kernels and Adam, and serves as the right preconditioner of
+ * FGMRES (FEMGPU_PREC_LEARNED), with ILU(0) as the fallback when a restart
+ * cycle stalls.  Parameters: femgpu_gnn_nparams() floats. */
+typedef struct femgpu_gnn femgpu_gnn;
+int femgpu_gnn_nparams(void);
+/* theta NULL: all parameters zero. */
+int femgpu_gnn_create(femgpu_gnn **ctx, int bf16_activations, const float *theta);
+void femgpu_gnn_destroy(femgpu_gnn *ctx);
+int femgpu_gnn_set_stream(femgpu_gnn *ctx, void *stream);
+/* Set the parameters (resets the Adam state) / read parameters, gradient. */
+int femgpu_gnn_set_params(femgpu_gnn *ctx, const float *theta);
+int femgpu_gnn_get_params(femgpu_gnn *ctx, float *theta);
+int femgpu_gnn_get_grad(femgpu_gnn *ctx, float *grad);
+/* Attach the graph of an n-row CSR matrix (one diagonal entry per row,
+ * structurally symmetric, rows sorted): host arrays, or device arrays with
+ * nnz = IA[n]. */
+int femgpu_gnn_attach_csr(femgpu_gnn *ctx, int n, const int *IA, const int *JA, const double *AA);
+int femgpu_gnn_attach_csr_dev(femgpu_gnn *ctx, int n, int nnz, const int *IA, const int *JA,
+		const double *AA);
+/* z = N(r) over the attached graph (n entries). */
+int femgpu_gnn_apply(femgpu_gnn *ctx, const double *r_host, double *z_host);
+int femgpu_gnn_apply_dev(femgpu_gnn *ctx, const double *r, double *z);
+/* Forward and backward of L = ||z - t||^2 / ||t||^2 for one pair: z receives
+ * N(r), the gradient is stored (accumulate != 0 adds to it); loss (host, may
+ * be NULL: no synchronisation) receives L. */
+int femgpu_gnn_loss_grad_dev(femgpu_gnn *ctx, const double *r, const double *t, double *z, int accumulate,
+		double *loss);
+int femgpu_gnn_loss_grad(femgpu_gnn *ctx, const double *r_host, const double *t_host, double *loss,
+		float *grad_host, double *z_host);
+/* Training loss: 0 supervised ||z - t||^2/||t||^2 against the ILU(0)
+ * correction t (default), 1 residual ||A z - r||^2/||r||^2 (t unused), 2 the
+ * sum of both. */
+int femgpu_gnn_set_loss(femgpu_gnn *ctx, int kind);
+/* Adam (beta 0.9, 0.999, eps 1e-8) on the stored gradient scaled by gscale. */
+int femgpu_gnn_adam_step(femgpu_gnn *ctx, float lr, float gscale);
+/* Use ctx as the FEMGPU_PREC_LEARNED preconditioner of a CSR transport
+ * context (re-attached to the matrix at every precond_setup). */
+int femgpu_transport_set_learned(femgpu_transport *t, femgpu_gnn *ctx);
+/* Device pointers of the context's CSR matrix (IA [neq+1], JA [nnz], AA
+ * [nnz+1]); FEMGPU_E_ARG for EBE/EDE storage. */
+int femgpu_transport_csr_dev(femgpu_transport *t, const int **IA, const int **JA, const double **AA);
+/* Copy up to max (v_i, M^-1 v_i) pairs of the last FGMRES restart cycle
+ * (Arnoldi vectors and their preconditioned images, neq entries each) into
+ * device arrays V, Z with leading dimension ld; returns the count (>= 0). */
+int femgpu_transport_krylov_pairs(femgpu_transport *t, int max, double *V, double *Z, int ld);
 
 /* ---- stateless device kernels (device pointers, stream as void*) -------- */
 /* csrmv.c:3-24 in FP64 / FP32 values. */
