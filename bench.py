@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--precond", default="ILU0")
     ap.add_argument("--kmax", type=int, default=50)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="transport", choices=["transport", "euler"])
+    ap.add_argument("--euler-nx", type=int, default=1024)
+    ap.add_argument("--euler-ny", type=int, default=256)
+    ap.add_argument("--no-learned", action="store_true")
     return ap.parse_args()
 
 
@@ -293,11 +297,54 @@ def run_ours(a):
         line["cpu_baseline"] = cpu
     if clocks:
         line["clocks"] = clocks
+    T.close()
+    if not a.no_learned:
+        line["learned"] = learned_leg(m, p, a, s)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    T.close()
     if dist:
         dist.destroy_process_group()
+
+
+WEIGHTS = os.path.join(ROOT, "fem_codes_gb300", "weights", "gnn_transport.npy")
+
+
+def learned_leg(m, p, a, s, steps=1):
+    """Time to solution of the same Picard step with the learned
+    preconditioner (FGMRES(kmax), FP64 Arnoldi, bf16 network activations,
+    ILU(0) fallback on a stalled cycle); None without trained weights."""
+    import torch
+    import fem_codes_gb300 as fg
+    from fem_codes_gb300.learned import MeshGNN
+    if not os.path.exists(WEIGHTS):
+        return None
+    net = MeshGNN(np.load(WEIGHTS))
+    T = fg.SSTransport.from_problem(m, p, scheme="CSR", reorder="SYMRCM", precond="LEARNED", kmax=a.kmax,
+                                    lmax=400, tol=1e-8, solver="FGMRES", precision="FP64", stall_ratio=0.9)
+    T.set_stream(s.cuda_stream)
+    T.set_learned(net)
+    out = {}
+    try:
+        def step():
+            T.build_dev()
+            T.precond_setup_dev(2)
+            return T.solve_dev(raise_on_nonconvergence=False)
+        step()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        its = [step() for _ in range(steps)]
+        e1.record(s)
+        torch.cuda.synchronize()
+        out = {"ms_per_step": e0.elapsed_time(e1) / steps, "gmres_iters": its, "fell_back_to_ilu0": T.fell_back(),
+               "true_rel_residual": T.true_residual(),
+               "network": "3 message-passing layers, width 32, fp32 weights, bf16 activations",
+               "weights": "fem_codes_gb300/weights/gnn_transport.npy (python -m fem_codes_gb300.train_learned)"}
+    finally:
+        T.close()
+        net.close()
+    return out
 
 
 def kernel_times(T, s, a, reps=10):
@@ -386,9 +433,161 @@ def launches_estimate(a, iters):
     return tot
 
 
+# ------------------------------------------------------------------ Euler
+EULER_METRIC = "time per implicit time step (predictor + 2 correctors, GMRES to 1e-8)"
+
+
+def euler_setup(nx, ny):
+    from fem_codes_gb300.mesh import euler_cfl_dt, refletido_problem, structured_mesh
+    m = structured_mesh(nx, ny, lx=4.0, ly=1.0)
+    return m, refletido_problem(m), euler_cfl_dt(m, 5.0)
+
+
+def euler_config(a):
+    return {"workload": f"2D Euler REFLETIDO (oblique shock reflection, Mach 2.9 inflow, gamma 1.4) on a 4x1 "
+                        f"domain, {a.euler_nx}x{a.euler_ny} cells ({2 * a.euler_nx * a.euler_ny} triangles), "
+                        "SUPG+CAU, Predictor_Old alpha 0.5, 2 correctors, dt from CFL 5, EBE 12x12 FP64, "
+                        "BlockDiag-preconditioned GMRES(50) to 1e-8",
+            "nx": a.euler_nx, "ny": a.euler_ny, "kmax": 50,
+            "step": "one time step: predictor + 2 x (build + block-diagonal setup + GMRES + update)",
+            "l2": "inputs larger than L2 (element matrices 603 MB)"}
+
+
+def euler_cpu(steps=1, nx=256, ny=64):
+    """The oracle's predictor (reference algorithm, one core) on a smaller
+    REFLETIDO mesh: seconds per time step."""
+    from oracle import pyoracle
+    m, pb, dt = euler_setup(nx, ny)
+    t0 = time.perf_counter()
+    _, its = pyoracle.euler_predictor(m.x, m.y, m.vert, pb.node_id, pb.neq, pb.upresc, pb.u0, steps, 2, dt=dt,
+                                      kmax=50, lmax=100, tol=1e-8)
+    return (time.perf_counter() - t0) / steps, m.nel, its
+
+
+def run_euler(a):
+    import torch
+    import fem_codes_gb300 as fg
+    rank = int(os.environ.get("RANK", "0"))
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        sec, nel, its = euler_cpu()
+        full = 2 * a.euler_nx * a.euler_ny
+        ms = 1e3 * sec * full / nel
+        print(json.dumps({"impl": "reference", "metric": EULER_METRIC, "value": ms, "unit": "ms",
+                          "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms,
+                          "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": euler_config(a),
+                          "cpu_baseline": {"value": ms, "unit": "ms", "cores": 1, "kind": "port",
+                                           "sample": f"1 time step on the 256x64 mesh ({nel} triangles, GMRES "
+                                                     f"iters {its.reshape(-1).tolist()}), scaled by the element "
+                                                     f"count to {full} triangles"},
+                          "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        sec, nel, its = euler_cpu()
+        full = 2 * a.euler_nx * a.euler_ny
+        cpu = {"value": 1e3 * sec * full / nel, "unit": "ms", "cores": 1, "kind": "port",
+               "sample": f"1 time step on the 256x64 mesh ({nel} triangles, GMRES iters {its.reshape(-1).tolist()}),"
+                         f" scaled by the element count to {full} triangles"}
+    m, pb, dt = euler_setup(a.euler_nx, a.euler_ny)
+    E = fg.Euler.from_problem(m, pb, alpha=0.5, dt=dt, stab_tol=1e-6, kmax=50, lmax=100, tol=1e-8, ncorr=2)
+    s = torch.cuda.Stream()
+    E.set_stream(s.cuda_stream)
+    n1 = pb.neq + 1
+    L = E._L
+    u_h = torch.from_numpy(pb.u0.copy()).pin_memory()
+    # warm-up from the initial state through the host-buffer entry point; the
+    # device keeps the state for the timed steps, u_h the same state
+    rc = L.femgpu_euler_predictor(E.handle, ctypes.c_void_p(u_h.data_ptr()), a.warmup, None, None)
+    if rc:
+        raise fg.FemGpuError(rc, "warm-up")
+    torch.cuda.synchronize()
+    clk = Clocks()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    its = E.predictor_dev(a.steps)
+    e1.record(s)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1) / a.steps
+    phase = E.last_times()
+    # end to end: host state in, one step, host state out, per step
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        rc = L.femgpu_euler_predictor(E.handle, ctypes.c_void_p(u_h.data_ptr()), 1, None, None)
+        if rc:
+            raise fg.FemGpuError(rc, "e2e step")
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / a.steps
+    peak, peak_kind = peaks()
+    kt = euler_kernel_times(E, s, pb.neq, m.nel)
+    mv_bytes = m.nel * (144 * 8 + 48) + 2 * pb.neq * 8
+    mv_gbs = mv_bytes / (kt["ebemv"] * 1e-3) / 1e9
+    build_gbs = m.nel * (144 * 8 + 12 * 8 + 12) / (kt["build"] * 1e-3) / 1e9
+    line = {"metric": EULER_METRIC, "value": ms, "unit": "ms", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": euler_config(a),
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": n1 * 8, "d2h_bytes_per_step": n1 * 8},
+            "roofline": {"kernel": "k_ebemv_blk<4> (12x12 FP64 EBE matvec, row gather)", "bound": "hbm",
+                         "achieved": mv_gbs, "peak": peak, "unit": "GB/s", "frac": mv_gbs / peak,
+                         "traffic": read_traffic("euler_ebemv"),
+                         "note": "FP64 issue-bound on GB300 (288 FP64 ops per element, no FMA contraction)"},
+            "build": {"kernel": "k_euler_element", "ms": kt["build"],
+                      "elements_per_s": m.nel / (kt["build"] * 1e-3), "GB/s": build_gbs},
+            "phase_ms_per_step": {k: round(1e3 * v / a.steps, 3) for k, v in
+                                  zip(["build", "precond_setup", "solve"], phase)},
+            "gmres_iters": its.reshape(-1).tolist(), "neq": pb.neq, "nel": m.nel, "dt": dt}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if clocks:
+        line["clocks"] = clocks
+    E.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def euler_kernel_times(E, s, neq, nel, reps=10):
+    import torch
+    L = E._L
+    vp = ctypes.c_void_p
+    ebe = L.femgpu_euler_ebe(E.handle)
+    L.femgpu_ebe_matvec_dev.argtypes = [vp, vp, vp]
+    L.femgpu_ebe_matvec_dev.restype = ctypes.c_int
+    x = torch.randn(neq + 1, dtype=torch.float64, device="cuda")
+    y = torch.zeros_like(x)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def timeit(fn):
+        for _ in range(2):
+            fn()
+        tot = 0.0
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(s):
+                flush.zero_()
+                e0.record(s)
+                fn()
+                e1.record(s)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / reps
+
+    torch.cuda.synchronize()
+    s.wait_stream(torch.cuda.current_stream())
+    return {"ebemv": timeit(lambda: L.femgpu_ebe_matvec_dev(ebe, vp(x.data_ptr()), vp(y.data_ptr()))),
+            "build": timeit(lambda: L.femgpu_euler_build_dev(E.handle))}
+
+
 def main():
     a = parse()
-    if a.impl == "reference":
+    if a.workload == "euler":
+        run_euler(a)
+    elif a.impl == "reference":
         run_reference(a)
     else:
         run_ours(a)

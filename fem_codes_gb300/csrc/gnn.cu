@@ -18,6 +18,7 @@
 // per block into partial sums, then over blocks in block order
 // (deterministic).
 #include <algorithm>
+#include <type_traits>
 
 #include <cuda_bf16.h>
 
@@ -113,136 +114,188 @@ __global__ void __launch_bounds__(RTPB) k_gnn_psums(int n, const double *a, cons
 	if (threadIdx.x == 0) { part[2 * blockIdx.x] = s0; part[2 * blockIdx.x + 1] = s1; }
 }
 
-__global__ void k_gnn_fsums(int nblk, const double *part, double *out, const int *active)
+// One block of 256 threads: thread t adds partials t, t+256, ... in order,
+// then a fixed shuffle tree (deterministic for a given block count).
+__global__ void __launch_bounds__(RTPB) k_gnn_fsums(int nblk, const double *part, double *out, const int *active)
 {
 	if (active && !*active) return;
+	__shared__ double sh[32];
 	double s0 = 0.0, s1 = 0.0;
-	for (int b = 0; b < nblk; b++) { s0 += part[2 * b]; s1 += part[2 * b + 1]; }
-	out[0] = s0;
-	out[1] = s1;
+	for (int b = threadIdx.x; b < nblk; b += blockDim.x) { s0 += part[2 * b]; s1 += part[2 * b + 1]; }
+	s0 = blk_sum(s0, sh);
+	s1 = blk_sum(s1, sh);
+	if (threadIdx.x == 0) { out[0] = s0; out[1] = s1; }
 }
 
 // ------------------------------------------------------------------ forward
 // stats: [0] = s (rms of r, 1 if zero), [1] = dbar.
+// A warp takes 32 consecutive nodes: lane q computes node q's scaled inputs
+// (the FP64 arithmetic once per node), then for each node of the group the
+// lanes compute its 32 features (lane = feature) and store one 64-byte row.
 template <typename TA>
 __global__ void k_gnn_encode(int n, const double *r, const double *stats, const double *d,
                              const float *__restrict__ th, TA *h0, unsigned *mask0, float2 *x, const int *active)
 {
 	if (active && !*active) return;
-	__shared__ float sw[3 * W];
-	for (int k = threadIdx.x; k < 3 * W; k += blockDim.x) sw[k] = th[GNN_OFF_WE + k];
-	__syncthreads();
+	const int lane = threadIdx.x & 31;
+	const float w0 = th[GNN_OFF_WE + lane], w1 = th[GNN_OFF_WE + W + lane], b = th[GNN_OFF_BE + lane];
 	const double s = stats[0], dbar = stats[1];
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		float rh = (float)(r[i] / s);
-		float x1 = rh * (float)dbar / (float)d[i];
-		if (x) x[i] = make_float2(rh, x1);
-		unsigned m = 0;
-		#pragma unroll
-		for (int f = 0; f < W; f++) {
-			float pre = rh * sw[f] + x1 * sw[W + f] + sw[2 * W + f];
-			float h = pre > 0.0f ? pre : 0.0f;
-			m |= (pre > 0.0f ? 1u : 0u) << f;
-			h0[(size_t)i * W + f] = st_act<TA>(h);
+	int warps = (gridDim.x * blockDim.x) >> 5;
+	for (int g0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; g0 < n; g0 += warps * 32) {
+		int i = g0 + lane;
+		float rh = 0.0f, x1 = 0.0f;
+		if (i < n) {
+			rh = (float)(r[i] / s);
+			x1 = rh * (float)dbar / (float)d[i];
+			if (x) x[i] = make_float2(rh, x1);
 		}
-		if (mask0) mask0[i] = m;
+		unsigned mine = 0;
+		int cnt = min(32, n - g0);
+		for (int q = 0; q < cnt; q++) {
+			float a = __shfl_sync(0xffffffffu, rh, q), c = __shfl_sync(0xffffffffu, x1, q);
+			float pre = a * w0 + c * w1 + b;
+			unsigned m = __ballot_sync(0xffffffffu, pre > 0.0f);
+			if (lane == q) mine = m;
+			h0[(size_t)(g0 + q) * W + lane] = st_act<TA>(pre > 0.0f ? pre : 0.0f);
+		}
+		if (mask0 && i < n) mask0[i] = mine;
 	}
 }
 
 // m1_i = sum wA h_j, m2_i = sum wT h_j: one warp per node, lane = feature.
+// Quarter-warp per node (four nodes in flight per warp): lane l of group
+// l/8 owns features 4*(l%8) .. +4 and gathers them with one 8-byte (bf16) or
+// 16-byte (FP32) load per neighbour.
 template <typename TA>
 __global__ void k_gnn_agg(int n, const int *__restrict__ gptr, const int *__restrict__ gcol,
                           const float *__restrict__ wA, const float *__restrict__ wT, const TA *__restrict__ h,
                           TA *m1, TA *m2, const int *active)
 {
 	if (active && !*active) return;
-	int lane = threadIdx.x & 31;
-	int warps = (gridDim.x * blockDim.x) >> 5;
-	for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
-		float a1 = 0.0f, a2 = 0.0f;
-		int lo = __ldg(&gptr[i]), hi = __ldg(&gptr[i + 1]);
-		for (int p = lo; p < hi; p++) {
-			int j = __ldg(&gcol[p]);
-			float hv = ld_act(&h[(size_t)j * W + lane]);
-			a1 += __ldg(&wA[p]) * hv;
-			a2 += __ldg(&wT[p]) * hv;
+	typedef typename std::conditional<sizeof(TA) == 2, uint2, uint4>::type V4;
+	const int lane = threadIdx.x & 31, sub = lane >> 3, fl = (lane & 7) * 4;
+	int groups = (gridDim.x * blockDim.x) >> 3;
+	for (int i = ((blockIdx.x * blockDim.x + threadIdx.x) >> 3); i - sub < n; i += groups) {
+		float a1[4] = {0.0f, 0.0f, 0.0f, 0.0f}, a2[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+		if (i < n) {
+			int lo = __ldg(&gptr[i]), hi = __ldg(&gptr[i + 1]);
+			#pragma unroll 2
+			for (int p = lo; p < hi; p++) {
+				int j = __ldg(&gcol[p]);
+				float wa = __ldg(&wA[p]), wt = __ldg(&wT[p]);
+				V4 raw = __ldg(reinterpret_cast<const V4 *>(&h[(size_t)j * W + fl]));
+				const TA *v = reinterpret_cast<const TA *>(&raw);
+				#pragma unroll
+				for (int q = 0; q < 4; q++) {
+					float hv = ld_act(&v[q]);
+					a1[q] += wa * hv;
+					a2[q] += wt * hv;
+				}
+			}
+			V4 o1, o2;
+			TA *p1 = reinterpret_cast<TA *>(&o1), *p2 = reinterpret_cast<TA *>(&o2);
+			#pragma unroll
+			for (int q = 0; q < 4; q++) { p1[q] = st_act<TA>(a1[q]); p2[q] = st_act<TA>(a2[q]); }
+			*reinterpret_cast<V4 *>(&m1[(size_t)i * W + fl]) = o1;
+			*reinterpret_cast<V4 *>(&m2[(size_t)i * W + fl]) = o2;
 		}
-		m1[(size_t)i * W + lane] = st_act<TA>(a1);
-		m2[(size_t)i * W + lane] = st_act<TA>(a2);
 	}
 }
 
-// h_out = h + relu(Wh^T h + W1^T m1 + W2^T m2 + b) on tiles of 64 nodes;
-// thread t: node t/4, outputs 8*(t%4) .. +8.
+// h_out = h + relu(Wh^T h + W1^T m1 + W2^T m2 + b) on tiles of UTILE = 128
+// nodes; thread t computes outputs 8*(t%4) .. +8 of nodes t/4 + 64 q (q < 2),
+// so each shared-memory weight load feeds two nodes.  Inputs are staged as
+// FP32 rows of 96 (+1 pad) in shared memory with 16-byte global loads.
+#define UTILE 128
+#define UNODE (UTILE / (UPD_TPB / 4))
 template <typename TA>
 __global__ void __launch_bounds__(UPD_TPB) k_gnn_update(int n, const float *__restrict__ th, const TA *h,
 		const TA *m1, const TA *m2, TA *hout, unsigned *mask, const int *active)
 {
 	if (active && !*active) return;
-	__shared__ __align__(16) float sW[3 * W * W + W];
-	__shared__ float sin_[TILE * PAD];
+	extern __shared__ __align__(16) float dyn[];
+	float *sW = dyn;                                   // [3*W*W + W]
+	float *sin_ = dyn + 3 * W * W + W;                 // [UTILE][PAD]
 	for (int k = threadIdx.x; k < 3 * W * W + W; k += blockDim.x) sW[k] = th[k];
 	const int t = threadIdx.x, node = t >> 2, fo = (t & 3) * 8;
-	int ntile = (n + TILE - 1) / TILE;
+	constexpr int VEC = 16 / sizeof(TA);               // elements per 16-byte load
+	int ntile = (n + UTILE - 1) / UTILE;
 	for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
-		int base = tile * TILE;
+		int base = tile * UTILE;
 		__syncthreads();
-		for (int e = t; e < TILE * 3 * W; e += blockDim.x) {
-			int nd = e / (3 * W), k = e - nd * 3 * W, i = base + nd;
-			float v = 0.0f;
+		for (int e = t; e < UTILE * 3 * W / VEC; e += blockDim.x) {
+			int nd = e / (3 * W / VEC), kv = (e - nd * (3 * W / VEC)) * VEC, i = base + nd;
+			const TA *src = kv < W ? h : (kv < 2 * W ? m1 : m2);
+			float *dst = &sin_[nd * PAD + kv];
 			if (i < n) {
-				const TA *src = k < W ? h : (k < 2 * W ? m1 : m2);
-				v = ld_act(&src[(size_t)i * W + (k & (W - 1))]);
+				uint4 raw = *reinterpret_cast<const uint4 *>(&src[(size_t)i * W + (kv & (W - 1))]);
+				const TA *v = reinterpret_cast<const TA *>(&raw);
+				#pragma unroll
+				for (int q = 0; q < VEC; q++) dst[q] = ld_act(&v[q]);
+			} else {
+				#pragma unroll
+				for (int q = 0; q < VEC; q++) dst[q] = 0.0f;
 			}
-			sin_[nd * PAD + k] = v;
 		}
 		__syncthreads();
-		float acc[8];
+		float acc[UNODE][8];
 		#pragma unroll
-		for (int j = 0; j < 8; j++) acc[j] = sW[3 * W * W + fo + j];
-		const float *in = &sin_[node * PAD];
+		for (int q = 0; q < UNODE; q++)
+			#pragma unroll
+			for (int j = 0; j < 8; j++) acc[q][j] = sW[3 * W * W + fo + j];
 		#pragma unroll 4
 		for (int k = 0; k < 3 * W; k++) {
-			float v = in[k];
 			const float4 *wr = reinterpret_cast<const float4 *>(&sW[k * W + fo]);
 			float4 w0 = wr[0], w1 = wr[1];
-			acc[0] += v * w0.x; acc[1] += v * w0.y; acc[2] += v * w0.z; acc[3] += v * w0.w;
-			acc[4] += v * w1.x; acc[5] += v * w1.y; acc[6] += v * w1.z; acc[7] += v * w1.w;
+			#pragma unroll
+			for (int q = 0; q < UNODE; q++) {
+				float v = sin_[(node + 64 * q) * PAD + k];
+				acc[q][0] += v * w0.x; acc[q][1] += v * w0.y; acc[q][2] += v * w0.z; acc[q][3] += v * w0.w;
+				acc[q][4] += v * w1.x; acc[q][5] += v * w1.y; acc[q][6] += v * w1.z; acc[q][7] += v * w1.w;
+			}
 		}
-		int i = base + node;
-		unsigned bits = 0;
 		#pragma unroll
-		for (int j = 0; j < 8; j++) {
-			float u = acc[j];
-			bits |= (u > 0.0f ? 1u : 0u) << (fo + j);
-			if (i < n) hout[(size_t)i * W + fo + j] = st_act<TA>(in[fo + j] + (u > 0.0f ? u : 0.0f));
+		for (int q = 0; q < UNODE; q++) {
+			int nd = node + 64 * q, i = base + nd;
+			const float *in = &sin_[nd * PAD];
+			unsigned bits = 0;
+			#pragma unroll
+			for (int j = 0; j < 8; j++) {
+				float u = acc[q][j];
+				bits |= (u > 0.0f ? 1u : 0u) << (fo + j);
+				if (i < n) hout[(size_t)i * W + fo + j] = st_act<TA>(in[fo + j] + (u > 0.0f ? u : 0.0f));
+			}
+			bits |= __shfl_xor_sync(0xffffffffu, bits, 1);
+			bits |= __shfl_xor_sync(0xffffffffu, bits, 2);
+			if (mask && i < n && (t & 3) == 0) mask[i] = bits;
 		}
-		bits |= __shfl_xor_sync(0xffffffffu, bits, 1);
-		bits |= __shfl_xor_sync(0xffffffffu, bits, 2);
-		if (mask && i < n && (t & 3) == 0) mask[i] = bits;
 	}
 }
 
-// z_i = s (Wd . h_i + bd) dbar / d_i.
+// z_i = s (Wd . h_i + bd) dbar / d_i: a warp reduces the rows of 32
+// consecutive nodes (lane = feature), lane q keeps node q's sum and does its
+// FP64 scaling (once per node).
 template <typename TA>
 __global__ void k_gnn_decode(int n, const TA *h, const float *__restrict__ th, const double *stats,
                              const double *d, double *z, const int *active)
 {
 	if (active && !*active) return;
-	__shared__ float sw[W + 1];
-	for (int k = threadIdx.x; k < W + 1; k += blockDim.x) sw[k] = th[GNN_OFF_WD + k];
-	__syncthreads();
+	const int lane = threadIdx.x & 31;
+	const float wd = th[GNN_OFF_WD + lane], bd = th[GNN_OFF_BD];
 	const double s = stats[0], dbar = stats[1];
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		float y = 0.0f;
-		#pragma unroll
-		for (int f = 0; f < W; f++) y += ld_act(&h[(size_t)i * W + f]) * sw[f];
-		y += sw[W];
-		z[i] = s * (double)y * dbar / d[i];
+	int warps = (gridDim.x * blockDim.x) >> 5;
+	for (int g0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; g0 < n; g0 += warps * 32) {
+		int cnt = min(32, n - g0);
+		float mine = 0.0f;
+		for (int q = 0; q < cnt; q++) {
+			float y = fg_warp_sumf(ld_act(&h[(size_t)(g0 + q) * W + lane]) * wd);
+			if (lane == q) mine = y;
+		}
+		int i = g0 + lane;
+		if (i < n) z[i] = s * (double)(mine + bd) * dbar / d[i];
 	}
 }
 
-// ----------------------------------------------------------------- backward
 // Loss gradients dL/dz: supervised (ILU target) 2 (z - t) / sum t^2, and
 // residual 2 A^T (A z - v) / sum v^2 with A = diag(d) (I + W) from the graph
 // (a_ij = d_i wA_ij; (A^T y)_j = d_j y_j + sum_q wT[q] d_col y_col).
@@ -487,6 +540,19 @@ __global__ void k_gnn_stats(const double *sums, int n, double *stats, const int 
 __global__ void k_gnn_dbar(const double *sums, int n, double *stats) { stats[1] = sums[0] / n; }
 
 // ---------------------------------------------------------------- launchers
+#define UPD_SMEM ((3 * W * W + W + UTILE * PAD) * (int)sizeof(float))
+
+static int update_attrs()
+{
+	static int done = 0;
+	if (!done) {
+		FG_TRY(cudaFuncSetAttribute(k_gnn_update<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM));
+		FG_TRY(cudaFuncSetAttribute(k_gnn_update<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                            UPD_SMEM));
+		done = 1;
+	}
+	return 0;
+}
 static int nb(long long n, int tpb, int cap)
 {
 	return (int)std::max<long long>(1, std::min<long long>((n + tpb - 1) / tpb, cap));
@@ -496,7 +562,7 @@ static void sums(fg_gnn *g, int n, const double *a, const double *b, int absval,
                  const int *active = nullptr)
 {
 	k_gnn_psums<<<GNN_RED_BLOCKS, RTPB, 0, g->stream>>>(n, a, b, absval, g->rpart, active);
-	k_gnn_fsums<<<1, 1, 0, g->stream>>>(GNN_RED_BLOCKS, g->rpart, out, active);
+	k_gnn_fsums<<<1, RTPB, 0, g->stream>>>(GNN_RED_BLOCKS, g->rpart, out, active);
 }
 
 extern "C" int fg_gnn_graph(fg_gnn *g, int n, const int *IA, const int *JA, const double *AA)
@@ -515,6 +581,7 @@ static int forward_t(fg_gnn *g, const double *r, double *z, int train, const int
 	cudaStream_t s = g->stream;
 	int n = g->n;
 	TA **H = (TA **)g->h, **M1 = (TA **)g->m1, **M2 = (TA **)g->m2;
+	FG_TRY((cudaError_t)update_attrs());
 	sums(g, n, r, nullptr, 0, g->sums, active);
 	k_gnn_stats<<<1, 1, 0, s>>>(g->sums, n, g->stats, active);
 	k_gnn_encode<TA><<<nb(n, 256, 16 * FG_SMS), 256, 0, s>>>(n, r, g->stats, g->d, g->theta, H[0],
@@ -523,14 +590,15 @@ static int forward_t(fg_gnn *g, const double *r, double *z, int train, const int
 	for (int l = 0; l < GNN_LAYERS; l++) {
 		int cur = train ? l : (l & 1), nxt = train ? l + 1 : ((l + 1) & 1);
 		int ml = train ? l : 0;
-		k_gnn_agg<TA><<<nb(32LL * n, 256, 32 * FG_SMS), 256, 0, s>>>(n, g->gptr, g->gcol, g->wA, g->wT, H[cur],
+		k_gnn_agg<TA><<<nb(8LL * n, 256, 32 * FG_SMS), 256, 0, s>>>(n, g->gptr, g->gcol, g->wA, g->wT, H[cur],
 		                                                            M1[ml], M2[ml], active);
-		k_gnn_update<TA><<<nb(n, TILE, 4 * FG_SMS), UPD_TPB, 0, s>>>(n, g->theta + GNN_OFF_L(l), H[cur], M1[ml],
+		k_gnn_update<TA><<<nb(n, UTILE, 4 * FG_SMS), UPD_TPB, UPD_SMEM, s>>>(n, g->theta + GNN_OFF_L(l), H[cur], M1[ml],
 		                                                             M2[ml], H[nxt],
 		                                                             train ? g->mask[l + 1] : nullptr, active);
 	}
 	int last = train ? GNN_LAYERS : (GNN_LAYERS & 1);
-	k_gnn_decode<TA><<<nb(n, 256, 16 * FG_SMS), 256, 0, s>>>(n, H[last], g->theta, g->stats, g->d, z, active);
+	k_gnn_decode<TA><<<nb(n, 256, 16 * FG_SMS), 256, 0, s>>>(n, H[last], g->theta, g->stats, g->d, z,
+	                                                                active);
 	return (int)cudaGetLastError();
 }
 
