@@ -188,3 +188,54 @@ def euler_cfl_dt(mesh: Mesh, cfl: float = 5.0, speed: float = 2.9, sound: float 
     cell size (the reference's decks give dt directly)."""
     h = min(float(mesh.x.max() - mesh.x.min()) / mesh.nx, float(mesh.y.max() - mesh.y.min()) / mesh.ny)
     return cfl * h / (speed + sound)
+
+
+@dataclasses.dataclass
+class NSProblem:
+    """A steady incompressible Navier-Stokes problem: numbering node_id
+    [nnodes, 3] (u, v, p; -1 prescribed; Fill_ID.c numbers node by node),
+    prescribed values upresc [nnodes, 3], nodal body force f [nnodes, 2],
+    Reynolds number and the reference velocity of the local Reynolds number."""
+    name: str
+    node_id: np.ndarray
+    neq: int
+    upresc: np.ndarray
+    f: np.ndarray
+    re: float
+    velmax: float
+
+
+def cavity_lid(x: float, y: float) -> float:
+    """CAVITY_v1presc.c: u = 1 on the lid y = 1 with cosine ramps over
+    x < 0.1 and x > 0.9, 0 elsewhere (evaluated with the C library's cos)."""
+    pi, eps1 = 3.14159265359, 0.1
+    eps2 = 1.0 - eps1
+    if abs(y - 1.0) <= 1e-15:
+        if x < eps1:
+            c = 1 - math.cos((eps1 - x) * pi / eps1)
+            return 1.0 - 0.25 * c * c
+        if x > eps2:
+            c = 1 - math.cos((x - eps2) * pi / eps1)
+            return 1.0 - 0.25 * c * c
+        return 1.0
+    return 0.0
+
+
+def cavity_problem(mesh: Mesh, re: float = 1000.0, lid: str = "smooth") -> NSProblem:
+    """Lid-driven cavity on the unit square: velocity prescribed on the whole
+    boundary (the lid by CAVITY_v1presc.c, or u = 1 on the whole lid with
+    lid="unit"), pressure pinned to 0 at node 0 (the corner x = y = 0)."""
+    x, y = mesh.x, mesh.y
+    bnd = (x == x.min()) | (x == x.max()) | (y == y.min()) | (y == y.max())
+    presc = np.zeros((mesh.nnodes, 3), dtype=bool)
+    presc[bnd, 0:2] = True
+    presc[0, 2] = True
+    node_id = np.full((mesh.nnodes, 3), -1, np.int32)
+    neq = int((~presc).sum())
+    node_id[~presc] = np.arange(neq, dtype=np.int32)
+    upresc = np.zeros((mesh.nnodes, 3))
+    if lid == "unit":
+        upresc[:, 0] = np.where(np.abs(y - 1.0) <= 1e-15, 1.0, 0.0)
+    else:
+        upresc[:, 0] = [cavity_lid(float(a), float(b)) for a, b in zip(x, y)]
+    return NSProblem("CAVITY", node_id, neq, upresc, np.zeros((mesh.nnodes, 2)), float(re), 1.0)

@@ -146,6 +146,30 @@ void orc_euler_build(const orc_euler *p, const double *u, const double *du, doub
 int orc_euler_predictor(const orc_euler *p, int kmax, int lmax, double tol, int nsteps, int ncorr,
                         double *u, double *uhist, int *iters);
 
+/* ---- steady Navier-Stokes (04_SS_NavierStokes_Equations/2D) ------------- */
+typedef struct {
+	int nnodes, nel, neq;
+	const double *x, *y;          /* [nnodes]                                   */
+	const int *vert;              /* [3*nel]                                    */
+	const int *node_id;           /* [3*nnodes] equation of (node, u|v|p) or -1 */
+	const double *upresc;         /* [3*nnodes] prescribed (u, v, p)            */
+	const double *f;              /* [2*nnodes] body force at the nodes         */
+	double re, velmax;
+} orc_ns;
+
+/* Build_K_F_MS.c:8-1190 (the branch it executes): Ae [nel*81], F [neq+1];
+ * first != 0 for the first build of a run; dold, nold [nel] are the
+ * per-element stabilisation state (delta_old, normres_old), updated. */
+void orc_ns_build(const orc_ns *p, const double *u, int first, double *dold, double *nold, double *Ae,
+                  double *F);
+/* eta_newton.c:5-68 given ||F||, ||Fold||. */
+double orc_eta_newton(int ecase, double nF, double nFold, double etaold, int pricek, int it, double talnl,
+                      double eta0);
+/* Process.c:62-194 from u = 0 with BlockDiagDOF3 + pgmres, at most maxit
+ * Newton iterations; returns the iterations done. */
+int orc_ns_newton(const orc_ns *p, int kmax, int lmax, double eta0, int ecase, double tolnl, int maxit,
+                  double *uhist, double *normF, double *wout, int *gmres);
+
 #ifdef __cplusplus
 }
 #endif

@@ -318,3 +318,56 @@ def euler_predictor(x, y, vert, node_id, neq, upresc, u0, nsteps, ncorr=2, gamma
                                       ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp, _ip]
     L.orc_euler_predictor(ctypes.byref(p), kmax, lmax, tol, nsteps, ncorr, u, uhist, iters)
     return uhist, iters
+
+
+class NSParams(ctypes.Structure):
+    """orc_ns of oracle.h."""
+    _fields_ = [("nnodes", ctypes.c_int), ("nel", ctypes.c_int), ("neq", ctypes.c_int),
+                ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("vert", ctypes.c_void_p),
+                ("node_id", ctypes.c_void_p), ("upresc", ctypes.c_void_p), ("f", ctypes.c_void_p),
+                ("re", ctypes.c_double), ("velmax", ctypes.c_double)]
+
+
+def _ns(x, y, vert, node_id, neq, upresc, f, re, velmax):
+    keep = [_c(x, np.float64), _c(y, np.float64), _c(vert, np.int32).reshape(-1),
+            _c(node_id, np.int32).reshape(-1), _c(upresc, np.float64).reshape(-1),
+            _c(f, np.float64).reshape(-1)]
+    p = NSParams(len(keep[0]), len(keep[2]) // 3, int(neq), *(k.ctypes.data for k in keep), float(re),
+                 float(velmax))
+    return p, keep
+
+
+def ns_builds(x, y, vert, node_id, neq, upresc, f, re, velmax, us):
+    """Consecutive Build_K_F_MS calls on the states us (first call flagged as
+    the run's first): (Ae [nb, nel, 81], F [nb, neq+1], delta_old, normres_old)."""
+    L = lib()
+    p, keep = _ns(x, y, vert, node_id, neq, upresc, f, re, velmax)
+    L.orc_ns_build.restype = None
+    L.orc_ns_build.argtypes = [ctypes.POINTER(NSParams), _dp, ctypes.c_int, _dp, _dp, _dp, _dp]
+    dold = np.zeros(p.nel)
+    nold = np.zeros(p.nel)
+    Ae = np.zeros((len(us), p.nel, 81))
+    F = np.zeros((len(us), neq + 1))
+    for b, u in enumerate(us):
+        A1 = np.zeros(p.nel * 81)
+        F1 = np.zeros(neq + 1)
+        L.orc_ns_build(ctypes.byref(p), _c(u, np.float64), 1 if b == 0 else 0, dold, nold, A1, F1)
+        Ae[b] = A1.reshape(p.nel, 81)
+        F[b] = F1
+    return Ae, F, dold, nold
+
+
+def ns_newton(x, y, vert, node_id, neq, upresc, f, re, velmax, kmax=30, lmax=50, eta0=0.1, ecase=2,
+              tolnl=1e-6, maxit=10):
+    """Process.c's damped Newton: (uhist [n, neq+1], |F| [n], w [n], GMRES iterations [n])."""
+    L = lib()
+    p, keep = _ns(x, y, vert, node_id, neq, upresc, f, re, velmax)
+    L.orc_ns_newton.restype = ctypes.c_int
+    L.orc_ns_newton.argtypes = [ctypes.POINTER(NSParams), ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, _dp, _dp, _ip]
+    uh = np.zeros((maxit, neq + 1))
+    nF = np.zeros(maxit)
+    w = np.zeros(maxit)
+    g = np.zeros(maxit, np.int32)
+    n = L.orc_ns_newton(ctypes.byref(p), kmax, lmax, eta0, ecase, tolnl, maxit, uh, nF, w, g)
+    return uh[:n], nF[:n], w[:n], g[:n]

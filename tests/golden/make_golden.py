@@ -1,8 +1,10 @@
 """Generate golden vectors by running the reference's own C paths, compiled
 from its sources by ``make -C oracle ref`` into oracle/_ref/: the steady-
 transport solve (libfemref.so, oracle/ref_harness.c), the multi-dof EBE
-operators (libfemref_*_blk.so, oracle/ref_block_harness.c) and the 2D Euler
-build and predictor (libfemref_euler.so, oracle/ref_euler_harness.c).
+operators (libfemref_*_blk.so, oracle/ref_block_harness.c), the 2D Euler
+build and predictor (libfemref_euler.so, oracle/ref_euler_harness.c) and the
+steady Navier-Stokes VMS build and damped Newton (libfemref_ns.so,
+oracle/ref_ns_harness.c).
 
 Usage:  python tests/golden/make_golden.py        (writes tests/golden/*.npz)
 
@@ -245,7 +247,76 @@ def main_euler():
         print(f"{name}: neq={neq} nel={mesh.nel} dt={dt:.4g} iters={list(iters)}")
 
 
+# Navier-Stokes (CAVITY) cases: name -> (n, perturb, seed, Re, Newton iterations, forcing case)
+NS_CASES = {
+    "ns_cavity_10x10": (10, 0.0, 5, 100.0, 6, 2),
+    "ns_cavity_12x12p": (12, 0.2, 6, 400.0, 5, 1),
+}
+
+
+def ns_lib():
+    """A fresh copy of the reference NS library: Build_K_F_MS counts its calls
+    in a file-scope variable, so every run needs its own instance."""
+    import shutil
+    import tempfile
+    d = tempfile.mkdtemp()
+    path = os.path.join(d, "libfemref_ns.so")
+    shutil.copy(os.path.join(ROOT, "oracle", "_ref", "libfemref_ns.so"), path)
+    L = ctypes.CDLL(path)
+    L.ref_ns_builds.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_double,
+                                ctypes.c_double, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]
+    L.ref_ns_newton.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_double,
+                                ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                ctypes.c_double, ctypes.c_int, _dp, _dp, _dp, _ip]
+    L.ref_ns_newton.restype = ctypes.c_int
+    L.CAVITY_v1presc.argtypes = [ctypes.c_double, ctypes.c_double]
+    L.CAVITY_v1presc.restype = ctypes.c_double
+    return L
+
+
+def main_ns():
+    """Three consecutive VMS builds on perturbed states (element matrices,
+    residuals, stabilisation state) and a damped-Newton run, through the
+    reference's sources (oracle/ref_ns_harness.c)."""
+    from fem_codes_gb300.mesh import cavity_problem
+    for name, (n, pert, seed, re, maxit, ecase) in NS_CASES.items():
+        mesh = structured_mesh(n, n, perturb=pert, seed=seed)
+        pb = cavity_problem(mesh, re)
+        L = ns_lib()
+        # the lid values exactly as the reference's plug-in computes them
+        up = pb.upresc.copy()
+        up[:, 0] = [L.CAVITY_v1presc(float(a), float(b)) for a, b in zip(mesh.x, mesh.y)]
+        neq = pb.neq
+        rng = np.random.default_rng(seed)
+        us = np.zeros((3, neq + 1))
+        for b in range(3):
+            us[b, :neq] = 0.3 * rng.uniform(-1.0, 1.0, neq)
+        vert = np.ascontiguousarray(mesh.vert.reshape(-1), np.int32)
+        nid = np.ascontiguousarray(pb.node_id.reshape(-1), np.int32)
+        Ae = np.zeros(3 * mesh.nel * 81)
+        F = np.zeros(3 * (neq + 1))
+        dold = np.zeros(mesh.nel)
+        nold = np.zeros(mesh.nel)
+        L.ref_ns_builds(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, re, 1.0, 3, us.reshape(-1), Ae, F,
+                        dold, nold)
+        kmax, lmax, eta0, tolnl = 30, 50, 0.1, 1e-6
+        L2 = ns_lib()
+        uh = np.zeros(maxit * (neq + 1))
+        nF = np.zeros(maxit)
+        w = np.zeros(maxit)
+        g = np.zeros(maxit, np.int32)
+        nit = L2.ref_ns_newton(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, re, 1.0, kmax, lmax, eta0,
+                               ecase, tolnl, maxit, uh, nF, w, g)
+        np.savez_compressed(
+            os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id, neq=neq,
+            upresc=up, f=pb.f, re=re, velmax=1.0, us=us, Ae=Ae.reshape(3, mesh.nel, 81), F=F.reshape(3, neq + 1),
+            delta_old=dold, normres_old=nold, kmax=kmax, lmax=lmax, eta0=eta0, ecase=ecase, tolnl=tolnl,
+            maxit=maxit, uhist=uh.reshape(maxit, neq + 1)[:nit], normF=nF[:nit], w=w[:nit], gmres=g[:nit])
+        print(f"{name}: neq={neq} nel={mesh.nel} newton={nit} |F|={nF[:nit]} gmres={g[:nit]}")
+
+
 def main():
+    main_ns()
     main_euler()
     main_blocks()
     lib = load_ref()
