@@ -19,7 +19,7 @@ import numpy as np
 
 from .build import LIB, build as _build
 
-__all__ = ["SSTransport", "Euler", "FemGpuError", "load", "OPTS"]
+__all__ = ["SSTransport", "Euler", "NavierStokes", "FemGpuError", "load", "OPTS"]
 
 _lib = None
 
@@ -63,6 +63,13 @@ class EulerOpts(ctypes.Structure):
                 ("alpha", ctypes.c_double), ("dt", ctypes.c_double), ("stab_tol", ctypes.c_double),
                 ("precond", ctypes.c_int), ("solver", ctypes.c_int), ("kmax", ctypes.c_int),
                 ("lmax", ctypes.c_int), ("tol", ctypes.c_double), ("ncorr", ctypes.c_int)]
+
+
+class NSOpts(ctypes.Structure):
+    """femgpu_ns_opts of femgpu.h."""
+    _fields_ = [("re", ctypes.c_double), ("velmax", ctypes.c_double), ("precond", ctypes.c_int),
+                ("solver", ctypes.c_int), ("kmax", ctypes.c_int), ("lmax", ctypes.c_int),
+                ("eta0", ctypes.c_double), ("eta_case", ctypes.c_int), ("tol_nl", ctypes.c_double)]
 
 
 _vp = ctypes.c_void_p
@@ -132,6 +139,28 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         f = getattr(L, name)
         f.argtypes = args
         f.restype = ctypes.c_int
+    L.femgpu_ns_default_opts.argtypes = [ctypes.POINTER(NSOpts)]
+    L.femgpu_ns_default_opts.restype = None
+    L.femgpu_ns_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(NSOpts), ctypes.c_int, _vp, _vp,
+                                   ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp]
+    L.femgpu_ns_create.restype = ctypes.c_int
+    L.femgpu_ns_destroy.argtypes = [_vp]
+    L.femgpu_ns_destroy.restype = None
+    for name, args in {
+        "femgpu_ns_set_stream": [_vp, _vp],
+        "femgpu_ns_reset": [_vp],
+        "femgpu_ns_build": [_vp, _vp, _vp, _vp],
+        "femgpu_ns_build_dev": [_vp],
+        "femgpu_ns_precond_setup": [_vp, _vp],
+        "femgpu_ns_solve": [_vp, _vp, _vp, _ip],
+        "femgpu_ns_newton": [_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp],
+    }.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    for name in ("femgpu_ns_u_dev", "femgpu_ns_ebe"):
+        getattr(L, name).argtypes = [_vp]
+        getattr(L, name).restype = _vp
     L.femgpu_gnn_nparams.restype = ctypes.c_int
     L.femgpu_gnn_nparams.argtypes = []
     L.femgpu_gnn_destroy.argtypes = [_vp]
@@ -520,3 +549,112 @@ class Euler:
 
     def u_dev(self):
         return self._L.femgpu_euler_u_dev(self._h)
+
+
+class NavierStokes:
+    """Steady incompressible Navier-Stokes on one GPU: VMS/NSGS element build
+    with bubble condensation, 3-dof block EBE storage with the nodal
+    block-diagonal preconditioner, GMRES and the damped Newton loop
+    (04_SS_NavierStokes_Equations/2D with StabilizationForm MS, EBE,
+    BlockDiag).  ``Build``, ``precond_setup``, ``solver`` and ``Process``
+    carry the names of the functions they replace; vectors have length
+    neq+1."""
+
+    def __init__(self, x, y, vert, node_id, neq, upresc, f=None, re=1000.0, velmax=1.0, precond="BlockDiag",
+                 solver="GMRES", kmax=50, lmax=100, eta0=0.1, eta_case=2, tol_nl=1e-8):
+        L = load()
+        o = NSOpts()
+        L.femgpu_ns_default_opts(ctypes.byref(o))
+        o.re, o.velmax = float(re), float(velmax)
+        o.precond = OPTS["precond"][precond.upper()]
+        o.solver = OPTS["solver"][solver.upper()]
+        o.kmax, o.lmax, o.eta0, o.eta_case, o.tol_nl = int(kmax), int(lmax), float(eta0), int(eta_case), float(tol_nl)
+        self.opts = o
+        self._keep = [_f64(x), _f64(y), _i32(np.asarray(vert).reshape(-1)), _i32(np.asarray(node_id).reshape(-1)),
+                      _f64(np.asarray(upresc).reshape(-1)),
+                      None if f is None else _f64(np.asarray(f).reshape(-1))]
+        self.nnodes = len(self._keep[0])
+        self.nel = self._keep[2].size // 3
+        self.neq = int(neq)
+        h = _vp()
+        rc = L.femgpu_ns_create(ctypes.byref(h), ctypes.byref(o), self.nnodes, _ptr(self._keep[0]),
+                                _ptr(self._keep[1]), self.nel, _ptr(self._keep[2]), _ptr(self._keep[3]), self.neq,
+                                _ptr(self._keep[4]), _ptr(self._keep[5]))
+        if rc:
+            raise FemGpuError(rc, "Preprocess")
+        self._h = h
+        self._L = L
+
+    @classmethod
+    def from_problem(cls, mesh, prob, **kw):
+        return cls(mesh.x, mesh.y, mesh.vert, prob.node_id, prob.neq, prob.upresc, f=prob.f, re=prob.re,
+                   velmax=prob.velmax, **kw)
+
+    def _check(self, rc, where):
+        if rc:
+            raise FemGpuError(rc, where)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.femgpu_ns_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_ptr):
+        self._check(self._L.femgpu_ns_set_stream(self._h, _vp(stream_ptr)), "set_stream")
+
+    def reset(self):
+        self._check(self._L.femgpu_ns_reset(self._h), "reset")
+
+    def Build(self, u=None, want_matrix=False):
+        """Build_K_F_MS from u. Returns (F, Ae [nel, 81] or None)."""
+        F = np.zeros(self.neq + 1)
+        Ae = np.zeros((self.nel, 81)) if want_matrix else None
+        uu = None if u is None else _f64(u)
+        self._check(self._L.femgpu_ns_build(self._h, _ptr(uu), _ptr(Ae), _ptr(F)), "Build")
+        return F, Ae
+
+    def precond_setup(self):
+        F = np.zeros(self.neq + 1)
+        self._check(self._L.femgpu_ns_precond_setup(self._h, _ptr(F)), "precond_setup")
+        return F
+
+    def solver(self, B=None):
+        BB = None if B is None else _f64(B)
+        X = np.zeros(self.neq + 1)
+        it = ctypes.c_int(0)
+        rc = self._L.femgpu_ns_solve(self._h, _ptr(BB), _ptr(X), ctypes.byref(it))
+        if rc and rc != -5:
+            raise FemGpuError(rc, "solver")
+        return X, it.value
+
+    def Process(self, maxit=2000):
+        """Damped Newton from u = 0: (u, uhist [n, neq+1], |F| [n], w [n],
+        GMRES iterations [n])."""
+        u = np.zeros(self.neq + 1)
+        uh = np.zeros((maxit, self.neq + 1))
+        nF = np.zeros(maxit)
+        w = np.zeros(maxit)
+        g = np.zeros(maxit, np.int32)
+        n = self._L.femgpu_ns_newton(self._h, int(maxit), _ptr(u), _ptr(uh), _ptr(nF), _ptr(w), _ptr(g))
+        if n < 0:
+            raise FemGpuError(n, "Process")
+        return u, uh[:n], nF[:n], w[:n], g[:n]
+
+    def u_dev(self):
+        return self._L.femgpu_ns_u_dev(self._h)

@@ -24,7 +24,7 @@ INC = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-I" + HOST,
 
 # Translation units whose arithmetic must round every operation separately
 # (element build: bit-parity with the reference compiled without contraction).
-NO_FMA = {"build.cu", "ebe_block.cu", "euler_build.cu"}
+NO_FMA = {"build.cu", "ebe_block.cu", "euler_build.cu", "ns_build.cu"}
 
 
 def _sources():

@@ -276,6 +276,57 @@ femgpu_ebe *femgpu_euler_ebe(femgpu_euler *ctx);
  * femgpu_euler_predictor(_dev) call (t[3]). */
 int femgpu_euler_last_times(const femgpu_euler *ctx, double *t);
 
+/* ---- steady incompressible Navier-Stokes: VMS build and damped Newton -----
+ * 04_SS_NavierStokes_Equations/2D with StabilizationForm MS (Build_K_F_MS),
+ * MatrixVectorProductScheme EBE, BlockDiag preconditioning (3x3 nodal blocks)
+ * and Process's damped Newton.  Unknowns per node (u, v, p). */
+typedef struct femgpu_ns_opts {
+	double re;           /* ReynoldsNumber                                   */
+	double velmax;       /* VelMax (reference velocity of the local Re)      */
+	int precond;         /* FEMGPU_PREC_NOT or FEMGPU_PREC_BLOCKDIAG         */
+	int solver;          /* femgpu_solver: PGMRES (reference) or FGMRES      */
+	int kmax, lmax;      /* KrylovBasisVectorsQuantity, LinearMaxIter        */
+	double eta0;         /* SolverTolerance: initial / maximal forcing term  */
+	int eta_case;        /* SolverToleranceCase 0..4 (eta_newton.c)          */
+	double tol_nl;       /* SolverToleranceNonLin: ||F|| <= tol_nl ||F_0||   */
+} femgpu_ns_opts;
+
+void femgpu_ns_default_opts(femgpu_ns_opts *o);
+typedef struct femgpu_ns femgpu_ns;
+
+/*   x, y      [nnodes]    node coordinates; vert [3*nel]
+ *   node_id   [3*nnodes]  equation of each (node, u|v|p), -1 prescribed
+ *   upresc    [3*nnodes]  prescribed values (v1presc, v2presc, ppresc)
+ *   f         [2*nnodes]  body force at the nodes (f1ext, f2ext; NULL = 0) */
+int femgpu_ns_create(femgpu_ns **ctx, const femgpu_ns_opts *opts, int nnodes, const double *x,
+		const double *y, int nel, const int *vert, const int *node_id, int neq, const double *upresc,
+		const double *f);
+void femgpu_ns_destroy(femgpu_ns *ctx);
+int femgpu_ns_set_stream(femgpu_ns *ctx, void *stream);
+/* Zero the per-element stabilisation state (delta_old, normres_old) and the
+ * build count, as at the start of Process (Process.c:49-56). */
+int femgpu_ns_reset(femgpu_ns *ctx);
+/* Build_K_F_MS (Build_K_F_MS.c:8-1190) from u [neq+1] (host; NULL = the
+ * device state): element matrices Ae_host [81*nel] and F_host [neq+1]
+ * (NULL skips); the first build after create/reset takes the reference's
+ * first-call branch of the stabilisation update. */
+int femgpu_ns_build(femgpu_ns *ctx, const double *u, double *Ae_host, double *F_host);
+int femgpu_ns_build_dev(femgpu_ns *ctx);
+/* BlockDiagDOF3_precond_EBE_setup: F := D^-1 F (F_host receives it). */
+int femgpu_ns_precond_setup(femgpu_ns *ctx, double *F_host);
+/* pgmres (6-argument form) on the 3-dof block EBE operator: X solves
+ * A X = B (B_host NULL: the context's F) to the current forcing term. */
+int femgpu_ns_solve(femgpu_ns *ctx, const double *B_host, double *X_host, int *iters);
+/* Process.c:62-194 from u = 0: at most maxit damped-Newton iterations (and
+ * the reference's 2000 cap), stopping when ||F|| <= tol_nl ||F_0||.  u_host
+ * [neq+1] receives the solution; uhist [maxit*(neq+1)], normF, w [maxit],
+ * gmres [maxit] the per-iteration history (each may be NULL).  Returns the
+ * number of Newton iterations done (>= 0) or an error code. */
+int femgpu_ns_newton(femgpu_ns *ctx, int maxit, double *u_host, double *uhist, double *normF, double *w,
+		int *gmres);
+double *femgpu_ns_u_dev(femgpu_ns *ctx);
+femgpu_ebe *femgpu_ns_ebe(femgpu_ns *ctx);
+
 /* ---- learned preconditioner ----------------------------------------------
  * No counterpart in the reference.  A mesh graph network (3 message-passing
  * layers of width 32, FP32 weights, bf16 or FP32 activations) on the graph of
