@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--precision", default="MIXED", choices=["FP64", "MIXED", "MIXED_IR"])
     ap.add_argument("--precond", default="ILU0")
     ap.add_argument("--kmax", type=int, default=50)
+    ap.add_argument("--ilu-blocks", type=int, default=0,
+                    help="0: ILU(0) of the whole matrix; P > 1: block ILU(0) over P row blocks")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="transport", choices=["transport", "euler"])
     ap.add_argument("--euler-nx", type=int, default=1024)
@@ -76,6 +78,7 @@ def config(a):
     return {"workload": f"steady transport SUPG+CAU {a.nx}x{a.ny} cells ({2 * a.nx * a.ny} triangles), "
                         "perturbed +-0.2h, CSR+SYMRCM, ILU(0)-FGMRES(50), rel tol 1e-8 (true residual)",
             "nx": a.nx, "ny": a.ny, "precision": a.precision, "precond": a.precond, "kmax": a.kmax,
+            "ilu_blocks": a.ilu_blocks,
             "step": "build + ILU(0) factor + solve to 1e-8", "l2": "inputs larger than L2 (matrix+factors > 129 MB)"}
 
 
@@ -190,7 +193,7 @@ def run_ours(a):
 
     T = fg.SSTransport.from_problem(m, p, scheme="CSR", reorder="SYMRCM", precond=a.precond, kmax=a.kmax,
                                     lmax=200, tol=1e-8, solver="FGMRES", precision=a.precision,
-                                    inner_tol=1e-4, ir_max=40)
+                                    inner_tol=1e-4, ir_max=40, ilu_blocks=a.ilu_blocks)
     L = T._L
     s = torch.cuda.Stream()
     T.set_stream(s.cuda_stream)

@@ -54,7 +54,8 @@ class Opts(ctypes.Structure):
                 ("shock", ctypes.c_int), ("hshock", ctypes.c_int), ("outflow", ctypes.c_int),
                 ("kmax", ctypes.c_int), ("lmax", ctypes.c_int), ("tol", ctypes.c_double),
                 ("nonlin_tol", ctypes.c_double), ("precision", ctypes.c_int), ("ir_max", ctypes.c_int),
-                ("solver", ctypes.c_int), ("inner_tol", ctypes.c_double), ("stall_ratio", ctypes.c_double)]
+                ("solver", ctypes.c_int), ("inner_tol", ctypes.c_double), ("stall_ratio", ctypes.c_double),
+                ("ilu_blocks", ctypes.c_int)]
 
 
 class EulerOpts(ctypes.Structure):
@@ -216,7 +217,7 @@ class SSTransport:
                  fsrc=None, scheme="CSR", reorder="NOT", precond="ILU0", shock="CAU",
                  hshock="2sqrtArea", outflow=False, kmax=30, lmax=1000, tol=1e-8,
                  nonlin_tol=0.0, precision="FP64", ir_max=30, solver="GMRES", inner_tol=1e-4,
-                 stall_ratio=0.9):
+                 stall_ratio=0.9, ilu_blocks=0):
         L = load()
         o = Opts()
         L.femgpu_transport_default_opts(ctypes.byref(o))
@@ -232,6 +233,7 @@ class SSTransport:
         o.solver = OPTS["solver"][solver.upper()]
         o.inner_tol = inner_tol
         o.stall_ratio = stall_ratio
+        o.ilu_blocks = int(ilu_blocks)
         self.opts = o
         self._keep = [_f64(x), _f64(y), _i32(node_type), _i32(np.asarray(vert).reshape(-1)),
                       _f64(upresc)]

@@ -38,6 +38,8 @@ typedef struct fg_sweep {
 	int *ppos;                 /* [n] padded position of each position       */
 	long long *val_off;        /* [nval] byte offset of each value slot      */
 	int *val_src;              /* [nval] CSR position (-1 zero, -2-r pivot)  */
+	int nchunk;                /* matrix blocks (block ILU(0); 1: global)    */
+	int *chunk_sb, *chunk_lev; /* [nchunk+1] first sub-block / level of each */
 } fg_sweep;
 
 typedef struct fg_ilu_sweeps {

@@ -19,7 +19,13 @@
 //     barrier per level.
 // Rows are computed in the reference's order (ascending columns) and the
 // FP64 variant rounds each operation separately, so its results are
-// bit-identical to the reference's sweeps.  Every wait is bounded: on timeout
+// bit-identical to the reference's sweeps.
+//
+// Block ILU(0) (ilu_blocks = P > 0): the rows are cut into P contiguous
+// blocks of the (reordered) numbering and couplings between blocks are
+// dropped, so each block factorises and sweeps independently: its levels
+// form a contiguous run of the program (levels are numbered block by block)
+// and one thread block per matrix block runs them, P thread blocks at once.  Every wait is bounded: on timeout
 // the block records FEMGPU_E_TIMEOUT, waits (bounded) for the copies it has in
 // flight and returns.
 #include "fg_common.cuh"
@@ -155,6 +161,8 @@ struct SweepArgs {
 	int nlev, nsb, D, stage_bytes;
 	int *err;
 	const int *active;
+	const int *chunk_sb;          // [P+1] first sub-block of each matrix block (NULL: one block)
+	const int *chunk_lev;         // [P+1] first level of each matrix block
 };
 
 // CW consumer warps (warps 0..CW-1) and one producer warp (warp CW).
@@ -173,6 +181,9 @@ k_sweep(SweepArgs a, const T *__restrict__ in, T *out)
 	volatile int *vfailed = &failed;
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, D = a.D;
 	const unsigned sbytes = (unsigned)a.stage_bytes;
+	// this thread block's run of sub-blocks and levels
+	const int sb0 = a.chunk_sb ? a.chunk_sb[blockIdx.x] : 0, sb1 = a.chunk_sb ? a.chunk_sb[blockIdx.x + 1] : a.nsb;
+	const int l0 = a.chunk_lev ? a.chunk_lev[blockIdx.x] : 0, l1 = a.chunk_lev ? a.chunk_lev[blockIdx.x + 1] : a.nlev;
 
 	if (tid == 0) {
 		failed = 0; issued = 0; pdone = 0;
@@ -186,16 +197,16 @@ k_sweep(SweepArgs a, const T *__restrict__ in, T *out)
 		bool stop = false;
 		int s = 0;
 		unsigned ph = 0;                                  // phase of empty[s] to wait for
-		for (int base = 0; base < a.nsb && !stop; base += 32) {
+		for (int base = sb0; base < sb1 && !stop; base += 32) {
 			// each lane fetches the offsets of one upcoming sub-block
 			int i = base + lane;
 			long long b0 = 0, b1 = 0;
 			int p0 = 0, vb = 0;
-			if (i < a.nsb) { b0 = a.blk_off[i]; b1 = a.blk_off[i + 1]; p0 = a.sb_in[i]; vb = a.sb_inb[i]; }
-			for (int j = 0; j < 32 && base + j < a.nsb; j++) {
+			if (i < sb1) { b0 = a.blk_off[i]; b1 = a.blk_off[i + 1]; p0 = a.sb_in[i]; vb = a.sb_inb[i]; }
+			for (int j = 0; j < 32 && base + j < sb1; j++) {
 				long long B0 = __shfl_sync(0xffffffffu, b0, j), B1 = __shfl_sync(0xffffffffu, b1, j);
 				int P0 = __shfl_sync(0xffffffffu, p0, j), VB = __shfl_sync(0xffffffffu, vb, j);
-				int sb = base + j;
+				int sb = base + j - sb0;                  // local sub-block index
 				int go = 1;
 				if (lane == 0) {
 					if (sb >= D && !mbar_wait_or_fail(&empty[s], ph, vfailed)) go = 0;
@@ -222,7 +233,7 @@ k_sweep(SweepArgs a, const T *__restrict__ in, T *out)
 	const int ctid = tid;                                 // ---- consumer warps
 	int sb = 0, s = 0;
 	unsigned ph = 0;                                      // phase of full[s] to wait for
-	for (int l = 0; l < a.nlev; l++) {
+	for (int l = l0; l < l1; l++) {
 		int nsub = 1, j = 0, s0 = s;
 		for (; j < nsub; j++) {
 			bool ok = mbar_wait_or_fail(&full[s], ph, vfailed);
@@ -312,10 +323,11 @@ __global__ void k_refresh(unsigned char *prog, const long long *val_off, const i
 __global__ void __launch_bounds__(FAC_THREADS, 1)
 k_ilu0_factor_cta(const int *__restrict__ IA, const double *__restrict__ AA,
                   const int *__restrict__ rows, const int *__restrict__ lev_start, int nlev,
-                  const int *__restrict__ fac_ptr, const int *__restrict__ fac_prog,
-                  double *LU, double *Dinv, int *err)
+                  const int *__restrict__ chunk_lev, const int *__restrict__ fac_ptr,
+                  const int *__restrict__ fac_prog, double *LU, double *Dinv, int *err)
 {
-	for (int l = 0; l < nlev; l++) {
+	const int l0 = chunk_lev ? chunk_lev[blockIdx.x] : 0, l1 = chunk_lev ? chunk_lev[blockIdx.x + 1] : nlev;
+	for (int l = l0; l < l1; l++) {
 		int b = lev_start[l], e = lev_start[l + 1];
 		for (int p = b + threadIdx.x; p < e; p += FAC_THREADS) {
 			int r = rows[p];
@@ -351,24 +363,42 @@ struct HostLevels {
 	std::vector<int> start, pstart, rows, pos, ppos;   // pos/ppos indexed by row
 };
 
-static HostLevels host_levels(const int *IA, const int *JA, int n, bool lower)
+// Matrix block of a row: P contiguous blocks of the numbering (P = 0: one).
+struct Blocks {
+	int P, n;
+	int of(int r) const { return P ? (int)((long long)r * P / n) : 0; }
+	bool same(int r, int c) const { return !P || of(r) == of(c); }
+};
+
+// Dependency levels of the forward (lower) or backward sweep; with blocks,
+// levels are numbered block by block (block b's levels follow block b-1's),
+// and clev [P+1] receives each block's first level.
+static HostLevels host_levels(const int *IA, const int *JA, int n, bool lower, const Blocks &B,
+                              std::vector<int> *clev = nullptr)
 {
 	HostLevels H;
 	std::vector<int> lev(n, 0);
-	int nlev = 0;
+	int P = B.P ? B.P : 1;
+	std::vector<int> bl(P, 0);                 // levels of each block
 	if (lower) {
 		for (int i = 0; i < n; i++) {
 			int L = 0;
-			for (int k = IA[i]; k < IA[i + 1] && JA[k] < i; k++) L = std::max(L, lev[JA[k]] + 1);
-			lev[i] = L; nlev = std::max(nlev, L + 1);
+			for (int k = IA[i]; k < IA[i + 1] && JA[k] < i; k++)
+				if (B.same(i, JA[k])) L = std::max(L, lev[JA[k]] + 1);
+			lev[i] = L; bl[B.of(i)] = std::max(bl[B.of(i)], L + 1);
 		}
 	} else {
 		for (int i = n - 1; i >= 0; i--) {
 			int L = 0;
-			for (int k = IA[i]; k < IA[i + 1]; k++) if (JA[k] > i) L = std::max(L, lev[JA[k]] + 1);
-			lev[i] = L; nlev = std::max(nlev, L + 1);
+			for (int k = IA[i]; k < IA[i + 1]; k++) if (JA[k] > i && B.same(i, JA[k])) L = std::max(L, lev[JA[k]] + 1);
+			lev[i] = L; bl[B.of(i)] = std::max(bl[B.of(i)], L + 1);
 		}
 	}
+	std::vector<int> boff(P + 1, 0);
+	for (int b = 0; b < P; b++) boff[b + 1] = boff[b] + bl[b];
+	for (int i = 0; i < n; i++) lev[i] += boff[B.of(i)];
+	if (clev) *clev = boff;
+	int nlev = boff[P];
 	H.nlev = nlev;
 	H.start.assign(nlev + 1, 0);
 	H.pstart.assign(nlev + 1, 0);
@@ -404,7 +434,7 @@ static int up_vec(X **d, const std::vector<X> &h)
 // and pivots, outputs in natural order.
 template <typename T, bool UPPER>
 static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, const HostLevels *target,
-                      fg_sweep &sw)
+                      const Blocks &B, const std::vector<int> &clev, fg_sweep &sw)
 {
 	const bool lower = !UPPER;
 	const long long tsize = sizeof(T);
@@ -419,7 +449,8 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 			int cc = std::min(SW_SUB, c - j0), w = 0;
 			for (int p = H.start[l] + j0; p < H.start[l] + j0 + cc; p++) {
 				int r = H.rows[p], cnt = 0;
-				for (int k = IA[r]; k < IA[r + 1]; k++) if (lower ? JA[k] < r : JA[k] > r) cnt++;
+				for (int k = IA[r]; k < IA[r + 1]; k++)
+					if ((lower ? JA[k] < r : JA[k] > r) && B.same(r, JA[k])) cnt++;
 				w = std::max(w, cnt);
 			}
 			subs.push_back({ l, j0, cc, w });
@@ -453,7 +484,7 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 			int r = H.rows[start + j];
 			for (int q = IA[r]; q < IA[r + 1]; q++) {
 				int col = JA[q];
-				if ((lower ? col < r : col > r) && end - H.pos[col] > SW_RING) hasfar = 1;
+				if ((lower ? col < r : col > r) && B.same(r, col) && end - H.pos[col] > SW_RING) hasfar = 1;
 			}
 		}
 		LevHdr h = { c, w, start, cp, nsub, hasfar, (int)al16(SW_HDR + (long long)(w + 1) * cp * 4),
@@ -467,7 +498,7 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 			outp[j] = lower ? target->ppos[r] : r;
 			for (int q = IA[r]; q < IA[r + 1]; q++) {
 				int col = JA[q];
-				if (lower ? !(col < r) : !(col > r)) continue;
+				if ((lower ? !(col < r) : !(col > r)) || !B.same(r, col)) continue;
 				int p = H.pos[col];
 				unsigned code = (end - p <= SW_RING) ? (SW_NEAR | (unsigned)(p & (SW_RING - 1)))
 				                                     : (unsigned)(lower ? target->ppos[col] : col);
@@ -486,6 +517,13 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 			}
 		}
 	}
+	// first sub-block of each matrix block (its first level's first sub-block)
+	std::vector<int> csb(clev.size(), nsb);
+	for (size_t b = 0, i = 0; b < clev.size(); b++) {
+		while (i < (size_t)nsb && subs[i].l < clev[b]) i++;
+		csb[b] = (int)i;
+	}
+	sw.nchunk = (int)clev.size() - 1;
 	sw.nlev = nlev;
 	sw.nsb = nsb;
 	sw.bytes = off[nsb];
@@ -505,13 +543,16 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 	if ((rc = up_vec(&sw.ppos, ppos_by_pos))) return rc;
 	if ((rc = up_vec(&sw.val_off, val_off))) return rc;
 	if ((rc = up_vec(&sw.val_src, val_src))) return rc;
+	if ((rc = up_vec(&sw.chunk_sb, csb))) return rc;
+	if ((rc = up_vec(&sw.chunk_lev, clev))) return rc;
 	return 0;
 }
 
 // Elimination program of every row, in forward level order (the layout
 // k_ilu0_factor_cta reads): the same sequence of updates as
 // ILUp_precond_setup.c:119-139, resolved against the pattern once.
-static int build_factor_prog(const int *IA, const int *JA, int n, const HostLevels &Lo, fg_ilu_sweeps &S)
+static int build_factor_prog(const int *IA, const int *JA, int n, const HostLevels &Lo, const Blocks &B,
+                             fg_ilu_sweeps &S)
 {
 	std::vector<int> ptr(n + 1, 0), prog;
 	prog.reserve((size_t)n * 24);
@@ -526,13 +567,14 @@ static int build_factor_prog(const int *IA, const int *JA, int n, const HostLeve
 		prog.push_back(0);
 		for (int q = 0; q < len && JA[rb + q] < r; q++) {
 			int jrow = JA[rb + q], cnt = 0;
+			if (!B.same(r, jrow)) continue;              // coupling to another block: dropped
 			size_t g = prog.size();
 			prog.push_back(q);
 			prog.push_back(jrow);
 			prog.push_back(0);
 			for (int k = IA[jrow]; k < IA[jrow + 1]; k++) {
 				int col = JA[k], pos = -1;
-				if (col <= jrow) continue;
+				if (col <= jrow || !B.same(r, col)) continue;
 				for (int m = 0; m < len; m++) if (JA[rb + m] == col) { pos = m; break; }
 				if (pos < 0) continue;
 				prog.push_back(col == r ? -1 : pos);
@@ -578,17 +620,17 @@ static int sweep_cw(void)
 // fma: fused multiply-subtract in the FP64 sweeps (the FGMRES solves); the
 // separately rounded form reproduces the reference bit for bit.
 template <typename T, bool UPPER>
-static void launch_sweep(const SweepArgs &a, int bytes, cudaStream_t s, const T *in, T *out, bool fma)
+static void launch_sweep(const SweepArgs &a, int grid, int bytes, cudaStream_t s, const T *in, T *out, bool fma)
 {
 	int cw = sweep_cw();
 	if (fma && sizeof(T) == 8) {
-		if (cw == 4) k_sweep<T, UPPER, 4, true><<<1, 160, bytes, s>>>(a, in, out);
-		else if (cw == 8) k_sweep<T, UPPER, 8, true><<<1, 288, bytes, s>>>(a, in, out);
-		else k_sweep<T, UPPER, 16, true><<<1, 544, bytes, s>>>(a, in, out);
+		if (cw == 4) k_sweep<T, UPPER, 4, true><<<grid, 160, bytes, s>>>(a, in, out);
+		else if (cw == 8) k_sweep<T, UPPER, 8, true><<<grid, 288, bytes, s>>>(a, in, out);
+		else k_sweep<T, UPPER, 16, true><<<grid, 544, bytes, s>>>(a, in, out);
 	} else {
-		if (cw == 4) k_sweep<T, UPPER, 4, false><<<1, 160, bytes, s>>>(a, in, out);
-		else if (cw == 8) k_sweep<T, UPPER, 8, false><<<1, 288, bytes, s>>>(a, in, out);
-		else k_sweep<T, UPPER, 16, false><<<1, 544, bytes, s>>>(a, in, out);
+		if (cw == 4) k_sweep<T, UPPER, 4, false><<<grid, 160, bytes, s>>>(a, in, out);
+		else if (cw == 8) k_sweep<T, UPPER, 8, false><<<grid, 288, bytes, s>>>(a, in, out);
+		else k_sweep<T, UPPER, 16, false><<<grid, 544, bytes, s>>>(a, in, out);
 	}
 }
 
@@ -608,12 +650,14 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 {
 	int n = t->neq, rc, D, sb;
 	fg_ilu_sweeps &S = t->sweeps;
-	HostLevels Lo = host_levels(hIA, hJA, n, true), Up = host_levels(hIA, hJA, n, false);
-	if ((rc = build_prog<double, true>(hIA, hJA, n, Up, nullptr, S.up64))) return rc;
-	if ((rc = build_prog<double, false>(hIA, hJA, n, Lo, &Up, S.lo64))) return rc;
-	if ((rc = build_prog<float, true>(hIA, hJA, n, Up, nullptr, S.up32))) return rc;
-	if ((rc = build_prog<float, false>(hIA, hJA, n, Lo, &Up, S.lo32))) return rc;
-	if ((rc = build_factor_prog(hIA, hJA, n, Lo, S))) return rc;
+	Blocks B = { t->o.ilu_blocks > 1 ? std::min(t->o.ilu_blocks, n) : 0, n };
+	std::vector<int> clo, cup;
+	HostLevels Lo = host_levels(hIA, hJA, n, true, B, &clo), Up = host_levels(hIA, hJA, n, false, B, &cup);
+	if ((rc = build_prog<double, true>(hIA, hJA, n, Up, nullptr, B, cup, S.up64))) return rc;
+	if ((rc = build_prog<double, false>(hIA, hJA, n, Lo, &Up, B, clo, S.lo64))) return rc;
+	if ((rc = build_prog<float, true>(hIA, hJA, n, Up, nullptr, B, cup, S.up32))) return rc;
+	if ((rc = build_prog<float, false>(hIA, hJA, n, Lo, &Up, B, clo, S.lo32))) return rc;
+	if ((rc = build_factor_prog(hIA, hJA, n, Lo, B, S))) return rc;
 	size_t nb = (size_t)std::max(Lo.pstart[Lo.nlev], Up.pstart[Up.nlev]) + 64;
 	FG_TRY(cudaMalloc((void **)&S.bl64, sizeof(double) * nb));
 	FG_TRY(cudaMalloc((void **)&S.y64, sizeof(double) * nb));
@@ -635,8 +679,9 @@ extern "C" int fg_ilu0_factor(femgpu_transport *t)
 {
 	cudaStream_t s = t->stream;
 	fg_ilu_sweeps &S = t->sweeps;
-	k_ilu0_factor_cta<<<1, FAC_THREADS, 0, s>>>(t->IA, t->A, S.lo64.rows, S.lo64.lev_start, S.lo64.nlev,
-	                                            S.fac_ptr, S.fac_prog, t->ilu.LU, t->ilu.Dinv, &t->st->err);
+	k_ilu0_factor_cta<<<S.lo64.nchunk, FAC_THREADS, 0, s>>>(t->IA, t->A, S.lo64.rows, S.lo64.lev_start,
+	                                                       S.lo64.nlev, S.lo64.chunk_lev, S.fac_ptr, S.fac_prog,
+	                                                       t->ilu.LU, t->ilu.Dinv, &t->st->err);
 	fg_sweep *pr[4] = { &S.lo64, &S.up64, &S.lo32, &S.up32 };
 	for (int i = 0; i < 4; i++) {
 		int g = fg_grid(pr[i]->nval);
@@ -662,12 +707,14 @@ static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, 
 	if (bytes < 0) return bytes;
 	a.prog = lo.prog; a.blk_off = lo.blk_off; a.sb_in = lo.sb_in; a.sb_inb = lo.sb_inb;
 	a.nlev = lo.nlev; a.nsb = lo.nsb; a.D = D; a.stage_bytes = sb;
-	launch_sweep<T, false>(a, bytes, s, bl, y, fma);
+	a.chunk_sb = lo.chunk_sb; a.chunk_lev = lo.chunk_lev;
+	launch_sweep<T, false>(a, lo.nchunk, bytes, s, bl, y, fma);
 	bytes = sweep_smem(up, sizeof(T), &D, &sb);
 	if (bytes < 0) return bytes;
 	a.prog = up.prog; a.blk_off = up.blk_off; a.sb_in = up.sb_in; a.sb_inb = up.sb_inb;
 	a.nlev = up.nlev; a.nsb = up.nsb; a.D = D; a.stage_bytes = sb;
-	launch_sweep<T, true>(a, bytes, s, y, (T *)z, fma);
+	a.chunk_sb = up.chunk_sb; a.chunk_lev = up.chunk_lev;
+	launch_sweep<T, true>(a, up.nchunk, bytes, s, y, (T *)z, fma);
 	return (int)cudaGetLastError();
 }
 
@@ -690,7 +737,8 @@ extern "C" void fg_ilu_free(femgpu_transport *t)
 	fg_sweep *all[4] = { &S.lo64, &S.up64, &S.lo32, &S.up32 };
 	for (int i = 0; i < 4; i++) {
 		void *p[] = { all[i]->prog, all[i]->blk_off, all[i]->sb_in, all[i]->sb_inb, all[i]->lev_start,
-		              all[i]->rows, all[i]->ppos, all[i]->val_off, all[i]->val_src };
+		              all[i]->rows, all[i]->ppos, all[i]->val_off, all[i]->val_src, all[i]->chunk_sb,
+		              all[i]->chunk_lev };
 		for (void *q : p) if (q) cudaFree(q);
 	}
 	void *v[] = { S.bl64, S.y64, S.bl32, S.y32, S.fac_ptr, S.fac_prog };

@@ -76,6 +76,10 @@ typedef struct femgpu_transport_opts {
 	                     /* inner solve inside the FP64 refinement           */
 	double stall_ratio;  /* learned preconditioner: fall back to ILU(0) when */
 	                     /* a restart cycle leaves rho > stall_ratio * rho0  */
+	int ilu_blocks;      /* 0: ILU(0) of the whole matrix (the reference's); */
+	                     /* P > 1: block ILU(0) over P contiguous row blocks */
+	                     /* of the numbering, couplings between blocks       */
+	                     /* dropped, one thread block per matrix block       */
 } femgpu_transport_opts;
 
 void femgpu_transport_default_opts(femgpu_transport_opts *o);
