@@ -19,7 +19,7 @@ import numpy as np
 
 from .build import LIB, build as _build
 
-__all__ = ["SSTransport", "Euler", "NavierStokes", "FemGpuError", "load", "OPTS"]
+__all__ = ["SSTransport", "Euler", "NavierStokes", "AMG", "FemGpuError", "load", "OPTS"]
 
 _lib = None
 
@@ -33,7 +33,7 @@ ERRORS = {
 OPTS = {
     "scheme": {"EBE": 0, "EDE": 1, "CSR": 2},
     "reorder": {"NOT": 0, "SYMRCM": 1},
-    "precond": {"NOT": 0, "ILU0": 1, "DIAG": 2, "BLOCKDIAG": 3, "LEARNED": 4},
+    "precond": {"NOT": 0, "ILU0": 1, "DIAG": 2, "BLOCKDIAG": 3, "LEARNED": 4, "AMG": 5},
     "shock": {"CAU": 0, "YZBETA": 1},
     "hshock": {"2SQRTAREA": 0, "SQRTAREA": 1, "OPTION1": 2, "OPTION2": 3},
     "precision": {"FP64": 0, "MIXED": 1, "MIXED_IR": 2},
@@ -166,6 +166,8 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
     L.femgpu_gnn_nparams.argtypes = []
     L.femgpu_gnn_destroy.argtypes = [_vp]
     L.femgpu_gnn_destroy.restype = None
+    L.femgpu_amg_destroy.argtypes = [_vp]
+    L.femgpu_amg_destroy.restype = None
     for name, args in {
         "femgpu_gnn_create": [ctypes.POINTER(_vp), ctypes.c_int, _vp],
         "femgpu_gnn_set_stream": [_vp, _vp],
@@ -181,6 +183,16 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_gnn_adam_step": [_vp, ctypes.c_float, ctypes.c_float],
         "femgpu_gnn_set_loss": [_vp, ctypes.c_int],
         "femgpu_transport_set_learned": [_vp, _vp],
+        "femgpu_amg_create": [ctypes.POINTER(_vp), ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int],
+        "femgpu_amg_set_stream": [_vp, _vp],
+        "femgpu_amg_setup": [_vp, ctypes.c_int, _vp, _vp, _vp],
+        "femgpu_amg_levels": [_vp],
+        "femgpu_amg_level": [_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp],
+        "femgpu_amg_apply": [_vp, _vp, _vp],
+        "femgpu_amg_apply_dev": [_vp, _vp, _vp],
+        "femgpu_transport_set_amg": [_vp, _vp],
+        "femgpu_dpa_match": [ctypes.c_int, _vp, _vp, _vp, ctypes.c_double, _vp],
+        "femgpu_dpa_galerkin": [ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_transport_krylov_pairs": [_vp, ctypes.c_int, _vp, _vp, ctypes.c_int],
         "femgpu_transport_csr_dev": [_vp, _vp, _vp, _vp],
     }.items():
@@ -418,6 +430,12 @@ class SSTransport:
         self._gnn = gnn
         self._check(self._L.femgpu_transport_set_learned(self._h, gnn.handle), "set_learned")
 
+    def set_amg(self, amg):
+        """Use an :class:`AMG` context as the FEMGPU_PREC_AMG preconditioner
+        (its hierarchy is rebuilt from the matrix at every precond_setup)."""
+        self._amg = amg
+        self._check(self._L.femgpu_transport_set_amg(self._h, amg.handle), "set_amg")
+
     def csr_dev(self):
         """(IA, JA, AA) device pointers of the CSR matrix."""
         p = [_vp(), _vp(), _vp()]
@@ -431,6 +449,78 @@ class SSTransport:
         if n < 0:
             raise FemGpuError(n, "krylov_pairs")
         return n
+
+
+class AMG:
+    """Double pairwise aggregation AMG preconditioner, parameters as the
+    deck string "AMG 2 NCL beta omega nr" (amg_precond.c:26-105): setup
+    builds the 2*NCL+1-level hierarchy on the host (AMG_precond_setup),
+    apply runs one V-cycle on the GPU (AMG_precond)."""
+
+    def __init__(self, ncl=2, beta=-1.0, omega=1.0, nr=2):
+        L = load()
+        self._L = L
+        h = _vp()
+        rc = L.femgpu_amg_create(ctypes.byref(h), int(ncl), float(beta), float(omega), int(nr))
+        if rc:
+            raise FemGpuError(rc, "amg_create")
+        self._h = h
+        self.n = 0
+
+    @classmethod
+    def from_spec(cls, spec):
+        """From the reference's deck string, e.g. "AMG 2 2 -1 1.0 2"."""
+        w = spec.split()
+        if len(w) < 6 or w[0] != "AMG" or int(w[1]) != 2:
+            raise ValueError(f"only the DPA form 'AMG 2 NCL beta omega nr' is provided: {spec!r}")
+        return cls(int(w[2]), float(w[3]), float(w[4]), int(w[5]))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, rc, where):
+        if rc:
+            raise FemGpuError(rc, where)
+
+    def setup(self, IA, JA, AA):
+        IA, JA, AA = _i32(IA), _i32(JA), _f64(AA)
+        self.n = IA.size - 1
+        self._check(self._L.femgpu_amg_setup(self._h, self.n, _ptr(IA), _ptr(JA), _ptr(AA)), "amg_setup")
+
+    def levels(self):
+        return self._L.femgpu_amg_levels(self._h)
+
+    def level(self, l):
+        """(IA, JA, AA, rmatch or None) of level l."""
+        nn = np.zeros(2, np.int32)
+        self._check(self._L.femgpu_amg_level(self._h, l, _ptr(nn), None, None, None, None), "amg_level")
+        n, nnz = int(nn[0]), int(nn[1])
+        IA, JA, AA = np.zeros(n + 1, np.int32), np.zeros(nnz, np.int32), np.zeros(nnz)
+        rm = np.zeros(n + 1, np.int32) if l < self.levels() - 1 else None
+        self._check(self._L.femgpu_amg_level(self._h, l, _ptr(nn), _ptr(IA), _ptr(JA), _ptr(AA), _ptr(rm)),
+                    "amg_level")
+        return IA, JA, AA, rm
+
+    def apply(self, q):
+        q = _f64(q)
+        z = np.zeros(self.n)
+        self._check(self._L.femgpu_amg_apply(self._h, _ptr(q), _ptr(z)), "amg_apply")
+        return z
+
+    def apply_dev(self, q_ptr, z_ptr):
+        self._check(self._L.femgpu_amg_apply_dev(self._h, _vp(q_ptr), _vp(z_ptr)), "amg_apply_dev")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.femgpu_amg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Euler:

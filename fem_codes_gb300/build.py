@@ -23,8 +23,9 @@ INC = ["-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-I" + HOST,
        "-I" + os.path.join(CUDA_HOME, "include")]
 
 # Translation units whose arithmetic must round every operation separately
-# (element build: bit-parity with the reference compiled without contraction).
-NO_FMA = {"build.cu", "ebe_block.cu", "euler_build.cu", "ns_build.cu"}
+# (element builds and the AMG smoother: bit-parity with the reference compiled
+# without contraction).
+NO_FMA = {"amg.cu", "build.cu", "ebe_block.cu", "euler_build.cu", "ns_build.cu"}
 
 
 def _sources():

@@ -139,6 +139,9 @@ struct femgpu_transport {
 	struct femgpu_gnn *gnn;
 	int fell_back;                  /* this solve switched to ILU(0)         */
 
+	/* AMG preconditioner (FEMGPU_PREC_AMG) */
+	struct femgpu_amg *amg;
+
 	/* timing */
 	cudaEvent_t ev[4];
 	float times[3];

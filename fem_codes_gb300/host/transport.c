@@ -126,8 +126,9 @@ int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts 
 	t = calloc(1, sizeof *t);
 	if (!t) return FEMGPU_E_NOMEM;
 	if (opts) t->o = *opts; else femgpu_transport_default_opts(&t->o);
-	if (t->o.scheme < 0 || t->o.scheme > 2 || t->o.precond < 0 || t->o.precond > 4 ||
+	if (t->o.scheme < 0 || t->o.scheme > 2 || t->o.precond < 0 || t->o.precond > 5 ||
 	    t->o.precond == FEMGPU_PREC_BLOCKDIAG ||
+	    (t->o.precond == FEMGPU_PREC_AMG && (t->o.scheme != FEMGPU_CSR || t->o.precision != FEMGPU_FP64)) ||
 	    (t->o.precond == FEMGPU_PREC_LEARNED && (t->o.scheme != FEMGPU_CSR || t->o.solver != FEMGPU_FGMRES ||
 	                                            t->o.precision != FEMGPU_FP64)) ||
 	    t->o.kmax < 1 || t->o.lmax < 1 || t->o.hshock < 0 || t->o.hshock > 3 ||
@@ -270,6 +271,7 @@ void femgpu_transport_destroy(femgpu_transport *t)
 	cudaStreamSynchronize(t->stream);
 	/* the network outlives this context: give it back its own stream */
 	if (t->gnn) femgpu_gnn_set_stream(t->gnn, NULL);
+	if (t->amg) femgpu_amg_set_stream(t->amg, NULL);
 	void *ptrs[] = { t->x, t->y, t->upresc, t->beta, t->fsrc, t->node_type, t->node_id, t->vert,
 		t->lm, t->ri_ptr, t->ri, t->IA, t->JA, t->sbe, t->diag, t->lm2, t->order, t->ec_ptr,
 		t->ec, t->e2_ptr, t->e2, t->A, t->ke, t->fe, t->A32, t->u, t->F, t->F0, t->invDiag,
@@ -290,6 +292,7 @@ int femgpu_transport_set_stream(femgpu_transport *t, void *stream)
 	CK(cudaStreamSynchronize(t->stream));
 	t->stream = stream ? (cudaStream_t)stream : t->own_stream;
 	if (t->gnn) KR(femgpu_gnn_set_stream(t->gnn, t->stream));
+	if (t->amg) KR(femgpu_amg_set_stream(t->amg, t->stream));
 	return 0;
 }
 
@@ -357,6 +360,27 @@ int femgpu_transport_build(femgpu_transport *t, const double *u_host, double *F_
 }
 
 /* ------------------------------------------------------- preconditioner */
+/* The AMG hierarchy of the current CSR matrix (set up on the host). */
+static int amg_rebuild(femgpu_transport *t)
+{
+	int rc, n = t->neq;
+	int *IA, *JA;
+	double *AA;
+	if (!t->amg) { fgh_set_error("AMG preconditioner not set"); return FEMGPU_E_NOT_BUILT; }
+	IA = malloc(sizeof(int) * ((size_t)n + 1));
+	JA = malloc(sizeof(int) * (size_t)(t->nnz ? t->nnz : 1));
+	AA = malloc(sizeof(double) * (size_t)(t->nnz ? t->nnz : 1));
+	rc = (IA && JA && AA) ? 0 : FEMGPU_E_NOMEM;
+	if (!rc && (cudaMemcpyAsync(IA, t->IA, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToHost, t->stream) ||
+	            cudaMemcpyAsync(JA, t->JA, sizeof(int) * (size_t)t->nnz, cudaMemcpyDeviceToHost, t->stream) ||
+	            cudaMemcpyAsync(AA, t->A, sizeof(double) * (size_t)t->nnz, cudaMemcpyDeviceToHost, t->stream) ||
+	            cudaStreamSynchronize(t->stream)))
+		rc = FEMGPU_E_CUDA;
+	if (!rc) rc = femgpu_amg_setup(t->amg, n, IA, JA, AA);
+	free(IA); free(JA); free(AA);
+	return rc;
+}
+
 int femgpu_transport_precond_setup_dev(femgpu_transport *t, int tag)
 {
 	(void)tag;   /* the symbolic phase of tag == 1 is done once at create */
@@ -376,6 +400,12 @@ int femgpu_transport_precond_setup_dev(femgpu_transport *t, int tag)
 		if (!t->gnn) { fgh_set_error("learned preconditioner not set"); return FEMGPU_E_NOT_BUILT; }
 		KR(femgpu_gnn_attach_csr_dev(t->gnn, t->neq, t->nnz, t->IA, t->JA, t->A));
 		t->fell_back = 0;
+	} else if (t->o.precond == FEMGPU_PREC_AMG) {
+		/* AMG_precond_setup (amg_precond.c:26-100): the hierarchy of the
+		 * current matrix on the host, then F := M^-1 F for pgmres */
+		int rc = amg_rebuild(t);
+		if (rc) return rc;
+		if (t->o.solver == FEMGPU_PGMRES) KR(fg_precond(t, t->F, t->F, NULL));
 	} else if (t->o.precond == FEMGPU_PREC_DIAG) {
 		KR(fg_diag_setup(t));
 	}
@@ -521,6 +551,15 @@ static int learned_cycles(femgpu_transport *t, const double *B, double *X, doubl
 		fgh_set_error("FGMRES (learned): %d restarts, rho %.3e > eps %.3e", l, k.st_host->rho, eps);
 		return FEMGPU_E_NOT_CONVERGED;
 	}
+	return 0;
+}
+
+int femgpu_transport_set_amg(femgpu_transport *t, femgpu_amg *g)
+{
+	if (!t || !g || t->o.precond != FEMGPU_PREC_AMG) return FEMGPU_E_ARG;
+	KR(femgpu_amg_set_stream(g, t->stream));
+	t->amg = g;
+	t->factored = 0;
 	return 0;
 }
 

@@ -43,7 +43,8 @@ enum femgpu_scheme   { FEMGPU_EBE = 0, FEMGPU_EDE = 1, FEMGPU_CSR = 2 };
 enum femgpu_reorder  { FEMGPU_REORDER_NOT = 0, FEMGPU_REORDER_SYMRCM = 1 };
 enum femgpu_precond  { FEMGPU_PREC_NOT = 0, FEMGPU_PREC_ILU0 = 1, FEMGPU_PREC_DIAG = 2,
                        FEMGPU_PREC_BLOCKDIAG = 3, /* Euler: nodal 4x4 blocks            */
-                       FEMGPU_PREC_LEARNED = 4    /* graph network, ILU(0) fallback    */ };
+                       FEMGPU_PREC_LEARNED = 4,   /* graph network, ILU(0) fallback    */
+                       FEMGPU_PREC_AMG = 5        /* DPA AMG V-cycle (femgpu_amg)      */ };
 enum femgpu_shock    { FEMGPU_SHOCK_CAU = 0, FEMGPU_SHOCK_YZBETA = 1 };
 enum femgpu_hshock   { FEMGPU_H_2SQRTAREA = 0, FEMGPU_H_SQRTAREA = 1,
                        FEMGPU_H_OPTION1 = 2, FEMGPU_H_OPTION2 = 3 };
@@ -382,6 +383,36 @@ int femgpu_transport_csr_dev(femgpu_transport *t, const int **IA, const int **JA
  * device arrays V, Z with leading dimension ld; returns the count (>= 0). */
 int femgpu_transport_krylov_pairs(femgpu_transport *t, int max, double *V, double *Z, int ld);
 
+/* ---- AMG preconditioner (double pairwise aggregation) ----------------------
+ * AMG_precond_setup / AMG_precond with the deck string "AMG 2 NCL beta omega
+ * nr" (00_CommonFiles/Solvers_and_Preconditioners/amg_precond.c:26-110):
+ * dpa_setup (CSR/AMG/amg_dpa.c:424-463) builds 2*NCL+1 levels by pairwise
+ * matching -- matching_c (amg_dpa.c:30-173) for beta >= 0, the
+ * half-approximate maximum-product matching bcm_CSRMatrixHMatch
+ * (bcm_linmatch.c) for beta == -1 -- and Galerkin products (dpa_galerkin,
+ * amg_dpa.c:175-392); the preconditioner is one dpa_Vcycle_precond
+ * (amg_dpa.c:485-506) with nr SOR sweeps of weight omega per level.  The
+ * set-up runs on the host, the V-cycle on the device; both give the
+ * reference's hierarchy and output bit for bit.  The classical Ruge-Stueben
+ * variant ("AMG 1 ...") and XDPA ("AMG 3 ...") are not provided. */
+typedef struct femgpu_amg femgpu_amg;
+int femgpu_amg_create(femgpu_amg **ctx, int ncl, double beta, double omega, int nr);
+void femgpu_amg_destroy(femgpu_amg *ctx);
+int femgpu_amg_set_stream(femgpu_amg *ctx, void *stream);
+/* Hierarchy of an n-row host CSR matrix (sorted rows, symmetric pattern). */
+int femgpu_amg_setup(femgpu_amg *ctx, int n, const int *IA, const int *JA, const double *AA);
+/* Matrices in the hierarchy (2*NCL+1), and level l's sizes n_nnz = {n, nnz}
+ * and (arrays may be NULL) CSR and matching rmatch [n+1] (partner or -1,
+ * rmatch[n] = number of pairs; levels below the coarsest). */
+int femgpu_amg_levels(const femgpu_amg *ctx);
+int femgpu_amg_level(const femgpu_amg *ctx, int l, int *n_nnz, int *IA, int *JA, double *AA, int *rmatch);
+/* z = M^-1 q, one V-cycle (q == z allowed). */
+int femgpu_amg_apply(femgpu_amg *ctx, const double *q_host, double *z_host);
+int femgpu_amg_apply_dev(femgpu_amg *ctx, const double *q, double *z);
+/* Use ctx as the FEMGPU_PREC_AMG preconditioner of a CSR transport context:
+ * precond_setup rebuilds the hierarchy from the current matrix. */
+int femgpu_transport_set_amg(femgpu_transport *t, femgpu_amg *ctx);
+
 /* ---- stateless device kernels (device pointers, stream as void*) -------- */
 /* csrmv.c:3-24 in FP64 / FP32 values. */
 int femgpu_csrmv_f64(int n, const int *IA, const int *JA, const double *AA,
@@ -412,6 +443,15 @@ int femgpu_symrcm(int n, const int *IA, const int *JA, int *perm);
 /* Dependency levels of the ILU(0) forward (lower != 0) or backward sweep:
  * returns the number of levels. */
 int femgpu_ilu_levels(int n, const int *IA, const int *JA, int lower);
+/* One step of the AMG set-up: the pairwise matching of matching_c
+ * (amg_dpa.c:30-173, beta >= 0) or bcm_CSRMatrixHMatch (bcm_linmatch.c,
+ * beta == -1), rmatch [n+1] as in femgpu_amg_level; and the Galerkin
+ * product dpa_galerkin (amg_dpa.c:175-392): nc_nnz = {rows, nnz} of the
+ * coarse matrix, whose CSR goes to IC/JC/AC when they are given (call once
+ * with NULL arrays for the sizes). */
+int femgpu_dpa_match(int n, const int *IA, const int *JA, const double *AA, double beta, int *rmatch);
+int femgpu_dpa_galerkin(int n, const int *IA, const int *JA, const double *AA, const int *rmatch, int *nc_nnz,
+		int *IC, int *JC, double *AC);
 
 /* Last CUDA/device error text of this thread (static buffer). */
 const char *femgpu_last_error(void);

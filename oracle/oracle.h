@@ -170,6 +170,18 @@ double orc_eta_newton(int ecase, double nF, double nFold, double etaold, int pri
 int orc_ns_newton(const orc_ns *p, int kmax, int lmax, double eta0, int ecase, double tolnl, int maxit,
                   double *uhist, double *normF, double *wout, int *gmres);
 
+/* ---- AMG (double pairwise aggregation) ------------------------------------ */
+/* One dpa_Vcycle_precond (amg_dpa.c:485-506): z = M^-1 q over nlev levels
+ * given as concatenated CSR arrays (n[l] rows each; IA blocks of n[l]+1
+ * offsets local to the level, JA/AA blocks of IA_l[n[l]] entries) and the
+ * matchings of levels 0..nlev-2 (blocks of n[l]+1). */
+int orc_amg_vcycle(int nlev, const int *n, const int *IA, const int *JA, const double *AA, const int *rm,
+                   double omega, int nr, const double *q, double *z);
+/* pgmres with csrmv (level 0) and that V-cycle, B := M^-1 B first (the
+ * AMG_precond_setup side effect); returns the inner iterations. */
+int orc_amg_gmres(int nlev, const int *n, const int *IA, const int *JA, const double *AA, const int *rm,
+                  double omega, int nr, int kmax, int lmax, double tol, double *B, double *X);
+
 #ifdef __cplusplus
 }
 #endif

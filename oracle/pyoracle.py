@@ -66,6 +66,12 @@ def lib() -> ctypes.CDLL:
         L.orc_csr_gmres.restype = ctypes.c_int
         L.orc_csr_gmres.argtypes = [ctypes.c_int, _ip, _ip, _dp, ctypes.c_int, ctypes.c_int,
                                     ctypes.c_int, ctypes.c_double, _dp, _dp]
+        L.orc_amg_vcycle.restype = ctypes.c_int
+        L.orc_amg_vcycle.argtypes = [ctypes.c_int, _ip, _ip, _ip, _dp, _ip, ctypes.c_double, ctypes.c_int,
+                                     _dp, _dp]
+        L.orc_amg_gmres.restype = ctypes.c_int
+        L.orc_amg_gmres.argtypes = [ctypes.c_int, _ip, _ip, _ip, _dp, _ip, ctypes.c_double, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp, _dp]
         L.orc_ddot.restype = ctypes.c_double
         L.orc_ddot.argtypes = [ctypes.c_int, _dp, _dp]
         L.orc_get_times.restype = None
@@ -271,6 +277,33 @@ def csr_gmres(IA, JA, AA, B, use_ilu0=True, kmax=30, lmax=1000, tol=1e-8):
     it = L.orc_csr_gmres(n, _c(IA, np.int32), _c(JA, np.int32), _c(AA, np.float64),
                          1 if use_ilu0 else 0, kmax, lmax, tol, B, X)
     return X, it, B
+
+
+def _amg_pack(levels):
+    n = np.array([lv[0].size - 1 for lv in levels], np.int32)
+    IA = np.concatenate([lv[0] for lv in levels]).astype(np.int32)
+    JA = np.concatenate([lv[1] for lv in levels]).astype(np.int32)
+    AA = np.concatenate([lv[2] for lv in levels]).astype(np.float64)
+    rm = np.concatenate([lv[3] for lv in levels[:-1]] + [np.zeros(1, np.int32)]).astype(np.int32)
+    return n, IA, JA, AA, rm
+
+
+def amg_vcycle(levels, omega, nr, q):
+    """One dpa_Vcycle_precond over levels [(IA, JA, AA, rmatch), ...]."""
+    n, IA, JA, AA, rm = _amg_pack(levels)
+    z = np.zeros(n[0])
+    lib().orc_amg_vcycle(len(levels), n, IA, JA, AA, rm, float(omega), int(nr), _c(q[: n[0]], np.float64), z)
+    return z
+
+
+def amg_gmres(levels, omega, nr, B, kmax=30, lmax=1000, tol=1e-8):
+    """pgmres + AMG V-cycle on the level-0 system; returns (X, iterations, M^-1 B)."""
+    n, IA, JA, AA, rm = _amg_pack(levels)
+    B = np.array(B[: n[0]], dtype=np.float64, copy=True)
+    B = np.concatenate([B, [0.0]])
+    X = np.zeros(n[0] + 1)
+    it = lib().orc_amg_gmres(len(levels), n, IA, JA, AA, rm, float(omega), int(nr), kmax, lmax, tol, B, X)
+    return X[: n[0]], it, B[: n[0]]
 
 
 class EulerParams(ctypes.Structure):

@@ -4,7 +4,8 @@ transport solve (libfemref.so, oracle/ref_harness.c), the multi-dof EBE
 operators (libfemref_*_blk.so, oracle/ref_block_harness.c), the 2D Euler
 build and predictor (libfemref_euler.so, oracle/ref_euler_harness.c) and the
 steady Navier-Stokes VMS build and damped Newton (libfemref_ns.so,
-oracle/ref_ns_harness.c).
+oracle/ref_ns_harness.c) and the double-pairwise AMG preconditioner
+(libfemref_amg.so, oracle/ref_amg_harness.c).
 
 Usage:  python tests/golden/make_golden.py        (writes tests/golden/*.npz)
 
@@ -315,7 +316,84 @@ def main_ns():
         print(f"{name}: neq={neq} nel={mesh.nel} newton={nit} |F|={nF[:nit]} gmres={g[:nit]}")
 
 
+# name -> (nx, ny, perturb, node rule, transport kwargs, AMG deck string)
+AMG_CASES = {
+    "amg_skew20x16_hmatch": (20, 16, 0.2, "inflow", dict(problem="SKEW"), "AMG 2 2 -1 1.0 2"),
+    "amg_skew20x16_count": (20, 16, 0.2, "inflow", dict(problem="SKEW"), "AMG 2 2 0.25 1.0 2"),
+    "amg_conv28x20_rcm": (28, 20, 0.1, "all", dict(problem="CONVECTION", reord="SYMRCM"), "AMG 2 3 -1 0.9 1"),
+    "amg_reaction24_beta0": (24, 24, 0.0, "all", dict(problem="REACTION"), "AMG 2 1 0 1.2 3"),
+}
+
+
+def amg_lib():
+    """A fresh copy of libfemref_amg.so (the reference keeps its AMG state
+    and the matching's pair counter in globals)."""
+    import shutil
+    import tempfile
+    d = tempfile.mkdtemp()
+    path = os.path.join(d, "libfemref_amg.so")
+    shutil.copy(os.path.join(ROOT, "oracle", "_ref", "libfemref_amg.so"), path)
+    L = ctypes.CDLL(path)
+    L.ref_amg_setup.argtypes = [ctypes.c_int, _ip, _ip, _dp, ctypes.c_char_p, _dp, _ip]
+    L.ref_amg_level.argtypes = [ctypes.c_int, _ip, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                ctypes.c_void_p]
+    L.ref_amg_apply.argtypes = [_dp, _dp]
+    L.ref_amg_gmres.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp, _dp]
+    L.ref_amg_gmres.restype = ctypes.c_int
+    return L
+
+
+def main_amg():
+    """AMG_precond_setup / AMG_precond (DPA) and the AMG-preconditioned
+    pgmres on steady-transport CSR matrices built by the reference
+    (oracle/ref_amg_harness.c): every level's CSR and matching, M^-1 F, two
+    V-cycle applications and the GMRES solution."""
+    lib = load_ref()
+    for name, (nx, ny, pert, rule, kw, spec) in AMG_CASES.items():
+        mesh = structured_mesh(nx, ny, perturb=pert, seed=99)
+        out = run_ref(lib, mesh, node_types(mesh, rule), scheme="CSR", precond="NOT", npicard=1, **kw)
+        IA, JA = out["IA"], out["JA"]
+        n, nnz = IA.size - 1, JA.size
+        AA = np.ascontiguousarray(out["Afirst"][:nnz])
+        F0 = np.ascontiguousarray(out["Ffirst"][:n])
+        L = amg_lib()
+        F = np.concatenate([F0, [0.0]])
+        info = np.zeros(4, np.int32)
+        L.ref_amg_setup(n, IA, JA, AA, spec.encode(), F, info)
+        levels = {}
+        for l in range(int(info[0])):
+            nn = np.zeros(2, np.int32)
+            L.ref_amg_level(l, nn, None, None, None, None)
+            a, b, c = np.zeros(nn[0] + 1, np.int32), np.zeros(nn[1], np.int32), np.zeros(nn[1])
+            rm = np.zeros(nn[0] + 1, np.int32) if l < info[0] - 1 else None
+            L.ref_amg_level(l, nn, a.ctypes.data_as(ctypes.c_void_p), b.ctypes.data_as(ctypes.c_void_p),
+                            c.ctypes.data_as(ctypes.c_void_p),
+                            None if rm is None else rm.ctypes.data_as(ctypes.c_void_p))
+            levels.update({f"IA{l}": a, f"JA{l}": b, f"AA{l}": c})
+            if rm is not None:
+                levels[f"rm{l}"] = rm
+        rng = np.random.default_rng(5)
+        qs = rng.uniform(-1.0, 1.0, (2, n))
+        zs = np.zeros((2, n))
+        for k in range(2):
+            L.ref_amg_apply(np.ascontiguousarray(qs[k]), zs[k])
+        B = F.copy()
+        X = np.zeros(n + 1)
+        kmax, lmax, tol = 30, 200, 1e-8
+        it = L.ref_amg_gmres(kmax, lmax, tol, B, X)
+        ntype = node_types(mesh, rule)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), spec=np.array(spec), IA=IA, JA=JA, AA=AA, F=F0,
+                            x=mesh.x, y=mesh.y, vert=mesh.vert, node_type=ntype, beta=out["beta"],
+                            fsrc=out["fsrc"], upresc=out["upresc"], problem=np.array(kw["problem"]),
+                            reord=np.array(kw.get("reord", "NOT")),
+                            nlev=int(info[0]), Fprec=F[:n], q=qs, z=zs, kmax=kmax, lmax=lmax, tol=tol,
+                            X=X[:n], iters=it, **levels)
+        sizes = [levels[f"IA{l}"].size - 1 for l in range(int(info[0]))]
+        print(f"{name}: n={n} nnz={nnz} levels={sizes} gmres={it}")
+
+
 def main():
+    main_amg()
     main_ns()
     main_euler()
     main_blocks()

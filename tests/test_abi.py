@@ -42,7 +42,7 @@ def test_element_builds_compiled_without_contraction():
     reference (element builds and block operators) are compiled with
     --fmad=false."""
     from fem_codes_gb300 import build as b
-    assert {"build.cu", "ebe_block.cu", "euler_build.cu", "ns_build.cu"} <= b.NO_FMA
+    assert {"amg.cu", "build.cu", "ebe_block.cu", "euler_build.cu", "ns_build.cu"} <= b.NO_FMA
 
 
 def test_euler_bad_options_rejected_without_gpu(lib):
