@@ -4,14 +4,19 @@
 Workload: 2D advection-diffusion on the unit square, 2048x1024 cells split
 into 4,194,304 linear triangles (2,100,225 nodes), interior nodes perturbed by
 a seeded uniform offset of +-0.2h (seed 1234), k = 1e-4, beta = (cos30, sin30),
-f = 0, SUPG + CAU shock capturing, CSR storage with SYMRCM reordering.
+f = 0, SUPG + CAU shock capturing, CSR storage in the mesh's own node
+numbering (the reference's "reordering NOT"; --reorder SYMRCM for its reverse
+Cuthill-McKee option).
 
 A step is one nonlinear (Picard) iteration: element build and assembly,
 ILU(0) factorisation, and the linear solve to a relative residual of 1e-8 on
-the unpreconditioned FP64 residual ||F - A u|| / ||F|| (right-preconditioned
-flexible GMRES(50); the reference's left-preconditioned stopping rule is not
-used because it accepts residuals of 1e-1 on this mesh).  Steps continue the
-Picard sequence from the warm-up steps.
+the unpreconditioned FP64 residual ||F - A u|| / ||F||, checked on the true
+residual (right-preconditioned flexible GMRES(80); the reference's
+left-preconditioned stopping rule is not used because it accepts residuals of
+1e-1 on this mesh).  Default preconditioner: block ILU(0) over 8 contiguous
+row blocks of the SYMRCM numbering, each factorised and swept by its own
+thread block (--ilu-blocks 0: ILU(0) of the whole matrix, one level-scheduled
+sweep).  Steps continue the Picard sequence from the warm-up steps.
 
 Arms: --impl ours (default): the GPU library through its device API (value)
 and through the host-buffer C ABI (e2e).  --impl reference: the reference's
@@ -46,10 +51,11 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nx", type=int, default=2048)
     ap.add_argument("--ny", type=int, default=1024)
-    ap.add_argument("--precision", default="MIXED", choices=["FP64", "MIXED", "MIXED_IR"])
+    ap.add_argument("--precision", default="FP64", choices=["FP64", "MIXED", "MIXED_IR"])
     ap.add_argument("--precond", default="ILU0")
-    ap.add_argument("--kmax", type=int, default=50)
-    ap.add_argument("--ilu-blocks", type=int, default=0,
+    ap.add_argument("--reorder", default="SYMRCM", choices=["NOT", "SYMRCM"])
+    ap.add_argument("--kmax", type=int, default=80)
+    ap.add_argument("--ilu-blocks", type=int, default=8,
                     help="0: ILU(0) of the whole matrix; P > 1: block ILU(0) over P row blocks")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="transport", choices=["transport", "euler"])
@@ -76,8 +82,11 @@ def workload(nx, ny):
 
 def config(a):
     return {"workload": f"steady transport SUPG+CAU {a.nx}x{a.ny} cells ({2 * a.nx * a.ny} triangles), "
-                        "perturbed +-0.2h, CSR+SYMRCM, ILU(0)-FGMRES(50), rel tol 1e-8 (true residual)",
-            "nx": a.nx, "ny": a.ny, "precision": a.precision, "precond": a.precond, "kmax": a.kmax,
+                        f"perturbed +-0.2h, CSR ({a.reorder} numbering), "
+                        + (f"block ILU(0) x{a.ilu_blocks}" if a.ilu_blocks > 1 else "ILU(0)")
+                        + f"-FGMRES({a.kmax}) {a.precision}, rel tol 1e-8 (true residual)",
+            "nx": a.nx, "ny": a.ny, "reorder": a.reorder, "precision": a.precision, "precond": a.precond,
+            "kmax": a.kmax,
             "ilu_blocks": a.ilu_blocks,
             "step": "build + ILU(0) factor + solve to 1e-8", "l2": "inputs larger than L2 (matrix+factors > 129 MB)"}
 
@@ -127,12 +136,12 @@ class Clocks:
 
 
 # --------------------------------------------------------------------- CPU
-def cpu_run(m, p, npicard, kmax):
+def cpu_run(m, p, npicard, kmax, reorder):
     """The reference's algorithm (oracle restatement, one core): set-up, then
     npicard Picard steps with its ILU(0) and left-preconditioned pgmres."""
     from oracle import pyoracle
     out = pyoracle.run_transport(m.x, m.y, p.node_type, m.vert, p.k, p.gamma, p.beta, p.fsrc, p.upresc,
-                                 scheme="CSR", reord="SYMRCM", precond="ILU0", kmax=kmax, lmax=1000,
+                                 scheme="CSR", reord=reorder, precond="ILU0", kmax=kmax, lmax=1000,
                                  tol=1e-8, npicard=npicard)
     times, steps = pyoracle.last_times(npicard)
     import scipy.sparse as sp
@@ -149,7 +158,7 @@ def run_reference(a):
         return
     m, p = workload(a.nx, a.ny)
     n = a.warmup + a.steps
-    times, steps, iters, rel = cpu_run(m, p, n, a.kmax)
+    times, steps, iters, rel = cpu_run(m, p, n, a.kmax, a.reorder)
     timed = steps[a.warmup:]
     ms = 1e3 * float(np.mean(timed))
     cores = 1
@@ -185,13 +194,13 @@ def run_ours(a):
     m, p = workload(a.nx, a.ny)
     if rank == 0 and not a.no_cpu_baseline:
         # bounded sample: one Picard step of the same workload on one core
-        times, steps, iters, rel = cpu_run(m, p, 1, a.kmax)
+        times, steps, iters, rel = cpu_run(m, p, 1, a.kmax, a.reorder)
         cpu = {"value": 1e3 * float(steps[0]), "unit": "ms", "cores": 1, "kind": "port",
                "sample": f"1 Picard step of the full workload, reference algorithm (left-preconditioned "
                          f"pgmres, {int(iters[0])} iters, true rel. residual {rel:.2e}), set-up "
                          f"{times[0]:.1f} s excluded"}
 
-    T = fg.SSTransport.from_problem(m, p, scheme="CSR", reorder="SYMRCM", precond=a.precond, kmax=a.kmax,
+    T = fg.SSTransport.from_problem(m, p, scheme="CSR", reorder=a.reorder, precond=a.precond, kmax=a.kmax,
                                     lmax=200, tol=1e-8, solver="FGMRES", precision=a.precision,
                                     inner_tol=1e-4, ir_max=40, ilu_blocks=a.ilu_blocks)
     L = T._L
@@ -315,15 +324,17 @@ WEIGHTS = os.path.join(ROOT, "fem_codes_gb300", "weights", "gnn_transport.npy")
 def learned_leg(m, p, a, s, steps=1):
     """Time to solution of the same Picard step with the learned
     preconditioner (FGMRES(kmax), FP64 Arnoldi, bf16 network activations,
-    ILU(0) fallback on a stalled cycle); None without trained weights."""
+    fallback to the step's ILU(0) on a stalled cycle); None without trained
+    weights."""
     import torch
     import fem_codes_gb300 as fg
     from fem_codes_gb300.learned import MeshGNN
     if not os.path.exists(WEIGHTS):
         return None
     net = MeshGNN(np.load(WEIGHTS))
-    T = fg.SSTransport.from_problem(m, p, scheme="CSR", reorder="SYMRCM", precond="LEARNED", kmax=a.kmax,
-                                    lmax=400, tol=1e-8, solver="FGMRES", precision="FP64", stall_ratio=0.9)
+    T = fg.SSTransport.from_problem(m, p, scheme="CSR", reorder=a.reorder, precond="LEARNED", kmax=a.kmax,
+                                    lmax=400, tol=1e-8, solver="FGMRES", precision="FP64", stall_ratio=0.9,
+                                    ilu_blocks=a.ilu_blocks)
     T.set_stream(s.cuda_stream)
     T.set_learned(net)
     out = {}

@@ -47,6 +47,11 @@ typedef struct fg_ilu_sweeps {
 	double *bl64, *y64;
 	float *bl32, *y32;
 	int *fac_ptr, *fac_prog;   /* precompiled elimination of each row        */
+	/* the same elimination for the cluster kernel: per level-order position
+	 * {rb, offset, length, len | dpos << 8 | ngroups << 16}, and per row
+	 * [nops, operand addresses..., per group (q, cnt, dst...)] */
+	int *fac2_hdr, *fac2;
+	int fac2_ok;
 } fg_ilu_sweeps;
 
 typedef struct fg_ilu {
@@ -171,6 +176,8 @@ int fg_precond(femgpu_transport *t, const double *p, double *z, const int *activ
  * 1: FP32 preconditioner, 2: FP32 preconditioner and operator). */
 int fg_kry_pgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X);
 int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int mixed);
+/* st->rho = ||B - A X|| (overwrites V[0]). */
+int fg_kry_true_rho(const fg_krylov *k, const fg_linop *op, const double *B, double *X);
 int fg_kry_dot(const fg_krylov *k, const double *a, const double *b, int n, double *out_dev);
 /* The transport context's Krylov buffers and operator as a view. */
 void fg_transport_krylov(femgpu_transport *t, fg_krylov *k, fg_linop *op);

@@ -357,6 +357,166 @@ k_ilu0_factor_cta(const int *__restrict__ IA, const double *__restrict__ AA,
 	}
 }
 
+// The same factorisation on a thread-block cluster: each level's rows are
+// split over the cluster's CTAs (a single SM's FP64 pipe would otherwise
+// bound it), with one cluster barrier per level.  A row's loads come in three
+// rounds -- its header; its matrix values and elimination program; every
+// operand from earlier levels (pivots and U entries, read from L2: other CTAs
+// wrote them) -- and the first two do not depend on the factorisation, so
+// for each thread's first row of the next level they are issued during the
+// current level (header into registers at its start, values and program by
+// cp.async into the other half of a double buffer before the barrier).  After
+// a barrier only the operand round and the arithmetic remain.  The
+// arithmetic is the reference's, in its order.
+#define FAC2_T 64                     // threads per CTA
+#define FAC2_MAXP 64                  // program ints per row
+#define FAC2_MAXOPS 32                // operands per row
+#define FAC2_BUF (FAC2_T * ((FAC_CAP + 1) * 8 + FAC2_MAXP * 4))
+#define FAC2_SMEM (FAC2_T * FAC2_MAXOPS * 8 + 2 * FAC2_BUF)
+
+__device__ __forceinline__ void cluster_barrier()
+{
+	asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+	asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_rank()
+{
+	unsigned r;
+	asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+	return r;
+}
+
+__device__ __forceinline__ unsigned cluster_size()
+{
+	unsigned r;
+	asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+	return r;
+}
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src)
+{
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" :: "r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(void *dst, const void *src)
+{
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" :: "r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+__global__ void __launch_bounds__(FAC2_T)
+k_ilu0_factor_cluster(const double *__restrict__ AA, const int *__restrict__ rows,
+                      const int *__restrict__ lev_start, int nlev, const int4 *__restrict__ hdr,
+                      const int *__restrict__ prog, double *LU, double *Dinv, int *err)
+{
+	extern __shared__ __align__(16) unsigned char fsm[];
+	// per-thread scratch, element i of thread t at [i * FAC2_T + t] (no bank conflicts)
+	double *so = (double *)fsm + threadIdx.x;
+	unsigned char *bufs = fsm + FAC2_T * FAC2_MAXOPS * 8;
+#define SO(i) so[(i) * FAC2_T]
+#define SV(B, i) ((double *)(bufs + (B) * FAC2_BUF))[(i) * FAC2_T + threadIdx.x]
+#define SP(B, i) ((int *)(bufs + (B) * FAC2_BUF + FAC2_T * (FAC_CAP + 1) * 8))[(i) * FAC2_T + threadIdx.x]
+	const int C = (int)cluster_size(), rank = (int)cluster_rank(), tid = (int)threadIdx.x;
+	// level bounds: [b, e) this level, e1 the next level's end, e2 the one after
+	int b = lev_start[0], e = nlev > 0 ? lev_start[1] : 0, e1 = nlev > 1 ? lev_start[2] : e;
+	int cur = 0, have = 0;                   // buffer of the prefetched first row; its validity
+	int4 ph = make_int4(0, 0, 0, 0);
+	int pr_ = 0;
+	for (int l = 0; l < nlev; l++) {
+		int e2 = (l + 3 <= nlev) ? lev_start[l + 3] : e1;
+		int per = (e - b + C - 1) / C, p0 = b + rank * per, p1 = min(e, p0 + per);
+		// round 1 of the next level's first row, into registers
+		int nper = (e1 - e + C - 1) / C, np0 = e + rank * nper, np1 = min(e1, np0 + nper);
+		int np = np0 + tid;
+		bool nhave = (l + 1 < nlev) && np < np1;
+		int4 nh = make_int4(0, 0, 0, 0);
+		int nr = 0;
+		if (nhave) { nh = hdr[np]; nr = rows[np]; }
+		for (int p = p0 + tid; p < p1; p += FAC2_T) {
+			int4 h;
+			int r;
+			const int B = cur;
+			if (p == p0 + tid && have) {
+				h = ph; r = pr_;
+				cp_async_wait_all();
+			} else {
+				h = hdr[p]; r = rows[p];
+				const int len0 = h.w & 255;
+				for (int q0 = 0; q0 < len0; q0 += 8) {
+					double t[8];
+#pragma unroll
+					for (int u = 0; u < 8; u++) t[u] = (q0 + u < len0) ? AA[h.x + q0 + u] : 0.0;
+#pragma unroll
+					for (int u = 0; u < 8; u++) if (q0 + u < len0) SV(B, q0 + u) = t[u];
+				}
+				for (int i0 = 0; i0 < h.z; i0 += 8) {
+					int t[8];
+#pragma unroll
+					for (int u = 0; u < 8; u++) t[u] = (i0 + u < h.z) ? prog[h.y + i0 + u] : 0;
+#pragma unroll
+					for (int u = 0; u < 8; u++) if (i0 + u < h.z) SP(B, i0 + u) = t[u];
+				}
+			}
+			const int rb = h.x, len = h.w & 255, dpos = (h.w >> 8) & 255, ng = h.w >> 16;
+			// round 3: pivots (code < 0: -1-row) and U entries of earlier levels
+			const int nops = SP(B, 0);
+			for (int i0 = 0; i0 < nops; i0 += 8) {
+				double t[8];
+#pragma unroll
+				for (int u = 0; u < 8; u++) {
+					int a = (i0 + u < nops) ? SP(B, 1 + i0 + u) : 0;
+					t[u] = (i0 + u < nops) ? __ldcg(a >= 0 ? LU + a : Dinv + (-1 - a)) : 0.0;
+				}
+#pragma unroll
+				for (int u = 0; u < 8; u++) if (i0 + u < nops) SO(i0 + u) = t[u];
+			}
+			// the elimination (ILUp_precond_setup.c:119-139), in the reference's order
+			double d = SV(B, dpos);
+			int gp = 1 + nops, oi = 0;
+			for (int gi = 0; gi < ng; gi++) {
+				int q = SP(B, gp), cnt = SP(B, gp + 1);
+				double lq = __dmul_rn(SV(B, q), SO(oi));
+				oi++;
+				SV(B, q) = lq;
+				for (int c = 0; c < cnt; c++) {
+					double prod = __dmul_rn(lq, SO(oi));
+					oi++;
+					int dst = SP(B, gp + 2 + c);
+					if (dst < 0) d = __dsub_rn(d, prod);
+					else SV(B, dst) = __dsub_rn(SV(B, dst), prod);
+				}
+				gp += 2 + cnt;
+			}
+			for (int q = 0; q < len; q++) LU[rb + q] = (q == dpos) ? d : SV(B, q);
+			if (d == 0.0) { fg_set_err(err, FEMGPU_E_ZERO_PIVOT); Dinv[r] = 0.0; }
+			else Dinv[r] = 1.0 / d;
+		}
+		// round 2 of the next level's first row: cp.async into the other buffer
+		if (nhave) {
+			const int B = cur ^ 1, len = nh.w & 255;
+			for (int q = 0; q < len; q++) cp_async8(&SV(B, q), AA + nh.x + q);
+			for (int i = 0; i < nh.z; i++) cp_async4(&SP(B, i), prog + nh.y + i);
+			cp_async_commit();
+			cur = B;
+		}
+		have = nhave;
+		ph = nh;
+		pr_ = nr;
+		__syncwarp();
+		cluster_barrier();
+		b = e;
+		e = e1;
+		e1 = e2;
+	}
+	cp_async_wait_all();
+#undef SO
+#undef SV
+#undef SP
+}
+
 // ------------------------------------------------------- host: programs
 struct HostLevels {
 	int nlev;
@@ -592,6 +752,80 @@ static int build_factor_prog(const int *IA, const int *JA, int n, const HostLeve
 	return up_vec(&S.fac_prog, prog);
 }
 
+// The elimination program of k_ilu0_factor_cluster (no matrix blocks): per
+// level-order position a header and a row program whose operand addresses
+// come first.  fac2_ok = 0 when a row exceeds the kernel's per-row capacity.
+static int build_factor_prog2(const int *IA, const int *JA, int n, const HostLevels &Lo, fg_ilu_sweeps &S)
+{
+	std::vector<int> hdr((size_t)n * 4), prog, ops, grp;
+	prog.reserve((size_t)n * 28);
+	S.fac2_ok = 1;
+	for (int p = 0; p < n; p++) {
+		int r = Lo.rows[p], rb = IA[r], len = IA[r + 1] - rb, dpos = -1, ng = 0;
+		for (int q = 0; q < len; q++) if (JA[rb + q] == r) dpos = q;
+		ops.clear();
+		grp.clear();
+		for (int q = 0; q < len && JA[rb + q] < r; q++) {
+			int jrow = JA[rb + q];
+			size_t g = grp.size();
+			grp.push_back(q);
+			grp.push_back(0);
+			ops.push_back(-1 - jrow);
+			for (int k = IA[jrow]; k < IA[jrow + 1]; k++) {
+				int col = JA[k], pos = -1;
+				if (col <= jrow) continue;
+				for (int m = 0; m < len; m++) if (JA[rb + m] == col) { pos = m; break; }
+				if (pos < 0) continue;
+				grp.push_back(col == r ? -1 : pos);
+				ops.push_back(k);
+				grp[g + 1]++;
+			}
+			ng++;
+		}
+		int plen = 1 + (int)ops.size() + (int)grp.size();
+		if (len > FAC_CAP || dpos < 0 || plen > FAC2_MAXP || (int)ops.size() > FAC2_MAXOPS || ng > 32767) {
+			S.fac2_ok = 0;
+			return 0;
+		}
+		hdr[4 * (size_t)p] = rb;
+		hdr[4 * (size_t)p + 1] = (int)prog.size();
+		hdr[4 * (size_t)p + 2] = plen;
+		hdr[4 * (size_t)p + 3] = len | (dpos << 8) | (ng << 16);
+		prog.push_back((int)ops.size());
+		prog.insert(prog.end(), ops.begin(), ops.end());
+		prog.insert(prog.end(), grp.begin(), grp.end());
+	}
+	int rc;
+	if ((rc = up_vec(&S.fac2_hdr, hdr))) return rc;
+	return up_vec(&S.fac2, prog);
+}
+
+// Cluster size for the factorisation: 16 CTAs when the device can place such
+// a cluster, else 8 (0: no cluster launch; the single-block kernel runs).
+static int factor_cluster_size(void)
+{
+	static int C = -1;
+	if (C < 0) {
+		C = 0;
+		if (cudaFuncSetAttribute(k_ilu0_factor_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, FAC2_SMEM) !=
+		    cudaSuccess) { cudaGetLastError(); return C; }
+		cudaFuncSetAttribute(k_ilu0_factor_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+		cudaGetLastError();
+		for (int c = 16; c >= 8 && !C; c /= 2) {
+			cudaLaunchConfig_t cfg = {};
+			cudaLaunchAttribute at[1];
+			at[0].id = cudaLaunchAttributeClusterDimension;
+			at[0].val.clusterDim.x = (unsigned)c; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+			cfg.gridDim = dim3((unsigned)c); cfg.blockDim = dim3(FAC2_T); cfg.dynamicSmemBytes = FAC2_SMEM;
+			cfg.attrs = at; cfg.numAttrs = 1;
+			int ncl = 0;
+			if (cudaOccupancyMaxActiveClusters(&ncl, k_ilu0_factor_cluster, &cfg) == cudaSuccess && ncl >= 1) C = c;
+			cudaGetLastError();
+		}
+	}
+	return C;
+}
+
 #define SW_SET(T, U, CW, F) FG_TRY(cudaFuncSetAttribute(k_sweep<T, U, CW, F>, \
 	cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP))
 #define SW_SET_CW(CW) SW_SET(double, false, CW, false); SW_SET(double, true, CW, false); \
@@ -658,6 +892,8 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 	if ((rc = build_prog<float, true>(hIA, hJA, n, Up, nullptr, B, cup, S.up32))) return rc;
 	if ((rc = build_prog<float, false>(hIA, hJA, n, Lo, &Up, B, clo, S.lo32))) return rc;
 	if ((rc = build_factor_prog(hIA, hJA, n, Lo, B, S))) return rc;
+	S.fac2_ok = 0;
+	if (!B.P && (rc = build_factor_prog2(hIA, hJA, n, Lo, S))) return rc;
 	size_t nb = (size_t)std::max(Lo.pstart[Lo.nlev], Up.pstart[Up.nlev]) + 64;
 	FG_TRY(cudaMalloc((void **)&S.bl64, sizeof(double) * nb));
 	FG_TRY(cudaMalloc((void **)&S.y64, sizeof(double) * nb));
@@ -679,9 +915,22 @@ extern "C" int fg_ilu0_factor(femgpu_transport *t)
 {
 	cudaStream_t s = t->stream;
 	fg_ilu_sweeps &S = t->sweeps;
-	k_ilu0_factor_cta<<<S.lo64.nchunk, FAC_THREADS, 0, s>>>(t->IA, t->A, S.lo64.rows, S.lo64.lev_start,
-	                                                       S.lo64.nlev, S.lo64.chunk_lev, S.fac_ptr, S.fac_prog,
-	                                                       t->ilu.LU, t->ilu.Dinv, &t->st->err);
+	int C = S.fac2_ok ? factor_cluster_size() : 0;
+	if (C) {
+		cudaLaunchConfig_t cfg = {};
+		cudaLaunchAttribute at[1];
+		at[0].id = cudaLaunchAttributeClusterDimension;
+		at[0].val.clusterDim.x = (unsigned)C; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
+		cfg.gridDim = dim3((unsigned)C); cfg.blockDim = dim3(FAC2_T); cfg.dynamicSmemBytes = FAC2_SMEM;
+		cfg.stream = s; cfg.attrs = at; cfg.numAttrs = 1;
+		FG_TRY(cudaLaunchKernelEx(&cfg, k_ilu0_factor_cluster, (const double *)t->A, (const int *)S.lo64.rows,
+		                          (const int *)S.lo64.lev_start, S.lo64.nlev, (const int4 *)S.fac2_hdr,
+		                          (const int *)S.fac2, t->ilu.LU, t->ilu.Dinv, &t->st->err));
+	} else {
+		k_ilu0_factor_cta<<<S.lo64.nchunk, FAC_THREADS, 0, s>>>(t->IA, t->A, S.lo64.rows, S.lo64.lev_start,
+		                                                       S.lo64.nlev, S.lo64.chunk_lev, S.fac_ptr,
+		                                                       S.fac_prog, t->ilu.LU, t->ilu.Dinv, &t->st->err);
+	}
 	fg_sweep *pr[4] = { &S.lo64, &S.up64, &S.lo32, &S.up32 };
 	for (int i = 0; i < 4; i++) {
 		int g = fg_grid(pr[i]->nval);
@@ -741,6 +990,6 @@ extern "C" void fg_ilu_free(femgpu_transport *t)
 		              all[i]->chunk_lev };
 		for (void *q : p) if (q) cudaFree(q);
 	}
-	void *v[] = { S.bl64, S.y64, S.bl32, S.y32, S.fac_ptr, S.fac_prog };
+	void *v[] = { S.bl64, S.y64, S.bl32, S.y32, S.fac_ptr, S.fac_prog, S.fac2_hdr, S.fac2 };
 	for (void *q : v) if (q) cudaFree(q);
 }

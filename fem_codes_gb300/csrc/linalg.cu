@@ -476,6 +476,32 @@ extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 	return (int)cudaGetLastError();
 }
 
+// st->rho = ||B - q|| for q = A X (the last cycle's state is left alone).
+__global__ void __launch_bounds__(RED_TPB) k_true_rho(const double *q, const double *B, int n, double *partials,
+                                                      fg_status *st)
+{
+	__shared__ double sh[32];
+	double part = 0.0;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		double r = -__dadd_rn(q[k], -B[k]);
+		part += r * r;
+	}
+	part = block_sum(part, sh);
+	double tot;
+	if (last_block_total(part, partials, &st->ticket, &tot, sh)) st->rho = sqrt(tot);
+}
+
+// True residual of the current iterate into st->rho; A X goes to V[kmax],
+// which holds no Arnoldi vector of a finished cycle.
+extern "C" int fg_kry_true_rho(const fg_krylov *k, const fg_linop *op, const double *B, double *X)
+{
+	int rc;
+	double *q = k->V + (size_t)k->kmax * k->ldv;
+	if ((rc = op->matvec(op->ctx, X, q, nullptr))) return rc;
+	k_true_rho<<<k->nblk, RED_TPB, 0, k->stream>>>(q, B, k->n, k->partials, k->st);
+	return (int)cudaGetLastError();
+}
+
 // ------------------------------------------- the transport context's view
 static int tr_matvec(void *c, const double *p, double *q, const int *a)
 {

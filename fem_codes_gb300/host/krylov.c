@@ -86,10 +86,18 @@ int fgh_kry_cycles(const fg_krylov *k, const fg_linop *op, const double *B, doub
 {
 	int l = 0, rc;
 	if ((rc = fgh_kry_begin(k, eps))) return rc;
-	do {
-		if ((rc = fgh_kry_cycle(k, op, B, X, kind))) return rc;
-		l++;
-	} while (k->st_host->rho > eps && l < lmax);
+	for (;;) {
+		do {
+			if ((rc = fgh_kry_cycle(k, op, B, X, kind))) return rc;
+			l++;
+		} while (k->st_host->rho > eps && l < lmax);
+		/* FGMRES stops on the unpreconditioned residual: confirm the
+		 * recurrence's estimate with ||B - A X|| before accepting it */
+		if (kind < 0 || k->st_host->rho > eps) break;
+		KR(fg_kry_true_rho(k, op, B, X));
+		if ((rc = sync_status(k))) return rc;
+		if (k->st_host->rho <= eps || l >= lmax) break;
+	}
 	*iters += k->st_host->total;
 	if (k->st_host->rho > eps) {
 		fgh_set_error("GMRES: %d restarts, rho %.3e > eps %.3e", l, k->st_host->rho, eps);

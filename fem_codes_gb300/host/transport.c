@@ -539,7 +539,14 @@ static int learned_cycles(femgpu_transport *t, const double *B, double *X, doubl
 			continue;
 		}
 		if (rc) return rc;
-		if (k.st_host->rho <= eps) break;
+		if (k.st_host->rho <= eps) {
+			/* accept on the unpreconditioned residual ||B - A X||, not the estimate */
+			KR(fg_kry_true_rho(&k, &op, B, X));
+			CK(cudaMemcpyAsync(k.st_host, k.st, sizeof(fg_status), cudaMemcpyDeviceToHost, t->stream));
+			CK(cudaStreamSynchronize(t->stream));
+			if (k.st_host->rho <= eps) break;
+			continue;
+		}
 		if (!t->fell_back && !(k.st_host->rho <= t->o.stall_ratio * prev)) {
 			KR(fg_ilu0_factor(t));
 			t->fell_back = 1;
