@@ -409,8 +409,9 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 __global__ void __launch_bounds__(FAC2_T)
 k_ilu0_factor_cluster(const double *__restrict__ AA, const int *__restrict__ rows,
-                      const int *__restrict__ lev_start, int nlev, const int4 *__restrict__ hdr,
-                      const int *__restrict__ prog, double *LU, double *Dinv, int *err)
+                      const int *__restrict__ lev_start, int nlev, const int *__restrict__ chunk_lev,
+                      const int4 *__restrict__ hdr, const int *__restrict__ prog, double *LU, double *Dinv,
+                      int *err)
 {
 	extern __shared__ __align__(16) unsigned char fsm[];
 	// per-thread scratch, element i of thread t at [i * FAC2_T + t] (no bank conflicts)
@@ -420,18 +421,21 @@ k_ilu0_factor_cluster(const double *__restrict__ AA, const int *__restrict__ row
 #define SV(B, i) ((double *)(bufs + (B) * FAC2_BUF))[(i) * FAC2_T + threadIdx.x]
 #define SP(B, i) ((int *)(bufs + (B) * FAC2_BUF + FAC2_T * (FAC_CAP + 1) * 8))[(i) * FAC2_T + threadIdx.x]
 	const int C = (int)cluster_size(), rank = (int)cluster_rank(), tid = (int)threadIdx.x;
+	// block ILU(0): cluster k factorises matrix block k (its run of levels)
+	const int ck = (int)(blockIdx.x / (unsigned)C);
+	const int L0 = chunk_lev ? chunk_lev[ck] : 0, L1 = chunk_lev ? chunk_lev[ck + 1] : nlev;
 	// level bounds: [b, e) this level, e1 the next level's end, e2 the one after
-	int b = lev_start[0], e = nlev > 0 ? lev_start[1] : 0, e1 = nlev > 1 ? lev_start[2] : e;
+	int b = lev_start[L0], e = L1 > L0 ? lev_start[L0 + 1] : b, e1 = L1 > L0 + 1 ? lev_start[L0 + 2] : e;
 	int cur = 0, have = 0;                   // buffer of the prefetched first row; its validity
 	int4 ph = make_int4(0, 0, 0, 0);
 	int pr_ = 0;
-	for (int l = 0; l < nlev; l++) {
-		int e2 = (l + 3 <= nlev) ? lev_start[l + 3] : e1;
+	for (int l = L0; l < L1; l++) {
+		int e2 = (l + 3 <= L1) ? lev_start[l + 3] : e1;
 		int per = (e - b + C - 1) / C, p0 = b + rank * per, p1 = min(e, p0 + per);
 		// round 1 of the next level's first row, into registers
 		int nper = (e1 - e + C - 1) / C, np0 = e + rank * nper, np1 = min(e1, np0 + nper);
 		int np = np0 + tid;
-		bool nhave = (l + 1 < nlev) && np < np1;
+		bool nhave = (l + 1 < L1) && np < np1;
 		int4 nh = make_int4(0, 0, 0, 0);
 		int nr = 0;
 		if (nhave) { nh = hdr[np]; nr = rows[np]; }
@@ -752,10 +756,11 @@ static int build_factor_prog(const int *IA, const int *JA, int n, const HostLeve
 	return up_vec(&S.fac_prog, prog);
 }
 
-// The elimination program of k_ilu0_factor_cluster (no matrix blocks): per
-// level-order position a header and a row program whose operand addresses
-// come first.  fac2_ok = 0 when a row exceeds the kernel's per-row capacity.
-static int build_factor_prog2(const int *IA, const int *JA, int n, const HostLevels &Lo, fg_ilu_sweeps &S)
+// The elimination program of k_ilu0_factor_cluster: per level-order
+// position a header and a row program whose operand addresses come first
+// (couplings between matrix blocks dropped, as in build_factor_prog).  fac2_ok = 0 when a row exceeds the kernel's per-row capacity.
+static int build_factor_prog2(const int *IA, const int *JA, int n, const HostLevels &Lo, const Blocks &B,
+                              fg_ilu_sweeps &S)
 {
 	std::vector<int> hdr((size_t)n * 4), prog, ops, grp;
 	prog.reserve((size_t)n * 28);
@@ -767,13 +772,14 @@ static int build_factor_prog2(const int *IA, const int *JA, int n, const HostLev
 		grp.clear();
 		for (int q = 0; q < len && JA[rb + q] < r; q++) {
 			int jrow = JA[rb + q];
+			if (!B.same(r, jrow)) continue;              // coupling to another block: dropped
 			size_t g = grp.size();
 			grp.push_back(q);
 			grp.push_back(0);
 			ops.push_back(-1 - jrow);
 			for (int k = IA[jrow]; k < IA[jrow + 1]; k++) {
 				int col = JA[k], pos = -1;
-				if (col <= jrow) continue;
+				if (col <= jrow || !B.same(r, col)) continue;
 				for (int m = 0; m < len; m++) if (JA[rb + m] == col) { pos = m; break; }
 				if (pos < 0) continue;
 				grp.push_back(col == r ? -1 : pos);
@@ -800,18 +806,19 @@ static int build_factor_prog2(const int *IA, const int *JA, int n, const HostLev
 	return up_vec(&S.fac2, prog);
 }
 
-// Cluster size for the factorisation: 16 CTAs when the device can place such
-// a cluster, else 8 (0: no cluster launch; the single-block kernel runs).
-static int factor_cluster_size(void)
+// Cluster size for the factorisation of P matrix blocks (one cluster each):
+// the largest of 16, 8, 4, 2 CTAs with which P clusters fit on the device at
+// once; 0 when none does (the one-block-per-matrix-block kernel runs).
+static int factor_cluster_size(int P)
 {
-	static int C = -1;
-	if (C < 0) {
-		C = 0;
+	static int init = 0, fits[17];
+	if (!init) {
+		init = 1;
 		if (cudaFuncSetAttribute(k_ilu0_factor_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, FAC2_SMEM) !=
-		    cudaSuccess) { cudaGetLastError(); return C; }
+		    cudaSuccess) { cudaGetLastError(); return 0; }
 		cudaFuncSetAttribute(k_ilu0_factor_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 		cudaGetLastError();
-		for (int c = 16; c >= 8 && !C; c /= 2) {
+		for (int c = 16; c >= 2; c /= 2) {
 			cudaLaunchConfig_t cfg = {};
 			cudaLaunchAttribute at[1];
 			at[0].id = cudaLaunchAttributeClusterDimension;
@@ -819,11 +826,13 @@ static int factor_cluster_size(void)
 			cfg.gridDim = dim3((unsigned)c); cfg.blockDim = dim3(FAC2_T); cfg.dynamicSmemBytes = FAC2_SMEM;
 			cfg.attrs = at; cfg.numAttrs = 1;
 			int ncl = 0;
-			if (cudaOccupancyMaxActiveClusters(&ncl, k_ilu0_factor_cluster, &cfg) == cudaSuccess && ncl >= 1) C = c;
+			if (cudaOccupancyMaxActiveClusters(&ncl, k_ilu0_factor_cluster, &cfg) == cudaSuccess) fits[c] = ncl;
 			cudaGetLastError();
 		}
 	}
-	return C;
+	for (int c = 16; c >= 2; c /= 2)
+		if (fits[c] >= P) return c;
+	return 0;
 }
 
 #define SW_SET(T, U, CW, F) FG_TRY(cudaFuncSetAttribute(k_sweep<T, U, CW, F>, \
@@ -893,7 +902,7 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 	if ((rc = build_prog<float, false>(hIA, hJA, n, Lo, &Up, B, clo, S.lo32))) return rc;
 	if ((rc = build_factor_prog(hIA, hJA, n, Lo, B, S))) return rc;
 	S.fac2_ok = 0;
-	if (!B.P && (rc = build_factor_prog2(hIA, hJA, n, Lo, S))) return rc;
+	if ((rc = build_factor_prog2(hIA, hJA, n, Lo, B, S))) return rc;
 	size_t nb = (size_t)std::max(Lo.pstart[Lo.nlev], Up.pstart[Up.nlev]) + 64;
 	FG_TRY(cudaMalloc((void **)&S.bl64, sizeof(double) * nb));
 	FG_TRY(cudaMalloc((void **)&S.y64, sizeof(double) * nb));
@@ -915,17 +924,18 @@ extern "C" int fg_ilu0_factor(femgpu_transport *t)
 {
 	cudaStream_t s = t->stream;
 	fg_ilu_sweeps &S = t->sweeps;
-	int C = S.fac2_ok ? factor_cluster_size() : 0;
+	int P = S.lo64.nchunk, C = S.fac2_ok ? factor_cluster_size(P) : 0;
 	if (C) {
 		cudaLaunchConfig_t cfg = {};
 		cudaLaunchAttribute at[1];
 		at[0].id = cudaLaunchAttributeClusterDimension;
 		at[0].val.clusterDim.x = (unsigned)C; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
-		cfg.gridDim = dim3((unsigned)C); cfg.blockDim = dim3(FAC2_T); cfg.dynamicSmemBytes = FAC2_SMEM;
+		cfg.gridDim = dim3((unsigned)(C * P)); cfg.blockDim = dim3(FAC2_T); cfg.dynamicSmemBytes = FAC2_SMEM;
 		cfg.stream = s; cfg.attrs = at; cfg.numAttrs = 1;
 		FG_TRY(cudaLaunchKernelEx(&cfg, k_ilu0_factor_cluster, (const double *)t->A, (const int *)S.lo64.rows,
-		                          (const int *)S.lo64.lev_start, S.lo64.nlev, (const int4 *)S.fac2_hdr,
-		                          (const int *)S.fac2, t->ilu.LU, t->ilu.Dinv, &t->st->err));
+		                          (const int *)S.lo64.lev_start, S.lo64.nlev, (const int *)S.lo64.chunk_lev,
+		                          (const int4 *)S.fac2_hdr, (const int *)S.fac2, t->ilu.LU, t->ilu.Dinv,
+		                          &t->st->err));
 	} else {
 		k_ilu0_factor_cta<<<S.lo64.nchunk, FAC_THREADS, 0, s>>>(t->IA, t->A, S.lo64.rows, S.lo64.lev_start,
 		                                                       S.lo64.nlev, S.lo64.chunk_lev, S.fac_ptr,
