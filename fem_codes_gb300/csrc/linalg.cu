@@ -15,6 +15,7 @@
 #include "fg_gnn.h"
 #include "fg_amg.h"
 #include <math.h>
+#include <stdlib.h>
 
 // ============================================================= matvecs ====
 // csrmv.c:15-20: Q[i] = sum_j AA[j] P[JA[j]] in column order.
@@ -318,6 +319,91 @@ __global__ void __launch_bounds__(RED_TPB) k_mgs(const double *V, size_t ldv, in
 		H[j * ldh + i] = (j <= i) ? tot : sqrt(tot);
 }
 
+// Classical Gram-Schmidt for FGMRES (the flexible solver's own
+// orthogonalisation; the left-preconditioned pgmres keeps the reference's
+// MGS above).  One projection = a fused multi-dot h = V^T w over the m basis
+// vectors (partial sums per block, then a fixed-order finish: deterministic)
+// and one update w -= V h, which can also form ||w||^2.
+#define MD_J 8                        // basis vectors per multi-dot block row
+
+__global__ void __launch_bounds__(RED_TPB) k_mdot(const double *V, size_t ldv, int n, int m, const double *w,
+                                                  double *partials, fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	__shared__ double sh[MD_J][RED_TPB / 32];
+	const int j0 = blockIdx.y * MD_J, G = gridDim.x;
+	double acc[MD_J];
+#pragma unroll
+	for (int q = 0; q < MD_J; q++) acc[q] = 0.0;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += G * blockDim.x) {
+		double wk = w[k];
+#pragma unroll
+		for (int q = 0; q < MD_J; q++)
+			if (j0 + q < m) acc[q] += V[(size_t)(j0 + q) * ldv + k] * wk;
+	}
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+	for (int q = 0; q < MD_J; q++) {
+		double v = fg_warp_sum(acc[q]);
+		if (lane == 0) sh[q][wid] = v;
+	}
+	__syncthreads();
+	if (threadIdx.x < MD_J && j0 + (int)threadIdx.x < m) {
+		double t = 0.0;
+		for (int q = 0; q < RED_TPB / 32; q++) t += sh[threadIdx.x][q];
+		partials[(size_t)(j0 + threadIdx.x) * G + blockIdx.x] = t;
+	}
+}
+
+// h[j] = sum over blocks of partials[j][.]; H(j, i) = h[j] (accumulate: +=).
+__global__ void k_mdot_fin(const double *partials, int G, int m, double *h, double *Hcol, int ldh, int accumulate,
+                           fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	const int j = blockIdx.x;
+	double t = 0.0;
+	for (int b = threadIdx.x; b < G; b += 32) t += partials[(size_t)j * G + b];
+	t = fg_warp_sum(t);
+	if (threadIdx.x == 0) {
+		h[j] = t;
+		Hcol[(size_t)j * ldh] = accumulate ? Hcol[(size_t)j * ldh] + t : t;
+	}
+}
+
+// w -= sum_j h[j] v_j; norm != 0: Hn = ||w|| (last block).
+__global__ void __launch_bounds__(RED_TPB) k_cgs_update(const double *V, size_t ldv, int n, int m, double *w,
+                                                        const double *h, int norm, double *Hn, double *partials,
+                                                        fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	__shared__ double sh[32];
+	double part = 0.0;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		double x = w[k];
+		for (int j = 0; j < m; j++) x -= h[j] * V[(size_t)j * ldv + k];
+		w[k] = x;
+		part += x * x;
+	}
+	if (!norm) return;
+	part = block_sum(part, sh);
+	double tot;
+	if (last_block_total(part, partials, &st->ticket, &tot, sh)) *Hn = sqrt(tot);
+}
+
+// Orthogonalisation of Arnoldi step i: 0 MGS (one fused kernel per basis
+// vector), 1 CGS, 2 CGS with one re-orthogonalisation (FEMGPU_GS selects;
+// default 1).
+static int gs_mode(void)
+{
+	static int g = -1;
+	if (g < 0) {
+		const char *e = getenv("FEMGPU_GS");
+		int v = e ? atoi(e) : 1;
+		g = (v >= 0 && v <= 2) ? v : 1;
+	}
+	return g;
+}
+
 // u = u * (1/h), dscal of pgmres.c:85 / :121.
 __global__ void k_scale(double *u, int n, const double *h, fg_status *st)
 {
@@ -465,8 +551,21 @@ extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 			}
 			if ((rc = op->matvec(op->ctx, z, w, active))) return rc;
 		}
-		for (int j = 0; j <= i + 1; j++)
-			k_mgs<<<G, RED_TPB, 0, s>>>(V, ldv, n, i, j, k->H, ldh, k->partials, k->st);
+		const int gs = gs_mode();
+		if (gs == 0) {
+			for (int j = 0; j <= i + 1; j++)
+				k_mgs<<<G, RED_TPB, 0, s>>>(V, ldv, n, i, j, k->H, ldh, k->partials, k->st);
+		} else {
+			const int m = i + 1;
+			double *h = k->partials + (size_t)G * (kmax + 1);
+			for (int pass = 0; pass < gs; pass++) {
+				const int last = pass == gs - 1;
+				k_mdot<<<dim3(G, (m + MD_J - 1) / MD_J), RED_TPB, 0, s>>>(V, ldv, n, m, w, k->partials, k->st);
+				k_mdot_fin<<<m, 32, 0, s>>>(k->partials, G, m, h, k->H + i, ldh, pass, k->st);
+				k_cgs_update<<<G, RED_TPB, 0, s>>>(V, ldv, n, m, w, h, last, k->H + (i + 1) * ldh + i,
+				                                   k->partials, k->st);
+			}
+		}
 		k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(w, n, k->H + (i + 1) * ldh + i, k->st);
 		k_givens<<<1, 1, 0, s>>>(k->H, ldh, k->cs, k->sn, k->ge, i, kmax, k->st);
 	}

@@ -34,7 +34,7 @@ int fgh_kry_alloc(fg_krylov *k, int n, int kmax, int zmode, void *stream)
 	DM(k->gy, sizeof(double) * m1);
 	if (zmode == 1) DM(k->Z, sizeof(double) * k->ldv * (size_t)kmax);
 	if (zmode == 2) DM(k->Z32, sizeof(float) * k->ldv * (size_t)kmax);
-	DM(k->partials, sizeof(double) * (size_t)k->nblk);
+	DM(k->partials, sizeof(double) * ((size_t)k->nblk * (m1 + 1) + m1 + 1));
 	DM(k->st, sizeof(fg_status));
 	CK(cudaMemsetAsync(k->V, 0, sizeof(double) * k->ldv * m1, k->stream));
 	CK(cudaMemsetAsync(k->st, 0, sizeof(fg_status), k->stream));

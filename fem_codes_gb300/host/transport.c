@@ -255,7 +255,9 @@ int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts 
 		else DM(t->Z32, sizeof(float) * t->ldv * (size_t)t->kmax);
 	}
 	t->nblk_red = 2 * 152;
-	DM(t->partials, sizeof(double) * (size_t)t->nblk_red);
+	/* reduction partials: one row per basis vector for the CGS multi-dot,
+	 * then the projection coefficients */
+	DM(t->partials, sizeof(double) * ((size_t)t->nblk_red * ((size_t)t->kmax + 2) + (size_t)t->kmax + 2));
 	for (i = 0; i < 4; i++) CK(cudaEventCreate(&t->ev[i]));
 	CK(cudaDeviceSynchronize());
 	rc = sync_err(t);
