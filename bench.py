@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--workload", default="transport", choices=["transport", "euler"])
     ap.add_argument("--euler-nx", type=int, default=1024)
     ap.add_argument("--euler-ny", type=int, default=256)
+    ap.add_argument("--euler-precision", default="MIXED_IR", choices=["FP64", "MIXED_IR"],
+                    help="MIXED_IR: FP32 element matrices and preconditioner inside FGMRES, FP64 residuals")
+    ap.add_argument("--euler-solver", default="GMRES", choices=["GMRES", "FGMRES"])
     ap.add_argument("--no-learned", action="store_true")
     return ap.parse_args()
 
@@ -460,11 +463,18 @@ def euler_setup(nx, ny):
 def euler_config(a):
     return {"workload": f"2D Euler REFLETIDO (oblique shock reflection, Mach 2.9 inflow, gamma 1.4) on a 4x1 "
                         f"domain, {a.euler_nx}x{a.euler_ny} cells ({2 * a.euler_nx * a.euler_ny} triangles), "
-                        "SUPG+CAU, Predictor_Old alpha 0.5, 2 correctors, dt from CFL 5, EBE 12x12 FP64, "
-                        "BlockDiag-preconditioned GMRES(50) to 1e-8",
-            "nx": a.euler_nx, "ny": a.euler_ny, "kmax": 50,
+                        "SUPG+CAU, Predictor_Old alpha 0.5, 2 correctors, dt from CFL 5, "
+                        + ("EBE 12x12 FP64, BlockDiag-preconditioned " + euler_solver(a) if a.euler_precision == "FP64"
+                           else "EBE 12x12 FP32 element matrices and FP32 BlockDiag inside FGMRES, FP64 Arnoldi and "
+                                "residuals,") + "(50) to 1e-8",
+            "nx": a.euler_nx, "ny": a.euler_ny, "kmax": 50, "precision": a.euler_precision,
+            "solver": euler_solver(a),
             "step": "one time step: predictor + 2 x (build + block-diagonal setup + GMRES + update)",
             "l2": "inputs larger than L2 (element matrices 603 MB)"}
+
+
+def euler_solver(a):
+    return "FGMRES" if a.euler_precision != "FP64" else a.euler_solver
 
 
 def euler_cpu(steps=1, nx=256, ny=64):
@@ -508,7 +518,8 @@ def run_euler(a):
                "sample": f"1 time step on the 256x64 mesh ({nel} triangles, GMRES iters {its.reshape(-1).tolist()}),"
                          f" scaled by the element count to {full} triangles"}
     m, pb, dt = euler_setup(a.euler_nx, a.euler_ny)
-    E = fg.Euler.from_problem(m, pb, alpha=0.5, dt=dt, stab_tol=1e-6, kmax=50, lmax=100, tol=1e-8, ncorr=2)
+    E = fg.Euler.from_problem(m, pb, alpha=0.5, dt=dt, stab_tol=1e-6, kmax=50, lmax=100, tol=1e-8, ncorr=2,
+                              solver=euler_solver(a), precision=a.euler_precision)
     s = torch.cuda.Stream()
     E.set_stream(s.cuda_stream)
     n1 = pb.neq + 1
@@ -537,24 +548,63 @@ def run_euler(a):
         if rc:
             raise fg.FemGpuError(rc, "e2e step")
     e2e_ms = 1e3 * (time.perf_counter() - t0) / a.steps
+    err = None
+    if a.euler_precision != "FP64":
+        # u_h holds the state after the warm-up and the end-to-end steps (each
+        # of which restarts from u_h with a = 0): the same calls in FP64 FGMRES
+        # at this tolerance and at 1e-11, and the relative max-norm differences
+        def fp64_run(tol):
+            E64 = fg.Euler.from_problem(m, pb, alpha=0.5, dt=dt, stab_tol=1e-6, kmax=50, lmax=400, tol=tol, ncorr=2,
+                                        solver="FGMRES", precision="FP64")
+            E64.set_stream(s.cuda_stream)
+            u64 = torch.from_numpy(pb.u0.copy()).pin_memory()
+            for nst in [a.warmup] + [1] * a.steps:
+                rc = L.femgpu_euler_predictor(E64.handle, ctypes.c_void_p(u64.data_ptr()), nst, None, None)
+                if rc:
+                    raise fg.FemGpuError(rc, "FP64 comparison run")
+            torch.cuda.synchronize()
+            E64.close()
+            return u64[:pb.neq].clone()
+
+        def rel(x, y):
+            return (x - y).abs().max().item() / max(y.abs().max().item(), 1e-300)
+
+        u8, u11 = fp64_run(1e-8), fp64_run(1e-11)
+        um = u_h[:pb.neq]
+        err = {"mixed_vs_fp64": rel(um, u8), "mixed_vs_fp64_tight": rel(um, u11), "fp64_vs_fp64_tight": rel(u8, u11)}
     peak, peak_kind = peaks()
-    kt = euler_kernel_times(E, s, pb.neq, m.nel)
-    mv_bytes = m.nel * (144 * 8 + 48) + 2 * pb.neq * 8
-    mv_gbs = mv_bytes / (kt["ebemv"] * 1e-3) / 1e9
+    mixed = a.euler_precision != "FP64"
+    kt = euler_kernel_times(E, s, pb.neq, m.nel, mixed=mixed)
+    if mixed:   # the solve's operator: FP32 element matrices, FP32 vector in, FP64 out
+        mv_bytes = m.nel * (144 * 4 + 48) + pb.neq * (4 + 8)
+        mv_gbs = mv_bytes / (kt["ebemv32"] * 1e-3) / 1e9
+        mv_name, mv_note, mv_traffic = ("k_ebemv_blk32<4> (12x12 FP32 EBE matvec, row gather)",
+                                        "FP32 fused multiply-adds, FP64 row totals", None)
+    else:
+        mv_bytes = m.nel * (144 * 8 + 48) + 2 * pb.neq * 8
+        mv_gbs = mv_bytes / (kt["ebemv"] * 1e-3) / 1e9
+        mv_name, mv_note, mv_traffic = ("k_ebemv_blk<4> (12x12 FP64 EBE matvec, row gather)",
+                                        "FP64 issue-bound on GB300 (288 FP64 ops per element, no FMA contraction)",
+                                        read_traffic("euler_ebemv"))
     build_gbs = m.nel * (144 * 8 + 12 * 8 + 12) / (kt["build"] * 1e-3) / 1e9
     line = {"metric": EULER_METRIC, "value": ms, "unit": "ms", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
-            "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if a.euler_precision == "FP64" else "f64/f32 mixed",
             "data": "synthetic", "config": euler_config(a),
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": n1 * 8, "d2h_bytes_per_step": n1 * 8},
-            "roofline": {"kernel": "k_ebemv_blk<4> (12x12 FP64 EBE matvec, row gather)", "bound": "hbm",
+            "roofline": {"kernel": mv_name, "bound": "hbm",
                          "achieved": mv_gbs, "peak": peak, "unit": "GB/s", "frac": mv_gbs / peak,
-                         "traffic": read_traffic("euler_ebemv"),
-                         "note": "FP64 issue-bound on GB300 (288 FP64 ops per element, no FMA contraction)"},
+                         "traffic": mv_traffic, "note": mv_note},
+            "kernel_ms": {k: round(v, 4) for k, v in kt.items()},
             "build": {"kernel": "k_euler_element", "ms": kt["build"],
                       "elements_per_s": m.nel / (kt["build"] * 1e-3), "GB/s": build_gbs},
             "phase_ms_per_step": {k: round(1e3 * v / a.steps, 3) for k, v in
                                   zip(["build", "precond_setup", "solve"], phase)},
             "gmres_iters": its.reshape(-1).tolist(), "neq": pb.neq, "nel": m.nel, "dt": dt}
+    if err is not None:
+        err["what"] = (f"max |u - u_ref| / max |u_ref| after {a.warmup + a.steps} time steps; fp64: FP64 FGMRES at "
+                       "1e-8 (agrees with the oracle to 1e-8 on the tested meshes), fp64_tight: FP64 FGMRES at 1e-11")
+        line["err_vs_fp64"] = err
     if cpu:
         line["cpu_baseline"] = cpu
     if clocks:
@@ -564,7 +614,7 @@ def run_euler(a):
         print(json.dumps(line), flush=True)
 
 
-def euler_kernel_times(E, s, neq, nel, reps=10):
+def euler_kernel_times(E, s, neq, nel, reps=10, mixed=False):
     import torch
     L = E._L
     vp = ctypes.c_void_p
@@ -593,8 +643,14 @@ def euler_kernel_times(E, s, neq, nel, reps=10):
 
     torch.cuda.synchronize()
     s.wait_stream(torch.cuda.current_stream())
-    return {"ebemv": timeit(lambda: L.femgpu_ebe_matvec_dev(ebe, vp(x.data_ptr()), vp(y.data_ptr()))),
-            "build": timeit(lambda: L.femgpu_euler_build_dev(E.handle))}
+    out = {"ebemv": timeit(lambda: L.femgpu_ebe_matvec_dev(ebe, vp(x.data_ptr()), vp(y.data_ptr())))}
+    if mixed:
+        L.femgpu_ebe_matvec32_dev.argtypes = [vp, vp, vp]
+        L.femgpu_ebe_matvec32_dev.restype = ctypes.c_int
+        x32 = x.float()
+        out["ebemv32"] = timeit(lambda: L.femgpu_ebe_matvec32_dev(ebe, vp(x32.data_ptr()), vp(y.data_ptr())))
+    out["build"] = timeit(lambda: L.femgpu_euler_build_dev(E.handle))
+    return out
 
 
 def main():

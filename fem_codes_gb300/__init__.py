@@ -63,7 +63,8 @@ class EulerOpts(ctypes.Structure):
     _fields_ = [("gamma", ctypes.c_double), ("mach", ctypes.c_double), ("dimensionless", ctypes.c_int),
                 ("alpha", ctypes.c_double), ("dt", ctypes.c_double), ("stab_tol", ctypes.c_double),
                 ("precond", ctypes.c_int), ("solver", ctypes.c_int), ("kmax", ctypes.c_int),
-                ("lmax", ctypes.c_int), ("tol", ctypes.c_double), ("ncorr", ctypes.c_int)]
+                ("lmax", ctypes.c_int), ("tol", ctypes.c_double), ("ncorr", ctypes.c_int),
+                ("precision", ctypes.c_int)]
 
 
 class NSOpts(ctypes.Structure):
@@ -534,7 +535,7 @@ class Euler:
 
     def __init__(self, x, y, vert, node_id, neq, upresc, gamma=1.4, mach=1.0, dimensionless=False,
                  alpha=0.5, dt=1e-3, stab_tol=1e-6, precond="BlockDiag", solver="GMRES", kmax=30,
-                 lmax=100, tol=1e-8, ncorr=2):
+                 lmax=100, tol=1e-8, ncorr=2, precision="FP64"):
         L = load()
         o = EulerOpts()
         L.femgpu_euler_default_opts(ctypes.byref(o))
@@ -543,6 +544,7 @@ class Euler:
         o.precond = OPTS["precond"][precond.upper()]
         o.solver = OPTS["solver"][solver.upper()]
         o.kmax, o.lmax, o.tol, o.ncorr = int(kmax), int(lmax), float(tol), int(ncorr)
+        o.precision = OPTS["precision"][precision.upper()]
         self.opts = o
         self._keep = [_f64(x), _f64(y), _i32(np.asarray(vert).reshape(-1)),
                       _i32(np.asarray(node_id).reshape(-1)), _f64(np.asarray(upresc).reshape(-1))]

@@ -8,7 +8,8 @@
 // Every product is a per-row (or per-node) gather over the incident elements
 // in ascending element order, so the additions happen in the reference's
 // order; this file is compiled without FMA contraction, so results are
-// bit-identical to the reference.
+// bit-identical to the reference.  The FP32 variants at the end serve the
+// mixed-precision flexible solves only (explicit fused multiply-adds).
 #include "fg_common.cuh"
 #include "fg_ebe.h"
 
@@ -51,6 +52,36 @@ __global__ void k_ebemv_blk(int neq, const int *__restrict__ ri_ptr, const int *
 					first = false;
 				}
 				q = q + s;
+			}
+		}
+		Q[I] = q;
+	}
+}
+
+// Mixed precision (not a reference operation): FP32 element matrices and
+// vector, each element row accumulated by FP32 fused multiply-adds, the row's
+// incident element rows summed in FP64.
+template <int NDOF>
+__global__ void k_ebemv_blk32(int neq, const int *__restrict__ ri_ptr, const int *__restrict__ ri,
+                              const int *__restrict__ lm, const float *__restrict__ A,
+                              const float *__restrict__ P, double *__restrict__ Q)
+{
+	constexpr int M = 3 * NDOF;
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I <= neq; I += gridDim.x * blockDim.x) {
+		double q = 0.0;
+		if (I < neq) {
+			for (int t = ri_ptr[I]; t < ri_ptr[I + 1]; t++) {
+				int code = __ldg(&ri[t]), e = code / M, a = code - e * M;
+				const int *l = lm + (long long)e * M;
+				const float *row = A + (long long)e * M * M + a * M;
+				float s = 0.0f;
+				#pragma unroll
+				for (int b = 0; b < M; b++) {
+					int j = __ldg(&l[b]);
+					float p = (j == neq) ? 0.0f : __ldg(&P[j]);
+					s = fmaf(__ldg(&row[b]), p, s);
+				}
+				q += (double)s;
 			}
 		}
 		Q[I] = q;
@@ -176,6 +207,35 @@ __global__ void k_blockdiag_apply(int nnodes, int neq, const int *node_id, const
 }
 
 __global__ void k_zero_one(double *z, int i) { z[i] = 0.0; }
+__global__ void k_zero_one32(float *z, int i) { z[i] = 0.0f; }
+
+// z = D^-1 p per node (BlockDiag_precond's arithmetic), stored in FP32.
+template <int NDOF>
+__global__ void k_blockdiag_apply32(int nnodes, int neq, const int *node_id, const double *B, const double *p,
+                                    float *z)
+{
+	constexpr int D2 = NDOF * NDOF;
+	for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nnodes; n += gridDim.x * blockDim.x) {
+		int id[NDOF];
+		double v[NDOF];
+		#pragma unroll
+		for (int c = 0; c < NDOF; c++) { id[c] = blk_id(node_id, NDOF, neq, n, c); v[c] = p[id[c]]; }
+		const double *Bn = B + (long long)n * D2;
+		#pragma unroll
+		for (int r = 0; r < NDOF; r++) {
+			double s = Bn[NDOF * r] * v[0];
+			#pragma unroll
+			for (int c = 1; c < NDOF; c++) s = s + Bn[NDOF * r + c] * v[c];
+			if (id[r] != neq) z[id[r]] = (float)s;
+		}
+	}
+}
+
+__global__ void k_to_f32_blk(const double *__restrict__ a, float *__restrict__ b, long long n)
+{
+	for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+		b[i] = (float)a[i];
+}
 
 // ------------------------------------------------------------- launchers
 extern "C" int fg_ebe_lm(femgpu_ebe *c)
@@ -225,5 +285,31 @@ extern "C" int fg_ebe_blockdiag_apply(femgpu_ebe *c, const double *p, double *z,
 		k_blockdiag_apply<3, 0><<<g, FG_TPB, 0, c->stream>>>(c->nnodes, c->neq, c->node_id, B, p, z);
 	}
 	k_zero_one<<<1, 1, 0, c->stream>>>(z, c->neq);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_ebe_to_f32(femgpu_ebe *c)
+{
+	long long n = (long long)c->nel * c->m * c->m;
+	if (!c->A32) FG_TRY(cudaMalloc((void **)&c->A32, sizeof(float) * (size_t)n));
+	k_to_f32_blk<<<fg_grid(n), FG_TPB, 0, c->stream>>>(c->A, c->A32, n);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_ebe_matvec32(femgpu_ebe *c, const float *P, double *Q)
+{
+	int g = fg_grid(c->neq + 1LL, 128, 32);
+	if (!c->A32) return FEMGPU_E_NOT_BUILT;
+	if (c->ndof == 4) k_ebemv_blk32<4><<<g, 128, 0, c->stream>>>(c->neq, c->ri_ptr, c->ri, c->lm, c->A32, P, Q);
+	else k_ebemv_blk32<3><<<g, 128, 0, c->stream>>>(c->neq, c->ri_ptr, c->ri, c->lm, c->A32, P, Q);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_ebe_blockdiag_apply32(femgpu_ebe *c, const double *p, float *z)
+{
+	int g = fg_grid(c->nnodes);
+	if (c->ndof == 4) k_blockdiag_apply32<4><<<g, FG_TPB, 0, c->stream>>>(c->nnodes, c->neq, c->node_id, c->invBD, p, z);
+	else k_blockdiag_apply32<3><<<g, FG_TPB, 0, c->stream>>>(c->nnodes, c->neq, c->node_id, c->invBD, p, z);
+	k_zero_one32<<<1, 1, 0, c->stream>>>(z, c->neq);
 	return (int)cudaGetLastError();
 }

@@ -19,6 +19,7 @@ struct femgpu_ebe {
 	int *vert, *node_id, *lm;
 	int *ri_ptr, *ri, *ni_ptr, *ni;
 	double *A, *BD, *invBD;
+	float *A32;             /* FP32 copy of A (mixed-precision solves)  */
 	double *P, *Q;          /* scratch for the host-buffer entry points */
 	int have_bd;
 };
@@ -27,6 +28,11 @@ int fg_ebe_lm(femgpu_ebe *c);
 int fg_ebe_matvec(femgpu_ebe *c, const double *P, double *Q, int offdiag);
 int fg_ebe_blockdiag_setup(femgpu_ebe *c);
 int fg_ebe_blockdiag_apply(femgpu_ebe *c, const double *p, double *z, int mode);
+/* Mixed precision: A32 = (float) A; Q = A32 P with FP32 element rows and
+ * FP64 row totals; z = D^-1 p in FP64 arithmetic, stored in FP32. */
+int fg_ebe_to_f32(femgpu_ebe *c);
+int fg_ebe_matvec32(femgpu_ebe *c, const float *P, double *Q);
+int fg_ebe_blockdiag_apply32(femgpu_ebe *c, const double *p, float *z);
 
 #ifdef __cplusplus
 }

@@ -57,7 +57,7 @@ void femgpu_ebe_destroy(femgpu_ebe *c)
 	cudaStreamSynchronize(c->stream);
 	{
 		void *p[] = { c->vert, c->node_id, c->lm, c->ri_ptr, c->ri, c->ni_ptr, c->ni, c->A, c->BD,
-		              c->invBD, c->P, c->Q };
+		              c->invBD, c->P, c->Q, c->A32 };
 		for (i = 0; i < (int)(sizeof p / sizeof p[0]); i++) if (p[i]) cudaFree(p[i]);
 	}
 	if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -88,6 +88,14 @@ int femgpu_ebe_matvec_dev(femgpu_ebe *c, const double *P, double *Q)
 {
 	if (!c || !P || !Q) return FEMGPU_E_ARG;
 	KR(fg_ebe_matvec(c, P, Q, 0));
+	return 0;
+}
+
+int femgpu_ebe_matvec32_dev(femgpu_ebe *c, const float *P, double *Q)
+{
+	if (!c || !P || !Q) return FEMGPU_E_ARG;
+	if (!c->A32) { fgh_set_error("no FP32 element matrices"); return FEMGPU_E_NOT_BUILT; }
+	KR(fg_ebe_matvec32(c, P, Q));
 	return 0;
 }
 

@@ -47,12 +47,30 @@ static int op_precond(void *ctx, const double *p, double *z, const int *active)
 	return fg_ebe_blockdiag_apply(((femgpu_euler *)ctx)->ebe, p, z, 0);
 }
 
+/* mixed precision: z = D^-1 p in FP32, q = A32 z */
+static int op_precond32(void *ctx, const double *p, float *z, const int *active)
+{
+	femgpu_euler *c = (femgpu_euler *)ctx;
+	(void)active;
+	if (c->o.precond == FEMGPU_PREC_BLOCKDIAG) return fg_ebe_blockdiag_apply32(c->ebe, p, z);
+	return fg_to_f32(p, z, (long long)c->neq + 1, c->stream);
+}
+
+static int op_matvec_xf(void *ctx, const float *p, double *q, const int *active, int op32)
+{
+	(void)active;
+	if (!op32) return FEMGPU_E_ARG;                   /* only the FP32 operator is provided */
+	return fg_ebe_matvec32(((femgpu_euler *)ctx)->ebe, p, q);
+}
+
 static void linop(femgpu_euler *c, fg_linop *op)
 {
 	memset(op, 0, sizeof *op);
 	op->ctx = c;
 	op->matvec = op_matvec;
 	op->precond = c->o.precond == FEMGPU_PREC_BLOCKDIAG ? op_precond : NULL;
+	op->precond32 = op_precond32;
+	op->matvec_xf = op_matvec_xf;
 }
 
 static int uploadd(double **dst, const double *src, size_t n)
@@ -88,7 +106,8 @@ static int create(femgpu_euler *c, const femgpu_euler_opts *o, int nnodes, const
 	CK(cudaMemsetAsync(c->a, 0, sizeof(double) * n1, c->stream));
 	CK(cudaMemsetAsync(c->R, 0, sizeof(double) * n1, c->stream));
 	CK(cudaMemsetAsync(c->Da, 0, sizeof(double) * n1, c->stream));
-	rc = fgh_kry_alloc(&c->kry, neq, o->kmax, o->solver == FEMGPU_FGMRES ? 1 : 0, c->stream);
+	rc = fgh_kry_alloc(&c->kry, neq, o->kmax,
+	                   o->solver != FEMGPU_FGMRES ? 0 : o->precision == FEMGPU_MIXED_IR ? 2 : 1, c->stream);
 	if (rc) return rc;
 	for (i = 0; i < 4; i++) CK(cudaEventCreate(&c->ev[i]));
 	CK(cudaStreamSynchronize(c->stream));
@@ -108,7 +127,9 @@ int femgpu_euler_create(femgpu_euler **out, const femgpu_euler_opts *opts, int n
 	if (nnodes <= 0 || nel <= 0 || neq <= 0 || !x || !y || !vert || !node_id || !upresc ||
 	    o.kmax < 1 || o.lmax < 1 || o.ncorr < 1 || !(o.dt > 0.0) || !(o.tol > 0.0) ||
 	    (o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_BLOCKDIAG) ||
-	    (o.solver != FEMGPU_PGMRES && o.solver != FEMGPU_FGMRES)) {
+	    (o.solver != FEMGPU_PGMRES && o.solver != FEMGPU_FGMRES) ||
+	    (o.precision != FEMGPU_FP64 && o.precision != FEMGPU_MIXED_IR) ||
+	    (o.precision == FEMGPU_MIXED_IR && o.solver != FEMGPU_FGMRES)) {
 		fgh_set_error("femgpu_euler_create: bad argument or option");
 		return FEMGPU_E_ARG;
 	}
@@ -186,6 +207,7 @@ int femgpu_euler_precond_setup_dev(femgpu_euler *c)
 {
 	if (!c) return FEMGPU_E_ARG;
 	if (!c->built) { fgh_set_error("precond_setup before build"); return FEMGPU_E_NOT_BUILT; }
+	if (c->o.precision == FEMGPU_MIXED_IR) KR(fg_ebe_to_f32(c->ebe));
 	if (c->o.precond != FEMGPU_PREC_BLOCKDIAG) return 0;     /* NO_precond_setup */
 	KR(fg_ebe_blockdiag_setup(c->ebe));
 	c->ebe->have_bd = 1;
@@ -220,8 +242,9 @@ static int solve(femgpu_euler *c, const double *B, double *X, int *iters)
 	if (rc) return rc;
 	if (!(normb2 > 0.0)) return normb2 == 0.0 ? 0 : FEMGPU_E_BREAKDOWN;
 	linop(c, &op);
-	rc = fgh_kry_cycles(&c->kry, &op, B, X, c->o.solver == FEMGPU_PGMRES ? -1 : 0, c->o.tol * sqrt(normb2),
-	                    c->o.lmax, &it);
+	rc = fgh_kry_cycles(&c->kry, &op, B, X,
+	                    c->o.solver == FEMGPU_PGMRES ? -1 : c->o.precision == FEMGPU_MIXED_IR ? 2 : 0,
+	                    c->o.tol * sqrt(normb2), c->o.lmax, &it);
 	if (iters) *iters = it;
 	return rc;
 }

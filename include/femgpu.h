@@ -200,6 +200,10 @@ double *femgpu_ebe_A_dev(femgpu_ebe *ctx);
  * Q = A P; P[neq] read as 0, Q[neq] = 0. */
 int femgpu_ebe_matvec(femgpu_ebe *ctx, const double *P_host, double *Q_host);
 int femgpu_ebe_matvec_dev(femgpu_ebe *ctx, const double *P, double *Q);
+/* Mixed precision (no reference counterpart): Q = A P with the FP32 copy of
+ * the element matrices (made by a FEMGPU_MIXED_IR precond_setup) and an FP32
+ * P; FP32 element rows, FP64 row totals.  FEMGPU_E_NOT_BUILT without the copy. */
+int femgpu_ebe_matvec32_dev(femgpu_ebe *ctx, const float *P, double *Q);
 /* ebe2mvNDOF4 (EBE/ebe2mvNDOF4.c:4-79, ndof 4): off-diagonal node blocks of
  * every element, then with_inverse ? Q = P + D^-1 Q (BlockDiag2_precond.c)
  * : Q += D P (NOBlockDiag2_precond.c).  Needs femgpu_ebe_blockdiag_setup. */
@@ -231,6 +235,11 @@ typedef struct femgpu_euler_opts {
 	int kmax, lmax;      /* KrylovBasisVectorsQuantity, SolverMaxIter        */
 	double tol;          /* SolverTolerance                                  */
 	int ncorr;           /* NonLinearMaxIter correctors per step (ITERATION) */
+	int precision;       /* FEMGPU_FP64 (the reference's), or FEMGPU_MIXED_IR */
+	                     /* with FGMRES: FP32 element matrices and           */
+	                     /* preconditioner inside the Arnoldi cycles, every  */
+	                     /* restart from the FP64 residual, a solve accepted */
+	                     /* on the FP64 residual                             */
 } femgpu_euler_opts;
 
 void femgpu_euler_default_opts(femgpu_euler_opts *o);

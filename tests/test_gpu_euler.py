@@ -130,6 +130,41 @@ def test_euler_fgmres_matches_pgmres(gpu_lib):
     assert _rel(ub, ua) < 1e-7
 
 
+MIXED_RTOL = 1e-6   # mixed vs FP64 precision, same solver and criterion (relative, max norm)
+RULE_RTOL = 5e-5    # true-residual (FGMRES) vs the reference's preconditioned-residual stop, both at 1e-8
+
+
+def test_euler_mixed_precision_vs_fp64_and_oracle(gpu_lib):
+    """FP32 element matrices and block-diagonal preconditioner inside FGMRES,
+    each restart from the FP64 residual and each solve accepted on the FP64
+    residual (1e-8): the predictor states stay within MIXED_RTOL of the FP64
+    FGMRES run, and both within RULE_RTOL of the FP64 oracle (the reference's
+    left-preconditioned GMRES, whose 1e-8 applies to ||D^-1 r||)."""
+    import fem_codes_gb300 as fg
+    m = structured_mesh(64, 16, lx=4.0, ly=1.0)
+    pb = refletido_problem(m)
+    dt = euler_cfl_dt(m, 5.0)
+    uo, _ = pyoracle.euler_predictor(m.x, m.y, m.vert, pb.node_id, pb.neq, pb.upresc, pb.u0, 3, 2, dt=dt,
+                                     kmax=30, lmax=100, tol=1e-8)
+    kw = dict(dt=dt, kmax=30, lmax=100, tol=1e-8, ncorr=2, solver="FGMRES")
+    with fg.Euler.from_problem(m, pb, precision="MIXED_IR", **kw) as eu:
+        um, its = eu.Predictor(pb.u0, 3)
+    with fg.Euler.from_problem(m, pb, precision="FP64", **kw) as eu:
+        u64, _ = eu.Predictor(pb.u0, 3)
+    assert _rel(um, u64) < MIXED_RTOL
+    assert _rel(u64, uo) < RULE_RTOL
+    assert _rel(um, uo) < RULE_RTOL
+    assert (its > 0).all()
+
+
+def test_euler_mixed_precision_needs_fgmres(gpu_lib):
+    import fem_codes_gb300 as fg
+    g = _load(CASES[0])
+    with pytest.raises(fg.FemGpuError) as ei:
+        _euler(g, precision="MIXED_IR")
+    assert ei.value.code == -1
+
+
 def test_euler_call_order(gpu_lib):
     import fem_codes_gb300 as fg
     g = _load(CASES[0])
