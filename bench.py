@@ -579,7 +579,7 @@ def run_euler(a):
         mv_bytes = m.nel * (144 * 4 + 48) + pb.neq * (4 + 8)
         mv_gbs = mv_bytes / (kt["ebemv32"] * 1e-3) / 1e9
         mv_name, mv_note, mv_traffic = ("k_ebemv_blk32<4> (12x12 FP32 EBE matvec, row gather)",
-                                        "FP32 fused multiply-adds, FP64 row totals", None)
+                                        "FP32 fused multiply-adds, FP64 row totals", read_traffic("euler_ebemv32"))
     else:
         mv_bytes = m.nel * (144 * 8 + 48) + 2 * pb.neq * 8
         mv_gbs = mv_bytes / (kt["ebemv"] * 1e-3) / 1e9
