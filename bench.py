@@ -43,7 +43,7 @@ METRIC = "time-to-solution at 1e-8 residual, learned vs ILU/AMG precond; matvec 
 L2_BYTES = 129 * 1024 * 1024
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -65,7 +65,7 @@ def parse():
                     help="MIXED_IR: FP32 element matrices and preconditioner inside FGMRES, FP64 residuals")
     ap.add_argument("--euler-solver", default="GMRES", choices=["GMRES", "FGMRES"])
     ap.add_argument("--no-learned", action="store_true")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def peaks():
@@ -136,6 +136,18 @@ class Clocks:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def max_over_ranks(x, dist=None):
+    """The job's time per step with N replicas: the slowest rank's (an
+    all-reduce MAX on the process group; CUDA tensor for NCCL, CPU for gloo)."""
+    if dist is None or not dist.is_initialized():
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 # --------------------------------------------------------------------- CPU
@@ -237,10 +249,7 @@ def run_ours(a):
     clocks = clk.stop()
     ms = e0.elapsed_time(e1) / a.steps
     rel = T.true_residual()
-    if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(ms, dist)
 
     # ---- end to end through the host-buffer C ABI (pinned host memory) ----
     u_h = torch.zeros(n1, dtype=torch.float64, pin_memory=True)
