@@ -71,7 +71,8 @@ class NSOpts(ctypes.Structure):
     """femgpu_ns_opts of femgpu.h."""
     _fields_ = [("re", ctypes.c_double), ("velmax", ctypes.c_double), ("precond", ctypes.c_int),
                 ("solver", ctypes.c_int), ("kmax", ctypes.c_int), ("lmax", ctypes.c_int),
-                ("eta0", ctypes.c_double), ("eta_case", ctypes.c_int), ("tol_nl", ctypes.c_double)]
+                ("eta0", ctypes.c_double), ("eta_case", ctypes.c_int), ("tol_nl", ctypes.c_double),
+                ("scheme", ctypes.c_int)]
 
 
 _vp = ctypes.c_void_p
@@ -156,6 +157,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_ns_precond_setup": [_vp, _vp],
         "femgpu_ns_solve": [_vp, _vp, _vp, _ip],
         "femgpu_ns_newton": [_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp],
+        "femgpu_ns_csr": [_vp, _vp, _vp, _vp, _vp],
     }.items():
         f = getattr(L, name)
         f.argtypes = args
@@ -655,10 +657,11 @@ class NavierStokes:
     neq+1."""
 
     def __init__(self, x, y, vert, node_id, neq, upresc, f=None, re=1000.0, velmax=1.0, precond="BlockDiag",
-                 solver="GMRES", kmax=50, lmax=100, eta0=0.1, eta_case=2, tol_nl=1e-8):
+                 solver="GMRES", kmax=50, lmax=100, eta0=0.1, eta_case=2, tol_nl=1e-8, scheme="EBE"):
         L = load()
         o = NSOpts()
         L.femgpu_ns_default_opts(ctypes.byref(o))
+        o.scheme = OPTS["scheme"][scheme.upper()]
         o.re, o.velmax = float(re), float(velmax)
         o.precond = OPTS["precond"][precond.upper()]
         o.solver = OPTS["solver"][solver.upper()]
@@ -736,6 +739,14 @@ class NavierStokes:
         if rc and rc != -5:
             raise FemGpuError(rc, "solver")
         return X, it.value
+
+    def csr(self):
+        """CSR storage: (IA, JA, AA) of the last build."""
+        nn = np.zeros(2, np.int32)
+        self._check(self._L.femgpu_ns_csr(self._h, _ptr(nn), None, None, None), "csr")
+        IA, JA, AA = np.zeros(nn[0] + 1, np.int32), np.zeros(nn[1], np.int32), np.zeros(nn[1] + 1)
+        self._check(self._L.femgpu_ns_csr(self._h, _ptr(nn), _ptr(IA), _ptr(JA), _ptr(AA)), "csr")
+        return IA, JA, AA
 
     def Process(self, maxit=2000):
         """Damped Newton from u = 0: (u, uhist [n, neq+1], |F| [n], w [n],

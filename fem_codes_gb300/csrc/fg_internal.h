@@ -176,7 +176,14 @@ int fg_precond(femgpu_transport *t, const double *p, double *z, const int *activ
  * 1: FP32 preconditioner, 2: FP32 preconditioner and operator). */
 int fg_kry_pgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X);
 int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int mixed);
-/* st->rho = ||B - A X|| (overwrites V[0]). */
+/* CSR storage for M equations per element (M = 9: Navier-Stokes): pattern,
+ * CSR_by_Element slots [M*M*nel], and the per-row assembly from element
+ * matrices Ae [nel][M][M] (device arrays; pattern arrays allocated here). */
+int fg_build_csr_m(int M, int nel, int neq, const int *ri_ptr, const int *ri, const int *lm, cudaStream_t s,
+                   int *err, int **IA, int **JA, int **sbe, int *nnz);
+int fg_assemble_csr_m(int M, int neq, int nnz, const int *IA, const int *sbe, const int *ri_ptr, const int *ri,
+                      const double *Ae, double *AA, cudaStream_t s);
+/* st->rho = ||B - A X|| (A X is formed in V[kmax]). */
 int fg_kry_true_rho(const fg_krylov *k, const fg_linop *op, const double *B, double *X);
 int fg_kry_dot(const fg_krylov *k, const double *a, const double *b, int n, double *out_dev);
 /* The transport context's Krylov buffers and operator as a view. */

@@ -1,6 +1,6 @@
 /* State of a steady Navier-Stokes context (VMS build, 3-dof block EBE
- * storage, nodal block-diagonal preconditioner, Krylov workspace, damped
- * Newton vectors).  Plain C; shared by ns_build.cu and host/ns.c.
+ * storage with the nodal block-diagonal preconditioner, or CSR storage with
+ * ILU(0); Krylov workspace, damped Newton vectors).  Plain C; shared by ns_build.cu and host/ns.c.
  * Device layout: x, y [nnodes]; upresc [3*nnodes]; nodal force f [2*nnodes];
  * u, F, s, Fold [neq+1]; element residuals Re [9*nel]; stabilisation state
  * dold, nold [nel]; element matrices in the block-EBE context (A [81*nel]). */
@@ -27,6 +27,14 @@ struct femgpu_ns {
 	int setup_tag;                 /* precond_setup calls                     */
 	int have_bd;
 	fg_krylov kry;
+	/* CSR storage (scheme FEMGPU_CSR): pattern, CSR_by_Element slots
+	 * [81*nel], values [nnz+1]; the ILU(0) engine works on a transport
+	 * context that holds only this CSR system and its factors */
+	int *IA, *JA, *sbe;
+	double *AA;
+	int nnz;
+	femgpu_transport *ilu;
+	int have_ilu;
 };
 
 /* Build_K_F_MS on the device state u: element matrices into ebe->A, F, and

@@ -234,6 +234,97 @@ extern "C" int fg_build_csr(femgpu_transport *t)
 	return herr ? herr : 0;
 }
 
+// ------------------------------------------------------- block CSR -----
+// The same CSR set-up for M equations per element (the Navier-Stokes
+// csr_Initialization.c:18-85: rows of lm[e][0..M), the diagonal included,
+// sorted unique; CSR_by_Element slot M*a+b of element e, or nnz when either
+// equation is prescribed).  Incidence codes e*M + a.
+template <int M>
+__global__ void k_csr_rows_m(const int *ri_ptr, const int *ri, const int *lm, int neq, int *rowlen, const int *IA,
+                             int *JA, int *err)
+{
+	int row[FG_MAXROW];
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < neq; I += gridDim.x * blockDim.x) {
+		int m = 0, ok = 1;
+		for (int q = ri_ptr[I]; q < ri_ptr[I + 1]; q++) {
+			int e = ri[q] / M;
+			for (int b = 0; b < M; b++) {
+				int J = lm[M * e + b];
+				if (J != neq) ok &= ins_sorted(row, &m, J);
+			}
+		}
+		if (!ok) fg_set_err(err, FEMGPU_E_MESH);
+		if (rowlen) rowlen[I] = m;
+		if (JA) {
+			int base = IA[I];
+			for (int q = 0; q < m; q++) JA[base + q] = row[q];
+		}
+	}
+}
+
+template <int M>
+__global__ void k_csr_sbe_m(const int *lm, const int *IA, const int *JA, int nel, int neq, int nnz, int *sbe)
+{
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nel; e += gridDim.x * blockDim.x)
+		for (int a = 0; a < M; a++)
+			for (int b = 0; b < M; b++) {
+				int I = lm[M * e + a], J = lm[M * e + b];
+				sbe[(long long)M * M * e + M * a + b] = (I == neq || J == neq) ? nnz
+					: bsearch_row(JA, IA[I], IA[I + 1], J);
+			}
+}
+
+// csr_assembly.c:3-19 per row: each slot sums its elements' entries in
+// ascending element order (the reference's += over elements), AA[nnz] = 0.
+template <int M>
+__global__ void k_assemble_csr_m(int neq, int nnz, const int *IA, const int *sbe, const int *ri_ptr, const int *ri,
+                                 const double *Ae, double *AA)
+{
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < neq; I += gridDim.x * blockDim.x) {
+		for (int k = IA[I]; k < IA[I + 1]; k++) AA[k] = 0.0;
+		for (int q = ri_ptr[I]; q < ri_ptr[I + 1]; q++) {
+			int code = __ldg(&ri[q]), e = code / M, a = code - e * M;
+			const int *sl = sbe + (long long)M * M * e + M * a;
+			const double *row = Ae + (long long)M * M * e + M * a;
+			for (int b = 0; b < M; b++) {
+				int pos = __ldg(&sl[b]);
+				if (pos < nnz) AA[pos] = AA[pos] + __ldg(&row[b]);
+			}
+		}
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) AA[nnz] = 0.0;
+}
+
+extern "C" int fg_build_csr_m(int M, int nel, int neq, const int *ri_ptr, const int *ri, const int *lm,
+                              cudaStream_t s, int *err, int **IA, int **JA, int **sbe, int *nnz)
+{
+	int *rowlen = nullptr, herr = 0;
+	if (M != 9) return FEMGPU_E_ARG;
+	FG_TRY(cudaMalloc(&rowlen, sizeof(int) * (neq + 1)));
+	FG_TRY(cudaMalloc(IA, sizeof(int) * (neq + 1)));
+	k_csr_rows_m<9><<<fg_grid(neq, 128), 128, 0, s>>>(ri_ptr, ri, lm, neq, rowlen, nullptr, nullptr, err);
+	int rc = fg_scan(rowlen, *IA, neq, s);
+	if (rc) return rc;
+	FG_TRY(cudaMemcpy(nnz, *IA + neq, sizeof(int), cudaMemcpyDeviceToHost));
+	FG_TRY(cudaMalloc(JA, sizeof(int) * ((size_t)*nnz + 1)));
+	FG_TRY(cudaMalloc(sbe, sizeof(int) * 81 * (size_t)nel));
+	k_csr_rows_m<9><<<fg_grid(neq, 128), 128, 0, s>>>(ri_ptr, ri, lm, neq, nullptr, *IA, *JA, err);
+	k_csr_sbe_m<9><<<fg_grid(nel), FG_TPB, 0, s>>>(lm, *IA, *JA, nel, neq, *nnz, *sbe);
+	FG_TRY(cudaGetLastError());
+	FG_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+	FG_TRY(cudaStreamSynchronize(s));
+	cudaFree(rowlen);
+	return herr ? herr : 0;
+}
+
+extern "C" int fg_assemble_csr_m(int M, int neq, int nnz, const int *IA, const int *sbe, const int *ri_ptr,
+                                 const int *ri, const double *Ae, double *AA, cudaStream_t s)
+{
+	if (M != 9) return FEMGPU_E_ARG;
+	k_assemble_csr_m<9><<<fg_grid(neq, 128, 32), 128, 0, s>>>(neq, nnz, IA, sbe, ri_ptr, ri, Ae, AA);
+	return (int)cudaGetLastError();
+}
+
 // ------------------------------------------------------------- EDE -------
 // Sorted vertex triple of ede_Initialization.c:24-78 (its tie rule kept).
 __device__ __forceinline__ void ede_sort3(const int *l, int *I, int *o)

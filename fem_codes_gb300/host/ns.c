@@ -2,10 +2,10 @@
  * Host driver of the steady Navier-Stokes path: the control flow of the
  * reference's Process (04_SS_NavierStokes_Equations/2D/01_CommonFiles/
  * Process.c:62-194: damped Newton with backtracking on ||F||, F the
- * block-diagonally preconditioned residual) and its forcing terms
- * (eta_newton.c:5-68) around device kernels for the VMS build, the 3-dof
- * block-EBE operator, the nodal block-diagonal preconditioner and GMRES.
- * Plain C.
+ * preconditioned residual) and its forcing terms (eta_newton.c:5-68)
+ * around device kernels for the VMS build, the 3-dof block-EBE operator with
+ * the nodal block-diagonal preconditioner or the CSR operator with ILU(0)
+ * (the drivers' two configurations), and GMRES.  Plain C.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -45,6 +45,79 @@ static int op_precond(void *ctx, const double *p, double *z, const int *active)
 	return fg_ebe_blockdiag_apply(((femgpu_ns *)ctx)->ebe, p, z, 0);
 }
 
+/* CSR storage: csrmv and ILUp_precond */
+static int op_matvec_csr(void *ctx, const double *p, double *q, const int *active)
+{
+	femgpu_ns *c = (femgpu_ns *)ctx;
+	return fg_csrmv64(c->neq, c->IA, c->JA, c->AA, p, q, active, c->stream);
+}
+
+static int op_precond_ilu(void *ctx, const double *p, double *z, const int *active)
+{
+	return fg_ilu0_apply64(((femgpu_ns *)ctx)->ilu, p, z, active);
+}
+
+/* csr_Initialization (reordering NOT) on the device, and the ILU(0) engine
+ * (level schedules and sweep programs of the pattern, factor storage) on a
+ * transport context that holds only this CSR system. */
+static int create_csr(femgpu_ns *c)
+{
+	femgpu_transport *t;
+	int *hIA = NULL, *hJA = NULL, *err = NULL, rc;
+	size_t n1 = (size_t)c->neq + 1;
+	DM(err, sizeof(int));
+	CK(cudaMemset(err, 0, sizeof(int)));
+	rc = fg_build_csr_m(9, c->nel, c->neq, c->ebe->ri_ptr, c->ebe->ri, c->ebe->lm, c->stream, err, &c->IA, &c->JA,
+	                    &c->sbe, &c->nnz);
+	cudaFree(err);
+	if (rc) { fgh_set_error("Navier-Stokes CSR pattern: %d", rc); return rc > 0 ? FEMGPU_E_CUDA : rc; }
+	DM(c->AA, sizeof(double) * ((size_t)c->nnz + 1));
+	CK(cudaMemset(c->AA, 0, sizeof(double) * ((size_t)c->nnz + 1)));
+	if (c->o.precond != FEMGPU_PREC_ILU0) return 0;
+	t = c->ilu = calloc(1, sizeof *t);
+	if (!t) return FEMGPU_E_NOMEM;
+	femgpu_transport_default_opts(&t->o);
+	t->o.precond = FEMGPU_PREC_ILU0;
+	t->o.solver = c->o.solver;
+	t->neq = c->neq; t->nnz = c->nnz;
+	t->IA = c->IA; t->JA = c->JA; t->A = c->AA;
+	t->stream = c->stream;
+	DM(t->st, sizeof(fg_status));
+	CK(cudaMemset(t->st, 0, sizeof(fg_status)));
+	t->ilu.n = c->neq; t->ilu.nnz = c->nnz;
+	DM(t->ilu.LU, sizeof(double) * ((size_t)c->nnz + 1));
+	DM(t->ilu.Dinv, sizeof(double) * n1);
+	hIA = malloc(sizeof(int) * n1);
+	hJA = malloc(sizeof(int) * ((size_t)c->nnz + 1));
+	if (!hIA || !hJA) { free(hIA); free(hJA); return FEMGPU_E_NOMEM; }
+	rc = (cudaMemcpy(hIA, c->IA, sizeof(int) * n1, cudaMemcpyDeviceToHost) != cudaSuccess ||
+	      cudaMemcpy(hJA, c->JA, sizeof(int) * (size_t)c->nnz, cudaMemcpyDeviceToHost) != cudaSuccess)
+	     ? FEMGPU_E_CUDA : fg_ilu_prepare(t, hIA, hJA);
+	free(hIA); free(hJA);
+	if (rc) { fgh_set_error("Navier-Stokes ILU(0) set-up: %d", rc); return rc > 0 ? FEMGPU_E_CUDA : rc; }
+	c->have_ilu = 1;
+	return 0;
+}
+
+static void destroy_csr(femgpu_ns *c)
+{
+	femgpu_transport *t = c->ilu;
+	if (t) {
+		if (c->have_ilu) fg_ilu_free(t);
+		if (t->st) cudaFree(t->st);
+		if (t->ilu.LU) cudaFree(t->ilu.LU);
+		if (t->ilu.Dinv) cudaFree(t->ilu.Dinv);
+		free(t);
+		c->ilu = NULL;
+	}
+	if (c->IA) cudaFree(c->IA);
+	if (c->JA) cudaFree(c->JA);
+	if (c->sbe) cudaFree(c->sbe);
+	if (c->AA) cudaFree(c->AA);
+	c->IA = c->JA = c->sbe = NULL;
+	c->AA = NULL;
+}
+
 static int up(double **dst, const double *src, size_t n)
 {
 	int rc = fgh_dmalloc((void **)dst, sizeof(double) * n);
@@ -76,6 +149,7 @@ static int create(femgpu_ns *c, const femgpu_ns_opts *o, int nnodes, const doubl
 		return rc;
 	rc = fgh_kry_alloc(&c->kry, neq, o->kmax, o->solver == FEMGPU_FGMRES ? 1 : 0, c->stream);
 	if (rc) return rc;
+	if (o->scheme == FEMGPU_CSR && (rc = create_csr(c))) return rc;
 	CK(cudaStreamSynchronize(c->stream));
 	return 0;
 }
@@ -91,7 +165,10 @@ int femgpu_ns_create(femgpu_ns **out, const femgpu_ns_opts *opts, int nnodes, co
 	if (opts) o = *opts; else femgpu_ns_default_opts(&o);
 	if (nnodes <= 0 || nel <= 0 || neq <= 0 || !x || !y || !vert || !node_id || !upresc || !(o.re > 0.0) ||
 	    o.kmax < 1 || o.lmax < 1 || o.eta_case < 0 || o.eta_case > 4 || !(o.eta0 > 0.0) ||
-	    (o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_BLOCKDIAG) ||
+	    (o.scheme != FEMGPU_EBE && o.scheme != FEMGPU_CSR) ||
+	    (o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_BLOCKDIAG && o.precond != FEMGPU_PREC_ILU0) ||
+	    (o.precond == FEMGPU_PREC_BLOCKDIAG && o.scheme != FEMGPU_EBE) ||     /* setPreconditioner.c:54-73 */
+	    (o.precond == FEMGPU_PREC_ILU0 && o.scheme != FEMGPU_CSR) ||
 	    (o.solver != FEMGPU_PGMRES && o.solver != FEMGPU_FGMRES)) {
 		fgh_set_error("femgpu_ns_create: bad argument or option");
 		return FEMGPU_E_ARG;
@@ -109,6 +186,7 @@ void femgpu_ns_destroy(femgpu_ns *c)
 	int i;
 	if (!c) return;
 	if (c->stream) cudaStreamSynchronize(c->stream);
+	destroy_csr(c);
 	if (c->ebe) femgpu_ebe_destroy(c->ebe);
 	{
 		void *p[] = { c->x, c->y, c->upresc, c->f, c->u, c->F, c->s, c->Fold, c->Re, c->dold, c->nold };
@@ -125,6 +203,7 @@ int femgpu_ns_set_stream(femgpu_ns *c, void *stream)
 	CK(cudaStreamSynchronize(c->stream));
 	c->stream = stream ? (cudaStream_t)stream : c->own_stream;
 	c->kry.stream = c->stream;
+	if (c->ilu) c->ilu->stream = c->stream;
 	KR(femgpu_ebe_set_stream(c->ebe, c->stream));
 	return 0;
 }
@@ -147,8 +226,22 @@ int femgpu_ns_build_dev(femgpu_ns *c)
 {
 	if (!c) return FEMGPU_E_ARG;
 	KR(fg_ns_build(c, c->nbuild == 0));
+	if (c->o.scheme == FEMGPU_CSR)                              /* csr_assembly, element by element */
+		KR(fg_assemble_csr_m(9, c->neq, c->nnz, c->IA, c->sbe, c->ebe->ri_ptr, c->ebe->ri, c->ebe->A, c->AA,
+		                     c->stream));
 	c->nbuild++;
 	c->have_bd = 0;
+	return 0;
+}
+
+int femgpu_ns_csr(femgpu_ns *c, int *n_nnz, int *IA, int *JA, double *AA)
+{
+	if (!c || !n_nnz || c->o.scheme != FEMGPU_CSR) return FEMGPU_E_ARG;
+	n_nnz[0] = c->neq; n_nnz[1] = c->nnz;
+	if (IA) CK(cudaMemcpyAsync(IA, c->IA, sizeof(int) * ((size_t)c->neq + 1), cudaMemcpyDeviceToHost, c->stream));
+	if (JA) CK(cudaMemcpyAsync(JA, c->JA, sizeof(int) * (size_t)c->nnz, cudaMemcpyDeviceToHost, c->stream));
+	if (AA) CK(cudaMemcpyAsync(AA, c->AA, sizeof(double) * ((size_t)c->nnz + 1), cudaMemcpyDeviceToHost, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
 	return 0;
 }
 
@@ -171,6 +264,17 @@ static int setup_dev(femgpu_ns *c)
 {
 	if (!c->nbuild) { fgh_set_error("precond_setup before build"); return FEMGPU_E_NOT_BUILT; }
 	c->setup_tag++;
+	if (c->o.precond == FEMGPU_PREC_ILU0) {
+		/* ILUp_precond_setup.c:8-167 at fill level 0, then F := M^-1 F */
+		int err = 0;
+		KR(fg_ilu0_factor(c->ilu));
+		CK(cudaMemcpyAsync(&err, &c->ilu->st->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+		CK(cudaStreamSynchronize(c->stream));
+		if (err) { fgh_set_error("ILU(0) factorisation: %d", err); return err; }
+		c->have_bd = 1;
+		if (c->o.solver == FEMGPU_PGMRES) KR(fg_ilu0_apply64(c->ilu, c->F, c->F, NULL));
+		return 0;
+	}
 	if (c->o.precond != FEMGPU_PREC_BLOCKDIAG) return 0;
 	KR(fg_ebe_blockdiag_setup(c->ebe));
 	c->ebe->have_bd = 1;
@@ -195,7 +299,7 @@ static int solve(femgpu_ns *c, const double *B, double *X, int *iters)
 	fg_linop op;
 	double nb2;
 	int it = 0, rc;
-	if (c->o.precond == FEMGPU_PREC_BLOCKDIAG && !c->have_bd) {
+	if (c->o.precond != FEMGPU_PREC_NOT && !c->have_bd) {
 		fgh_set_error("solve before precond_setup");
 		return FEMGPU_E_NOT_BUILT;
 	}
@@ -205,8 +309,9 @@ static int solve(femgpu_ns *c, const double *B, double *X, int *iters)
 	if (!(nb2 > 0.0)) return nb2 == 0.0 ? 0 : FEMGPU_E_BREAKDOWN;
 	memset(&op, 0, sizeof op);
 	op.ctx = c;
-	op.matvec = op_matvec;
-	op.precond = c->o.precond == FEMGPU_PREC_BLOCKDIAG ? op_precond : NULL;
+	op.matvec = c->o.scheme == FEMGPU_CSR ? op_matvec_csr : op_matvec;
+	op.precond = c->o.precond == FEMGPU_PREC_BLOCKDIAG ? op_precond
+	           : c->o.precond == FEMGPU_PREC_ILU0 ? op_precond_ilu : NULL;
 	rc = fgh_kry_cycles(&c->kry, &op, B, X, c->o.solver == FEMGPU_PGMRES ? -1 : 0, c->tol * sqrt(nb2), c->o.lmax,
 	                    &it);
 	*iters = it;

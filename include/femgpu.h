@@ -297,12 +297,16 @@ int femgpu_euler_last_times(const femgpu_euler *ctx, double *t);
 typedef struct femgpu_ns_opts {
 	double re;           /* ReynoldsNumber                                   */
 	double velmax;       /* VelMax (reference velocity of the local Re)      */
-	int precond;         /* FEMGPU_PREC_NOT or FEMGPU_PREC_BLOCKDIAG         */
+	int precond;         /* FEMGPU_PREC_NOT, FEMGPU_PREC_BLOCKDIAG (EBE) or  */
+	                     /* FEMGPU_PREC_ILU0 (CSR)                           */
 	int solver;          /* femgpu_solver: PGMRES (reference) or FGMRES      */
 	int kmax, lmax;      /* KrylovBasisVectorsQuantity, LinearMaxIter        */
 	double eta0;         /* SolverTolerance: initial / maximal forcing term  */
 	int eta_case;        /* SolverToleranceCase 0..4 (eta_newton.c)          */
 	double tol_nl;       /* SolverToleranceNonLin: ||F|| <= tol_nl ||F_0||   */
+	int scheme;          /* FEMGPU_EBE (9x9 element blocks) or FEMGPU_CSR    */
+	                     /* (csr_Initialization.c / csr_assembly.c, numbering */
+	                     /* of the node ids as given: reordering NOT)         */
 } femgpu_ns_opts;
 
 void femgpu_ns_default_opts(femgpu_ns_opts *o);
@@ -338,6 +342,10 @@ int femgpu_ns_solve(femgpu_ns *ctx, const double *B_host, double *X_host, int *i
  * number of Newton iterations done (>= 0) or an error code. */
 int femgpu_ns_newton(femgpu_ns *ctx, int maxit, double *u_host, double *uhist, double *normF, double *w,
 		int *gmres);
+/* CSR storage: sizes n_nnz = {neq, nnz} and (arrays may be NULL) the pattern
+ * IA [neq+1], JA [nnz] and the values of the last build AA [nnz+1];
+ * FEMGPU_E_ARG for EBE storage. */
+int femgpu_ns_csr(femgpu_ns *ctx, int *n_nnz, int *IA, int *JA, double *AA);
 double *femgpu_ns_u_dev(femgpu_ns *ctx);
 femgpu_ebe *femgpu_ns_ebe(femgpu_ns *ctx);
 

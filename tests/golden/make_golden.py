@@ -270,6 +270,12 @@ def ns_lib():
                                 ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                 ctypes.c_double, ctypes.c_int, _dp, _dp, _dp, _ip]
     L.ref_ns_newton.restype = ctypes.c_int
+    L.ref_ns_newton_csr.argtypes = L.ref_ns_newton.argtypes
+    L.ref_ns_newton_csr.restype = ctypes.c_int
+    L.ref_ns_builds_csr.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_int, _dp, ctypes.c_int, _ip, _ip, _dp, _dp, _dp, _dp,
+                                    _dp]
+    L.ref_ns_builds_csr.restype = ctypes.c_int
     L.CAVITY_v1presc.argtypes = [ctypes.c_double, ctypes.c_double]
     L.CAVITY_v1presc.restype = ctypes.c_double
     return L
@@ -308,12 +314,31 @@ def main_ns():
         g = np.zeros(maxit, np.int32)
         nit = L2.ref_ns_newton(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, re, 1.0, kmax, lmax, eta0,
                                ecase, tolnl, maxit, uh, nF, w, g)
+        # CSR storage with ILU(0): pattern, three builds' assembled values,
+        # F := M^-1 F, one ILU(0) application, and the damped-Newton run
+        cap = 81 * mesh.nel
+        cIA, cJA = np.zeros(neq + 1, np.int32), np.zeros(cap, np.int32)
+        cAA, cF = np.zeros(3 * (cap + 1)), np.zeros(3 * (neq + 1))
+        cFp, cz = np.zeros(neq + 1), np.zeros(neq + 1)
+        cp = np.zeros(neq + 1)
+        cp[:neq] = rng.uniform(-1.0, 1.0, neq)
+        nnz = ns_lib().ref_ns_builds_csr(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, re, 1.0, 3,
+                                         us.reshape(-1), cap, cIA, cJA, cAA, cF, cFp, cp, cz)
+        cAA = cAA.reshape(3, cap + 1)[:, : nnz + 1]
+        cuh = np.zeros(maxit * (neq + 1))
+        cnF, cw, cg = np.zeros(maxit), np.zeros(maxit), np.zeros(maxit, np.int32)
+        cnit = ns_lib().ref_ns_newton_csr(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, re, 1.0, kmax,
+                                          lmax, eta0, ecase, tolnl, maxit, cuh, cnF, cw, cg)
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id, neq=neq,
             upresc=up, f=pb.f, re=re, velmax=1.0, us=us, Ae=Ae.reshape(3, mesh.nel, 81), F=F.reshape(3, neq + 1),
             delta_old=dold, normres_old=nold, kmax=kmax, lmax=lmax, eta0=eta0, ecase=ecase, tolnl=tolnl,
-            maxit=maxit, uhist=uh.reshape(maxit, neq + 1)[:nit], normF=nF[:nit], w=w[:nit], gmres=g[:nit])
-        print(f"{name}: neq={neq} nel={mesh.nel} newton={nit} |F|={nF[:nit]} gmres={g[:nit]}")
+            maxit=maxit, uhist=uh.reshape(maxit, neq + 1)[:nit], normF=nF[:nit], w=w[:nit], gmres=g[:nit],
+            csr_IA=cIA, csr_JA=cJA[:nnz], csr_AA=cAA, csr_F=cF.reshape(3, neq + 1), csr_Fp=cFp, csr_p=cp,
+            csr_z=cz, csr_uhist=cuh.reshape(maxit, neq + 1)[:cnit], csr_normF=cnF[:cnit], csr_w=cw[:cnit],
+            csr_gmres=cg[:cnit])
+        print(f"{name}: neq={neq} nel={mesh.nel} newton={nit} |F|={nF[:nit]} gmres={g[:nit]}; "
+              f"CSR nnz={nnz} ILU(0) newton={cnit} |F|={cnF[:cnit]} gmres={cg[:cnit]}")
 
 
 # name -> (nx, ny, perturb, node rule, transport kwargs, AMG deck string)

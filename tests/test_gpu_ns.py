@@ -74,6 +74,47 @@ def test_ns_newton_vs_reference(gpu_lib, name):
     assert np.array_equal(u, uh[-1])
 
 
+@pytest.mark.parametrize("name", CASES)
+def test_ns_csr_builds_and_ilu0_setup_bitexact(gpu_lib, name):
+    """CSR storage (csr_Initialization / csr_assembly of the NS driver) and
+    ILU(0) precond_setup: pattern, assembled values and residual of three
+    consecutive builds, and F := M^-1 F, all bit-identical to the reference."""
+    g = _load(name)
+    neq = int(g["neq"])
+    with _ns(g, scheme="CSR", precond="ILU0") as ns:
+        for b in range(len(g["us"])):
+            F, _ = ns.Build(g["us"][b])
+            IA, JA, AA = ns.csr()
+            assert np.array_equal(IA, g["csr_IA"]) and np.array_equal(JA, g["csr_JA"]), b
+            assert np.array_equal(AA, g["csr_AA"][b]), b
+            assert np.array_equal(F, g["csr_F"][b]), b
+        Fp = ns.precond_setup()
+    assert np.array_equal(Fp[:neq], g["csr_Fp"][:neq])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_ns_csr_ilu0_newton_vs_reference(gpu_lib, name):
+    """The damped Newton loop with CSR storage and ILU(0), against the
+    reference's run: the bars of test_ns_newton_vs_reference."""
+    g = _load(name)
+    with _ns(g, scheme="CSR", precond="ILU0") as ns:
+        u, uh, nF, w, its = ns.Process(int(g["maxit"]))
+    assert len(nF) == len(g["csr_normF"])
+    assert np.array_equal(w, g["csr_w"])
+    assert _rel(nF, g["csr_normF"]) < 1e-6
+    assert _rel(uh, g["csr_uhist"]) < 1e-6
+    assert np.abs(its.astype(int) - g["csr_gmres"].astype(int)).max() <= 3
+
+
+def test_ns_scheme_and_preconditioner_pairs(gpu_lib):
+    import fem_codes_gb300 as fg
+    g = _load(CASES[0])
+    for kw in (dict(scheme="CSR", precond="BlockDiag"), dict(scheme="EBE", precond="ILU0")):
+        with pytest.raises(fg.FemGpuError) as ei:
+            _ns(g, **kw)
+        assert ei.value.code == -1
+
+
 def test_ns_builds_large_vs_oracle(gpu_lib):
     import fem_codes_gb300 as fg
     m = structured_mesh(48, 40, perturb=0.25, seed=9)
