@@ -106,3 +106,52 @@ def test_ilu_levels_natural_grid(lib):
 def test_bad_arguments_rejected_without_gpu(lib):
     assert lib.femgpu_symrcm(0, None, None, None) == -1
     assert lib.femgpu_ilu_levels(-3, None, None, 1) == -1
+
+
+def test_ns_bad_options_rejected_without_gpu(lib):
+    """femgpu_ns_create validates its options before touching the device:
+    storage / preconditioner pairs the reference's setPreconditioner.c
+    rejects (BlockDiag needs EBE, ILU needs CSR), an unknown scheme, a bad
+    forcing-term case."""
+    import fem_codes_gb300 as fg
+    x = np.zeros(3)
+    v = np.zeros(3, np.int32)
+    nid = np.zeros(9, np.int32)
+    up = np.zeros(9)
+    bad = [dict(scheme=2, precond=3), dict(scheme=0, precond=1), dict(scheme=1, precond=0),
+           dict(eta_case=7), dict(kmax=0)]
+    for kw in bad:
+        o = fg.NSOpts()
+        lib.femgpu_ns_default_opts(ctypes.byref(o))
+        assert (o.scheme, o.precond, o.solver) == (0, 3, 0)
+        for k, v_ in kw.items():
+            setattr(o, k, v_)
+        h = ctypes.c_void_p()
+        rc = lib.femgpu_ns_create(ctypes.byref(h), ctypes.byref(o), 3, x.ctypes.data, x.ctypes.data, 1,
+                                  v.ctypes.data, nid.ctypes.data, 3, up.ctypes.data, None)
+        assert rc == -1 and not h.value, kw
+
+
+def test_amg_and_transport_options_rejected_without_gpu(lib):
+    """AMG parameters outside amg_precond.c's forms, and the transport's AMG
+    preconditioner with EBE storage or a mixed precision, are refused before
+    any device work."""
+    import fem_codes_gb300 as fg
+    h = ctypes.c_void_p()
+    for ncl, beta, omega, nr in [(0, 0.25, 1.0, 2), (2, -0.5, 1.0, 2), (2, 0.25, 0.0, 2), (2, 0.25, 1.0, 0)]:
+        assert lib.femgpu_amg_create(ctypes.byref(h), ncl, ctypes.c_double(beta), ctypes.c_double(omega), nr) == -1
+    assert lib.femgpu_amg_setup(None, 1, None, None, None) == -1
+    m = structured_mesh(4, 4)
+    p = skew_problem(m)
+    vert = np.ascontiguousarray(m.vert.reshape(-1), np.int32)
+    nt = np.ascontiguousarray(p.node_type, np.int32)
+    for scheme, precision in [(0, 0), (2, 1)]:
+        o = fg.Opts()
+        lib.femgpu_transport_default_opts(ctypes.byref(o))
+        o.precond, o.scheme, o.precision, o.solver = 5, scheme, precision, 1
+        t = ctypes.c_void_p()
+        rc = lib.femgpu_transport_create(ctypes.byref(t), ctypes.byref(o), m.nnodes, m.x.ctypes.data,
+                                         m.y.ctypes.data, nt.ctypes.data, m.nel, vert.ctypes.data,
+                                         ctypes.c_double(p.k), ctypes.c_double(p.gamma), None,
+                                         np.array([0.8, 0.5]).ctypes.data, None, p.upresc.ctypes.data)
+        assert rc == -1 and not t.value, (scheme, precision)
