@@ -419,10 +419,11 @@ class SSTransport:
         return it.value
 
     def fell_back(self):
-        """True when the last learned-preconditioned solve switched to ILU(0)."""
+        """0, or how the last learned-preconditioned solve continued after a
+        stall: 1 ILU(0), 2 the attached AMG context."""
         info = np.zeros(7, np.int32)
         self._check(self._L.femgpu_transport_info(self._h, _ptr(info)), "info")
-        return bool(info[6])
+        return int(info[6])
 
     def u_dev(self):
         return self._L.femgpu_transport_u_dev(self._h)
@@ -435,7 +436,8 @@ class SSTransport:
 
     def set_amg(self, amg):
         """Use an :class:`AMG` context as the FEMGPU_PREC_AMG preconditioner
-        (its hierarchy is rebuilt from the matrix at every precond_setup)."""
+        (its hierarchy is rebuilt from the matrix at every precond_setup), or
+        as the fallback of the learned preconditioner."""
         self._amg = amg
         self._check(self._L.femgpu_transport_set_amg(self._h, amg.handle), "set_amg")
 

@@ -225,7 +225,8 @@ extern "C" int fg_precond(femgpu_transport *t, const double *p, double *z, const
 {
 	cudaStream_t s = t->stream;
 	if (t->o.precond == FEMGPU_PREC_LEARNED && !t->fell_back) return fg_gnn_forward(t->gnn, p, z, 0, active);
-	if (t->o.precond == FEMGPU_PREC_AMG) return fg_amg_vcycle(t->amg, p, z, active);
+	if (t->o.precond == FEMGPU_PREC_AMG || (t->o.precond == FEMGPU_PREC_LEARNED && t->fell_back == 2))
+		return fg_amg_vcycle(t->amg, p, z, active);
 	if (t->o.precond == FEMGPU_PREC_NOT) {
 		if (p != z) FG_TRY(cudaMemcpyAsync(z, p, sizeof(double) * t->neq, cudaMemcpyDeviceToDevice, s));
 		return 0;

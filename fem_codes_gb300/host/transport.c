@@ -518,7 +518,21 @@ static int cycles(femgpu_transport *t, const double *B, double *X, int kind, dou
  * the residual above stall_ratio times its value at the cycle's start
  * switches the rest of the solve to ILU(0) (factored then), continuing from
  * the current iterate; a breakdown (zero or NaN Arnoldi norm) restarts the
- * solve from X = 0 with ILU(0). */
+ * solve from X = 0 with ILU(0).  With an AMG context attached
+ * (femgpu_transport_set_amg) the fallback is its V-cycle instead. */
+static int fall_back(femgpu_transport *t)
+{
+	if (t->amg) {
+		int rc = amg_rebuild(t);
+		if (rc) return rc;
+		t->fell_back = 2;
+		return 0;
+	}
+	KR(fg_ilu0_factor(t));
+	t->fell_back = 1;
+	return 0;
+}
+
 static int learned_cycles(femgpu_transport *t, const double *B, double *X, double eps, double rho0,
                           int *iters)
 {
@@ -534,8 +548,7 @@ static int learned_cycles(femgpu_transport *t, const double *B, double *X, doubl
 		if (rc == FEMGPU_E_BREAKDOWN && !t->fell_back) {
 			done += k.st_host->total;
 			CK(cudaMemsetAsync(X, 0, sizeof(double) * (size_t)t->neq, t->stream));
-			KR(fg_ilu0_factor(t));
-			t->fell_back = 1;
+			if ((rc = fall_back(t))) return rc;
 			prev = rho0;
 			if ((rc = fgh_kry_begin(&k, eps))) return rc;
 			continue;
@@ -549,10 +562,7 @@ static int learned_cycles(femgpu_transport *t, const double *B, double *X, doubl
 			if (k.st_host->rho <= eps) break;
 			continue;
 		}
-		if (!t->fell_back && !(k.st_host->rho <= t->o.stall_ratio * prev)) {
-			KR(fg_ilu0_factor(t));
-			t->fell_back = 1;
-		}
+		if (!t->fell_back && !(k.st_host->rho <= t->o.stall_ratio * prev) && (rc = fall_back(t))) return rc;
 		prev = k.st_host->rho;
 	} while (l < t->o.lmax);
 	*iters += done + k.st_host->total;
@@ -565,7 +575,7 @@ static int learned_cycles(femgpu_transport *t, const double *B, double *X, doubl
 
 int femgpu_transport_set_amg(femgpu_transport *t, femgpu_amg *g)
 {
-	if (!t || !g || t->o.precond != FEMGPU_PREC_AMG) return FEMGPU_E_ARG;
+	if (!t || !g || (t->o.precond != FEMGPU_PREC_AMG && t->o.precond != FEMGPU_PREC_LEARNED)) return FEMGPU_E_ARG;
 	KR(femgpu_amg_set_stream(g, t->stream));
 	t->amg = g;
 	t->factored = 0;

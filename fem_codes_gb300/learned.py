@@ -250,10 +250,11 @@ def train(gnn: MeshGNN, sets, epochs=4, lr=2e-3, batch=8, seed=0, log=None, loss
     return hist
 
 
-def evaluate(spec, gnn=None, kmax=50, tol=1e-8, lmax=400, stall_ratio=0.9, precond=None):
+def evaluate(spec, gnn=None, kmax=50, tol=1e-8, lmax=400, stall_ratio=0.9, precond=None, amg=None):
     """FGMRES(kmax) on one problem's first Picard system with the learned
     preconditioner (gnn given), ILU(0) or none: (iterations, seconds to
-    solution, true relative residual, fell back)."""
+    solution, true relative residual, fell back: 0 no, 1 to ILU(0), 2 to the
+    AMG context amg when one is given)."""
     import torch
     nx, angle, k, seed = spec
     m, p = transport_problem(nx, nx, angle, k, seed)
@@ -262,6 +263,8 @@ def evaluate(spec, gnn=None, kmax=50, tol=1e-8, lmax=400, stall_ratio=0.9, preco
                                  tol=tol, solver="FGMRES", stall_ratio=stall_ratio)
     if gnn is not None and pc == "LEARNED":
         T.set_learned(gnn)
+        if amg is not None:
+            T.set_amg(amg)
     T.build_dev()
     torch.cuda.synchronize()
     t0 = time.perf_counter()

@@ -114,8 +114,8 @@ void femgpu_transport_destroy(femgpu_transport *ctx);
 int femgpu_transport_set_stream(femgpu_transport *ctx, void *stream);
 
 /* Sizes: info[0]=neq, [1]=nnzero, [2]=nedge, [3]=bandwidth after reordering,
- * [4]=ILU levels (L), [5]=ILU levels (U), [6]=1 when the last learned-
- * preconditioned solve fell back to ILU(0) (7 ints). */
+ * [4]=ILU levels (L), [5]=ILU levels (U), [6]=1 (2) when the last learned-
+ * preconditioned solve fell back to ILU(0) (to AMG) (7 ints). */
 int femgpu_transport_info(const femgpu_transport *ctx, int *info);
 
 /* Copies of the device-built structure, for parity checks against the
@@ -426,8 +426,9 @@ int femgpu_amg_level(const femgpu_amg *ctx, int l, int *n_nnz, int *IA, int *JA,
 /* z = M^-1 q, one V-cycle (q == z allowed). */
 int femgpu_amg_apply(femgpu_amg *ctx, const double *q_host, double *z_host);
 int femgpu_amg_apply_dev(femgpu_amg *ctx, const double *q, double *z);
-/* Use ctx as the FEMGPU_PREC_AMG preconditioner of a CSR transport context:
- * precond_setup rebuilds the hierarchy from the current matrix. */
+/* Use ctx as the FEMGPU_PREC_AMG preconditioner of a CSR transport context
+ * (precond_setup rebuilds the hierarchy from the current matrix), or as the
+ * fallback of a FEMGPU_PREC_LEARNED context (built when a solve stalls). */
 int femgpu_transport_set_amg(femgpu_transport *t, femgpu_amg *ctx);
 
 /* ---- stateless device kernels (device pointers, stream as void*) -------- */

@@ -108,6 +108,20 @@ def test_trained_network_beats_no_preconditioner(gpu_lib):
     net.close()
 
 
+def test_learned_falls_back_to_amg_on_stall(gpu_lib):
+    """With an AMG context attached, a stalled learned solve continues with
+    the AMG V-cycle (built from the current matrix at the switch) and
+    converges on the true residual."""
+    import fem_codes_gb300 as fg
+    from fem_codes_gb300 import learned as Ld
+    net = Ld.MeshGNN(seed=123)
+    amg = fg.AMG(ncl=3, beta=-1.0, omega=1.0, nr=2)
+    out = Ld.evaluate((48, 0.9, 1e-4, 5), net, kmax=30, lmax=400, stall_ratio=1e-3, amg=amg)
+    assert out["fell_back"] == 2 and out["converged"]
+    amg.close()
+    net.close()
+
+
 def test_learned_falls_back_to_ilu_on_stall(gpu_lib):
     """An untrained (random) network that does not reduce the residual fast
     enough hands the solve to ILU(0), which then converges; the network
