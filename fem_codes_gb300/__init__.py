@@ -72,7 +72,7 @@ class NSOpts(ctypes.Structure):
     _fields_ = [("re", ctypes.c_double), ("velmax", ctypes.c_double), ("precond", ctypes.c_int),
                 ("solver", ctypes.c_int), ("kmax", ctypes.c_int), ("lmax", ctypes.c_int),
                 ("eta0", ctypes.c_double), ("eta_case", ctypes.c_int), ("tol_nl", ctypes.c_double),
-                ("scheme", ctypes.c_int)]
+                ("scheme", ctypes.c_int), ("ilu_blocks", ctypes.c_int)]
 
 
 _vp = ctypes.c_void_p
@@ -659,11 +659,13 @@ class NavierStokes:
     neq+1."""
 
     def __init__(self, x, y, vert, node_id, neq, upresc, f=None, re=1000.0, velmax=1.0, precond="BlockDiag",
-                 solver="GMRES", kmax=50, lmax=100, eta0=0.1, eta_case=2, tol_nl=1e-8, scheme="EBE"):
+                 solver="GMRES", kmax=50, lmax=100, eta0=0.1, eta_case=2, tol_nl=1e-8, scheme="EBE",
+                 ilu_blocks=0):
         L = load()
         o = NSOpts()
         L.femgpu_ns_default_opts(ctypes.byref(o))
         o.scheme = OPTS["scheme"][scheme.upper()]
+        o.ilu_blocks = int(ilu_blocks)
         o.re, o.velmax = float(re), float(velmax)
         o.precond = OPTS["precond"][precond.upper()]
         o.solver = OPTS["solver"][solver.upper()]

@@ -79,6 +79,7 @@ static int create_csr(femgpu_ns *c)
 	femgpu_transport_default_opts(&t->o);
 	t->o.precond = FEMGPU_PREC_ILU0;
 	t->o.solver = c->o.solver;
+	t->o.ilu_blocks = c->o.ilu_blocks;
 	t->neq = c->neq; t->nnz = c->nnz;
 	t->IA = c->IA; t->JA = c->JA; t->A = c->AA;
 	t->stream = c->stream;
@@ -165,7 +166,7 @@ int femgpu_ns_create(femgpu_ns **out, const femgpu_ns_opts *opts, int nnodes, co
 	if (opts) o = *opts; else femgpu_ns_default_opts(&o);
 	if (nnodes <= 0 || nel <= 0 || neq <= 0 || !x || !y || !vert || !node_id || !upresc || !(o.re > 0.0) ||
 	    o.kmax < 1 || o.lmax < 1 || o.eta_case < 0 || o.eta_case > 4 || !(o.eta0 > 0.0) ||
-	    (o.scheme != FEMGPU_EBE && o.scheme != FEMGPU_CSR) ||
+	    (o.scheme != FEMGPU_EBE && o.scheme != FEMGPU_CSR) || o.ilu_blocks < 0 ||
 	    (o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_BLOCKDIAG && o.precond != FEMGPU_PREC_ILU0) ||
 	    (o.precond == FEMGPU_PREC_BLOCKDIAG && o.scheme != FEMGPU_EBE) ||     /* setPreconditioner.c:54-73 */
 	    (o.precond == FEMGPU_PREC_ILU0 && o.scheme != FEMGPU_CSR) ||

@@ -307,6 +307,9 @@ typedef struct femgpu_ns_opts {
 	int scheme;          /* FEMGPU_EBE (9x9 element blocks) or FEMGPU_CSR    */
 	                     /* (csr_Initialization.c / csr_assembly.c, numbering */
 	                     /* of the node ids as given: reordering NOT)         */
+	int ilu_blocks;      /* CSR + ILU(0): 0 the whole matrix (the            */
+	                     /* reference's), P > 1 block ILU(0) over P row      */
+	                     /* blocks (as femgpu_transport_opts.ilu_blocks)     */
 } femgpu_ns_opts;
 
 void femgpu_ns_default_opts(femgpu_ns_opts *o);
