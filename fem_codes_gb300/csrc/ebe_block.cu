@@ -72,14 +72,30 @@ __global__ void k_ebemv_blk32(int neq, const int *__restrict__ ri_ptr, const int
 		if (I < neq) {
 			for (int t = ri_ptr[I]; t < ri_ptr[I + 1]; t++) {
 				int code = __ldg(&ri[t]), e = code / M, a = code - e * M;
-				const int *l = lm + (long long)e * M;
-				const float *row = A + (long long)e * M * M + a * M;
+				int l[M];
+				float r[M];
+				if constexpr (M % 4 == 0) {
+					// rows of M floats and lm blocks of M ints start on 16-byte
+					// boundaries: M/4 16-byte loads each
+					#pragma unroll
+					for (int v = 0; v < M / 4; v++) {
+						int4 li = __ldg(reinterpret_cast<const int4 *>(lm + (long long)e * M) + v);
+						float4 rv = __ldg(reinterpret_cast<const float4 *>(A + (long long)e * M * M + a * M) + v);
+						l[4 * v] = li.x; l[4 * v + 1] = li.y; l[4 * v + 2] = li.z; l[4 * v + 3] = li.w;
+						r[4 * v] = rv.x; r[4 * v + 1] = rv.y; r[4 * v + 2] = rv.z; r[4 * v + 3] = rv.w;
+					}
+				} else {
+					#pragma unroll
+					for (int b = 0; b < M; b++) {
+						l[b] = __ldg(&lm[(long long)e * M + b]);
+						r[b] = __ldg(&A[(long long)e * M * M + a * M + b]);
+					}
+				}
 				float s = 0.0f;
 				#pragma unroll
 				for (int b = 0; b < M; b++) {
-					int j = __ldg(&l[b]);
-					float p = (j == neq) ? 0.0f : __ldg(&P[j]);
-					s = fmaf(__ldg(&row[b]), p, s);
+					float p = (l[b] == neq) ? 0.0f : __ldg(&P[l[b]]);
+					s = fmaf(r[b], p, s);
 				}
 				q += (double)s;
 			}
