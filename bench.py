@@ -311,7 +311,7 @@ def run_ours(a):
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s"},
         "matvec": {"kernel": "k_csrmv64 (FP64 CSR)", "GB/s": spmv_gbs, "frac": spmv_gbs / peak,
-                   "us": kern["spmv_f64"] * 1e3,
+                   "us": kern["spmv_f64"] * 1e3, "bytes": spmv_bytes,
                    "f32_us": kern["spmv_f32"] * 1e3,
                    "f32_GB/s": (nnz * 8 + (neq + 1) * 4 + 2 * neq * 4) / (kern["spmv_f32"] * 1e-3) / 1e9},
         "breakdown_ms": {k: round(v, 4) for k, v in kern.items()},
@@ -327,6 +327,8 @@ def run_ours(a):
     T.close()
     if not a.no_learned:
         line["learned"] = learned_leg(m, p, a, s)
+    if rank == 0:
+        line["matvec_compare"] = matvec_compare(m, p, s, peak)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -373,6 +375,52 @@ def learned_leg(m, p, a, s, steps=1):
     finally:
         T.close()
         net.close()
+    return out
+
+
+def matvec_compare(m, p, s, peak, reps=10):
+    """The C2 comparison of the three storage schemes' products (csrmv.c,
+    ebemv.c, edemv.c, each bit-identical to the reference): one EBE and one
+    EDE context on the same mesh, one Build, then Q = A P timed with CUDA
+    events on stream s, L2 flushed between launches.  Algorithmic bytes:
+    CSR nnz*12 + (n+1)*4 + 2n*8; EBE Ne*(9*8 + 3*4) + incidence lists
+    n + 3*Ne codes + 2n*8; EDE (nedge+1)*32 + nedge*8 + incidence + 2n*8."""
+    import torch
+    import fem_codes_gb300 as fg
+    out = {}
+    vp = ctypes.c_void_p
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    for scheme in ("EBE", "EDE"):
+        T = fg.SSTransport.from_problem(m, p, scheme=scheme, precond="NOT", kmax=8, lmax=1, solver="FGMRES")
+        T.set_stream(s.cuda_stream)
+        T.build_dev()
+        x = torch.randn(T.neq + 1, dtype=torch.float64, device="cuda")
+        y = torch.zeros_like(x)
+        torch.cuda.synchronize()
+        for _ in range(2):
+            T._L.femgpu_transport_matvec_dev(T.handle, vp(x.data_ptr()), vp(y.data_ptr()))
+        tot = 0.0
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(s):
+                flush.zero_()
+                e0.record(s)
+                T._L.femgpu_transport_matvec_dev(T.handle, vp(x.data_ptr()), vp(y.data_ptr()))
+                e1.record(s)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        ms = tot / reps
+        n, ne = T.neq, m.nel
+        if scheme == "EBE":
+            alg = ne * (9 * 8 + 3 * 4) + (n + 1) * 4 + 3 * ne * 4 + 2 * n * 8
+            kern = "k_ebemv (3x3 FP64 element matrices, row gather)"
+        else:
+            alg = (T.nedge + 1) * 32 + T.nedge * 8 + (n + 1) * 4 + 2 * T.nedge * 4 + 2 * n * 8
+            kern = "k_edemv (4 FP64 values per edge, row gather)"
+        out[scheme] = {"kernel": kern, "us": 1e3 * ms, "GB/s": alg / (ms * 1e-3) / 1e9,
+                       "frac": alg / (ms * 1e-3) / 1e9 / peak, "bytes": alg}
+        T.close()
     return out
 
 
@@ -437,12 +485,18 @@ def read_traffic(kind):
     summary (profiles/), or None if not captured."""
     path = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
     try:
-        for line in open(path):
-            k, v = line.split(":", 1)
-            if k.strip() == kind:
-                return float(v.split()[0])
-    except Exception:
+        lines = open(path).read().splitlines()
+    except OSError:
         return None
+    for line in lines:
+        if line.startswith("#") or ":" not in line:
+            continue
+        k, v = line.split(":", 1)
+        if k.strip() == kind:
+            try:
+                return float(v.split()[0])
+            except (ValueError, IndexError):
+                return None
     return None
 
 
