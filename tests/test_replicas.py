@@ -64,3 +64,13 @@ def test_reference_arm_prints_on_rank0_only(monkeypatch):
     with redirect_stdout(buf):
         bench.run_reference(bench.parse(["--impl", "reference"]))
     assert buf.getvalue() == ""
+
+
+def test_bench_reads_committed_traffic():
+    """The roofline's DRAM traffic comes from the committed ncu summary."""
+    sys.path.insert(0, ROOT)
+    import bench
+    for kind in ("ilu_apply", "spmv", "euler_ebemv", "euler_ebemv32"):
+        v = bench.read_traffic(kind)
+        assert v is not None and v > 1e7, kind
+    assert bench.read_traffic("no such kernel") is None
