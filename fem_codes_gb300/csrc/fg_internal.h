@@ -40,6 +40,9 @@ typedef struct fg_sweep {
 	int *val_src;              /* [nval] CSR position (-1 zero, -2-r pivot)  */
 	int nchunk;                /* matrix blocks (block ILU(0); 1: global)    */
 	int *chunk_sb, *chunk_lev; /* [nchunk+1] first sub-block / level of each */
+	int rw;                    /* record layout width (0: ELL sub-blocks)    */
+	int bvo, cmax;             /* record layout: input slice offset in a
+	                            * stage, most rows of a sub-block            */
 } fg_sweep;
 
 typedef struct fg_ilu_sweeps {
@@ -175,7 +178,10 @@ int fg_precond(femgpu_transport *t, const double *p, double *z, const int *activ
  * (pgmres.c:58-184) / of flexible right-preconditioned GMRES (mixed 0: FP64,
  * 1: FP32 preconditioner, 2: FP32 preconditioner and operator). */
 int fg_kry_pgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X);
-int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int mixed);
+/* cycle: index of this restart cycle within the solve (picks the
+ * orthogonalisation, see gs_mode in linalg.cu) */
+int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int mixed,
+                        int cycle);
 /* CSR storage for M equations per element (M = 9: Navier-Stokes): pattern,
  * CSR_by_Element slots [M*M*nel], and the per-row assembly from element
  * matrices Ae [nel][M][M] (device arrays; pattern arrays allocated here). */

@@ -163,6 +163,7 @@ struct SweepArgs {
 	const int *active;
 	const int *chunk_sb;          // [P+1] first sub-block of each matrix block (NULL: one block)
 	const int *chunk_lev;         // [P+1] first level of each matrix block
+	int bvo, cmax;                // record layout: input slice offset, most rows of a sub-block
 };
 
 // CW consumer warps (warps 0..CW-1) and one producer warp (warp CW).
@@ -283,6 +284,150 @@ k_sweep(SweepArgs a, const T *__restrict__ in, T *out)
 	if (*vfailed && ctid == 0) {
 		fg_set_err(a.err, FEMGPU_E_TIMEOUT);
 		// let the producer stop, then wait (bounded) for the copies it issued
+		for (int i = 0; i < SW_WAIT_LIMIT && !*(volatile int *)&pdone; i++) __nanosleep(64);
+		int last = *(volatile int *)&issued;
+		for (int q = sb; q < last; q++) (void)mbar_wait(&full[q % D], (unsigned)((q / D) & 1));
+	}
+}
+
+// ------------------------------------------------ record layout (fixed width)
+// When every row of a sweep has at most 8 dependencies, each sub-block is a
+// 16-byte header {rows, sub-blocks of the level, level-order position of the
+// first row, far flag} followed by one record per row: W dependency codes and
+// the output slot (ints, padded to 16 bytes), then W factor values and, in
+// the backward sweep, the inverted pivot (padded to 16 bytes).  Rows with
+// fewer dependencies are padded with the zero ring slot and a zero value,
+// after their real terms, so the order of the real operations is unchanged.
+// A record is an odd number of 16-byte words (a quarter warp's 16-byte loads
+// then fall in distinct banks), and the input slice sits at the same offset
+// of every stage: a consumer thread issues all loads of its row before the
+// header arrives, which shortens the per-level chain of dependent loads.
+__host__ __device__ constexpr int rec_ib(int w) { return ((w + 1) * 4 + 15) & ~15; }
+__host__ __device__ constexpr int rec_vb(int w, bool upper, int ts) { return ((w + (upper ? 1 : 0)) * ts + 15) & ~15; }
+__host__ __device__ constexpr int rec_bytes(int w, bool upper, int ts)
+{
+	return (((rec_ib(w) + rec_vb(w, upper, ts)) / 16) & 1) ? rec_ib(w) + rec_vb(w, upper, ts)
+	                                                        : rec_ib(w) + rec_vb(w, upper, ts) + 16;
+}
+#define SW2_CW 16                     // consumer warps of the record-layout sweep (SW_SUB rows)
+
+template <typename T, bool UPPER, bool FMA, int W>
+__global__ void __launch_bounds__((SW2_CW + 1) * 32, 1)
+k_sweep_rec(SweepArgs a, const T *__restrict__ in, T *out)
+{
+	constexpr int CW = SW2_CW;
+	constexpr int IB = rec_ib(W), VB = rec_vb(W, UPPER, (int)sizeof(T)), RB = rec_bytes(W, UPPER, (int)sizeof(T));
+	static_assert(SW_SUB == CW * 32, "one row per consumer thread and sub-block");
+	if (a.active && !*a.active) return;
+	extern __shared__ __align__(128) unsigned char sm[];
+	const unsigned ring_b = (unsigned)al16((SW_RING + 1) * sizeof(T));
+	T *ring = (T *)sm;
+	unsigned long long *full = (unsigned long long *)(sm + ring_b);
+	unsigned long long *empty = full + SW_MAXD;
+	unsigned char *stages = sm + ((ring_b + SW_BAR_BYTES + 127) & ~127u);
+	__shared__ int failed, issued, pdone;
+	volatile int *vfailed = &failed;
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, D = a.D;
+	const unsigned sbytes = (unsigned)a.stage_bytes;
+	const int sb0 = a.chunk_sb ? a.chunk_sb[blockIdx.x] : 0, sb1 = a.chunk_sb ? a.chunk_sb[blockIdx.x + 1] : a.nsb;
+	const int l0 = a.chunk_lev ? a.chunk_lev[blockIdx.x] : 0, l1 = a.chunk_lev ? a.chunk_lev[blockIdx.x + 1] : a.nlev;
+
+	if (tid == 0) {
+		failed = 0; issued = 0; pdone = 0;
+		ring[SW_RING] = T(0);
+		for (int s = 0; s < D; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+		fence_mbar_init();
+	}
+	__syncthreads();
+
+	if (warp == CW) {                                     // ---- producer warp
+		bool stop = false;
+		int s = 0;
+		unsigned ph = 0;
+		for (int base = sb0; base < sb1 && !stop; base += 32) {
+			int i = base + lane;
+			long long b0 = 0, b1 = 0;
+			int p0 = 0, vb = 0;
+			if (i < sb1) { b0 = a.blk_off[i]; b1 = a.blk_off[i + 1]; p0 = a.sb_in[i]; vb = a.sb_inb[i]; }
+			for (int j = 0; j < 32 && base + j < sb1; j++) {
+				long long B0 = __shfl_sync(0xffffffffu, b0, j), B1 = __shfl_sync(0xffffffffu, b1, j);
+				int P0 = __shfl_sync(0xffffffffu, p0, j), VB = __shfl_sync(0xffffffffu, vb, j);
+				int sb = base + j - sb0;
+				int go = 1;
+				if (lane == 0) {
+					if (sb >= D && !mbar_wait_or_fail(&empty[s], ph, vfailed)) go = 0;
+					if (*vfailed) go = 0;
+					if (go) {
+						unsigned bb = (unsigned)(B1 - B0);
+						unsigned char *dst = stages + (unsigned)s * sbytes;
+						fence_proxy_async();
+						mbar_expect_tx(&full[s], bb + (unsigned)VB);
+						bulk_g2s(dst, a.prog + B0, bb, &full[s]);
+						if (VB) bulk_g2s(dst + a.bvo, in + P0, (unsigned)VB, &full[s]);
+						*(volatile int *)&issued = sb + 1;
+					}
+				}
+				go = __shfl_sync(0xffffffffu, go, 0);
+				if (!go) { stop = true; break; }
+				if (++s == D) { s = 0; if (sb >= D) ph ^= 1u; else if (sb == D - 1) ph = 0; }
+			}
+		}
+		if (lane == 0) *(volatile int *)&pdone = 1;
+		return;
+	}
+
+	const int ctid = tid;                                 // ---- consumer warps
+	// the record this thread reads in every stage (clamped into the staged rows;
+	// rows past a sub-block's count are read but not used)
+	const unsigned roff = 16u + (unsigned)(ctid < a.cmax ? ctid : a.cmax - 1) * RB;
+	const unsigned boff = (unsigned)a.bvo + (unsigned)(ctid < a.cmax ? ctid : a.cmax - 1) * sizeof(T);
+	int sb = 0, s = 0;
+	unsigned ph = 0;
+	for (int l = l0; l < l1; l++) {
+		int nsub = 1, j = 0, s0 = s;
+		for (; j < nsub; j++) {
+			bool ok = mbar_wait_or_fail(&full[s], ph, vfailed);
+			if (!ok) { *vfailed = 1; break; }
+			const unsigned char *st = stages + (unsigned)s * sbytes;
+			union { int4 q[IB / 16]; int i[IB / 4]; } ci;
+			union { int4 q[VB / 16]; T v[VB / sizeof(T)]; } cv;
+#pragma unroll
+			for (int q = 0; q < IB / 16; q++) ci.q[q] = ((const int4 *)(st + roff))[q];
+#pragma unroll
+			for (int q = 0; q < VB / 16; q++) cv.q[q] = ((const int4 *)(st + roff + IB))[q];
+			T x = *(const T *)(st + boff);
+			const int4 h = *(const int4 *)st;         // rows, sub-blocks, start, far flag
+			if (j == 0) nsub = h.y;
+			T d[W];
+#pragma unroll
+			for (int k = 0; k < W; k++) {
+				unsigned c = (unsigned)ci.i[k] & ~SW_NEAR;
+				d[k] = ring[c < SW_RING ? c : SW_RING];
+			}
+			if (ctid < h.x) {
+				if (h.w) {
+#pragma unroll
+					for (int k = 0; k < W; k++)
+						if (!((unsigned)ci.i[k] & SW_NEAR)) d[k] = __ldcg(&out[ci.i[k]]);
+				}
+#pragma unroll
+				for (int k = 0; k < W; k++) x = fmsub<T, FMA>(x, d[k], cv.v[k]);
+				if (UPPER) x = mul(x, cv.v[W]);
+				ring[(h.z + ctid) & (SW_RING - 1)] = x;
+				out[ci.i[W]] = x;
+			}
+			if (++s == D) { s = 0; ph ^= 1u; }
+		}
+		consumer_sync<CW>();
+		if (ctid == 0) {
+			int q = s0;
+			for (int c = 0; c < j; c++) { mbar_arrive(&empty[q]); if (++q == D) q = 0; }
+		}
+		sb += j;
+		if (*vfailed) break;
+	}
+	if (*vfailed && ctid == 0) {
+		fg_set_err(a.err, FEMGPU_E_TIMEOUT);
 		for (int i = 0; i < SW_WAIT_LIMIT && !*(volatile int *)&pdone; i++) __nanosleep(64);
 		int last = *(volatile int *)&issued;
 		for (int q = sb; q < last; q++) (void)mbar_wait(&full[q % D], (unsigned)((q / D) & 1));
@@ -593,6 +738,17 @@ static int up_vec(X **d, const std::vector<X> &h)
 	return 0;
 }
 
+// Width of the record layout for a sweep whose widest row has w dependencies
+// (0: the ELL sub-block layout, used above 8 or when FEMGPU_SWEEP_LAYOUT=ell).
+static int rec_width(int w)
+{
+	const char *e = getenv("FEMGPU_SWEEP_LAYOUT");
+	if (e && !strcmp(e, "ell")) return 0;
+	static const int widths[] = { 2, 3, 4, 6, 8 };
+	for (int v : widths) if (w <= v) return v;
+	return 0;
+}
+
 // One sweep program.  Forward (lower): L part, outputs to the backward
 // sweep's padded level order (target = the U levels' ppos).  Backward: U part
 // and pivots, outputs in natural order.
@@ -621,17 +777,24 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 		}
 	}
 	int nsb = (int)subs.size();
+	int wmax = 0, cmax = 1;
+	for (const Sub &S : subs) { wmax = std::max(wmax, S.w); cmax = std::max(cmax, S.c); }
+	const int rw = rec_width(wmax);                                   // 0: ELL sub-blocks
+	const long long RB = rw ? rec_bytes(rw, UPPER, (int)tsize) : 0;
 	std::vector<long long> off(nsb + 1, 0);
 	std::vector<int> sb_in(nsb), sb_inb(nsb);
-	long long maxblk = 0;
+	long long maxblk = 0, bvo = 0, maxin = 0;
 	for (int i = 0; i < nsb; i++) {
 		int cp = (subs[i].c + 3) & ~3;
-		long long bb = blk_bytes<T, UPPER>(subs[i].w, cp);
+		long long bb = rw ? 16 + (long long)subs[i].c * RB : blk_bytes<T, UPPER>(subs[i].w, cp);
 		off[i + 1] = off[i] + bb;
 		sb_in[i] = H.pstart[subs[i].l] + subs[i].j0;                 // j0 is a multiple of 4
 		sb_inb[i] = (int)al16((long long)cp * tsize);
 		maxblk = std::max(maxblk, bb + sb_inb[i]);
+		bvo = std::max(bvo, bb);
+		maxin = std::max(maxin, (long long)sb_inb[i]);
 	}
+	if (rw) maxblk = bvo + maxin;                                     // input slice at a fixed offset
 	std::vector<unsigned char> prog((size_t)off[nsb] + 16, 0);
 	std::vector<long long> val_off;
 	std::vector<int> val_src;
@@ -650,6 +813,29 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 				int col = JA[q];
 				if ((lower ? col < r : col > r) && B.same(r, col) && end - H.pos[col] > SW_RING) hasfar = 1;
 			}
+		}
+		if (rw) {
+			const int hh[4] = { c, nsub, start, hasfar };
+			memcpy(b, hh, sizeof hh);
+			for (int j = 0; j < c; j++) {
+				int *ri = (int *)(b + 16 + (size_t)j * RB), r = H.rows[start + j], k = 0;
+				long long vo = off[i] + 16 + (long long)j * RB + rec_ib(rw);
+				for (int q = 0; q < rw; q++) ri[q] = (int)(SW_NEAR | SW_RING);   // the zero slot
+				ri[rw] = lower ? target->ppos[r] : r;
+				for (int q = IA[r]; q < IA[r + 1]; q++) {
+					int col = JA[q];
+					if ((lower ? !(col < r) : !(col > r)) || !B.same(r, col)) continue;
+					int p = H.pos[col];
+					ri[k] = (int)((end - p <= SW_RING) ? (SW_NEAR | (unsigned)(p & (SW_RING - 1)))
+					                                   : (unsigned)(lower ? target->ppos[col] : col));
+					val_off.push_back(vo + k * tsize);
+					val_src.push_back(q);
+					k++;
+				}
+				for (; k < rw; k++) { val_off.push_back(vo + k * tsize); val_src.push_back(-1); }
+				if (!lower) { val_off.push_back(vo + rw * tsize); val_src.push_back(-2 - r); }
+			}
+			continue;
 		}
 		LevHdr h = { c, w, start, cp, nsub, hasfar, (int)al16(SW_HDR + (long long)(w + 1) * cp * 4),
 		             (int)blk_bytes<T, UPPER>(w, cp) };
@@ -688,6 +874,9 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 		csb[b] = (int)i;
 	}
 	sw.nchunk = (int)clev.size() - 1;
+	sw.rw = rw;
+	sw.bvo = (int)bvo;
+	sw.cmax = cmax;
 	sw.nlev = nlev;
 	sw.nsb = nsb;
 	sw.bytes = off[nsb];
@@ -840,11 +1029,21 @@ static int factor_cluster_size(int P)
 #define SW_SET_CW(CW) SW_SET(double, false, CW, false); SW_SET(double, true, CW, false); \
 	SW_SET(double, false, CW, true); SW_SET(double, true, CW, true); \
 	SW_SET(float, false, CW, false); SW_SET(float, true, CW, false)
+#define SR_SET(T, U, F, W) FG_TRY(cudaFuncSetAttribute(k_sweep_rec<T, U, F, W>, \
+	cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP))
+#define SR_SET_W(W) SR_SET(double, false, false, W); SR_SET(double, true, false, W); \
+	SR_SET(double, false, true, W); SR_SET(double, true, true, W); \
+	SR_SET(float, false, false, W); SR_SET(float, true, false, W)
 static int sweep_attrs(void)
 {
 	SW_SET_CW(4);
 	SW_SET_CW(8);
 	SW_SET_CW(16);
+	SR_SET_W(2);
+	SR_SET_W(3);
+	SR_SET_W(4);
+	SR_SET_W(6);
+	SR_SET_W(8);
 	return 0;
 }
 
@@ -862,9 +1061,28 @@ static int sweep_cw(void)
 
 // fma: fused multiply-subtract in the FP64 sweeps (the FGMRES solves); the
 // separately rounded form reproduces the reference bit for bit.
-template <typename T, bool UPPER>
-static void launch_sweep(const SweepArgs &a, int grid, int bytes, cudaStream_t s, const T *in, T *out, bool fma)
+template <typename T, bool UPPER, bool FMA>
+static void launch_rec(const SweepArgs &a, int rw, int grid, int bytes, cudaStream_t s, const T *in, T *out)
 {
+	const int nt = (SW2_CW + 1) * 32;
+	switch (rw) {
+	case 2: k_sweep_rec<T, UPPER, FMA, 2><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 3: k_sweep_rec<T, UPPER, FMA, 3><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 4: k_sweep_rec<T, UPPER, FMA, 4><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 6: k_sweep_rec<T, UPPER, FMA, 6><<<grid, nt, bytes, s>>>(a, in, out); break;
+	default: k_sweep_rec<T, UPPER, FMA, 8><<<grid, nt, bytes, s>>>(a, in, out); break;
+	}
+}
+
+template <typename T, bool UPPER>
+static void launch_sweep(const SweepArgs &a, int rw, int grid, int bytes, cudaStream_t s, const T *in, T *out,
+                         bool fma)
+{
+	if (rw) {
+		if (fma && sizeof(T) == 8) launch_rec<T, UPPER, true>(a, rw, grid, bytes, s, in, out);
+		else launch_rec<T, UPPER, false>(a, rw, grid, bytes, s, in, out);
+		return;
+	}
 	int cw = sweep_cw();
 	if (fma && sizeof(T) == 8) {
 		if (cw == 4) k_sweep<T, UPPER, 4, true><<<grid, 160, bytes, s>>>(a, in, out);
@@ -966,14 +1184,14 @@ static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, 
 	if (bytes < 0) return bytes;
 	a.prog = lo.prog; a.blk_off = lo.blk_off; a.sb_in = lo.sb_in; a.sb_inb = lo.sb_inb;
 	a.nlev = lo.nlev; a.nsb = lo.nsb; a.D = D; a.stage_bytes = sb;
-	a.chunk_sb = lo.chunk_sb; a.chunk_lev = lo.chunk_lev;
-	launch_sweep<T, false>(a, lo.nchunk, bytes, s, bl, y, fma);
+	a.chunk_sb = lo.chunk_sb; a.chunk_lev = lo.chunk_lev; a.bvo = lo.bvo; a.cmax = lo.cmax;
+	launch_sweep<T, false>(a, lo.rw, lo.nchunk, bytes, s, bl, y, fma);
 	bytes = sweep_smem(up, sizeof(T), &D, &sb);
 	if (bytes < 0) return bytes;
 	a.prog = up.prog; a.blk_off = up.blk_off; a.sb_in = up.sb_in; a.sb_inb = up.sb_inb;
 	a.nlev = up.nlev; a.nsb = up.nsb; a.D = D; a.stage_bytes = sb;
-	a.chunk_sb = up.chunk_sb; a.chunk_lev = up.chunk_lev;
-	launch_sweep<T, true>(a, up.nchunk, bytes, s, y, (T *)z, fma);
+	a.chunk_sb = up.chunk_sb; a.chunk_lev = up.chunk_lev; a.bvo = up.bvo; a.cmax = up.cmax;
+	launch_sweep<T, true>(a, up.rw, up.nchunk, bytes, s, y, (T *)z, fma);
 	return (int)cudaGetLastError();
 }
 

@@ -391,17 +391,26 @@ __global__ void __launch_bounds__(RED_TPB) k_cgs_update(const double *V, size_t 
 	if (last_block_total(part, partials, &st->ticket, &tot, sh)) *Hn = sqrt(tot);
 }
 
-// Orthogonalisation of Arnoldi step i: 0 MGS (one fused kernel per basis
-// vector), 1 CGS, 2 CGS with one re-orthogonalisation (FEMGPU_GS selects;
-// default 1).
-static int gs_mode(void)
+// Orthogonalisation of the Arnoldi steps of restart cycle `cycle': 0 MGS
+// (one fused kernel per basis vector), 1 CGS, 2 CGS with one
+// re-orthogonalisation (CGS2), 3 CGS in a solve's first cycle and CGS2 in
+// every later one (FEMGPU_GS selects; default 3).  Single-pass CGS is the
+// fastest and, within one cycle, converges like MGS on the transport solves
+// (8-block ILU(0), FGMRES(80): 56-59 iterations either way); across restarts
+// it loses orthogonality (global ILU(0), FGMRES(50) at 2048x1024: 166-216
+// iterations against 46-51 for MGS and 45-56 for CGS2).  Re-orthogonalising
+// only where the first pass lost more than half of ||w||^2 (the
+// Daniel-Gragg-Kaufman-Stewart test) saved nothing: near convergence nearly
+// every step fails that test.
+static int gs_mode(int cycle)
 {
 	static int g = -1;
 	if (g < 0) {
 		const char *e = getenv("FEMGPU_GS");
-		int v = e ? atoi(e) : 1;
-		g = (v >= 0 && v <= 2) ? v : 1;
+		int v = e ? atoi(e) : 3;
+		g = (v >= 0 && v <= 3) ? v : 3;
 	}
+	if (g == 3) return cycle == 0 ? 1 : 2;
 	return g;
 }
 
@@ -525,7 +534,7 @@ extern "C" int fg_kry_pgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 // Arnoldi residual is the unpreconditioned one.  mixed: 0 FP64 throughout,
 // 1 FP32 preconditioner (FP64 operator), 2 FP32 preconditioner and operator.
 extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X,
-                                   int mixed)
+                                   int mixed, int cycle)
 {
 	cudaStream_t s = k->stream;
 	int n = k->n, kmax = k->kmax, ldh = kmax + 1, G = k->nblk, rc;
@@ -552,7 +561,7 @@ extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 			}
 			if ((rc = op->matvec(op->ctx, z, w, active))) return rc;
 		}
-		const int gs = gs_mode();
+		const int gs = gs_mode(cycle);
 		if (gs == 0) {
 			for (int j = 0; j <= i + 1; j++)
 				k_mgs<<<G, RED_TPB, 0, s>>>(V, ldv, n, i, j, k->H, ldh, k->partials, k->st);
@@ -646,7 +655,7 @@ extern "C" int fg_fgmres_cycle(femgpu_transport *t, const double *B, double *X, 
 	fg_krylov k;
 	fg_linop op;
 	fg_transport_krylov(t, &k, &op);
-	return fg_kry_fgmres_cycle(&k, &op, B, X, mixed);
+	return fg_kry_fgmres_cycle(&k, &op, B, X, mixed, 0);
 }
 
 // out = a . b (deterministic), device scalar.

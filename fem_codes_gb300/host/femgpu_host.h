@@ -43,9 +43,11 @@ void fgh_kry_free(struct fg_krylov *k);
 int fgh_kry_cycles(const struct fg_krylov *k, const struct fg_linop *op, const double *B, double *X,
                    int kind, double eps, int lmax, int *iters);
 /* The pieces of fgh_kry_cycles: reset the status for a solve to eps, then
- * run one restart cycle and read the status back (k->st_host). */
+ * run one restart cycle (the solve's cycle-th) and read the status back
+ * (k->st_host). */
 int fgh_kry_begin(const struct fg_krylov *k, double eps);
-int fgh_kry_cycle(const struct fg_krylov *k, const struct fg_linop *op, const double *B, double *X, int kind);
+int fgh_kry_cycle(const struct fg_krylov *k, const struct fg_linop *op, const double *B, double *X, int kind,
+                  int cycle);
 /* ||B||^2 on the device, returned to the host (synchronises the stream). */
 int fgh_kry_dot_host(const struct fg_krylov *k, const double *a, const double *b, int n, double *out);
 

@@ -74,10 +74,10 @@ int fgh_kry_begin(const fg_krylov *k, double eps)
 	return 0;
 }
 
-int fgh_kry_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int kind)
+int fgh_kry_cycle(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int kind, int cycle)
 {
 	if (kind < 0) KR(fg_kry_pgmres_cycle(k, op, B, X));
-	else KR(fg_kry_fgmres_cycle(k, op, B, X, kind));
+	else KR(fg_kry_fgmres_cycle(k, op, B, X, kind, cycle));
 	return sync_status(k);
 }
 
@@ -88,7 +88,7 @@ int fgh_kry_cycles(const fg_krylov *k, const fg_linop *op, const double *B, doub
 	if ((rc = fgh_kry_begin(k, eps))) return rc;
 	for (;;) {
 		do {
-			if ((rc = fgh_kry_cycle(k, op, B, X, kind))) return rc;
+			if ((rc = fgh_kry_cycle(k, op, B, X, kind, l))) return rc;
 			l++;
 		} while (k->st_host->rho > eps && l < lmax);
 		/* FGMRES stops on the unpreconditioned residual: confirm the

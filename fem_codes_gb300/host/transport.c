@@ -538,18 +538,19 @@ static int learned_cycles(femgpu_transport *t, const double *B, double *X, doubl
 {
 	fg_krylov k;
 	fg_linop op;
-	int l = 0, rc, done = 0;
+	int l = 0, c = 0, rc, done = 0;            /* c: cycles since the solve (re)started */
 	double prev = rho0;
 	fg_transport_krylov(t, &k, &op);
 	if ((rc = fgh_kry_begin(&k, eps))) return rc;
 	do {
-		rc = fgh_kry_cycle(&k, &op, B, X, 0);
+		rc = fgh_kry_cycle(&k, &op, B, X, 0, c++);
 		l++;
 		if (rc == FEMGPU_E_BREAKDOWN && !t->fell_back) {
 			done += k.st_host->total;
 			CK(cudaMemsetAsync(X, 0, sizeof(double) * (size_t)t->neq, t->stream));
 			if ((rc = fall_back(t))) return rc;
 			prev = rho0;
+			c = 0;
 			if ((rc = fgh_kry_begin(&k, eps))) return rc;
 			continue;
 		}
