@@ -749,6 +749,17 @@ static int rec_width(int w)
 	return 0;
 }
 
+// Dependencies at most this many level-order positions before the end of
+// their row's level are read from the shared-memory ring, older ones from
+// global memory.  FEMGPU_SWEEP_NEAR lowers the limit (1..SW_RING) so that
+// small systems exercise the global-memory path too.
+static int sweep_near_limit(void)
+{
+	const char *e = getenv("FEMGPU_SWEEP_NEAR");
+	int v = e ? atoi(e) : SW_RING;
+	return (v >= 1 && v <= SW_RING) ? v : SW_RING;
+}
+
 // One sweep program.  Forward (lower): L part, outputs to the backward
 // sweep's padded level order (target = the U levels' ppos).  Backward: U part
 // and pivots, outputs in natural order.
@@ -758,6 +769,7 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 {
 	const bool lower = !UPPER;
 	const long long tsize = sizeof(T);
+	const int near_lim = sweep_near_limit();
 	int nlev = H.nlev;
 	// sub-blocks: (level, first row within the level, rows, width)
 	struct Sub { int l, j0, c, w; };
@@ -811,7 +823,7 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 			int r = H.rows[start + j];
 			for (int q = IA[r]; q < IA[r + 1]; q++) {
 				int col = JA[q];
-				if ((lower ? col < r : col > r) && B.same(r, col) && end - H.pos[col] > SW_RING) hasfar = 1;
+				if ((lower ? col < r : col > r) && B.same(r, col) && end - H.pos[col] > near_lim) hasfar = 1;
 			}
 		}
 		if (rw) {
@@ -826,7 +838,7 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 					int col = JA[q];
 					if ((lower ? !(col < r) : !(col > r)) || !B.same(r, col)) continue;
 					int p = H.pos[col];
-					ri[k] = (int)((end - p <= SW_RING) ? (SW_NEAR | (unsigned)(p & (SW_RING - 1)))
+					ri[k] = (int)((end - p <= near_lim) ? (SW_NEAR | (unsigned)(p & (SW_RING - 1)))
 					                                   : (unsigned)(lower ? target->ppos[col] : col));
 					val_off.push_back(vo + k * tsize);
 					val_src.push_back(q);
@@ -850,7 +862,7 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 				int col = JA[q];
 				if ((lower ? !(col < r) : !(col > r)) || !B.same(r, col)) continue;
 				int p = H.pos[col];
-				unsigned code = (end - p <= SW_RING) ? (SW_NEAR | (unsigned)(p & (SW_RING - 1)))
+				unsigned code = (end - p <= near_lim) ? (SW_NEAR | (unsigned)(p & (SW_RING - 1)))
 				                                     : (unsigned)(lower ? target->ppos[col] : col);
 				dep[(size_t)k * cp + j] = (int)code;
 				val_off.push_back(off[i] + voff + ((long long)k * cp + j) * tsize);

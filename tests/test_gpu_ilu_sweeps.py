@@ -1,0 +1,97 @@
+"""GPU parity of the ILU(0) triangular sweeps (ILUp_precond.c:26-46) in both
+program layouts -- fixed-width row records and ELL sub-blocks -- against the
+oracle's ILU(0) (ILUp_precond_setup.c:66-167 / ILUp_precond.c:26-46 restated
+in oracle/), on systems that reach the sweep's less common paths:
+
+* levels wider than one 512-row sub-block (a 600x600 mesh in its natural
+  numbering has levels of up to ~600 rows), so a level spans two staged
+  sub-blocks;
+* dependencies older than the shared-memory ring, which the sweep reads back
+  from global memory; FEMGPU_SWEEP_NEAR lowers the ring's reach when the
+  programs are built, so a small system takes that path for most rows.
+
+Bar: the separately rounded sweeps (pgmres) are bit-identical to the oracle;
+the fused sweeps (FGMRES) are bit-identical across layouts and ring reaches
+and within FMA_TOL of the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from fem_codes_gb300.mesh import skew_problem, structured_mesh
+
+pytestmark = pytest.mark.gpu
+
+FMA_TOL = 1e-12    # fused multiply-subtract vs separately rounded sweeps (relative max-norm)
+
+
+def apply_ilu(m, p, reorder, solver, layout=None, near=None, blocks=0):
+    """Factor and apply the device ILU(0) of the transport system once; the
+    layout and ring reach are fixed when the sweep programs are built."""
+    import fem_codes_gb300 as fg
+    env = {"FEMGPU_SWEEP_LAYOUT": layout, "FEMGPU_SWEEP_NEAR": near}
+    saved = {k: os.environ.get(k) for k in env}
+    try:
+        for k, v in env.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = str(v)
+        with fg.SSTransport.from_problem(m, p, scheme="CSR", reorder=reorder, precond="ILU0", solver=solver,
+                                         kmax=30, ilu_blocks=blocks) as T:
+            _, A = T.Build(u=np.zeros(T.neq + 1), want_matrix=True)
+            T.precond_setup(1)
+            pat = T.pattern()
+            x = np.zeros(T.neq + 1)
+            x[:-1] = np.random.default_rng(11).standard_normal(T.neq)
+            return T.precond(x)[:-1], x, pat, A
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def oracle_apply(pat, A, x):
+    IA, JA = np.asarray(pat["IA"]), np.asarray(pat["JA"])
+    LU, Dinv = pyoracle.ilu0(IA, JA, A)
+    n = IA.size - 1
+    return pyoracle.ilu0_apply(IA, JA, LU, Dinv, x)[:n]
+
+
+@pytest.mark.parametrize("layout", ["rec", "ell"])
+def test_levels_wider_than_a_sub_block(gpu_lib, layout):
+    m = structured_mesh(600, 600, perturb=0.2, seed=1234)
+    p = skew_problem(m)
+    z, x, pat, A = apply_ilu(m, p, "NOT", "GMRES", layout=layout)
+    assert np.array_equal(z, oracle_apply(pat, A, x))
+    zf, _, _, _ = apply_ilu(m, p, "NOT", "FGMRES", layout=layout)
+    zr, _, _, _ = apply_ilu(m, p, "NOT", "FGMRES", layout="rec" if layout == "ell" else "ell")
+    assert np.array_equal(zf, zr)
+    assert np.max(np.abs(zf - z)) <= FMA_TOL * np.max(np.abs(z))
+
+
+@pytest.mark.parametrize("layout", ["rec", "ell"])
+@pytest.mark.parametrize("reorder", ["SYMRCM", "NOT"])
+def test_dependencies_older_than_the_ring(gpu_lib, layout, reorder):
+    m = structured_mesh(60, 40, perturb=0.2, seed=7)
+    p = skew_problem(m)
+    z, x, pat, A = apply_ilu(m, p, reorder, "GMRES", layout=layout, near=8)
+    assert np.array_equal(z, oracle_apply(pat, A, x))
+    zf, _, _, _ = apply_ilu(m, p, reorder, "FGMRES", layout=layout, near=8)
+    zd, _, _, _ = apply_ilu(m, p, reorder, "FGMRES", layout=layout)
+    assert np.array_equal(zf, zd)
+
+
+@pytest.mark.parametrize("near", [None, 8])
+def test_block_ilu_layouts_agree(gpu_lib, near):
+    """Block ILU(0) (couplings between the 4 blocks dropped) has no oracle
+    counterpart: both layouts and both ring reaches give the same bits."""
+    m = structured_mesh(64, 48, perturb=0.2, seed=3)
+    p = skew_problem(m)
+    ref, _, _, _ = apply_ilu(m, p, "SYMRCM", "FGMRES", layout="ell", blocks=4)
+    z, _, _, _ = apply_ilu(m, p, "SYMRCM", "FGMRES", layout="rec", near=near, blocks=4)
+    assert np.array_equal(z, ref)
+    assert np.all(np.isfinite(z))
