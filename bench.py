@@ -55,7 +55,7 @@ def parse(argv=None):
     ap.add_argument("--precond", default="ILU0")
     ap.add_argument("--reorder", default="SYMRCM", choices=["NOT", "SYMRCM"])
     ap.add_argument("--kmax", type=int, default=80)
-    ap.add_argument("--ilu-blocks", type=int, default=8,
+    ap.add_argument("--ilu-blocks", type=int, default=16,
                     help="0: ILU(0) of the whole matrix; P > 1: block ILU(0) over P row blocks")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="transport", choices=["transport", "euler", "ns"])

@@ -99,6 +99,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
     for name, args in {
         "femgpu_transport_set_stream": [_vp, _vp],
         "femgpu_transport_info": [_vp, _vp],
+        "femgpu_transport_ilu_blocks": [_vp, _vp, ctypes.c_int],
         "femgpu_transport_get_pattern": [_vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_transport_build": [_vp, _vp, _vp, _vp],
         "femgpu_transport_precond_setup": [_vp, ctypes.c_int, _vp],
@@ -393,6 +394,18 @@ class SSTransport:
         if n < 0:
             raise FemGpuError(n, "Process")
         return uh[:n], its[:n]
+
+    def ilu_blocks(self):
+        """First row of each block ILU(0) run plus the row count (a 2-entry
+        array for global ILU(0))."""
+        P = self._L.femgpu_transport_ilu_blocks(self._h, None, 0)
+        if P < 0:
+            raise FemGpuError(P, "ilu_blocks")
+        first = np.zeros(P + 1, np.int32)
+        rc = self._L.femgpu_transport_ilu_blocks(self._h, _ptr(first), P + 1)
+        if rc < 0:
+            raise FemGpuError(rc, "ilu_blocks")
+        return first
 
     def true_residual(self):
         r = ctypes.c_double(0.0)

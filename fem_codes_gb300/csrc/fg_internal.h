@@ -55,6 +55,8 @@ typedef struct fg_ilu_sweeps {
 	 * [nops, operand addresses..., per group (q, cnt, dst...)] */
 	int *fac2_hdr, *fac2;
 	int fac2_ok;
+	int nblocks;               /* matrix blocks (1: global ILU(0))           */
+	int *block_first;          /* host [nblocks+1] first row of each block   */
 } fg_ilu_sweeps;
 
 typedef struct fg_ilu {

@@ -672,12 +672,101 @@ struct HostLevels {
 	std::vector<int> start, pstart, rows, pos, ppos;   // pos/ppos indexed by row
 };
 
-// Matrix block of a row: P contiguous blocks of the numbering (P = 0: one).
+// Matrix block of a row: P contiguous runs of the numbering (P = 0: one).
 struct Blocks {
-	int P, n;
-	int of(int r) const { return P ? (int)((long long)r * P / n) : 0; }
-	bool same(int r, int c) const { return !P || of(r) == of(c); }
+	int P = 0;
+	std::vector<int> id;                                  // block of each row (P > 0)
+	int of(int r) const { return P ? id[r] : 0; }
+	bool same(int r, int c) const { return !P || id[r] == id[c]; }
 };
+
+// Block ILU(0) cuts: P contiguous runs of the numbering; couplings between
+// runs are dropped.  A sweep costs one barrier per level and its P thread
+// blocks run side by side, so the deepest run (levels counted with the
+// couplings dropped) sets its time, while where the cuts fall sets how many
+// FGMRES iterations the weaker preconditioner costs.  After SYMRCM every front
+// is a dependency chain about as long as the front is wide, so equal row
+// counts leave the middle runs deepest.  FEMGPU_ILU_BLOCK_CUT selects:
+//   levels (default)  run b starts at the first row where the running maximum
+//                     of the full factor's forward level reaches
+//                     ceil(b * levels / P): equal spans of fronts;
+//   depth             the smallest budget T for which the greedy scan (open a
+//                     new run at the row whose level would reach T) makes at
+//                     most P runs (bisection), the runs with the most rows then
+//                     halved until there are P: the shallowest deepest run;
+//   rows              row r in run floor(r * P / n).
+// Measured at 2048x1024 with FGMRES(80) to 1e-8 (ms per Picard step, ILU
+// application, iterations): rows P=8 148 / 1.90 ms / 56-59; levels P=16
+// 125 / 1.47 ms / 57-59; depth P=16 136 / 1.38 ms / 65-67, P=12 134 / 1.50
+// ms / 60-63.
+static std::vector<int> greedy_runs(const int *IA, const int *JA, int n, int T, std::vector<int> &lev)
+{
+	std::vector<int> first(1, 0);
+	int start = 0;
+	for (int i = 0; i < n; i++) {
+		int L = 0;
+		for (int k = IA[i]; k < IA[i + 1] && JA[k] < i; k++)
+			if (JA[k] >= start) L = std::max(L, lev[JA[k]] + 1);
+		if (L >= T) { start = i; L = 0; first.push_back(i); }
+		lev[i] = L;
+	}
+	first.push_back(n);
+	return first;
+}
+
+static Blocks make_blocks(const int *IA, const int *JA, int n, int P, std::vector<int> *first_out)
+{
+	Blocks B;
+	if (P <= 1 || n <= 1) { if (first_out) *first_out = { 0, n }; return B; }
+	P = std::min(P, n);
+	std::vector<int> cut;
+	const char *e = getenv("FEMGPU_ILU_BLOCK_CUT");
+	if (e && !strcmp(e, "rows")) {
+		cut.assign(P + 1, n);
+		for (int b = 0; b < P; b++) cut[b] = (int)(((long long)b * n + P - 1) / P);
+	} else if (!e || strcmp(e, "depth")) {
+		std::vector<int> lev(n, 0), run(n, 0);
+		int top = 0;
+		for (int i = 0; i < n; i++) {
+			int L = 0;
+			for (int k = IA[i]; k < IA[i + 1] && JA[k] < i; k++) L = std::max(L, lev[JA[k]] + 1);
+			lev[i] = L;
+			top = std::max(top, L);
+			run[i] = top;
+		}
+		const long long nl = (long long)top + 1;
+		cut.assign(P + 1, n);
+		cut[0] = 0;
+		for (int b = 1, i = 0; b < P; b++) {
+			const long long fl = (nl * b + P - 1) / P;
+			while (i < n && run[i] < fl) i++;
+			cut[b] = i;
+		}
+		for (int b = 1; b < P; b++) cut[b] = std::max(cut[b], cut[b - 1] + 1);     // no empty run
+		for (int b = P - 1; b >= 1; b--) cut[b] = std::min(cut[b], cut[b + 1] - 1);
+	} else {
+		std::vector<int> lev(n, 0);
+		int lo = 1, hi = n;                       // T = n always gives one run
+		while (lo < hi) {
+			int T = lo + (hi - lo) / 2;
+			if ((int)greedy_runs(IA, JA, n, T, lev).size() - 1 <= P) hi = T;
+			else lo = T + 1;
+		}
+		cut = greedy_runs(IA, JA, n, lo, lev);
+		while ((int)cut.size() - 1 < P) {          // halve the run with the most rows
+			int bb = 0;
+			for (int b = 1; b + 1 < (int)cut.size(); b++)
+				if (cut[b + 1] - cut[b] > cut[bb + 1] - cut[bb]) bb = b;
+			cut.insert(cut.begin() + bb + 1, cut[bb] + (cut[bb + 1] - cut[bb]) / 2);
+		}
+	}
+	B.P = P;
+	B.id.assign(n, 0);
+	for (int b = 0; b < P; b++)
+		for (int r = cut[b]; r < cut[b + 1]; r++) B.id[r] = b;
+	if (first_out) *first_out = cut;
+	return B;
+}
 
 // Dependency levels of the forward (lower) or backward sweep; with blocks,
 // levels are numbered block by block (block b's levels follow block b-1's),
@@ -1123,7 +1212,13 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 {
 	int n = t->neq, rc, D, sb;
 	fg_ilu_sweeps &S = t->sweeps;
-	Blocks B = { t->o.ilu_blocks > 1 ? std::min(t->o.ilu_blocks, n) : 0, n };
+	std::vector<int> first;
+	Blocks B = make_blocks(hIA, hJA, n, t->o.ilu_blocks, &first);
+	free(S.block_first);
+	S.block_first = (int *)malloc(sizeof(int) * first.size());
+	if (!S.block_first) return FEMGPU_E_NOMEM;
+	memcpy(S.block_first, first.data(), sizeof(int) * first.size());
+	S.nblocks = (int)first.size() - 1;
 	std::vector<int> clo, cup;
 	HostLevels Lo = host_levels(hIA, hJA, n, true, B, &clo), Up = host_levels(hIA, hJA, n, false, B, &cup);
 	if ((rc = build_prog<double, true>(hIA, hJA, n, Up, nullptr, B, cup, S.up64))) return rc;
@@ -1232,4 +1327,7 @@ extern "C" void fg_ilu_free(femgpu_transport *t)
 	}
 	void *v[] = { S.bl64, S.y64, S.bl32, S.y32, S.fac_ptr, S.fac_prog, S.fac2_hdr, S.fac2 };
 	for (void *q : v) if (q) cudaFree(q);
+	free(S.block_first);
+	S.block_first = nullptr;
+	S.nblocks = 0;
 }

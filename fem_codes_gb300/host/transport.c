@@ -307,6 +307,18 @@ int femgpu_transport_info(const femgpu_transport *t, int *info)
 	return 0;
 }
 
+int femgpu_transport_ilu_blocks(const femgpu_transport *t, int *first, int cap)
+{
+	if (!t) return FEMGPU_E_ARG;
+	if (!t->sweeps.block_first) return FEMGPU_E_NOT_BUILT;
+	int P = t->sweeps.nblocks;
+	if (first) {
+		if (cap < P + 1) return FEMGPU_E_ARG;
+		memcpy(first, t->sweeps.block_first, sizeof(int) * ((size_t)P + 1));
+	}
+	return P;
+}
+
 int femgpu_transport_get_pattern(const femgpu_transport *t, int *IA, int *JA, int *sbe, int *order,
 		int *node_id)
 {

@@ -118,6 +118,15 @@ int femgpu_transport_set_stream(femgpu_transport *ctx, void *stream);
  * preconditioned solve fell back to ILU(0) (to AMG) (7 ints). */
 int femgpu_transport_info(const femgpu_transport *ctx, int *info);
 
+/* Block ILU(0) (opts.ilu_blocks = P > 1) drops the couplings between P
+ * contiguous row runs of the (reordered) numbering, cut at equal spans of the
+ * full factor's dependency levels (FEMGPU_ILU_BLOCK_CUT=depth: the shallowest
+ * deepest run; =rows: equal row counts).  Returns the
+ * number of runs (1: global ILU(0)) and, when first != NULL, writes the first
+ * row of each run and the row count (runs + 1 ints; cap = room in first).
+ * FEMGPU_E_NOT_BUILT before the ILU(0) structure exists (CSR + ILU0 only). */
+int femgpu_transport_ilu_blocks(const femgpu_transport *ctx, int *first, int cap);
+
 /* Copies of the device-built structure, for parity checks against the
  * reference (IA [neq+1], JA [nnz], CSR_by_Element [9*nel]; EDE: lm2 [2*nedge],
  * EDGE_by_Element [3*nel], order [3*nel]; node ids [nnodes]). NULL skips. */

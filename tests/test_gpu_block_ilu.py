@@ -1,10 +1,14 @@
 """Block ILU(0) (ilu_blocks = P): ILU(0) of the block-diagonal part of the
 CSR matrix over P contiguous row blocks of the numbering, one thread block
-per matrix block on the GPU.  The preconditioner application is checked
-bit for bit against the oracle's ILU(0) of the same block-diagonal matrix
-(the reference's factorisation and sweeps applied to the matrix with the
-inter-block couplings dropped), and FGMRES with it reaches the true-residual
-tolerance."""
+per matrix block on the GPU.  The runs are cut at equal spans of the full
+factor's dependency levels (FEMGPU_ILU_BLOCK_CUT=depth: the shallowest
+deepest run; =rows: equal row counts); the test reads the cut the library
+chose, checks it against its own restatement of each rule, and builds the
+oracle's block-diagonal matrix from it.  The preconditioner application is
+checked bit for bit against the oracle's ILU(0) of the same block-diagonal
+matrix (the reference's factorisation and sweeps applied to the matrix with
+the inter-block couplings dropped), and FGMRES with it reaches the
+true-residual tolerance."""
 import numpy as np
 import pytest
 
@@ -14,18 +18,67 @@ from fem_codes_gb300.mesh import skew_problem, structured_mesh
 pytestmark = pytest.mark.gpu
 
 
-def _block_diag(IA, JA, AA, P):
+def level_counts(IA, JA, blk, lower=True):
+    """Dependency levels of each block with the couplings between blocks dropped."""
+    n = len(IA) - 1
+    lev = np.zeros(n, np.int64)
+    order = range(n) if lower else range(n - 1, -1, -1)
+    for i in order:
+        cols = JA[IA[i]:IA[i + 1]]
+        cols = cols[((cols < i) if lower else (cols > i)) & (blk[cols] == blk[i])]
+        lev[i] = lev[cols].max() + 1 if cols.size else 0
+    return np.array([lev[blk == b].max() + 1 for b in range(blk.max() + 1)])
+
+
+def level_cut(IA, JA, P):
+    """First rows of the default cut: run b starts where the running maximum
+    of the full factor's forward level first reaches ceil(b * levels / P)."""
+    n = len(IA) - 1
+    lev = np.zeros(n, np.int64)
+    for i in range(n):
+        cols = JA[IA[i]:IA[i + 1]]
+        cols = cols[cols < i]
+        lev[i] = lev[cols].max() + 1 if cols.size else 0
+    run = np.maximum.accumulate(lev)
+    nl = int(run[-1]) + 1
+    cut = np.zeros(P + 1, np.int64)
+    cut[P] = n
+    i = 0
+    for b in range(1, P):
+        fl = (nl * b + P - 1) // P
+        while i < n and run[i] < fl:
+            i += 1
+        cut[b] = i
+    for b in range(1, P):
+        cut[b] = max(cut[b], cut[b - 1] + 1)
+    for b in range(P - 1, 0, -1):
+        cut[b] = min(cut[b], cut[b + 1] - 1)
+    return cut
+
+
+def block_ids(first):
+    blk = np.zeros(first[-1], np.int64)
+    for b in range(len(first) - 1):
+        blk[first[b]:first[b + 1]] = b
+    return blk
+
+
+def _block_diag(IA, JA, AA, blk):
     n = len(IA) - 1
     rows = np.repeat(np.arange(n), np.diff(IA))
-    blk = (np.arange(n, dtype=np.int64) * P // n).astype(np.int64)
     keep = blk[rows] == blk[JA]
     IAf = np.concatenate([[0], np.cumsum(np.bincount(rows[keep], minlength=n))]).astype(np.int32)
     return IAf, JA[keep].astype(np.int32), AA[: len(JA)][keep]
 
 
+@pytest.mark.parametrize("mode", ["levels", "depth", "rows"])
 @pytest.mark.parametrize("nx,ny,P", [(48, 32, 7), (96, 64, 16), (64, 64, 1000)])
-def test_block_ilu_apply_bitexact(gpu_lib, nx, ny, P):
+def test_block_ilu_apply_bitexact(gpu_lib, nx, ny, P, mode, monkeypatch):
     import fem_codes_gb300 as fg
+    if mode == "levels":
+        monkeypatch.delenv("FEMGPU_ILU_BLOCK_CUT", raising=False)
+    else:
+        monkeypatch.setenv("FEMGPU_ILU_BLOCK_CUT", mode)
     m = structured_mesh(nx, ny, perturb=0.2, seed=7)
     p = skew_problem(m)
     with fg.SSTransport.from_problem(m, p, scheme="CSR", reorder="SYMRCM", precond="ILU0", solver="GMRES",
@@ -33,7 +86,20 @@ def test_block_ilu_apply_bitexact(gpu_lib, nx, ny, P):
         F, AA = T.Build(want_matrix=True)
         T.precond_setup(1)
         pat = T.pattern()
-        IAf, JAf, AAf = _block_diag(pat["IA"], pat["JA"], AA, min(P, T.neq))
+        IA, JA = np.asarray(pat["IA"]), np.asarray(pat["JA"])
+        first = T.ilu_blocks()
+        P = min(P, T.neq)
+        assert first.size == P + 1 and first[0] == 0 and first[-1] == T.neq and np.all(np.diff(first) > 0)
+        blk = block_ids(first)
+        if mode == "rows":
+            assert np.array_equal(blk, np.arange(T.neq, dtype=np.int64) * P // T.neq)
+        elif mode == "levels":
+            assert np.array_equal(first, level_cut(IA, JA, P))
+        else:
+            # no contiguous cut into P runs has a shallower deepest run
+            depth = level_counts(IA, JA, blk).max()
+            assert depth <= level_counts(IA, JA, np.arange(T.neq, dtype=np.int64) * P // T.neq).max()
+        IAf, JAf, AAf = _block_diag(IA, JA, AA, blk)
         LU, Dinv = pyoracle.ilu0(IAf, JAf, AAf)
         r = np.random.default_rng(3).uniform(-1, 1, T.neq + 1)
         r[T.neq] = 0.0
