@@ -41,6 +41,8 @@ typedef struct fg_sweep {
 	int nchunk;                /* matrix blocks (block ILU(0); 1: global)    */
 	int *chunk_sb, *chunk_lev; /* [nchunk+1] first sub-block / level of each */
 	int rw;                    /* record layout width (0: ELL sub-blocks)    */
+	int df;                    /* record layout swept without level barriers */
+	int skew;                  /* ... levels a warp may run ahead            */
 	int bvo, cmax;             /* record layout: input slice offset in a
 	                            * stage, most rows of a sub-block            */
 } fg_sweep;

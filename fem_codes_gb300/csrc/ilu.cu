@@ -110,6 +110,19 @@ __device__ __forceinline__ void fence_mbar_init()
 	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// Release store / acquire load of a shared-memory flag (CTA scope).
+__device__ __forceinline__ void st_release_cta(int *p, int v)
+{
+	asm volatile("st.release.cta.shared.s32 [%0], %1;" :: "r"(smem_u32(p)), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int ld_acquire_cta(const int *p)
+{
+	int v;
+	asm volatile("ld.acquire.cta.shared.s32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+	return v;
+}
+
 // Synchronise the CW consumer warps (shared-memory ordering included).
 template <int CW>
 __device__ __forceinline__ void consumer_sync()
@@ -164,6 +177,7 @@ struct SweepArgs {
 	const int *chunk_sb;          // [P+1] first sub-block of each matrix block (NULL: one block)
 	const int *chunk_lev;         // [P+1] first level of each matrix block
 	int bvo, cmax;                // record layout: input slice offset, most rows of a sub-block
+	int skew;                     // dataflow: levels a warp may run ahead of the slowest one
 };
 
 // CW consumer warps (warps 0..CW-1) and one producer warp (warp CW).
@@ -431,6 +445,172 @@ k_sweep_rec(SweepArgs a, const T *__restrict__ in, T *out)
 		for (int i = 0; i < SW_WAIT_LIMIT && !*(volatile int *)&pdone; i++) __nanosleep(64);
 		int last = *(volatile int *)&issued;
 		for (int q = sb; q < last; q++) (void)mbar_wait(&full[q % D], (unsigned)((q / D) & 1));
+	}
+}
+
+// ------------------------------------------- dataflow sweep (record layout)
+// The same records, without a barrier per level: every consumer warp
+// publishes the last level it has finished (prog[warp], shared memory) and,
+// before computing a sub-block, waits only for the warps whose rows its own
+// rows read (a table of 16 bytes per warp in the sub-block header: for each
+// producer warp the smallest level distance of a dependency it supplies, 255
+// when it supplies none within S + 1 levels) and for every warp to have
+// finished level l - S - 1 (S = the program's skew).  The second wait bounds
+// how far warps drift apart, so a ring slot is rewritten only after every
+// reader of its old value is done: the program reads from the ring only
+// dependencies within SW_RING - S * (widest level) positions of their level's
+// end.  A warp publishes a level with a release store right after its ring
+// writes and only then stores the level's outputs to global memory, so no
+// level waits for its own global stores; a dependency read back from global
+// memory therefore waits for its producer's next level (whose release covers
+// those stores), and the program keeps such dependencies at least two levels
+// back.  A warp
+// releases a stage (mbarrier of CW arrivals) as soon as its rows are in
+// registers.  Header: {rows, sub-blocks of the level, first position, far
+// flag}, then CW need tables of 16 bytes, then the records.
+#define DF_HDR (16 + SW2_CW * 16)
+
+template <typename T, bool UPPER, bool FMA, int W>
+__global__ void __launch_bounds__((SW2_CW + 1) * 32, 1)
+k_sweep_df(SweepArgs a, const T *__restrict__ in, T *out)
+{
+	constexpr int CW = SW2_CW;
+	constexpr int IB = rec_ib(W), VB = rec_vb(W, UPPER, (int)sizeof(T)), RB = rec_bytes(W, UPPER, (int)sizeof(T));
+	static_assert(SW_SUB == CW * 32, "one row per consumer thread and sub-block");
+	static_assert(CW <= 16, "one need byte per consumer warp in a 16-byte table");
+	if (a.active && !*a.active) return;
+	extern __shared__ __align__(128) unsigned char sm[];
+	const unsigned ring_b = (unsigned)al16((SW_RING + 1) * sizeof(T));
+	T *ring = (T *)sm;
+	unsigned long long *full = (unsigned long long *)(sm + ring_b);
+	unsigned long long *empty = full + SW_MAXD;
+	unsigned char *stages = sm + ((ring_b + SW_BAR_BYTES + 127) & ~127u);
+	__shared__ int failed, issued, pdone;
+	__shared__ int prog[CW];
+	volatile int *vfailed = &failed;
+	volatile int *vprog = prog;
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, D = a.D;
+	const unsigned sbytes = (unsigned)a.stage_bytes;
+	const int sb0 = a.chunk_sb ? a.chunk_sb[blockIdx.x] : 0, sb1 = a.chunk_sb ? a.chunk_sb[blockIdx.x + 1] : a.nsb;
+	const int l0 = a.chunk_lev ? a.chunk_lev[blockIdx.x] : 0, l1 = a.chunk_lev ? a.chunk_lev[blockIdx.x + 1] : a.nlev;
+
+	if (tid == 0) {
+		failed = 0; issued = 0; pdone = 0;
+		ring[SW_RING] = T(0);
+		for (int s = 0; s < D; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], CW); }
+		fence_mbar_init();
+	}
+	if (tid < CW) prog[tid] = -1;
+	__syncthreads();
+
+	if (warp == CW) {                                     // ---- producer warp
+		bool stop = false;
+		int s = 0;
+		unsigned ph = 0;
+		for (int base = sb0; base < sb1 && !stop; base += 32) {
+			int i = base + lane;
+			long long b0 = 0, b1 = 0;
+			int p0 = 0, vb = 0;
+			if (i < sb1) { b0 = a.blk_off[i]; b1 = a.blk_off[i + 1]; p0 = a.sb_in[i]; vb = a.sb_inb[i]; }
+			for (int j = 0; j < 32 && base + j < sb1; j++) {
+				long long B0 = __shfl_sync(0xffffffffu, b0, j), B1 = __shfl_sync(0xffffffffu, b1, j);
+				int P0 = __shfl_sync(0xffffffffu, p0, j), VB = __shfl_sync(0xffffffffu, vb, j);
+				int sb = base + j - sb0;
+				int go = 1;
+				if (lane == 0) {
+					if (sb >= D && !mbar_wait_or_fail(&empty[s], ph, vfailed)) go = 0;
+					if (*vfailed) go = 0;
+					if (go) {
+						unsigned bb = (unsigned)(B1 - B0);
+						unsigned char *dst = stages + (unsigned)s * sbytes;
+						fence_proxy_async();
+						mbar_expect_tx(&full[s], bb + (unsigned)VB);
+						bulk_g2s(dst, a.prog + B0, bb, &full[s]);
+						if (VB) bulk_g2s(dst + a.bvo, in + P0, (unsigned)VB, &full[s]);
+						*(volatile int *)&issued = sb + 1;
+					}
+				}
+				go = __shfl_sync(0xffffffffu, go, 0);
+				if (!go) { stop = true; break; }
+				if (++s == D) { s = 0; if (sb >= D) ph ^= 1u; else if (sb == D - 1) ph = 0; }
+			}
+		}
+		if (lane == 0) *(volatile int *)&pdone = 1;
+		return;
+	}
+
+	const int ctid = tid;                                 // ---- consumer warps
+	const unsigned roff = (unsigned)DF_HDR + (unsigned)(ctid < a.cmax ? ctid : a.cmax - 1) * RB;
+	const unsigned boff = (unsigned)a.bvo + (unsigned)(ctid < a.cmax ? ctid : a.cmax - 1) * sizeof(T);
+	int s = 0, waited = 0;
+	unsigned ph = 0;
+	bool fail = false;
+	T ydef = T(0);                                        // an output not yet stored to global memory
+	int odef = -1;
+	for (int l = l0; l < l1 && !fail; l++) {
+		const int ll = l - l0;
+		int nsub = 1;
+		for (int j = 0; j < nsub; j++) {
+			if (!mbar_wait_or_fail(&full[s], ph, vfailed)) { *vfailed = 1; fail = true; break; }
+			waited++;
+			const unsigned char *st = stages + (unsigned)s * sbytes;
+			union { int4 q[IB / 16]; int i[IB / 4]; } ci;
+			union { int4 q[VB / 16]; T v[VB / sizeof(T)]; } cv;
+#pragma unroll
+			for (int k = 0; k < IB / 16; k++) ci.q[k] = ((const int4 *)(st + roff))[k];
+#pragma unroll
+			for (int k = 0; k < VB / 16; k++) cv.q[k] = ((const int4 *)(st + roff + IB))[k];
+			const T x0 = *(const T *)(st + boff);
+			const int4 h = *(const int4 *)st;
+			const int need = lane < CW ? (int)st[16 + warp * 16 + lane] : 255;
+			if (j == 0) nsub = h.y;
+			__syncwarp();
+			if (lane == 0) mbar_arrive(&empty[s]);        // this warp's rows are in registers
+			if (++s == D) { s = 0; ph ^= 1u; }
+			if (32 * warp >= h.x) continue;               // no rows of this warp here
+			// producers of this warp's dependencies, and every warp within the skew
+			const int want = ll - (need == 255 ? a.skew + 1 : need);
+			bool ready = false;
+			for (int it = 0; it < SW_WAIT_LIMIT; it++) {
+				const bool mine = lane >= CW || lane == warp || ld_acquire_cta(&prog[lane]) >= want;
+				if (__all_sync(0xffffffffu, mine)) { ready = true; break; }
+				if (__any_sync(0xffffffffu, *vfailed != 0)) break;
+			}
+			if (!ready) { *vfailed = 1; fail = true; break; }
+			__syncwarp();                                 // the lanes' acquires order every lane's reads
+			T d[W];
+#pragma unroll
+			for (int k = 0; k < W; k++) {
+				unsigned c = (unsigned)ci.i[k] & ~SW_NEAR;
+				d[k] = ring[c < SW_RING ? c : SW_RING];
+			}
+			if (ctid < h.x) {
+				if (h.w) {
+#pragma unroll
+					for (int k = 0; k < W; k++)
+						if (!((unsigned)ci.i[k] & SW_NEAR)) d[k] = __ldcg(&out[ci.i[k]]);
+				}
+				T y = x0;
+#pragma unroll
+				for (int k = 0; k < W; k++) y = fmsub<T, FMA>(y, d[k], cv.v[k]);
+				if (UPPER) y = mul(y, cv.v[W]);
+				ring[(h.z + ctid) & (SW_RING - 1)] = y;
+				if (odef >= 0) out[odef] = ydef;          // an earlier sub-block of this level
+				ydef = y;
+				odef = ci.i[W];
+			}
+		}
+		if (fail) break;
+		__syncwarp();
+		if (lane == 0) st_release_cta(&prog[warp], ll);
+		if (odef >= 0) { out[odef] = ydef; odef = -1; }
+	}
+	consumer_sync<CW>();
+	if (*vfailed && ctid == 0) {
+		fg_set_err(a.err, FEMGPU_E_TIMEOUT);
+		for (int i = 0; i < SW_WAIT_LIMIT && !*(volatile int *)&pdone; i++) __nanosleep(64);
+		int last = *(volatile int *)&issued;
+		for (int q = waited; q < last; q++) (void)mbar_wait(&full[q % D], (unsigned)((q / D) & 1));
 	}
 }
 
@@ -849,6 +1029,24 @@ static int sweep_near_limit(void)
 	return (v >= 1 && v <= SW_RING) ? v : SW_RING;
 }
 
+// Record-layout sweeps run as dataflow (k_sweep_df) unless
+// FEMGPU_SWEEP_SYNC=barrier asks for one barrier per level (k_sweep_rec).  At
+// 2048x1024 with 16 blocks: 1.36 ms per FP64 application against 1.47.
+static bool sweep_dataflow(void)
+{
+	const char *e = getenv("FEMGPU_SWEEP_SYNC");
+	return !(e && !strcmp(e, "barrier"));
+}
+
+// Levels a dataflow warp may run ahead of the slowest one (FEMGPU_SWEEP_SKEW,
+// 1..64; default 4).
+static int sweep_skew(void)
+{
+	const char *e = getenv("FEMGPU_SWEEP_SKEW");
+	int v = e ? atoi(e) : 4;
+	return (v >= 1 && v <= 64) ? v : 4;
+}
+
 // One sweep program.  Forward (lower): L part, outputs to the backward
 // sweep's padded level order (target = the U levels' ppos).  Backward: U part
 // and pivots, outputs in natural order.
@@ -858,7 +1056,7 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 {
 	const bool lower = !UPPER;
 	const long long tsize = sizeof(T);
-	const int near_lim = sweep_near_limit();
+	int near_lim = sweep_near_limit();
 	int nlev = H.nlev;
 	// sub-blocks: (level, first row within the level, rows, width)
 	struct Sub { int l, j0, c, w; };
@@ -878,16 +1076,27 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 		}
 	}
 	int nsb = (int)subs.size();
-	int wmax = 0, cmax = 1;
+	int wmax = 0, cmax = 1, lmax = 1;
 	for (const Sub &S : subs) { wmax = std::max(wmax, S.w); cmax = std::max(cmax, S.c); }
+	for (int l = 0; l < nlev; l++) lmax = std::max(lmax, H.start[l + 1] - H.start[l]);
 	const int rw = rec_width(wmax);                                   // 0: ELL sub-blocks
 	const long long RB = rw ? rec_bytes(rw, UPPER, (int)tsize) : 0;
+	// dataflow: the ring holds only what no warp up to the skew behind can still overwrite
+	const int skew = sweep_skew();
+	bool df = rw && sweep_dataflow() && SW_RING - skew * lmax >= 2 * lmax;
+	if (df) near_lim = std::min(near_lim, SW_RING - skew * lmax);
+	if (df && near_lim < 2 * lmax) df = false;      // a far dependency must be two levels back
+	const long long hdrb = df ? DF_HDR : 16;
+	std::vector<int> lev_of(df ? n : 0);
+	if (df)
+		for (int l = 0; l < nlev; l++)
+			for (int q = H.start[l]; q < H.start[l + 1]; q++) lev_of[q] = l;
 	std::vector<long long> off(nsb + 1, 0);
 	std::vector<int> sb_in(nsb), sb_inb(nsb);
 	long long maxblk = 0, bvo = 0, maxin = 0;
 	for (int i = 0; i < nsb; i++) {
 		int cp = (subs[i].c + 3) & ~3;
-		long long bb = rw ? 16 + (long long)subs[i].c * RB : blk_bytes<T, UPPER>(subs[i].w, cp);
+		long long bb = rw ? hdrb + (long long)subs[i].c * RB : blk_bytes<T, UPPER>(subs[i].w, cp);
 		off[i + 1] = off[i] + bb;
 		sb_in[i] = H.pstart[subs[i].l] + subs[i].j0;                 // j0 is a multiple of 4
 		sb_inb[i] = (int)al16((long long)cp * tsize);
@@ -918,9 +1127,28 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 		if (rw) {
 			const int hh[4] = { c, nsub, start, hasfar };
 			memcpy(b, hh, sizeof hh);
+			if (df) {
+				// need[w][pw]: smallest level distance of a dependency of warp w's rows
+				// produced by warp pw (255: none within skew + 1 levels)
+				unsigned char *need = b + 16;
+				memset(need, 255, (size_t)SW2_CW * 16);
+				for (int j = 0; j < c; j++) {
+					int r = H.rows[start + j];
+					for (int q = IA[r]; q < IA[r + 1]; q++) {
+						int col = JA[q];
+						if ((lower ? !(col < r) : !(col > r)) || !B.same(r, col)) continue;
+						int p = H.pos[col], lp = lev_of[p], dl = l - lp;
+						if (end - p > near_lim) dl--;      // read back from global memory: the next level's release
+						if (dl > skew + 1) continue;
+						int pw = ((p - H.start[lp]) % SW_SUB) / 32;
+						unsigned char &e = need[(j / 32) * 16 + pw];
+						if (dl < (int)e) e = (unsigned char)dl;
+					}
+				}
+			}
 			for (int j = 0; j < c; j++) {
-				int *ri = (int *)(b + 16 + (size_t)j * RB), r = H.rows[start + j], k = 0;
-				long long vo = off[i] + 16 + (long long)j * RB + rec_ib(rw);
+				int *ri = (int *)(b + hdrb + (size_t)j * RB), r = H.rows[start + j], k = 0;
+				long long vo = off[i] + hdrb + (long long)j * RB + rec_ib(rw);
 				for (int q = 0; q < rw; q++) ri[q] = (int)(SW_NEAR | SW_RING);   // the zero slot
 				ri[rw] = lower ? target->ppos[r] : r;
 				for (int q = IA[r]; q < IA[r + 1]; q++) {
@@ -976,6 +1204,8 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 	}
 	sw.nchunk = (int)clev.size() - 1;
 	sw.rw = rw;
+	sw.df = df;
+	sw.skew = skew;
 	sw.bvo = (int)bvo;
 	sw.cmax = cmax;
 	sw.nlev = nlev;
@@ -1132,9 +1362,14 @@ static int factor_cluster_size(int P)
 	SW_SET(float, false, CW, false); SW_SET(float, true, CW, false)
 #define SR_SET(T, U, F, W) FG_TRY(cudaFuncSetAttribute(k_sweep_rec<T, U, F, W>, \
 	cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP))
+#define SD_SET(T, U, F, W) FG_TRY(cudaFuncSetAttribute(k_sweep_df<T, U, F, W>, \
+	cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP))
 #define SR_SET_W(W) SR_SET(double, false, false, W); SR_SET(double, true, false, W); \
 	SR_SET(double, false, true, W); SR_SET(double, true, true, W); \
-	SR_SET(float, false, false, W); SR_SET(float, true, false, W)
+	SR_SET(float, false, false, W); SR_SET(float, true, false, W); \
+	SD_SET(double, false, false, W); SD_SET(double, true, false, W); \
+	SD_SET(double, false, true, W); SD_SET(double, true, true, W); \
+	SD_SET(float, false, false, W); SD_SET(float, true, false, W)
 static int sweep_attrs(void)
 {
 	SW_SET_CW(4);
@@ -1163,6 +1398,19 @@ static int sweep_cw(void)
 // fma: fused multiply-subtract in the FP64 sweeps (the FGMRES solves); the
 // separately rounded form reproduces the reference bit for bit.
 template <typename T, bool UPPER, bool FMA>
+static void launch_df(const SweepArgs &a, int rw, int grid, int bytes, cudaStream_t s, const T *in, T *out)
+{
+	const int nt = (SW2_CW + 1) * 32;
+	switch (rw) {
+	case 2: k_sweep_df<T, UPPER, FMA, 2><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 3: k_sweep_df<T, UPPER, FMA, 3><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 4: k_sweep_df<T, UPPER, FMA, 4><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 6: k_sweep_df<T, UPPER, FMA, 6><<<grid, nt, bytes, s>>>(a, in, out); break;
+	default: k_sweep_df<T, UPPER, FMA, 8><<<grid, nt, bytes, s>>>(a, in, out); break;
+	}
+}
+
+template <typename T, bool UPPER, bool FMA>
 static void launch_rec(const SweepArgs &a, int rw, int grid, int bytes, cudaStream_t s, const T *in, T *out)
 {
 	const int nt = (SW2_CW + 1) * 32;
@@ -1176,9 +1424,14 @@ static void launch_rec(const SweepArgs &a, int rw, int grid, int bytes, cudaStre
 }
 
 template <typename T, bool UPPER>
-static void launch_sweep(const SweepArgs &a, int rw, int grid, int bytes, cudaStream_t s, const T *in, T *out,
-                         bool fma)
+static void launch_sweep(const SweepArgs &a, int rw, int df, int grid, int bytes, cudaStream_t s, const T *in,
+                         T *out, bool fma)
 {
+	if (rw && df) {
+		if (fma && sizeof(T) == 8) launch_df<T, UPPER, true>(a, rw, grid, bytes, s, in, out);
+		else launch_df<T, UPPER, false>(a, rw, grid, bytes, s, in, out);
+		return;
+	}
 	if (rw) {
 		if (fma && sizeof(T) == 8) launch_rec<T, UPPER, true>(a, rw, grid, bytes, s, in, out);
 		else launch_rec<T, UPPER, false>(a, rw, grid, bytes, s, in, out);
@@ -1291,14 +1544,14 @@ static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, 
 	if (bytes < 0) return bytes;
 	a.prog = lo.prog; a.blk_off = lo.blk_off; a.sb_in = lo.sb_in; a.sb_inb = lo.sb_inb;
 	a.nlev = lo.nlev; a.nsb = lo.nsb; a.D = D; a.stage_bytes = sb;
-	a.chunk_sb = lo.chunk_sb; a.chunk_lev = lo.chunk_lev; a.bvo = lo.bvo; a.cmax = lo.cmax;
-	launch_sweep<T, false>(a, lo.rw, lo.nchunk, bytes, s, bl, y, fma);
+	a.chunk_sb = lo.chunk_sb; a.chunk_lev = lo.chunk_lev; a.bvo = lo.bvo; a.cmax = lo.cmax; a.skew = lo.skew;
+	launch_sweep<T, false>(a, lo.rw, lo.df, lo.nchunk, bytes, s, bl, y, fma);
 	bytes = sweep_smem(up, sizeof(T), &D, &sb);
 	if (bytes < 0) return bytes;
 	a.prog = up.prog; a.blk_off = up.blk_off; a.sb_in = up.sb_in; a.sb_inb = up.sb_inb;
 	a.nlev = up.nlev; a.nsb = up.nsb; a.D = D; a.stage_bytes = sb;
-	a.chunk_sb = up.chunk_sb; a.chunk_lev = up.chunk_lev; a.bvo = up.bvo; a.cmax = up.cmax;
-	launch_sweep<T, true>(a, up.rw, up.nchunk, bytes, s, y, (T *)z, fma);
+	a.chunk_sb = up.chunk_sb; a.chunk_lev = up.chunk_lev; a.bvo = up.bvo; a.cmax = up.cmax; a.skew = up.skew;
+	launch_sweep<T, true>(a, up.rw, up.df, up.nchunk, bytes, s, y, (T *)z, fma);
 	return (int)cudaGetLastError();
 }
 

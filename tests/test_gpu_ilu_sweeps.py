@@ -8,7 +8,9 @@ in oracle/), on systems that reach the sweep's less common paths:
   sub-blocks;
 * dependencies older than the shared-memory ring, which the sweep reads back
   from global memory; FEMGPU_SWEEP_NEAR lowers the ring's reach when the
-  programs are built, so a small system takes that path for most rows.
+  programs are built, so a small system takes that path for most rows;
+* both level synchronisations of the record layout: dataflow (warps wait on
+  each other's progress flags, the default) and one barrier per level.
 
 Bar: the separately rounded sweeps (pgmres) are bit-identical to the oracle;
 the fused sweeps (FGMRES) are bit-identical across layouts and ring reaches
@@ -26,11 +28,12 @@ pytestmark = pytest.mark.gpu
 FMA_TOL = 1e-12    # fused multiply-subtract vs separately rounded sweeps (relative max-norm)
 
 
-def apply_ilu(m, p, reorder, solver, layout=None, near=None, blocks=0):
+def apply_ilu(m, p, reorder, solver, layout=None, near=None, blocks=0, sync=None):
     """Factor and apply the device ILU(0) of the transport system once; the
-    layout and ring reach are fixed when the sweep programs are built."""
+    layout, ring reach and level synchronisation (dataflow or one barrier per
+    level) are fixed when the sweep programs are built."""
     import fem_codes_gb300 as fg
-    env = {"FEMGPU_SWEEP_LAYOUT": layout, "FEMGPU_SWEEP_NEAR": near}
+    env = {"FEMGPU_SWEEP_LAYOUT": layout, "FEMGPU_SWEEP_NEAR": near, "FEMGPU_SWEEP_SYNC": sync}
     saved = {k: os.environ.get(k) for k in env}
     try:
         for k, v in env.items():
@@ -61,37 +64,39 @@ def oracle_apply(pat, A, x):
     return pyoracle.ilu0_apply(IA, JA, LU, Dinv, x)[:n]
 
 
-@pytest.mark.parametrize("layout", ["rec", "ell"])
-def test_levels_wider_than_a_sub_block(gpu_lib, layout):
+@pytest.mark.parametrize("layout,sync", [("rec", "dataflow"), ("rec", "barrier"), ("ell", None)])
+def test_levels_wider_than_a_sub_block(gpu_lib, layout, sync):
     m = structured_mesh(600, 600, perturb=0.2, seed=1234)
     p = skew_problem(m)
-    z, x, pat, A = apply_ilu(m, p, "NOT", "GMRES", layout=layout)
+    z, x, pat, A = apply_ilu(m, p, "NOT", "GMRES", layout=layout, sync=sync)
     assert np.array_equal(z, oracle_apply(pat, A, x))
-    zf, _, _, _ = apply_ilu(m, p, "NOT", "FGMRES", layout=layout)
+    zf, _, _, _ = apply_ilu(m, p, "NOT", "FGMRES", layout=layout, sync=sync)
     zr, _, _, _ = apply_ilu(m, p, "NOT", "FGMRES", layout="rec" if layout == "ell" else "ell")
     assert np.array_equal(zf, zr)
     assert np.max(np.abs(zf - z)) <= FMA_TOL * np.max(np.abs(z))
 
 
-@pytest.mark.parametrize("layout", ["rec", "ell"])
+@pytest.mark.parametrize("layout,sync", [("rec", "dataflow"), ("rec", "barrier"), ("ell", None)])
 @pytest.mark.parametrize("reorder", ["SYMRCM", "NOT"])
-def test_dependencies_older_than_the_ring(gpu_lib, layout, reorder):
+def test_dependencies_older_than_the_ring(gpu_lib, layout, sync, reorder):
     m = structured_mesh(60, 40, perturb=0.2, seed=7)
     p = skew_problem(m)
-    z, x, pat, A = apply_ilu(m, p, reorder, "GMRES", layout=layout, near=8)
+    z, x, pat, A = apply_ilu(m, p, reorder, "GMRES", layout=layout, near=8, sync=sync)
     assert np.array_equal(z, oracle_apply(pat, A, x))
-    zf, _, _, _ = apply_ilu(m, p, reorder, "FGMRES", layout=layout, near=8)
-    zd, _, _, _ = apply_ilu(m, p, reorder, "FGMRES", layout=layout)
+    zf, _, _, _ = apply_ilu(m, p, reorder, "FGMRES", layout=layout, near=8, sync=sync)
+    zd, _, _, _ = apply_ilu(m, p, reorder, "FGMRES", layout=layout, sync=sync)
     assert np.array_equal(zf, zd)
 
 
+@pytest.mark.parametrize("sync", ["dataflow", "barrier"])
 @pytest.mark.parametrize("near", [None, 8])
-def test_block_ilu_layouts_agree(gpu_lib, near):
+def test_block_ilu_layouts_agree(gpu_lib, near, sync):
     """Block ILU(0) (couplings between the 4 blocks dropped) has no oracle
-    counterpart: both layouts and both ring reaches give the same bits."""
+    counterpart: both layouts, both synchronisations and both ring reaches
+    give the same bits."""
     m = structured_mesh(64, 48, perturb=0.2, seed=3)
     p = skew_problem(m)
     ref, _, _, _ = apply_ilu(m, p, "SYMRCM", "FGMRES", layout="ell", blocks=4)
-    z, _, _, _ = apply_ilu(m, p, "SYMRCM", "FGMRES", layout="rec", near=near, blocks=4)
+    z, _, _, _ = apply_ilu(m, p, "SYMRCM", "FGMRES", layout="rec", near=near, blocks=4, sync=sync)
     assert np.array_equal(z, ref)
     assert np.all(np.isfinite(z))
