@@ -305,7 +305,7 @@ k_sweep(SweepArgs a, const T *__restrict__ in, T *out)
 }
 
 // ------------------------------------------------ record layout (fixed width)
-// When every row of a sweep has at most 8 dependencies, each sub-block is a
+// When every row of a sweep has at most 16 dependencies, each sub-block is a
 // 16-byte header {rows, sub-blocks of the level, level-order position of the
 // first row, far flag} followed by one record per row: W dependency codes and
 // the output slot (ints, padded to 16 bytes), then W factor values and, in
@@ -1008,12 +1008,12 @@ static int up_vec(X **d, const std::vector<X> &h)
 }
 
 // Width of the record layout for a sweep whose widest row has w dependencies
-// (0: the ELL sub-block layout, used above 8 or when FEMGPU_SWEEP_LAYOUT=ell).
+// (0: the ELL sub-block layout, used above 16 or when FEMGPU_SWEEP_LAYOUT=ell).
 static int rec_width(int w)
 {
 	const char *e = getenv("FEMGPU_SWEEP_LAYOUT");
 	if (e && !strcmp(e, "ell")) return 0;
-	static const int widths[] = { 2, 3, 4, 6, 8 };
+	static const int widths[] = { 2, 3, 4, 6, 8, 12, 16 };
 	for (int v : widths) if (w <= v) return v;
 	return 0;
 }
@@ -1079,7 +1079,14 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 	int wmax = 0, cmax = 1, lmax = 1;
 	for (const Sub &S : subs) { wmax = std::max(wmax, S.w); cmax = std::max(cmax, S.c); }
 	for (int l = 0; l < nlev; l++) lmax = std::max(lmax, H.start[l + 1] - H.start[l]);
-	const int rw = rec_width(wmax);                                   // 0: ELL sub-blocks
+	int rw = rec_width(wmax);                                         // 0: ELL sub-blocks
+	if (rw) {
+		// wide records must still leave room for two stages of the widest sub-block
+		const long long fixed = (al16((SW_RING + 1) * tsize) + SW_BAR_BYTES + 127) & ~127LL;
+		const long long stage = DF_HDR + (long long)cmax * rec_bytes(rw, UPPER, (int)tsize) +
+		                        al16((long long)((cmax + 3) & ~3) * tsize);
+		if (fixed + 2 * ((stage + 127) & ~127LL) > SW_SMEM_CAP) rw = 0;
+	}
 	const long long RB = rw ? rec_bytes(rw, UPPER, (int)tsize) : 0;
 	// dataflow: the ring holds only what no warp up to the skew behind can still overwrite
 	const int skew = sweep_skew();
@@ -1380,6 +1387,8 @@ static int sweep_attrs(void)
 	SR_SET_W(4);
 	SR_SET_W(6);
 	SR_SET_W(8);
+	SR_SET_W(12);
+	SR_SET_W(16);
 	return 0;
 }
 
@@ -1406,7 +1415,9 @@ static void launch_df(const SweepArgs &a, int rw, int grid, int bytes, cudaStrea
 	case 3: k_sweep_df<T, UPPER, FMA, 3><<<grid, nt, bytes, s>>>(a, in, out); break;
 	case 4: k_sweep_df<T, UPPER, FMA, 4><<<grid, nt, bytes, s>>>(a, in, out); break;
 	case 6: k_sweep_df<T, UPPER, FMA, 6><<<grid, nt, bytes, s>>>(a, in, out); break;
-	default: k_sweep_df<T, UPPER, FMA, 8><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 8: k_sweep_df<T, UPPER, FMA, 8><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 12: k_sweep_df<T, UPPER, FMA, 12><<<grid, nt, bytes, s>>>(a, in, out); break;
+	default: k_sweep_df<T, UPPER, FMA, 16><<<grid, nt, bytes, s>>>(a, in, out); break;
 	}
 }
 
@@ -1419,7 +1430,9 @@ static void launch_rec(const SweepArgs &a, int rw, int grid, int bytes, cudaStre
 	case 3: k_sweep_rec<T, UPPER, FMA, 3><<<grid, nt, bytes, s>>>(a, in, out); break;
 	case 4: k_sweep_rec<T, UPPER, FMA, 4><<<grid, nt, bytes, s>>>(a, in, out); break;
 	case 6: k_sweep_rec<T, UPPER, FMA, 6><<<grid, nt, bytes, s>>>(a, in, out); break;
-	default: k_sweep_rec<T, UPPER, FMA, 8><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 8: k_sweep_rec<T, UPPER, FMA, 8><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 12: k_sweep_rec<T, UPPER, FMA, 12><<<grid, nt, bytes, s>>>(a, in, out); break;
+	default: k_sweep_rec<T, UPPER, FMA, 16><<<grid, nt, bytes, s>>>(a, in, out); break;
 	}
 }
 
