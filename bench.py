@@ -291,9 +291,13 @@ def run_ours(a):
         # algorithmic bytes: L and U values + 4-byte indices once, pivots, in/out vectors
         alg = nnz * (vs + 4) + neq * vs + 4 * neq * vs
         t_k = kern[sweep_key]
-        name = ("k_sweep (ILU(0) forward+backward, ELL layout" if os.environ.get("FEMGPU_SWEEP_LAYOUT") == "ell"
-                else "k_sweep_rec (ILU(0) forward+backward, row records") + \
-            f", level-pipelined, one CTA per matrix block, {max(a.ilu_blocks, 1)} blocks)"
+        if os.environ.get("FEMGPU_SWEEP_LAYOUT") == "ell":
+            name = "k_sweep (ILU(0) forward+backward, ELL layout, a barrier per level"
+        elif os.environ.get("FEMGPU_SWEEP_SYNC") == "barrier":
+            name = "k_sweep_rec (ILU(0) forward+backward, row records, a barrier per level"
+        else:
+            name = "k_sweep_df (ILU(0) forward+backward, row records, dataflow between warps"
+        name += f", TMA-staged, one CTA per matrix block, {max(a.ilu_blocks, 1)} blocks)"
     else:
         alg = nnz * 12 + (neq + 1) * 4 + 2 * neq * 8
         t_k = kern["spmv_f64"]
