@@ -100,3 +100,46 @@ def test_block_ilu_layouts_agree(gpu_lib, near, sync):
     z, _, _, _ = apply_ilu(m, p, "SYMRCM", "FGMRES", layout="rec", near=near, blocks=4, sync=sync)
     assert np.array_equal(z, ref)
     assert np.all(np.isfinite(z))
+
+
+FP32_RTOL = 1e-4   # FP32 sweeps (FP32 factor copies) vs FP64 sweeps, relative max-norm, small systems
+
+
+@pytest.mark.parametrize("blocks", [0, 4])
+def test_fp32_sweeps_both_synchronisations(gpu_lib, blocks):
+    """The FP32 programs (the MIXED precision's preconditioner) through the
+    device entry point: dataflow and barrier synchronisation give the same
+    bits, and the result is the FP64 application to FP32 accuracy."""
+    import ctypes
+    import torch
+    import fem_codes_gb300 as fg
+    m = structured_mesh(96, 64, perturb=0.2, seed=5)
+    p = skew_problem(m)
+    got = {}
+    for sync in ("dataflow", "barrier"):
+        saved = os.environ.get("FEMGPU_SWEEP_SYNC")
+        os.environ["FEMGPU_SWEEP_SYNC"] = sync
+        try:
+            with fg.SSTransport.from_problem(m, p, scheme="CSR", reorder="SYMRCM", precond="ILU0",
+                                             solver="FGMRES", ilu_blocks=blocks) as T:
+                T.Build(u=np.zeros(T.neq + 1))
+                T.precond_setup(1)
+                xh = np.zeros(T.neq + 1)
+                xh[:-1] = np.random.default_rng(13).standard_normal(T.neq)
+                x = torch.from_numpy(xh).cuda()
+                z = torch.zeros(T.neq + 1, dtype=torch.float32, device="cuda")
+                torch.cuda.synchronize()
+                rc = T._L.femgpu_transport_precond32_dev(T.handle, ctypes.c_void_p(x.data_ptr()),
+                                                         ctypes.c_void_p(z.data_ptr()))
+                assert rc == 0
+                torch.cuda.synchronize()
+                got[sync] = (z.cpu().numpy()[:-1].astype(np.float64), T.precond(xh)[:-1])
+        finally:
+            if saved is None:
+                os.environ.pop("FEMGPU_SWEEP_SYNC", None)
+            else:
+                os.environ["FEMGPU_SWEEP_SYNC"] = saved
+    z32, z64 = got["dataflow"]
+    assert np.array_equal(z32, got["barrier"][0])
+    assert np.array_equal(z64, got["barrier"][1])
+    assert np.max(np.abs(z32 - z64)) <= FP32_RTOL * np.max(np.abs(z64))
