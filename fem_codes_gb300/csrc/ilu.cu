@@ -488,7 +488,6 @@ k_sweep_df(SweepArgs a, const T *__restrict__ in, T *out)
 	__shared__ int failed, issued, pdone;
 	__shared__ int prog[CW];
 	volatile int *vfailed = &failed;
-	volatile int *vprog = prog;
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, D = a.D;
 	const unsigned sbytes = (unsigned)a.stage_bytes;
 	const int sb0 = a.chunk_sb ? a.chunk_sb[blockIdx.x] : 0, sb1 = a.chunk_sb ? a.chunk_sb[blockIdx.x + 1] : a.nsb;
