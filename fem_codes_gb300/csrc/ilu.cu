@@ -180,6 +180,65 @@ struct SweepArgs {
 	int skew;                     // dataflow: levels a warp may run ahead of the slowest one
 };
 
+// The producer warp of every sweep kernel: streams this thread block's
+// sub-blocks [sb0, sb1) and their input slices into the D-stage ring with
+// cp.async.bulk (completion on full[s]), reusing a stage once the consumers
+// have released it (empty[s]); stops when a consumer has failed.  The input
+// slice lands at the stage's fixed offset a.bvo (record layouts,
+// slice_at_bvo) or right after the sub-block (ELL layout).
+template <typename T>
+__device__ __forceinline__ void sweep_producer(const SweepArgs &a, const T *in, unsigned char *stages,
+                                               unsigned sbytes, unsigned long long *full,
+                                               unsigned long long *empty, int D, int sb0, int sb1, int lane,
+                                               volatile int *vfailed, int *issued, int *pdone, bool slice_at_bvo)
+{
+	bool stop = false;
+	int s = 0;
+	unsigned ph = 0;                                      // phase of empty[s] to wait for
+	for (int base = sb0; base < sb1 && !stop; base += 32) {
+		// each lane fetches the offsets of one upcoming sub-block
+		int i = base + lane;
+		long long b0 = 0, b1 = 0;
+		int p0 = 0, vb = 0;
+		if (i < sb1) { b0 = a.blk_off[i]; b1 = a.blk_off[i + 1]; p0 = a.sb_in[i]; vb = a.sb_inb[i]; }
+		for (int j = 0; j < 32 && base + j < sb1; j++) {
+			long long B0 = __shfl_sync(0xffffffffu, b0, j), B1 = __shfl_sync(0xffffffffu, b1, j);
+			int P0 = __shfl_sync(0xffffffffu, p0, j), VB = __shfl_sync(0xffffffffu, vb, j);
+			int sb = base + j - sb0;                      // local sub-block index
+			int go = 1;
+			if (lane == 0) {
+				if (sb >= D && !mbar_wait_or_fail(&empty[s], ph, vfailed)) go = 0;
+				if (*vfailed) go = 0;
+				if (go) {
+					unsigned bb = (unsigned)(B1 - B0);
+					unsigned char *dst = stages + (unsigned)s * sbytes;
+					fence_proxy_async();
+					mbar_expect_tx(&full[s], bb + (unsigned)VB);
+					bulk_g2s(dst, a.prog + B0, bb, &full[s]);
+					if (VB) bulk_g2s(dst + (slice_at_bvo ? (unsigned)a.bvo : bb), in + P0, (unsigned)VB, &full[s]);
+					*(volatile int *)issued = sb + 1;
+				}
+			}
+			go = __shfl_sync(0xffffffffu, go, 0);
+			if (!go) { stop = true; break; }
+			if (++s == D) { s = 0; if (sb >= D) ph ^= 1u; else if (sb == D - 1) ph = 0; }
+		}
+	}
+	if (lane == 0) *(volatile int *)pdone = 1;
+}
+
+// After a consumer failed (one thread): record the timeout, let the producer
+// stop, then wait (bounded) for the copies it issued beyond the `done' stages
+// this thread consumed, so no copy lands in shared memory after the exit.
+__device__ __forceinline__ void sweep_drain(const SweepArgs &a, unsigned long long *full, int D, int done,
+                                            int *issued, int *pdone)
+{
+	fg_set_err(a.err, FEMGPU_E_TIMEOUT);
+	for (int i = 0; i < SW_WAIT_LIMIT && !*(volatile int *)pdone; i++) __nanosleep(64);
+	int last = *(volatile int *)issued;
+	for (int q = done; q < last; q++) (void)mbar_wait(&full[q % D], (unsigned)((q / D) & 1));
+}
+
 // CW consumer warps (warps 0..CW-1) and one producer warp (warp CW).
 template <typename T, bool UPPER, int CW, bool FMA>
 __global__ void __launch_bounds__((CW + 1) * 32, 1)
@@ -209,39 +268,7 @@ k_sweep(SweepArgs a, const T *__restrict__ in, T *out)
 	__syncthreads();
 
 	if (warp == CW) {                                     // ---- producer warp
-		bool stop = false;
-		int s = 0;
-		unsigned ph = 0;                                  // phase of empty[s] to wait for
-		for (int base = sb0; base < sb1 && !stop; base += 32) {
-			// each lane fetches the offsets of one upcoming sub-block
-			int i = base + lane;
-			long long b0 = 0, b1 = 0;
-			int p0 = 0, vb = 0;
-			if (i < sb1) { b0 = a.blk_off[i]; b1 = a.blk_off[i + 1]; p0 = a.sb_in[i]; vb = a.sb_inb[i]; }
-			for (int j = 0; j < 32 && base + j < sb1; j++) {
-				long long B0 = __shfl_sync(0xffffffffu, b0, j), B1 = __shfl_sync(0xffffffffu, b1, j);
-				int P0 = __shfl_sync(0xffffffffu, p0, j), VB = __shfl_sync(0xffffffffu, vb, j);
-				int sb = base + j - sb0;                  // local sub-block index
-				int go = 1;
-				if (lane == 0) {
-					if (sb >= D && !mbar_wait_or_fail(&empty[s], ph, vfailed)) go = 0;
-					if (*vfailed) go = 0;
-					if (go) {
-						unsigned bb = (unsigned)(B1 - B0);
-						unsigned char *dst = stages + (unsigned)s * sbytes;
-						fence_proxy_async();
-						mbar_expect_tx(&full[s], bb + (unsigned)VB);
-						bulk_g2s(dst, a.prog + B0, bb, &full[s]);
-						if (VB) bulk_g2s(dst + bb, in + P0, (unsigned)VB, &full[s]);
-						*(volatile int *)&issued = sb + 1;
-					}
-				}
-				go = __shfl_sync(0xffffffffu, go, 0);
-				if (!go) { stop = true; break; }
-				if (++s == D) { s = 0; if (sb >= D) ph ^= 1u; else if (sb == D - 1) ph = 0; }
-			}
-		}
-		if (lane == 0) *(volatile int *)&pdone = 1;
+		sweep_producer(a, in, stages, sbytes, full, empty, D, sb0, sb1, lane, vfailed, &issued, &pdone, false);
 		return;
 	}
 
@@ -295,13 +322,7 @@ k_sweep(SweepArgs a, const T *__restrict__ in, T *out)
 		sb += j;
 		if (*vfailed) break;
 	}
-	if (*vfailed && ctid == 0) {
-		fg_set_err(a.err, FEMGPU_E_TIMEOUT);
-		// let the producer stop, then wait (bounded) for the copies it issued
-		for (int i = 0; i < SW_WAIT_LIMIT && !*(volatile int *)&pdone; i++) __nanosleep(64);
-		int last = *(volatile int *)&issued;
-		for (int q = sb; q < last; q++) (void)mbar_wait(&full[q % D], (unsigned)((q / D) & 1));
-	}
+	if (*vfailed && ctid == 0) sweep_drain(a, full, D, sb, &issued, &pdone);
 }
 
 // ------------------------------------------------ record layout (fixed width)
@@ -355,38 +376,7 @@ k_sweep_rec(SweepArgs a, const T *__restrict__ in, T *out)
 	__syncthreads();
 
 	if (warp == CW) {                                     // ---- producer warp
-		bool stop = false;
-		int s = 0;
-		unsigned ph = 0;
-		for (int base = sb0; base < sb1 && !stop; base += 32) {
-			int i = base + lane;
-			long long b0 = 0, b1 = 0;
-			int p0 = 0, vb = 0;
-			if (i < sb1) { b0 = a.blk_off[i]; b1 = a.blk_off[i + 1]; p0 = a.sb_in[i]; vb = a.sb_inb[i]; }
-			for (int j = 0; j < 32 && base + j < sb1; j++) {
-				long long B0 = __shfl_sync(0xffffffffu, b0, j), B1 = __shfl_sync(0xffffffffu, b1, j);
-				int P0 = __shfl_sync(0xffffffffu, p0, j), VB = __shfl_sync(0xffffffffu, vb, j);
-				int sb = base + j - sb0;
-				int go = 1;
-				if (lane == 0) {
-					if (sb >= D && !mbar_wait_or_fail(&empty[s], ph, vfailed)) go = 0;
-					if (*vfailed) go = 0;
-					if (go) {
-						unsigned bb = (unsigned)(B1 - B0);
-						unsigned char *dst = stages + (unsigned)s * sbytes;
-						fence_proxy_async();
-						mbar_expect_tx(&full[s], bb + (unsigned)VB);
-						bulk_g2s(dst, a.prog + B0, bb, &full[s]);
-						if (VB) bulk_g2s(dst + a.bvo, in + P0, (unsigned)VB, &full[s]);
-						*(volatile int *)&issued = sb + 1;
-					}
-				}
-				go = __shfl_sync(0xffffffffu, go, 0);
-				if (!go) { stop = true; break; }
-				if (++s == D) { s = 0; if (sb >= D) ph ^= 1u; else if (sb == D - 1) ph = 0; }
-			}
-		}
-		if (lane == 0) *(volatile int *)&pdone = 1;
+		sweep_producer(a, in, stages, sbytes, full, empty, D, sb0, sb1, lane, vfailed, &issued, &pdone, true);
 		return;
 	}
 
@@ -440,12 +430,7 @@ k_sweep_rec(SweepArgs a, const T *__restrict__ in, T *out)
 		sb += j;
 		if (*vfailed) break;
 	}
-	if (*vfailed && ctid == 0) {
-		fg_set_err(a.err, FEMGPU_E_TIMEOUT);
-		for (int i = 0; i < SW_WAIT_LIMIT && !*(volatile int *)&pdone; i++) __nanosleep(64);
-		int last = *(volatile int *)&issued;
-		for (int q = sb; q < last; q++) (void)mbar_wait(&full[q % D], (unsigned)((q / D) & 1));
-	}
+	if (*vfailed && ctid == 0) sweep_drain(a, full, D, sb, &issued, &pdone);
 }
 
 // ------------------------------------------- dataflow sweep (record layout)
@@ -503,38 +488,7 @@ k_sweep_df(SweepArgs a, const T *__restrict__ in, T *out)
 	__syncthreads();
 
 	if (warp == CW) {                                     // ---- producer warp
-		bool stop = false;
-		int s = 0;
-		unsigned ph = 0;
-		for (int base = sb0; base < sb1 && !stop; base += 32) {
-			int i = base + lane;
-			long long b0 = 0, b1 = 0;
-			int p0 = 0, vb = 0;
-			if (i < sb1) { b0 = a.blk_off[i]; b1 = a.blk_off[i + 1]; p0 = a.sb_in[i]; vb = a.sb_inb[i]; }
-			for (int j = 0; j < 32 && base + j < sb1; j++) {
-				long long B0 = __shfl_sync(0xffffffffu, b0, j), B1 = __shfl_sync(0xffffffffu, b1, j);
-				int P0 = __shfl_sync(0xffffffffu, p0, j), VB = __shfl_sync(0xffffffffu, vb, j);
-				int sb = base + j - sb0;
-				int go = 1;
-				if (lane == 0) {
-					if (sb >= D && !mbar_wait_or_fail(&empty[s], ph, vfailed)) go = 0;
-					if (*vfailed) go = 0;
-					if (go) {
-						unsigned bb = (unsigned)(B1 - B0);
-						unsigned char *dst = stages + (unsigned)s * sbytes;
-						fence_proxy_async();
-						mbar_expect_tx(&full[s], bb + (unsigned)VB);
-						bulk_g2s(dst, a.prog + B0, bb, &full[s]);
-						if (VB) bulk_g2s(dst + a.bvo, in + P0, (unsigned)VB, &full[s]);
-						*(volatile int *)&issued = sb + 1;
-					}
-				}
-				go = __shfl_sync(0xffffffffu, go, 0);
-				if (!go) { stop = true; break; }
-				if (++s == D) { s = 0; if (sb >= D) ph ^= 1u; else if (sb == D - 1) ph = 0; }
-			}
-		}
-		if (lane == 0) *(volatile int *)&pdone = 1;
+		sweep_producer(a, in, stages, sbytes, full, empty, D, sb0, sb1, lane, vfailed, &issued, &pdone, true);
 		return;
 	}
 
@@ -605,12 +559,7 @@ k_sweep_df(SweepArgs a, const T *__restrict__ in, T *out)
 		if (odef >= 0) { out[odef] = ydef; odef = -1; }
 	}
 	consumer_sync<CW>();
-	if (*vfailed && ctid == 0) {
-		fg_set_err(a.err, FEMGPU_E_TIMEOUT);
-		for (int i = 0; i < SW_WAIT_LIMIT && !*(volatile int *)&pdone; i++) __nanosleep(64);
-		int last = *(volatile int *)&issued;
-		for (int q = waited; q < last; q++) (void)mbar_wait(&full[q % D], (unsigned)((q / D) & 1));
-	}
+	if (*vfailed && ctid == 0) sweep_drain(a, full, D, waited, &issued, &pdone);
 }
 
 // Gather the sweep input into padded level order: in[ppos[i]] = (T) p[rows[i]].
