@@ -100,6 +100,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_transport_set_stream": [_vp, _vp],
         "femgpu_transport_info": [_vp, _vp],
         "femgpu_transport_ilu_blocks": [_vp, _vp, ctypes.c_int],
+        "femgpu_ilu_block_cut": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp],
         "femgpu_transport_get_pattern": [_vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_transport_build": [_vp, _vp, _vp, _vp],
         "femgpu_transport_precond_setup": [_vp, ctypes.c_int, _vp],
@@ -223,6 +224,21 @@ def _f64(a):
 
 def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def ilu_block_cut(IA, JA, P):
+    """First row of each block ILU(0) run (plus the row count) for a CSR
+    pattern with ascending columns, computed on the host exactly as a
+    transport context with ilu_blocks = P cuts its own (needs no GPU)."""
+    L = load()
+    IA = np.ascontiguousarray(IA, dtype=np.int32)
+    JA = np.ascontiguousarray(JA, dtype=np.int32)
+    n = IA.size - 1
+    first = np.zeros(max(min(P, n), 1) + 1, np.int32)
+    rc = L.femgpu_ilu_block_cut(n, _ptr(IA), _ptr(JA), int(P), _ptr(first))
+    if rc < 0:
+        raise FemGpuError(rc, "ilu_block_cut")
+    return first[: rc + 1]
 
 
 class SSTransport:

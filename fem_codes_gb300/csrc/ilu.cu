@@ -1422,6 +1422,17 @@ static int sweep_smem(const fg_sweep &sw, size_t tsize, int *D, int *stage_bytes
 	return (int)(fixed + (size_t)d * sb);
 }
 
+// Host only (no device call): the block ILU(0) cut of a CSR pattern, as
+// fg_ilu_prepare computes it.  first receives min(P, n) + 1 row boundaries.
+extern "C" int femgpu_ilu_block_cut(int n, const int *IA, const int *JA, int P, int *first)
+{
+	if (n <= 0 || !IA || !JA || !first) return FEMGPU_E_ARG;
+	std::vector<int> f;
+	(void)make_blocks(IA, JA, n, P, &f);
+	memcpy(first, f.data(), sizeof(int) * f.size());
+	return (int)f.size() - 1;
+}
+
 extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJA)
 {
 	int n = t->neq, rc, D, sb;

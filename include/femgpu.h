@@ -127,6 +127,11 @@ int femgpu_transport_info(const femgpu_transport *ctx, int *info);
  * FEMGPU_E_NOT_BUILT before the ILU(0) structure exists (CSR + ILU0 only). */
 int femgpu_transport_ilu_blocks(const femgpu_transport *ctx, int *first, int cap);
 
+/* The same cut for a CSR pattern (ascending columns per row) on the host, no
+ * device needed: returns the number of runs R = min(P, n) (1 when P <= 1) and
+ * writes R + 1 row boundaries to first. */
+int femgpu_ilu_block_cut(int n, const int *IA, const int *JA, int P, int *first);
+
 /* Copies of the device-built structure, for parity checks against the
  * reference (IA [neq+1], JA [nnz], CSR_by_Element [9*nel]; EDE: lm2 [2*nedge],
  * EDGE_by_Element [3*nel], order [3*nel]; node ids [nnodes]). NULL skips. */
