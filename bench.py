@@ -58,6 +58,7 @@ def parse(argv=None):
     ap.add_argument("--ilu-blocks", type=int, default=16,
                     help="0: ILU(0) of the whole matrix; P > 1: block ILU(0) over P row blocks")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-amg", action="store_true", help="skip the AMG-preconditioned leg")
     ap.add_argument("--workload", default="transport", choices=["transport", "euler", "ns"])
     ap.add_argument("--ns-n", type=int, default=256,
                     help="Navier-Stokes cavity cells per side (the 1024 of the full configuration takes ~70 s "
@@ -333,6 +334,8 @@ def run_ours(a):
     T.close()
     if not a.no_learned:
         line["learned"] = learned_leg(m, p, a, s)
+    if not a.no_amg:
+        line["amg"] = amg_leg(m, p, a, s)
     if rank == 0:
         line["matvec_compare"] = matvec_compare(m, p, s, peak)
     if rank == 0:
@@ -381,6 +384,49 @@ def learned_leg(m, p, a, s, steps=1):
     finally:
         T.close()
         net.close()
+    return out
+
+
+def amg_leg(m, p, a, s, steps=1):
+    """Time to solution of the same Picard step with the DPA AMG preconditioner
+    (amg_dpa.c: pairwise aggregation with 3 coarsening sweeps per level, beta -1,
+    SOR omega 1.0, 2 sweeps per side; the hierarchy is rebuilt on the host from
+    each step's matrix, as AMG_precond_setup does), FGMRES(kmax) in FP64 with at
+    most 25 restart cycles."""
+    import torch
+    import fem_codes_gb300 as fg
+    T = fg.SSTransport.from_problem(m, p, scheme="CSR", reorder=a.reorder, precond="AMG", kmax=a.kmax,
+                                    lmax=25, tol=1e-8, solver="FGMRES", precision="FP64")
+    T.set_stream(s.cuda_stream)
+    amg = fg.AMG(ncl=3, beta=-1.0, omega=1.0, nr=2)
+    out = {}
+    try:
+        T.set_amg(amg)
+
+        def step():
+            T.build_dev()
+            T.precond_setup_dev(2)
+            return T.solve_dev(raise_on_nonconvergence=False)
+        step()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        its, setup_s = [], 0.0
+        e0.record(s)
+        for _ in range(steps):
+            T.build_dev()
+            t0 = time.perf_counter()
+            T.precond_setup_dev(2)                      # host hierarchy (synchronises the stream)
+            setup_s += time.perf_counter() - t0
+            its.append(T.solve_dev(raise_on_nonconvergence=False))
+        e1.record(s)
+        torch.cuda.synchronize()
+        out = {"ms_per_step": e0.elapsed_time(e1) / steps, "setup_ms_per_step": 1e3 * setup_s / steps,
+               "gmres_iters": its, "true_rel_residual": T.true_residual(), "levels": amg.levels(),
+               "amg": "DPA pairwise aggregation, ncl 3, beta -1, SOR omega 1.0 x 2, one V-cycle per application"}
+    finally:
+        T.close()
+        amg.close()
     return out
 
 
