@@ -3,31 +3,38 @@
 //
 // The triangular sweeps have ~2.5*nx dependency levels after SYMRCM (5118
 // for a 2048x1024 grid) of a few hundred rows each, so they are bound by
-// per-level latency, not bandwidth.  They run in ONE thread block:
+// per-level latency, not bandwidth.  Each matrix block is swept by ONE
+// thread block:
 //   * at set-up, each sweep is compiled into a "program": every level is cut
-//     into sub-blocks of at most SW_SUB rows, each a 16-byte aligned block in
-//     ELL layout -- dependency codes, factor values (refreshed after every
-//     factorisation), output slots and, for the backward sweep, inverted
-//     pivots;
+//     into sub-blocks of at most SW_SUB rows, 16-byte aligned -- one record
+//     per row (dependency codes, output slot, factor values, the inverted
+//     pivot backward; k_sweep_rec / k_sweep_df) when no row has more than 16
+//     dependencies, else ELL arrays (k_sweep); factor values are refreshed
+//     after every factorisation;
 //   * one producer warp streams sub-blocks (and their slice of the input
 //     vector) into a ring of shared-memory stages with TMA bulk copies
 //     (cp.async.bulk, completion on a "full" mbarrier; stage reuse gated by an
 //     "empty" mbarrier the consumer warps arrive on);
 //   * consumer warps compute a level, publish its values in a shared-memory
 //     ring indexed by level-order position (older dependencies are re-read
-//     from global memory) and synchronise among themselves with one named
-//     barrier per level.
+//     from global memory) and synchronise either with one named barrier per
+//     level (k_sweep, k_sweep_rec) or through per-warp progress flags that a
+//     warp waits on only for the warps it reads from (k_sweep_df, the
+//     default for records).
 // Rows are computed in the reference's order (ascending columns) and the
 // FP64 variant rounds each operation separately, so its results are
-// bit-identical to the reference's sweeps.
+// bit-identical to the reference's sweeps; FGMRES uses the fused
+// multiply-subtract variant.
 //
-// Block ILU(0) (ilu_blocks = P > 0): the rows are cut into P contiguous
-// blocks of the (reordered) numbering and couplings between blocks are
-// dropped, so each block factorises and sweeps independently: its levels
-// form a contiguous run of the program (levels are numbered block by block)
-// and one thread block per matrix block runs them, P thread blocks at once.  Every wait is bounded: on timeout
-// the block records FEMGPU_E_TIMEOUT, waits (bounded) for the copies it has in
-// flight and returns.
+// Block ILU(0) (ilu_blocks = P > 1): the rows are cut into P contiguous runs
+// of the (reordered) numbering (make_blocks: by default at equal spans of the
+// full factor's dependency levels) and couplings between runs are dropped, so
+// each block factorises and sweeps independently: its levels form a
+// contiguous run of the program (levels are numbered block by block) and one
+// thread block per matrix block runs them, P thread blocks at once.  The
+// factorisation runs one thread-block cluster per matrix block.  Every wait is
+// bounded: on timeout the block records FEMGPU_E_TIMEOUT, waits (bounded) for
+// the copies it has in flight and returns.
 #include "fg_common.cuh"
 #include <string.h>
 #include <vector>
@@ -449,10 +456,9 @@ k_sweep_rec(SweepArgs a, const T *__restrict__ in, T *out)
 // level waits for its own global stores; a dependency read back from global
 // memory therefore waits for its producer's next level (whose release covers
 // those stores), and the program keeps such dependencies at least two levels
-// back.  A warp
-// releases a stage (mbarrier of CW arrivals) as soon as its rows are in
-// registers.  Header: {rows, sub-blocks of the level, first position, far
-// flag}, then CW need tables of 16 bytes, then the records.
+// back.  A warp releases a stage (mbarrier of CW arrivals) as soon as its
+// rows are in registers.  Header: {rows, sub-blocks of the level, first
+// position, far flag}, then CW need tables of 16 bytes, then the records.
 #define DF_HDR (16 + SW2_CW * 16)
 
 template <typename T, bool UPPER, bool FMA, int W>
