@@ -553,18 +553,20 @@ def read_traffic(kind):
 
 
 def launches_estimate(a, iters):
-    """Kernel launches of the timed steps: build (2) + factor (5) + per FGMRES
-    iteration (precond 3, matvec 1, MGS j+2, scale, Givens) + per cycle (4)."""
+    """Kernel launches of the timed steps (a FGMRES cycle enqueues all kmax
+    steps; those past convergence are predicated off but launched): build 2
+    (element build, CSR assembly with the RHS) + factor 5 (cluster elimination,
+    4 program refreshes) + per cycle 5 (residual start 3, back-substitution and
+    update 2) + per step (preconditioner 3: gather and two sweeps; matvec 1;
+    classical Gram-Schmidt 3, re-orthogonalised in restarted cycles 6; scale;
+    Givens) + the true-residual check 2."""
     kmax = a.kmax
     tot = 0
     for it in iters:
-        it = int(it)
-        cyc = (it + kmax - 1) // kmax
-        inner = sum(3 + 1 + (j % kmax) + 2 + 2 for j in range(it))
-        # predicated-off iterations of the last cycle are launched too
-        pad = cyc * kmax - it
-        inner += sum(3 + 1 + ((it + q) % kmax) + 2 + 2 for q in range(pad))
-        tot += 2 + 5 + inner + 5 * cyc + 1
+        cyc = max(1, (int(it) + kmax - 1) // kmax)
+        for c in range(cyc):
+            tot += 5 + kmax * (3 + 1 + (3 if c == 0 else 6) + 2)
+        tot += 2 + 5 + 2
     return tot
 
 
