@@ -106,6 +106,8 @@ def test_ilu_levels_natural_grid(lib):
 def test_bad_arguments_rejected_without_gpu(lib):
     assert lib.femgpu_symrcm(0, None, None, None) == -1
     assert lib.femgpu_ilu_levels(-3, None, None, 1) == -1
+    assert lib.femgpu_ilu_block_cut(0, None, None, 4, None) == -1
+    assert lib.femgpu_transport_ilu_blocks(None, None, 0) == -1
 
 
 def test_ns_bad_options_rejected_without_gpu(lib):
