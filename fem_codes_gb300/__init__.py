@@ -100,7 +100,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_transport_set_stream": [_vp, _vp],
         "femgpu_transport_info": [_vp, _vp],
         "femgpu_transport_ilu_blocks": [_vp, _vp, ctypes.c_int],
-        "femgpu_ilu_block_cut": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp],
+        "femgpu_ilu_block_cut": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, ctypes.c_int],
         "femgpu_transport_get_pattern": [_vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_transport_build": [_vp, _vp, _vp, _vp],
         "femgpu_transport_precond_setup": [_vp, ctypes.c_int, _vp],
@@ -235,7 +235,7 @@ def ilu_block_cut(IA, JA, P):
     JA = np.ascontiguousarray(JA, dtype=np.int32)
     n = IA.size - 1
     first = np.zeros(max(min(P, n), 1) + 1, np.int32)
-    rc = L.femgpu_ilu_block_cut(n, _ptr(IA), _ptr(JA), int(P), _ptr(first))
+    rc = L.femgpu_ilu_block_cut(n, _ptr(IA), _ptr(JA), int(P), _ptr(first), first.size)
     if rc < 0:
         raise FemGpuError(rc, "ilu_block_cut")
     return first[: rc + 1]

@@ -1429,12 +1429,27 @@ static int sweep_smem(const fg_sweep &sw, size_t tsize, int *D, int *stage_bytes
 }
 
 // Host only (no device call): the block ILU(0) cut of a CSR pattern, as
-// fg_ilu_prepare computes it.  first receives min(P, n) + 1 row boundaries.
-extern "C" int femgpu_ilu_block_cut(int n, const int *IA, const int *JA, int P, int *first)
+// fg_ilu_prepare computes it.  first receives R + 1 row boundaries, R =
+// max(min(P, n), 1); cap is the room in first.  The pattern is checked first
+// (IA[0] == 0, IA non-decreasing, every column in 0..n-1, columns ascending in
+// each row): the cut's level scan indexes by column and stops at the first
+// column at or past the row.
+extern "C" int femgpu_ilu_block_cut(int n, const int *IA, const int *JA, int P, int *first, int cap)
 {
 	if (n <= 0 || !IA || !JA || !first) return FEMGPU_E_ARG;
+	const int R = std::max(std::min(P, n), 1);
+	if (cap < R + 1) return FEMGPU_E_ARG;
+	if (IA[0] != 0) return FEMGPU_E_ARG;
+	for (int i = 0; i < n; i++) {
+		if (IA[i + 1] < IA[i]) return FEMGPU_E_ARG;
+		for (int k = IA[i]; k < IA[i + 1]; k++) {
+			if (JA[k] < 0 || JA[k] >= n) return FEMGPU_E_ARG;
+			if (k > IA[i] && JA[k] <= JA[k - 1]) return FEMGPU_E_ARG;
+		}
+	}
 	std::vector<int> f;
 	(void)make_blocks(IA, JA, n, P, &f);
+	if ((int)f.size() > cap) return FEMGPU_E_ARG;
 	memcpy(first, f.data(), sizeof(int) * f.size());
 	return (int)f.size() - 1;
 }

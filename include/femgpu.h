@@ -7,8 +7,10 @@
  * function pointers with struct arguments (FemFunctionsType /
  * FemOtherFunctionsType, 01_SS_Transport_Equation/2D/01_CommonFiles/
  * SSTranspEquation.h:97-121); this ABI exposes the same operations with plain
- * pointers and sizes, so a thin shim assigns them to those pointers (see
- * INTEGRATION.md).  Every entry point returns 0 or a negative FEMGPU_E* code;
+ * pointers and sizes, so a thin shim assigns them to those pointers (the shims
+ * for the transport, Euler and Navier-Stokes drivers are in
+ * fem_codes_gb300/shims/).  Every
+ * entry point returns 0 or a negative FEMGPU_E* code;
  * none aborts the process and none traps the GPU.
  *
  * Host-buffer entry points (no suffix) take arrays in host memory laid out
@@ -127,10 +129,12 @@ int femgpu_transport_info(const femgpu_transport *ctx, int *info);
  * FEMGPU_E_NOT_BUILT before the ILU(0) structure exists (CSR + ILU0 only). */
 int femgpu_transport_ilu_blocks(const femgpu_transport *ctx, int *first, int cap);
 
-/* The same cut for a CSR pattern (ascending columns per row) on the host, no
- * device needed: returns the number of runs R = min(P, n) (1 when P <= 1) and
- * writes R + 1 row boundaries to first. */
-int femgpu_ilu_block_cut(int n, const int *IA, const int *JA, int P, int *first);
+/* The same cut for a CSR pattern on the host, no device needed: returns the
+ * number of runs R = max(min(P, n), 1) and writes R + 1 row boundaries to
+ * first (cap = room in first; FEMGPU_E_ARG when cap < R + 1).  The pattern
+ * must have IA[0] = 0, non-decreasing IA, columns in 0..n-1 and strictly
+ * ascending columns in every row; anything else returns FEMGPU_E_ARG. */
+int femgpu_ilu_block_cut(int n, const int *IA, const int *JA, int P, int *first, int cap);
 
 /* Copies of the device-built structure, for parity checks against the
  * reference (IA [neq+1], JA [nnz], CSR_by_Element [9*nel]; EDE: lm2 [2*nedge],
@@ -456,16 +460,17 @@ int femgpu_csrmv_f32(int n, const int *IA, const int *JA, const float *AA,
 		const float *P, float *Q, void *stream);
 
 /* Allocation-free residual norm.  No counterpart in the reference: it exists
- * for callers that cannot call cudaMalloc -- code running inside a CUDA graph
- * capture or a memory-pool-restricted host application, or a driver that
- * must not grow device memory between steps.  Computes, for a CSR system in
- * device memory, out2[0] = ||F - A u||^2 and out2[1] = ||F||^2 (out2: two
- * doubles of device memory), the quantity femgpu_transport_true_residual
- * reports.  Its block partial sums live in a fixed static device array
- * (32 KB, held by every GPU that loads the library until exit), so
- * n <= 4,194,304 rows; larger n returns FEMGPU_E_ARG.  The first call on a
- * device looks up that array's device address (make it before any stream
- * capture).  All calls share the array: calls that overlap on the GPU race,
+ * for callers that cannot call cudaMalloc -- a host application that hands the
+ * library a fixed device-memory budget, or a driver that must not grow device
+ * memory between steps.  Computes, for a CSR system in device memory,
+ * out2[0] = ||F - A u||^2 and out2[1] = ||F||^2 (out2: two doubles of device
+ * memory), the quantity femgpu_transport_true_residual reports.  Its block
+ * partial sums live in a fixed static device array (32 KB, held by every GPU
+ * that loads the library until exit), so n <= 4,194,304 rows; larger n returns
+ * FEMGPU_E_ARG.  The first call on a device looks up that array's device
+ * address with the device current and keeps it for the process (make that
+ * first call before any stream capture; after cudaDeviceReset the kept address
+ * is stale).  All calls share the array: calls that overlap on the GPU race,
  * so serialise them. */
 int femgpu_csr_resnorm_noalloc(int n, const int *IA, const int *JA, const double *AA,
 		const double *u, const double *F, double *out2, void *stream);

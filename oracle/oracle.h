@@ -95,6 +95,9 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 void orc_get_times(double *t);
 /* Wall time (seconds) of each of the first n Picard iterations of that run. */
 void orc_get_step_times(double *t, int n);
+void orc_set_refine(double to, double tol, int maxrounds);
+void orc_set_refine_window(int from, double budget_s);
+void orc_get_refine(double *res, int *rounds, int n);
 
 /* Operator application out = Op(in) on vectors of neq+1 entries. */
 typedef void (*orc_apply_fn)(const void *ctx, double *in, double *out);

@@ -18,19 +18,26 @@ _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _lib = None
 
 
-def build() -> str:
-    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
-    return os.path.join(HERE, "liboracle.so")
+_libfast = None
 
 
-def lib() -> ctypes.CDLL:
-    global _lib
-    if _lib is None:
-        path = os.path.join(HERE, "liboracle.so")
+def build(name: str = "liboracle.so") -> str:
+    subprocess.run(["make", "-s", "-C", HERE, name], check=True)
+    return os.path.join(HERE, name)
+
+
+def lib(fast: bool = False) -> ctypes.CDLL:
+    """The oracle library: liboracle.so (bit-stable FP64, the parity checker)
+    or, with fast=True, liboracle_fast.so (the same sources -Ofast, as the
+    reference's Makefiles build it; the timed CPU baseline)."""
+    global _lib, _libfast
+    if (_libfast if fast else _lib) is None:
+        name = "liboracle_fast.so" if fast else "liboracle.so"
+        path = os.path.join(HERE, name)
         srcs = [os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith((".c", ".h"))
                 and not f.startswith("ref_")]
         if not os.path.exists(path) or any(os.path.getmtime(path) < os.path.getmtime(f) for f in srcs):
-            build()
+            build(name)
         L = ctypes.CDLL(path)
         L.orc_transport_run.restype = ctypes.c_int
         L.orc_transport_run.argtypes = [
@@ -78,8 +85,17 @@ def lib() -> ctypes.CDLL:
         L.orc_get_times.argtypes = [_dp]
         L.orc_get_step_times.restype = None
         L.orc_get_step_times.argtypes = [_dp, ctypes.c_int]
-        _lib = L
-    return _lib
+        L.orc_set_refine.restype = None
+        L.orc_set_refine.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_int]
+        L.orc_set_refine_window.restype = None
+        L.orc_set_refine_window.argtypes = [ctypes.c_int, ctypes.c_double]
+        L.orc_get_refine.restype = None
+        L.orc_get_refine.argtypes = [_dp, _ip, ctypes.c_int]
+        if fast:
+            _libfast = L
+        else:
+            _lib = L
+    return _libfast if fast else _lib
 
 
 def _c(a, dt):
@@ -88,9 +104,18 @@ def _c(a, dt):
 
 def run_transport(x, y, node_type, vert, k, gamma, beta, fsrc, upresc, scheme="CSR",
                   reord="NOT", precond="ILU0", shock="CAU", hshock="2sqrtArea", outflow="NOT",
-                  kmax=30, lmax=1000, tol=1e-8, npicard=3, nonlin_tol=0.0, Pin=None):
-    """Full steady-transport run; same outputs as the reference harness."""
-    L = lib()
+                  kmax=30, lmax=1000, tol=1e-8, npicard=3, nonlin_tol=0.0, Pin=None, fast=False,
+                  refine_to=0.0, refine_tol=1e-12, refine_max=40, refine_from=0, refine_budget_s=0.0):
+    """Full steady-transport run; same outputs as the reference harness.
+    fast: the -Ofast build.  refine_to > 0: the to-solution variant (every
+    Picard solve from step refine_from on refined with the reference's pgmres
+    until the true relative residual is <= refine_to, the Picard loop ending
+    once refine_budget_s seconds went into refined steps (0: no bound));
+    out["refine"] then holds, per Picard step, the final true residual (-1 for
+    unrefined steps) and the refinement rounds."""
+    L = lib(fast)
+    L.orc_set_refine(float(refine_to), float(refine_tol), int(refine_max))
+    L.orc_set_refine_window(int(refine_from), float(refine_budget_s))
     nn, ne = len(x), len(vert)
     node_type = _c(node_type, np.int32)
     neq_ub = int((node_type >= 1).sum())
@@ -119,12 +144,18 @@ def run_transport(x, y, node_type, vert, k, gamma, beta, fsrc, upresc, scheme="C
         hshock.encode(), outflow.encode(), kmax, lmax, tol, npicard, nonlin_tol,
         info, node_id, etype, IA, JA, sbe, order, Afirst, Ffirst, Fprec, Pin, Qmv, Zpc,
         uhist, iters)
+    L.orc_set_refine(0.0, 0.0, 0)
     if nit < 0:
         raise RuntimeError(f"oracle run failed ({nit})")
     neq, nnz, nedge, bw = (int(v) for v in info)
     out = dict(neq=neq, nnzero=nnz, nedge=nedge, bandwidth=bw, npicard_run=nit,
                node_id=node_id, etype=etype, Ffirst=Ffirst, Fprec=Fprec, Pin=Pin, Qmv=Qmv,
                Zpc=Zpc, uhist=uhist[: nit * (neq + 1)].reshape(nit, neq + 1), iters=iters[:nit])
+    if refine_to > 0:
+        res = np.zeros(max(nit, 1))
+        rounds = np.zeros(max(nit, 1), np.int32)
+        L.orc_get_refine(res, rounds, max(nit, 1))
+        out["refine"] = {"true_rel_residual": res[:nit], "rounds": rounds[:nit]}
     if scheme.upper() == "CSR":
         out.update(IA=IA[: neq + 1], JA=JA[:nnz], sbe=sbe.reshape(ne, 9), Afirst=Afirst[: nnz + 1])
     elif scheme.upper() == "EDE":
@@ -182,10 +213,10 @@ def block_ops(ndof, nnodes, vert, node_id, neq, A, P, p, F):
     return out
 
 
-def last_times(npicard=0):
+def last_times(npicard=0, fast=False):
     """(phase times [setup, build, precond_setup, solve], per-step times) of
     the last run_transport, in seconds."""
-    L = lib()
+    L = lib(fast)
     t = np.zeros(4)
     L.orc_get_times(t)
     s = np.zeros(max(npicard, 1))
@@ -338,10 +369,11 @@ def euler_build(x, y, vert, node_id, neq, upresc, u, du, gamma=1.4, alpha=0.5, d
 
 
 def euler_predictor(x, y, vert, node_id, neq, upresc, u0, nsteps, ncorr=2, gamma=1.4, alpha=0.5,
-                    dt=1e-3, stab_tol=1e-6, kmax=30, lmax=100, tol=1e-8, mach=1.0, dimensionless=False):
+                    dt=1e-3, stab_tol=1e-6, kmax=30, lmax=100, tol=1e-8, mach=1.0, dimensionless=False,
+                    fast=False):
     """Predictor_Old with StopByIterations: (u after each step [nsteps, neq+1],
-    GMRES iterations [nsteps, ncorr])."""
-    L = lib()
+    GMRES iterations [nsteps, ncorr]); fast: the -Ofast build (timing)."""
+    L = lib(fast)
     p, keep = _euler(x, y, vert, node_id, neq, upresc, gamma, alpha, dt, stab_tol, mach, dimensionless)
     u = np.array(u0, dtype=np.float64)
     uhist = np.zeros((nsteps, neq + 1))

@@ -21,6 +21,46 @@ static double g_times[4];
 #define ORC_MAX_STEPS 256
 static double g_step[ORC_MAX_STEPS];    /* wall time of each Picard iteration */
 
+/* To-solution variant of the CPU baseline (no reference counterpart): when
+ * g_refine_to > 0, every Picard solve is followed by host-checked iterative
+ * refinement with the reference's own solver -- r = F - A u in FP64, the
+ * left-preconditioned correction system (M^-1 A) d = M^-1 r solved by the same
+ * pgmres (at the loosest tolerance expected to reach the target, no tighter
+ * than g_refine_tol), u += d -- until the true relative residual
+ * ||F - A u|| / ||F|| is at most g_refine_to (or g_refine_max rounds).  The
+ * reference's own stop (pgmres.c:49-53,184) bounds only the preconditioned
+ * residual, which at 2048x1024 leaves a true residual near 0.5. */
+static double g_refine_to = 0.0, g_refine_tol = 1e-12;
+static int g_refine_max = 40;
+/* Refinement starts at Picard step g_refine_from (0-based; earlier steps stop
+ * where the reference stops), and once g_refine_budget seconds have gone into
+ * refined steps the Picard loop ends after the current step (0: no bound). */
+static int g_refine_from = 0;
+static double g_refine_budget = 0.0;
+static double g_refine_res[ORC_MAX_STEPS];   /* true residual after each Picard solve */
+static int g_refine_its[ORC_MAX_STEPS];      /* refinement rounds of each Picard solve */
+
+void orc_set_refine(double to, double tol, int maxrounds)
+{
+	g_refine_to = to;
+	g_refine_tol = tol > 0 ? tol : 1e-12;
+	g_refine_max = maxrounds > 0 ? maxrounds : 40;
+	g_refine_from = 0;
+	g_refine_budget = 0.0;
+}
+
+void orc_set_refine_window(int from, double budget_s)
+{
+	g_refine_from = from > 0 ? from : 0;
+	g_refine_budget = budget_s > 0 ? budget_s : 0.0;
+}
+
+void orc_get_refine(double *res, int *rounds, int n)
+{
+	int i;
+	for (i = 0; i < n && i < ORC_MAX_STEPS; i++) { res[i] = g_refine_res[i]; rounds[i] = g_refine_its[i]; }
+}
+
 static double now_s(void)
 {
 	struct timespec ts;
@@ -784,6 +824,43 @@ int orc_pgmres_cb(int neq, orc_apply_fn mv, orc_apply_fn prec, const void *ctx, 
 	return orc_pgmres(&o, kmax, lmax, tol, B, X);
 }
 
+/* The refinement loop of the to-solution variant (see g_refine_to): returns
+ * the final true relative residual; *its accumulates the pgmres iterations.
+ * refine == 0: only the true residual of the reference's own solution. */
+static double refine_solve(const orc_op *o, double *u, const double *Fraw, int kmax, int lmax, double tol,
+                           int *its, int *rounds, int refine)
+{
+	int n = o->neq, k, r;
+	double *v = malloc(((size_t)n + 1) * sizeof(double)), *q = malloc(((size_t)n + 1) * sizeof(double));
+	double *d = malloc(((size_t)n + 1) * sizeof(double)), nb, rel = 0.0, prev = 0.0, ratio = 1.0, tr = tol;
+	nb = sqrt(orc_ddot(n, Fraw, Fraw));
+	for (r = 0; ; r++) {
+		memcpy(v, u, ((size_t)n + 1) * sizeof(double));
+		v[n] = 0.0;
+		op_mv(o, v, q);
+		for (k = 0; k < n; k++) q[k] = Fraw[k] - q[k];
+		q[n] = 0.0;
+		rel = nb > 0 ? sqrt(orc_ddot(n, q, q)) / nb : 0.0;
+		if (!refine || rel <= g_refine_to || r >= g_refine_max || !(rel == rel)) break;
+		/* The loosest pgmres tolerance expected to reach the target: the last
+		 * solve reduced the true residual by (rel/prev) at preconditioned
+		 * tolerance tr, so the true/preconditioned ratio is about
+		 * (rel/prev)/tr; aim at half the target, within [g_refine_tol, 0.5]. */
+		ratio = r == 0 ? rel / tol : (rel / prev) / tr;
+		if (!(ratio >= 1.0)) ratio = 1.0;
+		tr = 0.5 * g_refine_to / rel / ratio;
+		if (tr < g_refine_tol) tr = g_refine_tol;
+		if (tr > 0.5) tr = 0.5;
+		prev = rel;
+		op_prec(o, q, q);                       /* the correction system's RHS, M^-1 r */
+		*its += orc_pgmres(o, kmax, lmax, tr, q, d);
+		for (k = 0; k < n; k++) u[k] += d[k];
+	}
+	*rounds = r;
+	free(v); free(q); free(d);
+	return rel;
+}
+
 /* Diag_precond_{CSR,EBE,EDE}_setup.c: extract the diagonal, invert, F *= 1/D. */
 static void diag_setup(orc_op *o, double *invDiag, double *F)
 {
@@ -846,7 +923,7 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 	orc_op o;
 	int *lm = malloc(3 * (size_t)nel * sizeof(int)), neq, I, it = 0;
 	size_t nA;
-	double *A, *F, *u, *uold, *LU = NULL, *Dinv = NULL, *invDiag = NULL, err = 100.0;
+	double *A, *F, *u, *uold, *LU = NULL, *Dinv = NULL, *invDiag = NULL, *Fraw = NULL, err = 100.0;
 
 	double t0 = now_s(), t1;
 	memset(&t, 0, sizeof t);
@@ -903,16 +980,20 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 	uold = calloc((size_t)neq + 1, sizeof(double));
 	if (o.prec == 1) { LU = calloc(nA, sizeof(double)); Dinv = calloc((size_t)neq + 1, sizeof(double)); }
 	if (o.prec == 2) invDiag = calloc((size_t)neq + 1, sizeof(double));
+	if (g_refine_to > 0) Fraw = calloc((size_t)neq + 1, sizeof(double));
 	o.A = A; o.LU = LU; o.Dinv = Dinv;
 	t1 = now_s();
 	g_times[0] = t1 - t0;
 
-	while (it < npicard && (nonlin_tol <= 0 || err > nonlin_tol)) {
+	double refined_s = 0.0;
+	while (it < npicard && (nonlin_tol <= 0 || err > nonlin_tol) &&
+	       !(g_refine_to > 0 && g_refine_budget > 0 && refined_s > g_refine_budget)) {
 		double tstep = now_s();
 		it++;
 		memcpy(uold, u, (size_t)neq * sizeof(double));
 		t0 = tstep;
 		orc_build_supg(&t, u, A, F);
+		if (Fraw) memcpy(Fraw, F, ((size_t)neq + 1) * sizeof(double));
 		t1 = now_s();
 		g_times[1] += t1 - t0;
 		if (it == 1) {
@@ -938,7 +1019,15 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 		}
 		t0 = now_s();
 		iters[it-1] = orc_pgmres(&o, kmax, lmax, tol, F, u);
+		if (g_refine_to > 0 && it - 1 < ORC_MAX_STEPS) {
+			int rounds = 0;
+			double rel = refine_solve(&o, u, Fraw, kmax, lmax, tol, &iters[it-1], &rounds,
+			                          it - 1 >= g_refine_from);
+			g_refine_res[it-1] = rel;
+			g_refine_its[it-1] = rounds;
+		}
 		t1 = now_s();
+		if (g_refine_to > 0 && it - 1 >= g_refine_from) refined_s += t1 - tstep;
 		g_times[3] += t1 - t0;
 		if (it - 1 < ORC_MAX_STEPS) g_step[it-1] = t1 - tstep;
 		memcpy(uhist + (size_t)(it-1)*((size_t)neq + 1), u, ((size_t)neq + 1) * sizeof(double));
@@ -948,7 +1037,7 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 			if (I == 0 || d > err) err = d;
 		}
 	}
-	free(lm); free(A); free(F); free(u); free(uold); free(LU); free(Dinv); free(invDiag);
+	free(lm); free(A); free(F); free(u); free(uold); free(LU); free(Dinv); free(invDiag); free(Fraw);
 	return it;
 }
 

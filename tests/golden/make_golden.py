@@ -7,7 +7,8 @@ steady Navier-Stokes VMS build and damped Newton (libfemref_ns.so,
 oracle/ref_ns_harness.c) and the double-pairwise AMG preconditioner
 (libfemref_amg.so, oracle/ref_amg_harness.c).
 
-Usage:  python tests/golden/make_golden.py        (writes tests/golden/*.npz)
+Usage:  python tests/golden/make_golden.py [case ...]   (writes tests/golden/*.npz;
+        with case names, only those steady-transport cases)
 
 The fixtures hold the inputs (mesh, node types, coefficient arrays evaluated by
 the reference's plug-in callbacks) and every output the harness dumps: CSR
@@ -132,6 +133,11 @@ CASES = {
                                                        npicard=1)),
     "hemker12_ede_diag": (12, 12, 0.0, "inflow", dict(problem="HEMKER", scheme="EDE", precond="Diag",
                                                       npicard=1)),
+    # the plain-method configuration itself: 64x64 cells, CSR, ILU(0)-GMRES(30)
+    # to 1e-8 (1000 restarts), the Picard loop run to its cap of 51 iterations
+    # (Process.c:34; the iteration stagnates near max|du| = 0.04)
+    "c1_skew64_csr_ilu0_51": (64, 64, 0.0, "inflow", dict(scheme="CSR", reord="NOT", precond="ILU0", kmax=30,
+                                                         lmax=1000, npicard=51)),
 }
 
 
@@ -417,13 +423,18 @@ def main_amg():
         print(f"{name}: n={n} nnz={nnz} levels={sizes} gmres={it}")
 
 
-def main():
-    main_amg()
-    main_ns()
-    main_euler()
-    main_blocks()
+def main(only=()):
+    """Every fixture, or (names given on the command line) only those
+    steady-transport cases."""
+    if not only:
+        main_amg()
+        main_ns()
+        main_euler()
+        main_blocks()
     lib = load_ref()
     for name, (nx, ny, pert, rule, kw) in CASES.items():
+        if only and name not in only:
+            continue
         mesh = structured_mesh(nx, ny, perturb=pert, seed=1234)
         ntype = node_types(mesh, rule)
         out = run_ref(lib, mesh, ntype, **kw)
@@ -438,4 +449,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

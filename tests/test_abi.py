@@ -106,8 +106,46 @@ def test_ilu_levels_natural_grid(lib):
 def test_bad_arguments_rejected_without_gpu(lib):
     assert lib.femgpu_symrcm(0, None, None, None) == -1
     assert lib.femgpu_ilu_levels(-3, None, None, 1) == -1
-    assert lib.femgpu_ilu_block_cut(0, None, None, 4, None) == -1
+    assert lib.femgpu_ilu_block_cut(0, None, None, 4, None, 0) == -1
     assert lib.femgpu_transport_ilu_blocks(None, None, 0) == -1
+
+
+def test_block_cut_checks_capacity_and_pattern(lib):
+    """femgpu_ilu_block_cut writes R + 1 = max(min(P, n), 1) + 1 ints: a
+    buffer with less room, and patterns its level scan cannot read (a column
+    out of range, columns not ascending, IA not starting at 0 or decreasing),
+    are rejected before anything is written."""
+    IA, JA = _pattern(12, 8)
+    n = IA.size - 1
+    vp = ctypes.c_void_p
+
+    def cut(IA_, JA_, P, cap):
+        first = np.full(cap + 1, -7, np.int32)
+        rc = lib.femgpu_ilu_block_cut(IA_.size - 1, IA_.ctypes.data_as(vp), JA_.ctypes.data_as(vp), P,
+                                      first.ctypes.data_as(vp), cap)
+        return rc, first
+
+    rc, first = cut(IA, JA, 4, 5)
+    assert rc == 4 and first[0] == 0 and first[4] == n and first[5] == -7
+    assert cut(IA, JA, 4, 4)[0] == -1                  # room for 4 boundaries, 5 needed
+    assert cut(IA, JA, 0, 2)[0] == 1                   # P <= 0: one run, 2 ints
+    assert cut(IA, JA, 0, 1)[0] == -1
+    bad = JA.copy()
+    bad[3] = -1
+    assert cut(IA, bad, 4, 5)[0] == -1                 # negative column
+    bad = JA.copy()
+    bad[3] = n
+    assert cut(IA, bad, 4, 5)[0] == -1                 # column past the last row
+    r = next(i for i in range(n) if IA[i + 1] - IA[i] >= 2)
+    bad = JA.copy()
+    bad[IA[r]], bad[IA[r] + 1] = bad[IA[r] + 1], bad[IA[r]]
+    assert cut(IA, bad, 4, 5)[0] == -1                 # columns not ascending
+    badIA = IA.copy()
+    badIA[0] = 1
+    assert cut(badIA, JA, 4, 5)[0] == -1
+    badIA = IA.copy()
+    badIA[5] = badIA[4] - 1
+    assert cut(badIA, JA, 4, 5)[0] == -1
 
 
 def test_ns_bad_options_rejected_without_gpu(lib):
