@@ -158,6 +158,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_ns_build_dev": [_vp],
         "femgpu_ns_precond_setup": [_vp, _vp],
         "femgpu_ns_solve": [_vp, _vp, _vp, _ip],
+        "femgpu_ns_set_tol": [_vp, ctypes.c_double],
         "femgpu_ns_newton": [_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp],
         "femgpu_ns_csr": [_vp, _vp, _vp, _vp, _vp],
     }.items():

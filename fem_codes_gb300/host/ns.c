@@ -319,6 +319,13 @@ static int solve(femgpu_ns *c, const double *B, double *X, int *iters)
 	return rc;
 }
 
+int femgpu_ns_set_tol(femgpu_ns *c, double tol)
+{
+	if (!c || !(tol > 0.0)) return FEMGPU_E_ARG;
+	c->tol = tol;
+	return 0;
+}
+
 int femgpu_ns_solve(femgpu_ns *c, const double *B_host, double *X_host, int *iters)
 {
 	int it = 0, rc;

@@ -356,6 +356,10 @@ int femgpu_ns_precond_setup(femgpu_ns *ctx, double *F_host);
 /* pgmres (6-argument form) on the 3-dof block EBE operator: X solves
  * A X = B (B_host NULL: the context's F) to the current forcing term. */
 int femgpu_ns_solve(femgpu_ns *ctx, const double *B_host, double *X_host, int *iters);
+/* The relative tolerance of the next femgpu_ns_solve calls: the forcing term
+ * that the reference's Process keeps in Parameters->SolverTolerance
+ * (eta_newton.c, Process.c:118-140); femgpu_ns_newton sets its own. */
+int femgpu_ns_set_tol(femgpu_ns *ctx, double tol);
 /* Process.c:62-194 from u = 0: at most maxit damped-Newton iterations (and
  * the reference's 2000 cap), stopping when ||F|| <= tol_nl ||F_0||.  u_host
  * [neq+1] receives the solution; uhist [maxit*(neq+1)], normF, w [maxit],

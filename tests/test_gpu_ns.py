@@ -4,10 +4,12 @@ the 3-dof block EBE operator, Process's damped Newton) against the
 reference's own outputs (tests/golden/ns_*.npz) and the oracle.
 
 Bars: element matrices and residuals of consecutive builds are
-bit-identical; Newton iterates and residual norms agree to a relative 1e-6
+bit-identical; Newton iterates and residual norms agree to a relative 1e-8
 (the device sums dot products in another order than ddot, which moves the
-GMRES iterates and the forcing terms in the last bits), damping factors
-exactly and GMRES counts within 3."""
+GMRES iterates and the forcing terms in the last bits: measured on GB300,
+with the same GMRES counts in every Newton iteration, the iterates differ by
+at most 6e-15 and ||F|| by 5e-12, relative), damping factors exactly and
+GMRES counts within 3."""
 import glob
 import os
 
@@ -21,6 +23,7 @@ from fem_codes_gb300.mesh import cavity_problem, structured_mesh
 pytestmark = pytest.mark.gpu
 
 CASES = sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "ns_*.npz")))
+SOL_RTOL = 1e-8
 
 
 def _load(name):
@@ -68,8 +71,8 @@ def test_ns_newton_vs_reference(gpu_lib, name):
         u, uh, nF, w, its = ns.Process(int(g["maxit"]))
     assert len(nF) == len(g["normF"])
     assert np.array_equal(w, g["w"])
-    assert _rel(nF, g["normF"]) < 1e-6
-    assert _rel(uh, g["uhist"]) < 1e-6
+    assert _rel(nF, g["normF"]) < SOL_RTOL
+    assert _rel(uh, g["uhist"]) < SOL_RTOL
     assert np.abs(its.astype(int) - g["gmres"].astype(int)).max() <= 3
     assert np.array_equal(u, uh[-1])
 
@@ -101,8 +104,8 @@ def test_ns_csr_ilu0_newton_vs_reference(gpu_lib, name):
         u, uh, nF, w, its = ns.Process(int(g["maxit"]))
     assert len(nF) == len(g["csr_normF"])
     assert np.array_equal(w, g["csr_w"])
-    assert _rel(nF, g["csr_normF"]) < 1e-6
-    assert _rel(uh, g["csr_uhist"]) < 1e-6
+    assert _rel(nF, g["csr_normF"]) < SOL_RTOL
+    assert _rel(uh, g["csr_uhist"]) < SOL_RTOL
     assert np.abs(its.astype(int) - g["csr_gmres"].astype(int)).max() <= 3
 
 

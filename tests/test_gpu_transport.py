@@ -65,17 +65,54 @@ def test_structure_and_operators_bitexact(gpu_lib, name):
         assert np.array_equal(Z, g["Zpc"]), "precond"
 
 
+# Free-running Picard sequences longer than this are compared step by step
+# (test_c1_every_picard_iterate_from_the_reference_iterate): the SUPG+CAU
+# Picard map of the plain-method configuration stagnates without contracting
+# (max |du| ~ 0.04, 51 iterations to the cap), so a rounding-level difference
+# in one solve grows from step to step -- measured on GB300, the free-running
+# GPU sequence leaves 1e-8 of the reference's at the 16th iterate.
+FREE_RUN_STEPS = 8
+
+
 @pytest.mark.parametrize("name", golden_names())
 def test_picard_iterates_match_reference(gpu_lib, name):
     g, meta = load_golden(name)
     T, kw = make(g, meta)
+    n = min(kw["npicard"], FREE_RUN_STEPS)
     with T:
-        uh, its = T.Process(kw["npicard"])
-    ref = g["uhist"]
+        uh, its = T.Process(n)
+    ref = g["uhist"][:n]
     assert uh.shape == ref.shape
     for i in range(ref.shape[0]):
         assert rel(uh[i, :-1], ref[i, :-1]) < REL_TOL, f"iterate {i}"
-    assert np.all(np.abs(its - g["iters"]) <= 1), (its, g["iters"])
+    assert np.all(np.abs(its - g["iters"][:n]) <= 1), (its, g["iters"])
+
+
+def test_c1_every_picard_iterate_from_the_reference_iterate(gpu_lib):
+    """The plain-method configuration (64x64 cells, CSR, ILU(0)-GMRES(30) to
+    1e-8, 51 Picard iterations to the reference's cap): every iterate of the
+    reference's run is reproduced to 1e-8 by one GPU Picard step (Build,
+    precond_setup, pgmres) started from the reference's previous iterate, with
+    the reference's GMRES count give or take one; the free-running GPU
+    sequence stays within 1e-6 of the reference's over all 51 iterations."""
+    g, meta = load_golden("c1_skew64_csr_ilu0_51")
+    ref, ref_its = g["uhist"], g["iters"]
+    assert ref.shape[0] == 51
+    T, kw = make(g, meta)
+    with T:
+        u_prev = np.zeros(T.neq + 1)
+        for i in range(ref.shape[0]):
+            T.Build(u=u_prev)
+            T.precond_setup(i + 1)
+            u, it = T.solver()
+            assert rel(u[:-1], ref[i, :-1]) < REL_TOL, f"iterate {i}"
+            assert abs(it - int(ref_its[i])) <= 1, (i, it, ref_its[i])
+            u_prev = ref[i]
+    T, kw = make(g, meta)
+    with T:
+        uh, its = T.Process(51)
+    worst = max(rel(uh[i, :-1], ref[i, :-1]) for i in range(51))
+    assert worst < 1e-6, worst
 
 
 @pytest.mark.parametrize("nx,ny,pert,scheme,reorder,precond", [
