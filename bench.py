@@ -347,6 +347,8 @@ def run_ours(a):
 
     # ---- per-kernel rooflines (CUDA events on the context's stream) ----
     peak, peak_kind = peaks()
+    chain_lv = np.zeros(2, np.int32)
+    chain = T._L.femgpu_transport_ilu_chain(T.handle, chain_lv.ctypes.data_as(ctypes.c_void_p)) == 1
     kern = kernel_times(T, s, a)
     nnz, neq = T.nnzero, T.neq
     # dominant kernel of a step: the preconditioner sweeps (two per iteration)
@@ -362,7 +364,10 @@ def run_ours(a):
         # algorithmic bytes: L and U values + 4-byte indices once, pivots, in/out vectors
         alg = nnz * (vs + 4) + neq * vs + 4 * neq * vs
         t_k = kern[sweep_key]
-        if os.environ.get("FEMGPU_SWEEP_LAYOUT") == "ell":
+        if chain:
+            name = ("k_sweep_cs (ILU(0) forward+backward, chain-scan: rows chained along the SYMRCM fronts solved "
+                    "32 at a time by a warp scan, row records, dataflow between warps")
+        elif os.environ.get("FEMGPU_SWEEP_LAYOUT") == "ell":
             name = "k_sweep (ILU(0) forward+backward, ELL layout, a barrier per level"
         elif os.environ.get("FEMGPU_SWEEP_SYNC") == "barrier":
             name = "k_sweep_rec (ILU(0) forward+backward, row records, a barrier per level"
@@ -394,6 +399,7 @@ def run_ours(a):
         "breakdown_ms": {k: round(v, 4) for k, v in kern.items()},
         "gmres_iters": [int(i) for i in iters], "true_rel_residual": rel,
         "neq": neq, "nnz": nnz, "ilu_levels": [T.ilu_levels_L, T.ilu_levels_U],
+        "ilu_chain_levels": [int(v) for v in chain_lv] if chain else None,
         "wall_ms_per_step": 1e3 * wall / a.steps,
         "gpu_launches": launches_estimate(a, iters),
     }

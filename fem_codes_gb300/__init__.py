@@ -64,7 +64,7 @@ class EulerOpts(ctypes.Structure):
                 ("alpha", ctypes.c_double), ("dt", ctypes.c_double), ("stab_tol", ctypes.c_double),
                 ("precond", ctypes.c_int), ("solver", ctypes.c_int), ("kmax", ctypes.c_int),
                 ("lmax", ctypes.c_int), ("tol", ctypes.c_double), ("ncorr", ctypes.c_int),
-                ("precision", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("scheme", ctypes.c_int), ("ilu_blocks", ctypes.c_int)]
 
 
 class NSOpts(ctypes.Structure):
@@ -100,7 +100,10 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_transport_set_stream": [_vp, _vp],
         "femgpu_transport_info": [_vp, _vp],
         "femgpu_transport_ilu_blocks": [_vp, _vp, ctypes.c_int],
+        "femgpu_transport_ilu_chain": [_vp, _vp],
         "femgpu_ilu_block_cut": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, ctypes.c_int],
+        "femgpu_ilu_chain_segments": [ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
+                                      ctypes.c_int, ctypes.c_int],
         "femgpu_transport_get_pattern": [_vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_transport_build": [_vp, _vp, _vp, _vp],
         "femgpu_transport_precond_setup": [_vp, ctypes.c_int, _vp],
@@ -136,6 +139,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_euler_precond_setup": [_vp, _vp],
         "femgpu_euler_precond_setup_dev": [_vp],
         "femgpu_euler_solve": [_vp, _vp, _vp, _ip],
+        "femgpu_euler_csr": [_vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_euler_solve_dev": [_vp, _ip],
         "femgpu_euler_predictor": [_vp, _vp, ctypes.c_int, _vp, _vp],
         "femgpu_euler_predictor_dev": [_vp, ctypes.c_int, _vp],
@@ -240,6 +244,30 @@ def ilu_block_cut(IA, JA, P):
     if rc < 0:
         raise FemGpuError(rc, "ilu_block_cut")
     return first[: rc + 1]
+
+
+def ilu_chain_segments(IA, JA, P, lower=True):
+    """The chain-scan segmentation of one ILU(0) sweep of a CSR pattern (the
+    programs a transport context with ilu_blocks = P builds for its FGMRES and
+    FP32 sweeps), computed on the host: dict with slot_row, slot_pred, lstart
+    and the level counts."""
+    L = load()
+    IA = np.ascontiguousarray(IA, dtype=np.int32)
+    JA = np.ascontiguousarray(JA, dtype=np.int32)
+    n = IA.size - 1
+    info = np.zeros(4, np.int32)
+    ns = L.femgpu_ilu_chain_segments(n, _ptr(IA), _ptr(JA), int(P), int(lower), _ptr(info), None, None, None, 0, 0)
+    if ns < 0:
+        raise FemGpuError(ns, "ilu_chain_segments")
+    row = np.zeros(ns, np.int32)
+    pred = np.zeros(ns, np.int32)
+    lstart = np.zeros(int(info[0]) + 1, np.int32)
+    rc = L.femgpu_ilu_chain_segments(n, _ptr(IA), _ptr(JA), int(P), int(lower), _ptr(info), _ptr(row), _ptr(pred),
+                                     _ptr(lstart), ns, lstart.size)
+    if rc < 0:
+        raise FemGpuError(rc, "ilu_chain_segments")
+    return dict(slot_row=row, slot_pred=pred, lstart=lstart, levels=int(info[0]), deepest=int(info[1]),
+                deepest_rows=int(info[2]), width=int(info[3]))
 
 
 class SSTransport:
@@ -448,6 +476,14 @@ class SSTransport:
             raise FemGpuError(rc, "solve_dev")
         return it.value
 
+    def ilu_chain(self):
+        """1 when the ILU(0) sweeps of FGMRES and of the FP32 solves run the
+        chain-scan programs, else 0 (femgpu_transport_ilu_chain)."""
+        rc = self._L.femgpu_transport_ilu_chain(self._h, None)
+        if rc < 0:
+            raise FemGpuError(rc, "ilu_chain")
+        return rc
+
     def fell_back(self):
         """0, or how the last learned-preconditioned solve continued after a
         stall: 1 ILU(0), 2 the attached AMG context."""
@@ -569,10 +605,12 @@ class Euler:
 
     def __init__(self, x, y, vert, node_id, neq, upresc, gamma=1.4, mach=1.0, dimensionless=False,
                  alpha=0.5, dt=1e-3, stab_tol=1e-6, precond="BlockDiag", solver="GMRES", kmax=30,
-                 lmax=100, tol=1e-8, ncorr=2, precision="FP64"):
+                 lmax=100, tol=1e-8, ncorr=2, precision="FP64", scheme="EBE", ilu_blocks=0):
         L = load()
         o = EulerOpts()
         L.femgpu_euler_default_opts(ctypes.byref(o))
+        o.scheme = OPTS["scheme"][scheme.upper()]
+        o.ilu_blocks = int(ilu_blocks)
         o.gamma, o.mach, o.dimensionless = float(gamma), float(mach), int(bool(dimensionless))
         o.alpha, o.dt, o.stab_tol = float(alpha), float(dt), float(stab_tol)
         o.precond = OPTS["precond"][precond.upper()]
@@ -636,10 +674,22 @@ class Euler:
         return R, Ae
 
     def precond_setup(self):
-        """BlockDiag_precond_EBE_setup: blocks, inverses, R := D^-1 R. Returns R."""
+        """BlockDiag_precond_EBE_setup (blocks, inverses) or, CSR storage,
+        ILUp_precond_setup (ILU(0) factors); then R := M^-1 R. Returns R."""
         R = np.zeros(self.neq + 1)
         self._check(self._L.femgpu_euler_precond_setup(self._h, _ptr(R)), "precond_setup")
         return R
+
+    def csr(self):
+        """CSR storage: (IA, JA, CSR_by_Element [nel, 144], AA of the last build)."""
+        nn = np.zeros(2, np.int32)
+        self._check(self._L.femgpu_euler_csr(self._h, _ptr(nn), None, None, None, None), "csr")
+        IA = np.zeros(int(nn[0]) + 1, np.int32)
+        JA = np.zeros(max(int(nn[1]), 1), np.int32)
+        sbe = np.zeros((self.nel, 144), np.int32)
+        AA = np.zeros(int(nn[1]) + 1)
+        self._check(self._L.femgpu_euler_csr(self._h, _ptr(nn), _ptr(IA), _ptr(JA), _ptr(sbe), _ptr(AA)), "csr")
+        return IA, JA[: int(nn[1])], sbe, AA
 
     def solver(self, B=None, raise_on_nonconvergence=True):
         """pgmres (6-argument form) on the block EBE operator: X = A^-1 B

@@ -24,6 +24,7 @@ struct femgpu_euler {
 	double *u, *a, *R, *Da, *Re;
 	fg_krylov kry;
 	int built, have_bd;
+	fg_blockcsr csr;               /* scheme FEMGPU_CSR: 12 equations per element */
 	cudaEvent_t ev[4];
 	double times[3];               /* build, precond setup, solve (s)            */
 };

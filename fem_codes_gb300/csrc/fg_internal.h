@@ -45,10 +45,21 @@ typedef struct fg_sweep {
 	int skew;                  /* ... levels a warp may run ahead            */
 	int bvo, cmax;             /* record layout: input slice offset in a
 	                            * stage, most rows of a sub-block            */
+	/* chain-scan programs (k_sweep_cs): levels of warp segments, 32 slots a
+	 * segment chunk; per slot the byte offset of its five scan multipliers
+	 * (-1: padding), the CSR position of its chain coefficient (-1: none)
+	 * and its row */
+	int cs, nslot;
+	long long *cs_voff;
+	int *cs_src, *cs_row;
 } fg_sweep;
 
 typedef struct fg_ilu_sweeps {
 	fg_sweep lo64, up64, lo32, up32;
+	/* chain-scan programs of the same factor for the fused (FGMRES) FP64 and
+	 * the FP32 sweeps; chain = 0 when the sweeps have too few chained rows */
+	fg_sweep lo64c, up64c, lo32c, up32c;
+	int chain;
 	double *bl64, *y64;
 	float *bl32, *y32;
 	int *fac_ptr, *fac_prog;   /* precompiled elimination of each row        */
@@ -60,6 +71,18 @@ typedef struct fg_ilu_sweeps {
 	int nblocks;               /* matrix blocks (1: global ILU(0))           */
 	int *block_first;          /* host [nblocks+1] first row of each block   */
 } fg_ilu_sweeps;
+
+/* CSR storage of a multi-dof element system (csr_Initialization.c of the
+ * Navier-Stokes and Euler drivers, reordering NOT): pattern, CSR_by_Element
+ * slots [M*M*nel], values [nnz+1]; with ILU(0), the factorisation and
+ * sweep engine run on a transport context that holds only this system. */
+typedef struct fg_blockcsr {
+	int *IA, *JA, *sbe;
+	double *AA;
+	int nnz;
+	struct femgpu_transport *ilu;
+	int have_ilu;
+} fg_blockcsr;
 
 typedef struct fg_ilu {
 	int n, nnz;

@@ -27,14 +27,9 @@ struct femgpu_ns {
 	int setup_tag;                 /* precond_setup calls                     */
 	int have_bd;
 	fg_krylov kry;
-	/* CSR storage (scheme FEMGPU_CSR): pattern, CSR_by_Element slots
-	 * [81*nel], values [nnz+1]; the ILU(0) engine works on a transport
-	 * context that holds only this CSR system and its factors */
-	int *IA, *JA, *sbe;
-	double *AA;
-	int nnz;
-	femgpu_transport *ilu;
-	int have_ilu;
+	/* CSR storage (scheme FEMGPU_CSR, 9 equations per element) and its
+	 * ILU(0) (host/blockcsr.c) */
+	fg_blockcsr csr;
 };
 
 /* Build_K_F_MS on the device state u: element matrices into ebe->A, F, and

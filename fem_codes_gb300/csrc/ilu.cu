@@ -568,6 +568,178 @@ k_sweep_df(SweepArgs a, const T *__restrict__ in, T *out)
 	if (*vfailed && ctid == 0) sweep_drain(a, full, D, waited, &issued, &pdone);
 }
 
+// ------------------------------------------------ chain-scan sweep (records)
+// After SYMRCM the rows of a matrix block form fronts, and along a front every
+// row depends on its predecessor in the sweep order: y_i = a_i + b_i y_pred,
+// with a_i the row's other terms (backward: times the inverted pivot) and b_i
+// its coupling to the predecessor -- a first-order linear recurrence.  The
+// program groups up to 32 chained rows into a segment, gives segments (not
+// rows) dependency levels, and packs each level's segments into 32-slot
+// chunks, one per warp (a segment never straddles two chunks; unused slots are
+// padding).  A warp computes a_i for its 32 slots from earlier levels, then
+// solves its segments' recurrences with a Kogge-Stone scan over the lanes:
+// five steps a_t += M_k,t a_{t-2^k}, the multipliers (products of b along the
+// segment, zero across a segment start) precompiled from the factor by
+// k_chain_mult.  At 2048x1024 with 16 blocks the deepest block falls from
+// 1340 row levels to 349 segment levels.  The scan reassociates the
+// recurrence, so results agree with the row-by-row sweeps to rounding, not bit
+// for bit: it serves the fused-arithmetic (FGMRES) and FP32 sweeps only.
+// Records: W dependency codes (the predecessor excluded) and the output slot
+// (-1: padding), then W values, the inverted pivot (backward) and M_0..M_4.
+// Staging, progress flags, need tables and bounded waits are k_sweep_df's.
+__host__ __device__ constexpr int rec_vb_cs(int w, bool upper, int ts) { return ((w + (upper ? 1 : 0) + 5) * ts + 15) & ~15; }
+__host__ __device__ constexpr int rec_bytes_cs(int w, bool upper, int ts)
+{
+	return (((rec_ib(w) + rec_vb_cs(w, upper, ts)) / 16) & 1) ? rec_ib(w) + rec_vb_cs(w, upper, ts)
+	                                                           : rec_ib(w) + rec_vb_cs(w, upper, ts) + 16;
+}
+
+template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c);
+template <> __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+template <> __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+
+template <typename T, bool UPPER, int W>
+__global__ void __launch_bounds__((SW2_CW + 1) * 32, 1)
+k_sweep_cs(SweepArgs a, const T *__restrict__ in, T *out)
+{
+	constexpr int CW = SW2_CW;
+	constexpr int IB = rec_ib(W), VB = rec_vb_cs(W, UPPER, (int)sizeof(T)), RB = rec_bytes_cs(W, UPPER, (int)sizeof(T));
+	constexpr int MO = W + (UPPER ? 1 : 0);              // first scan multiplier
+	static_assert(SW_SUB == CW * 32, "one slot per consumer thread and sub-block");
+	if (a.active && !*a.active) return;
+	extern __shared__ __align__(128) unsigned char sm[];
+	const unsigned ring_b = (unsigned)al16((SW_RING + 1) * sizeof(T));
+	T *ring = (T *)sm;
+	unsigned long long *full = (unsigned long long *)(sm + ring_b);
+	unsigned long long *empty = full + SW_MAXD;
+	unsigned char *stages = sm + ((ring_b + SW_BAR_BYTES + 127) & ~127u);
+	__shared__ int failed, issued, pdone;
+	__shared__ int prog[CW];
+	volatile int *vfailed = &failed;
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, D = a.D;
+	const unsigned sbytes = (unsigned)a.stage_bytes;
+	const int sb0 = a.chunk_sb ? a.chunk_sb[blockIdx.x] : 0, sb1 = a.chunk_sb ? a.chunk_sb[blockIdx.x + 1] : a.nsb;
+	const int l0 = a.chunk_lev ? a.chunk_lev[blockIdx.x] : 0, l1 = a.chunk_lev ? a.chunk_lev[blockIdx.x + 1] : a.nlev;
+
+	if (tid == 0) {
+		failed = 0; issued = 0; pdone = 0;
+		ring[SW_RING] = T(0);
+		for (int s = 0; s < D; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], CW); }
+		fence_mbar_init();
+	}
+	if (tid < CW) prog[tid] = -1;
+	__syncthreads();
+
+	if (warp == CW) {                                     // ---- producer warp
+		sweep_producer(a, in, stages, sbytes, full, empty, D, sb0, sb1, lane, vfailed, &issued, &pdone, true);
+		return;
+	}
+
+	const int ctid = tid;                                 // ---- consumer warps
+	const unsigned roff = (unsigned)DF_HDR + (unsigned)(ctid < a.cmax ? ctid : a.cmax - 1) * RB;
+	const unsigned boff = (unsigned)a.bvo + (unsigned)(ctid < a.cmax ? ctid : a.cmax - 1) * sizeof(T);
+	int s = 0, waited = 0;
+	unsigned ph = 0;
+	bool fail = false;
+	T ydef = T(0);                                        // an output not yet stored to global memory
+	int odef = -1;
+	for (int l = l0; l < l1 && !fail; l++) {
+		const int ll = l - l0;
+		int nsub = 1;
+		for (int j = 0; j < nsub; j++) {
+			if (!mbar_wait_or_fail(&full[s], ph, vfailed)) { *vfailed = 1; fail = true; break; }
+			waited++;
+			const unsigned char *st = stages + (unsigned)s * sbytes;
+			union { int4 q[IB / 16]; int i[IB / 4]; } ci;
+			union { int4 q[VB / 16]; T v[VB / sizeof(T)]; } cv;
+#pragma unroll
+			for (int k = 0; k < IB / 16; k++) ci.q[k] = ((const int4 *)(st + roff))[k];
+#pragma unroll
+			for (int k = 0; k < VB / 16; k++) cv.q[k] = ((const int4 *)(st + roff + IB))[k];
+			const T x0 = *(const T *)(st + boff);
+			const int4 h = *(const int4 *)st;
+			const int need = lane < CW ? (int)st[16 + warp * 16 + lane] : 255;
+			if (j == 0) nsub = h.y;
+			__syncwarp();
+			if (lane == 0) mbar_arrive(&empty[s]);        // this warp's slots are in registers
+			if (++s == D) { s = 0; ph ^= 1u; }
+			if (32 * warp >= h.x) continue;               // no chunk of this warp here (uniform)
+			const int want = ll - (need == 255 ? a.skew + 1 : need);
+			bool ready = false;
+			for (int it = 0; it < SW_WAIT_LIMIT; it++) {
+				const bool mine = lane >= CW || lane == warp || ld_acquire_cta(&prog[lane]) >= want;
+				if (__all_sync(0xffffffffu, mine)) { ready = true; break; }
+				if (__any_sync(0xffffffffu, *vfailed != 0)) break;
+			}
+			if (!ready) { *vfailed = 1; fail = true; break; }
+			__syncwarp();
+			T d[W];
+#pragma unroll
+			for (int k = 0; k < W; k++) {
+				unsigned c = (unsigned)ci.i[k] & ~SW_NEAR;
+				d[k] = ring[c < SW_RING ? c : SW_RING];
+			}
+			if (h.w) {
+#pragma unroll
+				for (int k = 0; k < W; k++)
+					if (!((unsigned)ci.i[k] & SW_NEAR)) d[k] = __ldcg(&out[ci.i[k]]);
+			}
+			T y = x0;
+#pragma unroll
+			for (int k = 0; k < W; k++) y = fmsub<T, true>(y, d[k], cv.v[k]);
+			if (UPPER) y = mul(y, cv.v[W]);
+			// the segments' recurrences across the warp's lanes
+#pragma unroll
+			for (int k = 0; k < 5; k++) {
+				const T up = __shfl_up_sync(0xffffffffu, y, 1 << k);
+				if (lane >= (1 << k)) y = fma_t(cv.v[MO + k], up, y);
+			}
+			ring[(h.z + ctid) & (SW_RING - 1)] = y;
+			if (odef >= 0) out[odef] = ydef;              // an earlier sub-block of this level
+			ydef = y;
+			odef = ci.i[W];
+		}
+		if (fail) break;
+		__syncwarp();
+		if (lane == 0) st_release_cta(&prog[warp], ll);
+		if (odef >= 0) { out[odef] = ydef; odef = -1; }
+	}
+	consumer_sync<CW>();
+	if (*vfailed && ctid == 0) sweep_drain(a, full, D, waited, &issued, &pdone);
+}
+
+// Scan multipliers of a chain-scan program from the factor, one warp per
+// 32-slot chunk: b = -L(row, pred) forward, -Dinv[row] U(row, pred) backward
+// (0 at a segment start and in padding); M_0 = b and, as the scan composes
+// the recurrences, M_{k+1,t} = M_k,t M_k,t-2^k for t >= 2^k (else M_k,t).
+template <typename T, bool UPPER>
+__global__ void k_chain_mult(unsigned char *prog, const long long *voff, const int *src, const int *row, int nslot,
+                             const double *LU, const double *Dinv)
+{
+	const int lane = threadIdx.x & 31;
+	const int w0 = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+	const int nw = (int)((gridDim.x * (unsigned)blockDim.x) >> 5);
+	for (int c = w0; c * 32 < nslot; c += nw) {          // uniform per warp
+		const int i = c * 32 + lane;
+		const int sr = i < nslot ? src[i] : -1;
+		double m = 0.0;
+		if (sr >= 0) m = UPPER ? -(Dinv[row[i]] * LU[sr]) : -LU[sr];
+		double M[5];
+		M[0] = m;
+#pragma unroll
+		for (int k = 0; k < 4; k++) {
+			const double up = __shfl_up_sync(0xffffffffu, M[k], 1 << k);
+			M[k + 1] = lane >= (1 << k) ? M[k] * up : M[k];
+		}
+		const long long o = i < nslot ? voff[i] : -1;
+		if (o >= 0) {
+			T *dst = (T *)(prog + o);
+#pragma unroll
+			for (int k = 0; k < 5; k++) dst[k] = (T)M[k];
+		}
+	}
+}
+
 // Gather the sweep input into padded level order: in[ppos[i]] = (T) p[rows[i]].
 template <typename T, typename TI>
 __global__ void k_perm_in(const TI *__restrict__ p, const int *__restrict__ rows,
@@ -992,6 +1164,14 @@ static bool sweep_dataflow(void)
 	return !(e && !strcmp(e, "barrier"));
 }
 
+// Chain-scan programs for the fused and FP32 sweeps (FEMGPU_SWEEP_CHAIN=0
+// keeps the row-by-row programs for them too).
+static bool sweep_chain(void)
+{
+	const char *e = getenv("FEMGPU_SWEEP_CHAIN");
+	return !(e && !strcmp(e, "0"));
+}
+
 // Levels a dataflow warp may run ahead of the slowest one (FEMGPU_SWEEP_SKEW,
 // 1..64; default 4).
 static int sweep_skew(void)
@@ -1193,6 +1373,288 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 	return 0;
 }
 
+// ------------------------------------------- host: chain-scan programs
+// Segments of one sweep (the order of k_sweep_cs): rows in sweep order
+// (forward ascending, backward descending) within their matrix block; a row
+// joins the current segment when it depends on its sweep predecessor, the
+// segment has fewer than 32 rows and the row's other dependencies are all on
+// earlier levels than the segment's -- otherwise it starts a new segment,
+// whose level is one past its dependencies' (the predecessor among them).
+// This cut keeps segments of consecutive fronts aligned, so a block's depth
+// is about its fronts plus a front's chunk count, not fronts plus front width.
+// Each level's segments are packed, in order, into 32-slot chunks.
+struct ChainLevels {
+	int nlev = 0, nslot = 0, maxw = 0;
+	std::vector<int> lstart;   // [nlev+1] first slot of each level (multiples of 32)
+	std::vector<int> slot_row; // [nslot] row in each slot (-1 padding)
+	std::vector<int> slot_pred; // [nslot] CSR position of the chain coefficient (-1: segment start, padding)
+	std::vector<int> slot;     // [n] slot of each row
+	std::vector<int> clev;     // [P+1] first level of each matrix block
+	int rowlev_max = 0;        // deepest block in row levels (for the choice of program)
+};
+
+static ChainLevels host_chain_levels(const int *IA, const int *JA, int n, bool lower, const Blocks &B)
+{
+	ChainLevels H;
+	const int P = B.P ? B.P : 1;
+	std::vector<int> seg_of(n), seg_lev, seg_blk, seg_first, seg_pred_pos(n, -1), rowlev(n, 0);
+	std::vector<int> bl(P, 0), blrow(P, 0);
+	int cur = -1, run = 0;
+	for (int s = 0; s < n; s++) {
+		const int i = lower ? s : n - 1 - s, pred = lower ? i - 1 : i + 1, b = B.of(i);
+		int elev = 0, ppos = -1, rl = 0, nd = 0;
+		for (int k = IA[i]; k < IA[i + 1]; k++) {
+			const int c = JA[k];
+			if (!(lower ? c < i : c > i) || !B.same(i, c)) continue;
+			rl = std::max(rl, rowlev[c] + 1);
+			if (c == pred) { ppos = k; continue; }
+			elev = std::max(elev, seg_lev[seg_of[c]] + 1);
+			nd++;
+		}
+		rowlev[i] = rl;
+		blrow[b] = std::max(blrow[b], rl + 1);
+		bool chain = ppos >= 0 && cur >= 0 && seg_blk[cur] == b && run < 32 && elev <= seg_lev[cur] &&
+		             seg_of[pred] == cur;
+		if (chain) {
+			seg_of[i] = cur;
+			seg_pred_pos[i] = ppos;
+			run++;
+		} else {
+			if (ppos >= 0) { elev = std::max(elev, seg_lev[seg_of[pred]] + 1); nd++; }
+			seg_lev.push_back(elev);
+			seg_blk.push_back(b);
+			seg_first.push_back(i);
+			cur = (int)seg_lev.size() - 1;
+			seg_of[i] = cur;
+			run = 1;
+			bl[b] = std::max(bl[b], elev + 1);
+		}
+		H.maxw = std::max(H.maxw, nd);
+	}
+	for (int b = 0; b < P; b++) H.rowlev_max = std::max(H.rowlev_max, blrow[b]);
+	std::vector<int> boff(P + 1, 0);
+	for (int b = 0; b < P; b++) boff[b + 1] = boff[b] + bl[b];
+	H.clev = boff;
+	H.nlev = boff[P];
+	const int nseg = (int)seg_lev.size();
+	// segments by global level, in creation order; their rows in sweep order
+	std::vector<int> lcount(H.nlev + 1, 0), seg_len(nseg, 0), order(nseg);
+	for (int g = 0; g < nseg; g++) lcount[seg_lev[g] + boff[seg_blk[g]] + 1]++;
+	for (int l = 0; l < H.nlev; l++) lcount[l + 1] += lcount[l];
+	{
+		std::vector<int> fill(lcount.begin(), lcount.end() - 1);
+		for (int g = 0; g < nseg; g++) order[fill[seg_lev[g] + boff[seg_blk[g]]]++] = g;
+	}
+	for (int i = 0; i < n; i++) seg_len[seg_of[i]]++;
+	std::vector<int> seg_slot(nseg);
+	H.lstart.assign(H.nlev + 1, 0);
+	int slot = 0;
+	for (int l = 0; l < H.nlev; l++) {
+		H.lstart[l] = slot;
+		int used = 32;                                    // lanes used in the current chunk
+		for (int q = lcount[l]; q < lcount[l + 1]; q++) {
+			const int g = order[q];
+			if (used + seg_len[g] > 32) { if (used < 32) slot += 32 - used; used = 0; }
+			seg_slot[g] = slot;
+			slot += seg_len[g];
+			used += seg_len[g];
+		}
+		if (used < 32) slot += 32 - used;
+	}
+	H.lstart[H.nlev] = slot;
+	H.nslot = slot;
+	H.slot_row.assign(slot, -1);
+	H.slot_pred.assign(slot, -1);
+	H.slot.assign(n, 0);
+	std::vector<int> next(seg_slot);
+	for (int s = 0; s < n; s++) {
+		const int i = lower ? s : n - 1 - s, g = seg_of[i], sl = next[g]++;
+		H.slot[i] = sl;
+		H.slot_row[sl] = i;
+		H.slot_pred[sl] = seg_pred_pos[i];
+	}
+	return H;
+}
+
+// The chain-scan program of one sweep (k_sweep_cs): sub-blocks of up to
+// SW_SUB slots of one level, the k_sweep_df header and need tables, one record
+// per slot, the input slice at a fixed stage offset.  Forward: L part, outputs
+// to the backward program's slots; backward: U part and pivots, outputs in
+// natural order.  Returns FEMGPU_E_MESH when the ring cannot hold the widest
+// level (the caller keeps the row-by-row programs then).
+template <typename T, bool UPPER>
+static int build_prog_chain(const int *IA, const int *JA, int n, const ChainLevels &H, const ChainLevels *target,
+                            const Blocks &B, fg_sweep &sw)
+{
+	const bool lower = !UPPER;
+	const long long tsize = sizeof(T);
+	const int nlev = H.nlev;
+	int rw = rec_width(std::max(H.maxw, 1));
+	if (!rw) return FEMGPU_E_MESH;
+	const long long RB = rec_bytes_cs(rw, UPPER, (int)tsize), IBy = rec_ib(rw);
+	int lmax = 32;
+	for (int l = 0; l < nlev; l++) lmax = std::max(lmax, H.lstart[l + 1] - H.lstart[l]);
+	int skew = std::min(sweep_skew(), 4);
+	while (skew > 1 && SW_RING - skew * lmax < 2 * lmax) skew--;
+	int near_lim = std::min(sweep_near_limit(), SW_RING - skew * lmax);
+	if (near_lim < 2 * lmax) return FEMGPU_E_MESH;
+	struct Sub { int l, j0, c; };
+	std::vector<Sub> subs;
+	for (int l = 0; l < nlev; l++) {
+		const int c = H.lstart[l + 1] - H.lstart[l];
+		for (int j0 = 0; j0 < c; j0 += SW_SUB) subs.push_back({ l, j0, std::min(SW_SUB, c - j0) });
+	}
+	const int nsb = (int)subs.size();
+	int cmax = 32;
+	for (const Sub &S : subs) cmax = std::max(cmax, S.c);
+	const long long fixed = (al16((SW_RING + 1) * tsize) + SW_BAR_BYTES + 127) & ~127LL;
+	const long long stage = DF_HDR + (long long)cmax * RB + al16((long long)cmax * tsize);
+	if (fixed + 2 * ((stage + 127) & ~127LL) > SW_SMEM_CAP) return FEMGPU_E_MESH;
+	std::vector<int> lev_of(H.nslot);
+	for (int l = 0; l < nlev; l++)
+		for (int q = H.lstart[l]; q < H.lstart[l + 1]; q++) lev_of[q] = l;
+	std::vector<long long> off(nsb + 1, 0);
+	std::vector<int> sb_in(nsb), sb_inb(nsb);
+	long long bvo = 0, maxin = 0;
+	for (int i = 0; i < nsb; i++) {
+		const long long bb = DF_HDR + (long long)subs[i].c * RB;
+		off[i + 1] = off[i] + bb;
+		sb_in[i] = H.lstart[subs[i].l] + subs[i].j0;
+		sb_inb[i] = (int)al16((long long)subs[i].c * tsize);
+		bvo = std::max(bvo, bb);
+		maxin = std::max(maxin, (long long)sb_inb[i]);
+	}
+	std::vector<unsigned char> prog((size_t)off[nsb] + 16, 0);
+	std::vector<long long> val_off, cs_voff(H.nslot, -1);
+	std::vector<int> val_src, cs_src(H.nslot, -1), cs_row(H.nslot, 0);
+	val_off.reserve((size_t)H.nslot * (rw + 1));
+	val_src.reserve((size_t)H.nslot * (rw + 1));
+	for (int i = 0; i < nsb; i++) {
+		const Sub &S = subs[i];
+		const int l = S.l, c = S.c, start = H.lstart[l] + S.j0, end = H.lstart[l + 1];
+		const int nsub = (end - H.lstart[l] + SW_SUB - 1) / SW_SUB;
+		unsigned char *b = prog.data() + off[i];
+		int hasfar = 0;
+		for (int j = 0; j < c; j++) {
+			const int r = H.slot_row[start + j];
+			if (r < 0) continue;
+			for (int q = IA[r]; q < IA[r + 1]; q++) {
+				const int col = JA[q];
+				if ((lower ? col < r : col > r) && B.same(r, col) && q != H.slot_pred[start + j] &&
+				    end - H.slot[col] > near_lim) hasfar = 1;
+			}
+		}
+		const int hh[4] = { c, nsub, start, hasfar };
+		memcpy(b, hh, sizeof hh);
+		unsigned char *need = b + 16;
+		memset(need, 255, (size_t)SW2_CW * 16);
+		for (int j = 0; j < c; j++) {
+			const int r = H.slot_row[start + j];
+			int *ri = (int *)(b + DF_HDR + (size_t)j * RB), k = 0;
+			const long long vo = off[i] + DF_HDR + (long long)j * RB + IBy;
+			for (int q = 0; q < rw; q++) ri[q] = (int)(SW_NEAR | SW_RING);     // the zero slot
+			if (r < 0) {                                                       // padding
+				ri[rw] = -1;
+				for (int q = 0; q < rw + (UPPER ? 1 : 0); q++) { val_off.push_back(vo + q * tsize); val_src.push_back(-1); }
+				continue;
+			}
+			ri[rw] = lower ? target->slot[r] : r;
+			for (int q = IA[r]; q < IA[r + 1]; q++) {
+				const int col = JA[q];
+				if ((lower ? !(col < r) : !(col > r)) || !B.same(r, col) || q == H.slot_pred[start + j]) continue;
+				const int p = H.slot[col], lp = lev_of[p];
+				int dl = l - lp;
+				const bool nearp = end - p <= near_lim;
+				ri[k] = (int)(nearp ? (SW_NEAR | (unsigned)(p & (SW_RING - 1))) : (unsigned)(lower ? target->slot[col] : col));
+				if (!nearp) dl--;                     // read back from global memory: the next level's release
+				if (dl <= skew + 1) {
+					const int pw = ((p - H.lstart[lp]) % SW_SUB) / 32;
+					unsigned char &e = need[(j / 32) * 16 + pw];
+					if (dl < (int)e) e = (unsigned char)dl;
+				}
+				val_off.push_back(vo + k * tsize);
+				val_src.push_back(q);
+				k++;
+			}
+			for (; k < rw; k++) { val_off.push_back(vo + k * tsize); val_src.push_back(-1); }
+			if (!lower) { val_off.push_back(vo + rw * tsize); val_src.push_back(-2 - r); }
+			cs_voff[start + j] = vo + (rw + (UPPER ? 1 : 0)) * tsize;
+			cs_src[start + j] = H.slot_pred[start + j];
+			cs_row[start + j] = r;
+		}
+		// padding slots: multipliers zero (the refresh writes them too)
+		for (int j = 0; j < c; j++)
+			if (H.slot_row[start + j] < 0) cs_voff[start + j] = off[i] + DF_HDR + (long long)j * RB + IBy +
+			                                                    (rw + (UPPER ? 1 : 0)) * tsize;
+	}
+	// every index the kernel will follow stays inside its array: dependency
+	// codes (ring slots or output positions), output positions, input slices
+	{
+		const long long nout = lower ? target->nslot : n;
+		for (int i = 0; i < nsb; i++) {
+			const unsigned char *b = prog.data() + off[i];
+			const int c = subs[i].c;
+			if (sb_in[i] < 0 || (long long)sb_in[i] + c > H.nslot) return FEMGPU_E_MESH;
+			for (int j = 0; j < c; j++) {
+				const int *ri = (const int *)(b + DF_HDR + (size_t)j * RB);
+				for (int q = 0; q < rw; q++) {
+					const unsigned code = (unsigned)ri[q];
+					if (code & SW_NEAR) { if ((code & ~SW_NEAR) > SW_RING) return FEMGPU_E_MESH; }
+					else if ((long long)code >= nout) return FEMGPU_E_MESH;
+				}
+				if (ri[rw] < -1 || ri[rw] >= nout) return FEMGPU_E_MESH;
+			}
+		}
+		for (size_t q = 0; q < cs_voff.size(); q++)
+			if (cs_voff[q] < 0 || cs_voff[q] + 5 * tsize > off[nsb]) return FEMGPU_E_MESH;
+		for (size_t q = 0; q < val_off.size(); q++)
+			if (val_off[q] < 0 || val_off[q] + tsize > off[nsb]) return FEMGPU_E_MESH;
+	}
+	std::vector<int> csb(H.clev.size(), nsb);
+	for (size_t bk = 0, i = 0; bk < H.clev.size(); bk++) {
+		while (i < (size_t)nsb && subs[i].l < H.clev[bk]) i++;
+		csb[bk] = (int)i;
+	}
+	// real rows in slot order (the gather of the sweep input)
+	std::vector<int> rows, ppos;
+	rows.reserve(n);
+	ppos.reserve(n);
+	for (int q = 0; q < H.nslot; q++)
+		if (H.slot_row[q] >= 0) { rows.push_back(H.slot_row[q]); ppos.push_back(q); }
+	std::vector<int> lev_start(H.lstart);
+	sw.nchunk = (int)H.clev.size() - 1;
+	sw.rw = rw;
+	sw.df = 1;
+	sw.cs = 1;
+	sw.skew = skew;
+	sw.bvo = (int)bvo;
+	sw.cmax = cmax;
+	sw.nlev = nlev;
+	sw.nsb = nsb;
+	sw.bytes = off[nsb];
+	sw.maxblk = bvo + maxin;
+	sw.nval = (long long)val_off.size();
+	sw.npad = H.nslot;
+	sw.nslot = H.nslot;
+	int rc;
+	FG_TRY(cudaMalloc((void **)&sw.prog, prog.size()));
+	FG_TRY(cudaMemcpy(sw.prog, prog.data(), prog.size(), cudaMemcpyHostToDevice));
+	if ((rc = up_vec(&sw.blk_off, off))) return rc;
+	if ((rc = up_vec(&sw.sb_in, sb_in))) return rc;
+	if ((rc = up_vec(&sw.sb_inb, sb_inb))) return rc;
+	if ((rc = up_vec(&sw.lev_start, lev_start))) return rc;
+	if ((rc = up_vec(&sw.rows, rows))) return rc;
+	if ((rc = up_vec(&sw.ppos, ppos))) return rc;
+	if ((rc = up_vec(&sw.val_off, val_off))) return rc;
+	if ((rc = up_vec(&sw.val_src, val_src))) return rc;
+	if ((rc = up_vec(&sw.chunk_sb, csb))) return rc;
+	if ((rc = up_vec(&sw.chunk_lev, H.clev))) return rc;
+	if ((rc = up_vec(&sw.cs_voff, cs_voff))) return rc;
+	if ((rc = up_vec(&sw.cs_src, cs_src))) return rc;
+	if ((rc = up_vec(&sw.cs_row, cs_row))) return rc;
+	return 0;
+}
+
 // Elimination program of every row, in forward level order (the layout
 // k_ilu0_factor_cta reads): the same sequence of updates as
 // ILUp_precond_setup.c:119-139, resolved against the pattern once.
@@ -1325,7 +1787,11 @@ static int factor_cluster_size(int P)
 	cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP))
 #define SD_SET(T, U, F, W) FG_TRY(cudaFuncSetAttribute(k_sweep_df<T, U, F, W>, \
 	cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP))
-#define SR_SET_W(W) SR_SET(double, false, false, W); SR_SET(double, true, false, W); \
+#define SC_SET(T, U, W) FG_TRY(cudaFuncSetAttribute(k_sweep_cs<T, U, W>, \
+	cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP))
+#define SR_SET_W(W) SC_SET(double, false, W); SC_SET(double, true, W); SC_SET(float, false, W); \
+	SC_SET(float, true, W); \
+	SR_SET(double, false, false, W); SR_SET(double, true, false, W); \
 	SR_SET(double, false, true, W); SR_SET(double, true, true, W); \
 	SR_SET(float, false, false, W); SR_SET(float, true, false, W); \
 	SD_SET(double, false, false, W); SD_SET(double, true, false, W); \
@@ -1375,6 +1841,21 @@ static void launch_df(const SweepArgs &a, int rw, int grid, int bytes, cudaStrea
 	}
 }
 
+template <typename T, bool UPPER>
+static void launch_cs(const SweepArgs &a, int rw, int grid, int bytes, cudaStream_t s, const T *in, T *out)
+{
+	const int nt = (SW2_CW + 1) * 32;
+	switch (rw) {
+	case 2: k_sweep_cs<T, UPPER, 2><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 3: k_sweep_cs<T, UPPER, 3><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 4: k_sweep_cs<T, UPPER, 4><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 6: k_sweep_cs<T, UPPER, 6><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 8: k_sweep_cs<T, UPPER, 8><<<grid, nt, bytes, s>>>(a, in, out); break;
+	case 12: k_sweep_cs<T, UPPER, 12><<<grid, nt, bytes, s>>>(a, in, out); break;
+	default: k_sweep_cs<T, UPPER, 16><<<grid, nt, bytes, s>>>(a, in, out); break;
+	}
+}
+
 template <typename T, bool UPPER, bool FMA>
 static void launch_rec(const SweepArgs &a, int rw, int grid, int bytes, cudaStream_t s, const T *in, T *out)
 {
@@ -1392,8 +1873,12 @@ static void launch_rec(const SweepArgs &a, int rw, int grid, int bytes, cudaStre
 
 template <typename T, bool UPPER>
 static void launch_sweep(const SweepArgs &a, int rw, int df, int grid, int bytes, cudaStream_t s, const T *in,
-                         T *out, bool fma)
+                         T *out, bool fma, int cs = 0)
 {
+	if (cs) {
+		launch_cs<T, UPPER>(a, rw, grid, bytes, s, in, out);
+		return;
+	}
 	if (rw && df) {
 		if (fma && sizeof(T) == 8) launch_df<T, UPPER, true>(a, rw, grid, bytes, s, in, out);
 		else launch_df<T, UPPER, false>(a, rw, grid, bytes, s, in, out);
@@ -1454,6 +1939,35 @@ extern "C" int femgpu_ilu_block_cut(int n, const int *IA, const int *JA, int P, 
 	return (int)f.size() - 1;
 }
 
+// Host only (no device call): the chain-scan segmentation of one ILU(0)
+// sweep of a CSR pattern with P blocks, as fg_ilu_prepare computes it.
+extern "C" int femgpu_ilu_chain_segments(int n, const int *IA, const int *JA, int P, int lower, int *info,
+                                         int *slot_row, int *slot_pred, int *lstart, int cap_slots, int cap_levels)
+{
+	if (n <= 0 || !IA || !JA || !info) return FEMGPU_E_ARG;
+	if (IA[0] != 0) return FEMGPU_E_ARG;
+	for (int i = 0; i < n; i++) {
+		if (IA[i + 1] < IA[i]) return FEMGPU_E_ARG;
+		for (int k = IA[i]; k < IA[i + 1]; k++)
+			if (JA[k] < 0 || JA[k] >= n || (k > IA[i] && JA[k] <= JA[k - 1])) return FEMGPU_E_ARG;
+	}
+	Blocks B = make_blocks(IA, JA, n, P, nullptr);
+	ChainLevels H = host_chain_levels(IA, JA, n, lower != 0, B);
+	int deep = 0;
+	for (size_t b = 0; b + 1 < H.clev.size(); b++) deep = std::max(deep, H.clev[b + 1] - H.clev[b]);
+	info[0] = H.nlev;
+	info[1] = deep;
+	info[2] = H.rowlev_max;
+	info[3] = H.maxw;
+	if (slot_row || slot_pred || lstart) {
+		if (cap_slots < H.nslot || cap_levels < H.nlev + 1) return FEMGPU_E_ARG;
+		if (slot_row) memcpy(slot_row, H.slot_row.data(), sizeof(int) * H.nslot);
+		if (slot_pred) memcpy(slot_pred, H.slot_pred.data(), sizeof(int) * H.nslot);
+		if (lstart) memcpy(lstart, H.lstart.data(), sizeof(int) * (H.nlev + 1));
+	}
+	return H.nslot;
+}
+
 extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJA)
 {
 	int n = t->neq, rc, D, sb;
@@ -1474,7 +1988,31 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 	if ((rc = build_factor_prog(hIA, hJA, n, Lo, B, S))) return rc;
 	S.fac2_ok = 0;
 	if ((rc = build_factor_prog2(hIA, hJA, n, Lo, B, S))) return rc;
+	S.chain = 0;
 	size_t nb = (size_t)std::max(Lo.pstart[Lo.nlev], Up.pstart[Up.nlev]) + 64;
+	if (sweep_chain()) {
+		ChainLevels CL = host_chain_levels(hIA, hJA, n, true, B), CU = host_chain_levels(hIA, hJA, n, false, B);
+		int deepL = 0, deepU = 0;
+		for (size_t b = 0; b + 1 < CL.clev.size(); b++) deepL = std::max(deepL, CL.clev[b + 1] - CL.clev[b]);
+		for (size_t b = 0; b + 1 < CU.clev.size(); b++) deepU = std::max(deepU, CU.clev[b + 1] - CU.clev[b]);
+		// worth it only when the segments remove most of the levels
+		if (4 * (deepL + deepU) <= 3 * (CL.rowlev_max + CU.rowlev_max)) {
+			int r1 = build_prog_chain<double, true>(hIA, hJA, n, CU, nullptr, B, S.up64c);
+			int r2 = r1 ? r1 : build_prog_chain<double, false>(hIA, hJA, n, CL, &CU, B, S.lo64c);
+			int r3 = r2 ? r2 : build_prog_chain<float, true>(hIA, hJA, n, CU, nullptr, B, S.up32c);
+			int r4 = r3 ? r3 : build_prog_chain<float, false>(hIA, hJA, n, CL, &CU, B, S.lo32c);
+			if (r4 && r4 != FEMGPU_E_MESH) return r4;
+			S.chain = r4 == 0;
+			if (S.chain) {
+				nb = std::max(nb, (size_t)std::max(CL.nslot, CU.nslot) + 64);
+				const fg_sweep *cs[4] = { &S.lo64c, &S.up64c, &S.lo32c, &S.up32c };
+				for (int i = 0; i < 4; i++) {
+					rc = sweep_smem(*cs[i], i < 2 ? sizeof(double) : sizeof(float), &D, &sb);
+					if (rc < 0) { S.chain = 0; break; }
+				}
+			}
+		}
+	}
 	FG_TRY(cudaMalloc((void **)&S.bl64, sizeof(double) * nb));
 	FG_TRY(cudaMalloc((void **)&S.y64, sizeof(double) * nb));
 	FG_TRY(cudaMalloc((void **)&S.bl32, sizeof(float) * nb));
@@ -1512,13 +2050,29 @@ extern "C" int fg_ilu0_factor(femgpu_transport *t)
 		                                                       S.lo64.nlev, S.lo64.chunk_lev, S.fac_ptr,
 		                                                       S.fac_prog, t->ilu.LU, t->ilu.Dinv, &t->st->err);
 	}
-	fg_sweep *pr[4] = { &S.lo64, &S.up64, &S.lo32, &S.up32 };
-	for (int i = 0; i < 4; i++) {
+	fg_sweep *pr[8] = { &S.lo64, &S.up64, &S.lo32, &S.up32, &S.lo64c, &S.up64c, &S.lo32c, &S.up32c };
+	for (int i = 0; i < (S.chain ? 8 : 4); i++) {
 		int g = fg_grid(pr[i]->nval);
-		if (i < 2) k_refresh<double><<<g, FG_TPB, 0, s>>>(pr[i]->prog, pr[i]->val_off, pr[i]->val_src,
-		                                                 pr[i]->nval, t->ilu.LU, t->ilu.Dinv);
+		const bool f64 = (i & 2) == 0;
+		if (f64) k_refresh<double><<<g, FG_TPB, 0, s>>>(pr[i]->prog, pr[i]->val_off, pr[i]->val_src,
+		                                               pr[i]->nval, t->ilu.LU, t->ilu.Dinv);
 		else k_refresh<float><<<g, FG_TPB, 0, s>>>(pr[i]->prog, pr[i]->val_off, pr[i]->val_src,
 		                                          pr[i]->nval, t->ilu.LU, t->ilu.Dinv);
+	}
+	if (S.chain) {
+		for (int i = 4; i < 8; i++) {
+			const fg_sweep &c = *pr[i];
+			const int g = fg_grid((long long)c.nslot);
+			const bool f64 = (i & 2) == 0, up = (i & 1) != 0;
+			if (f64 && up) k_chain_mult<double, true><<<g, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
+			                                                              c.nslot, t->ilu.LU, t->ilu.Dinv);
+			else if (f64) k_chain_mult<double, false><<<g, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
+			                                                              c.nslot, t->ilu.LU, t->ilu.Dinv);
+			else if (up) k_chain_mult<float, true><<<g, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
+			                                                           c.nslot, t->ilu.LU, t->ilu.Dinv);
+			else k_chain_mult<float, false><<<g, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
+			                                                    c.nslot, t->ilu.LU, t->ilu.Dinv);
+		}
 	}
 	return (int)cudaGetLastError();
 }
@@ -1538,39 +2092,47 @@ static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, 
 	a.prog = lo.prog; a.blk_off = lo.blk_off; a.sb_in = lo.sb_in; a.sb_inb = lo.sb_inb;
 	a.nlev = lo.nlev; a.nsb = lo.nsb; a.D = D; a.stage_bytes = sb;
 	a.chunk_sb = lo.chunk_sb; a.chunk_lev = lo.chunk_lev; a.bvo = lo.bvo; a.cmax = lo.cmax; a.skew = lo.skew;
-	launch_sweep<T, false>(a, lo.rw, lo.df, lo.nchunk, bytes, s, bl, y, fma);
+	launch_sweep<T, false>(a, lo.rw, lo.df, lo.nchunk, bytes, s, bl, y, fma, lo.cs);
 	bytes = sweep_smem(up, sizeof(T), &D, &sb);
 	if (bytes < 0) return bytes;
 	a.prog = up.prog; a.blk_off = up.blk_off; a.sb_in = up.sb_in; a.sb_inb = up.sb_inb;
 	a.nlev = up.nlev; a.nsb = up.nsb; a.D = D; a.stage_bytes = sb;
 	a.chunk_sb = up.chunk_sb; a.chunk_lev = up.chunk_lev; a.bvo = up.bvo; a.cmax = up.cmax; a.skew = up.skew;
-	launch_sweep<T, true>(a, up.rw, up.df, up.nchunk, bytes, s, y, (T *)z, fma);
+	launch_sweep<T, true>(a, up.rw, up.df, up.nchunk, bytes, s, y, (T *)z, fma, up.cs);
 	return (int)cudaGetLastError();
 }
 
+// FGMRES sweeps (fused arithmetic) and FP32 sweeps take the chain-scan
+// programs when the factor has them; the reference's left-preconditioned
+// GMRES keeps the row-by-row programs, bit-identical to its ILUp_precond.
 extern "C" int fg_ilu0_apply64(femgpu_transport *t, const double *p, double *z, const int *active)
 {
 	fg_ilu_sweeps &S = t->sweeps;
-	return apply_t<double, double, double>(t, S.lo64, S.up64, S.bl64, S.y64, p, z, active,
-	                                       t->o.solver == FEMGPU_FGMRES);
+	const bool fma = t->o.solver == FEMGPU_FGMRES;
+	if (fma && S.chain)
+		return apply_t<double, double, double>(t, S.lo64c, S.up64c, S.bl64, S.y64, p, z, active, true);
+	return apply_t<double, double, double>(t, S.lo64, S.up64, S.bl64, S.y64, p, z, active, fma);
 }
 
 extern "C" int fg_ilu0_apply32(femgpu_transport *t, const double *p, float *z, const int *active)
 {
 	fg_ilu_sweeps &S = t->sweeps;
+	if (S.chain) return apply_t<float, double, float>(t, S.lo32c, S.up32c, S.bl32, S.y32, p, z, active, false);
 	return apply_t<float, double, float>(t, S.lo32, S.up32, S.bl32, S.y32, p, z, active, false);
 }
 
 extern "C" void fg_ilu_free(femgpu_transport *t)
 {
 	fg_ilu_sweeps &S = t->sweeps;
-	fg_sweep *all[4] = { &S.lo64, &S.up64, &S.lo32, &S.up32 };
-	for (int i = 0; i < 4; i++) {
+	fg_sweep *all[8] = { &S.lo64, &S.up64, &S.lo32, &S.up32, &S.lo64c, &S.up64c, &S.lo32c, &S.up32c };
+	for (int i = 0; i < 8; i++) {
 		void *p[] = { all[i]->prog, all[i]->blk_off, all[i]->sb_in, all[i]->sb_inb, all[i]->lev_start,
 		              all[i]->rows, all[i]->ppos, all[i]->val_off, all[i]->val_src, all[i]->chunk_sb,
-		              all[i]->chunk_lev };
+		              all[i]->chunk_lev, all[i]->cs_voff, all[i]->cs_src, all[i]->cs_row };
 		for (void *q : p) if (q) cudaFree(q);
+		memset(all[i], 0, sizeof(fg_sweep));
 	}
+	S.chain = 0;
 	void *v[] = { S.bl64, S.y64, S.bl32, S.y32, S.fac_ptr, S.fac_prog, S.fac2_hdr, S.fac2 };
 	for (void *q : v) if (q) cudaFree(q);
 	free(S.block_first);

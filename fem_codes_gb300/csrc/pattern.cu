@@ -295,21 +295,34 @@ __global__ void k_assemble_csr_m(int neq, int nnz, const int *IA, const int *sbe
 	if (blockIdx.x == 0 && threadIdx.x == 0) AA[nnz] = 0.0;
 }
 
-extern "C" int fg_build_csr_m(int M, int nel, int neq, const int *ri_ptr, const int *ri, const int *lm,
-                              cudaStream_t s, int *err, int **IA, int **JA, int **sbe, int *nnz)
+// M = 9 (Navier-Stokes, 3 dofs per node) or 12 (Euler, 4 dofs per node;
+// 03_Euler_Equations/2D/01_CommonFiles/csr_Initialization.c is the same
+// algorithm over 12 equations per element).
+template <int M>
+static int build_csr_m(int nel, int neq, const int *ri_ptr, const int *ri, const int *lm, cudaStream_t s, int *err,
+                       int **IA, int **JA, int **sbe, int *nnz, int *rowlen)
 {
-	int *rowlen = nullptr, herr = 0;
-	if (M != 9) return FEMGPU_E_ARG;
-	FG_TRY(cudaMalloc(&rowlen, sizeof(int) * (neq + 1)));
-	FG_TRY(cudaMalloc(IA, sizeof(int) * (neq + 1)));
-	k_csr_rows_m<9><<<fg_grid(neq, 128), 128, 0, s>>>(ri_ptr, ri, lm, neq, rowlen, nullptr, nullptr, err);
+	k_csr_rows_m<M><<<fg_grid(neq, 128), 128, 0, s>>>(ri_ptr, ri, lm, neq, rowlen, nullptr, nullptr, err);
 	int rc = fg_scan(rowlen, *IA, neq, s);
 	if (rc) return rc;
 	FG_TRY(cudaMemcpy(nnz, *IA + neq, sizeof(int), cudaMemcpyDeviceToHost));
 	FG_TRY(cudaMalloc(JA, sizeof(int) * ((size_t)*nnz + 1)));
-	FG_TRY(cudaMalloc(sbe, sizeof(int) * 81 * (size_t)nel));
-	k_csr_rows_m<9><<<fg_grid(neq, 128), 128, 0, s>>>(ri_ptr, ri, lm, neq, nullptr, *IA, *JA, err);
-	k_csr_sbe_m<9><<<fg_grid(nel), FG_TPB, 0, s>>>(lm, *IA, *JA, nel, neq, *nnz, *sbe);
+	FG_TRY(cudaMalloc(sbe, sizeof(int) * M * M * (size_t)nel));
+	k_csr_rows_m<M><<<fg_grid(neq, 128), 128, 0, s>>>(ri_ptr, ri, lm, neq, nullptr, *IA, *JA, err);
+	k_csr_sbe_m<M><<<fg_grid(nel), FG_TPB, 0, s>>>(lm, *IA, *JA, nel, neq, *nnz, *sbe);
+	return 0;
+}
+
+extern "C" int fg_build_csr_m(int M, int nel, int neq, const int *ri_ptr, const int *ri, const int *lm,
+                              cudaStream_t s, int *err, int **IA, int **JA, int **sbe, int *nnz)
+{
+	int *rowlen = nullptr, herr = 0, rc;
+	if (M != 9 && M != 12) return FEMGPU_E_ARG;
+	FG_TRY(cudaMalloc(&rowlen, sizeof(int) * (neq + 1)));
+	FG_TRY(cudaMalloc(IA, sizeof(int) * (neq + 1)));
+	rc = M == 9 ? build_csr_m<9>(nel, neq, ri_ptr, ri, lm, s, err, IA, JA, sbe, nnz, rowlen)
+	            : build_csr_m<12>(nel, neq, ri_ptr, ri, lm, s, err, IA, JA, sbe, nnz, rowlen);
+	if (rc) { cudaFree(rowlen); return rc; }
 	FG_TRY(cudaGetLastError());
 	FG_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
 	FG_TRY(cudaStreamSynchronize(s));
@@ -320,8 +333,9 @@ extern "C" int fg_build_csr_m(int M, int nel, int neq, const int *ri_ptr, const 
 extern "C" int fg_assemble_csr_m(int M, int neq, int nnz, const int *IA, const int *sbe, const int *ri_ptr,
                                  const int *ri, const double *Ae, double *AA, cudaStream_t s)
 {
-	if (M != 9) return FEMGPU_E_ARG;
-	k_assemble_csr_m<9><<<fg_grid(neq, 128, 32), 128, 0, s>>>(neq, nnz, IA, sbe, ri_ptr, ri, Ae, AA);
+	if (M == 9) k_assemble_csr_m<9><<<fg_grid(neq, 128, 32), 128, 0, s>>>(neq, nnz, IA, sbe, ri_ptr, ri, Ae, AA);
+	else if (M == 12) k_assemble_csr_m<12><<<fg_grid(neq, 128, 32), 128, 0, s>>>(neq, nnz, IA, sbe, ri_ptr, ri, Ae, AA);
+	else return FEMGPU_E_ARG;
 	return (int)cudaGetLastError();
 }
 

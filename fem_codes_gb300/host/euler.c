@@ -4,7 +4,8 @@
  * stopped after NonLinearMaxIter correctors as StopByIterations does,
  * Criteria.c:25-31) around device kernels for the build
  * (Build_M_K_F_SUPG), the nodal block-diagonal preconditioner, the block-EBE
- * matvec and GMRES.  Plain C.
+ * matvec and GMRES, or -- CSR storage -- the element matrices assembled into
+ * the driver's CSR pattern (csr_assembly.c), csrmv and ILU(0).  Plain C.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -32,6 +33,7 @@ void femgpu_euler_default_opts(femgpu_euler_opts *o)
 	o->lmax = 100;
 	o->tol = 1e-8;
 	o->ncorr = 2;
+	o->scheme = FEMGPU_EBE;
 }
 
 /* ---- operator callbacks of the Krylov solver ---------------------------- */
@@ -63,10 +65,27 @@ static int op_matvec_xf(void *ctx, const float *p, double *q, const int *active,
 	return fg_ebe_matvec32(((femgpu_euler *)ctx)->ebe, p, q);
 }
 
+/* CSR storage: csrmv and ILUp_precond */
+static int op_matvec_csr(void *ctx, const double *p, double *q, const int *active)
+{
+	femgpu_euler *c = (femgpu_euler *)ctx;
+	return fg_csrmv64(c->neq, c->csr.IA, c->csr.JA, c->csr.AA, p, q, active, c->stream);
+}
+
+static int op_precond_ilu(void *ctx, const double *p, double *z, const int *active)
+{
+	return fg_ilu0_apply64(((femgpu_euler *)ctx)->csr.ilu, p, z, active);
+}
+
 static void linop(femgpu_euler *c, fg_linop *op)
 {
 	memset(op, 0, sizeof *op);
 	op->ctx = c;
+	if (c->o.scheme == FEMGPU_CSR) {
+		op->matvec = op_matvec_csr;
+		op->precond = c->o.precond == FEMGPU_PREC_ILU0 ? op_precond_ilu : NULL;
+		return;
+	}
 	op->matvec = op_matvec;
 	op->precond = c->o.precond == FEMGPU_PREC_BLOCKDIAG ? op_precond : NULL;
 	op->precond32 = op_precond32;
@@ -109,6 +128,9 @@ static int create(femgpu_euler *c, const femgpu_euler_opts *o, int nnodes, const
 	rc = fgh_kry_alloc(&c->kry, neq, o->kmax,
 	                   o->solver != FEMGPU_FGMRES ? 0 : o->precision == FEMGPU_MIXED_IR ? 2 : 1, c->stream);
 	if (rc) return rc;
+	if (o->scheme == FEMGPU_CSR &&
+	    (rc = fgh_blockcsr_create(&c->csr, 12, c->ebe, nel, neq, c->stream, o->precond == FEMGPU_PREC_ILU0,
+	                              o->solver, o->ilu_blocks))) return rc;
 	for (i = 0; i < 4; i++) CK(cudaEventCreate(&c->ev[i]));
 	CK(cudaStreamSynchronize(c->stream));
 	return 0;
@@ -126,7 +148,10 @@ int femgpu_euler_create(femgpu_euler **out, const femgpu_euler_opts *opts, int n
 	if (opts) o = *opts; else femgpu_euler_default_opts(&o);
 	if (nnodes <= 0 || nel <= 0 || neq <= 0 || !x || !y || !vert || !node_id || !upresc ||
 	    o.kmax < 1 || o.lmax < 1 || o.ncorr < 1 || !(o.dt > 0.0) || !(o.tol > 0.0) ||
-	    (o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_BLOCKDIAG) ||
+	    (o.scheme != FEMGPU_EBE && o.scheme != FEMGPU_CSR) || o.ilu_blocks < 0 ||
+	    (o.scheme == FEMGPU_EBE && o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_BLOCKDIAG) ||
+	    (o.scheme == FEMGPU_CSR && o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_ILU0) ||
+	    (o.scheme == FEMGPU_CSR && o.precision != FEMGPU_FP64) ||
 	    (o.solver != FEMGPU_PGMRES && o.solver != FEMGPU_FGMRES) ||
 	    (o.precision != FEMGPU_FP64 && o.precision != FEMGPU_MIXED_IR) ||
 	    (o.precision == FEMGPU_MIXED_IR && o.solver != FEMGPU_FGMRES)) {
@@ -146,6 +171,7 @@ void femgpu_euler_destroy(femgpu_euler *c)
 	int i;
 	if (!c) return;
 	if (c->stream) cudaStreamSynchronize(c->stream);
+	fgh_blockcsr_destroy(&c->csr);
 	if (c->ebe) femgpu_ebe_destroy(c->ebe);
 	{
 		void *p[] = { c->x, c->y, c->upresc, c->u, c->a, c->R, c->Da, c->Re };
@@ -164,6 +190,22 @@ int femgpu_euler_set_stream(femgpu_euler *c, void *stream)
 	c->stream = stream ? (cudaStream_t)stream : c->own_stream;
 	c->kry.stream = c->stream;
 	KR(femgpu_ebe_set_stream(c->ebe, c->stream));
+	fgh_blockcsr_set_stream(&c->csr, c->stream);
+	return 0;
+}
+
+int femgpu_euler_csr(femgpu_euler *c, int *n_nnz, int *IA, int *JA, int *sbe, double *AA)
+{
+	if (!c || !n_nnz || c->o.scheme != FEMGPU_CSR) return FEMGPU_E_ARG;
+	n_nnz[0] = c->neq; n_nnz[1] = c->csr.nnz;
+	if (IA) CK(cudaMemcpyAsync(IA, c->csr.IA, sizeof(int) * ((size_t)c->neq + 1), cudaMemcpyDeviceToHost,
+	                           c->stream));
+	if (JA) CK(cudaMemcpyAsync(JA, c->csr.JA, sizeof(int) * (size_t)c->csr.nnz, cudaMemcpyDeviceToHost, c->stream));
+	if (sbe) CK(cudaMemcpyAsync(sbe, c->csr.sbe, sizeof(int) * 144 * (size_t)c->nel, cudaMemcpyDeviceToHost,
+	                            c->stream));
+	if (AA) CK(cudaMemcpyAsync(AA, c->csr.AA, sizeof(double) * ((size_t)c->csr.nnz + 1), cudaMemcpyDeviceToHost,
+	                           c->stream));
+	CK(cudaStreamSynchronize(c->stream));
 	return 0;
 }
 
@@ -182,6 +224,7 @@ int femgpu_euler_build_dev(femgpu_euler *c)
 {
 	if (!c) return FEMGPU_E_ARG;
 	KR(fg_euler_build(c, c->u, c->a));
+	if (c->o.scheme == FEMGPU_CSR) KR(fgh_blockcsr_assemble(&c->csr, 12, c->ebe, c->neq, c->stream));
 	c->built = 1;
 	c->have_bd = 0;
 	return 0;
@@ -208,6 +251,13 @@ int femgpu_euler_precond_setup_dev(femgpu_euler *c)
 	if (!c) return FEMGPU_E_ARG;
 	if (!c->built) { fgh_set_error("precond_setup before build"); return FEMGPU_E_NOT_BUILT; }
 	if (c->o.precision == FEMGPU_MIXED_IR) KR(fg_ebe_to_f32(c->ebe));
+	if (c->o.precond == FEMGPU_PREC_ILU0) {
+		/* ILUp_precond_setup.c:8-167 at fill level 0, then R := M^-1 R */
+		KR(fgh_blockcsr_factor(&c->csr, c->stream));
+		c->have_bd = 1;
+		if (c->o.solver == FEMGPU_PGMRES) KR(fg_ilu0_apply64(c->csr.ilu, c->R, c->R, NULL));
+		return 0;
+	}
 	if (c->o.precond != FEMGPU_PREC_BLOCKDIAG) return 0;     /* NO_precond_setup */
 	KR(fg_ebe_blockdiag_setup(c->ebe));
 	c->ebe->have_bd = 1;
@@ -232,7 +282,7 @@ static int solve(femgpu_euler *c, const double *B, double *X, int *iters)
 	fg_linop op;
 	double normb2;
 	int it = 0, rc;
-	if (c->o.precond == FEMGPU_PREC_BLOCKDIAG && !c->have_bd) {
+	if (c->o.precond != FEMGPU_PREC_NOT && !c->have_bd) {
 		fgh_set_error("solve before precond_setup");
 		return FEMGPU_E_NOT_BUILT;
 	}

@@ -51,6 +51,23 @@ int fgh_kry_cycle(const struct fg_krylov *k, const struct fg_linop *op, const do
 /* ||B||^2 on the device, returned to the host (synchronises the stream). */
 int fgh_kry_dot_host(const struct fg_krylov *k, const double *a, const double *b, int n, double *out);
 
+/* Block CSR storage of an EBE element system with M = 3*ndof equations per
+ * element (host/blockcsr.c): the pattern built on the device from the EBE
+ * context's lm and incidence lists and, when ilu0, the ILU(0) structure of
+ * a transport context (solver: the Krylov solver its sweeps serve,
+ * ilu_blocks as femgpu_transport_opts.ilu_blocks). */
+struct fg_blockcsr;
+struct femgpu_ebe;
+int fgh_blockcsr_create(struct fg_blockcsr *b, int M, const struct femgpu_ebe *ebe, int nel, int neq,
+                        cudaStream_t s, int ilu0, int solver, int ilu_blocks);
+void fgh_blockcsr_destroy(struct fg_blockcsr *b);
+/* csr_assembly.c per row from the element matrices ebe->A. */
+int fgh_blockcsr_assemble(struct fg_blockcsr *b, int M, const struct femgpu_ebe *ebe, int neq, cudaStream_t s);
+/* ILU(0) factorisation (ILUp_precond_setup.c:66-167 at fill level 0) of
+ * the current values; FEMGPU_E_ZERO_PIVOT on a zero pivot. */
+int fgh_blockcsr_factor(struct fg_blockcsr *b, cudaStream_t s);
+void fgh_blockcsr_set_stream(struct fg_blockcsr *b, cudaStream_t s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,74 +49,12 @@ static int op_precond(void *ctx, const double *p, double *z, const int *active)
 static int op_matvec_csr(void *ctx, const double *p, double *q, const int *active)
 {
 	femgpu_ns *c = (femgpu_ns *)ctx;
-	return fg_csrmv64(c->neq, c->IA, c->JA, c->AA, p, q, active, c->stream);
+	return fg_csrmv64(c->neq, c->csr.IA, c->csr.JA, c->csr.AA, p, q, active, c->stream);
 }
 
 static int op_precond_ilu(void *ctx, const double *p, double *z, const int *active)
 {
-	return fg_ilu0_apply64(((femgpu_ns *)ctx)->ilu, p, z, active);
-}
-
-/* csr_Initialization (reordering NOT) on the device, and the ILU(0) engine
- * (level schedules and sweep programs of the pattern, factor storage) on a
- * transport context that holds only this CSR system. */
-static int create_csr(femgpu_ns *c)
-{
-	femgpu_transport *t;
-	int *hIA = NULL, *hJA = NULL, *err = NULL, rc;
-	size_t n1 = (size_t)c->neq + 1;
-	DM(err, sizeof(int));
-	CK(cudaMemset(err, 0, sizeof(int)));
-	rc = fg_build_csr_m(9, c->nel, c->neq, c->ebe->ri_ptr, c->ebe->ri, c->ebe->lm, c->stream, err, &c->IA, &c->JA,
-	                    &c->sbe, &c->nnz);
-	cudaFree(err);
-	if (rc) { fgh_set_error("Navier-Stokes CSR pattern: %d", rc); return rc > 0 ? FEMGPU_E_CUDA : rc; }
-	DM(c->AA, sizeof(double) * ((size_t)c->nnz + 1));
-	CK(cudaMemset(c->AA, 0, sizeof(double) * ((size_t)c->nnz + 1)));
-	if (c->o.precond != FEMGPU_PREC_ILU0) return 0;
-	t = c->ilu = calloc(1, sizeof *t);
-	if (!t) return FEMGPU_E_NOMEM;
-	femgpu_transport_default_opts(&t->o);
-	t->o.precond = FEMGPU_PREC_ILU0;
-	t->o.solver = c->o.solver;
-	t->o.ilu_blocks = c->o.ilu_blocks;
-	t->neq = c->neq; t->nnz = c->nnz;
-	t->IA = c->IA; t->JA = c->JA; t->A = c->AA;
-	t->stream = c->stream;
-	DM(t->st, sizeof(fg_status));
-	CK(cudaMemset(t->st, 0, sizeof(fg_status)));
-	t->ilu.n = c->neq; t->ilu.nnz = c->nnz;
-	DM(t->ilu.LU, sizeof(double) * ((size_t)c->nnz + 1));
-	DM(t->ilu.Dinv, sizeof(double) * n1);
-	hIA = malloc(sizeof(int) * n1);
-	hJA = malloc(sizeof(int) * ((size_t)c->nnz + 1));
-	if (!hIA || !hJA) { free(hIA); free(hJA); return FEMGPU_E_NOMEM; }
-	rc = (cudaMemcpy(hIA, c->IA, sizeof(int) * n1, cudaMemcpyDeviceToHost) != cudaSuccess ||
-	      cudaMemcpy(hJA, c->JA, sizeof(int) * (size_t)c->nnz, cudaMemcpyDeviceToHost) != cudaSuccess)
-	     ? FEMGPU_E_CUDA : fg_ilu_prepare(t, hIA, hJA);
-	free(hIA); free(hJA);
-	if (rc) { fgh_set_error("Navier-Stokes ILU(0) set-up: %d", rc); return rc > 0 ? FEMGPU_E_CUDA : rc; }
-	c->have_ilu = 1;
-	return 0;
-}
-
-static void destroy_csr(femgpu_ns *c)
-{
-	femgpu_transport *t = c->ilu;
-	if (t) {
-		if (c->have_ilu) fg_ilu_free(t);
-		if (t->st) cudaFree(t->st);
-		if (t->ilu.LU) cudaFree(t->ilu.LU);
-		if (t->ilu.Dinv) cudaFree(t->ilu.Dinv);
-		free(t);
-		c->ilu = NULL;
-	}
-	if (c->IA) cudaFree(c->IA);
-	if (c->JA) cudaFree(c->JA);
-	if (c->sbe) cudaFree(c->sbe);
-	if (c->AA) cudaFree(c->AA);
-	c->IA = c->JA = c->sbe = NULL;
-	c->AA = NULL;
+	return fg_ilu0_apply64(((femgpu_ns *)ctx)->csr.ilu, p, z, active);
 }
 
 static int up(double **dst, const double *src, size_t n)
@@ -150,7 +88,9 @@ static int create(femgpu_ns *c, const femgpu_ns_opts *o, int nnodes, const doubl
 		return rc;
 	rc = fgh_kry_alloc(&c->kry, neq, o->kmax, o->solver == FEMGPU_FGMRES ? 1 : 0, c->stream);
 	if (rc) return rc;
-	if (o->scheme == FEMGPU_CSR && (rc = create_csr(c))) return rc;
+	if (o->scheme == FEMGPU_CSR &&
+	    (rc = fgh_blockcsr_create(&c->csr, 9, c->ebe, c->nel, c->neq, c->stream, o->precond == FEMGPU_PREC_ILU0,
+	                              o->solver, o->ilu_blocks))) return rc;
 	CK(cudaStreamSynchronize(c->stream));
 	return 0;
 }
@@ -187,7 +127,7 @@ void femgpu_ns_destroy(femgpu_ns *c)
 	int i;
 	if (!c) return;
 	if (c->stream) cudaStreamSynchronize(c->stream);
-	destroy_csr(c);
+	fgh_blockcsr_destroy(&c->csr);
 	if (c->ebe) femgpu_ebe_destroy(c->ebe);
 	{
 		void *p[] = { c->x, c->y, c->upresc, c->f, c->u, c->F, c->s, c->Fold, c->Re, c->dold, c->nold };
@@ -204,7 +144,7 @@ int femgpu_ns_set_stream(femgpu_ns *c, void *stream)
 	CK(cudaStreamSynchronize(c->stream));
 	c->stream = stream ? (cudaStream_t)stream : c->own_stream;
 	c->kry.stream = c->stream;
-	if (c->ilu) c->ilu->stream = c->stream;
+	fgh_blockcsr_set_stream(&c->csr, c->stream);
 	KR(femgpu_ebe_set_stream(c->ebe, c->stream));
 	return 0;
 }
@@ -228,8 +168,7 @@ int femgpu_ns_build_dev(femgpu_ns *c)
 	if (!c) return FEMGPU_E_ARG;
 	KR(fg_ns_build(c, c->nbuild == 0));
 	if (c->o.scheme == FEMGPU_CSR)                              /* csr_assembly, element by element */
-		KR(fg_assemble_csr_m(9, c->neq, c->nnz, c->IA, c->sbe, c->ebe->ri_ptr, c->ebe->ri, c->ebe->A, c->AA,
-		                     c->stream));
+		KR(fgh_blockcsr_assemble(&c->csr, 9, c->ebe, c->neq, c->stream));
 	c->nbuild++;
 	c->have_bd = 0;
 	return 0;
@@ -238,10 +177,12 @@ int femgpu_ns_build_dev(femgpu_ns *c)
 int femgpu_ns_csr(femgpu_ns *c, int *n_nnz, int *IA, int *JA, double *AA)
 {
 	if (!c || !n_nnz || c->o.scheme != FEMGPU_CSR) return FEMGPU_E_ARG;
-	n_nnz[0] = c->neq; n_nnz[1] = c->nnz;
-	if (IA) CK(cudaMemcpyAsync(IA, c->IA, sizeof(int) * ((size_t)c->neq + 1), cudaMemcpyDeviceToHost, c->stream));
-	if (JA) CK(cudaMemcpyAsync(JA, c->JA, sizeof(int) * (size_t)c->nnz, cudaMemcpyDeviceToHost, c->stream));
-	if (AA) CK(cudaMemcpyAsync(AA, c->AA, sizeof(double) * ((size_t)c->nnz + 1), cudaMemcpyDeviceToHost, c->stream));
+	n_nnz[0] = c->neq; n_nnz[1] = c->csr.nnz;
+	if (IA) CK(cudaMemcpyAsync(IA, c->csr.IA, sizeof(int) * ((size_t)c->neq + 1), cudaMemcpyDeviceToHost,
+	                           c->stream));
+	if (JA) CK(cudaMemcpyAsync(JA, c->csr.JA, sizeof(int) * (size_t)c->csr.nnz, cudaMemcpyDeviceToHost, c->stream));
+	if (AA) CK(cudaMemcpyAsync(AA, c->csr.AA, sizeof(double) * ((size_t)c->csr.nnz + 1), cudaMemcpyDeviceToHost,
+	                           c->stream));
 	CK(cudaStreamSynchronize(c->stream));
 	return 0;
 }
@@ -267,13 +208,9 @@ static int setup_dev(femgpu_ns *c)
 	c->setup_tag++;
 	if (c->o.precond == FEMGPU_PREC_ILU0) {
 		/* ILUp_precond_setup.c:8-167 at fill level 0, then F := M^-1 F */
-		int err = 0;
-		KR(fg_ilu0_factor(c->ilu));
-		CK(cudaMemcpyAsync(&err, &c->ilu->st->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-		CK(cudaStreamSynchronize(c->stream));
-		if (err) { fgh_set_error("ILU(0) factorisation: %d", err); return err; }
+		KR(fgh_blockcsr_factor(&c->csr, c->stream));
 		c->have_bd = 1;
-		if (c->o.solver == FEMGPU_PGMRES) KR(fg_ilu0_apply64(c->ilu, c->F, c->F, NULL));
+		if (c->o.solver == FEMGPU_PGMRES) KR(fg_ilu0_apply64(c->csr.ilu, c->F, c->F, NULL));
 		return 0;
 	}
 	if (c->o.precond != FEMGPU_PREC_BLOCKDIAG) return 0;

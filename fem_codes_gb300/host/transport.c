@@ -319,6 +319,17 @@ int femgpu_transport_ilu_blocks(const femgpu_transport *t, int *first, int cap)
 	return P;
 }
 
+int femgpu_transport_ilu_chain(const femgpu_transport *t, int *levels)
+{
+	if (!t) return FEMGPU_E_ARG;
+	if (!t->sweeps.block_first) return FEMGPU_E_NOT_BUILT;
+	if (levels) {
+		levels[0] = t->sweeps.chain ? t->sweeps.lo64c.nlev : 0;
+		levels[1] = t->sweeps.chain ? t->sweeps.up64c.nlev : 0;
+	}
+	return t->sweeps.chain ? 1 : 0;
+}
+
 int femgpu_transport_get_pattern(const femgpu_transport *t, int *IA, int *JA, int *sbe, int *order,
 		int *node_id)
 {

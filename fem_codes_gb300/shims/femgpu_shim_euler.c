@@ -2,9 +2,10 @@
  * femgpu_shim_euler.c -- binds libfemgpu into the 2D Euler driver
  * (03_Euler_Equations/2D) through the reference's own function pointers
  * (FemFunctionsType / FemOtherFunctionsType, EulerEquations.h:136-170), for
- * EBE storage with the nodal block-diagonal preconditioner and the
- * predictor-multicorrector (Predictor_Old.c) that calls Build,
- * precond_setup and the 6-argument solver once per corrector.
+ * EBE storage with the nodal block-diagonal preconditioner or CSR storage
+ * (reordering NOT) with ILU(0), and the predictor-multicorrector
+ * (Predictor_Old.c) that calls Build, precond_setup and the 6-argument
+ * solver once per corrector.
  *
  * Build, inside the driver's 01_CommonFiles (its own header):
  *     gcc -DEulerEquations2D -I. -I<repo>/include -c femgpu_shim_euler.c
@@ -55,9 +56,9 @@ static int fail(const char *what, int rc)
 void femgpu_shim_euler_set_abort(int on) { g_abort = on; }
 int femgpu_shim_euler_error(void) { return g_err; }
 femgpu_euler *femgpu_shim_euler_context(void) { return g_eu; }
-/* copy != 0: every Build also copies the 12x12 element matrices into
- * MatrixData->Aaux (the EBE layout A[e][144]); by default they stay on the
- * device. */
+/* copy != 0: every Build also copies the matrix storage back -- the 12x12
+ * element matrices into MatrixData->Aaux (EBE layout A[e][144]) or the CSR
+ * values into MatrixData->AA; by default they stay on the device. */
 void femgpu_shim_euler_copy_matrix(int copy) { g_copy_matrix = copy; }
 /* fgmres != 0: flexible GMRES accepted on the unpreconditioned residual (and
  * precond_setup leaves R unpreconditioned) instead of the reference's pgmres. */
@@ -70,12 +71,17 @@ static int eu_of(ParametersType *P, FemStructsType *FS, FemFunctionsType *FF)
 	double *x, *y, *up;
 	int *nid, *vert;
 	if (g_eu) return 0;
-	if (strcasecmp(P->MatrixVectorProductScheme, "EBE") != 0) return FEMGPU_E_ARG;
 	if (strcasecmp(P->StabilizationForm, "SUPG") != 0 || strcasecmp(P->ShockCapture, "CAU") != 0)
 		return FEMGPU_E_ARG;
 	femgpu_euler_default_opts(&o);
+	if (!strcasecmp(P->MatrixVectorProductScheme, "EBE")) o.scheme = FEMGPU_EBE;
+	else if (!strcasecmp(P->MatrixVectorProductScheme, "CSR") && !strcasecmp(P->reordering, "NOT"))
+		o.scheme = FEMGPU_CSR;
+	else return FEMGPU_E_ARG;
 	if (!strcasecmp(P->Preconditioner, "NOT")) o.precond = FEMGPU_PREC_NOT;
-	else if (!strcasecmp(P->Preconditioner, "BlockDiag")) o.precond = FEMGPU_PREC_BLOCKDIAG;
+	else if (!strcasecmp(P->Preconditioner, "BlockDiag") && o.scheme == FEMGPU_EBE) o.precond = FEMGPU_PREC_BLOCKDIAG;
+	else if (!strncmp(P->Preconditioner, "ILU", 3) && (!P->Preconditioner[3] || atoi(P->Preconditioner + 3) == 0) &&
+	         o.scheme == FEMGPU_CSR) o.precond = FEMGPU_PREC_ILU0;
 	else return FEMGPU_E_ARG;
 	o.gamma = FF->gamma(FS->Node[0].x, FS->Node[0].y);
 	o.mach = P->Mach;
@@ -113,12 +119,18 @@ out:
 }
 
 /* FemOtherFunctions->Build (Build_M_K_F_SUPG.c:6): Ae = Me + alpha dt Ke and
- * R = -(Me du + Ke u) from FS->u and FS->du, R into FS->F. */
+ * R = -(Me du + Ke u) from FS->u and FS->du, R into FS->F (CSR storage: the
+ * element matrices assembled into the pattern, csr_assembly.c). */
 int femgpu_shim_euler_Build(ParametersType *P, MatrixDataType *M, FemStructsType *FS, FemFunctionsType *FF)
 {
+	const int csr = !strcasecmp(P->MatrixVectorProductScheme, "CSR");
 	int rc = eu_of(P, FS, FF);
 	if (rc) return fail("Build (context)", rc);
-	rc = femgpu_euler_build(g_eu, FS->u, FS->du, g_copy_matrix ? M->Aaux : NULL, FS->F);
+	rc = femgpu_euler_build(g_eu, FS->u, FS->du, g_copy_matrix && !csr ? M->Aaux : NULL, FS->F);
+	if (!rc && g_copy_matrix && csr) {
+		int nn[2];
+		rc = femgpu_euler_csr(g_eu, nn, NULL, NULL, NULL, M->AA);
+	}
 	return rc ? fail("Build", rc) : 0;
 }
 
@@ -133,22 +145,25 @@ int femgpu_shim_euler_precond_setup(ParametersType *P, MatrixDataType *M, FemStr
 	return rc ? fail("precond_setup", rc) : 0;
 }
 
-/* FemFunctions->mv (ebemvNDOF4.c:5-112): Q = A P. */
+/* FemFunctions->mv (ebemvNDOF4.c:5-112): Q = A P (EBE storage). */
 int femgpu_shim_euler_mv(ParametersType *P, MatrixDataType *M, FemStructsType *FS, double *Pv, double *Q)
 {
 	int rc;
-	(void)P; (void)M; (void)FS;
+	(void)M; (void)FS;
 	if (!g_eu) return fail("mv", FEMGPU_E_NOT_BUILT);
+	if (strcasecmp(P->MatrixVectorProductScheme, "EBE") != 0) return fail("mv (CSR storage)", FEMGPU_E_ARG);
 	rc = femgpu_ebe_matvec(femgpu_euler_ebe(g_eu), Pv, Q);
 	return rc ? fail("mv", rc) : 0;
 }
 
-/* FemFunctions->precond (BlockDiag_precond.c): z = D^-1 p, p == z allowed. */
+/* FemFunctions->precond (BlockDiag_precond.c): z = D^-1 p, p == z allowed
+ * (EBE storage). */
 int femgpu_shim_euler_precond(ParametersType *P, MatrixDataType *M, FemStructsType *FS, double *p, double *z)
 {
 	int rc;
-	(void)P; (void)M; (void)FS;
+	(void)M; (void)FS;
 	if (!g_eu) return fail("precond", FEMGPU_E_NOT_BUILT);
+	if (strcasecmp(P->Preconditioner, "BlockDiag") != 0) return fail("precond (not BlockDiag)", FEMGPU_E_ARG);
 	rc = femgpu_ebe_blockdiag_apply(femgpu_euler_ebe(g_eu), p, z);
 	return rc ? fail("precond", rc) : 0;
 }

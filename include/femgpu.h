@@ -129,12 +129,36 @@ int femgpu_transport_info(const femgpu_transport *ctx, int *info);
  * FEMGPU_E_NOT_BUILT before the ILU(0) structure exists (CSR + ILU0 only). */
 int femgpu_transport_ilu_blocks(const femgpu_transport *ctx, int *first, int cap);
 
+/* 1 when the context's ILU(0) has chain-scan programs -- which its FGMRES
+ * (fused-arithmetic) and FP32 sweeps then run: rows chained to their sweep
+ * predecessor solved 32 at a time by a warp scan, results equal to the
+ * row-by-row sweeps to rounding -- else 0 (too few chained rows; the
+ * reference's GMRES always runs the bit-identical row-by-row sweeps).
+ * levels [2] (may be NULL) receives their level counts (forward, backward).
+ * FEMGPU_E_NOT_BUILT before the ILU(0) structure exists. */
+int femgpu_transport_ilu_chain(const femgpu_transport *ctx, int *levels);
+
 /* The same cut for a CSR pattern on the host, no device needed: returns the
  * number of runs R = max(min(P, n), 1) and writes R + 1 row boundaries to
  * first (cap = room in first; FEMGPU_E_ARG when cap < R + 1).  The pattern
  * must have IA[0] = 0, non-decreasing IA, columns in 0..n-1 and strictly
  * ascending columns in every row; anything else returns FEMGPU_E_ARG. */
 int femgpu_ilu_block_cut(int n, const int *IA, const int *JA, int P, int *first, int cap);
+
+/* The chain-scan segmentation of one ILU(0) sweep (lower != 0: forward) of a
+ * CSR pattern with the block cut of P, on the host, no device needed: rows
+ * of a matrix block in sweep order are grouped into segments of up to 32,
+ * each row after a segment's first depending on its predecessor (the
+ * recurrence a warp scan solves), segments get dependency levels and each
+ * level's segments are packed into 32-slot chunks.  Returns the slot count
+ * (padding included) and info[4] = {levels, deepest block's segment levels,
+ * deepest block's row levels, most dependencies of a row besides its
+ * predecessor}; when the arrays are given (room: cap_slots, cap_levels),
+ * slot_row [slots] (-1 padding), slot_pred [slots] (CSR position of the row's
+ * coupling to its predecessor, -1 at a segment start) and lstart [levels+1]
+ * (first slot of each level).  Same pattern checks as femgpu_ilu_block_cut. */
+int femgpu_ilu_chain_segments(int n, const int *IA, const int *JA, int P, int lower, int *info,
+		int *slot_row, int *slot_pred, int *lstart, int cap_slots, int cap_levels);
 
 /* Copies of the device-built structure, for parity checks against the
  * reference (IA [neq+1], JA [nnz], CSR_by_Element [9*nel]; EDE: lm2 [2*nedge],
@@ -257,13 +281,20 @@ typedef struct femgpu_euler_opts {
 	                     /* with FGMRES: FP32 element matrices and           */
 	                     /* preconditioner inside the Arnoldi cycles, every  */
 	                     /* restart from the FP64 residual, a solve accepted */
-	                     /* on the FP64 residual                             */
+	                     /* on the FP64 residual (EBE storage)               */
+	int scheme;          /* MatrixVectorProductScheme: FEMGPU_EBE (12x12     */
+	                     /* element blocks, NOT / BLOCKDIAG) or FEMGPU_CSR   */
+	                     /* (csr_Initialization.c / csr_assembly.c of the    */
+	                     /* Euler driver, reordering NOT; NOT / ILU0)        */
+	int ilu_blocks;      /* CSR + ILU0: 0 the whole matrix (the reference's), */
+	                     /* P > 1 block ILU(0) over P row blocks (as         */
+	                     /* femgpu_transport_opts.ilu_blocks)                */
 } femgpu_euler_opts;
 
 void femgpu_euler_default_opts(femgpu_euler_opts *o);
 
 /* Device-resident Euler problem (replaces MatrixDataType / FemStructsType of
- * EulerEquations.h:84-134 for the EBE scheme). */
+ * EulerEquations.h:84-134 for the EBE and CSR schemes). */
 typedef struct femgpu_euler femgpu_euler;
 
 /* Preprocess for the EBE scheme (Preprocess.c, Fill_ID.c, Fill_LM.c):
@@ -292,6 +323,11 @@ int femgpu_euler_precond_setup_dev(femgpu_euler *ctx);
 /* solver (pgmres.c:4-211 with FemFunctions->mv = ebemvNDOF4): Da solves
  * A Da = R.  B_host [neq+1] replaces R when non-NULL; X_host receives Da. */
 int femgpu_euler_solve(femgpu_euler *ctx, const double *B_host, double *X_host, int *iters);
+/* CSR storage: sizes n_nnz = {neq, nnz} and (arrays may be NULL) the pattern
+ * IA [neq+1], JA [nnz], CSR_by_Element sbe [144*nel] (nnz for a prescribed
+ * row or column, csr_Initialization.c) and the values of the last build AA
+ * [nnz+1]; FEMGPU_E_ARG for EBE storage. */
+int femgpu_euler_csr(femgpu_euler *ctx, int *n_nnz, int *IA, int *JA, int *sbe, double *AA);
 int femgpu_euler_solve_dev(femgpu_euler *ctx, int *iters);
 /* Predictor_Old (Time_Integration/Predictor_Old.c:46-132) for nsteps time
  * steps of ncorr correctors from u (host [neq+1], in/out; NULL = the device

@@ -8,6 +8,11 @@
  *
  * The solver is the 6-argument GMRES adapter of ref_gmres6.h (the shipped
  * pgmres.c has only the steady-transport 4-argument form).
+ *
+ * CSR storage with ILU(0) (csr_Initialization.c and csr_assembly.c of the
+ * Euler driver, reordering NOT, csrmv, ILUp_precond_setup.c /
+ * ILUp_precond.c: setMatrixVectorProductType.c:24 and setPreconditioner.c:
+ * 118-128) is the csr != 0 form of the set-up.
  */
 #include "EulerEquations.h"
 
@@ -26,11 +31,16 @@ double REFLETIDO_v1presc(double, double);
 double REFLETIDO_v2presc(double, double);
 double REFLETIDO_epresc(double, double);
 static double zero_theta(double x, double y) { return 0.0; }
+void csr_Initialization(ParametersType *, NodeType *, int **, int **, int **, int **, int ***, int **, int ***);
+void csr_assembly(ParametersType *, MatrixDataType *, FemStructsType *, int, double (*)[12]);
+int csrmv(ParametersType *, MatrixDataType *, FemStructsType *, double *, double *);
+int ILUp_precond_setup(ParametersType *, MatrixDataType *, FemStructsType *, int, double *);
+int ILUp_precond(ParametersType *, MatrixDataType *, FemStructsType *, double *, double *);
 
 #include "ref_gmres6.h"
 
-static void setup(int nnodes, const double *x, const double *y, const int *node_id, int nel, const int *vert,
-                  int neq, double alpha, double dt, double stab_tol,
+static void setup(int csr, int nnodes, const double *x, const double *y, const int *node_id, int nel,
+                  const int *vert, int neq, double alpha, double dt, double stab_tol,
                   ParametersType **Po, MatrixDataType **Mo, FemStructsType **FSo, FemFunctionsType **FFo)
 {
 	int I, k;
@@ -40,14 +50,15 @@ static void setup(int nnodes, const double *x, const double *y, const int *node_
 	FemFunctionsType *FF = mycalloc("FF", 1, sizeof(FemFunctionsType));
 	NodeType *Node = mycalloc("Node", nnodes, sizeof(NodeType));
 	ElementType *El = mycalloc("El", nel, sizeof(ElementType));
-	int **lm = mycalloc("lm", nel, sizeof(int *));
+	int **lm = mycalloc("lm", nel, sizeof(int *)), *lmaux = mycalloc("lmaux", nel * 12, sizeof(int));
 	double **A = mycalloc("A", nel, sizeof(double *)), *Aaux = mycalloc("Aaux", nel * 144, sizeof(double));
 	AuxBuildStructuresType *aux = mycalloc("aux", 1, sizeof(AuxBuildStructuresType));
 	P->nnodes = nnodes; P->nel = nel; P->neq = neq;
 	P->Alpha = alpha; P->Alpha_Build = alpha; P->DeltaT = dt; P->DeltaT_Build = dt;
 	P->StabilizationTolerance = stab_tol;
-	strcpy(P->MatrixVectorProductScheme, "EBE");
-	strcpy(P->Preconditioner, "BlockDiag");
+	strcpy(P->MatrixVectorProductScheme, csr ? "CSR" : "EBE");
+	strcpy(P->Preconditioner, csr ? "ILU0" : "BlockDiag");
+	strcpy(P->reordering, "NOT");
 	for (I = 0; I < nnodes; I++) {
 		Node[I].x = x[I]; Node[I].y = y[I];
 		Node[I].rhoType = Node[I].v1Type = Node[I].v2Type = Node[I].eType = 1;
@@ -55,11 +66,17 @@ static void setup(int nnodes, const double *x, const double *y, const int *node_
 	}
 	for (I = 0; I < nel; I++) {
 		for (k = 0; k < 3; k++) El[I].Vertex[k] = vert[3 * I + k];
-		lm[I] = mycalloc("lm", 12, sizeof(int));
+		lm[I] = lmaux + 12 * I;
 		A[I] = Aaux + 144 * I;
 	}
 	Fill_LM(neq, nel, lm, Node, El);
 	M->A = A; M->Aaux = Aaux;
+	if (csr) {
+		int *IA, *JA, *perm, *invperm, **sbe;
+		csr_Initialization(P, Node, &JA, &IA, &perm, &invperm, &lm, &lmaux, &sbe);
+		M->AA = mycalloc("AA", P->nnzero + 1, sizeof(double));
+		M->IA = IA; M->JA = JA; M->Scheme_by_Element = sbe; M->Perm = perm; M->invPerm = invperm;
+	}
 	aux->tolerance = stab_tol;
 	FS->lm = lm; FS->Node = Node; FS->Element = El; FS->AuxBuild = aux;
 	FS->F = mycalloc("F", neq + 1, sizeof(double));
@@ -72,9 +89,10 @@ static void setup(int nnodes, const double *x, const double *y, const int *node_
 	FF->Ax_Ay_calculations = dimensional_Ax_Ay_calculations;
 	FF->ShockCapture = Delta_CAU;
 	FF->BC_theta = zero_theta;
-	FF->assembly = ebe_assembly;
-	FF->mv = ebemvNDOF4;
-	FF->precond = BlockDiag_precond;
+	FF->assembly = csr ? csr_assembly : ebe_assembly;
+	FF->mv = csr ? csrmv : ebemvNDOF4;
+	FF->precond = csr ? ILUp_precond : BlockDiag_precond;
+	FF->precond_setup = csr ? ILUp_precond_setup : BlockDiag_precond_EBE_setup;
 	*Po = P; *Mo = M; *FSo = FS; *FFo = FF;
 }
 
@@ -84,7 +102,7 @@ int ref_euler_build(int nnodes, const double *x, const double *y, const int *nod
                     double *Ae, double *R)
 {
 	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF;
-	setup(nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
+	setup(0, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
 	memcpy(FS->u, u, sizeof(double) * (neq + 1));
 	memcpy(FS->du, du, sizeof(double) * (neq + 1));
 	Build_M_K_F_SUPG(P, M, FS, FF);
@@ -96,13 +114,13 @@ int ref_euler_build(int nnodes, const double *x, const double *y, const int *nod
 /* Predictor_Old.c:46-132 with ncorr correctors per step (StopByIterations,
  * Criteria.c:25-31) and nsteps steps, BlockDiag + EBE + the GMRES above.
  * u in/out; ahist [nsteps*(neq+1)], uhist likewise; iters [nsteps*ncorr]. */
-int ref_euler_predictor(int nnodes, const double *x, const double *y, const int *node_id, int nel,
-                        const int *vert, int neq, double alpha, double dt, double stab_tol, int kmax,
-                        int lmax, double tol, int nsteps, int ncorr, double *u_io, double *uhist, int *iters)
+static int predictor(int csr, int nnodes, const double *x, const double *y, const int *node_id, int nel,
+                     const int *vert, int neq, double alpha, double dt, double stab_tol, int kmax,
+                     int lmax, double tol, int nsteps, int ncorr, double *u_io, double *uhist, int *iters)
 {
 	int I, step, i, tag = 1;
 	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF;
-	setup(nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
+	setup(csr, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
 	P->KrylovBasisVectorsQuantity = kmax; P->LinearMaxIter = lmax; P->SolverTolerance = tol;
 	double *u = FS->u, *a = FS->du, *R = FS->F, *Da = calloc(neq + 1, sizeof(double));
 	memcpy(u, u_io, sizeof(double) * (neq + 1));
@@ -111,7 +129,7 @@ int ref_euler_predictor(int nnodes, const double *x, const double *y, const int 
 		for (i = 0; i < ncorr; i++) {
 			int before = P->iterations;
 			Build_M_K_F_SUPG(P, M, FS, FF);
-			BlockDiag_precond_EBE_setup(P, M, FS, tag++, R);
+			FF->precond_setup(P, M, FS, tag++, R);
 			gmres6(P, M, FS, FF, R, Da);
 			iters[step * ncorr + i] = P->iterations - before;
 			for (I = 0; I < neq; I++) a[I] += 1 * Da[I];
@@ -122,4 +140,55 @@ int ref_euler_predictor(int nnodes, const double *x, const double *y, const int 
 	memcpy(u_io, u, sizeof(double) * (neq + 1));
 	free(Da);
 	return 0;
+}
+
+int ref_euler_predictor(int nnodes, const double *x, const double *y, const int *node_id, int nel,
+                        const int *vert, int neq, double alpha, double dt, double stab_tol, int kmax,
+                        int lmax, double tol, int nsteps, int ncorr, double *u_io, double *uhist, int *iters)
+{
+	return predictor(0, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, kmax, lmax, tol, nsteps, ncorr,
+	                 u_io, uhist, iters);
+}
+
+/* The same predictor with CSR storage and ILU(0). */
+int ref_euler_predictor_csr(int nnodes, const double *x, const double *y, const int *node_id, int nel,
+                            const int *vert, int neq, double alpha, double dt, double stab_tol, int kmax,
+                            int lmax, double tol, int nsteps, int ncorr, double *u_io, double *uhist, int *iters)
+{
+	return predictor(1, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, kmax, lmax, tol, nsteps, ncorr,
+	                 u_io, uhist, iters);
+}
+
+/* CSR set-up and one Build with CSR assembly on (u, du): pattern IA [neq+1],
+ * JA [nnz_cap], CSR_by_Element sbe [nel*144], the assembled values AA
+ * [nnz_cap+1], the residual R [neq+1], R after precond_setup (ILU(0),
+ * R := M^-1 R) Rp [neq+1] and one ILU(0) application z = M^-1 p [neq+1].
+ * Returns nnz (or -1 when nnz_cap is too small). */
+int ref_euler_build_csr(int nnodes, const double *x, const double *y, const int *node_id, int nel, const int *vert,
+                        int neq, double alpha, double dt, double stab_tol, const double *u, const double *du,
+                        int nnz_cap, int *IA, int *JA, int *sbe, double *AA, double *R, double *Rp, const double *p,
+                        double *z)
+{
+	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF;
+	int nnz, e;
+	size_t n1 = (size_t)neq + 1;
+	setup(1, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
+	nnz = P->nnzero;
+	if (nnz > nnz_cap) return -1;
+	memcpy(IA, M->IA, sizeof(int) * n1);
+	memcpy(JA, M->JA, sizeof(int) * (size_t)nnz);
+	for (e = 0; e < nel; e++) memcpy(sbe + (size_t)144 * e, M->Scheme_by_Element[e], sizeof(int) * 144);
+	memcpy(FS->u, u, sizeof(double) * n1);
+	memcpy(FS->du, du, sizeof(double) * n1);
+	Build_M_K_F_SUPG(P, M, FS, FF);
+	memcpy(AA, M->AA, sizeof(double) * ((size_t)nnz + 1));
+	memcpy(R, FS->F, sizeof(double) * n1);
+	memcpy(Rp, FS->F, sizeof(double) * n1);
+	FF->precond_setup(P, M, FS, 1, Rp);
+	{
+		double *pp = mycalloc("p", n1, sizeof(double));
+		memcpy(pp, p, sizeof(double) * n1);
+		FF->precond(P, M, FS, pp, z);
+	}
+	return nnz;
 }

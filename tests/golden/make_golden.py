@@ -224,6 +224,11 @@ def main_euler():
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp,
                                         _ip]
+    lib.ref_euler_predictor_csr.argtypes = lib.ref_euler_predictor.argtypes
+    lib.ref_euler_build_csr.restype = ctypes.c_int
+    lib.ref_euler_build_csr.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp, ctypes.c_int,
+                                        _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp]
     for name, (nx, ny, pert, seed, alpha, cfl, stol, nsteps, ncorr) in EULER_CASES.items():
         mesh = structured_mesh(nx, ny, lx=4.0, ly=1.0, perturb=pert, seed=seed)
         pb = refletido_problem(mesh)
@@ -245,13 +250,36 @@ def main_euler():
         iters = np.zeros(nsteps * ncorr, np.int32)
         lib.ref_euler_predictor(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol,
                                 kmax, lmax, tol, nsteps, ncorr, up, uhist, iters)
+        # CSR storage with ILU(0): pattern, slot map, assembled values, R := M^-1 R,
+        # one ILU(0) application, and the predictor run with ILU(0)-GMRES
+        cap = 144 * mesh.nel
+        IA = np.zeros(neq + 1, np.int32)
+        JA = np.zeros(cap, np.int32)
+        sbe = np.zeros(144 * mesh.nel, np.int32)
+        AA = np.zeros(cap + 1)
+        Rc = np.zeros(neq + 1)
+        Rp = np.zeros(neq + 1)
+        pz = rng.uniform(-1.0, 1.0, neq + 1)
+        pz[neq] = 0.0
+        zc = np.zeros(neq + 1)
+        nnz = lib.ref_euler_build_csr(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol, u,
+                                      du, cap, IA, JA, sbe, AA, Rc, Rp, pz, zc)
+        assert nnz > 0
+        upc = pb.u0.copy()
+        uhc = np.zeros(nsteps * (neq + 1))
+        itc = np.zeros(nsteps * ncorr, np.int32)
+        lib.ref_euler_predictor_csr(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol,
+                                    kmax, lmax, tol, nsteps, ncorr, upc, uhc, itc)
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id,
             neq=neq, upresc=pb.upresc, u0=pb.u0, gamma=pb.gamma, alpha=alpha, dt=dt, stab_tol=stol,
             u=u, du=du, Ae=Ae.reshape(mesh.nel, 144), R=R, kmax=kmax, lmax=lmax, tol=tol,
             nsteps=nsteps, ncorr=ncorr, uhist=uhist.reshape(nsteps, neq + 1),
-            iters=iters.reshape(nsteps, ncorr))
-        print(f"{name}: neq={neq} nel={mesh.nel} dt={dt:.4g} iters={list(iters)}")
+            iters=iters.reshape(nsteps, ncorr),
+            csr_IA=IA, csr_JA=JA[:nnz], csr_sbe=sbe.reshape(mesh.nel, 144), csr_AA=AA[: nnz + 1], csr_R=Rc,
+            csr_Rp=Rp, csr_p=pz, csr_z=zc, csr_uhist=uhc.reshape(nsteps, neq + 1),
+            csr_iters=itc.reshape(nsteps, ncorr))
+        print(f"{name}: neq={neq} nel={mesh.nel} dt={dt:.4g} iters={list(iters)} nnz={nnz} csr iters={list(itc)}")
 
 
 # Navier-Stokes (CAVITY) cases: name -> (n, perturb, seed, Re, Newton iterations, forcing case)
@@ -425,7 +453,10 @@ def main_amg():
 
 def main(only=()):
     """Every fixture, or (names given on the command line) only those
-    steady-transport cases."""
+    steady-transport cases ("euler": only the Euler cases)."""
+    if only == ("euler",):
+        main_euler()
+        return
     if not only:
         main_amg()
         main_ns()

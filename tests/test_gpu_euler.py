@@ -172,3 +172,50 @@ def test_euler_call_order(gpu_lib):
         with pytest.raises(fg.FemGpuError) as ei:
             eu.precond_setup()
         assert ei.value.code == -9
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_euler_csr_build_and_ilu0_setup_bitexact(gpu_lib, name):
+    """CSR storage (the Euler driver's csr_Initialization.c / csr_assembly.c,
+    setMatrixVectorProductType.c:24) with ILU(0) (setPreconditioner.c:
+    118-128): pattern, CSR_by_Element slots, the assembled values and the
+    residual of a Build, and R := M^-1 R of precond_setup, all bit-identical
+    to the reference's."""
+    g = _load(name)
+    with _euler(g, scheme="CSR", precond="ILU0") as eu:
+        R, _ = eu.Build(g["u"], g["du"])
+        IA, JA, sbe, AA = eu.csr()
+        Rp = eu.precond_setup()
+    assert np.array_equal(IA, g["csr_IA"]) and np.array_equal(JA, g["csr_JA"])
+    assert np.array_equal(sbe, g["csr_sbe"])
+    assert np.array_equal(AA, g["csr_AA"])
+    assert np.array_equal(R, g["csr_R"])
+    assert np.array_equal(Rp, g["csr_Rp"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_euler_csr_ilu0_predictor_vs_reference(gpu_lib, name):
+    """Predictor_Old with CSR storage and ILU(0)-GMRES against the
+    reference's run: iterates to 1e-8, GMRES counts within one."""
+    g = _load(name)
+    with _euler(g, scheme="CSR", precond="ILU0") as eu:
+        uh, its = eu.Predictor(g["u0"], int(g["nsteps"]))
+    assert _rel(uh, g["csr_uhist"]) < SOL_RTOL
+    assert np.abs(its.astype(int) - g["csr_iters"].astype(int)).max() <= 1
+
+
+def test_euler_csr_block_ilu0_fgmres_converges(gpu_lib):
+    """Block ILU(0) over 8 row blocks of the 4-dof CSR system with FGMRES
+    (accepted on the true residual): the predictor's states stay within the
+    solver tolerance's reach of the FP64 ILU(0)-GMRES run."""
+    import fem_codes_gb300 as fg
+    m = structured_mesh(64, 16, lx=4.0, ly=1.0)
+    pb = refletido_problem(m)
+    dt = euler_cfl_dt(m, 5.0)
+    kw = dict(dt=dt, kmax=50, lmax=100, tol=1e-10, ncorr=2, scheme="CSR", precond="ILU0")
+    with fg.Euler.from_problem(m, pb, **kw) as eu:
+        ref, _ = eu.Predictor(pb.u0, 3)
+    with fg.Euler.from_problem(m, pb, solver="FGMRES", ilu_blocks=8, **kw) as eu:
+        uh, its = eu.Predictor(pb.u0, 3)
+    assert np.all(its > 0)
+    assert _rel(uh, ref) < 1e-6

@@ -13,8 +13,14 @@ in oracle/), on systems that reach the sweep's less common paths:
   each other's progress flags, the default) and one barrier per level.
 
 Bar: the separately rounded sweeps (pgmres) are bit-identical to the oracle;
-the fused sweeps (FGMRES) are bit-identical across layouts and ring reaches
-and within FMA_TOL of the oracle."""
+the fused row-by-row sweeps are bit-identical across layouts and ring reaches
+and within FMA_TOL of the oracle.
+
+The chain-scan programs (k_sweep_cs, which FGMRES and the FP32 sweeps take
+when the factor has them) solve chained rows with a warp scan, so they are
+checked against the separately rounded sweeps within CHAIN_TOL, on the same
+paths: global and block factors, wide levels, the ring's reach lowered so
+most dependencies come back from global memory, and in FP32."""
 import os
 
 import numpy as np
@@ -26,14 +32,19 @@ from fem_codes_gb300.mesh import skew_problem, structured_mesh
 pytestmark = pytest.mark.gpu
 
 FMA_TOL = 1e-12    # fused multiply-subtract vs separately rounded sweeps (relative max-norm)
+# chain scan (the recurrence along a segment reassociated over log2(32) steps)
+# vs separately rounded sweeps, relative max-norm
+CHAIN_TOL = 1e-11
 
 
-def apply_ilu(m, p, reorder, solver, layout=None, near=None, blocks=0, sync=None):
+def apply_ilu(m, p, reorder, solver, layout=None, near=None, blocks=0, sync=None, chain="0", info=None):
     """Factor and apply the device ILU(0) of the transport system once; the
-    layout, ring reach and level synchronisation (dataflow or one barrier per
-    level) are fixed when the sweep programs are built."""
+    layout, ring reach, level synchronisation (dataflow or one barrier per
+    level) and the chain-scan programs (chain "0": row-by-row only) are fixed
+    when the sweep programs are built."""
     import fem_codes_gb300 as fg
-    env = {"FEMGPU_SWEEP_LAYOUT": layout, "FEMGPU_SWEEP_NEAR": near, "FEMGPU_SWEEP_SYNC": sync}
+    env = {"FEMGPU_SWEEP_LAYOUT": layout, "FEMGPU_SWEEP_NEAR": near, "FEMGPU_SWEEP_SYNC": sync,
+           "FEMGPU_SWEEP_CHAIN": chain}
     saved = {k: os.environ.get(k) for k in env}
     try:
         for k, v in env.items():
@@ -48,6 +59,8 @@ def apply_ilu(m, p, reorder, solver, layout=None, near=None, blocks=0, sync=None
             pat = T.pattern()
             x = np.zeros(T.neq + 1)
             x[:-1] = np.random.default_rng(11).standard_normal(T.neq)
+            if info is not None:
+                info["chain"] = T.ilu_chain()
             return T.precond(x)[:-1], x, pat, A
     finally:
         for k, v in saved.items():
@@ -142,4 +155,65 @@ def test_fp32_sweeps_both_synchronisations(gpu_lib, blocks):
     z32, z64 = got["dataflow"]
     assert np.array_equal(z32, got["barrier"][0])
     assert np.array_equal(z64, got["barrier"][1])
+    assert np.max(np.abs(z32 - z64)) <= FP32_RTOL * np.max(np.abs(z64))
+
+
+def _rel_max(a, b):
+    return np.max(np.abs(a - b)) / np.max(np.abs(b))
+
+
+@pytest.mark.parametrize("reorder,blocks,near", [("SYMRCM", 0, None), ("SYMRCM", 16, None), ("SYMRCM", 4, 8),
+                                                 ("NOT", 0, None), ("NOT", 0, 8)])
+def test_chain_sweeps_match_row_sweeps(gpu_lib, reorder, blocks, near):
+    """Chain-scan FGMRES sweeps against the separately rounded row-by-row
+    sweeps of the same factor (global or block), with the ring's full or
+    lowered reach; the programs are in use (femgpu_transport_info)."""
+    m = structured_mesh(160, 96, perturb=0.2, seed=21)
+    p = skew_problem(m)
+    z, x, pat, A = apply_ilu(m, p, reorder, "GMRES", blocks=blocks)
+    if blocks == 0:
+        assert np.array_equal(z, oracle_apply(pat, A, x))
+    info = {}
+    zc, xc, _, _ = apply_ilu(m, p, reorder, "FGMRES", blocks=blocks, near=near, chain=None, info=info)
+    assert np.array_equal(xc, x)
+    assert info["chain"] == 1
+    assert _rel_max(zc, z) <= CHAIN_TOL, _rel_max(zc, z)
+
+
+def test_chain_sweeps_wide_levels(gpu_lib):
+    """600x600 cells in the natural numbering: segment levels of several
+    32-slot chunks, spanning more than one staged sub-block."""
+    m = structured_mesh(600, 600, perturb=0.2, seed=1234)
+    p = skew_problem(m)
+    z, _, _, _ = apply_ilu(m, p, "NOT", "GMRES")
+    info = {}
+    zc, _, _, _ = apply_ilu(m, p, "NOT", "FGMRES", chain=None, info=info)
+    assert info["chain"] == 1
+    assert _rel_max(zc, z) <= CHAIN_TOL, _rel_max(zc, z)
+
+
+@pytest.mark.parametrize("blocks", [0, 8])
+def test_chain_fp32_sweeps(gpu_lib, blocks):
+    """The FP32 chain-scan programs (the MIXED precision's preconditioner)
+    give the FP64 application to FP32 accuracy."""
+    import ctypes
+    import torch
+    import fem_codes_gb300 as fg
+    m = structured_mesh(96, 64, perturb=0.2, seed=5)
+    p = skew_problem(m)
+    with fg.SSTransport.from_problem(m, p, scheme="CSR", reorder="SYMRCM", precond="ILU0", solver="GMRES",
+                                     ilu_blocks=blocks) as T:
+        T.Build(u=np.zeros(T.neq + 1))
+        T.precond_setup(1)
+        assert T.ilu_chain() == 1
+        xh = np.zeros(T.neq + 1)
+        xh[:-1] = np.random.default_rng(13).standard_normal(T.neq)
+        z64 = T.precond(xh)[:-1]
+        x = torch.from_numpy(xh).cuda()
+        z = torch.zeros(T.neq + 1, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        rc = T._L.femgpu_transport_precond32_dev(T.handle, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(z.data_ptr()))
+        assert rc == 0
+        torch.cuda.synchronize()
+        z32 = z.cpu().numpy()[:-1].astype(np.float64)
     assert np.max(np.abs(z32 - z64)) <= FP32_RTOL * np.max(np.abs(z64))
