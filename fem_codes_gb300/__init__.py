@@ -119,6 +119,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_transport_solve_dev": [_vp, _ip],
         "femgpu_transport_true_residual": [_vp, ctypes.POINTER(ctypes.c_double)],
         "femgpu_transport_last_times": [_vp, _vp],
+        "femgpu_transport_write_vtu": [_vp, ctypes.c_char_p, _vp],
         "femgpu_csrmv_f64": [ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_csrmv_f32": [ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     }.items():
@@ -475,6 +476,12 @@ class SSTransport:
         if rc and (rc != -5 or raise_on_nonconvergence):
             raise FemGpuError(rc, "solve_dev")
         return it.value
+
+    def write_vtu(self, path, u=None):
+        """Paraview_Output: the reference's VTU file of the solution u [neq+1]
+        (None: the last solution) at path."""
+        uu = None if u is None else _f64(u)
+        self._check(self._L.femgpu_transport_write_vtu(self._h, os.fsencode(path), _ptr(uu)), "write_vtu")
 
     def ilu_chain(self):
         """1 when the ILU(0) sweeps of FGMRES and of the FP32 solves run the

@@ -71,7 +71,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 sys.stderr.write(o)
     tmp = LIB + ".tmp"
     _compile([NVCC] + ARCH + ["-shared", "-o", tmp] + objs +
-             ["-L" + os.path.join(CUDA_HOME, "lib64"), "-lcudart"])
+             ["-L" + os.path.join(CUDA_HOME, "lib64"), "-lcudart", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

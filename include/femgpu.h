@@ -201,6 +201,13 @@ int femgpu_transport_solve_bx(femgpu_transport *ctx, const double *B_host, doubl
  * skips). Returns the number of Picard iterations run (> 0) or an error. */
 int femgpu_transport_process(femgpu_transport *ctx, int npicard, double *u_hist, int *iters);
 
+/* Paraview_Output (Paraview_Output.c:5-85): writes the VTU file the
+ * reference writes for a solution -- ASCII UnstructuredGrid with the nodal
+ * solution (prescribed value at prescribed nodes) as point data and as the
+ * third coordinate, byte for byte -- to path.  u_host [neq+1] (NULL: the
+ * context's device u, i.e. the last solution). */
+int femgpu_transport_write_vtu(femgpu_transport *ctx, const char *path, const double *u_host);
+
 /* Device-pointer forms (stream-ordered, no synchronisation). */
 int femgpu_transport_build_dev(femgpu_transport *ctx);
 int femgpu_transport_precond_setup_dev(femgpu_transport *ctx, int tag);

@@ -306,3 +306,30 @@ int ref_transport_run(int nnodes, const double *x, const double *y, const int *n
 	}
 	return it;
 }
+
+/* Paraview_Output.c on a given nodal numbering (node_id, -1 prescribed) and
+ * solution u [neq+1] of a problem's plug-ins: the file goes where the
+ * reference writes it, ../03_output/<names>.vtu relative to the working
+ * directory. */
+int Paraview_Output(ParametersType *, FemStructsType *, FemFunctionsType *);
+int ref_transport_vtu(int nnodes, const double *x, const double *y, const int *node_id, int nel, const int *vert,
+                      int problem, int neq, const double *u)
+{
+	int I, J;
+	ParametersType *P = mycalloc("P", 1, sizeof(ParametersType));
+	FemStructsType *FS = mycalloc("FS", 1, sizeof(FemStructsType));
+	FemFunctionsType *FF = mycalloc("FF", 1, sizeof(FemFunctionsType));
+	NodeType *Node = mycalloc("Node", nnodes, sizeof(NodeType));
+	ElementType *El = mycalloc("El", nel, sizeof(ElementType));
+	strcpy(P->Experiments, "HARNESS"); strcpy(P->ProblemTitle, "VTU"); strcpy(P->StabilizationForm, "SUPG");
+	strcpy(P->ShockCapture, "CAU"); strcpy(P->h_Shock, "2sqrtArea"); strcpy(P->MatrixVectorProductScheme, "CSR");
+	strcpy(P->Preconditioner, "ILU0");
+	P->nnodes = nnodes; P->nel = nel; P->neq = neq;
+	for (I = 0; I < nnodes; I++) { Node[I].x = x[I]; Node[I].y = y[I]; Node[I].id = node_id[I]; }
+	for (I = 0; I < nel; I++) for (J = 0; J < 3; J++) El[I].Vertex[J] = vert[3 * I + J];
+	FS->Node = Node; FS->Element = El;
+	FS->u = mycalloc("u", neq + 1, sizeof(double));
+	memcpy(FS->u, u, sizeof(double) * (neq + 1));
+	set_problem(problem, FF);
+	return Paraview_Output(P, FS, FF);
+}

@@ -451,13 +451,48 @@ def main_amg():
         print(f"{name}: n={n} nnz={nnz} levels={sizes} gmres={it}")
 
 
+def main_vtu():
+    """Paraview_Output.c on the reference's own final Picard iterate of the
+    skew16_csr_ilu0_rcm run: the VTU file's bytes and the inputs."""
+    import tempfile
+    lib = load_ref()
+    lib.ref_transport_vtu.restype = ctypes.c_int
+    lib.ref_transport_vtu.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_int, _dp]
+    nx, ny, pert, rule, kw = CASES["skew16_csr_ilu0_rcm"]
+    mesh = structured_mesh(nx, ny, perturb=pert, seed=1234)
+    out = run_ref(lib, mesh, node_types(mesh, rule), **kw)
+    u = np.ascontiguousarray(out["uhist"][-1])
+    with tempfile.TemporaryDirectory() as d:
+        os.makedirs(os.path.join(d, "run"))
+        os.makedirs(os.path.join(d, "03_output"))
+        cwd = os.getcwd()
+        os.chdir(os.path.join(d, "run"))
+        try:
+            lib.ref_transport_vtu(mesh.nnodes, mesh.x, mesh.y, np.ascontiguousarray(out["node_id"], np.int32),
+                                  mesh.nel, np.ascontiguousarray(mesh.vert.reshape(-1), np.int32),
+                                  PROBLEMS["SKEW"], out["neq"], u)
+        finally:
+            os.chdir(cwd)
+        files = os.listdir(os.path.join(d, "03_output"))
+        assert len(files) == 1
+        data = open(os.path.join(d, "03_output", files[0]), "rb").read()
+    np.savez_compressed(os.path.join(HERE, "vtu_skew16_rcm.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert,
+                        node_type=node_types(mesh, rule), node_id=out["node_id"], neq=out["neq"], u=u,
+                        vtu=np.frombuffer(data, dtype=np.uint8))
+    print(f"vtu_skew16_rcm: {len(data)} bytes")
+
+
 def main(only=()):
     """Every fixture, or (names given on the command line) only those
     steady-transport cases ("euler": only the Euler cases)."""
     if only == ("euler",):
         main_euler()
         return
+    if only == ("vtu",):
+        main_vtu()
+        return
     if not only:
+        main_vtu()
         main_amg()
         main_ns()
         main_euler()
