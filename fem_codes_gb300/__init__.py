@@ -141,6 +141,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_euler_precond_setup_dev": [_vp],
         "femgpu_euler_solve": [_vp, _vp, _vp, _ip],
         "femgpu_euler_csr": [_vp, _vp, _vp, _vp, _vp, _vp],
+        "femgpu_euler_set_amg": [_vp, _vp],
         "femgpu_euler_solve_dev": [_vp, _ip],
         "femgpu_euler_predictor": [_vp, _vp, ctypes.c_int, _vp, _vp],
         "femgpu_euler_predictor_dev": [_vp, ctypes.c_int, _vp],
@@ -164,6 +165,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_ns_precond_setup": [_vp, _vp],
         "femgpu_ns_solve": [_vp, _vp, _vp, _ip],
         "femgpu_ns_set_tol": [_vp, ctypes.c_double],
+        "femgpu_ns_set_amg": [_vp, _vp],
         "femgpu_ns_newton": [_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp],
         "femgpu_ns_csr": [_vp, _vp, _vp, _vp, _vp],
     }.items():
@@ -687,6 +689,12 @@ class Euler:
         self._check(self._L.femgpu_euler_precond_setup(self._h, _ptr(R)), "precond_setup")
         return R
 
+    def set_amg(self, amg):
+        """Use an :class:`AMG` context as the FEMGPU_PREC_AMG preconditioner
+        of a CSR context (hierarchy rebuilt at every precond_setup)."""
+        self._amg = amg
+        self._check(self._L.femgpu_euler_set_amg(self._h, amg.handle), "set_amg")
+
     def csr(self):
         """CSR storage: (IA, JA, CSR_by_Element [nel, 144], AA of the last build)."""
         nn = np.zeros(2, np.int32)
@@ -822,6 +830,12 @@ class NavierStokes:
         self._check(self._L.femgpu_ns_precond_setup(self._h, _ptr(F)), "precond_setup")
         return F
 
+
+    def set_amg(self, amg):
+        """Use an :class:`AMG` context as the FEMGPU_PREC_AMG preconditioner
+        of a CSR context (hierarchy rebuilt at every precond_setup)."""
+        self._amg = amg
+        self._check(self._L.femgpu_ns_set_amg(self._h, amg.handle), "set_amg")
     def solver(self, B=None):
         BB = None if B is None else _f64(B)
         X = np.zeros(self.neq + 1)

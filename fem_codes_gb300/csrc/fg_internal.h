@@ -82,6 +82,7 @@ typedef struct fg_blockcsr {
 	int nnz;
 	struct femgpu_transport *ilu;
 	int have_ilu;
+	struct femgpu_amg *amg;        /* AMG preconditioner (owned by the caller) */
 } fg_blockcsr;
 
 typedef struct fg_ilu {

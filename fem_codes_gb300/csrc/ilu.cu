@@ -1496,8 +1496,10 @@ static int build_prog_chain(const int *IA, const int *JA, int n, const ChainLeve
 	for (int l = 0; l < nlev; l++) lmax = std::max(lmax, H.lstart[l + 1] - H.lstart[l]);
 	int skew = std::min(sweep_skew(), 4);
 	while (skew > 1 && SW_RING - skew * lmax < 2 * lmax) skew--;
-	int near_lim = std::min(sweep_near_limit(), SW_RING - skew * lmax);
-	if (near_lim < 2 * lmax) return FEMGPU_E_MESH;
+	if (SW_RING - skew * lmax < 2 * lmax) return FEMGPU_E_MESH;
+	// a dependency read back from global memory must be two levels back: a
+	// lowered reach (FEMGPU_SWEEP_NEAR) stops at two of the widest levels
+	const int near_lim = std::max(std::min(sweep_near_limit(), SW_RING - skew * lmax), 2 * lmax);
 	struct Sub { int l, j0, c; };
 	std::vector<Sub> subs;
 	for (int l = 0; l < nlev; l++) {

@@ -15,6 +15,7 @@
 #include "femgpu_host.h"
 #include "../csrc/fg_internal.h"
 #include "../csrc/fg_ebe.h"
+#include "../csrc/fg_amg.h"
 
 #define DM(ptr, bytes) do { int r_ = fgh_dmalloc((void **)&(ptr), (bytes)); if (r_) return r_; } while (0)
 
@@ -95,4 +96,24 @@ int fgh_blockcsr_factor(fg_blockcsr *b, cudaStream_t s)
 void fgh_blockcsr_set_stream(fg_blockcsr *b, cudaStream_t s)
 {
 	if (b->ilu) b->ilu->stream = s;
+	if (b->amg) femgpu_amg_set_stream(b->amg, s);
+}
+
+int fgh_blockcsr_amg_setup(fg_blockcsr *b, int neq, cudaStream_t s)
+{
+	int *IA, *JA, rc;
+	double *AA;
+	if (!b->amg) { fgh_set_error("AMG preconditioner not set"); return FEMGPU_E_NOT_BUILT; }
+	IA = malloc(sizeof(int) * ((size_t)neq + 1));
+	JA = malloc(sizeof(int) * (size_t)(b->nnz ? b->nnz : 1));
+	AA = malloc(sizeof(double) * (size_t)(b->nnz ? b->nnz : 1));
+	rc = (IA && JA && AA) ? 0 : FEMGPU_E_NOMEM;
+	if (!rc && (cudaMemcpyAsync(IA, b->IA, sizeof(int) * ((size_t)neq + 1), cudaMemcpyDeviceToHost, s) ||
+	            cudaMemcpyAsync(JA, b->JA, sizeof(int) * (size_t)b->nnz, cudaMemcpyDeviceToHost, s) ||
+	            cudaMemcpyAsync(AA, b->AA, sizeof(double) * (size_t)b->nnz, cudaMemcpyDeviceToHost, s) ||
+	            cudaStreamSynchronize(s)))
+		rc = FEMGPU_E_CUDA;
+	if (!rc) rc = femgpu_amg_setup(b->amg, neq, IA, JA, AA);
+	free(IA); free(JA); free(AA);
+	return rc;
 }

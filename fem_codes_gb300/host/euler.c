@@ -16,6 +16,7 @@
 #include "femgpu.h"
 #include "femgpu_host.h"
 #include "../csrc/fg_euler.h"
+#include "../csrc/fg_amg.h"
 
 #define DM(ptr, bytes) do { int r_ = fgh_dmalloc((void **)&(ptr), (bytes)); if (r_) return r_; } while (0)
 
@@ -77,13 +78,19 @@ static int op_precond_ilu(void *ctx, const double *p, double *z, const int *acti
 	return fg_ilu0_apply64(((femgpu_euler *)ctx)->csr.ilu, p, z, active);
 }
 
+static int op_precond_amg(void *ctx, const double *p, double *z, const int *active)
+{
+	return fg_amg_vcycle(((femgpu_euler *)ctx)->csr.amg, p, z, active);
+}
+
 static void linop(femgpu_euler *c, fg_linop *op)
 {
 	memset(op, 0, sizeof *op);
 	op->ctx = c;
 	if (c->o.scheme == FEMGPU_CSR) {
 		op->matvec = op_matvec_csr;
-		op->precond = c->o.precond == FEMGPU_PREC_ILU0 ? op_precond_ilu : NULL;
+		op->precond = c->o.precond == FEMGPU_PREC_ILU0 ? op_precond_ilu
+		            : c->o.precond == FEMGPU_PREC_AMG ? op_precond_amg : NULL;
 		return;
 	}
 	op->matvec = op_matvec;
@@ -150,7 +157,8 @@ int femgpu_euler_create(femgpu_euler **out, const femgpu_euler_opts *opts, int n
 	    o.kmax < 1 || o.lmax < 1 || o.ncorr < 1 || !(o.dt > 0.0) || !(o.tol > 0.0) ||
 	    (o.scheme != FEMGPU_EBE && o.scheme != FEMGPU_CSR) || o.ilu_blocks < 0 ||
 	    (o.scheme == FEMGPU_EBE && o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_BLOCKDIAG) ||
-	    (o.scheme == FEMGPU_CSR && o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_ILU0) ||
+	    (o.scheme == FEMGPU_CSR && o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_ILU0 &&
+	     o.precond != FEMGPU_PREC_AMG) ||
 	    (o.scheme == FEMGPU_CSR && o.precision != FEMGPU_FP64) ||
 	    (o.solver != FEMGPU_PGMRES && o.solver != FEMGPU_FGMRES) ||
 	    (o.precision != FEMGPU_FP64 && o.precision != FEMGPU_MIXED_IR) ||
@@ -191,6 +199,15 @@ int femgpu_euler_set_stream(femgpu_euler *c, void *stream)
 	c->kry.stream = c->stream;
 	KR(femgpu_ebe_set_stream(c->ebe, c->stream));
 	fgh_blockcsr_set_stream(&c->csr, c->stream);
+	return 0;
+}
+
+int femgpu_euler_set_amg(femgpu_euler *c, femgpu_amg *g)
+{
+	if (!c || !g || c->o.precond != FEMGPU_PREC_AMG) return FEMGPU_E_ARG;
+	KR(femgpu_amg_set_stream(g, c->stream));
+	c->csr.amg = g;
+	c->have_bd = 0;
 	return 0;
 }
 
@@ -256,6 +273,13 @@ int femgpu_euler_precond_setup_dev(femgpu_euler *c)
 		KR(fgh_blockcsr_factor(&c->csr, c->stream));
 		c->have_bd = 1;
 		if (c->o.solver == FEMGPU_PGMRES) KR(fg_ilu0_apply64(c->csr.ilu, c->R, c->R, NULL));
+		return 0;
+	}
+	if (c->o.precond == FEMGPU_PREC_AMG) {
+		/* AMG_precond_setup (amg_precond.c:26-100) on the CSR matrix, R := M^-1 R */
+		KR(fgh_blockcsr_amg_setup(&c->csr, c->neq, c->stream));
+		c->have_bd = 1;
+		if (c->o.solver == FEMGPU_PGMRES) KR(fg_amg_vcycle(c->csr.amg, c->R, c->R, NULL));
 		return 0;
 	}
 	if (c->o.precond != FEMGPU_PREC_BLOCKDIAG) return 0;     /* NO_precond_setup */

@@ -67,6 +67,9 @@ int fgh_blockcsr_assemble(struct fg_blockcsr *b, int M, const struct femgpu_ebe 
  * the current values; FEMGPU_E_ZERO_PIVOT on a zero pivot. */
 int fgh_blockcsr_factor(struct fg_blockcsr *b, cudaStream_t s);
 void fgh_blockcsr_set_stream(struct fg_blockcsr *b, cudaStream_t s);
+/* AMG_precond_setup (amg_precond.c:26-100) on the current values: the
+ * hierarchy of the attached AMG context, set up on the host. */
+int fgh_blockcsr_amg_setup(struct fg_blockcsr *b, int neq, cudaStream_t s);
 
 #ifdef __cplusplus
 }

@@ -16,6 +16,7 @@
 #include "femgpu.h"
 #include "femgpu_host.h"
 #include "../csrc/fg_ns.h"
+#include "../csrc/fg_amg.h"
 
 #define DM(ptr, bytes) do { int r_ = fgh_dmalloc((void **)&(ptr), (bytes)); if (r_) return r_; } while (0)
 
@@ -55,6 +56,12 @@ static int op_matvec_csr(void *ctx, const double *p, double *q, const int *activ
 static int op_precond_ilu(void *ctx, const double *p, double *z, const int *active)
 {
 	return fg_ilu0_apply64(((femgpu_ns *)ctx)->csr.ilu, p, z, active);
+}
+
+/* CSR storage: AMG_precond, one V-cycle */
+static int op_precond_amg(void *ctx, const double *p, double *z, const int *active)
+{
+	return fg_amg_vcycle(((femgpu_ns *)ctx)->csr.amg, p, z, active);
 }
 
 static int up(double **dst, const double *src, size_t n)
@@ -107,7 +114,9 @@ int femgpu_ns_create(femgpu_ns **out, const femgpu_ns_opts *opts, int nnodes, co
 	if (nnodes <= 0 || nel <= 0 || neq <= 0 || !x || !y || !vert || !node_id || !upresc || !(o.re > 0.0) ||
 	    o.kmax < 1 || o.lmax < 1 || o.eta_case < 0 || o.eta_case > 4 || !(o.eta0 > 0.0) ||
 	    (o.scheme != FEMGPU_EBE && o.scheme != FEMGPU_CSR) || o.ilu_blocks < 0 ||
-	    (o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_BLOCKDIAG && o.precond != FEMGPU_PREC_ILU0) ||
+	    (o.precond != FEMGPU_PREC_NOT && o.precond != FEMGPU_PREC_BLOCKDIAG && o.precond != FEMGPU_PREC_ILU0 &&
+	     o.precond != FEMGPU_PREC_AMG) ||
+	    (o.precond == FEMGPU_PREC_AMG && o.scheme != FEMGPU_CSR) ||
 	    (o.precond == FEMGPU_PREC_BLOCKDIAG && o.scheme != FEMGPU_EBE) ||     /* setPreconditioner.c:54-73 */
 	    (o.precond == FEMGPU_PREC_ILU0 && o.scheme != FEMGPU_CSR) ||
 	    (o.solver != FEMGPU_PGMRES && o.solver != FEMGPU_FGMRES)) {
@@ -213,6 +222,14 @@ static int setup_dev(femgpu_ns *c)
 		if (c->o.solver == FEMGPU_PGMRES) KR(fg_ilu0_apply64(c->csr.ilu, c->F, c->F, NULL));
 		return 0;
 	}
+	if (c->o.precond == FEMGPU_PREC_AMG) {
+		/* AMG_precond_setup (amg_precond.c:26-100): the hierarchy of the
+		 * current CSR matrix on the host, then F := M^-1 F */
+		KR(fgh_blockcsr_amg_setup(&c->csr, c->neq, c->stream));
+		c->have_bd = 1;
+		if (c->o.solver == FEMGPU_PGMRES) KR(fg_amg_vcycle(c->csr.amg, c->F, c->F, NULL));
+		return 0;
+	}
 	if (c->o.precond != FEMGPU_PREC_BLOCKDIAG) return 0;
 	KR(fg_ebe_blockdiag_setup(c->ebe));
 	c->ebe->have_bd = 1;
@@ -249,11 +266,21 @@ static int solve(femgpu_ns *c, const double *B, double *X, int *iters)
 	op.ctx = c;
 	op.matvec = c->o.scheme == FEMGPU_CSR ? op_matvec_csr : op_matvec;
 	op.precond = c->o.precond == FEMGPU_PREC_BLOCKDIAG ? op_precond
-	           : c->o.precond == FEMGPU_PREC_ILU0 ? op_precond_ilu : NULL;
+	           : c->o.precond == FEMGPU_PREC_ILU0 ? op_precond_ilu
+	           : c->o.precond == FEMGPU_PREC_AMG ? op_precond_amg : NULL;
 	rc = fgh_kry_cycles(&c->kry, &op, B, X, c->o.solver == FEMGPU_PGMRES ? -1 : 0, c->tol * sqrt(nb2), c->o.lmax,
 	                    &it);
 	*iters = it;
 	return rc;
+}
+
+int femgpu_ns_set_amg(femgpu_ns *c, femgpu_amg *g)
+{
+	if (!c || !g || c->o.precond != FEMGPU_PREC_AMG) return FEMGPU_E_ARG;
+	KR(femgpu_amg_set_stream(g, c->stream));
+	c->csr.amg = g;
+	c->have_bd = 0;
+	return 0;
 }
 
 int femgpu_ns_set_tol(femgpu_ns *c, double tol)

@@ -3,7 +3,7 @@
  * (03_Euler_Equations/2D) through the reference's own function pointers
  * (FemFunctionsType / FemOtherFunctionsType, EulerEquations.h:136-170), for
  * EBE storage with the nodal block-diagonal preconditioner or CSR storage
- * (reordering NOT) with ILU(0), and the predictor-multicorrector
+ * (reordering NOT) with ILU(0) or the DPA AMG, and the predictor-multicorrector
  * (Predictor_Old.c) that calls Build, precond_setup and the 6-argument
  * solver once per corrector.
  *
@@ -39,6 +39,19 @@
 #include <strings.h>
 
 static femgpu_euler *g_eu;
+static femgpu_amg *g_amg;
+
+/* The deck's "AMG 2 NCL beta omega nr" (amg_precond.c:26-40): the DPA form
+ * only; 0 on success. */
+static int amg_of(const char *spec)
+{
+	int type = 0, ncl = 0, nr = 0;
+	double beta = 0.0, omega = 0.0;
+	if (g_amg) return 0;
+	if (sscanf(spec, "AMG %d %d %lf %lf %d", &type, &ncl, &beta, &omega, &nr) != 5 || type != 2)
+		return FEMGPU_E_ARG;
+	return femgpu_amg_create(&g_amg, ncl, beta, omega, nr);
+}
 static int g_abort = 1, g_err, g_copy_matrix, g_fgmres;
 
 /* A solve that reached its iteration limit is not a failure: the reference's
@@ -82,6 +95,10 @@ static int eu_of(ParametersType *P, FemStructsType *FS, FemFunctionsType *FF)
 	else if (!strcasecmp(P->Preconditioner, "BlockDiag") && o.scheme == FEMGPU_EBE) o.precond = FEMGPU_PREC_BLOCKDIAG;
 	else if (!strncmp(P->Preconditioner, "ILU", 3) && (!P->Preconditioner[3] || atoi(P->Preconditioner + 3) == 0) &&
 	         o.scheme == FEMGPU_CSR) o.precond = FEMGPU_PREC_ILU0;
+	else if (!strncmp(P->Preconditioner, "AMG", 3) && o.scheme == FEMGPU_CSR) {
+		if ((rc = amg_of(P->Preconditioner))) return rc;
+		o.precond = FEMGPU_PREC_AMG;
+	}
 	else return FEMGPU_E_ARG;
 	o.gamma = FF->gamma(FS->Node[0].x, FS->Node[0].y);
 	o.mach = P->Mach;
@@ -113,6 +130,7 @@ static int eu_of(ParametersType *P, FemStructsType *FS, FemFunctionsType *FF)
 	for (E = 0; E < ne; E++)
 		for (k = 0; k < 3; k++) vert[3 * E + k] = FS->Element[E].Vertex[k];
 	rc = femgpu_euler_create(&g_eu, &o, nn, x, y, ne, vert, nid, P->neq, up);
+	if (!rc && o.precond == FEMGPU_PREC_AMG) rc = femgpu_euler_set_amg(g_eu, g_amg);
 out:
 	free(x); free(y); free(up); free(nid); free(vert);
 	return rc;
@@ -194,5 +212,7 @@ void femgpu_shim_euler_install(FemFunctionsType *FF, FemOtherFunctionsType *FOF)
 void femgpu_shim_euler_release(void)
 {
 	if (g_eu) femgpu_euler_destroy(g_eu);
+	if (g_amg) femgpu_amg_destroy(g_amg);
 	g_eu = NULL;
+	g_amg = NULL;
 }

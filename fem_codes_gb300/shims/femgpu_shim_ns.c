@@ -5,7 +5,7 @@
  * SSNavierStokesEquations.h:130-156): the VMS build (Build_K_F_MS), its
  * precond_setup and the 6-argument solver that the damped-Newton Process
  * (Process.c:62-194) calls, with EBE storage and BlockDiag (3x3 nodal
- * blocks) or CSR storage and ILU(0).
+ * blocks) or CSR storage and ILU(0) or the DPA AMG ("AMG 2 NCL beta omega nr").
  *
  * Build, inside the driver's 01_CommonFiles (its own header):
  *     gcc -DSSNavierStokesEquations2D -I. -I<repo>/include -c femgpu_shim_ns.c
@@ -39,6 +39,19 @@
 #include <strings.h>
 
 static femgpu_ns *g_ns;
+static femgpu_amg *g_amg;
+
+/* The deck's "AMG 2 NCL beta omega nr" (amg_precond.c:26-40): the DPA form
+ * only; 0 on success. */
+static int amg_of(const char *spec)
+{
+	int type = 0, ncl = 0, nr = 0;
+	double beta = 0.0, omega = 0.0;
+	if (g_amg) return 0;
+	if (sscanf(spec, "AMG %d %d %lf %lf %d", &type, &ncl, &beta, &omega, &nr) != 5 || type != 2)
+		return FEMGPU_E_ARG;
+	return femgpu_amg_create(&g_amg, ncl, beta, omega, nr);
+}
 static int g_abort = 1, g_err, g_copy_matrix, g_fgmres;
 
 /* A solve that reached its iteration limit is not a failure: the reference's
@@ -77,6 +90,10 @@ static int ns_of(ParametersType *P, FemStructsType *FS, FemFunctionsType *FF)
 	else if (!strcasecmp(P->Preconditioner, "BlockDiag")) o.precond = FEMGPU_PREC_BLOCKDIAG;
 	else if (!strcasecmp(P->Preconditioner, "ILU0") || !strcasecmp(P->Preconditioner, "ILU"))
 		o.precond = FEMGPU_PREC_ILU0;
+	else if (!strncmp(P->Preconditioner, "AMG", 3)) {
+		if ((rc = amg_of(P->Preconditioner))) return rc;
+		o.precond = FEMGPU_PREC_AMG;
+	}
 	else return FEMGPU_E_ARG;
 	if (strcasecmp(P->StabilizationForm, "MS") != 0) return FEMGPU_E_ARG;
 	o.re = P->ReynoldsNumber;
@@ -108,6 +125,7 @@ static int ns_of(ParametersType *P, FemStructsType *FS, FemFunctionsType *FF)
 	for (E = 0; E < ne; E++)
 		for (k = 0; k < 3; k++) vert[3 * E + k] = FS->Element[E].Vertex[k];
 	rc = femgpu_ns_create(&g_ns, &o, nn, x, y, ne, vert, nid, P->neq, up, f);
+	if (!rc && o.precond == FEMGPU_PREC_AMG) rc = femgpu_ns_set_amg(g_ns, g_amg);
 out:
 	free(x); free(y); free(up); free(f); free(nid); free(vert);
 	return rc;
@@ -160,5 +178,7 @@ void femgpu_shim_ns_install(FemFunctionsType *FF, FemOtherFunctionsType *FOF)
 void femgpu_shim_ns_release(void)
 {
 	if (g_ns) femgpu_ns_destroy(g_ns);
+	if (g_amg) femgpu_amg_destroy(g_amg);
 	g_ns = NULL;
+	g_amg = NULL;
 }

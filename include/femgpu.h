@@ -279,7 +279,8 @@ typedef struct femgpu_euler_opts {
 	double alpha;        /* Alpha of the predictor                           */
 	double dt;           /* DeltaT                                           */
 	double stab_tol;     /* StabilizationTolerance (CAU switch, Delta_CAU.c:71) */
-	int precond;         /* FEMGPU_PREC_NOT or FEMGPU_PREC_BLOCKDIAG         */
+	int precond;         /* FEMGPU_PREC_NOT, FEMGPU_PREC_BLOCKDIAG (EBE),     */
+	                     /* FEMGPU_PREC_ILU0 or FEMGPU_PREC_AMG (CSR)        */
 	int solver;          /* femgpu_solver: PGMRES (reference) or FGMRES      */
 	int kmax, lmax;      /* KrylovBasisVectorsQuantity, SolverMaxIter        */
 	double tol;          /* SolverTolerance                                  */
@@ -292,7 +293,7 @@ typedef struct femgpu_euler_opts {
 	int scheme;          /* MatrixVectorProductScheme: FEMGPU_EBE (12x12     */
 	                     /* element blocks, NOT / BLOCKDIAG) or FEMGPU_CSR   */
 	                     /* (csr_Initialization.c / csr_assembly.c of the    */
-	                     /* Euler driver, reordering NOT; NOT / ILU0)        */
+	                     /* Euler driver, reordering NOT; NOT / ILU0 / AMG)  */
 	int ilu_blocks;      /* CSR + ILU0: 0 the whole matrix (the reference's), */
 	                     /* P > 1 block ILU(0) over P row blocks (as         */
 	                     /* femgpu_transport_opts.ilu_blocks)                */
@@ -358,8 +359,8 @@ int femgpu_euler_last_times(const femgpu_euler *ctx, double *t);
 typedef struct femgpu_ns_opts {
 	double re;           /* ReynoldsNumber                                   */
 	double velmax;       /* VelMax (reference velocity of the local Re)      */
-	int precond;         /* FEMGPU_PREC_NOT, FEMGPU_PREC_BLOCKDIAG (EBE) or  */
-	                     /* FEMGPU_PREC_ILU0 (CSR)                           */
+	int precond;         /* FEMGPU_PREC_NOT, FEMGPU_PREC_BLOCKDIAG (EBE),     */
+	                     /* FEMGPU_PREC_ILU0 or FEMGPU_PREC_AMG (CSR)        */
 	int solver;          /* femgpu_solver: PGMRES (reference) or FGMRES      */
 	int kmax, lmax;      /* KrylovBasisVectorsQuantity, LinearMaxIter        */
 	double eta0;         /* SolverTolerance: initial / maximal forcing term  */
@@ -498,6 +499,13 @@ int femgpu_amg_apply_dev(femgpu_amg *ctx, const double *q, double *z);
  * (precond_setup rebuilds the hierarchy from the current matrix), or as the
  * fallback of a FEMGPU_PREC_LEARNED context (built when a solve stalls). */
 int femgpu_transport_set_amg(femgpu_transport *t, femgpu_amg *ctx);
+/* The same for the Navier-Stokes and Euler contexts with CSR storage and
+ * precond FEMGPU_PREC_AMG (setPreconditioner.c:63-73 of the Navier-Stokes
+ * driver, :130-140 of the Euler driver): precond_setup builds the hierarchy
+ * of the current CSR matrix and (left-preconditioned GMRES) applies one
+ * V-cycle to the right-hand side; the solves apply one V-cycle per step. */
+int femgpu_ns_set_amg(femgpu_ns *ns, femgpu_amg *ctx);
+int femgpu_euler_set_amg(femgpu_euler *eu, femgpu_amg *ctx);
 
 /* ---- stateless device kernels (device pointers, stream as void*) -------- */
 /* csrmv.c:3-24 in FP64 / FP32 values. */

@@ -270,8 +270,10 @@ def main_euler():
         itc = np.zeros(nsteps * ncorr, np.int32)
         lib.ref_euler_predictor_csr(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol,
                                     kmax, lmax, tol, nsteps, ncorr, upc, uhc, itc)
+        amg_Fp = amg_fprec(IA, JA[:nnz], AA[:nnz], Rc[:neq], AMG_SYS_SPEC)
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id,
+            amg_spec=np.array(AMG_SYS_SPEC), amg_Fp=amg_Fp,
             neq=neq, upresc=pb.upresc, u0=pb.u0, gamma=pb.gamma, alpha=alpha, dt=dt, stab_tol=stol,
             u=u, du=du, Ae=Ae.reshape(mesh.nel, 144), R=R, kmax=kmax, lmax=lmax, tol=tol,
             nsteps=nsteps, ncorr=ncorr, uhist=uhist.reshape(nsteps, neq + 1),
@@ -363,8 +365,11 @@ def main_ns():
         cnF, cw, cg = np.zeros(maxit), np.zeros(maxit), np.zeros(maxit, np.int32)
         cnit = ns_lib().ref_ns_newton_csr(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, re, 1.0, kmax,
                                           lmax, eta0, ecase, tolnl, maxit, cuh, cnF, cw, cg)
+        # AMG_precond_setup (DPA) on the last build's CSR system: F := M^-1 F
+        amg_Fp = amg_fprec(cIA, cJA[:nnz], cAA[2][:nnz], cF.reshape(3, neq + 1)[2][:neq], AMG_SYS_SPEC)
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id, neq=neq,
+            amg_spec=np.array(AMG_SYS_SPEC), amg_Fp=amg_Fp,
             upresc=up, f=pb.f, re=re, velmax=1.0, us=us, Ae=Ae.reshape(3, mesh.nel, 81), F=F.reshape(3, neq + 1),
             delta_old=dold, normres_old=nold, kmax=kmax, lmax=lmax, eta0=eta0, ecase=ecase, tolnl=tolnl,
             maxit=maxit, uhist=uh.reshape(maxit, neq + 1)[:nit], normF=nF[:nit], w=w[:nit], gmres=g[:nit],
@@ -400,6 +405,22 @@ def amg_lib():
     L.ref_amg_gmres.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, _dp, _dp]
     L.ref_amg_gmres.restype = ctypes.c_int
     return L
+
+
+# the AMG deck string of the Navier-Stokes and Euler CSR cases (DPA, 2
+# coarsening sweeps per level, beta -1: the half-approximate matching)
+AMG_SYS_SPEC = "AMG 2 2 -1 1.0 2"
+
+
+def amg_fprec(IA, JA, AA, F, spec):
+    """AMG_precond_setup's F := M^-1 F on an assembled CSR system (n rows)."""
+    n = IA.size - 1
+    L = amg_lib()
+    Fp = np.concatenate([np.ascontiguousarray(F, np.float64), [0.0]])
+    info = np.zeros(4, np.int32)
+    L.ref_amg_setup(n, np.ascontiguousarray(IA, np.int32), np.ascontiguousarray(JA, np.int32),
+                    np.ascontiguousarray(AA, np.float64), spec.encode(), Fp, info)
+    return Fp[:n].copy()
 
 
 def main_amg():
@@ -487,6 +508,9 @@ def main(only=()):
     steady-transport cases ("euler": only the Euler cases)."""
     if only == ("euler",):
         main_euler()
+        return
+    if only == ("ns",):
+        main_ns()
         return
     if only == ("vtu",):
         main_vtu()

@@ -219,3 +219,23 @@ def test_euler_csr_block_ilu0_fgmres_converges(gpu_lib):
         uh, its = eu.Predictor(pb.u0, 3)
     assert np.all(its > 0)
     assert _rel(uh, ref) < 1e-6
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_euler_csr_amg_setup_bitexact(gpu_lib, name):
+    """CSR storage with the AMG preconditioner (setPreconditioner.c:130-140 of
+    the Euler driver): R := M^-1 R of precond_setup equals the reference's
+    AMG_precond_setup on the same CSR system bit for bit."""
+    import fem_codes_gb300 as fg
+    g = _load(name)
+    _, _, ncl, beta, omega, nr = str(g["amg_spec"]).split()
+    amg = fg.AMG(ncl=int(ncl), beta=float(beta), omega=float(omega), nr=int(nr))
+    neq = int(g["neq"])
+    try:
+        with _euler(g, scheme="CSR", precond="AMG") as eu:
+            eu.set_amg(amg)
+            eu.Build(g["u"], g["du"])
+            Rp = eu.precond_setup()
+    finally:
+        amg.close()
+    assert np.array_equal(Rp[:neq], g["amg_Fp"])

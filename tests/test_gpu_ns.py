@@ -160,3 +160,25 @@ def test_ns_cavity_newton_converges(gpu_lib):
     ux[free] = u[pb.node_id[free, 0]]
     mid = (np.abs(m.x - 0.5) < 1e-12) & (m.y > 0.1) & (m.y < 0.4)
     assert (ux[mid] < 0).all()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_ns_csr_amg_setup_bitexact(gpu_lib, name):
+    """CSR storage with the AMG preconditioner (the driver's "AMG 2 ..."
+    choice, setPreconditioner.c:63-73): after three consecutive builds,
+    precond_setup's F := M^-1 F equals the reference's AMG_precond_setup on
+    the same CSR system bit for bit."""
+    import fem_codes_gb300 as fg
+    g = _load(name)
+    _, _, ncl, beta, omega, nr = str(g["amg_spec"]).split()
+    amg = fg.AMG(ncl=int(ncl), beta=float(beta), omega=float(omega), nr=int(nr))
+    neq = int(g["neq"])
+    try:
+        with _ns(g, scheme="CSR", precond="AMG") as ns:
+            ns.set_amg(amg)
+            for b in range(len(g["us"])):
+                ns.Build(g["us"][b])
+            Fp = ns.precond_setup()
+    finally:
+        amg.close()
+    assert np.array_equal(Fp[:neq], g["amg_Fp"])
