@@ -41,6 +41,15 @@ OPTS = {
 }
 
 
+def _precond_code(precond):
+    """femgpu_precond of a deck-style preconditioner name and its level of
+    fill: "ILU<p>" (ILUp_precond_setup.c:15) -> (FEMGPU_PREC_ILU0, p)."""
+    name = precond.upper()
+    if name.startswith("ILU") and name[3:].isdigit():
+        return OPTS["precond"]["ILU0"], int(name[3:])
+    return OPTS["precond"][name], 0
+
+
 class FemGpuError(RuntimeError):
     def __init__(self, code, where=""):
         msg = ERRORS.get(code, f"error {code}")
@@ -55,7 +64,7 @@ class Opts(ctypes.Structure):
                 ("kmax", ctypes.c_int), ("lmax", ctypes.c_int), ("tol", ctypes.c_double),
                 ("nonlin_tol", ctypes.c_double), ("precision", ctypes.c_int), ("ir_max", ctypes.c_int),
                 ("solver", ctypes.c_int), ("inner_tol", ctypes.c_double), ("stall_ratio", ctypes.c_double),
-                ("ilu_blocks", ctypes.c_int)]
+                ("ilu_blocks", ctypes.c_int), ("ilu_level", ctypes.c_int)]
 
 
 class EulerOpts(ctypes.Structure):
@@ -102,6 +111,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_transport_ilu_blocks": [_vp, _vp, ctypes.c_int],
         "femgpu_transport_ilu_chain": [_vp, _vp],
         "femgpu_ilu_block_cut": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, ctypes.c_int],
+        "femgpu_iluk_pattern": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp, ctypes.c_int],
         "femgpu_ilu_chain_segments": [ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
                                       ctypes.c_int, ctypes.c_int],
         "femgpu_transport_get_pattern": [_vp, _vp, _vp, _vp, _vp, _vp],
@@ -249,6 +259,24 @@ def ilu_block_cut(IA, JA, P):
     return first[: rc + 1]
 
 
+def iluk_pattern(IA, JA, p):
+    """The ILU(p) pattern of a CSR pattern (LEVEL_OF_FILL_lu): (fIA, fJA),
+    rows stored lower ascending, diagonal, upper in elimination order."""
+    L = load()
+    IA = np.ascontiguousarray(IA, dtype=np.int32)
+    JA = np.ascontiguousarray(JA, dtype=np.int32)
+    n = IA.size - 1
+    nnz = L.femgpu_iluk_pattern(n, _ptr(IA), _ptr(JA), int(p), None, None, 0)
+    if nnz < 0:
+        raise FemGpuError(nnz, "iluk_pattern")
+    fIA = np.zeros(n + 1, np.int32)
+    fJA = np.zeros(nnz, np.int32)
+    rc = L.femgpu_iluk_pattern(n, _ptr(IA), _ptr(JA), int(p), _ptr(fIA), _ptr(fJA), nnz)
+    if rc < 0:
+        raise FemGpuError(rc, "iluk_pattern")
+    return fIA, fJA
+
+
 def ilu_chain_segments(IA, JA, P, lower=True):
     """The chain-scan segmentation of one ILU(0) sweep of a CSR pattern (the
     programs a transport context with ilu_blocks = P builds for its FGMRES and
@@ -287,7 +315,7 @@ class SSTransport:
         L.femgpu_transport_default_opts(ctypes.byref(o))
         o.scheme = OPTS["scheme"][scheme.upper()]
         o.reorder = OPTS["reorder"][reorder.upper()]
-        o.precond = OPTS["precond"][precond.upper()]
+        o.precond, o.ilu_level = _precond_code(precond)
         o.shock = OPTS["shock"][shock.upper()]
         o.hshock = OPTS["hshock"][hshock.upper()]
         o.outflow = 1 if outflow else 0

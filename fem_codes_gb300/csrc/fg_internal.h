@@ -70,6 +70,12 @@ typedef struct fg_ilu_sweeps {
 	int fac2_ok;
 	int nblocks;               /* matrix blocks (1: global ILU(0))           */
 	int *block_first;          /* host [nblocks+1] first row of each block   */
+	/* ILU(p), p > 0: the filled pattern the factor and sweeps use (rows as
+	 * the reference stores them), each matrix entry's position in it, and
+	 * the matrix values scattered onto it before every factorisation */
+	int fill, fnnz;
+	int *fIA, *fJA, *fmap;
+	double *fA;
 } fg_ilu_sweeps;
 
 /* CSR storage of a multi-dof element system (csr_Initialization.c of the

@@ -2031,11 +2031,25 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 	return sweep_attrs();
 }
 
+// ILU(p): the matrix's values onto the filled pattern (fill entries zero).
+__global__ void k_fill_scatter(const double *__restrict__ A, const int *__restrict__ map, int nnz, double *fA)
+{
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += gridDim.x * blockDim.x) fA[map[k]] = A[k];
+}
+
 extern "C" int fg_ilu0_factor(femgpu_transport *t)
 {
 	cudaStream_t s = t->stream;
 	fg_ilu_sweeps &S = t->sweeps;
 	int P = S.lo64.nchunk, C = S.fac2_ok ? factor_cluster_size(P) : 0;
+	const double *A = t->A;
+	const int *IA = t->IA;
+	if (S.fill) {
+		FG_TRY(cudaMemsetAsync(S.fA, 0, sizeof(double) * ((size_t)S.fnnz + 1), s));
+		k_fill_scatter<<<fg_grid(t->nnz), FG_TPB, 0, s>>>(t->A, S.fmap, t->nnz, S.fA);
+		A = S.fA;
+		IA = S.fIA;
+	}
 	if (C) {
 		cudaLaunchConfig_t cfg = {};
 		cudaLaunchAttribute at[1];
@@ -2043,12 +2057,12 @@ extern "C" int fg_ilu0_factor(femgpu_transport *t)
 		at[0].val.clusterDim.x = (unsigned)C; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;
 		cfg.gridDim = dim3((unsigned)(C * P)); cfg.blockDim = dim3(FAC2_T); cfg.dynamicSmemBytes = FAC2_SMEM;
 		cfg.stream = s; cfg.attrs = at; cfg.numAttrs = 1;
-		FG_TRY(cudaLaunchKernelEx(&cfg, k_ilu0_factor_cluster, (const double *)t->A, (const int *)S.lo64.rows,
+		FG_TRY(cudaLaunchKernelEx(&cfg, k_ilu0_factor_cluster, A, (const int *)S.lo64.rows,
 		                          (const int *)S.lo64.lev_start, S.lo64.nlev, (const int *)S.lo64.chunk_lev,
 		                          (const int4 *)S.fac2_hdr, (const int *)S.fac2, t->ilu.LU, t->ilu.Dinv,
 		                          &t->st->err));
 	} else {
-		k_ilu0_factor_cta<<<S.lo64.nchunk, FAC_THREADS, 0, s>>>(t->IA, t->A, S.lo64.rows, S.lo64.lev_start,
+		k_ilu0_factor_cta<<<S.lo64.nchunk, FAC_THREADS, 0, s>>>(IA, A, S.lo64.rows, S.lo64.lev_start,
 		                                                       S.lo64.nlev, S.lo64.chunk_lev, S.fac_ptr,
 		                                                       S.fac_prog, t->ilu.LU, t->ilu.Dinv, &t->st->err);
 	}
@@ -2135,8 +2149,12 @@ extern "C" void fg_ilu_free(femgpu_transport *t)
 		memset(all[i], 0, sizeof(fg_sweep));
 	}
 	S.chain = 0;
-	void *v[] = { S.bl64, S.y64, S.bl32, S.y32, S.fac_ptr, S.fac_prog, S.fac2_hdr, S.fac2 };
+	void *v[] = { S.bl64, S.y64, S.bl32, S.y32, S.fac_ptr, S.fac_prog, S.fac2_hdr, S.fac2, S.fIA, S.fJA, S.fmap,
+	              S.fA };
 	for (void *q : v) if (q) cudaFree(q);
+	S.fIA = S.fJA = S.fmap = nullptr;
+	S.fA = nullptr;
+	S.fill = 0;
 	free(S.block_first);
 	S.block_first = nullptr;
 	S.nblocks = 0;

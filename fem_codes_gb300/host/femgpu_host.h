@@ -51,6 +51,11 @@ int fgh_kry_cycle(const struct fg_krylov *k, const struct fg_linop *op, const do
 /* ||B||^2 on the device, returned to the host (synchronises the stream). */
 int fgh_kry_dot_host(const struct fg_krylov *k, const double *a, const double *b, int n, double *out);
 
+/* Symbolic ILU(p) (host/iluk.c): the filled pattern in the reference's row
+ * layout (lower ascending, diagonal, upper in elimination order) and the
+ * position of each of the matrix's entries in it (malloc'd arrays). */
+int fgh_iluk_pattern(int n, const int *IA, const int *JA, int p, int **fIA, int **fJA, int **map);
+
 /* Block CSR storage of an EBE element system with M = 3*ndof equations per
  * element (host/blockcsr.c): the pattern built on the device from the EBE
  * context's lm and incidence lists and, when ilu0, the ILU(0) structure of

@@ -135,6 +135,7 @@ int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts 
 	    t->o.precision < 0 || t->o.precision > 2 || t->o.solver < 0 || t->o.solver > 1 ||
 	    (t->o.precision != FEMGPU_FP64 && (t->o.solver != FEMGPU_FGMRES || t->o.scheme != FEMGPU_CSR)) ||
 	    (t->o.precond == FEMGPU_PREC_ILU0 && t->o.scheme != FEMGPU_CSR) ||
+	    t->o.ilu_level < 0 || (t->o.ilu_level > 0 && t->o.precond != FEMGPU_PREC_ILU0) ||
 	    (t->o.reorder == FEMGPU_REORDER_SYMRCM && t->o.scheme != FEMGPU_CSR)) {
 		/* setPreconditioner.c:84-93: ILU is defined for CSR only */
 		fgh_set_error("unsupported option combination");
@@ -228,11 +229,38 @@ int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts 
 	}
 
 	if (t->o.precond == FEMGPU_PREC_ILU0 || t->o.precond == FEMGPU_PREC_LEARNED) {
+		const int *pIA = hIA, *pJA = hJA;
+		int *fIA = NULL, *fJA = NULL, *fmap = NULL;
 		t->ilu.n = neq;
 		t->ilu.nnz = t->nnz;
+		if (t->o.precond == FEMGPU_PREC_ILU0 && t->o.ilu_level > 0) {
+			/* ILU(p): LEVEL_OF_FILL_lu's pattern on the host, the factor and
+			 * sweeps on it (ILUp_precond_setup.c:17-45) */
+			fg_ilu_sweeps *S = &t->sweeps;
+			rc = fgh_iluk_pattern(neq, hIA, hJA, t->o.ilu_level, &fIA, &fJA, &fmap);
+			if (rc) { free(hIA); free(hJA); return rc; }
+			S->fnnz = fIA[neq];
+			rc = fgh_dmalloc((void **)&S->fIA, sizeof(int) * ((size_t)neq + 1));
+			if (!rc) rc = fgh_dmalloc((void **)&S->fJA, sizeof(int) * ((size_t)S->fnnz + 1));
+			if (!rc) rc = fgh_dmalloc((void **)&S->fmap, sizeof(int) * ((size_t)t->nnz + 1));
+			if (!rc) rc = fgh_dmalloc((void **)&S->fA, sizeof(double) * ((size_t)S->fnnz + 1));
+			if (!rc && (cudaMemcpy(S->fIA, fIA, sizeof(int) * ((size_t)neq + 1), cudaMemcpyHostToDevice) ||
+			            cudaMemcpy(S->fJA, fJA, sizeof(int) * (size_t)S->fnnz, cudaMemcpyHostToDevice) ||
+			            cudaMemcpy(S->fmap, fmap, sizeof(int) * (size_t)t->nnz, cudaMemcpyHostToDevice)))
+				rc = FEMGPU_E_CUDA;
+			if (rc) { free(fIA); free(fJA); free(fmap); free(hIA); free(hJA); return rc; }
+			S->fill = 1;
+			t->ilu.nnz = S->fnnz;
+			nA = (size_t)S->fnnz + 1;
+			pIA = fIA;
+			pJA = fJA;
+		}
 		DM(t->ilu.LU, sizeof(double) * nA);
 		DM(t->ilu.Dinv, sizeof(double) * ((size_t)neq + 1));
-		rc = fg_ilu_prepare(t, hIA, hJA);
+		rc = fg_ilu_prepare(t, pIA, pJA);
+		free(fIA);
+		free(fJA);
+		free(fmap);
 		if (rc) {
 			fgh_set_error("ILU(0) sweep programs: %d (%s)", rc, rc > 0 ? cudaGetErrorString((cudaError_t)rc) : "");
 			return rc > 0 ? FEMGPU_E_CUDA : rc;

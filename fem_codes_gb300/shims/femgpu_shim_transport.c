@@ -92,8 +92,11 @@ static int deck_options(const ParametersType *P, femgpu_transport_opts *o)
 	o->reorder = !strcasecmp(P->reordering, "SYMRCM") ? FEMGPU_REORDER_SYMRCM : FEMGPU_REORDER_NOT;
 	if (!strcasecmp(P->Preconditioner, "NOT")) o->precond = FEMGPU_PREC_NOT;
 	else if (!strcasecmp(P->Preconditioner, "Diag")) o->precond = FEMGPU_PREC_DIAG;
-	else if (ilu_level(P->Preconditioner) == 0) o->precond = FEMGPU_PREC_ILU0;
-	else return FEMGPU_E_ARG;                   /* LU, SGS, SOR, ILU(p >= 1): not provided */
+	else if (ilu_level(P->Preconditioner) >= 0) {
+		o->precond = FEMGPU_PREC_ILU0;
+		o->ilu_level = ilu_level(P->Preconditioner);
+	}
+	else return FEMGPU_E_ARG;                   /* LU, SGS, SOR: not provided */
 	if (strcasecmp(P->StabilizationForm, "SUPG") != 0) return FEMGPU_E_ARG;   /* DD: not provided */
 	o->shock = !strcasecmp(P->ShockCapture, "YZBeta") ? FEMGPU_SHOCK_YZBETA : FEMGPU_SHOCK_CAU;
 	if (!strcasecmp(P->h_Shock, "sqrtArea")) o->hshock = FEMGPU_H_SQRTAREA;
@@ -123,7 +126,7 @@ static int ctx_of(ParametersType *P, FemStructsType *FS, FemFunctionsType *FF)
 		o = g_over;
 		o.scheme = deck.scheme; o.reorder = deck.reorder; o.precond = deck.precond; o.shock = deck.shock;
 		o.hshock = deck.hshock; o.outflow = deck.outflow; o.kmax = deck.kmax; o.lmax = deck.lmax;
-		o.tol = deck.tol; o.nonlin_tol = deck.nonlin_tol;
+		o.tol = deck.tol; o.nonlin_tol = deck.nonlin_tol; o.ilu_level = deck.ilu_level;
 	}
 	x = malloc(sizeof(double) * (size_t)nn);
 	y = malloc(sizeof(double) * (size_t)nn);

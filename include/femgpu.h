@@ -83,6 +83,9 @@ typedef struct femgpu_transport_opts {
 	                     /* P > 1: block ILU(0) over P contiguous row blocks */
 	                     /* of the numbering, couplings between blocks       */
 	                     /* dropped, one thread block per matrix block       */
+	int ilu_level;       /* level of fill p of FEMGPU_PREC_ILU0 -- the deck's */
+	                     /* "ILU<p>" (ILUp_precond_setup.c:15): 0 ILU(0),    */
+	                     /* p > 0 ILU(p) on LEVEL_OF_FILL_lu's pattern       */
 } femgpu_transport_opts;
 
 void femgpu_transport_default_opts(femgpu_transport_opts *o);
@@ -535,6 +538,13 @@ int femgpu_csr_resnorm_noalloc(int n, const int *IA, const int *JA, const double
  * Cuthill-McKee permutation perm[new] = old of a structurally symmetric CSR
  * pattern, with the reference's tie-breaking. */
 int femgpu_symrcm(int n, const int *IA, const int *JA, int *perm);
+/* LEVEL_OF_FILL_lu (Solvers_and_Preconditioners/ilup.c:164-302): the ILU(p)
+ * pattern of a CSR pattern (every row with its diagonal) for level of fill p,
+ * each row stored as the reference stores it -- lower part ascending, the
+ * diagonal, the upper part in the order the symbolic elimination found it.
+ * Returns the filled nnz; fIA [n+1] and fJA [cap] receive the pattern when
+ * non-NULL (FEMGPU_E_ARG when cap is too small). */
+int femgpu_iluk_pattern(int n, const int *IA, const int *JA, int p, int *fIA, int *fJA, int cap);
 /* Dependency levels of the ILU(0) forward (lower != 0) or backward sweep:
  * returns the number of levels. */
 int femgpu_ilu_levels(int n, const int *IA, const int *JA, int lower);

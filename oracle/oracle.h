@@ -69,6 +69,9 @@ void orc_edemv(int neq, int nedge, const int *lm2, const double *A, double *P, d
  * with p = 0): LU[nnz] holds L (col < row) and U (col > row); Dinv[n] = 1/pivot.
  * Returns 0, or 1 + row of the first zero pivot. */
 int orc_ilu0_factor(int n, const int *IA, const int *JA, const double *AA, double *LU, double *Dinv);
+int orc_iluk_pattern(int n, const int *IA, const int *JA, int p, int *fIA, int *fJA);
+void orc_iluk_scatter(int n, const int *IA, const int *JA, const double *AA, const int *fIA, const int *fJA,
+                      double *fA);
 /* ILUp_precond.c:26-46: z = (LU)^-1 p; p may alias z. */
 void orc_ilu0_apply(int n, const int *IA, const int *JA, const double *LU, const double *Dinv,
                     const double *p, double *z);

@@ -290,6 +290,35 @@ def ilu0(IA, JA, AA):
     return LU, Dinv
 
 
+def iluk_pattern(IA, JA, p):
+    """LEVEL_OF_FILL_lu: the ILU(p) pattern (fIA, fJA), rows lower ascending,
+    diagonal, upper in elimination order."""
+    L = lib()
+    L.orc_iluk_pattern.restype = ctypes.c_int
+    L.orc_iluk_pattern.argtypes = [ctypes.c_int, _ip, _ip, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    IA, JA = _c(IA, np.int32), _c(JA, np.int32)
+    n = IA.size - 1
+    nnz = L.orc_iluk_pattern(n, IA, JA, int(p), None, None)
+    fIA = np.zeros(n + 1, np.int32)
+    fJA = np.zeros(nnz, np.int32)
+    L.orc_iluk_pattern(n, IA, JA, int(p), fIA.ctypes.data, fJA.ctypes.data)
+    return fIA, fJA
+
+
+def iluk(IA, JA, AA, p):
+    """ILUp (ILUp_precond_setup.c:66-167) with level of fill p: (fIA, fJA, LU,
+    Dinv) on the filled pattern."""
+    fIA, fJA = iluk_pattern(IA, JA, p)
+    L = lib()
+    L.orc_iluk_scatter.restype = None
+    L.orc_iluk_scatter.argtypes = [ctypes.c_int, _ip, _ip, _dp, _ip, _ip, _dp]
+    n = IA.size - 1
+    fA = np.zeros(fJA.size + 1)
+    L.orc_iluk_scatter(n, _c(IA, np.int32), _c(JA, np.int32), _c(AA, np.float64), fIA, fJA, fA)
+    LU, Dinv = ilu0(fIA, fJA, fA)
+    return fIA, fJA, LU, Dinv
+
+
 def ilu0_apply(IA, JA, LU, Dinv, p):
     L = lib()
     n = IA.size - 1

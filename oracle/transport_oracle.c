@@ -689,6 +689,82 @@ int orc_ilu0_factor(int n, const int *IA, const int *JA, const double *AA, doubl
 	return 0;
 }
 
+/* ILU(p) pattern: LEVEL_OF_FILL_lu (ilup.c:164-302).  Row i: the matrix's
+ * entries at level 0, then for each lower entry k taken leftmost first, every
+ * entry c of U(k,:) at level lev(i,k) + lev(k,c) + 1 <= p (new, or lowering
+ * an existing level).  The filled row is emitted as the reference stores it:
+ * lower ascending, the diagonal, upper in discovery order (the backward
+ * sweep's order, ILUp_precond.c:38-46).  With that layout orc_ilu0_factor
+ * and orc_ilu0_apply are the reference's ILUp / ILUp_precond on the filled
+ * pattern.  Returns the filled nnz (fIA/fJA may be NULL to count), or -1. */
+int orc_iluk_pattern(int n, const int *IA, const int *JA, int p, int *fIA, int *fJA)
+{
+	int *lev = malloc((size_t)n * sizeof(int)), *buf = malloc((size_t)n * sizeof(int));
+	int *pos = malloc((size_t)n * sizeof(int)), *ucnt = calloc((size_t)n, sizeof(int));
+	int **ucol = calloc((size_t)n, sizeof(int *)), **ulev = calloc((size_t)n, sizeof(int *));
+	int i, j, nnz = 0;
+	for (j = 0; j < n; j++) pos[j] = -1;
+	if (fIA) fIA[0] = 0;
+	for (i = 0; i < n; i++) {
+		int nl = 0, nu = i, piv;
+		for (j = IA[i]; j < IA[i+1]; j++) {
+			int c = JA[j];
+			if (c < i) { buf[nl] = c; lev[nl] = 0; pos[c] = nl++; }
+			else if (c > i) { buf[nu] = c; lev[nu] = 0; pos[c] = nu++; }
+		}
+		for (piv = 0; piv < nl; piv++) {
+			int best = piv, k, q;
+			for (q = piv + 1; q < nl; q++) if (buf[q] < buf[best]) best = q;
+			if (best != piv) {
+				int tc = buf[piv], tl = lev[piv];
+				buf[piv] = buf[best]; lev[piv] = lev[best];
+				buf[best] = tc; lev[best] = tl;
+				pos[buf[piv]] = piv; pos[buf[best]] = best;
+			}
+			k = buf[piv];
+			for (q = 0; q < ucnt[k]; q++) {
+				int c = ucol[k][q], l = ulev[k][q] + lev[piv] + 1;
+				if (l > p) continue;
+				if (pos[c] == -1) {
+					if (c < i) { buf[nl] = c; lev[nl] = l; pos[c] = nl++; }
+					else if (c > i) { buf[nu] = c; lev[nu] = l; pos[c] = nu++; }
+				} else if (l < lev[pos[c]]) lev[pos[c]] = l;
+			}
+		}
+		for (j = 0; j < nl; j++) pos[buf[j]] = -1;
+		for (j = i; j < nu; j++) pos[buf[j]] = -1;
+		ucnt[i] = nu - i;
+		if (ucnt[i]) {
+			ucol[i] = malloc((size_t)ucnt[i] * sizeof(int));
+			ulev[i] = malloc((size_t)ucnt[i] * sizeof(int));
+			memcpy(ucol[i], buf + i, (size_t)ucnt[i] * sizeof(int));
+			memcpy(ulev[i], lev + i, (size_t)ucnt[i] * sizeof(int));
+		}
+		if (fJA) {
+			memcpy(fJA + nnz, buf, (size_t)nl * sizeof(int));
+			fJA[nnz + nl] = i;
+			memcpy(fJA + nnz + nl + 1, buf + i, (size_t)ucnt[i] * sizeof(int));
+		}
+		nnz += nl + 1 + ucnt[i];
+		if (fIA) fIA[i + 1] = nnz;
+	}
+	for (i = 0; i < n; i++) { free(ucol[i]); free(ulev[i]); }
+	free(lev); free(buf); free(pos); free(ucnt); free(ucol); free(ulev);
+	return nnz;
+}
+
+/* A's values on the filled pattern (zero at fill entries). */
+void orc_iluk_scatter(int n, const int *IA, const int *JA, const double *AA, const int *fIA, const int *fJA,
+                      double *fA)
+{
+	int i, j, q;
+	for (i = 0; i < n; i++)
+		for (q = fIA[i]; q < fIA[i+1]; q++) {
+			fA[q] = 0.0;
+			for (j = IA[i]; j < IA[i+1]; j++) if (JA[j] == fJA[q]) { fA[q] = AA[j]; break; }
+		}
+}
+
 /* ILUp_precond.c:26-46 */
 void orc_ilu0_apply(int n, const int *IA, const int *JA, const double *LU, const double *Dinv,
                     const double *p, double *z)
@@ -718,8 +794,9 @@ double orc_ddot(int n, const double *x, const double *y)
 /* Operator bundle for the solver; mvf/pcf (with ctx) replace the built-in
  * schemes when set. */
 typedef struct {
-	int scheme, neq, nel, nedge, prec;       /* prec: 0 none, 1 ILU0, 2 Diag */
+	int scheme, neq, nel, nedge, prec;       /* prec: 0 none, 1 ILU(p), 2 Diag */
 	const int *IA, *JA, *lm, *lm2;
+	const int *fIA, *fJA;                    /* ILU(p), p > 0: the filled pattern (NULL: A's) */
 	const double *A, *LU, *Dinv, *invDiag;
 	orc_apply_fn mvf, pcf;
 	const void *ctx;
@@ -737,7 +814,8 @@ static void op_prec(const orc_op *o, double *p, double *z)
 {
 	int i;
 	if (o->pcf) o->pcf(o->ctx, p, z);
-	else if (o->prec == 1) orc_ilu0_apply(o->neq, o->IA, o->JA, o->LU, o->Dinv, p, z);
+	else if (o->prec == 1) orc_ilu0_apply(o->neq, o->fIA ? o->fIA : o->IA, o->fJA ? o->fJA : o->JA, o->LU,
+	                                      o->Dinv, p, z);
 	else if (o->prec == 2) for (i = 0; i < o->neq; i++) z[i] = p[i]*o->invDiag[i];  /* Diag_precond.c:3-14 */
 }
 
@@ -923,7 +1001,9 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 	orc_op o;
 	int *lm = malloc(3 * (size_t)nel * sizeof(int)), neq, I, it = 0;
 	size_t nA;
-	double *A, *F, *u, *uold, *LU = NULL, *Dinv = NULL, *invDiag = NULL, *Fraw = NULL, err = 100.0;
+	double *A, *F, *u, *uold, *LU = NULL, *Dinv = NULL, *invDiag = NULL, *Fraw = NULL, *fA = NULL, err = 100.0;
+	int *fIA = NULL, *fJA = NULL;
+	size_t nLU = 0;
 
 	double t0 = now_s(), t1;
 	memset(&t, 0, sizeof t);
@@ -973,12 +1053,22 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 	o.scheme = t.scheme;
 	o.prec = strcasecmp(precond, "NOT") == 0 ? 0 : strcasecmp(precond, "Diag") == 0 ? 2 : 1;
 	if (o.prec == 1 && t.scheme != ORC_CSR) { free(lm); return -2; }
+	/* "ILU<p>" (ILUp_precond_setup.c:15): p > 0 factors on the filled pattern */
+	if (o.prec == 1 && strncasecmp(precond, "ILU", 3) == 0 && atoi(precond + 3) > 0) {
+		int lvl = atoi(precond + 3), fnnz = orc_iluk_pattern(neq, IA_out, JA_out, lvl, NULL, NULL);
+		fIA = malloc(((size_t)neq + 1) * sizeof(int));
+		fJA = malloc((size_t)fnnz * sizeof(int) + 4);
+		fA = malloc((size_t)fnnz * sizeof(double) + 8);
+		orc_iluk_pattern(neq, IA_out, JA_out, lvl, fIA, fJA);
+		o.fIA = fIA; o.fJA = fJA;
+		nLU = (size_t)fnnz + 1;
+	}
 
 	A = calloc(nA, sizeof(double));
 	F = calloc((size_t)neq + 1, sizeof(double));
 	u = calloc((size_t)neq + 1, sizeof(double));
 	uold = calloc((size_t)neq + 1, sizeof(double));
-	if (o.prec == 1) { LU = calloc(nA, sizeof(double)); Dinv = calloc((size_t)neq + 1, sizeof(double)); }
+	if (o.prec == 1) { LU = calloc(nLU ? nLU : nA, sizeof(double)); Dinv = calloc((size_t)neq + 1, sizeof(double)); }
 	if (o.prec == 2) invDiag = calloc((size_t)neq + 1, sizeof(double));
 	if (g_refine_to > 0) Fraw = calloc((size_t)neq + 1, sizeof(double));
 	o.A = A; o.LU = LU; o.Dinv = Dinv;
@@ -1005,7 +1095,11 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 			free(tmp);
 		}
 		t0 = now_s();
-		if (o.prec == 1) {
+		if (o.prec == 1 && o.fIA) {
+			orc_iluk_scatter(neq, o.IA, o.JA, A, o.fIA, o.fJA, fA);
+			if (orc_ilu0_factor(neq, o.fIA, o.fJA, fA, LU, Dinv)) { it = -3; break; }
+			orc_ilu0_apply(neq, o.fIA, o.fJA, LU, Dinv, F, F);
+		} else if (o.prec == 1) {
 			if (orc_ilu0_factor(neq, o.IA, o.JA, A, LU, Dinv)) { it = -3; break; }
 			orc_ilu0_apply(neq, o.IA, o.JA, LU, Dinv, F, F);
 		} else if (o.prec == 2) {
@@ -1038,6 +1132,7 @@ int orc_transport_run(int nnodes, const double *x, const double *y, const int *n
 		}
 	}
 	free(lm); free(A); free(F); free(u); free(uold); free(LU); free(Dinv); free(invDiag); free(Fraw);
+	free(fIA); free(fJA); free(fA);
 	return it;
 }
 

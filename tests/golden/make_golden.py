@@ -133,6 +133,9 @@ CASES = {
                                                        npicard=1)),
     "hemker12_ede_diag": (12, 12, 0.0, "inflow", dict(problem="HEMKER", scheme="EDE", precond="Diag",
                                                       npicard=1)),
+    # ILU(p) with fill: "ILU1" / "ILU2" (ILUp_precond_setup.c:15, LEVEL_OF_FILL_lu)
+    "skew16_csr_ilu1_rcm": (16, 16, 0.2, "inflow", dict(scheme="CSR", reord="SYMRCM", precond="ILU1", npicard=2)),
+    "skew24x12_csr_ilu2": (24, 12, 0.1, "inflow", dict(scheme="CSR", reord="NOT", precond="ILU2", npicard=2)),
     # the plain-method configuration itself: 64x64 cells, CSR, ILU(0)-GMRES(30)
     # to 1e-8 (1000 restarts), the Picard loop run to its cap of 51 iterations
     # (Process.c:34; the iteration stagnates near max|du| = 0.04)

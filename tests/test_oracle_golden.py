@@ -30,7 +30,7 @@ def test_oracle_bitexact(name):
 def test_golden_cases_cover_options():
     metas = [load_golden(n)[1] for n in golden_names()]
     assert {m.get("scheme") for m in metas} == {"CSR", "EBE", "EDE"}
-    assert {m.get("precond") for m in metas} == {"ILU0", "NOT", "Diag"}
+    assert {m.get("precond") for m in metas} == {"ILU0", "ILU1", "ILU2", "NOT", "Diag"}
     assert {m.get("shock", "CAU") for m in metas} == {"CAU", "YZBeta"}
     assert {m.get("hshock", "2sqrtArea") for m in metas} == {"2sqrtArea", "sqrtArea", "Option1", "Option2"}
     assert {m.get("reord", "NOT") for m in metas} == {"NOT", "SYMRCM"}
