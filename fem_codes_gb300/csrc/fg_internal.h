@@ -60,6 +60,10 @@ typedef struct fg_ilu_sweeps {
 	 * the FP32 sweeps; chain = 0 when the sweeps have too few chained rows */
 	fg_sweep lo64c, up64c, lo32c, up32c;
 	int chain;
+	/* the FP64 chain programs' layout with double-single values (ds = 1:
+	 * the fused FP64 sweeps run on the FP32 pipes, 48-bit significands) */
+	unsigned char *prog_lo_ds, *prog_up_ds;
+	int ds;
 	double *bl64, *y64;
 	float *bl32, *y32;
 	int *fac_ptr, *fac_prog;   /* precompiled elimination of each row        */

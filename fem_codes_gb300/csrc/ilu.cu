@@ -155,6 +155,69 @@ template <typename T, bool FMA> __device__ __forceinline__ T fmsub(T x, T a, T b
 	return fms(x, a, b);
 }
 
+// ---------------------------------------------------- double-single values
+// A value held as the unevaluated sum hi + lo of two floats (|lo| at most
+// half an ulp of hi): 48 significand bits on the FP32 pipes, which on this
+// part issue 64 times as many operations per clock as the FP64 pipe.  The
+// arithmetic is built from the error-free transformations of Knuth's two-sum
+// (a + b = s + e exactly) and of the fused-multiply-add two-product
+// (a * b = p + e exactly, e = fma(a, b, -p)); a product's cross terms and the
+// final addition of the low parts are rounded once each (the "sloppy"
+// double-single sum), so an operation errs by a few units of 2^-48 of its
+// operands -- as accurate as the preconditioner needs, not bit-identical.
+struct __align__(8) dsf { float hi, lo; };
+
+__device__ __forceinline__ dsf ds_two_sum(float a, float b)
+{
+	const float s = a + b, v = s - a;
+	return dsf{ s, (a - (s - v)) + (b - v) };
+}
+
+__device__ __forceinline__ dsf ds_fast_two_sum(float a, float b)     // |a| >= |b|
+{
+	const float s = a + b;
+	return dsf{ s, b - (s - a) };
+}
+
+// c + a * b
+__device__ __forceinline__ dsf ds_fma(dsf a, dsf b, dsf c)
+{
+	const float p = a.hi * b.hi;
+	float e = fmaf(a.hi, b.hi, -p);
+	e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+	dsf s = ds_two_sum(c.hi, p);
+	s.lo += e + c.lo;
+	return ds_fast_two_sum(s.hi, s.lo);
+}
+
+__host__ __device__ __forceinline__ dsf ds_neg(dsf a) { return dsf{ -a.hi, -a.lo }; }
+
+__device__ __forceinline__ dsf ds_from(double v)
+{
+	const float h = __double2float_rn(v);
+	return dsf{ h, __double2float_rn(v - (double)h) };
+}
+
+template <> __device__ __forceinline__ dsf fmsub<dsf, true>(dsf x, dsf a, dsf b) { return ds_fma(ds_neg(a), b, x); }
+template <> __device__ __forceinline__ dsf mul(dsf a, dsf b) { return ds_fma(a, b, dsf{ 0.0f, 0.0f }); }
+
+// zero, FP64 -> T, and the cache-global load / warp shuffle of a T
+template <typename T> __device__ __forceinline__ T zero_t() { return T(0); }
+template <> __device__ __forceinline__ dsf zero_t<dsf>() { return dsf{ 0.0f, 0.0f }; }
+template <typename T> __device__ __forceinline__ T from_d(double v) { return (T)v; }
+template <> __device__ __forceinline__ dsf from_d<dsf>(double v) { return ds_from(v); }
+template <typename T> __device__ __forceinline__ T ld_cg(const T *p) { return __ldcg(p); }
+template <> __device__ __forceinline__ dsf ld_cg<dsf>(const dsf *p)
+{
+	const float2 v = __ldcg((const float2 *)p);
+	return dsf{ v.x, v.y };
+}
+template <typename T> __device__ __forceinline__ T shfl_up_t(T v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
+template <> __device__ __forceinline__ dsf shfl_up_t<dsf>(dsf v, int d)
+{
+	return dsf{ __shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d) };
+}
+
 // Sub-block: 32-byte header, dep[w*cp] (int), out[cp] (int), pad to 16,
 // val[w*cp] (T), and for the backward sweep dinv[cp] (T); the stage then
 // holds the sub-block's slice of the input vector.  Header: rows c, ELL
@@ -597,6 +660,7 @@ __host__ __device__ constexpr int rec_bytes_cs(int w, bool upper, int ts)
 template <typename T> __device__ __forceinline__ T fma_t(T a, T b, T c);
 template <> __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 template <> __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+template <> __device__ __forceinline__ dsf fma_t(dsf a, dsf b, dsf c) { return ds_fma(a, b, c); }
 
 template <typename T, bool UPPER, int W>
 __global__ void __launch_bounds__((SW2_CW + 1) * 32, 1)
@@ -623,7 +687,7 @@ k_sweep_cs(SweepArgs a, const T *__restrict__ in, T *out)
 
 	if (tid == 0) {
 		failed = 0; issued = 0; pdone = 0;
-		ring[SW_RING] = T(0);
+		ring[SW_RING] = zero_t<T>();
 		for (int s = 0; s < D; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], CW); }
 		fence_mbar_init();
 	}
@@ -641,7 +705,7 @@ k_sweep_cs(SweepArgs a, const T *__restrict__ in, T *out)
 	int s = 0, waited = 0;
 	unsigned ph = 0;
 	bool fail = false;
-	T ydef = T(0);                                        // an output not yet stored to global memory
+	T ydef = zero_t<T>();                                 // an output not yet stored to global memory
 	int odef = -1;
 	for (int l = l0; l < l1 && !fail; l++) {
 		const int ll = l - l0;
@@ -682,7 +746,7 @@ k_sweep_cs(SweepArgs a, const T *__restrict__ in, T *out)
 			if (h.w) {
 #pragma unroll
 				for (int k = 0; k < W; k++)
-					if (!((unsigned)ci.i[k] & SW_NEAR)) d[k] = __ldcg(&out[ci.i[k]]);
+					if (!((unsigned)ci.i[k] & SW_NEAR)) d[k] = ld_cg(&out[ci.i[k]]);
 			}
 			T y = x0;
 #pragma unroll
@@ -691,7 +755,7 @@ k_sweep_cs(SweepArgs a, const T *__restrict__ in, T *out)
 			// the segments' recurrences across the warp's lanes
 #pragma unroll
 			for (int k = 0; k < 5; k++) {
-				const T up = __shfl_up_sync(0xffffffffu, y, 1 << k);
+				const T up = shfl_up_t(y, 1 << k);
 				if (lane >= (1 << k)) y = fma_t(cv.v[MO + k], up, y);
 			}
 			ring[(h.z + ctid) & (SW_RING - 1)] = y;
@@ -735,7 +799,7 @@ __global__ void k_chain_mult(unsigned char *prog, const long long *voff, const i
 		if (o >= 0) {
 			T *dst = (T *)(prog + o);
 #pragma unroll
-			for (int k = 0; k < 5; k++) dst[k] = (T)M[k];
+			for (int k = 0; k < 5; k++) dst[k] = from_d<T>(M[k]);
 		}
 	}
 }
@@ -749,6 +813,24 @@ __global__ void k_perm_in(const TI *__restrict__ p, const int *__restrict__ rows
 		in[ppos[i]] = (T)p[rows[i]];
 }
 
+// The same gather into double-single values, and back from double-single
+// (the backward sweep's natural-order output) to FP64.
+__global__ void k_perm_in_ds(const double *__restrict__ p, const int *__restrict__ rows,
+                             const int *__restrict__ ppos, int n, dsf *in)
+{
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		in[ppos[i]] = ds_from(p[rows[i]]);
+}
+
+__global__ void k_ds_to_double(const dsf *__restrict__ x, int n, double *z, const int *active)
+{
+	if (active && !*active) return;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const dsf v = x[i];
+		z[i] = (double)v.hi + (double)v.lo;
+	}
+}
+
 // Refresh the value slots of a program from the factor (after every factorisation).
 template <typename T>
 __global__ void k_refresh(unsigned char *prog, const long long *val_off, const int *val_src, long long nval,
@@ -758,7 +840,7 @@ __global__ void k_refresh(unsigned char *prog, const long long *val_off, const i
 	     i += (long long)gridDim.x * blockDim.x) {
 		int s = val_src[i];
 		double v = (s >= 0) ? LU[s] : (s == -1 ? 0.0 : Dinv[-2 - s]);
-		*(T *)(prog + val_off[i]) = (T)v;
+		*(T *)(prog + val_off[i]) = from_d<T>(v);
 	}
 }
 
@@ -1169,6 +1251,14 @@ static bool sweep_dataflow(void)
 static bool sweep_chain(void)
 {
 	const char *e = getenv("FEMGPU_SWEEP_CHAIN");
+	return !(e && !strcmp(e, "0"));
+}
+
+// Double-single chain sweeps for the fused FP64 (FGMRES) applications
+// (FEMGPU_SWEEP_DS=0: FP64 chain sweeps).
+static bool sweep_ds(void)
+{
+	const char *e = getenv("FEMGPU_SWEEP_DS");
 	return !(e && !strcmp(e, "0"));
 }
 
@@ -1792,7 +1882,7 @@ static int factor_cluster_size(int P)
 #define SC_SET(T, U, W) FG_TRY(cudaFuncSetAttribute(k_sweep_cs<T, U, W>, \
 	cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP))
 #define SR_SET_W(W) SC_SET(double, false, W); SC_SET(double, true, W); SC_SET(float, false, W); \
-	SC_SET(float, true, W); \
+	SC_SET(float, true, W); SC_SET(dsf, false, W); SC_SET(dsf, true, W); \
 	SR_SET(double, false, false, W); SR_SET(double, true, false, W); \
 	SR_SET(double, false, true, W); SR_SET(double, true, true, W); \
 	SR_SET(float, false, false, W); SR_SET(float, true, false, W); \
@@ -1991,6 +2081,7 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 	S.fac2_ok = 0;
 	if ((rc = build_factor_prog2(hIA, hJA, n, Lo, B, S))) return rc;
 	S.chain = 0;
+	S.ds = 0;
 	size_t nb = (size_t)std::max(Lo.pstart[Lo.nlev], Up.pstart[Up.nlev]) + 64;
 	if (sweep_chain()) {
 		ChainLevels CL = host_chain_levels(hIA, hJA, n, true, B), CU = host_chain_levels(hIA, hJA, n, false, B);
@@ -2012,6 +2103,16 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 					rc = sweep_smem(*cs[i], i < 2 ? sizeof(double) : sizeof(float), &D, &sb);
 					if (rc < 0) { S.chain = 0; break; }
 				}
+			}
+			if (S.chain && sweep_ds()) {
+				// the FP64 programs' bytes (codes and offsets are the same;
+				// the refresh rewrites the values as double-single)
+				const size_t bl = (size_t)S.lo64c.bytes + 16, bu = (size_t)S.up64c.bytes + 16;
+				FG_TRY(cudaMalloc((void **)&S.prog_lo_ds, bl));
+				FG_TRY(cudaMalloc((void **)&S.prog_up_ds, bu));
+				FG_TRY(cudaMemcpy(S.prog_lo_ds, S.lo64c.prog, bl, cudaMemcpyDeviceToDevice));
+				FG_TRY(cudaMemcpy(S.prog_up_ds, S.up64c.prog, bu, cudaMemcpyDeviceToDevice));
+				S.ds = 1;
 			}
 		}
 	}
@@ -2075,6 +2176,19 @@ extern "C" int fg_ilu0_factor(femgpu_transport *t)
 		else k_refresh<float><<<g, FG_TPB, 0, s>>>(pr[i]->prog, pr[i]->val_off, pr[i]->val_src,
 		                                          pr[i]->nval, t->ilu.LU, t->ilu.Dinv);
 	}
+	if (S.ds) {
+		const fg_sweep &L = S.lo64c, &U = S.up64c;
+		k_refresh<dsf><<<fg_grid(L.nval), FG_TPB, 0, s>>>(S.prog_lo_ds, L.val_off, L.val_src, L.nval, t->ilu.LU,
+		                                                  t->ilu.Dinv);
+		k_refresh<dsf><<<fg_grid(U.nval), FG_TPB, 0, s>>>(S.prog_up_ds, U.val_off, U.val_src, U.nval, t->ilu.LU,
+		                                                  t->ilu.Dinv);
+		k_chain_mult<dsf, false><<<fg_grid((long long)L.nslot), FG_TPB, 0, s>>>(S.prog_lo_ds, L.cs_voff, L.cs_src,
+		                                                                      L.cs_row, L.nslot, t->ilu.LU,
+		                                                                      t->ilu.Dinv);
+		k_chain_mult<dsf, true><<<fg_grid((long long)U.nslot), FG_TPB, 0, s>>>(S.prog_up_ds, U.cs_voff, U.cs_src,
+		                                                                     U.cs_row, U.nslot, t->ilu.LU,
+		                                                                     t->ilu.Dinv);
+	}
 	if (S.chain) {
 		for (int i = 4; i < 8; i++) {
 			const fg_sweep &c = *pr[i];
@@ -2121,10 +2235,42 @@ static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, 
 // FGMRES sweeps (fused arithmetic) and FP32 sweeps take the chain-scan
 // programs when the factor has them; the reference's left-preconditioned
 // GMRES keeps the row-by-row programs, bit-identical to its ILUp_precond.
+// The double-single chain sweeps: gather into double-single slots, the
+// forward and backward chain-scan programs with double-single values, the
+// backward output (natural order, in the gather buffer) back to FP64.
+static int apply_ds(femgpu_transport *t, const double *p, double *z, const int *active)
+{
+	fg_ilu_sweeps &S = t->sweeps;
+	const fg_sweep &lo = S.lo64c, &up = S.up64c;
+	cudaStream_t s = t->stream;
+	const int n = t->neq;
+	int D, sb, bytes;
+	dsf *bl = (dsf *)S.bl64, *y = (dsf *)S.y64;
+	k_perm_in_ds<<<fg_grid(n), FG_TPB, 0, s>>>(p, lo.rows, lo.ppos, n, bl);
+	SweepArgs a;
+	a.err = &t->st->err;
+	a.active = active;
+	bytes = sweep_smem(lo, sizeof(dsf), &D, &sb);
+	if (bytes < 0) return bytes;
+	a.prog = S.prog_lo_ds; a.blk_off = lo.blk_off; a.sb_in = lo.sb_in; a.sb_inb = lo.sb_inb;
+	a.nlev = lo.nlev; a.nsb = lo.nsb; a.D = D; a.stage_bytes = sb;
+	a.chunk_sb = lo.chunk_sb; a.chunk_lev = lo.chunk_lev; a.bvo = lo.bvo; a.cmax = lo.cmax; a.skew = lo.skew;
+	launch_cs<dsf, false>(a, lo.rw, lo.nchunk, bytes, s, bl, y);
+	bytes = sweep_smem(up, sizeof(dsf), &D, &sb);
+	if (bytes < 0) return bytes;
+	a.prog = S.prog_up_ds; a.blk_off = up.blk_off; a.sb_in = up.sb_in; a.sb_inb = up.sb_inb;
+	a.nlev = up.nlev; a.nsb = up.nsb; a.D = D; a.stage_bytes = sb;
+	a.chunk_sb = up.chunk_sb; a.chunk_lev = up.chunk_lev; a.bvo = up.bvo; a.cmax = up.cmax; a.skew = up.skew;
+	launch_cs<dsf, true>(a, up.rw, up.nchunk, bytes, s, y, bl);
+	k_ds_to_double<<<fg_grid(n), FG_TPB, 0, s>>>(bl, n, z, active);
+	return (int)cudaGetLastError();
+}
+
 extern "C" int fg_ilu0_apply64(femgpu_transport *t, const double *p, double *z, const int *active)
 {
 	fg_ilu_sweeps &S = t->sweeps;
 	const bool fma = t->o.solver == FEMGPU_FGMRES;
+	if (fma && S.ds) return apply_ds(t, p, z, active);
 	if (fma && S.chain)
 		return apply_t<double, double, double>(t, S.lo64c, S.up64c, S.bl64, S.y64, p, z, active, true);
 	return apply_t<double, double, double>(t, S.lo64, S.up64, S.bl64, S.y64, p, z, active, fma);
@@ -2155,6 +2301,10 @@ extern "C" void fg_ilu_free(femgpu_transport *t)
 	S.fIA = S.fJA = S.fmap = nullptr;
 	S.fA = nullptr;
 	S.fill = 0;
+	if (S.prog_lo_ds) cudaFree(S.prog_lo_ds);
+	if (S.prog_up_ds) cudaFree(S.prog_up_ds);
+	S.prog_lo_ds = S.prog_up_ds = nullptr;
+	S.ds = 0;
 	free(S.block_first);
 	S.block_first = nullptr;
 	S.nblocks = 0;
