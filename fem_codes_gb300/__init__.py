@@ -84,6 +84,33 @@ class NSOpts(ctypes.Structure):
                 ("scheme", ctypes.c_int), ("ilu_blocks", ctypes.c_int)]
 
 
+class Deck(ctypes.Structure):
+    """femgpu_deck of femgpu.h (a parameter deck as the drivers read it)."""
+    _fields_ = [("equation", ctypes.c_int)] + \
+        [(n, ctypes.c_char * k) for n, k in (
+            ("Experiments", 200), ("ProblemTitle", 300), ("Solver", 200), ("Preconditioner", 1000),
+            ("Scaling", 200), ("reordering", 200), ("MatrixVectorProductScheme", 200), ("StabilizationForm", 200),
+            ("ShockCapture", 200), ("h_Shock", 200), ("OutputFlow", 200), ("TimeIntegration", 200),
+            ("StopAtSteadyState", 200), ("Dimensionless", 200), ("StopMulticorrection", 200))] + \
+        [(n, ctypes.c_double) for n in ("SolverTolerance", "NonLinearTolerance", "TimeIntegrationTolerance",
+                                       "StabilizationTolerance", "Alpha", "DeltaT", "FinalTime", "Mach")] + \
+        [("invY", ctypes.c_double * 4)] + \
+        [(n, ctypes.c_double) for n in ("ReynoldsNumber", "VelMax", "SolverToleranceNonLin")] + \
+        [(n, ctypes.c_int) for n in ("SolverMaxIter", "KrylovBasisVectorsQuantity", "LinearMaxIter",
+                                    "NonLinearMaxIter", "SolverToleranceCase", "nnodes", "nel")]
+
+    def as_dict(self):
+        out = {}
+        for name, typ in self._fields_:
+            v = getattr(self, name)
+            if isinstance(v, bytes):
+                v = v.decode()
+            elif name == "invY":
+                v = list(v)
+            out[name] = v
+        return out
+
+
 _vp = ctypes.c_void_p
 _ip = ctypes.POINTER(ctypes.c_int)
 
@@ -112,6 +139,14 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_transport_ilu_chain": [_vp, _vp],
         "femgpu_ilu_block_cut": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, ctypes.c_int],
         "femgpu_iluk_pattern": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp, ctypes.c_int],
+        "femgpu_deck_read": [ctypes.c_char_p, ctypes.c_int, _vp],
+        "femgpu_deck_mesh_file": [_vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int],
+        "femgpu_mesh_read": [ctypes.c_char_p, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+        "femgpu_mesh_side_types": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp],
+        "femgpu_deck_transport_opts": [_vp, _vp],
+        "femgpu_deck_euler_opts": [_vp, _vp],
+        "femgpu_deck_ns_opts": [_vp, _vp],
+        "femgpu_deck_amg": [_vp, _vp, _vp, _vp, _vp],
         "femgpu_ilu_chain_segments": [ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
                                       ctypes.c_int, ctypes.c_int],
         "femgpu_transport_get_pattern": [_vp, _vp, _vp, _vp, _vp, _vp],
@@ -257,6 +292,70 @@ def ilu_block_cut(IA, JA, P):
     if rc < 0:
         raise FemGpuError(rc, "ilu_block_cut")
     return first[: rc + 1]
+
+
+EQUATIONS = {"transport": 0, "euler": 1, "ns": 2}
+NODE_TYPES = {"transport": 1, "euler": 4, "ns": 3}
+
+
+def read_deck(path, equation="transport"):
+    """A parameter deck as the driver's Preprocess reads it (femgpu_deck):
+    the Deck structure (``as_dict()`` for a dict)."""
+    L = load()
+    d = Deck()
+    rc = L.femgpu_deck_read(os.fsencode(path), EQUATIONS[equation], ctypes.byref(d))
+    if rc:
+        raise FemGpuError(rc, f"read_deck {path}")
+    return d
+
+
+def deck_mesh_file(deck, directory):
+    """The mesh file a driver opens for a deck: <dir>/<title>_<nnodes>_<nel>.dat."""
+    L = load()
+    buf = ctypes.create_string_buffer(4096)
+    rc = L.femgpu_deck_mesh_file(ctypes.byref(deck), os.fsencode(directory), buf, 4096)
+    if rc:
+        raise FemGpuError(rc, "deck_mesh_file")
+    return buf.value.decode()
+
+
+def read_mesh(path, equation="transport"):
+    """A mesh file in the drivers' format: dict(x, y, node_type [nnodes, k],
+    vert [nel, 3], elem_type).  For transport the element types are the
+    boundary sides its Preprocess sets (femgpu_mesh_side_types); Euler and
+    Navier-Stokes keep the file's column."""
+    L = load()
+    k = NODE_TYPES[equation]
+    nn, ne = ctypes.c_int(0), ctypes.c_int(0)
+    p = os.fsencode(path)
+    rc = L.femgpu_mesh_read(p, k, ctypes.byref(nn), ctypes.byref(ne), None, None, None, None, None)
+    if rc:
+        raise FemGpuError(rc, f"read_mesh {path}")
+    x, y = np.zeros(nn.value), np.zeros(nn.value)
+    nt = np.zeros((nn.value, k), np.int32)
+    vert = np.zeros((ne.value, 3), np.int32)
+    et = np.zeros(ne.value, np.int32)
+    rc = L.femgpu_mesh_read(p, k, ctypes.byref(nn), ctypes.byref(ne), _ptr(x), _ptr(y), _ptr(nt), _ptr(vert),
+                            _ptr(et))
+    if rc:
+        raise FemGpuError(rc, f"read_mesh {path}")
+    if equation == "transport":
+        rc = L.femgpu_mesh_side_types(nn.value, _ptr(x), _ptr(y), ne.value, _ptr(vert), _ptr(et))
+        if rc:
+            raise FemGpuError(rc, f"read_mesh {path}")
+    return dict(x=x, y=y, node_type=nt if k > 1 else nt[:, 0].copy(), vert=vert, elem_type=et)
+
+
+def deck_opts(deck):
+    """The deck's strings as the library's options (Opts, EulerOpts or NSOpts)."""
+    L = load()
+    eq = deck.equation
+    o = (Opts, EulerOpts, NSOpts)[eq]()
+    f = (L.femgpu_deck_transport_opts, L.femgpu_deck_euler_opts, L.femgpu_deck_ns_opts)[eq]
+    rc = f(ctypes.byref(deck), ctypes.byref(o))
+    if rc:
+        raise FemGpuError(rc, "deck_opts")
+    return o
 
 
 def iluk_pattern(IA, JA, p):

@@ -62,6 +62,9 @@ int fgh_blockcsr_create(fg_blockcsr *b, int M, const femgpu_ebe *ebe, int nel, i
 void fgh_blockcsr_destroy(fg_blockcsr *b)
 {
 	femgpu_transport *t = b->ilu;
+	/* the AMG context is the caller's and outlives this one: give it back
+	 * its own stream before the owner's stream goes away */
+	if (b->amg) femgpu_amg_set_stream(b->amg, NULL);
 	if (t) {
 		if (b->have_ilu) fg_ilu_free(t);
 		if (t->st) cudaFree(t->st);

@@ -506,7 +506,9 @@ int femgpu_transport_set_amg(femgpu_transport *t, femgpu_amg *ctx);
  * precond FEMGPU_PREC_AMG (setPreconditioner.c:63-73 of the Navier-Stokes
  * driver, :130-140 of the Euler driver): precond_setup builds the hierarchy
  * of the current CSR matrix and (left-preconditioned GMRES) applies one
- * V-cycle to the right-hand side; the solves apply one V-cycle per step. */
+ * V-cycle to the right-hand side; the solves apply one V-cycle per step.
+ * In all three ctx runs on the context's stream while set and goes back to
+ * its own stream when the context is destroyed, so ctx must outlive it. */
 int femgpu_ns_set_amg(femgpu_ns *ns, femgpu_amg *ctx);
 int femgpu_euler_set_amg(femgpu_euler *eu, femgpu_amg *ctx);
 
@@ -532,6 +534,48 @@ int femgpu_csrmv_f32(int n, const int *IA, const int *JA, const float *AA,
  * so serialise them. */
 int femgpu_csr_resnorm_noalloc(int n, const int *IA, const int *JA, const double *AA,
 		const double *u, const double *F, double *out2, void *stream);
+
+/* ---- parameter decks and mesh files (no GPU needed) ------------------------
+ * The reading half of each driver's Preprocess (transport Preprocess.c:
+ * 44-99, Euler Preprocess.c:45-102, Navier-Stokes Preprocess.c:45-88): the
+ * deck's "value<TAB>:label" lines in the driver's order, and the mesh file
+ * <dir>/<ProblemTitle>_<nnodes>_<nel>.dat (node count; per node x, y and the
+ * driver's node types -- 1 for transport (Type), 4 for Euler (rhoType,
+ * v1Type, v2Type, eType), 3 for Navier-Stokes (v1Type, v2Type, pType); the
+ * element count; per element three vertices and its type). */
+enum femgpu_equation { FEMGPU_EQ_TRANSPORT = 0, FEMGPU_EQ_EULER = 1, FEMGPU_EQ_NS = 2 };
+typedef struct femgpu_deck {
+	int equation;
+	char Experiments[200], ProblemTitle[300], Solver[200], Preconditioner[1000], Scaling[200],
+	     reordering[200], MatrixVectorProductScheme[200], StabilizationForm[200], ShockCapture[200],
+	     h_Shock[200], OutputFlow[200], TimeIntegration[200], StopAtSteadyState[200], Dimensionless[200],
+	     StopMulticorrection[200];
+	double SolverTolerance, NonLinearTolerance, TimeIntegrationTolerance, StabilizationTolerance, Alpha,
+	       DeltaT, FinalTime, Mach, invY[4], ReynoldsNumber, VelMax, SolverToleranceNonLin;
+	int SolverMaxIter, KrylovBasisVectorsQuantity, LinearMaxIter, NonLinearMaxIter, SolverToleranceCase,
+	    nnodes, nel;
+} femgpu_deck;
+int femgpu_deck_read(const char *path, int equation, femgpu_deck *deck);
+/* The mesh file the driver opens for a deck: <dir>/<ProblemTitle>_<nnodes>_<nel>.dat. */
+int femgpu_deck_mesh_file(const femgpu_deck *deck, const char *dir, char *path, int cap);
+/* Read a mesh file with ntype node types per node: sizes into nnodes, nel;
+ * x, y [nnodes], node_type [ntype*nnodes], vert [3*nel], elem_type [nel]
+ * filled when non-NULL (call once with NULL arrays for the sizes). */
+int femgpu_mesh_read(const char *path, int ntype, int *nnodes, int *nel, double *x, double *y, int *node_type,
+		int *vert, int *elem_type);
+/* The element types the transport drivers' Preprocess sets after reading
+ * (01_SS_Transport_Equation/2D/01_CommonFiles/Preprocess.c:107-151): the
+ * side of the unit square an element has two vertices on (1 x=0, 2 y=0,
+ * 3 x=1, 4 y=1), 5-8 for the corner pairs the reference tests, -1 inside. */
+int femgpu_mesh_side_types(int nnodes, const double *x, const double *y, int nel, const int *vert, int *elem_type);
+/* The deck's strings as options (each driver's setMatrixVectorProductType.c,
+ * setPreconditioner.c, setStabilizationForm.c); FEMGPU_E_ARG for a choice
+ * the library does not provide.  femgpu_deck_amg parses "AMG 2 NCL beta
+ * omega nr" (amg_precond.c:26-40). */
+int femgpu_deck_transport_opts(const femgpu_deck *deck, femgpu_transport_opts *o);
+int femgpu_deck_euler_opts(const femgpu_deck *deck, femgpu_euler_opts *o);
+int femgpu_deck_ns_opts(const femgpu_deck *deck, femgpu_ns_opts *o);
+int femgpu_deck_amg(const femgpu_deck *deck, int *ncl, double *beta, double *omega, int *nr);
 
 /* ---- host utilities (no GPU needed) ------------------------------------- */
 /* REORDERING_SYMRCM (00_CommonFiles/Reordering/symrcm.c:4-242): reverse

@@ -333,3 +333,37 @@ int ref_transport_vtu(int nnodes, const double *x, const double *y, const int *n
 	set_problem(problem, FF);
 	return Paraview_Output(P, FS, FF);
 }
+
+/* The reference's own Preprocess (Preprocess.c:4-260) on a deck file, run in
+ * the working directory (it opens ../02_mesh/<title>_<nnodes>_<nel>.dat):
+ * the parameters it read (ints: nnodes, nel, neq, SolverMaxIter,
+ * KrylovBasisVectorsQuantity, nnzero; doubles: SolverTolerance,
+ * NonLinearTolerance; strings: the deck's 11 strings, 64 bytes apart), the
+ * nodes (x, y, Type, id) and elements (vertices, Type) it built. */
+int Preprocess(int, char **, ParametersType **, MatrixDataType **, FemStructsType **, FemFunctionsType **,
+               FemOtherFunctionsType **);
+int ref_transport_preprocess(const char *deck, int *iv, double *dv, char *sv, double *x, double *y, int *type,
+                             int *id, int *vert, int *etype, int cap_nodes, int cap_el)
+{
+	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF; FemOtherFunctionsType *FOF;
+	char *argv[2] = { "harness", (char *)deck };
+	int I;
+	const char *str[11];
+	Preprocess(2, argv, &P, &M, &FS, &FF, &FOF);
+	iv[0] = P->nnodes; iv[1] = P->nel; iv[2] = P->neq; iv[3] = P->SolverMaxIter;
+	iv[4] = P->KrylovBasisVectorsQuantity; iv[5] = P->nnzero;
+	dv[0] = P->SolverTolerance; dv[1] = P->NonLinearTolerance;
+	str[0] = P->Experiments; str[1] = P->ProblemTitle; str[2] = P->Solver; str[3] = P->Preconditioner;
+	str[4] = P->Scaling; str[5] = P->reordering; str[6] = P->MatrixVectorProductScheme;
+	str[7] = P->StabilizationForm; str[8] = P->ShockCapture; str[9] = P->h_Shock; str[10] = P->OutputFlow;
+	for (I = 0; I < 11; I++) strncpy(sv + 64 * I, str[I], 63);
+	if (P->nnodes > cap_nodes || P->nel > cap_el) return -1;
+	for (I = 0; I < P->nnodes; I++) {
+		x[I] = FS->Node[I].x; y[I] = FS->Node[I].y; type[I] = FS->Node[I].Type; id[I] = FS->Node[I].id;
+	}
+	for (I = 0; I < P->nel; I++) {
+		vert[3 * I] = FS->Element[I].Vertex[0]; vert[3 * I + 1] = FS->Element[I].Vertex[1];
+		vert[3 * I + 2] = FS->Element[I].Vertex[2]; etype[I] = FS->Element[I].Type;
+	}
+	return 0;
+}
