@@ -15,11 +15,14 @@ ILU(0) factorisation, and the linear solve to a relative residual of 1e-8 on
 the unpreconditioned FP64 residual ||F - A u|| / ||F||, checked on the true
 residual (right-preconditioned flexible GMRES(80); the reference's
 left-preconditioned stopping rule is not used because it accepts residuals of
-0.5 on this mesh).  Default preconditioner: block ILU(0) over 16 contiguous
+0.5 on this mesh).  Default preconditioner: block ILU(0) over 32 contiguous
 row blocks of the SYMRCM numbering cut at equal spans of the factor's
 dependency levels, each factorised by its own thread-block cluster and swept
-by its own thread block (--ilu-blocks 0: ILU(0) of the whole matrix).  Steps
-continue the Picard sequence from the warm-up steps.
+by its own thread block (--ilu-blocks 0: ILU(0) of the whole matrix).  The
+sweeps solve rows chained along the SYMRCM fronts 32 at a time by a warp scan
+in double-single arithmetic (48-bit significands on the FP32 pipes, the
+residual and Arnoldi in FP64).  Steps continue the Picard sequence from the
+warm-up steps.
 
 The same line carries an "euler" object (REFLETIDO on 1024x256 cells, a step
 being one implicit time step: predictor + 2 correctors) and an "ns" object
@@ -67,7 +70,7 @@ def parse(argv=None):
     ap.add_argument("--precond", default="ILU0")
     ap.add_argument("--reorder", default="SYMRCM", choices=["NOT", "SYMRCM"])
     ap.add_argument("--kmax", type=int, default=80)
-    ap.add_argument("--ilu-blocks", type=int, default=16,
+    ap.add_argument("--ilu-blocks", type=int, default=32,
                     help="0: ILU(0) of the whole matrix; P > 1: block ILU(0) over P row blocks")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-amg", action="store_true", help="skip the AMG-preconditioned leg")
@@ -365,8 +368,10 @@ def run_ours(a):
         alg = nnz * (vs + 4) + neq * vs + 4 * neq * vs
         t_k = kern[sweep_key]
         if chain:
+            ds = a.precision == "FP64" and os.environ.get("FEMGPU_SWEEP_DS", "1") != "0"
             name = ("k_sweep_cs (ILU(0) forward+backward, chain-scan: rows chained along the SYMRCM fronts solved "
-                    "32 at a time by a warp scan, row records, dataflow between warps")
+                    "32 at a time by a warp scan" + (" in double-single arithmetic" if ds else "")
+                    + ", row records, dataflow between warps")
         elif os.environ.get("FEMGPU_SWEEP_LAYOUT") == "ell":
             name = "k_sweep (ILU(0) forward+backward, ELL layout, a barrier per level"
         elif os.environ.get("FEMGPU_SWEEP_SYNC") == "barrier":

@@ -143,6 +143,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_deck_mesh_file": [_vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int],
         "femgpu_mesh_read": [ctypes.c_char_p, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_mesh_side_types": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp],
+        "femgpu_transport_set_sweep_wait": [_vp, ctypes.c_int],
         "femgpu_deck_transport_opts": [_vp, _vp],
         "femgpu_deck_euler_opts": [_vp, _vp],
         "femgpu_deck_ns_opts": [_vp, _vp],
@@ -619,6 +620,11 @@ class SSTransport:
         if rc < 0:
             raise FemGpuError(rc, "ilu_chain")
         return rc
+
+    def set_sweep_wait(self, spins=-1):
+        """Bound on a sweep warp's wait for its dependencies (-1: default);
+        also clears the context's device error word."""
+        self._check(self._L.femgpu_transport_set_sweep_wait(self._h, int(spins)), "set_sweep_wait")
 
     def fell_back(self):
         """0, or how the last learned-preconditioned solve continued after a

@@ -168,6 +168,7 @@ struct femgpu_transport {
 	float *invDiag32;
 	fg_ilu ilu;
 	fg_ilu_sweeps sweeps;
+	int sweep_wait1;                /* 1 + dependency-wait bound; 0: default */
 
 	/* Krylov workspace */
 	int kmax;

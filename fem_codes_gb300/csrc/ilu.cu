@@ -248,6 +248,7 @@ struct SweepArgs {
 	const int *chunk_lev;         // [P+1] first level of each matrix block
 	int bvo, cmax;                // record layout: input slice offset, most rows of a sub-block
 	int skew;                     // dataflow: levels a warp may run ahead of the slowest one
+	int wait;                     // spins of a warp waiting for the rows it depends on
 };
 
 // The producer warp of every sweep kernel: streams this thread block's
@@ -294,7 +295,10 @@ __device__ __forceinline__ void sweep_producer(const SweepArgs &a, const T *in, 
 			if (++s == D) { s = 0; if (sb >= D) ph ^= 1u; else if (sb == D - 1) ph = 0; }
 		}
 	}
-	if (lane == 0) *(volatile int *)pdone = 1;
+	if (lane == 0) {
+		__threadfence_block();                            // `issued' is final before `pdone'
+		*(volatile int *)pdone = 1;
+	}
 }
 
 // After a consumer failed (one thread): record the timeout, let the producer
@@ -305,6 +309,7 @@ __device__ __forceinline__ void sweep_drain(const SweepArgs &a, unsigned long lo
 {
 	fg_set_err(a.err, FEMGPU_E_TIMEOUT);
 	for (int i = 0; i < SW_WAIT_LIMIT && !*(volatile int *)pdone; i++) __nanosleep(64);
+	__threadfence_block();
 	int last = *(volatile int *)issued;
 	for (int q = done; q < last; q++) (void)mbar_wait(&full[q % D], (unsigned)((q / D) & 1));
 }
@@ -593,7 +598,7 @@ k_sweep_df(SweepArgs a, const T *__restrict__ in, T *out)
 			// producers of this warp's dependencies, and every warp within the skew
 			const int want = ll - (need == 255 ? a.skew + 1 : need);
 			bool ready = false;
-			for (int it = 0; it < SW_WAIT_LIMIT; it++) {
+			for (int it = 0; it < a.wait; it++) {
 				const bool mine = lane >= CW || lane == warp || ld_acquire_cta(&prog[lane]) >= want;
 				if (__all_sync(0xffffffffu, mine)) { ready = true; break; }
 				if (__any_sync(0xffffffffu, *vfailed != 0)) break;
@@ -730,7 +735,7 @@ k_sweep_cs(SweepArgs a, const T *__restrict__ in, T *out)
 			if (32 * warp >= h.x) continue;               // no chunk of this warp here (uniform)
 			const int want = ll - (need == 255 ? a.skew + 1 : need);
 			bool ready = false;
-			for (int it = 0; it < SW_WAIT_LIMIT; it++) {
+			for (int it = 0; it < a.wait; it++) {
 				const bool mine = lane >= CW || lane == warp || ld_acquire_cta(&prog[lane]) >= want;
 				if (__all_sync(0xffffffffu, mine)) { ready = true; break; }
 				if (__any_sync(0xffffffffu, *vfailed != 0)) break;
@@ -2207,6 +2212,14 @@ extern "C" int fg_ilu0_factor(femgpu_transport *t)
 	return (int)cudaGetLastError();
 }
 
+// The dependency-wait bound of the sweep warps: the context's override
+// (sweep_wait1 = bound + 1) or SW_WAIT_LIMIT.  Stage waits and the drain after
+// a timeout always keep SW_WAIT_LIMIT, so no bulk copy outlives its block.
+static int sweep_wait(const femgpu_transport *t)
+{
+	return t->sweep_wait1 > 0 ? t->sweep_wait1 - 1 : SW_WAIT_LIMIT;
+}
+
 template <typename T, typename TI, typename TO>
 static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, T *bl, T *y,
                    const TI *p, TO *z, const int *active, bool fma)
@@ -2217,6 +2230,7 @@ static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, 
 	SweepArgs a;
 	a.err = &t->st->err;
 	a.active = active;
+	a.wait = sweep_wait(t);
 	bytes = sweep_smem(lo, sizeof(T), &D, &sb);
 	if (bytes < 0) return bytes;
 	a.prog = lo.prog; a.blk_off = lo.blk_off; a.sb_in = lo.sb_in; a.sb_inb = lo.sb_inb;
@@ -2250,6 +2264,7 @@ static int apply_ds(femgpu_transport *t, const double *p, double *z, const int *
 	SweepArgs a;
 	a.err = &t->st->err;
 	a.active = active;
+	a.wait = sweep_wait(t);
 	bytes = sweep_smem(lo, sizeof(dsf), &D, &sb);
 	if (bytes < 0) return bytes;
 	a.prog = S.prog_lo_ds; a.blk_off = lo.blk_off; a.sb_in = lo.sb_in; a.sb_inb = lo.sb_inb;

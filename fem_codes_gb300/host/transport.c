@@ -358,6 +358,17 @@ int femgpu_transport_ilu_chain(const femgpu_transport *t, int *levels)
 	return t->sweeps.chain ? 1 : 0;
 }
 
+int femgpu_transport_set_sweep_wait(femgpu_transport *t, int spins)
+{
+	if (!t) return FEMGPU_E_ARG;
+	CK(cudaStreamSynchronize(t->stream));
+	t->sweep_wait1 = spins < 0 ? 0 : (spins == 0x7fffffff ? spins : spins + 1);
+	CK(cudaMemsetAsync(&t->st->err, 0, sizeof(int), t->stream));
+	t->st_host->err = 0;
+	CK(cudaStreamSynchronize(t->stream));
+	return 0;
+}
+
 int femgpu_transport_get_pattern(const femgpu_transport *t, int *IA, int *JA, int *sbe, int *order,
 		int *node_id)
 {

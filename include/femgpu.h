@@ -141,6 +141,15 @@ int femgpu_transport_ilu_blocks(const femgpu_transport *ctx, int *first, int cap
  * FEMGPU_E_NOT_BUILT before the ILU(0) structure exists. */
 int femgpu_transport_ilu_chain(const femgpu_transport *ctx, int *levels);
 
+/* Bound, in spins, on a sweep warp's wait for the rows its own rows depend
+ * on (spins < 0: the default, 2^24); a warp that gives up records
+ * FEMGPU_E_TIMEOUT, the other warps of its block stop, the block waits for
+ * the copies it has in flight (that wait keeps the default bound) and
+ * returns, and the call reports the error.  0 makes every sweep time out at
+ * its first dependent row, the way a test reaches the error path.  Also
+ * clears the context's device error word, so the context is usable again. */
+int femgpu_transport_set_sweep_wait(femgpu_transport *ctx, int spins);
+
 /* The same cut for a CSR pattern on the host, no device needed: returns the
  * number of runs R = max(min(P, n), 1) and writes R + 1 row boundaries to
  * first (cap = room in first; FEMGPU_E_ARG when cap < R + 1).  The pattern
