@@ -382,7 +382,7 @@ def run_ours(a):
     else:
         alg = nnz * 12 + (neq + 1) * 4 + 2 * neq * 8
         t_k = kern["spmv_f64"]
-        name = "k_csrmv64"
+        name = "k_csrmv_tile<double> (FP64 CSR, row tiles, coalesced slice, products staged in shared memory)"
     achieved = alg / (t_k * 1e-3) / 1e9
     traffic = read_traffic(dom)
     spmv_bytes = nnz * 12 + (neq + 1) * 4 + 2 * neq * 8
@@ -397,7 +397,7 @@ def run_ours(a):
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s"},
-        "matvec": {"kernel": "k_csrmv64 (FP64 CSR)", "GB/s": spmv_gbs, "frac": spmv_gbs / peak,
+        "matvec": {"kernel": "k_csrmv_tile<double> (FP64 CSR)", "GB/s": spmv_gbs, "frac": spmv_gbs / peak,
                    "us": kern["spmv_f64"] * 1e3, "bytes": spmv_bytes,
                    "f32_us": kern["spmv_f32"] * 1e3,
                    "f32_GB/s": (nnz * 8 + (neq + 1) * 4 + 2 * neq * 4) / (kern["spmv_f32"] * 1e-3) / 1e9},

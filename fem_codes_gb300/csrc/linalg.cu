@@ -18,71 +18,103 @@
 #include <stdlib.h>
 
 // ============================================================= matvecs ====
-// csrmv.c:15-20: Q[i] = sum_j AA[j] P[JA[j]] in column order.
-__global__ void k_csrmv64(int n, const int *__restrict__ IA, const int *__restrict__ JA,
-                          const double *__restrict__ AA, const double *__restrict__ P,
-                          double *__restrict__ Q, const int *active)
+// csrmv.c:15-20, Q[i] = sum_j AA[j] P[JA[j]] in column order, over tiles of
+// MV_ROWS consecutive rows.  A block streams its tile's slice of AA and JA
+// with coalesced loads (thread t takes entries t, t + MV_ROWS, ...), forms
+// each rounded product into shared memory, and then each thread adds up its
+// own row's products in column order -- the reference's rounding sequence,
+// so the FP64 product is bit-identical while no load is strided by the row
+// length.  A tile whose entries exceed MV_CAP is taken in runs of rows that
+// fit (a row longer than MV_CAP alone is gathered by its own thread).
+#define MV_ROWS 256
+#define MV_CAP 4096
+
+template <typename T> struct mv_ops;
+template <> struct mv_ops<double> {
+	static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+	static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+};
+template <> struct mv_ops<float> {
+	static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+	static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+};
+
+template <typename TA, typename TP, typename TACC, typename TO>
+__global__ void __launch_bounds__(MV_ROWS) k_csrmv_tile(int n, const int *__restrict__ IA,
+                                                        const int *__restrict__ JA, const TA *__restrict__ AA,
+                                                        const TP *__restrict__ P, TO *__restrict__ Q,
+                                                        const int *active)
 {
+	typedef mv_ops<TACC> op;
 	if (active && !*active) return;
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		double q = 0.0;
-		int e = __ldg(&IA[i + 1]);
-		for (int j = __ldg(&IA[i]); j < e; j++)
-			q = __dadd_rn(q, __dmul_rn(__ldg(&AA[j]), __ldg(&P[__ldg(&JA[j])])));
-		Q[i] = q;
+	__shared__ TACC prod[MV_CAP];
+	__shared__ int kpos[2];
+	const int tid = threadIdx.x;
+	const int r0 = blockIdx.x * MV_ROWS, r1 = min(r0 + MV_ROWS, n), i = r0 + tid;
+	const bool mine = i < r1;
+	const int kb = mine ? __ldg(&IA[i]) : 0, ke = mine ? __ldg(&IA[i + 1]) : 0;
+	int rs = r0;
+	while (rs < r1) {                                     // rs, re, k0, k1 are uniform over the block
+		if (i == rs) kpos[0] = kb;
+		__syncthreads();
+		const int k0 = kpos[0];
+		const int re = rs + __syncthreads_count(mine && i >= rs && ke - k0 <= MV_CAP);
+		if (re == rs) {                                   // a row longer than MV_CAP
+			if (i == rs) {
+				TACC q = TACC(0);
+				for (int j = kb; j < ke; j++)
+					q = op::add(q, op::mul((TACC)__ldg(&AA[j]), (TACC)__ldg(&P[__ldg(&JA[j])])));
+				Q[i] = (TO)q;
+			}
+			rs = re + 1;
+			continue;
+		}
+		if (i == re - 1) kpos[1] = ke;
+		__syncthreads();
+		const int k1 = kpos[1];
+		int k = k0 + tid;
+		for (; k + 3 * MV_ROWS < k1; k += 4 * MV_ROWS) {
+			const TA a0 = __ldcs(&AA[k]), a1 = __ldcs(&AA[k + MV_ROWS]);
+			const TA a2 = __ldcs(&AA[k + 2 * MV_ROWS]), a3 = __ldcs(&AA[k + 3 * MV_ROWS]);
+			const int c0 = __ldcs(&JA[k]), c1 = __ldcs(&JA[k + MV_ROWS]);
+			const int c2 = __ldcs(&JA[k + 2 * MV_ROWS]), c3 = __ldcs(&JA[k + 3 * MV_ROWS]);
+			const TP p0 = __ldg(&P[c0]), p1 = __ldg(&P[c1]), p2 = __ldg(&P[c2]), p3 = __ldg(&P[c3]);
+			prod[k - k0] = op::mul((TACC)a0, (TACC)p0);
+			prod[k - k0 + MV_ROWS] = op::mul((TACC)a1, (TACC)p1);
+			prod[k - k0 + 2 * MV_ROWS] = op::mul((TACC)a2, (TACC)p2);
+			prod[k - k0 + 3 * MV_ROWS] = op::mul((TACC)a3, (TACC)p3);
+		}
+		for (; k < k1; k += MV_ROWS) prod[k - k0] = op::mul((TACC)__ldcs(&AA[k]), (TACC)__ldg(&P[__ldcs(&JA[k])]));
+		__syncthreads();
+		if (i >= rs && i < re) {
+			TACC q = TACC(0);
+			for (int j = kb - k0; j < ke - k0; j++) q = op::add(q, prod[j]);
+			Q[i] = (TO)q;
+		}
+		__syncthreads();                                  // prod and kpos are reused by the next run
+		rs = re;
 	}
 }
 
-// FP32 values and input, G lanes per row, FP32 accumulation; output TO.
-template <int G, typename TO>
-__global__ void k_csrmv32(int n, const int *__restrict__ IA, const int *__restrict__ JA,
-                          const float *__restrict__ AA, const float *__restrict__ P,
-                          TO *__restrict__ Q, const int *active)
+template <typename TA, typename TP, typename TACC, typename TO>
+static int launch_csrmv(int n, const int *IA, const int *JA, const TA *AA, const TP *P, TO *Q, const int *active,
+                        cudaStream_t s)
 {
-	if (active && !*active) return;
-	int lane = threadIdx.x % G;
-	long long gstride = (long long)gridDim.x * blockDim.x / G;
-	for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += gstride) {
-		int b = __ldg(&IA[r]), e = __ldg(&IA[r + 1]);
-		float q = 0.f;
-		for (int j = b + lane; j < e; j += G) q = fmaf(__ldg(&AA[j]), __ldg(&P[__ldg(&JA[j])]), q);
-		#pragma unroll
-		for (int o = G / 2; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o, G);
-		if (lane == 0) Q[r] = (TO)q;
-	}
-}
-
-// FP64 values, FP32 input, FP64 accumulation (mixed mode with FP64 operator).
-template <int G>
-__global__ void k_csrmv64_xf(int n, const int *__restrict__ IA, const int *__restrict__ JA,
-                             const double *__restrict__ AA, const float *__restrict__ P,
-                             double *__restrict__ Q, const int *active)
-{
-	if (active && !*active) return;
-	int lane = threadIdx.x % G;
-	long long gstride = (long long)gridDim.x * blockDim.x / G;
-	for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G; r < n; r += gstride) {
-		int b = __ldg(&IA[r]), e = __ldg(&IA[r + 1]);
-		double q = 0.0;
-		for (int j = b + lane; j < e; j += G) q = fma(__ldg(&AA[j]), (double)__ldg(&P[__ldg(&JA[j])]), q);
-		#pragma unroll
-		for (int o = G / 2; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o, G);
-		if (lane == 0) Q[r] = q;
-	}
+	if (n <= 0) return 0;
+	k_csrmv_tile<TA, TP, TACC, TO><<<(n + MV_ROWS - 1) / MV_ROWS, MV_ROWS, 0, s>>>(n, IA, JA, AA, P, Q, active);
+	return (int)cudaGetLastError();
 }
 
 extern "C" int fg_csrmv64(int n, const int *IA, const int *JA, const double *AA, const double *P,
                           double *Q, const int *active, cudaStream_t s)
 {
-	k_csrmv64<<<fg_grid(n, 128, 32), 128, 0, s>>>(n, IA, JA, AA, P, Q, active);
-	return (int)cudaGetLastError();
+	return launch_csrmv<double, double, double, double>(n, IA, JA, AA, P, Q, active, s);
 }
 
 extern "C" int fg_csrmv32(int n, const int *IA, const int *JA, const float *AA, const float *P,
                           float *Q, const int *active, cudaStream_t s)
 {
-	k_csrmv32<4, float><<<fg_grid(4LL * n, 256, 32), 256, 0, s>>>(n, IA, JA, AA, P, Q, active);
-	return (int)cudaGetLastError();
+	return launch_csrmv<float, float, float, float>(n, IA, JA, AA, P, Q, active, s);
 }
 
 // ebemv.c:42-63 gathered per row: for each incident element (ascending),
@@ -157,12 +189,8 @@ extern "C" int fg_matvec(femgpu_transport *t, const double *P, double *Q, const 
 // with FP64 accumulation (op32 == 0) or FP32 values with FP32 accumulation.
 static int matvec_xf(femgpu_transport *t, const float *P, double *Q, const int *active, int op32)
 {
-	cudaStream_t s = t->stream;
-	if (op32) k_csrmv32<4, double><<<fg_grid(4LL * t->neq, 256, 32), 256, 0, s>>>(t->neq, t->IA, t->JA,
-		t->A32, P, Q, active);
-	else k_csrmv64_xf<4><<<fg_grid(4LL * t->neq, 256, 32), 256, 0, s>>>(t->neq, t->IA, t->JA, t->A, P, Q,
-		active);
-	return (int)cudaGetLastError();
+	if (op32) return launch_csrmv<float, float, float, double>(t->neq, t->IA, t->JA, t->A32, P, Q, active, t->stream);
+	return launch_csrmv<double, float, double, double>(t->neq, t->IA, t->JA, t->A, P, Q, active, t->stream);
 }
 
 // ============================================================ diagonal ====
