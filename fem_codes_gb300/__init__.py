@@ -167,6 +167,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_transport_last_times": [_vp, _vp],
         "femgpu_transport_write_vtu": [_vp, ctypes.c_char_p, _vp],
         "femgpu_csrmv_f64": [ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp],
+        "femgpu_csrmv_f64_fused": [ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_csrmv_f32": [ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp],
     }.items():
         f = getattr(L, name)

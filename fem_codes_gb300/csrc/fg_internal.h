@@ -211,6 +211,8 @@ int fg_csrmv64(int n, const int *IA, const int *JA, const double *AA, const doub
                double *Q, const int *active, cudaStream_t s);
 int fg_csrmv32(int n, const int *IA, const int *JA, const float *AA, const float *P,
                float *Q, const int *active, cudaStream_t s);
+int fg_csrmv64_fused(int n, const int *IA, const int *JA, const double *AA, const double *P,
+                     double *Q, const int *active, cudaStream_t s);
 int fg_diag_setup(femgpu_transport *t);
 int fg_precond(femgpu_transport *t, const double *p, double *z, const int *active);
 /* One restart cycle of the reference's left-preconditioned GMRES

@@ -26,6 +26,10 @@
 // so the FP64 product is bit-identical while no load is strided by the row
 // length.  A tile whose entries exceed MV_CAP is taken in runs of rows that
 // fit (a row longer than MV_CAP alone is gathered by its own thread).
+// FUSED: the row sums are fused multiply-adds q = fma(a, p, q) over staged
+// values and inputs (one FP64 operation per entry instead of two: on this
+// part the separately rounded form is bound by the FP64 pipe, the fused one
+// by HBM); the FGMRES operator, not bit-identical to csrmv.c.
 #define MV_ROWS 256
 #define MV_CAP 4096
 
@@ -39,15 +43,16 @@ template <> struct mv_ops<float> {
 	static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
 };
 
-template <typename TA, typename TP, typename TACC, typename TO>
+template <typename TA, typename TP, typename TACC, typename TO, bool FUSED>
 __global__ void __launch_bounds__(MV_ROWS) k_csrmv_tile(int n, const int *__restrict__ IA,
                                                         const int *__restrict__ JA, const TA *__restrict__ AA,
                                                         const TP *__restrict__ P, TO *__restrict__ Q,
                                                         const int *active)
 {
 	typedef mv_ops<TACC> op;
+	constexpr int CAP = FUSED ? MV_CAP / 2 : MV_CAP;
 	if (active && !*active) return;
-	__shared__ TACC prod[MV_CAP];
+	__shared__ TACC prod[MV_CAP];                         // FUSED: values [0, CAP), inputs [CAP, 2 CAP)
 	__shared__ int kpos[2];
 	const int tid = threadIdx.x;
 	const int r0 = blockIdx.x * MV_ROWS, r1 = min(r0 + MV_ROWS, n), i = r0 + tid;
@@ -58,12 +63,14 @@ __global__ void __launch_bounds__(MV_ROWS) k_csrmv_tile(int n, const int *__rest
 		if (i == rs) kpos[0] = kb;
 		__syncthreads();
 		const int k0 = kpos[0];
-		const int re = rs + __syncthreads_count(mine && i >= rs && ke - k0 <= MV_CAP);
-		if (re == rs) {                                   // a row longer than MV_CAP
+		const int re = rs + __syncthreads_count(mine && i >= rs && ke - k0 <= CAP);
+		if (re == rs) {                                   // a row longer than CAP
 			if (i == rs) {
 				TACC q = TACC(0);
-				for (int j = kb; j < ke; j++)
-					q = op::add(q, op::mul((TACC)__ldg(&AA[j]), (TACC)__ldg(&P[__ldg(&JA[j])])));
+				for (int j = kb; j < ke; j++) {
+					const TACC a = (TACC)__ldg(&AA[j]), x = (TACC)__ldg(&P[__ldg(&JA[j])]);
+					q = FUSED ? fma(a, x, q) : op::add(q, op::mul(a, x));
+				}
 				Q[i] = (TO)q;
 			}
 			rs = re + 1;
@@ -79,16 +86,30 @@ __global__ void __launch_bounds__(MV_ROWS) k_csrmv_tile(int n, const int *__rest
 			const int c0 = __ldcs(&JA[k]), c1 = __ldcs(&JA[k + MV_ROWS]);
 			const int c2 = __ldcs(&JA[k + 2 * MV_ROWS]), c3 = __ldcs(&JA[k + 3 * MV_ROWS]);
 			const TP p0 = __ldg(&P[c0]), p1 = __ldg(&P[c1]), p2 = __ldg(&P[c2]), p3 = __ldg(&P[c3]);
-			prod[k - k0] = op::mul((TACC)a0, (TACC)p0);
-			prod[k - k0 + MV_ROWS] = op::mul((TACC)a1, (TACC)p1);
-			prod[k - k0 + 2 * MV_ROWS] = op::mul((TACC)a2, (TACC)p2);
-			prod[k - k0 + 3 * MV_ROWS] = op::mul((TACC)a3, (TACC)p3);
+			if (FUSED) {
+				prod[k - k0] = (TACC)a0; prod[CAP + k - k0] = (TACC)p0;
+				prod[k - k0 + MV_ROWS] = (TACC)a1; prod[CAP + k - k0 + MV_ROWS] = (TACC)p1;
+				prod[k - k0 + 2 * MV_ROWS] = (TACC)a2; prod[CAP + k - k0 + 2 * MV_ROWS] = (TACC)p2;
+				prod[k - k0 + 3 * MV_ROWS] = (TACC)a3; prod[CAP + k - k0 + 3 * MV_ROWS] = (TACC)p3;
+			} else {
+				prod[k - k0] = op::mul((TACC)a0, (TACC)p0);
+				prod[k - k0 + MV_ROWS] = op::mul((TACC)a1, (TACC)p1);
+				prod[k - k0 + 2 * MV_ROWS] = op::mul((TACC)a2, (TACC)p2);
+				prod[k - k0 + 3 * MV_ROWS] = op::mul((TACC)a3, (TACC)p3);
+			}
 		}
-		for (; k < k1; k += MV_ROWS) prod[k - k0] = op::mul((TACC)__ldcs(&AA[k]), (TACC)__ldg(&P[__ldcs(&JA[k])]));
+		for (; k < k1; k += MV_ROWS) {
+			const TACC a = (TACC)__ldcs(&AA[k]), x = (TACC)__ldg(&P[__ldcs(&JA[k])]);
+			if (FUSED) { prod[k - k0] = a; prod[CAP + k - k0] = x; }
+			else prod[k - k0] = op::mul(a, x);
+		}
 		__syncthreads();
 		if (i >= rs && i < re) {
 			TACC q = TACC(0);
-			for (int j = kb - k0; j < ke - k0; j++) q = op::add(q, prod[j]);
+			if (FUSED)
+				for (int j = kb - k0; j < ke - k0; j++) q = fma(prod[j], prod[CAP + j], q);
+			else
+				for (int j = kb - k0; j < ke - k0; j++) q = op::add(q, prod[j]);
 			Q[i] = (TO)q;
 		}
 		__syncthreads();                                  // prod and kpos are reused by the next run
@@ -96,13 +117,20 @@ __global__ void __launch_bounds__(MV_ROWS) k_csrmv_tile(int n, const int *__rest
 	}
 }
 
-template <typename TA, typename TP, typename TACC, typename TO>
+template <typename TA, typename TP, typename TACC, typename TO, bool FUSED = false>
 static int launch_csrmv(int n, const int *IA, const int *JA, const TA *AA, const TP *P, TO *Q, const int *active,
                         cudaStream_t s)
 {
 	if (n <= 0) return 0;
-	k_csrmv_tile<TA, TP, TACC, TO><<<(n + MV_ROWS - 1) / MV_ROWS, MV_ROWS, 0, s>>>(n, IA, JA, AA, P, Q, active);
+	k_csrmv_tile<TA, TP, TACC, TO, FUSED><<<(n + MV_ROWS - 1) / MV_ROWS, MV_ROWS, 0, s>>>(n, IA, JA, AA, P, Q,
+	                                                                                     active);
 	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_csrmv64_fused(int n, const int *IA, const int *JA, const double *AA, const double *P,
+                                double *Q, const int *active, cudaStream_t s)
+{
+	return launch_csrmv<double, double, double, double, true>(n, IA, JA, AA, P, Q, active, s);
 }
 
 extern "C" int fg_csrmv64(int n, const int *IA, const int *JA, const double *AA, const double *P,
@@ -640,9 +668,15 @@ extern "C" int fg_kry_true_rho(const fg_krylov *k, const fg_linop *op, const dou
 }
 
 // ------------------------------------------- the transport context's view
+// The Krylov operator: FGMRES contexts with CSR storage apply the fused
+// product (their sweeps are the fused ones too); the reference's GMRES keeps
+// csrmv.c's rounding.
 static int tr_matvec(void *c, const double *p, double *q, const int *a)
 {
-	return fg_matvec((femgpu_transport *)c, p, q, a);
+	femgpu_transport *t = (femgpu_transport *)c;
+	if (t->o.solver == FEMGPU_FGMRES && t->o.scheme == FEMGPU_CSR)
+		return fg_csrmv64_fused(t->neq, t->IA, t->JA, t->A, p, q, a, t->stream);
+	return fg_matvec(t, p, q, a);
 }
 static int tr_precond(void *c, const double *p, double *z, const int *a)
 {

@@ -848,6 +848,14 @@ int femgpu_csrmv_f64(int n, const int *IA, const int *JA, const double *AA, cons
 	return 0;
 }
 
+int femgpu_csrmv_f64_fused(int n, const int *IA, const int *JA, const double *AA, const double *P, double *Q,
+		void *stream)
+{
+	if (n < 0 || !IA || !JA || !AA || !P || !Q) return FEMGPU_E_ARG;
+	KR(fg_csrmv64_fused(n, IA, JA, AA, P, Q, NULL, (cudaStream_t)stream));
+	return 0;
+}
+
 int femgpu_csrmv_f32(int n, const int *IA, const int *JA, const float *AA, const float *P, float *Q,
 		void *stream)
 {

@@ -527,6 +527,11 @@ int femgpu_csrmv_f64(int n, const int *IA, const int *JA, const double *AA,
 		const double *P, double *Q, void *stream);
 int femgpu_csrmv_f32(int n, const int *IA, const int *JA, const float *AA,
 		const float *P, float *Q, void *stream);
+/* The FP64 product as the FGMRES contexts apply it: each row's terms in
+ * column order as fused multiply-adds (one rounding per entry), so it is
+ * within rounding of, not bit-identical to, csrmv.c (femgpu_csrmv_f64 is). */
+int femgpu_csrmv_f64_fused(int n, const int *IA, const int *JA, const double *AA,
+		const double *P, double *Q, void *stream);
 
 /* Allocation-free residual norm.  No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc -- a host application that hands the

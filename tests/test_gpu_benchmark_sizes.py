@@ -28,6 +28,28 @@ def _rel(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
 
+def _check_fused_product(T, pat, A, P, Qref):
+    """The FGMRES operator (fused multiply-adds, one rounding per entry)
+    against csrmv.c's separately rounded sums: each row within
+    2 nnz_row eps of sum |a_ij p_j|."""
+    import ctypes
+    import torch
+    vp = ctypes.c_void_p
+    IAd, JAd, AAd = T.csr_dev()
+    Pd = torch.from_numpy(np.ascontiguousarray(P)).cuda()
+    Qd = torch.zeros_like(Pd)
+    torch.cuda.synchronize()
+    assert T._L.femgpu_csrmv_f64_fused(T.neq, vp(IAd), vp(JAd), vp(AAd), vp(Pd.data_ptr()), vp(Qd.data_ptr()),
+                                       None) == 0
+    torch.cuda.synchronize()
+    Qf = Qd.cpu().numpy()[:T.neq]
+    IA, JA = pat["IA"], pat["JA"]
+    rows = np.repeat(np.arange(T.neq), np.diff(IA))
+    mag = np.bincount(rows, weights=np.abs(A[:IA[-1]] * P[JA]), minlength=T.neq)
+    bound = 2.0 * np.diff(IA) * np.finfo(np.float64).eps * mag
+    assert np.all(np.abs(Qf - Qref[:T.neq]) <= bound), "fused CSR product"
+
+
 def test_transport_c2_structure_build_matvec_ilu0_bitexact(gpu_lib):
     import fem_codes_gb300 as fg
     m = structured_mesh(2048, 1024, perturb=0.2, seed=1234)
@@ -48,6 +70,7 @@ def test_transport_c2_structure_build_matvec_ilu0_bitexact(gpu_lib):
         assert np.array_equal(F, ref["Ffirst"]), "RHS"
         Q = T.ProductMatrixVector(ref["Pin"])
         assert np.array_equal(Q, ref["Qmv"]), "csrmv"
+        _check_fused_product(T, pat, A, ref["Pin"], ref["Qmv"])
         Fp = T.precond_setup(1)
         assert np.array_equal(Fp, ref["Fprec"]), "F := M^-1 F"
         Z = T.precond(ref["Pin"])
