@@ -34,7 +34,7 @@ OPTS = {
     "scheme": {"EBE": 0, "EDE": 1, "CSR": 2},
     "reorder": {"NOT": 0, "SYMRCM": 1},
     "precond": {"NOT": 0, "ILU0": 1, "DIAG": 2, "BLOCKDIAG": 3, "LEARNED": 4, "AMG": 5},
-    "shock": {"CAU": 0, "YZBETA": 1},
+    "shock": {"CAU": 0, "YZBETA": 1, "CAUDD": 2},
     "hshock": {"2SQRTAREA": 0, "SQRTAREA": 1, "OPTION1": 2, "OPTION2": 3},
     "precision": {"FP64": 0, "MIXED": 1, "MIXED_IR": 2},
     "solver": {"GMRES": 0, "PGMRES": 0, "FGMRES": 1},
@@ -56,6 +56,12 @@ class FemGpuError(RuntimeError):
         detail = _lib.femgpu_last_error().decode() if _lib is not None else ""
         super().__init__(f"{where}: {msg} ({code}) {detail}".strip())
         self.code = code
+
+
+class TransientOpts(ctypes.Structure):
+    _fields_ = [("stab", ctypes.c_int), ("alpha", ctypes.c_double), ("dt", ctypes.c_double),
+                ("final_time", ctypes.c_double), ("stop_norm", ctypes.c_int), ("max_corr", ctypes.c_int),
+                ("nonlin_tol", ctypes.c_double), ("steady_stop", ctypes.c_int), ("time_tol", ctypes.c_double)]
 
 
 class Opts(ctypes.Structure):
@@ -144,6 +150,9 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_mesh_read": [ctypes.c_char_p, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_mesh_side_types": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp],
         "femgpu_transport_set_sweep_wait": [_vp, ctypes.c_int],
+        "femgpu_transport_set_transient": [_vp, _vp],
+        "femgpu_transport_build_transient": [_vp, _vp, _vp, _vp, _vp],
+        "femgpu_transport_predictor": [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int],
         "femgpu_deck_transport_opts": [_vp, _vp],
         "femgpu_deck_euler_opts": [_vp, _vp],
         "femgpu_deck_ns_opts": [_vp, _vp],
@@ -621,6 +630,41 @@ class SSTransport:
         if rc < 0:
             raise FemGpuError(rc, "ilu_chain")
         return rc
+
+    # -- the transient driver (02_Transport_Equation/2D) --------------------
+    def set_transient(self, stab="SUPG", alpha=0.5, dt=1e-2, final_time=1.0, stop="ITERATION", max_corr=2,
+                      nonlin_tol=1e-3, steady="NOT", time_tol=1e-6):
+        """Switch to the transient driver: Build_M_K_R_SUPG / Build_M_K_R_DD
+        and Predictor_Old with the deck's StopMulticorrection (ITERATION |
+        NORM) and StopAtSteadyState (YES | NOT)."""
+        o = TransientOpts(stab={"SUPG": 0, "DD": 1}[stab.upper()], alpha=alpha, dt=dt, final_time=final_time,
+                          stop_norm={"ITERATION": 0, "NORM": 1}[stop.upper()], max_corr=int(max_corr),
+                          nonlin_tol=nonlin_tol, steady_stop={"NOT": 0, "YES": 1}[steady.upper()],
+                          time_tol=time_tol)
+        self._check(self._L.femgpu_transport_set_transient(self._h, ctypes.byref(o)), "set_transient")
+
+    def build_transient(self, u=None, a=None, want_matrix=False):
+        """One transient Build on (u, a): returns (R, storage values or None)."""
+        R = np.zeros(self.neq + 1)
+        A = np.zeros(self.storage_len()) if want_matrix else None
+        uu = None if u is None else _f64(u)
+        aa = None if a is None else _f64(a)
+        self._check(self._L.femgpu_transport_build_transient(self._h, _ptr(uu), _ptr(aa), _ptr(R), _ptr(A)),
+                    "build_transient")
+        return R, A
+
+    def predictor(self, u0, max_steps, iters_cap=16):
+        """Predictor_Old from u0: dict(u [steps, neq+1], t, ncorr, iters [steps, iters_cap])."""
+        u0 = _f64(u0)
+        uh = np.zeros((max_steps, self.neq + 1))
+        th = np.zeros(max_steps)
+        nc = np.zeros(max_steps, np.int32)
+        it = np.zeros((max_steps, iters_cap), np.int32)
+        n = self._L.femgpu_transport_predictor(self._h, _ptr(u0), int(max_steps), _ptr(uh), _ptr(th), _ptr(nc),
+                                               _ptr(it), int(iters_cap))
+        if n < 0:
+            raise FemGpuError(n, "predictor")
+        return dict(u=uh[:n], t=th[:n], ncorr=nc[:n], iters=it[:n])
 
     def set_sweep_wait(self, spins=-1):
         """Bound on a sweep warp's wait for its dependencies (-1: default);

@@ -20,6 +20,11 @@ struct BuildArgs {
 	double k, gamma, cbx, cby;
 	int nel, shock, hshock, beta_const, fsrc_zero;
 	double *ke, *fe;
+	// transient builds only
+	const double *du;             // the time derivative a (neq+1)
+	double adt;                   // Alpha * DeltaT
+	double *re;                   // per element and local row: load term, then three products
+	double *dold;                 // DD: the previous build's shock parameter per element
 };
 
 // Shock length scale: h_shock_2sqrtArea.c:3-8, h_shock_sqrtArea.c:3-61 (every
@@ -153,6 +158,258 @@ extern "C" int fg_build_elements(femgpu_transport *t)
 	return (int)cudaGetLastError();
 }
 
+// ------------------------------------------------------ transient builds ---
+// Shock capturing of the transient builds (02_Transport_Equation/2D/
+// 01_CommonFiles/CAU_ShockCapture.c:3-30, YZBeta_ShockCapture.c:3-24,
+// CAU_DD_ShockCapture.c:3-19): the residual carries the time derivative,
+// Ru = dueb + beta.grad u + gamma ueb - feb.  As in the steady form, the CAU
+// division by |grad u|^2 is only evaluated when |grad u| > 0 (the reference
+// discards its NaN otherwise).
+__device__ __forceinline__ double shock_capture_tr(int kind, double kx, double ky, double bx, double by,
+                                                   double g, double ue1, double ue2, double ue3,
+                                                   double ueb, double dueb, double feb, double y23, double y31,
+                                                   double y12, double x32, double x13, double x21,
+                                                   double invArea, double h)
+{
+	double BetaGradu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+	double Ru = dueb + BetaGradu + g*ueb - feb;
+	double G0 = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+	double G1 = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+	double nG = sqrt(G0*G0 + G1*G1);
+	if (kind == FEMGPU_SHOCK_YZBETA) {
+		double nRu = fabs(Ru), nu = fabs(ueb);
+		return (nu >= 1e-12 && nG >= 1e-12) ? 0.25*h*nRu/nG + 0.125*h*h*nRu/nu : 0.0;
+	}
+	if (kind == FEMGPU_SHOCK_CAUDD) return (nG > 1e-10) ? 0.5*h*fabs(Ru)/nG : 0.0;
+	if (!(nG > 0)) return 0.0;
+	const double third = 1./3.;
+	double bxp = BetaGradu*G0/(nG*nG), byp = BetaGradu*G1/(nG*nG);
+	double kp = bxp*bxp*kx + byp*byp*ky;
+	double nbp = sqrt(bxp*bxp + byp*byp);
+	double Pee = 0.5*h*nbp*nbp*nbp/kp;
+	if (third*Pee < 0.7) return 0.5*h*third*Pee*fabs(Ru)/nG;
+	return 0.5*h*0.7*fabs(Ru)/nG;
+}
+
+// Build_M_K_R_SUPG.c:36-180 (DD == false) and Build_M_K_R_DD.c:39-188
+// (DD == true), one thread per element: Ae = Me + Alpha*DeltaT*Ke to the
+// element buffer and, for the residual gather, per local row i the load term
+// and the three products me[i][j]*due[j] + ke[i][j]*ue[j] the reference
+// subtracts from R[lm[E][i]] in that order.  U and dU follow eval_U_dU.c
+// (prescribed nodes: upresc and 0).  The DD form keeps the shock parameter
+// of the previous build per element (cb = w cbtil + (1-w) cbtil_old, w = 1/2).
+template <bool DD>
+__global__ void __launch_bounds__(128) k_build_transient(BuildArgs a)
+{
+	const double third = 1.0/3.0, sixth = 1.0/6.0, twelfth = 1.0/12.0;
+	const double seventh = 1.0/7.0, three_twentieth = 3./20.0, nine_twentieth = 9./20.0,
+	             nine_forty_cents = 9./40.0, w = 0.5;
+	const double kx = a.k, ky = a.k, gamma = a.gamma;
+	for (int E = blockIdx.x * blockDim.x + threadIdx.x; E < a.nel; E += gridDim.x * blockDim.x) {
+		int J1 = __ldg(&a.vert[3*E]), J2 = __ldg(&a.vert[3*E+1]), J3 = __ldg(&a.vert[3*E+2]);
+		double X0 = __ldg(&a.x[J1]), X1 = __ldg(&a.x[J2]), X2 = __ldg(&a.x[J3]);
+		double Y0 = __ldg(&a.y[J1]), Y1 = __ldg(&a.y[J2]), Y2 = __ldg(&a.y[J3]);
+		double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
+		double x32 = X2 - X1, x13 = X0 - X2, x21 = X1 - X0;
+		double TwoA = x21*y31 - x13*y12, Area = 0.5*TwoA, invArea = 1.0/Area;
+		double bx, by;
+		if (a.beta_const) { bx = a.cbx; by = a.cby; }
+		else { bx = __ldg(&a.beta[2*E]); by = __ldg(&a.beta[2*E+1]); }
+		double fe1 = 0.0, fe2 = 0.0, fe3 = 0.0;
+		if (!a.fsrc_zero) { fe1 = __ldg(&a.fsrc[3*E]); fe2 = __ldg(&a.fsrc[3*E+1]); fe3 = __ldg(&a.fsrc[3*E+2]); }
+		double feb = third*(fe1+fe2+fe3);
+		int i1 = __ldg(&a.node_id[J1]), i2 = __ldg(&a.node_id[J2]), i3 = __ldg(&a.node_id[J3]);
+		double ue[3], due[3];
+		ue[0] = (i1 >= 0) ? a.u[i1] : __ldg(&a.upresc[J1]);
+		ue[1] = (i2 >= 0) ? a.u[i2] : __ldg(&a.upresc[J2]);
+		ue[2] = (i3 >= 0) ? a.u[i3] : __ldg(&a.upresc[J3]);
+		due[0] = (i1 >= 0) ? a.du[i1] : 0.0;
+		due[1] = (i2 >= 0) ? a.du[i2] : 0.0;
+		due[2] = (i3 >= 0) ? a.du[i3] : 0.0;
+		double ueb = third * (ue[0] + ue[1] + ue[2]);
+		double dueb = third * (due[0] + due[1] + due[2]);
+		double D12 = 0.25*invArea*((kx * y23 * y31) + (ky * x32 * x13));
+		double D13 = 0.25*invArea*((kx * y23 * y12) + (ky * x32 * x21));
+		double D23 = 0.25*invArea*((kx * y31 * y12) + (ky * x13 * x21));
+		double me[3][3], ke[3][3], f[3];
+		if (!DD) {
+			double h = sqrt(fabs(TwoA));
+			double norm = sqrt(bx*bx + by*by), tau = (norm > 0) ? 0.5*h/norm : 0.0;
+			double C11 = sixth*(bx*y23 + by*x32);
+			double C12 = sixth*(bx*y31 + by*x13);
+			double C13 = sixth*(bx*y12 + by*x21);
+			double R11 = sixth*(gamma*Area);
+			double R12 = twelfth*(gamma * Area);
+			double Cpg12 = 0.25*invArea*tau * (y23*(bx*bx*y31 + bx*by*x13) + x32*(bx*by*y31 + by*by*x13));
+			double Cpg13 = 0.25*invArea*tau * (y23*(bx*bx*y12 + bx*by*x21) + x32*(bx*by*y12 + by*by*x21));
+			double Cpg23 = 0.25*invArea*tau * (y31*(bx*bx*y12 + bx*by*x21) + x13*(bx*by*y12 + by*by*x21));
+			double Rpg11 = sixth*tau*gamma * (bx*y23 + by*x32);
+			double Rpg21 = sixth*tau*gamma * (bx*y31 + by*x13);
+			double Rpg31 = sixth*tau*gamma * (bx*y12 + by*x21);
+			double hs = h_shock(a.hshock, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
+			double Eu = shock_capture_tr(a.shock, kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb,
+			                             y23, y31, y12, x32, x13, x21, invArea, hs);
+			double Csc12 = Eu*0.25*invArea*(y23*y31 + x32*x13);
+			double Csc13 = Eu*0.25*invArea*(y23*y12 + x32*x21);
+			double Csc23 = Eu*0.25*invArea*(y31*y12 + x13*x21);
+			me[0][0] = sixth*Area  + tau*C11;
+			me[0][1] = twelfth*Area + tau*C11;
+			me[0][2] = twelfth*Area + tau*C11;
+			me[1][0] = twelfth*Area + tau*C12;
+			me[1][1] = sixth*Area  + tau*C12;
+			me[1][2] = twelfth*Area + tau*C12;
+			me[2][0] = twelfth*Area + tau*C13;
+			me[2][1] = twelfth*Area + tau*C13;
+			me[2][2] = sixth*Area  + tau*C13;
+			ke[0][0] = -(D12 + D13) + C11 - (Cpg12 + Cpg13) + R11 + Rpg11 - (Csc12 + Csc13);
+			ke[0][1] = D12 + C12 + Cpg12 + R12 + Rpg11 + Csc12;
+			ke[0][2] = D13 + C13 + Cpg13 + R12 + Rpg11 + Csc13;
+			ke[1][0] = D12 + C11 + Cpg12 + R12 + Rpg21 + Csc12;
+			ke[1][1] = -(D12 + D23) + C12 - (Cpg12 + Cpg23) + R11 + Rpg21 - (Csc12 + Csc23);
+			ke[1][2] = D23 + C13 + Cpg23 + R12 + Rpg21 + Csc23;
+			ke[2][0] = D13 + C11 + Cpg13 + R12 + Rpg31 + Csc13;
+			ke[2][1] = D23 + C12 + Cpg23 + R12 + Rpg31 + Csc23;
+			ke[2][2] = -(D13 + D23) + C13 - (Cpg13 + Cpg23) + R11 + Rpg31 - (Csc13 + Csc23);
+			f[0] = Area*twelfth*(2*fe1 +  fe2  +  fe3 ) + sixth*tau*(fe1+fe2+fe3)*(bx*y23 + by*x32);
+			f[1] = Area*twelfth*(  fe1 + 2*fe2 +  fe3 ) + sixth*tau*(fe1+fe2+fe3)*(bx*y31 + by*x13);
+			f[2] = Area*twelfth*(  fe1 +  fe2  + 2*fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y12 + by*x21);
+		} else {
+			double Mhh_1_12 = twelfth*Area, MhB_3_20 = three_twentieth*Area, MBh_3_20 = MhB_3_20;
+			double a1 = bx*y23 + by*x32, a2 = bx*y31 + by*x13, a3 = bx*y12 + by*x21;
+			double C12 = y23*y31 + x32*x13, C13 = y23*y12 + x32*x21, C23 = y31*y12 + x13*x21;
+			double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
+			double hs = h_shock(a.hshock, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
+			double cbtil = shock_capture_tr(a.shock, kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb,
+			                                y23, y31, y12, x32, x13, x21, invArea, hs);
+			double Eu = w*cbtil + (1-w)*a.dold[E];
+			a.dold[E] = cbtil;
+			double KDD12 = 0.25*Eu*invArea*C12, KDD13 = 0.25*Eu*invArea*C13, KDD23 = 0.25*Eu*invArea*C23;
+			double Khh[3][3], KhB[3], KBh[3];
+			Khh[0][0] = -(D12 + D13) + sixth*a1 + R11 -(KDD12 + KDD13);
+			Khh[0][1] = D12 + sixth*a2 + R12 + KDD12;
+			Khh[0][2] = D13 + sixth*a3 + R12 + KDD13;
+			Khh[1][0] = D12 + sixth*a1 + R12 + KDD12;
+			Khh[1][1] = -(D12 + D23) + sixth*a2 + R11 -(KDD12 + KDD23);
+			Khh[1][2] = D23 + sixth*a3 + R12 + KDD23;
+			Khh[2][0] = D13 + sixth*a1 + R12 + KDD13;
+			Khh[2][1] = D23 + sixth*a2 + R12 + KDD23;
+			Khh[2][2] = -(D13 + D23) + sixth*a3 + R11 -(KDD13 + KDD23);
+			KhB[0] = nine_twentieth*(0.5*a1 + a2 + a3) + three_twentieth*gamma*Area;
+			KhB[1] = nine_twentieth*(a1 + 0.5*a2 + a3) + three_twentieth*gamma*Area;
+			KhB[2] = nine_twentieth*(a1 + a2 + 0.5*a3) + three_twentieth*gamma*Area;
+			KBh[0] = nine_forty_cents*a1 + three_twentieth*gamma*Area;
+			KBh[1] = nine_forty_cents*a2 + three_twentieth*gamma*Area;
+			KBh[2] = nine_forty_cents*a3 + three_twentieth*gamma*Area;
+			double KBB = -9*nine_forty_cents*(D12+D13+D23) + seventh*three_twentieth*(a1+ a2+ a3)
+			             + 9*seventh*nine_forty_cents*Area - Eu*invArea*(C12 + C13 + C23)/360.;
+			double invKBB = 1.0/KBB;
+			double Fh[3];
+			Fh[0] = twelfth*Area*(2*fe1 + fe2 + fe3);
+			Fh[1] = twelfth*Area*(fe1 + 2*fe2 + fe3);
+			Fh[2] = twelfth*Area*(fe1 + fe2 + 2*fe3);
+			double FB = three_twentieth*Area*(fe1 + fe2 + fe3);
+			for (int i = 0; i < 3; i++) {
+				double m = Mhh_1_12 - invKBB*KhB[i]*MBh_3_20;
+				me[i][0] = m; me[i][1] = m; me[i][2] = m;
+				me[i][i] += Mhh_1_12;
+				f[i] = Fh[i] - invKBB*KhB[i]*FB;
+				for (int j = 0; j < 3; j++) ke[i][j] = Khh[i][j] - invKBB*KhB[i]*KBh[j];
+			}
+		}
+		double *Ae = a.ke + 9LL*E, *re = a.re + 12LL*E;
+		for (int i = 0; i < 3; i++) {
+			re[4*i] = f[i];
+			for (int j = 0; j < 3; j++) {
+				Ae[3*i + j] = me[i][j] + a.adt*ke[i][j];
+				re[4*i + 1 + j] = me[i][j]*due[j] + ke[i][j]*ue[j];
+			}
+		}
+	}
+}
+
+extern "C" int fg_build_transient(femgpu_transport *t, int dd, double adt)
+{
+	BuildArgs a;
+	a.x = t->x; a.y = t->y; a.u = t->u; a.upresc = t->upresc; a.beta = t->beta; a.fsrc = t->fsrc;
+	a.vert = t->vert; a.node_id = t->node_id;
+	a.k = t->k; a.gamma = t->gamma; a.cbx = t->cbx; a.cby = t->cby;
+	a.nel = t->nel; a.shock = t->o.shock; a.hshock = t->o.hshock;
+	a.beta_const = t->beta_const; a.fsrc_zero = t->fsrc_zero;
+	a.ke = (t->o.scheme == FEMGPU_EBE) ? t->A : t->ke;
+	a.fe = NULL;
+	a.du = t->du; a.adt = adt; a.re = t->re; a.dold = t->dold;
+	if (dd) k_build_transient<true><<<fg_grid(t->nel, 128, 32), 128, 0, t->stream>>>(a);
+	else k_build_transient<false><<<fg_grid(t->nel, 128, 32), 128, 0, t->stream>>>(a);
+	return (int)cudaGetLastError();
+}
+
+// The transient residual gathered per equation: for each incident element in
+// ascending order, R += load term, then R -= each of the three products
+// (the reference's scatter order); R[neq] = 0.
+__global__ void k_gather_R(int neq, const int *__restrict__ ri_ptr, const int *__restrict__ ri,
+                           const double *__restrict__ re, double *R)
+{
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I <= neq; I += gridDim.x * blockDim.x) {
+		double r = 0.0;
+		if (I < neq) {
+			for (int q = ri_ptr[I]; q < ri_ptr[I + 1]; q++) {
+				int code = __ldg(&ri[q]), e = code / 3, aa = code - 3 * e;
+				const double *p = re + 12LL * e + 4 * aa;
+				r += __ldg(&p[0]);
+				r -= __ldg(&p[1]);
+				r -= __ldg(&p[2]);
+				r -= __ldg(&p[3]);
+			}
+		}
+		R[I] = r;
+	}
+}
+
+// Predictor_Old.c:75-80: u_old = u, u += ((1 - alpha) dt) a, a = 0 ...
+__global__ void k_tr_predict(double *u, double *a, double *uold, int n, double c)
+{
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < n; I += gridDim.x * blockDim.x) {
+		double ui = u[I];
+		uold[I] = ui;
+		u[I] = ui + c*a[I];
+		a[I] = 0.0;
+	}
+}
+
+// ... and :124-125 (daxpy): a += 1*Da, u += (alpha dt) Da.
+__global__ void k_tr_correct(double *u, double *a, const double *Da, int n, double c)
+{
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < n; I += gridDim.x * blockDim.x) {
+		double d = Da[I];
+		a[I] = a[I] + 1.0*d;
+		u[I] = u[I] + c*d;
+	}
+}
+
+// Criteria.c:52-53: diff = u - u_old (into Da, free between steps).
+__global__ void k_tr_diff(const double *u, const double *uold, double *d, int n)
+{
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < n; I += gridDim.x * blockDim.x) d[I] = u[I] - uold[I];
+}
+
+extern "C" int fg_tr_diff(femgpu_transport *t)
+{
+	k_tr_diff<<<fg_grid(t->neq), FG_TPB, 0, t->stream>>>(t->u, t->uold, t->Da, t->neq);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_tr_predict(femgpu_transport *t, double c)
+{
+	k_tr_predict<<<fg_grid(t->neq), FG_TPB, 0, t->stream>>>(t->u, t->du, t->uold, t->neq, c);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_tr_correct(femgpu_transport *t, double c)
+{
+	k_tr_correct<<<fg_grid(t->neq), FG_TPB, 0, t->stream>>>(t->u, t->du, t->Da, t->neq, c);
+	return (int)cudaGetLastError();
+}
+
 // ------------------------------------------------------------ assembly ---
 #define FG_ROWCAP 32
 
@@ -194,7 +451,7 @@ __global__ void k_assemble_csr(int neq, int nnz, const int *IA, const int *sbe, 
 			}
 		}
 		for (int q = 0; q < len; q++) AA[base + q] = acc[q];
-		F[I] = gather_F(I, ri_ptr, ri, ke, fe, vert, node_type, upresc);
+		if (F) F[I] = gather_F(I, ri_ptr, ri, ke, fe, vert, node_type, upresc);
 	}
 	if (blockIdx.x == 0 && threadIdx.x == 0) AA[nnz] = 0.0;
 }
@@ -227,6 +484,22 @@ __global__ void k_assemble_F(int neq, const int *ri_ptr, const int *ri, const do
 {
 	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < neq; I += gridDim.x * blockDim.x)
 		F[I] = gather_F(I, ri_ptr, ri, ke, fe, vert, node_type, upresc);
+}
+
+// Storage assembly of the transient element matrices (the same gathers as
+// the steady build) and the residual gather into F.
+extern "C" int fg_assemble_transient(femgpu_transport *t)
+{
+	cudaStream_t s = t->stream;
+	int neq = t->neq;
+	if (t->o.scheme == FEMGPU_CSR)
+		k_assemble_csr<<<fg_grid(neq, 128, 32), 128, 0, s>>>(neq, t->nnz, t->IA, t->sbe, t->ri_ptr,
+			t->ri, t->ke, NULL, t->vert, t->node_type, t->upresc, t->A, NULL, &t->st->err);
+	else if (t->o.scheme == FEMGPU_EDE)
+		k_assemble_ede<<<fg_grid(t->nedge + 1LL), FG_TPB, 0, s>>>(t->nedge, t->ec_ptr, t->ec, t->order,
+			t->ke, t->A);
+	k_gather_R<<<fg_grid(neq + 1LL), FG_TPB, 0, s>>>(neq, t->ri_ptr, t->ri, t->re, t->F);
+	return (int)cudaGetLastError();
 }
 
 extern "C" int fg_assemble(femgpu_transport *t)

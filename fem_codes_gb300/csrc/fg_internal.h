@@ -170,6 +170,14 @@ struct femgpu_transport {
 	fg_ilu_sweeps sweeps;
 	int sweep_wait1;                /* 1 + dependency-wait bound; 0: default */
 
+	/* transient driver (femgpu_transport_set_transient) */
+	int transient;
+	femgpu_transient_opts tr;
+	double *du;                     /* the time derivative a (neq+1)         */
+	double *re;                     /* per element: load term + 3 products x3 */
+	double *dold;                   /* DD: previous shock parameter per elem */
+	double *uold, *Da;              /* predictor vectors (neq+1)             */
+
 	/* Krylov workspace */
 	int kmax;
 	size_t ldv;
@@ -204,6 +212,11 @@ int fg_compute_lm(femgpu_transport *t);                      /* lm from ids   */
 /* build.cu */
 int fg_build_elements(femgpu_transport *t);                  /* ke / A, fe    */
 int fg_assemble(femgpu_transport *t);                        /* A (CSR/EDE), F */
+int fg_build_transient(femgpu_transport *t, int dd, double adt);   /* Ae, re   */
+int fg_assemble_transient(femgpu_transport *t);              /* A, R -> F     */
+int fg_tr_predict(femgpu_transport *t, double c);            /* uold, u, a    */
+int fg_tr_correct(femgpu_transport *t, double c);            /* a, u += Da    */
+int fg_tr_diff(femgpu_transport *t);                         /* Da = u - uold */
 
 /* linalg.cu */
 int fg_matvec(femgpu_transport *t, const double *P, double *Q, const int *active);

@@ -30,6 +30,8 @@ int fgh_levels(int n, const int *IA, const int *JA, int lower, int *rows, int **
                int *ntask, int *nlev);
 void fgh_set_error(const char *fmt, ...);
 int fgh_dmalloc(void **p, size_t bytes);
+struct femgpu_transport;
+int fgh_transport_gmres(struct femgpu_transport *t, const double *B, double *X, int *iters);
 
 /* Krylov workspace (fg_internal.h fg_krylov) for n unknowns and kmax basis
  * vectors; zmode 0: no FGMRES Z, 1: FP64 Z, 2: FP32 Z. */

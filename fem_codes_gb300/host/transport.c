@@ -306,7 +306,7 @@ void femgpu_transport_destroy(femgpu_transport *t)
 		t->lm, t->ri_ptr, t->ri, t->IA, t->JA, t->sbe, t->diag, t->lm2, t->order, t->ec_ptr,
 		t->ec, t->e2_ptr, t->e2, t->A, t->ke, t->fe, t->A32, t->u, t->F, t->F0, t->invDiag,
 		t->invDiag32, t->ilu.LU, t->ilu.Dinv, t->V, t->H, t->cs, t->sn, t->ge, t->gy, t->w2,
-		t->Z, t->Z32, t->xr, t->dr, t->partials, t->st };
+		t->Z, t->Z32, t->xr, t->dr, t->partials, t->st, t->du, t->uold, t->Da, t->re, t->dold };
 	for (i = 0; i < (int)(sizeof ptrs / sizeof ptrs[0]); i++) if (ptrs[i]) cudaFree(ptrs[i]);
 	if (t->o.precond == FEMGPU_PREC_ILU0 || t->o.precond == FEMGPU_PREC_LEARNED) fg_ilu_free(t);
 	if (t->st_host) cudaFreeHost(t->st_host);
@@ -676,6 +676,15 @@ int femgpu_transport_krylov_pairs(femgpu_transport *t, int max, double *V, doubl
 	}
 	CK(cudaStreamSynchronize(t->stream));
 	return m;
+}
+
+static int gmres(femgpu_transport *t, const double *B, double *X, int *iters);
+
+/* The context's solver on device vectors (X := solve(B)), for the drivers
+ * built on a transport context (the transient time loop). */
+int fgh_transport_gmres(femgpu_transport *t, const double *B, double *X, int *iters)
+{
+	return gmres(t, B, X, iters);
 }
 
 static int gmres(femgpu_transport *t, const double *B, double *X, int *iters)

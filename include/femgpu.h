@@ -47,7 +47,8 @@ enum femgpu_precond  { FEMGPU_PREC_NOT = 0, FEMGPU_PREC_ILU0 = 1, FEMGPU_PREC_DI
                        FEMGPU_PREC_BLOCKDIAG = 3, /* Euler: nodal 4x4 blocks            */
                        FEMGPU_PREC_LEARNED = 4,   /* graph network, ILU(0) fallback    */
                        FEMGPU_PREC_AMG = 5        /* DPA AMG V-cycle (femgpu_amg)      */ };
-enum femgpu_shock    { FEMGPU_SHOCK_CAU = 0, FEMGPU_SHOCK_YZBETA = 1 };
+enum femgpu_shock    { FEMGPU_SHOCK_CAU = 0, FEMGPU_SHOCK_YZBETA = 1,
+                       FEMGPU_SHOCK_CAUDD = 2      /* transient DD builds only          */ };
 enum femgpu_hshock   { FEMGPU_H_2SQRTAREA = 0, FEMGPU_H_SQRTAREA = 1,
                        FEMGPU_H_OPTION1 = 2, FEMGPU_H_OPTION2 = 3 };
 /* Arithmetic of the solve (FGMRES only): FP64 throughout (the reference's);
@@ -212,6 +213,45 @@ int femgpu_transport_solve_bx(femgpu_transport *ctx, const double *B_host, doubl
  * u_hist [npicard*(neq+1)] and iters [npicard] receive each iterate (NULL
  * skips). Returns the number of Picard iterations run (> 0) or an error. */
 int femgpu_transport_process(femgpu_transport *ctx, int npicard, double *u_hist, int *iters);
+
+/* ---- transient scalar transport (02_Transport_Equation/2D) ----------------
+ * A transport context switched to the transient driver: its Build is
+ * Build_M_K_R_SUPG (Build_M_K_R_SUPG.c:6-183) or Build_M_K_R_DD
+ * (Build_M_K_R_DD.c:6-191, with its per-element shock-parameter state) --
+ * the storage gets Ae = Me + Alpha*DeltaT*Ke and F the residual
+ * R = F - Me a - Ke u -- and its time loop is Predictor_Old
+ * (Time_Integration/Predictor_Old.c:3-148) with the stop criteria of
+ * Criteria.c.  The context's other options (storage, reordering,
+ * preconditioner NOT / Diag / ILU0, solver, shock CAU / YZBETA / CAUDD,
+ * h_shock 2sqrtArea / Option1 / Option2) are the deck's as for the steady
+ * driver. */
+enum femgpu_stab { FEMGPU_STAB_SUPG = 0, FEMGPU_STAB_DD = 1 };
+typedef struct femgpu_transient_opts {
+	int stab;              /* StabilizationForm                                  */
+	double alpha, dt;      /* Alpha, DeltaT                                      */
+	double final_time;     /* FinalTime                                          */
+	int stop_norm;         /* StopMulticorrection: 0 ITERATION, 1 NORM           */
+	int max_corr;          /* NonLinearMaxIter                                   */
+	double nonlin_tol;     /* NonLinearTolerance (NORM)                          */
+	int steady_stop;       /* StopAtSteadyState: 1 YES, 0 NOT                    */
+	double time_tol;       /* TimeIntegrationTolerance (YES)                     */
+} femgpu_transient_opts;
+int femgpu_transport_set_transient(femgpu_transport *ctx, const femgpu_transient_opts *o);
+/* One transient Build on the state (u, a) (host [neq+1]; NULL: the context's):
+ * R_host [neq+1] the residual, A_host the storage values (as
+ * femgpu_transport_build); each call advances the DD state. */
+int femgpu_transport_build_transient(femgpu_transport *ctx, const double *u_host, const double *a_host,
+		double *R_host, double *A_host);
+/* Predictor_Old from u0_host [neq+1] (the problem's InitialSolution; a = 0,
+ * a fresh DD state): per step u += (1-alpha) dt a, a = 0, then corrections
+ * Build -> precond_setup -> solve(R, Da) -> a += Da, u += alpha dt Da until
+ * the multicorrection criterion holds, until the time criterion holds or
+ * max_steps steps.  u_hist [max_steps*(neq+1)], t_hist [max_steps],
+ * ncorr [max_steps] (corrections per step) and iters [max_steps*iters_cap]
+ * (GMRES iterations of each correction) are filled when non-NULL.  Returns
+ * the number of steps run or an error. */
+int femgpu_transport_predictor(femgpu_transport *ctx, const double *u0_host, int max_steps, double *u_hist,
+		double *t_hist, int *ncorr, int *iters, int iters_cap);
 
 /* Paraview_Output (Paraview_Output.c:5-85): writes the VTU file the
  * reference writes for a solution -- ASCII UnstructuredGrid with the nodal

@@ -24,9 +24,10 @@ def pytest_configure(config):
 def golden_names():
     """Steady-transport golden cases (blk_* hold block operators, eul_* the
     Euler build and predictor, ns_* the Navier-Stokes build and Newton,
-    amg_* the AMG hierarchy and V-cycle, vtu_* the reference's VTU output)."""
+    amg_* the AMG hierarchy and V-cycle, vtu_* the reference's VTU output,
+    tt_* the transient transport builds and time loop)."""
     return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                  if not os.path.basename(f).startswith(("amg_", "blk_", "eul_", "ns_", "vtu_")))
+                  if not os.path.basename(f).startswith(("amg_", "blk_", "eul_", "ns_", "vtu_", "tt_")))
 
 
 def load_golden(name):

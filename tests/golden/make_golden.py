@@ -4,8 +4,10 @@ transport solve (libfemref.so, oracle/ref_harness.c), the multi-dof EBE
 operators (libfemref_*_blk.so, oracle/ref_block_harness.c), the 2D Euler
 build and predictor (libfemref_euler.so, oracle/ref_euler_harness.c) and the
 steady Navier-Stokes VMS build and damped Newton (libfemref_ns.so,
-oracle/ref_ns_harness.c) and the double-pairwise AMG preconditioner
-(libfemref_amg.so, oracle/ref_amg_harness.c).
+oracle/ref_ns_harness.c), the double-pairwise AMG preconditioner
+(libfemref_amg.so, oracle/ref_amg_harness.c) and the transient transport
+builds and Predictor_Old (libfemref_transient.so,
+oracle/ref_transient_harness.c).
 
 Usage:  python tests/golden/make_golden.py [case ...]   (writes tests/golden/*.npz;
         with case names, only those steady-transport cases)
@@ -506,6 +508,99 @@ def main_vtu():
     print(f"vtu_skew16_rcm: {len(data)} bytes")
 
 
+# Transient transport (02_Transport_Equation/2D): problem -> (harness code, domain side, origin)
+TT_PROBLEMS = {"CONE": (0, 10.0, 0.0), "CONE2": (1, 10.0, -5.0), "CARTOLA": (2, 1.0, 0.0), "PUDIM": (3, 2.0, -1.0)}
+TT_BASE = dict(reord="NOT", precond="NOT", stab="SUPG", shock="CAU", hshock="2sqrtArea", stopmc="ITERATION",
+               steady="NOT", alpha=0.5, dt=0.1, final=1.0, nonlin_tol=1e-3, max_corr=2, time_tol=1e-6,
+               stab_tol=1e-6, kmax=30, lmax=20, tol=1e-8, maxsteps=12)
+TT_CASES = {
+    "tt_cone16_csr_ilu0_supg_rcm": dict(problem="CONE", n=16, scheme="CSR", reord="SYMRCM", precond="ILU0"),
+    "tt_cartola16_csr_ilu0_supg": dict(problem="CARTOLA", n=16, scheme="CSR", precond="ILU0", hshock="Option1",
+                                       stopmc="NORM", max_corr=4, dt=0.01, final=0.1),
+    "tt_cone2_16_csr_ilu0_dd_caudd": dict(problem="CONE2", n=16, scheme="CSR", reord="SYMRCM", precond="ILU0",
+                                          stab="DD", shock="CAUDD", hshock="Option1", dt=0.05, final=0.5),
+    "tt_cone16_ebe_diag_dd_caudd": dict(problem="CONE", n=16, scheme="EBE", precond="Diag", stab="DD",
+                                        shock="CAUDD", stopmc="NORM", max_corr=4),
+    "tt_pudim16_ede_not_supg_yzbeta": dict(problem="PUDIM", n=16, scheme="EDE", shock="YZBeta", hshock="Option2",
+                                           steady="YES", time_tol=1e-3, dt=0.05),
+    "tt_cone2_12_csr_diag_dd_cau": dict(problem="CONE2", n=12, scheme="CSR", precond="Diag", stab="DD",
+                                        shock="CAU", dt=0.05, final=0.5),
+}
+
+
+def transient_lib():
+    lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libfemref_transient.so"))
+    f = lib.ref_transient_run
+    f.restype = ctypes.c_int
+    s, d, i = ctypes.c_char_p, ctypes.c_double, ctypes.c_int
+    f.argtypes = [i, _dp, _dp, _ip, i, _ip, i, s, s, s, s, s, s, s, s, d, d, d, d, i, d, d, i, i, d,
+                  _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp,
+                  i, _dp, _dp, _ip, _ip]
+    return lib
+
+
+def transient_mesh(problem, n):
+    _, side, origin = TT_PROBLEMS[problem]
+    # PUDIM's initial data sits on the line x = 0, which only the unperturbed mesh holds
+    m = structured_mesh(n, n, lx=side, ly=side, perturb=0.0 if problem == "PUDIM" else 0.2, seed=1234)
+    m.x = m.x + origin
+    m.y = m.y + origin
+    bnd = (np.isclose(m.x, origin) | np.isclose(m.x, origin + side) | np.isclose(m.y, origin)
+           | np.isclose(m.y, origin + side))
+    return m, np.where(bnd, 0, 1).astype(np.int32)
+
+
+def run_transient(lib, name, case):
+    c = dict(TT_BASE)
+    c.update(case)
+    m, ntype = transient_mesh(c["problem"], c["n"])
+    nn, ne = m.nnodes, m.nel
+    neq = int((ntype == 1).sum())
+    cap = 16 * (nn + ne) + 16
+    info = np.zeros(4, np.int32)
+    node_id = np.zeros(nn, np.int32)
+    beta, fsrc, upresc = np.zeros(2 * ne), np.zeros(3 * ne), np.zeros(nn)
+    u0 = np.zeros(neq + 1)
+    IA, JA, sbe, order = (np.zeros(cap, np.int32) for _ in range(4))
+    rng = np.random.default_rng(7)
+    ub = rng.uniform(-0.5, 1.5, neq + 1)
+    dub = rng.uniform(-1.0, 1.0, neq + 1)
+    ub[neq] = dub[neq] = 0.0
+    A1, A2 = np.zeros(cap), np.zeros(cap)
+    R1, R2 = np.zeros(neq + 1), np.zeros(neq + 1)
+    ms = c["maxsteps"]
+    uh, th = np.zeros(ms * (neq + 1)), np.zeros(ms)
+    nc, its = np.zeros(ms, np.int32), np.zeros(ms * 64, np.int32)
+    e = lambda v: v.encode()
+    steps = lib.ref_transient_run(
+        nn, m.x, m.y, ntype, ne, np.ascontiguousarray(m.vert.reshape(-1), np.int32), TT_PROBLEMS[c["problem"]][0],
+        e(c["scheme"]), e(c["reord"]), e(c["precond"]), e(c["stab"]), e(c["shock"]), e(c["hshock"]),
+        e(c["stopmc"]), e(c["steady"]), c["alpha"], c["dt"], c["final"], c["nonlin_tol"], c["max_corr"],
+        c["time_tol"], c["stab_tol"], c["kmax"], c["lmax"], c["tol"], info, node_id, beta, fsrc, upresc, u0,
+        IA, JA, sbe, order, ub, dub, A1, R1, A2, R2, ms, uh, th, nc, its)
+    neq_r, nnz, nedge = int(info[0]), int(info[1]), int(info[2])
+    assert neq_r == neq
+    nA = {"CSR": nnz + 1, "EDE": 4 * (nedge + 1), "EBE": 9 * ne}[c["scheme"]]
+    out = dict(x=m.x, y=m.y, vert=m.vert, node_type=ntype, neq=neq, nnz=nnz, nedge=nedge, node_id=node_id,
+               beta=beta.reshape(ne, 2), fsrc=fsrc.reshape(ne, 3), upresc=upresc, u0=u0, ub=ub, dub=dub,
+               A1=A1[:nA], R1=R1, A2=A2[:nA], R2=R2, steps=steps, uhist=uh.reshape(ms, neq + 1)[:steps],
+               thist=th[:steps], ncorr=nc[:steps], iters=its.reshape(ms, 64)[:steps],
+               meta=np.array(repr(c)))
+    if c["scheme"] == "CSR":
+        out.update(IA=IA[:neq + 1], JA=JA[:nnz], sbe=sbe[:9 * ne].reshape(ne, 9))
+    elif c["scheme"] == "EDE":
+        out.update(lm2=JA[:2 * nedge].reshape(nedge, 2), ebe=sbe[:3 * ne].reshape(ne, 3),
+                   order=order[:3 * ne].reshape(ne, 3))
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(f"{name}: neq={neq} steps={steps} ncorr={list(nc[:steps])} iters={list(its.reshape(ms, 64)[:steps, 0])}")
+
+
+def main_transient():
+    lib = transient_lib()
+    for name, case in TT_CASES.items():
+        run_transient(lib, name, case)
+
+
 def main(only=()):
     """Every fixture, or (names given on the command line) only those
     steady-transport cases ("euler": only the Euler cases)."""
@@ -518,7 +613,11 @@ def main(only=()):
     if only == ("vtu",):
         main_vtu()
         return
+    if only == ("transient",):
+        main_transient()
+        return
     if not only:
+        main_transient()
         main_vtu()
         main_amg()
         main_ns()
