@@ -61,7 +61,8 @@ class FemGpuError(RuntimeError):
 class TransientOpts(ctypes.Structure):
     _fields_ = [("stab", ctypes.c_int), ("alpha", ctypes.c_double), ("dt", ctypes.c_double),
                 ("final_time", ctypes.c_double), ("stop_norm", ctypes.c_int), ("max_corr", ctypes.c_int),
-                ("nonlin_tol", ctypes.c_double), ("steady_stop", ctypes.c_int), ("time_tol", ctypes.c_double)]
+                ("nonlin_tol", ctypes.c_double), ("steady_stop", ctypes.c_int), ("time_tol", ctypes.c_double),
+                ("method", ctypes.c_int)]
 
 
 class Opts(ctypes.Structure):
@@ -633,14 +634,17 @@ class SSTransport:
 
     # -- the transient driver (02_Transport_Equation/2D) --------------------
     def set_transient(self, stab="SUPG", alpha=0.5, dt=1e-2, final_time=1.0, stop="ITERATION", max_corr=2,
-                      nonlin_tol=1e-3, steady="NOT", time_tol=1e-6):
+                      nonlin_tol=1e-3, steady="NOT", time_tol=1e-6, method="Predictor1"):
         """Switch to the transient driver: Build_M_K_R_SUPG / Build_M_K_R_DD
-        and Predictor_Old with the deck's StopMulticorrection (ITERATION |
-        NORM) and StopAtSteadyState (YES | NOT)."""
+        and the deck's TimeIntegration (Predictor1 | Predictor1_BDF |
+        Predictor1_TRBDF2) with its StopMulticorrection (ITERATION | NORM) and
+        StopAtSteadyState (YES | NOT)."""
         o = TransientOpts(stab={"SUPG": 0, "DD": 1}[stab.upper()], alpha=alpha, dt=dt, final_time=final_time,
                           stop_norm={"ITERATION": 0, "NORM": 1}[stop.upper()], max_corr=int(max_corr),
                           nonlin_tol=nonlin_tol, steady_stop={"NOT": 0, "YES": 1}[steady.upper()],
-                          time_tol=time_tol)
+                          time_tol=time_tol,
+                          method={"PREDICTOR1": 0, "PREDICTOR1_BDF": 1, "PREDICTOR1_TRBDF2": 2}[method.upper()])
+        self._stages = 2 if method.upper() == "PREDICTOR1_TRBDF2" else 1
         self._check(self._L.femgpu_transport_set_transient(self._h, ctypes.byref(o)), "set_transient")
 
     def build_transient(self, u=None, a=None, want_matrix=False):
@@ -654,17 +658,20 @@ class SSTransport:
         return R, A
 
     def predictor(self, u0, max_steps, iters_cap=16):
-        """Predictor_Old from u0: dict(u [steps, neq+1], t, ncorr, iters [steps, iters_cap])."""
+        """The time loop from u0: dict(u [stages, neq+1], t [steps], ncorr
+        [stages], iters [stages, iters_cap]) -- a stage is one multicorrection
+        loop, two per TRBDF2 step."""
         u0 = _f64(u0)
-        uh = np.zeros((max_steps, self.neq + 1))
+        S = getattr(self, "_stages", 1)
+        uh = np.zeros((S * max_steps, self.neq + 1))
         th = np.zeros(max_steps)
-        nc = np.zeros(max_steps, np.int32)
-        it = np.zeros((max_steps, iters_cap), np.int32)
+        nc = np.zeros(S * max_steps, np.int32)
+        it = np.zeros((S * max_steps, iters_cap), np.int32)
         n = self._L.femgpu_transport_predictor(self._h, _ptr(u0), int(max_steps), _ptr(uh), _ptr(th), _ptr(nc),
                                                _ptr(it), int(iters_cap))
         if n < 0:
             raise FemGpuError(n, "predictor")
-        return dict(u=uh[:n], t=th[:n], ncorr=nc[:n], iters=it[:n])
+        return dict(u=uh[:S * n], t=th[:n], ncorr=nc[:S * n], iters=it[:S * n])
 
     def set_sweep_wait(self, spins=-1):
         """Bound on a sweep warp's wait for its dependencies (-1: default);

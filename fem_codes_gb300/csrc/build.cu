@@ -386,6 +386,37 @@ __global__ void k_tr_correct(double *u, double *a, const double *Da, int n, doub
 	}
 }
 
+// Predictor_Old_TRBDF2.c:57-58 (daxpy): y += c x, then x = 0.
+__global__ void k_tr_axpy_zero(double *y, double *x, int n, double c)
+{
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < n; I += gridDim.x * blockDim.x) {
+		y[I] = y[I] + c*x[I];
+		x[I] = 0.0;
+	}
+}
+
+// Predictor_Old_BDF.c:111-115 / Predictor_Old_TRBDF2.c:101-105:
+// u = cp p - cq q, a = 0 (u may be p).
+__global__ void k_tr_lin(double *u, const double *p, const double *q, double *a, int n, double cp, double cq)
+{
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < n; I += gridDim.x * blockDim.x) {
+		u[I] = cp*p[I] - cq*q[I];
+		a[I] = 0.0;
+	}
+}
+
+extern "C" int fg_tr_axpy_zero(femgpu_transport *t, double c)
+{
+	k_tr_axpy_zero<<<fg_grid(t->neq), FG_TPB, 0, t->stream>>>(t->u, t->du, t->neq, c);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_tr_lin(femgpu_transport *t, const double *p, const double *q, double cp, double cq)
+{
+	k_tr_lin<<<fg_grid(t->neq), FG_TPB, 0, t->stream>>>(t->u, p, q, t->du, t->neq, cp, cq);
+	return (int)cudaGetLastError();
+}
+
 // Criteria.c:52-53: diff = u - u_old (into Da, free between steps).
 __global__ void k_tr_diff(const double *u, const double *uold, double *d, int n)
 {

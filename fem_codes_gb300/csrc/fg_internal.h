@@ -176,7 +176,7 @@ struct femgpu_transport {
 	double *du;                     /* the time derivative a (neq+1)         */
 	double *re;                     /* per element: load term + 3 products x3 */
 	double *dold;                   /* DD: previous shock parameter per elem */
-	double *uold, *Da;              /* predictor vectors (neq+1)             */
+	double *uold, *Da, *u1, *u2;    /* predictor vectors (neq+1)             */
 
 	/* Krylov workspace */
 	int kmax;
@@ -217,6 +217,8 @@ int fg_assemble_transient(femgpu_transport *t);              /* A, R -> F     */
 int fg_tr_predict(femgpu_transport *t, double c);            /* uold, u, a    */
 int fg_tr_correct(femgpu_transport *t, double c);            /* a, u += Da    */
 int fg_tr_diff(femgpu_transport *t);                         /* Da = u - uold */
+int fg_tr_axpy_zero(femgpu_transport *t, double c);          /* u += c a, a=0 */
+int fg_tr_lin(femgpu_transport *t, const double *p, const double *q, double cp, double cq); /* u=cp p-cq q */
 
 /* linalg.cu */
 int fg_matvec(femgpu_transport *t, const double *P, double *Q, const int *active);

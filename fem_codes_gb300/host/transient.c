@@ -104,58 +104,161 @@ static int stop_corr(const femgpu_transient_opts *o, double norm_a, double norm_
 	return i >= o->max_corr;
 }
 
+/* The loop's bookkeeping: the reference's Parameters->Alpha / DeltaT (the
+ * SUPG build's Alpha*DeltaT) and Alpha_Build / DeltaT_Build (the DD build's),
+ * the stage counter and the history arrays. */
+typedef struct {
+	femgpu_transport *t;
+	double Alpha, DeltaT, AlphaB, DeltaTB;
+	int tag, stage;
+	double *u_hist;
+	int *ncorr, *iters, iters_cap;
+} tr_loop;
+
+/* One multicorrection loop (Predictor_Old.c:87-134 and its BDF / TRBDF2
+ * forms): corrections until the criterion holds; u += c Da each time. */
+static int multicorrect(tr_loop *L, double c)
+{
+	femgpu_transport *t = L->t;
+	const femgpu_transient_opts *o = &t->tr;
+	const int dd = o->stab == FEMGPU_STAB_DD;
+	double norm_a, norm_Da;
+	int i = 0, rc;
+	do {
+		int it = 0;
+		i++;
+		KR(fg_build_transient(t, dd, dd ? L->AlphaB * L->DeltaTB : L->Alpha * L->DeltaT));
+		KR(fg_assemble_transient(t));
+		t->built = 1;
+		t->factored = 0;
+		KR(femgpu_transport_precond_setup_dev(t, L->tag++));
+		rc = fgh_transport_gmres(t, t->F, t->Da, &it);
+		if (rc && rc != FEMGPU_E_NOT_CONVERGED) return rc;    /* gmres stops at lmax cycles, as pgmres */
+		if (L->iters && i <= L->iters_cap) L->iters[(size_t)L->stage * L->iters_cap + (i - 1)] = it;
+		KR(fg_tr_correct(t, c));
+		KR(dnorm(t, t->du, &norm_a));
+		KR(dnorm(t, t->Da, &norm_Da));
+	} while (!stop_corr(o, norm_a, norm_Da, i));
+	if (L->u_hist)
+		CK(cudaMemcpyAsync(L->u_hist + (size_t)L->stage * ((size_t)t->neq + 1), t->u,
+		                   sizeof(double) * ((size_t)t->neq + 1), cudaMemcpyDeviceToHost, t->stream));
+	if (L->ncorr) L->ncorr[L->stage] = i;
+	L->stage++;
+	return 0;
+}
+
+/* Criteria.c:41-79 on u and the method's u_old. */
+static int stop_time(tr_loop *L, const double *uold, double time, int *done)
+{
+	femgpu_transport *t = L->t;
+	const femgpu_transient_opts *o = &t->tr;
+	if (o->steady_stop) {
+		double norm_u, norm_diff;
+		if (uold != t->uold)
+			CK(cudaMemcpyAsync(t->uold, uold, sizeof(double) * (size_t)t->neq, cudaMemcpyDeviceToDevice, t->stream));
+		KR(fg_tr_diff(t));                                    /* Da := u - u_old */
+		KR(dnorm(t, t->Da, &norm_diff));
+		KR(dnorm(t, t->u, &norm_u));
+		*done = o->time_tol * norm_u > norm_diff || fabs(o->final_time - time) < L->DeltaT;
+	} else {
+		*done = fabs(o->final_time - time) < 1e-15;
+	}
+	return 0;
+}
+
 int femgpu_transport_predictor(femgpu_transport *t, const double *u0_host, int max_steps, double *u_hist,
 		double *t_hist, int *ncorr, int *iters, int iters_cap)
 {
 	const femgpu_transient_opts *o;
-	size_t n1;
-	int step = 0, tag = 1, rc, done;
-	double time = 0.0, c1, c2;
+	size_t n1, nb;
+	int step = 0, done = 0;
+	double time = 0.0, alpha, dt;
+	tr_loop L;
 	if (!t || !u0_host || max_steps < 1 || (iters && iters_cap < 1)) return FEMGPU_E_ARG;
 	if (!t->transient) { fgh_set_error("predictor before set_transient"); return FEMGPU_E_NOT_BUILT; }
 	o = &t->tr;
 	n1 = (size_t)t->neq + 1;
-	/* Predictor_Old.c:16-45: a, delta_old zeroed, u = InitialSolution */
+	nb = sizeof(double) * (size_t)t->neq;
+	if (o->method != FEMGPU_TI_PREDICTOR1 && !t->u1 &&
+	    (fgh_dmalloc((void **)&t->u1, sizeof(double) * n1) || fgh_dmalloc((void **)&t->u2, sizeof(double) * n1)))
+		return FEMGPU_E_NOMEM;
+	/* a, delta_old zeroed, u = InitialSolution (Predictor_Old.c:16-45) */
 	CK(cudaMemcpyAsync(t->u, u0_host, sizeof(double) * n1, cudaMemcpyHostToDevice, t->stream));
 	CK(cudaMemsetAsync(t->du, 0, sizeof(double) * n1, t->stream));
 	CK(cudaMemsetAsync(t->dold, 0, sizeof(double) * (size_t)t->nel, t->stream));
-	c1 = (1.0 - o->alpha) * o->dt;
-	c2 = o->alpha * o->dt;
-	do {
-		double norm_a, norm_Da;
-		int i = 0;
-		step++;
-		time += o->dt;
-		KR(fg_tr_predict(t, c1));
-		KR(dnorm(t, t->du, &norm_a));
-		norm_Da = norm_a + 1.0;
+	alpha = o->alpha;
+	dt = o->dt;
+	memset(&L, 0, sizeof L);
+	L.t = t; L.tag = 1; L.u_hist = u_hist; L.ncorr = ncorr; L.iters = iters; L.iters_cap = iters_cap;
+	L.Alpha = alpha; L.DeltaT = dt; L.AlphaB = alpha; L.DeltaTB = dt;
+
+	if (o->method == FEMGPU_TI_PREDICTOR1) {
+		/* Predictor_Old.c:62-136 */
+		const double c1 = (1.0 - alpha) * dt, c2 = alpha * dt;
 		do {
-			int it = 0;
-			i++;
-			KR(build_transient_dev(t));
-			KR(femgpu_transport_precond_setup_dev(t, tag++));
-			rc = fgh_transport_gmres(t, t->F, t->Da, &it);
-			if (rc && rc != FEMGPU_E_NOT_CONVERGED) return rc;    /* gmres stops at lmax cycles, as pgmres */
-			if (iters && i <= iters_cap) iters[(size_t)(step - 1) * iters_cap + (i - 1)] = it;
-			KR(fg_tr_correct(t, c2));
-			KR(dnorm(t, t->du, &norm_a));
-			KR(dnorm(t, t->Da, &norm_Da));
-		} while (!stop_corr(o, norm_a, norm_Da, i));
-		if (u_hist) CK(cudaMemcpyAsync(u_hist + (size_t)(step - 1) * n1, t->u, sizeof(double) * n1,
-		                               cudaMemcpyDeviceToHost, t->stream));
-		if (t_hist) t_hist[step - 1] = time;
-		if (ncorr) ncorr[step - 1] = i;
-		/* Criteria.c:41-79 */
-		if (o->steady_stop) {
-			double norm_u, norm_diff;
-			KR(fg_tr_diff(t));                                    /* Da := u - u_old */
-			KR(dnorm(t, t->Da, &norm_diff));
-			KR(dnorm(t, t->u, &norm_u));
-			done = o->time_tol * norm_u > norm_diff || fabs(o->final_time - time) < o->dt;
-		} else {
-			done = fabs(o->final_time - time) < 1e-15;
+			step++;
+			time += dt;
+			KR(fg_tr_predict(t, c1));                         /* u_old = u, u += c1 a, a = 0 */
+			KR(multicorrect(&L, c2));
+			if (t_hist) t_hist[step - 1] = time;
+			KR(stop_time(&L, t->uold, time, &done));
+		} while (!done && step < max_steps);
+	} else if (o->method == FEMGPU_TI_BDF) {
+		/* Predictor_Old_BDF.c:50-160: an implicit first step built with
+		 * Alpha = 1 (the updates keep the deck's alpha), then BDF2 with
+		 * Alpha = 2/3; u_old stays the initial solution */
+		const double four_thirds = 4.0/3.0, two_thirds = 2.0/3.0, one_third = 1.0/3.0;
+		double *u_old = t->uold;
+		step = 1;
+		time += dt;
+		L.Alpha = 1.0;
+		CK(cudaMemcpyAsync(u_old, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+		CK(cudaMemcpyAsync(t->u1, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+		CK(cudaMemsetAsync(t->du, 0, nb, t->stream));
+		KR(multicorrect(&L, alpha * dt));
+		CK(cudaMemcpyAsync(t->u2, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+		if (t_hist) t_hist[0] = time;
+		L.Alpha = two_thirds;
+		while (step < max_steps) {
+			step++;
+			time += dt;
+			KR(fg_tr_lin(t, t->u2, t->u1, four_thirds, one_third));    /* u = 4/3 u2 - 1/3 u1, a = 0 */
+			KR(multicorrect(&L, two_thirds * dt));
+			CK(cudaMemcpyAsync(t->u1, t->u2, nb, cudaMemcpyDeviceToDevice, t->stream));
+			CK(cudaMemcpyAsync(t->u2, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+			if (t_hist) t_hist[step - 1] = time;
+			KR(stop_time(&L, u_old, time, &done));
+			if (done) break;
 		}
-		CK(cudaStreamSynchronize(t->stream));
-	} while (!done && step < max_steps);
+	} else {
+		/* Predictor_Old_TRBDF2.c:34-165; DeltaT_Build is set to the TR
+		 * sub-step once, then stays at the BDF2 sub-step */
+		const double lambda = 2.0 - sqrt(2.0);
+		const double A = 1.0/(lambda*(2.0 - lambda));
+		const double B = (1.0 - lambda)*(1.0 - lambda)/(lambda*(2.0 - lambda));
+		const double dtTR = lambda*dt, dtBDF2 = (1.0 - lambda)*dt;
+		double *u_old = t->u1;
+		CK(cudaMemcpyAsync(u_old, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+		L.DeltaTB = dtTR;
+		do {
+			double a_tr = 0.5, a_bdf = 1.0/(2.0 - lambda);
+			step++;
+			time += dtTR;
+			L.Alpha = a_tr;
+			L.DeltaT = dtTR;
+			KR(fg_tr_axpy_zero(t, a_tr*dtTR));                  /* u += alpha dtTR a, a = 0 */
+			KR(multicorrect(&L, a_tr*dtTR));
+			L.Alpha = a_bdf;
+			L.DeltaT = dtBDF2;
+			L.DeltaTB = dtBDF2;
+			time += dtBDF2;
+			KR(fg_tr_lin(t, t->u, u_old, A, B));                 /* u = A u - B u_old, a = 0 */
+			KR(multicorrect(&L, a_bdf*dtBDF2));
+			CK(cudaMemcpyAsync(u_old, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+			if (t_hist) t_hist[step - 1] = time;
+			KR(stop_time(&L, u_old, time, &done));
+		} while (!done && step < max_steps);
+	}
+	CK(cudaStreamSynchronize(t->stream));
 	return step;
 }

@@ -235,21 +235,32 @@ typedef struct femgpu_transient_opts {
 	double nonlin_tol;     /* NonLinearTolerance (NORM)                          */
 	int steady_stop;       /* StopAtSteadyState: 1 YES, 0 NOT                    */
 	double time_tol;       /* TimeIntegrationTolerance (YES)                     */
+	int method;            /* TimeIntegration: FEMGPU_TI_*                       */
 } femgpu_transient_opts;
+/* Predictor1 (Predictor_Old.c), Predictor1_BDF (Predictor_Old_BDF.c:3-176:
+ * one implicit step, then BDF2 with u = 4/3 u_n - 1/3 u_(n-1)) and
+ * Predictor1_TRBDF2 (Predictor_Old_TRBDF2.c:3-179: a trapezoidal stage of
+ * (2 - sqrt 2) dt, then a BDF2 stage), each with the reference's own
+ * Alpha / DeltaT bookkeeping for the builds. */
+enum femgpu_time_integration { FEMGPU_TI_PREDICTOR1 = 0, FEMGPU_TI_BDF = 1, FEMGPU_TI_TRBDF2 = 2 };
 int femgpu_transport_set_transient(femgpu_transport *ctx, const femgpu_transient_opts *o);
 /* One transient Build on the state (u, a) (host [neq+1]; NULL: the context's):
  * R_host [neq+1] the residual, A_host the storage values (as
  * femgpu_transport_build); each call advances the DD state. */
 int femgpu_transport_build_transient(femgpu_transport *ctx, const double *u_host, const double *a_host,
 		double *R_host, double *A_host);
-/* Predictor_Old from u0_host [neq+1] (the problem's InitialSolution; a = 0,
- * a fresh DD state): per step u += (1-alpha) dt a, a = 0, then corrections
- * Build -> precond_setup -> solve(R, Da) -> a += Da, u += alpha dt Da until
- * the multicorrection criterion holds, until the time criterion holds or
- * max_steps steps.  u_hist [max_steps*(neq+1)], t_hist [max_steps],
- * ncorr [max_steps] (corrections per step) and iters [max_steps*iters_cap]
- * (GMRES iterations of each correction) are filled when non-NULL.  Returns
- * the number of steps run or an error. */
+/* The time loop of opts.method from u0_host [neq+1] (the problem's
+ * InitialSolution; a = 0, a fresh DD state).  Predictor1: per step
+ * u += (1-alpha) dt a, a = 0, then corrections Build -> precond_setup ->
+ * solve(R, Da) -> a += Da, u += alpha dt Da until the multicorrection
+ * criterion holds; the steps continue until the time criterion holds or
+ * max_steps steps.  A stage is one multicorrection loop (two per TRBDF2
+ * step, one otherwise): u_hist [S*max_steps*(neq+1)], ncorr [S*max_steps]
+ * (corrections of each stage) and iters [S*max_steps*iters_cap] (GMRES
+ * iterations of each correction) hold the stages in order, S = 2 for TRBDF2
+ * and 1 otherwise; t_hist [max_steps] the time at the end of each step.
+ * Arrays are filled when non-NULL.  Returns the number of steps run or an
+ * error. */
 int femgpu_transport_predictor(femgpu_transport *ctx, const double *u0_host, int max_steps, double *u_hist,
 		double *t_hist, int *ncorr, int *iters, int iters_cap);
 

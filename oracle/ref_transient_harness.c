@@ -9,8 +9,9 @@
  * with eval_U_dU and the CAU / CAU_DD / YZBeta shock capturing and the
  * h_shock options, the assembly pointers, csrmv / ebemv / edemv, the NOT /
  * Diag / ILU(0) preconditioners, the CONE / CONE2 / CARTOLA / PUDIM
- * plug-ins, and the time loop itself: 00_CommonFiles/Time_Integration/
- * Predictor_Old.c with the stop criteria of Criteria.c.
+ * plug-ins, and the time loops themselves: 00_CommonFiles/Time_Integration/
+ * Predictor_Old.c, Predictor_Old_BDF.c and Predictor_Old_TRBDF2.c with the
+ * stop criteria of Criteria.c.
  *
  * One documented adapter: the driver's solver pointer takes (B, X)
  * (TranspEquation.h: solver(P, M, FS, FF, B, X)), while the shipped pgmres.c
@@ -63,29 +64,41 @@ static void set_problem(int problem, FemFunctionsType *FF)
 static int noscale(ParametersType *P, MatrixDataType *M, FemStructsType *FS) { return 0; }
 static int nounscale(ParametersType *P, MatrixDataType *M, FemStructsType *FS, double *x) { return 0; }
 
-/* The time loop's per-step record: Predictor_Old calls StopTimeIntegration
- * once at the end of every step; the wrapper stores the step's u and t, then
- * asks the reference's criterion (or stops at the step cap). */
+/* Records of the time loop.  Every multicorrection loop (one per step, two
+ * per TRBDF2 step -- a stage) ends when the reference's StopCriteria says
+ * so: the wrapper stores the stage's u and correction count then.  The time
+ * criterion is asked once per step of the time loop (not after BDF's first,
+ * implicit step): the wrapper stores t then and stops at the step cap. */
 static double *g_uhist, *g_thist;
-static int *g_iters, *g_ncorr, g_step, g_maxsteps, g_corr, g_steady;
+static int *g_iters, *g_ncorr, g_stage, g_tcheck, g_maxsteps, g_corr, g_steady, g_norm, g_neq, g_cap;
+static double *g_u;
+
+static int record_stage(ParametersType *P, double norm_a, double norm_Da, int i)
+{
+	int stop = g_norm ? StopByNorm(P, norm_a, norm_Da, i) : StopByIterations(P, norm_a, norm_Da, i);
+	if (stop) {
+		if (g_stage < g_cap) {
+			memcpy(g_uhist + (size_t)g_stage * (g_neq + 1), g_u, sizeof(double) * (g_neq + 1));
+			g_ncorr[g_stage] = g_corr;
+		}
+		g_stage++;
+		g_corr = 0;
+	}
+	return stop;
+}
 
 static int record_step(ParametersType *P, double *u, double *u_old, double t)
 {
-	int stop;
-	memcpy(g_uhist + (size_t)g_step * (P->neq + 1), u, sizeof(double) * (P->neq + 1));
-	g_thist[g_step] = t;
-	g_ncorr[g_step] = g_corr;
-	g_corr = 0;
-	g_step++;
-	stop = g_steady ? StopBySteadyState(P, u, u_old, t) : StopByTime(P, u, u_old, t);
-	return stop || g_step >= g_maxsteps;
+	int stop = g_steady ? StopBySteadyState(P, u, u_old, t) : StopByTime(P, u, u_old, t);
+	g_thist[g_tcheck++] = t;
+	return stop || g_tcheck >= g_maxsteps;
 }
 
 static int solver_rec(ParametersType *P, MatrixDataType *M, FemStructsType *FS, FemFunctionsType *FF, double *B,
                       double *X)
 {
 	int before = P->iterations, rc = gmres6(P, M, FS, FF, B, X);
-	g_iters[(size_t)g_step * 64 + (g_corr < 63 ? g_corr : 63)] = P->iterations - before;
+	if (g_stage < g_cap) g_iters[(size_t)g_stage * 64 + (g_corr < 63 ? g_corr : 63)] = P->iterations - before;
 	g_corr++;
 	return rc;
 }
@@ -94,19 +107,22 @@ static int solver_rec(ParametersType *P, MatrixDataType *M, FemStructsType *FS, 
  *   problem: 0 CONE, 1 CONE2, 2 CARTOLA, 3 PUDIM; ntype: Node Type (1 free, 0 prescribed)
  *   stab "SUPG" | "DD"; shock "CAU" | "CAUDD" | "YZBeta"; hshock "2sqrtArea" | "Option1" | "Option2"
  *   stopmc "ITERATION" | "NORM"; steady "YES" | "NOT"
+ *   tint "Predictor1" | "Predictor1_BDF" | "Predictor1_TRBDF2" (setStabilizationForm.c:10-19)
  * Outputs:
- *   info [4] = neq, nnzero, nedge, bandwidth after reordering; node_id [nnodes]
+ *   info [5] = neq, nnzero, nedge, bandwidth after reordering, (out) time checks; node_id [nnodes]
  *   beta [2*nel], fsrc [3*nel], upresc [nnodes]: the plug-ins as Build evaluates them
  *   u0 [neq+1]: the plug-in's initial solution
  *   IA/JA/sbe (CSR) or lm2 (JA, 2*nedge) / EDGE_by_Element (sbe, 3*nel) / order (3*nel) (EDE)
  *   two consecutive Builds on (ub, dub) (the DD build keeps per-element state):
  *   A1, R1 and A2, R2 (storage values EBE 9*nel / EDE 4*(nedge+1) / CSR nnz+1; R [neq+1])
- *   then Predictor_Old from u0: uhist [maxsteps*(neq+1)], thist [maxsteps], ncorr [maxsteps],
- *   iters [maxsteps*64] (GMRES iterations of each correction).
- * Returns the number of steps run. */
+ *   then the time loop from u0, stopped after maxsteps time checks: per stage (multicorrection
+ *   loop) uhist [cap*(neq+1)], ncorr [cap], iters [cap*64] (GMRES iterations of each correction),
+ *   cap = 2*maxsteps + 2; per time check thist [maxsteps].
+ * Returns the number of stages recorded; info[4] = the number of time checks. */
 int ref_transient_run(int nnodes, const double *x, const double *y, const int *ntype, int nel, const int *vert,
                       int problem, const char *scheme, const char *reord, const char *precond, const char *stab,
-                      const char *shock, const char *hshock, const char *stopmc, const char *steady, double alpha,
+                      const char *shock, const char *hshock, const char *stopmc, const char *steady,
+                      const char *tint, double alpha,
                       double dt, double final_time, double nonlin_tol, int max_corr, double time_tol, double stab_tol,
                       int kmax, int lmax, double tol, int *info, int *node_id, double *beta, double *fsrc,
                       double *upresc, double *u0, int *IA_out, int *JA_out, int *sbe_out, int *order_out,
@@ -131,7 +147,7 @@ int ref_transient_run(int nnodes, const double *x, const double *y, const int *n
 	strcpy(P->StabilizationForm, stab);
 	strcpy(P->ShockCapture, shock);
 	strcpy(P->h_Shock, hshock);
-	strcpy(P->TimeIntegration, "Predictor1");
+	strcpy(P->TimeIntegration, tint);
 	strcpy(P->StopMulticorrection, stopmc);
 	strcpy(P->StopAtSteadyState, steady);
 	P->SolverTolerance = tol;
@@ -269,10 +285,16 @@ int ref_transient_run(int nnodes, const double *x, const double *y, const int *n
 	}
 
 	/* the reference's time loop */
-	g_uhist = uhist; g_thist = thist; g_iters = iters; g_ncorr = ncorr;
-	g_step = 0; g_maxsteps = maxsteps; g_corr = 0; g_steady = strcasecmp(steady, "YES") == 0;
+	g_uhist = uhist; g_thist = thist; g_iters = iters; g_ncorr = ncorr; g_u = u; g_neq = neq;
+	g_stage = 0; g_tcheck = 0; g_maxsteps = maxsteps; g_corr = 0; g_cap = 2 * maxsteps + 2;
+	g_steady = strcasecmp(steady, "YES") == 0;
+	g_norm = strcasecmp(stopmc, "NORM") == 0;
+	FF->StopCriteria = record_stage;
 	FF->StopTimeIntegration = record_step;
 	FOF->solver = solver_rec;
-	Predictor_Old(P, M, FS, FF, FOF);
-	return g_step;
+	if (strcasecmp(tint, "Predictor1_BDF") == 0) Predictor_Old_BDF(P, M, FS, FF, FOF);
+	else if (strcasecmp(tint, "Predictor1_TRBDF2") == 0) Predictor_Old_TRBDF2(P, M, FS, FF, FOF);
+	else Predictor_Old(P, M, FS, FF, FOF);
+	info[4] = g_tcheck;
+	return g_stage < g_cap ? g_stage : g_cap;
 }

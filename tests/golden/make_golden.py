@@ -71,7 +71,7 @@ def run_ref(lib, mesh, ntype, problem="SKEW", scheme="CSR", reord="NOT", precond
     nn, ne = mesh.nnodes, mesh.nel
     neq_ub = int((ntype >= 1).sum())
     nnz_ub = 9 * ne + 1
-    info = np.zeros(4, np.int32)
+    info = np.zeros(5, np.int32)
     node_id = np.zeros(nn, np.int32)
     etype = np.zeros(ne, np.int32)
     beta = np.zeros(2 * ne)
@@ -422,7 +422,7 @@ def amg_fprec(IA, JA, AA, F, spec):
     n = IA.size - 1
     L = amg_lib()
     Fp = np.concatenate([np.ascontiguousarray(F, np.float64), [0.0]])
-    info = np.zeros(4, np.int32)
+    info = np.zeros(5, np.int32)
     L.ref_amg_setup(n, np.ascontiguousarray(IA, np.int32), np.ascontiguousarray(JA, np.int32),
                     np.ascontiguousarray(AA, np.float64), spec.encode(), Fp, info)
     return Fp[:n].copy()
@@ -443,7 +443,7 @@ def main_amg():
         F0 = np.ascontiguousarray(out["Ffirst"][:n])
         L = amg_lib()
         F = np.concatenate([F0, [0.0]])
-        info = np.zeros(4, np.int32)
+        info = np.zeros(5, np.int32)
         L.ref_amg_setup(n, IA, JA, AA, spec.encode(), F, info)
         levels = {}
         for l in range(int(info[0])):
@@ -511,7 +511,7 @@ def main_vtu():
 # Transient transport (02_Transport_Equation/2D): problem -> (harness code, domain side, origin)
 TT_PROBLEMS = {"CONE": (0, 10.0, 0.0), "CONE2": (1, 10.0, -5.0), "CARTOLA": (2, 1.0, 0.0), "PUDIM": (3, 2.0, -1.0)}
 TT_BASE = dict(reord="NOT", precond="NOT", stab="SUPG", shock="CAU", hshock="2sqrtArea", stopmc="ITERATION",
-               steady="NOT", alpha=0.5, dt=0.1, final=1.0, nonlin_tol=1e-3, max_corr=2, time_tol=1e-6,
+               steady="NOT", tint="Predictor1", alpha=0.5, dt=0.1, final=1.0, nonlin_tol=1e-3, max_corr=2, time_tol=1e-6,
                stab_tol=1e-6, kmax=30, lmax=20, tol=1e-8, maxsteps=12)
 TT_CASES = {
     "tt_cone16_csr_ilu0_supg_rcm": dict(problem="CONE", n=16, scheme="CSR", reord="SYMRCM", precond="ILU0"),
@@ -525,6 +525,12 @@ TT_CASES = {
                                            steady="YES", time_tol=1e-3, dt=0.05),
     "tt_cone2_12_csr_diag_dd_cau": dict(problem="CONE2", n=12, scheme="CSR", precond="Diag", stab="DD",
                                         shock="CAU", dt=0.05, final=0.5),
+    "tt_cone16_csr_ilu0_supg_bdf": dict(problem="CONE", n=16, scheme="CSR", reord="SYMRCM", precond="ILU0",
+                                        tint="Predictor1_BDF", maxsteps=8),
+    "tt_cone2_16_csr_ilu0_dd_trbdf2": dict(problem="CONE2", n=16, scheme="CSR", precond="ILU0", stab="DD",
+                                           shock="CAUDD", tint="Predictor1_TRBDF2", dt=0.05, maxsteps=6),
+    "tt_cartola16_ebe_diag_supg_trbdf2": dict(problem="CARTOLA", n=16, scheme="EBE", precond="Diag",
+                                              tint="Predictor1_TRBDF2", dt=0.01, maxsteps=6),
 }
 
 
@@ -533,7 +539,7 @@ def transient_lib():
     f = lib.ref_transient_run
     f.restype = ctypes.c_int
     s, d, i = ctypes.c_char_p, ctypes.c_double, ctypes.c_int
-    f.argtypes = [i, _dp, _dp, _ip, i, _ip, i, s, s, s, s, s, s, s, s, d, d, d, d, i, d, d, i, i, d,
+    f.argtypes = [i, _dp, _dp, _ip, i, _ip, i, s, s, s, s, s, s, s, s, s, d, d, d, d, i, d, d, i, i, d,
                   _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp,
                   i, _dp, _dp, _ip, _ip]
     return lib
@@ -557,7 +563,7 @@ def run_transient(lib, name, case):
     nn, ne = m.nnodes, m.nel
     neq = int((ntype == 1).sum())
     cap = 16 * (nn + ne) + 16
-    info = np.zeros(4, np.int32)
+    info = np.zeros(5, np.int32)
     node_id = np.zeros(nn, np.int32)
     beta, fsrc, upresc = np.zeros(2 * ne), np.zeros(3 * ne), np.zeros(nn)
     u0 = np.zeros(neq + 1)
@@ -569,13 +575,14 @@ def run_transient(lib, name, case):
     A1, A2 = np.zeros(cap), np.zeros(cap)
     R1, R2 = np.zeros(neq + 1), np.zeros(neq + 1)
     ms = c["maxsteps"]
-    uh, th = np.zeros(ms * (neq + 1)), np.zeros(ms)
-    nc, its = np.zeros(ms, np.int32), np.zeros(ms * 64, np.int32)
+    cap = 2 * ms + 2
+    uh, th = np.zeros(cap * (neq + 1)), np.zeros(ms)
+    nc, its = np.zeros(cap, np.int32), np.zeros(cap * 64, np.int32)
     e = lambda v: v.encode()
-    steps = lib.ref_transient_run(
+    stages = lib.ref_transient_run(
         nn, m.x, m.y, ntype, ne, np.ascontiguousarray(m.vert.reshape(-1), np.int32), TT_PROBLEMS[c["problem"]][0],
         e(c["scheme"]), e(c["reord"]), e(c["precond"]), e(c["stab"]), e(c["shock"]), e(c["hshock"]),
-        e(c["stopmc"]), e(c["steady"]), c["alpha"], c["dt"], c["final"], c["nonlin_tol"], c["max_corr"],
+        e(c["stopmc"]), e(c["steady"]), e(c["tint"]), c["alpha"], c["dt"], c["final"], c["nonlin_tol"], c["max_corr"],
         c["time_tol"], c["stab_tol"], c["kmax"], c["lmax"], c["tol"], info, node_id, beta, fsrc, upresc, u0,
         IA, JA, sbe, order, ub, dub, A1, R1, A2, R2, ms, uh, th, nc, its)
     neq_r, nnz, nedge = int(info[0]), int(info[1]), int(info[2])
@@ -583,16 +590,17 @@ def run_transient(lib, name, case):
     nA = {"CSR": nnz + 1, "EDE": 4 * (nedge + 1), "EBE": 9 * ne}[c["scheme"]]
     out = dict(x=m.x, y=m.y, vert=m.vert, node_type=ntype, neq=neq, nnz=nnz, nedge=nedge, node_id=node_id,
                beta=beta.reshape(ne, 2), fsrc=fsrc.reshape(ne, 3), upresc=upresc, u0=u0, ub=ub, dub=dub,
-               A1=A1[:nA], R1=R1, A2=A2[:nA], R2=R2, steps=steps, uhist=uh.reshape(ms, neq + 1)[:steps],
-               thist=th[:steps], ncorr=nc[:steps], iters=its.reshape(ms, 64)[:steps],
-               meta=np.array(repr(c)))
+               A1=A1[:nA], R1=R1, A2=A2[:nA], R2=R2, stages=stages, tchecks=int(info[4]),
+               uhist=uh.reshape(cap, neq + 1)[:stages], thist=th[:int(info[4])], ncorr=nc[:stages],
+               iters=its.reshape(cap, 64)[:stages], meta=np.array(repr(c)))
     if c["scheme"] == "CSR":
         out.update(IA=IA[:neq + 1], JA=JA[:nnz], sbe=sbe[:9 * ne].reshape(ne, 9))
     elif c["scheme"] == "EDE":
         out.update(lm2=JA[:2 * nedge].reshape(nedge, 2), ebe=sbe[:3 * ne].reshape(ne, 3),
                    order=order[:3 * ne].reshape(ne, 3))
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
-    print(f"{name}: neq={neq} steps={steps} ncorr={list(nc[:steps])} iters={list(its.reshape(ms, 64)[:steps, 0])}")
+    print(f"{name}: neq={neq} stages={stages} time checks={int(info[4])} ncorr={nc[:stages].tolist()} "
+          f"iters={its.reshape(cap, 64)[:stages, 0].tolist()}")
 
 
 def main_transient():
