@@ -22,7 +22,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SHIMS = os.path.join(ROOT, "fem_codes_gb300", "shims")
 INC = os.path.join(ROOT, "include")
-REF = os.environ.get("FEMREF_DIR", "/root/reference")
+from __graft_entry__ import REFERENCE_DIR as REF  # noqa: E402
 HAVE_REF = os.path.isdir(os.path.join(REF, "00_CommonFiles"))
 
 # shim, restated-layout header, reference macro, reference header directory and header
