@@ -151,6 +151,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_mesh_read": [ctypes.c_char_p, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
         "femgpu_mesh_side_types": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp],
         "femgpu_transport_set_sweep_wait": [_vp, ctypes.c_int],
+        "femgpu_euler_set_slip": [_vp, _vp, _vp, _vp],
         "femgpu_transport_set_transient": [_vp, _vp],
         "femgpu_transport_build_transient": [_vp, _vp, _vp, _vp, _vp],
         "femgpu_transport_predictor": [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int],
@@ -879,6 +880,15 @@ class Euler:
         of a CSR context (hierarchy rebuilt at every precond_setup)."""
         self._amg = amg
         self._check(self._L.femgpu_euler_set_amg(self._h, amg.handle), "set_amg")
+
+    def set_slip(self, slip=None, cs=None, sn=None):
+        """Slip walls: slip [nnodes] (the nodes with v1Type = -1) and the cosine
+        and sine of their wall angles; None removes them."""
+        if slip is None:
+            self._check(self._L.femgpu_euler_set_slip(self._h, None, None, None), "set_slip")
+            return
+        self._slip = (_i32(slip), _f64(cs), _f64(sn))
+        self._check(self._L.femgpu_euler_set_slip(self._h, *(_ptr(a) for a in self._slip)), "set_slip")
 
     def csr(self):
         """CSR storage: (IA, JA, CSR_by_Element [nel, 144], AA of the last build)."""

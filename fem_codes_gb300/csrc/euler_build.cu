@@ -328,6 +328,48 @@ __global__ void k_euler_correct(int n, double *u, double *a, const double *Da, d
 	}
 }
 
+// rotation.c:3-43 at Build_M_K_F_SUPG.c:1044-1056: for each vertex (in
+// vertex order) on a slip wall, the element matrix's 4x4 blocks in that
+// vertex's block row are transformed with the vertex's angle -- the velocity
+// rows rotated by P^T and the velocity columns by P, the reference's own
+// entry-by-entry formulas -- and the vertex's velocity entries of Re rotated.
+__global__ void k_euler_rotate(int nslip, const int *__restrict__ slip_el, const int *__restrict__ vert,
+                               const int *__restrict__ flag, const double *__restrict__ cs_n,
+                               const double *__restrict__ sn_n, double *A, double *Re)
+{
+	for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nslip; t += gridDim.x * blockDim.x) {
+		const int e = slip_el[t];
+		double *M = A + 144LL * e, *F = Re + 12LL * e;
+		for (int tag = 0; tag < 3; tag++) {
+			const int v = vert[3 * e + tag];
+			if (!flag[v]) continue;
+			const double cs = cs_n[v], sn = sn_n[v];
+			const int I = 4 * tag;
+			for (int K = 0; K < 3; K++) {
+				const int J = 4 * K;
+				double *r0 = M + 12 * I, *r1 = M + 12 * (I + 1), *r2 = M + 12 * (I + 2), *r3 = M + 12 * (I + 3);
+				const double b = r0[J + 1], c = r0[J + 2], ee = r1[J], f = r1[J + 1], g = r1[J + 2], h = r1[J + 3];
+				const double i = r2[J], j = r2[J + 1], k = r2[J + 2], l = r2[J + 3], n = r3[J + 1], o = r3[J + 2];
+				r0[J + 1] = b*cs - c*sn;
+				r0[J + 2] = b*sn + c*cs;
+				r1[J] = ee*cs - i*sn;
+				r1[J + 1] = cs*(f*cs - j*sn) - sn*(g*cs - k*sn);
+				r1[J + 2] = cs*(g*cs - k*sn) + sn*(f*cs - j*sn);
+				r1[J + 3] = h*cs - l*sn;
+				r2[J] = ee*sn + i*cs;
+				r2[J + 1] = cs*(f*sn + j*cs) - sn*(g*sn + k*cs);
+				r2[J + 2] = cs*(g*sn + k*cs) + sn*(f*sn + j*cs);
+				r2[J + 3] = h*sn + l*cs;
+				r3[J + 1] = n*cs - o*sn;
+				r3[J + 2] = n*sn + o*cs;
+			}
+			const double b = F[I + 1], c = F[I + 2];
+			F[I + 1] = b*cs - c*sn;
+			F[I + 2] = b*sn + c*cs;
+		}
+	}
+}
+
 extern "C" int fg_euler_build(femgpu_euler *c, const double *u, const double *du)
 {
 	EulerCoef cf;
@@ -338,6 +380,12 @@ extern "C" int fg_euler_build(femgpu_euler *c, const double *u, const double *du
 	k_euler_element<<<g, 128, 0, c->stream>>>(c->nel, b->vert, b->node_id, c->x, c->y, c->upresc, u, du, cf,
 	                                          b->A, c->Re);
 	FG_TRY(cudaGetLastError());
+	if (c->nslip_el > 0) {
+		k_euler_rotate<<<fg_grid(c->nslip_el), FG_TPB, 0, c->stream>>>(c->nslip_el, c->slip_el, b->vert,
+		                                                              c->slip_flag, c->slip_cs, c->slip_sn,
+		                                                              b->A, c->Re);
+		FG_TRY(cudaGetLastError());
+	}
 	k_euler_gather<<<fg_grid(c->neq + 1LL), FG_TPB, 0, c->stream>>>(c->neq, b->ri_ptr, b->ri, c->Re, c->R);
 	return (int)cudaGetLastError();
 }

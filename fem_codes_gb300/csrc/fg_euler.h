@@ -25,6 +25,10 @@ struct femgpu_euler {
 	fg_krylov kry;
 	int built, have_bd;
 	fg_blockcsr csr;               /* scheme FEMGPU_CSR: 12 equations per element */
+	/* slip walls (femgpu_euler_set_slip): per node flag and the cos / sin of
+	 * its wall angle, and the elements with a slip vertex */
+	int *slip_flag, *slip_el, nslip_el;
+	double *slip_cs, *slip_sn;
 	cudaEvent_t ev[4];
 	double times[3];               /* build, precond setup, solve (s)            */
 };

@@ -182,7 +182,8 @@ void femgpu_euler_destroy(femgpu_euler *c)
 	fgh_blockcsr_destroy(&c->csr);
 	if (c->ebe) femgpu_ebe_destroy(c->ebe);
 	{
-		void *p[] = { c->x, c->y, c->upresc, c->u, c->a, c->R, c->Da, c->Re };
+		void *p[] = { c->x, c->y, c->upresc, c->u, c->a, c->R, c->Da, c->Re, c->slip_flag, c->slip_el, c->slip_cs,
+		              c->slip_sn };
 		for (i = 0; i < (int)(sizeof p / sizeof p[0]); i++) if (p[i]) cudaFree(p[i]);
 	}
 	fgh_kry_free(&c->kry);
@@ -200,6 +201,45 @@ int femgpu_euler_set_stream(femgpu_euler *c, void *stream)
 	KR(femgpu_ebe_set_stream(c->ebe, c->stream));
 	fgh_blockcsr_set_stream(&c->csr, c->stream);
 	return 0;
+}
+
+int femgpu_euler_set_slip(femgpu_euler *c, const int *slip, const double *cs, const double *sn)
+{
+	int *vert = NULL, *el = NULL, n = 0, e, k, rc = 0;
+	if (!c) return FEMGPU_E_ARG;
+	CK(cudaStreamSynchronize(c->stream));
+	if (c->slip_flag) { cudaFree(c->slip_flag); cudaFree(c->slip_el); cudaFree(c->slip_cs); cudaFree(c->slip_sn); }
+	c->slip_flag = c->slip_el = NULL;
+	c->slip_cs = c->slip_sn = NULL;
+	c->nslip_el = 0;
+	if (!slip) return 0;
+	if (!cs || !sn) return FEMGPU_E_ARG;
+	vert = malloc(sizeof(int) * 3 * (size_t)c->nel);
+	el = malloc(sizeof(int) * (size_t)c->nel + sizeof(int));
+	if (!vert || !el) { free(vert); free(el); return FEMGPU_E_NOMEM; }
+	if (cudaMemcpy(vert, c->ebe->vert, sizeof(int) * 3 * (size_t)c->nel, cudaMemcpyDeviceToHost) != cudaSuccess) {
+		free(vert); free(el); return FEMGPU_E_CUDA;
+	}
+	for (e = 0; e < c->nel; e++) {
+		for (k = 0; k < 3; k++) if (slip[vert[3 * e + k]]) break;
+		if (k < 3) el[n++] = e;
+	}
+	free(vert);
+	if (fgh_dmalloc((void **)&c->slip_flag, sizeof(int) * (size_t)c->nnodes) ||
+	    fgh_dmalloc((void **)&c->slip_el, sizeof(int) * ((size_t)n + 1)) ||
+	    fgh_dmalloc((void **)&c->slip_cs, sizeof(double) * (size_t)c->nnodes) ||
+	    fgh_dmalloc((void **)&c->slip_sn, sizeof(double) * (size_t)c->nnodes))
+		rc = FEMGPU_E_NOMEM;
+	if (!rc && (cudaMemcpy(c->slip_flag, slip, sizeof(int) * (size_t)c->nnodes, cudaMemcpyHostToDevice) ||
+	            cudaMemcpy(c->slip_el, el, sizeof(int) * ((size_t)n + 1), cudaMemcpyHostToDevice) ||
+	            cudaMemcpy(c->slip_cs, cs, sizeof(double) * (size_t)c->nnodes, cudaMemcpyHostToDevice) ||
+	            cudaMemcpy(c->slip_sn, sn, sizeof(double) * (size_t)c->nnodes, cudaMemcpyHostToDevice)))
+		rc = FEMGPU_E_CUDA;
+	free(el);
+	if (!rc) c->nslip_el = n;
+	c->built = 0;
+	c->have_bd = 0;
+	return rc;
 }
 
 int femgpu_euler_set_amg(femgpu_euler *c, femgpu_amg *g)

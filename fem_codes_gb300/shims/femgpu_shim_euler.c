@@ -33,6 +33,7 @@
 #endif
 #include "femgpu.h"
 
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -131,6 +132,26 @@ static int eu_of(ParametersType *P, FemStructsType *FS, FemFunctionsType *FF)
 		for (k = 0; k < 3; k++) vert[3 * E + k] = FS->Element[E].Vertex[k];
 	rc = femgpu_euler_create(&g_eu, &o, nn, x, y, ne, vert, nid, P->neq, up);
 	if (!rc && o.precond == FEMGPU_PREC_AMG) rc = femgpu_euler_set_amg(g_eu, g_amg);
+	/* slip walls: the nodes with v1Type == -1, rotated by BC_theta as
+	 * Build_M_K_F_SUPG.c:1044-1056 and rotation.c:6-7 do */
+	if (!rc) {
+		int nslip = 0, *slip = calloc((size_t)nn, sizeof(int));
+		double *cs = malloc(sizeof(double) * (size_t)nn), *sn = malloc(sizeof(double) * (size_t)nn);
+		if (!slip || !cs || !sn) rc = FEMGPU_E_NOMEM;
+		for (I = 0; !rc && I < nn; I++) {
+			cs[I] = 1.0;
+			sn[I] = 0.0;
+			if (FS->Node[I].v1Type == -1) {
+				double th = FF->BC_theta(FS->Node[I].x, FS->Node[I].y);
+				slip[I] = 1;
+				cs[I] = cos(th);
+				sn[I] = sin(th);
+				nslip++;
+			}
+		}
+		if (!rc && nslip) rc = femgpu_euler_set_slip(g_eu, slip, cs, sn);
+		free(slip); free(cs); free(sn);
+	}
 out:
 	free(x); free(y); free(up); free(nid); free(vert);
 	return rc;

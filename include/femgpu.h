@@ -331,10 +331,10 @@ int femgpu_ebe_blockdiag_apply_dev(femgpu_ebe *ctx, const double *p, double *z);
 
 /* ---- 2D Euler: SUPG+CAU build and predictor-multicorrector -------------
  * 03_Euler_Equations/2D with StabilizationForm SUPG, ShockCapture CAU,
- * MatrixVectorProductScheme EBE, TimeIntegration Predictor1 (Predictor_Old)
- * and StopMulticorrection ITERATION.  Conservative unknowns per node in the
- * order (rho, rho u, rho v, rho E).  Slip walls (v1Type == -1, rotation.c)
- * are not supported: prescribe the wall-normal momentum instead. */
+ * MatrixVectorProductScheme EBE or CSR, TimeIntegration Predictor1
+ * (Predictor_Old) and StopMulticorrection ITERATION.  Conservative unknowns
+ * per node in the order (rho, rho u, rho v, rho E).  Slip walls (v1Type ==
+ * -1, rotation.c) through femgpu_euler_set_slip. */
 typedef struct femgpu_euler_opts {
 	double gamma;        /* ratio of specific heats (gamma(), constant)     */
 	double mach;         /* reference Mach number (dimensionless only)       */
@@ -571,6 +571,13 @@ int femgpu_transport_set_amg(femgpu_transport *t, femgpu_amg *ctx);
  * its own stream when the context is destroyed, so ctx must outlive it. */
 int femgpu_ns_set_amg(femgpu_ns *ns, femgpu_amg *ctx);
 int femgpu_euler_set_amg(femgpu_euler *eu, femgpu_amg *ctx);
+/* Slip walls of the Euler SUPG build (Build_M_K_F_SUPG.c:1044-1056 with
+ * rotation.c:3-43): slip [nnodes] != 0 marks the nodes the reference gives
+ * v1Type = -1; their rows and columns of each element matrix and their
+ * entries of the element residual are rotated by the wall angle BC_theta(x, y),
+ * whose cosine and sine the caller passes (cs, sn [nnodes], evaluated on the
+ * host as rotation.c evaluates them).  slip = NULL removes the walls. */
+int femgpu_euler_set_slip(femgpu_euler *eu, const int *slip, const double *cs, const double *sn);
 
 /* ---- stateless device kernels (device pointers, stream as void*) -------- */
 /* csrmv.c:3-24 in FP64 / FP32 values. */

@@ -111,6 +111,41 @@ int ref_euler_build(int nnodes, const double *x, const double *y, const int *nod
 	return 0;
 }
 
+/* A slip-wall angle with the shape of the reference's BC_theta plug-ins
+ * (CYLINDER/CYLINDER_theta.c: atan(-x/y) about the cylinder's centre); here
+ * about (2, -1), below the REFLETIDO domain, so it is defined on every wall
+ * node. */
+static double slip_theta(double x, double y) { return atan(-(x - 2.0) / (y + 1.0)); }
+
+/* One Build with slip walls: nodes with slip[I] != 0 get v1Type = -1, so
+ * Build_M_K_F_SUPG.c:1044-1056 rotates their rows and columns of Ae and their
+ * Re by BC_theta (rotation.c:3-43).  Outputs Ae [nel*144], R, and the
+ * cos / sin of each node's angle as rotation.c evaluates them (cs, sn
+ * [nnodes], 1 / 0 off the wall). */
+int ref_euler_build_slip(int nnodes, const double *x, const double *y, const int *node_id, const int *slip,
+                         int nel, const int *vert, int neq, double alpha, double dt, double stab_tol,
+                         const double *u, const double *du, double *Ae, double *R, double *cs, double *sn)
+{
+	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF;
+	int I;
+	setup(0, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
+	for (I = 0; I < nnodes; I++) {
+		cs[I] = 1.0; sn[I] = 0.0;
+		if (slip[I]) {
+			double th = slip_theta(x[I], y[I]);
+			FS->Node[I].v1Type = -1;
+			cs[I] = cos(th); sn[I] = sin(th);
+		}
+	}
+	FF->BC_theta = slip_theta;
+	memcpy(FS->u, u, sizeof(double) * (neq + 1));
+	memcpy(FS->du, du, sizeof(double) * (neq + 1));
+	Build_M_K_F_SUPG(P, M, FS, FF);
+	memcpy(Ae, M->Aaux, sizeof(double) * nel * 144);
+	memcpy(R, FS->F, sizeof(double) * (neq + 1));
+	return 0;
+}
+
 /* Predictor_Old.c:46-132 with ncorr correctors per step (StopByIterations,
  * Criteria.c:25-31) and nsteps steps, BlockDiag + EBE + the GMRES above.
  * u in/out; ahist [nsteps*(neq+1)], uhist likewise; iters [nsteps*ncorr]. */

@@ -230,6 +230,9 @@ def main_euler():
                                         ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp,
                                         _ip]
     lib.ref_euler_predictor_csr.argtypes = lib.ref_euler_predictor.argtypes
+    lib.ref_euler_build_slip.argtypes = [ctypes.c_int, _dp, _dp, _ip, _ip, ctypes.c_int, _ip, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp,
+                                         _dp, _dp]
     lib.ref_euler_build_csr.restype = ctypes.c_int
     lib.ref_euler_build_csr.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp, ctypes.c_int,
@@ -276,9 +279,17 @@ def main_euler():
         lib.ref_euler_predictor_csr(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol,
                                     kmax, lmax, tol, nsteps, ncorr, upc, uhc, itc)
         amg_Fp = amg_fprec(IA, JA[:nnz], AA[:nnz], Rc[:neq], AMG_SYS_SPEC)
+        # slip walls: the bottom wall's nodes whose v1 is free and v2 prescribed get
+        # v1Type = -1 (Build_M_K_F_SUPG.c:1044-1056, rotation.c)
+        slip = ((mesh.y == 0.0) & (pb.node_id[:, 1] >= 0) & (pb.node_id[:, 2] < 0)).astype(np.int32)
+        Ae_s, R_s = np.zeros(mesh.nel * 144), np.zeros(neq + 1)
+        cs, sn = np.zeros(mesh.nnodes), np.zeros(mesh.nnodes)
+        lib.ref_euler_build_slip(mesh.nnodes, mesh.x, mesh.y, nid, slip, mesh.nel, vert, neq, alpha, dt, stol, u,
+                                 du, Ae_s, R_s, cs, sn)
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id,
             amg_spec=np.array(AMG_SYS_SPEC), amg_Fp=amg_Fp,
+            slip=slip, slip_cs=cs, slip_sn=sn, slip_Ae=Ae_s.reshape(mesh.nel, 144), slip_R=R_s,
             neq=neq, upresc=pb.upresc, u0=pb.u0, gamma=pb.gamma, alpha=alpha, dt=dt, stab_tol=stol,
             u=u, du=du, Ae=Ae.reshape(mesh.nel, 144), R=R, kmax=kmax, lmax=lmax, tol=tol,
             nsteps=nsteps, ncorr=ncorr, uhist=uhist.reshape(nsteps, neq + 1),

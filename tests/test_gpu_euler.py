@@ -51,6 +51,23 @@ def test_euler_build_bitexact_vs_reference(gpu_lib, name):
 
 
 @pytest.mark.parametrize("name", CASES)
+def test_euler_build_slip_walls_bitexact_vs_reference(gpu_lib, name):
+    """Slip walls (v1Type = -1 on the bottom wall): the rotation of
+    Build_M_K_F_SUPG.c:1044-1056 / rotation.c, element matrices and residual
+    bit-identical to the reference's build; removing the walls restores the
+    unrotated build."""
+    g = _load(name)
+    with _euler(g) as eu:
+        eu.set_slip(g["slip"], g["slip_cs"], g["slip_sn"])
+        R, Ae = eu.Build(g["u"], g["du"], want_matrix=True)
+        assert np.array_equal(Ae, g["slip_Ae"])
+        assert np.array_equal(R, g["slip_R"])
+        eu.set_slip(None)
+        R, Ae = eu.Build(g["u"], g["du"], want_matrix=True)
+    assert np.array_equal(Ae, g["Ae"]) and np.array_equal(R, g["R"])
+
+
+@pytest.mark.parametrize("name", CASES)
 def test_euler_precond_setup_bitexact(gpu_lib, name):
     """R := D^-1 R after the build (BlockDiag_precond_EBE_setup.c:82)."""
     g = _load(name)
