@@ -153,6 +153,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_transport_set_sweep_wait": [_vp, ctypes.c_int],
         "femgpu_euler_set_slip": [_vp, _vp, _vp, _vp],
         "femgpu_transport_set_transient": [_vp, _vp],
+        "femgpu_transport_set_bubbles": [_vp, _vp, _vp],
         "femgpu_transport_build_transient": [_vp, _vp, _vp, _vp, _vp],
         "femgpu_transport_predictor": [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int],
         "femgpu_deck_transport_opts": [_vp, _vp],
@@ -644,7 +645,8 @@ class SSTransport:
                           stop_norm={"ITERATION": 0, "NORM": 1}[stop.upper()], max_corr=int(max_corr),
                           nonlin_tol=nonlin_tol, steady_stop={"NOT": 0, "YES": 1}[steady.upper()],
                           time_tol=time_tol,
-                          method={"PREDICTOR1": 0, "PREDICTOR1_BDF": 1, "PREDICTOR1_TRBDF2": 2}[method.upper()])
+                          method={"PREDICTOR1": 0, "PREDICTOR1_BDF": 1, "PREDICTOR1_TRBDF2": 2,
+                                  "PREDICTOR2": 3}[method.upper()])
         self._stages = 2 if method.upper() == "PREDICTOR1_TRBDF2" else 1
         self._check(self._L.femgpu_transport_set_transient(self._h, ctypes.byref(o)), "set_transient")
 
@@ -657,6 +659,11 @@ class SSTransport:
         self._check(self._L.femgpu_transport_build_transient(self._h, _ptr(uu), _ptr(aa), _ptr(R), _ptr(A)),
                     "build_transient")
         return R, A
+
+    def set_bubbles(self, uB=None, aB=None):
+        """The element bubbles (Predictor2) for the next build_transient."""
+        self._check(self._L.femgpu_transport_set_bubbles(self._h, _ptr(None if uB is None else _f64(uB)),
+                                                         _ptr(None if aB is None else _f64(aB))), "set_bubbles")
 
     def predictor(self, u0, max_steps, iters_cap=16):
         """The time loop from u0: dict(u [stages, neq+1], t [steps], ncorr

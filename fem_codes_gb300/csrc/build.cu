@@ -25,6 +25,9 @@ struct BuildArgs {
 	double adt;                   // Alpha * DeltaT
 	double *re;                   // per element and local row: load term, then three products
 	double *dold;                 // DD: the previous build's shock parameter per element
+	// Build_M_F_DD (Predictor_New): the bubble unknowns and the condensation
+	const double *uB, *aB;        // per element
+	double *bub;                  // per element: invN2, R2, M2[3] (calculate_DaB's inputs)
 };
 
 // Shock length scale: h_shock_2sqrtArea.c:3-8, h_shock_sqrtArea.c:3-61 (every
@@ -325,6 +328,183 @@ __global__ void __launch_bounds__(128) k_build_transient(BuildArgs a)
 			}
 		}
 	}
+}
+
+// Build_M_F_DD.c:58-215, one thread per element: the DD form with the
+// bubble kept as an unknown of the time loop (Predictor_New).  The bubble
+// row is condensed with N2 = MBB + alpha dt KBB: Me = M1 - invN2 N1 M2^T goes
+// to the element buffer, the residual contribution R1[i] - invN2 N1[i] R2 to
+// re[12E + 4i] (the three product slots zero, so the gather adds it alone),
+// and invN2, R2, M2 to the bubble buffer for calculate_DaB.
+__global__ void __launch_bounds__(128) k_build_mfdd(BuildArgs a)
+{
+	const double third = 1.0/3.0, sixth = 1.0/6.0, twelfth = 1.0/12.0;
+	const double seventh = 1.0/7.0, three_twentieth = 3./20.0, nine_twentieth = 9./20.0,
+	             nine_forty_cents = 9./40.0, w = 0.5;
+	const double kx = a.k, ky = a.k, gamma = a.gamma;
+	for (int E = blockIdx.x * blockDim.x + threadIdx.x; E < a.nel; E += gridDim.x * blockDim.x) {
+		int J1 = __ldg(&a.vert[3*E]), J2 = __ldg(&a.vert[3*E+1]), J3 = __ldg(&a.vert[3*E+2]);
+		double X0 = __ldg(&a.x[J1]), X1 = __ldg(&a.x[J2]), X2 = __ldg(&a.x[J3]);
+		double Y0 = __ldg(&a.y[J1]), Y1 = __ldg(&a.y[J2]), Y2 = __ldg(&a.y[J3]);
+		double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
+		double x32 = X2 - X1, x13 = X0 - X2, x21 = X1 - X0;
+		double TwoA = x21*y31 - x13*y12, Area = 0.5*TwoA, invArea = 1.0/Area;
+		double bx, by;
+		if (a.beta_const) { bx = a.cbx; by = a.cby; }
+		else { bx = __ldg(&a.beta[2*E]); by = __ldg(&a.beta[2*E+1]); }
+		double fe1 = 0.0, fe2 = 0.0, fe3 = 0.0;
+		if (!a.fsrc_zero) { fe1 = __ldg(&a.fsrc[3*E]); fe2 = __ldg(&a.fsrc[3*E+1]); fe3 = __ldg(&a.fsrc[3*E+2]); }
+		double feb = third*(fe1+fe2+fe3);
+		int i1 = __ldg(&a.node_id[J1]), i2 = __ldg(&a.node_id[J2]), i3 = __ldg(&a.node_id[J3]);
+		double ue[3], due[3];
+		ue[0] = (i1 >= 0) ? a.u[i1] : __ldg(&a.upresc[J1]);
+		ue[1] = (i2 >= 0) ? a.u[i2] : __ldg(&a.upresc[J2]);
+		ue[2] = (i3 >= 0) ? a.u[i3] : __ldg(&a.upresc[J3]);
+		due[0] = (i1 >= 0) ? a.du[i1] : 0.0;
+		due[1] = (i2 >= 0) ? a.du[i2] : 0.0;
+		due[2] = (i3 >= 0) ? a.du[i3] : 0.0;
+		double ueb = third * (ue[0] + ue[1] + ue[2]);
+		double dueb = third * (due[0] + due[1] + due[2]);
+		double Mhh_1_12 = twelfth*Area, MhB_3_20 = three_twentieth*Area, MBh_3_20 = MhB_3_20;
+		double MBB = (81.0/280.)*Area;
+		double a1 = bx*y23 + by*x32, a2 = bx*y31 + by*x13, a3 = bx*y12 + by*x21;
+		double C12 = y23*y31 + x32*x13, C13 = y23*y12 + x32*x21, C23 = y31*y12 + x13*x21;
+		double D12 = 0.25*invArea*((kx * y23 * y31) + (ky * x32 * x13));
+		double D13 = 0.25*invArea*((kx * y23 * y12) + (ky * x32 * x21));
+		double D23 = 0.25*invArea*((kx * y31 * y12) + (ky * x13 * x21));
+		double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
+		double hs = h_shock(a.hshock, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
+		double cbtil = shock_capture_tr(a.shock, kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb,
+		                                y23, y31, y12, x32, x13, x21, invArea, hs);
+		double Eu = w*cbtil + (1-w)*a.dold[E];
+		a.dold[E] = cbtil;
+		double KDD12 = 0.25*Eu*invArea*C12, KDD13 = 0.25*Eu*invArea*C13, KDD23 = 0.25*Eu*invArea*C23;
+		double Khh[3][3], KhB[3], KBh[3];
+		Khh[0][0] = -(D12 + D13) + sixth*a1 + R11 -(KDD12 + KDD13);
+		Khh[0][1] = D12 + sixth*a2 + R12 + KDD12;
+		Khh[0][2] = D13 + sixth*a3 + R12 + KDD13;
+		Khh[1][0] = D12 + sixth*a1 + R12 + KDD12;
+		Khh[1][1] = -(D12 + D23) + sixth*a2 + R11 -(KDD12 + KDD23);
+		Khh[1][2] = D23 + sixth*a3 + R12 + KDD23;
+		Khh[2][0] = D13 + sixth*a1 + R12 + KDD13;
+		Khh[2][1] = D23 + sixth*a2 + R12 + KDD23;
+		Khh[2][2] = -(D13 + D23) + sixth*a3 + R11 -(KDD13 + KDD23);
+		KhB[0] = nine_twentieth*(0.5*a1 + a2 + a3) + three_twentieth*gamma*Area;
+		KhB[1] = nine_twentieth*(a1 + 0.5*a2 + a3) + three_twentieth*gamma*Area;
+		KhB[2] = nine_twentieth*(a1 + a2 + 0.5*a3) + three_twentieth*gamma*Area;
+		KBh[0] = nine_forty_cents*a1 + three_twentieth*gamma*Area;
+		KBh[1] = nine_forty_cents*a2 + three_twentieth*gamma*Area;
+		KBh[2] = nine_forty_cents*a3 + three_twentieth*gamma*Area;
+		double KBB = -9*nine_forty_cents*(D12+D13+D23) + seventh*three_twentieth*(a1+ a2+ a3)
+		             + 9*seventh*nine_forty_cents*Area - Eu*invArea*(C12 + C13 + C23)/360.;
+		double Fh[3];
+		Fh[0] = twelfth*Area*(2*fe1 + fe2 + fe3);
+		Fh[1] = twelfth*Area*(fe1 + 2*fe2 + fe3);
+		Fh[2] = twelfth*Area*(fe1 + fe2 + 2*fe3);
+		double FB = three_twentieth*Area*(fe1 + fe2 + fe3);
+		const double alpha_dt_N2 = a.adt;                  // Alpha_Build * DeltaT_Build
+		double N2 = MBB + alpha_dt_N2*KBB;
+		double invN2 = 1.0/N2;
+		const double uBe = a.uB[E], duBe = a.aB[E];
+		double R2 = FB - MBB*duBe - KBB*uBe;
+		double M1[3][3], M2[3], N1[3], R1[3];
+		for (int i = 0; i < 3; i++) {
+			M1[i][0] = Mhh_1_12; M1[i][1] = Mhh_1_12; M1[i][2] = Mhh_1_12;
+			M1[i][i] += Mhh_1_12;
+			M2[i] = MBh_3_20 + alpha_dt_N2*KBh[i];
+			N1[i] = MhB_3_20 + alpha_dt_N2*KhB[i];
+			R1[i] = Fh[i] - MhB_3_20*duBe - KhB[i]*uBe;
+			R1[i] -= Mhh_1_12*due[i];
+			for (int j = 0; j < 3; j++) {
+				M1[i][j] += alpha_dt_N2*Khh[i][j];
+				R1[i] -= Mhh_1_12*due[j] + Khh[i][j]*ue[j];
+			}
+			R2 -= MBh_3_20*due[i] + KBh[i]*ue[i];
+		}
+		double *Me = a.ke + 9LL*E, *re = a.re + 12LL*E, *bb = a.bub + 5LL*E;
+		for (int i = 0; i < 3; i++) {
+			for (int j = 0; j < 3; j++) Me[3*i + j] = M1[i][j] - invN2*N1[i]*M2[j];
+			re[4*i] = R1[i] - invN2*N1[i]*R2;
+			re[4*i + 1] = 0.0; re[4*i + 2] = 0.0; re[4*i + 3] = 0.0;
+		}
+		bb[0] = invN2; bb[1] = R2; bb[2] = M2[0]; bb[3] = M2[1]; bb[4] = M2[2];
+	}
+}
+
+// calculate_DaB.c:8-29 and the bubble updates of Predictor_New.c:112-116:
+// DaB = invN2 (R2 - M2 . Da[lm]), aB += DaB, uB += (alpha dt) DaB.
+__global__ void k_bubble_correct(int nel, const int *__restrict__ lm, const double *__restrict__ bub,
+                                 const double *__restrict__ Da, int neq, double *aB, double *uB, double c)
+{
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nel; e += gridDim.x * blockDim.x) {
+		const double *b = bub + 5LL * e;
+		const int q1 = lm[3 * e], q2 = lm[3 * e + 1], q3 = lm[3 * e + 2];
+		const double d1 = q1 == neq ? 0.0 : Da[q1], d2 = q2 == neq ? 0.0 : Da[q2], d3 = q3 == neq ? 0.0 : Da[q3];
+		const double M2Da = b[2]*d1 + b[3]*d2 + b[4]*d3;
+		const double DaB = b[0]*(b[1] - M2Da);
+		aB[e] = aB[e] + 1.0*DaB;
+		uB[e] = uB[e] + c*DaB;
+	}
+}
+
+// Predictor_New.c:72-76 for the bubbles: uB += ((1 - alpha) dt) aB, aB = 0.
+__global__ void k_bubble_predict(int nel, double *aB, double *uB, double c)
+{
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nel; e += gridDim.x * blockDim.x) {
+		uB[e] = uB[e] + c*aB[e];
+		aB[e] = 0.0;
+	}
+}
+
+// uB_InitialSolution.c:4-41: the mean of the element's nodal values.
+__global__ void k_bubble_init(int nel, const int *__restrict__ vert, const int *__restrict__ node_id,
+                              const double *__restrict__ u, const double *__restrict__ upresc, double *uB,
+                              double *aB)
+{
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nel; e += gridDim.x * blockDim.x) {
+		double s = 0.0;
+		for (int k = 0; k < 3; k++) {
+			const int v = vert[3 * e + k], id = node_id[v];
+			s += id >= 0 ? u[id] : upresc[v];
+		}
+		uB[e] = s / 3;
+		aB[e] = 0.0;
+	}
+}
+
+extern "C" int fg_build_mfdd(femgpu_transport *t, double adt)
+{
+	BuildArgs a;
+	a.x = t->x; a.y = t->y; a.u = t->u; a.upresc = t->upresc; a.beta = t->beta; a.fsrc = t->fsrc;
+	a.vert = t->vert; a.node_id = t->node_id;
+	a.k = t->k; a.gamma = t->gamma; a.cbx = t->cbx; a.cby = t->cby;
+	a.nel = t->nel; a.shock = t->o.shock; a.hshock = t->o.hshock;
+	a.beta_const = t->beta_const; a.fsrc_zero = t->fsrc_zero;
+	a.ke = (t->o.scheme == FEMGPU_EBE) ? t->A : t->ke;
+	a.fe = NULL;
+	a.du = t->du; a.adt = adt; a.re = t->re; a.dold = t->dold;
+	a.uB = t->uB; a.aB = t->aB; a.bub = t->bub;
+	k_build_mfdd<<<fg_grid(t->nel, 128, 32), 128, 0, t->stream>>>(a);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_bubble_correct(femgpu_transport *t, double c)
+{
+	k_bubble_correct<<<fg_grid(t->nel), FG_TPB, 0, t->stream>>>(t->nel, t->lm, t->bub, t->Da, t->neq, t->aB, t->uB, c);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_bubble_predict(femgpu_transport *t, double c)
+{
+	k_bubble_predict<<<fg_grid(t->nel), FG_TPB, 0, t->stream>>>(t->nel, t->aB, t->uB, c);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_bubble_init(femgpu_transport *t)
+{
+	k_bubble_init<<<fg_grid(t->nel), FG_TPB, 0, t->stream>>>(t->nel, t->vert, t->node_id, t->u, t->upresc, t->uB,
+	                                                         t->aB);
+	return (int)cudaGetLastError();
 }
 
 extern "C" int fg_build_transient(femgpu_transport *t, int dd, double adt)

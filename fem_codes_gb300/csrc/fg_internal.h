@@ -126,6 +126,7 @@ typedef struct fg_krylov {
 	double *partials;               /* [nblk] reduction partials              */
 	fg_status *st;                  /* device status                          */
 	fg_status *st_host;             /* pinned host mirror                     */
+	int dsv;                        /* FGMRES: Arnoldi basis in double-single */
 } fg_krylov;
 
 /* Operator callbacks, stream-ordered, returning cudaError_t (> 0) or a
@@ -138,6 +139,11 @@ typedef struct fg_linop {
 	/* mixed precision (FGMRES): z = M^-1 p in FP32, and q = A z from an FP32
 	 * vector with FP64 (op32 == 0) or FP32 (op32 != 0) matrix values. */
 	int (*precond32)(void *ctx, const double *p, float *z, const int *active);
+	/* double-single Krylov basis (fg_krylov.dsv): z = M^-1 p from a
+	 * double-single p, and q = A p into a double-single q (pairs of floats,
+	 * 8 bytes per entry like the FP64 basis) */
+	int (*precond_dsin)(void *ctx, const void *p, double *z, const int *active);
+	int (*matvec_dsout)(void *ctx, const double *p, void *q, const int *active);
 	int (*matvec_xf)(void *ctx, const float *p, double *q, const int *active, int op32);
 } fg_linop;
 
@@ -177,6 +183,8 @@ struct femgpu_transport {
 	double *re;                     /* per element: load term + 3 products x3 */
 	double *dold;                   /* DD: previous shock parameter per elem */
 	double *uold, *Da, *u1, *u2;    /* predictor vectors (neq+1)             */
+	double *uB, *aB, *bub;          /* Predictor_New: bubble unknowns, rate, and
+	                                   invN2, R2, M2[3] per element          */
 
 	/* Krylov workspace */
 	int kmax;
@@ -217,6 +225,10 @@ int fg_assemble_transient(femgpu_transport *t);              /* A, R -> F     */
 int fg_tr_predict(femgpu_transport *t, double c);            /* uold, u, a    */
 int fg_tr_correct(femgpu_transport *t, double c);            /* a, u += Da    */
 int fg_tr_diff(femgpu_transport *t);                         /* Da = u - uold */
+int fg_build_mfdd(femgpu_transport *t, double adt);          /* Me, re, bub   */
+int fg_bubble_correct(femgpu_transport *t, double c);        /* DaB, aB, uB   */
+int fg_bubble_predict(femgpu_transport *t, double c);
+int fg_bubble_init(femgpu_transport *t);
 int fg_tr_axpy_zero(femgpu_transport *t, double c);          /* u += c a, a=0 */
 int fg_tr_lin(femgpu_transport *t, const double *p, const double *q, double cp, double cq); /* u=cp p-cq q */
 
@@ -228,6 +240,8 @@ int fg_csrmv32(int n, const int *IA, const int *JA, const float *AA, const float
                float *Q, const int *active, cudaStream_t s);
 int fg_csrmv64_fused(int n, const int *IA, const int *JA, const double *AA, const double *P,
                      double *Q, const int *active, cudaStream_t s);
+int fg_csrmv64_fused_ds(int n, const int *IA, const int *JA, const double *AA, const double *P,
+                        void *Q, const int *active, cudaStream_t s);
 int fg_diag_setup(femgpu_transport *t);
 int fg_precond(femgpu_transport *t, const double *p, double *z, const int *active);
 /* One restart cycle of the reference's left-preconditioned GMRES

@@ -156,47 +156,8 @@ template <typename T, bool FMA> __device__ __forceinline__ T fmsub(T x, T a, T b
 }
 
 // ---------------------------------------------------- double-single values
-// A value held as the unevaluated sum hi + lo of two floats (|lo| at most
-// half an ulp of hi): 48 significand bits on the FP32 pipes, which on this
-// part issue 64 times as many operations per clock as the FP64 pipe.  The
-// arithmetic is built from the error-free transformations of Knuth's two-sum
-// (a + b = s + e exactly) and of the fused-multiply-add two-product
-// (a * b = p + e exactly, e = fma(a, b, -p)); a product's cross terms and the
-// final addition of the low parts are rounded once each (the "sloppy"
-// double-single sum), so an operation errs by a few units of 2^-48 of its
-// operands -- as accurate as the preconditioner needs, not bit-identical.
-struct __align__(8) dsf { float hi, lo; };
-
-__device__ __forceinline__ dsf ds_two_sum(float a, float b)
-{
-	const float s = a + b, v = s - a;
-	return dsf{ s, (a - (s - v)) + (b - v) };
-}
-
-__device__ __forceinline__ dsf ds_fast_two_sum(float a, float b)     // |a| >= |b|
-{
-	const float s = a + b;
-	return dsf{ s, b - (s - a) };
-}
-
-// c + a * b
-__device__ __forceinline__ dsf ds_fma(dsf a, dsf b, dsf c)
-{
-	const float p = a.hi * b.hi;
-	float e = fmaf(a.hi, b.hi, -p);
-	e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
-	dsf s = ds_two_sum(c.hi, p);
-	s.lo += e + c.lo;
-	return ds_fast_two_sum(s.hi, s.lo);
-}
-
-__host__ __device__ __forceinline__ dsf ds_neg(dsf a) { return dsf{ -a.hi, -a.lo }; }
-
-__device__ __forceinline__ dsf ds_from(double v)
-{
-	const float h = __double2float_rn(v);
-	return dsf{ h, __double2float_rn(v - (double)h) };
-}
+// (fg_ds.cuh): the sweeps' values, multipliers and ring in float pairs.
+#include "fg_ds.cuh"
 
 template <> __device__ __forceinline__ dsf fmsub<dsf, true>(dsf x, dsf a, dsf b) { return ds_fma(ds_neg(a), b, x); }
 template <> __device__ __forceinline__ dsf mul(dsf a, dsf b) { return ds_fma(a, b, dsf{ 0.0f, 0.0f }); }
@@ -825,6 +786,14 @@ __global__ void k_perm_in_ds(const double *__restrict__ p, const int *__restrict
 {
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
 		in[ppos[i]] = ds_from(p[rows[i]]);
+}
+
+__global__ void k_perm_in_dsds(const dsf *__restrict__ p, const int *__restrict__ rows,
+                               const int *__restrict__ ppos, int n, dsf *in, const int *active)
+{
+	if (active && !*active) return;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		in[ppos[i]] = p[rows[i]];
 }
 
 __global__ void k_ds_to_double(const dsf *__restrict__ x, int n, double *z, const int *active)
@@ -2252,7 +2221,7 @@ static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, 
 // The double-single chain sweeps: gather into double-single slots, the
 // forward and backward chain-scan programs with double-single values, the
 // backward output (natural order, in the gather buffer) back to FP64.
-static int apply_ds(femgpu_transport *t, const double *p, double *z, const int *active)
+static int apply_ds(femgpu_transport *t, const double *p, const dsf *p_ds, double *z, const int *active)
 {
 	fg_ilu_sweeps &S = t->sweeps;
 	const fg_sweep &lo = S.lo64c, &up = S.up64c;
@@ -2260,7 +2229,8 @@ static int apply_ds(femgpu_transport *t, const double *p, double *z, const int *
 	const int n = t->neq;
 	int D, sb, bytes;
 	dsf *bl = (dsf *)S.bl64, *y = (dsf *)S.y64;
-	k_perm_in_ds<<<fg_grid(n), FG_TPB, 0, s>>>(p, lo.rows, lo.ppos, n, bl);
+	if (p_ds) k_perm_in_dsds<<<fg_grid(n), FG_TPB, 0, s>>>(p_ds, lo.rows, lo.ppos, n, bl, active);
+	else k_perm_in_ds<<<fg_grid(n), FG_TPB, 0, s>>>(p, lo.rows, lo.ppos, n, bl);
 	SweepArgs a;
 	a.err = &t->st->err;
 	a.active = active;
@@ -2285,10 +2255,23 @@ extern "C" int fg_ilu0_apply64(femgpu_transport *t, const double *p, double *z, 
 {
 	fg_ilu_sweeps &S = t->sweeps;
 	const bool fma = t->o.solver == FEMGPU_FGMRES;
-	if (fma && S.ds) return apply_ds(t, p, z, active);
+	if (fma && S.ds) return apply_ds(t, p, NULL, z, active);
 	if (fma && S.chain)
 		return apply_t<double, double, double>(t, S.lo64c, S.up64c, S.bl64, S.y64, p, z, active, true);
 	return apply_t<double, double, double>(t, S.lo64, S.up64, S.bl64, S.y64, p, z, active, fma);
+}
+
+// The double-single sweeps with a double-single input (the Krylov basis of
+// the double-single Arnoldi); available when fg_ilu0_ds_ready says so.
+extern "C" int fg_ilu0_ds_ready(const femgpu_transport *t)
+{
+	return t->sweeps.ds ? 1 : 0;
+}
+
+extern "C" int fg_ilu0_apply64_dsin(femgpu_transport *t, const void *p, double *z, const int *active)
+{
+	if (!t->sweeps.ds) return FEMGPU_E_NOT_BUILT;
+	return apply_ds(t, NULL, (const dsf *)p, z, active);
 }
 
 extern "C" int fg_ilu0_apply32(femgpu_transport *t, const double *p, float *z, const int *active)

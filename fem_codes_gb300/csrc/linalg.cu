@@ -12,6 +12,7 @@
 // they are rounded exactly like the reference compiled without contraction.
 // ILU(0) lives in ilu.cu.
 #include "fg_common.cuh"
+#include "fg_ds.cuh"
 #include "fg_gnn.h"
 #include "fg_amg.h"
 #include <math.h>
@@ -43,6 +44,12 @@ template <> struct mv_ops<float> {
 	static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
 };
 
+// The product's output type: FP64, FP32, or double-single.
+template <typename TO> __device__ __forceinline__ TO mv_out(double q);
+template <> __device__ __forceinline__ double mv_out<double>(double q) { return q; }
+template <> __device__ __forceinline__ float mv_out<float>(double q) { return (float)q; }
+template <> __device__ __forceinline__ dsf mv_out<dsf>(double q) { return ds_from(q); }
+
 template <typename TA, typename TP, typename TACC, typename TO, bool FUSED>
 __global__ void __launch_bounds__(MV_ROWS) k_csrmv_tile(int n, const int *__restrict__ IA,
                                                         const int *__restrict__ JA, const TA *__restrict__ AA,
@@ -71,7 +78,7 @@ __global__ void __launch_bounds__(MV_ROWS) k_csrmv_tile(int n, const int *__rest
 					const TACC a = (TACC)__ldg(&AA[j]), x = (TACC)__ldg(&P[__ldg(&JA[j])]);
 					q = FUSED ? fma(a, x, q) : op::add(q, op::mul(a, x));
 				}
-				Q[i] = (TO)q;
+				Q[i] = mv_out<TO>(q);
 			}
 			rs = re + 1;
 			continue;
@@ -110,7 +117,7 @@ __global__ void __launch_bounds__(MV_ROWS) k_csrmv_tile(int n, const int *__rest
 				for (int j = kb - k0; j < ke - k0; j++) q = fma(prod[j], prod[CAP + j], q);
 			else
 				for (int j = kb - k0; j < ke - k0; j++) q = op::add(q, prod[j]);
-			Q[i] = (TO)q;
+			Q[i] = mv_out<TO>(q);
 		}
 		__syncthreads();                                  // prod and kpos are reused by the next run
 		rs = re;
@@ -131,6 +138,14 @@ extern "C" int fg_csrmv64_fused(int n, const int *IA, const int *JA, const doubl
                                 double *Q, const int *active, cudaStream_t s)
 {
 	return launch_csrmv<double, double, double, double, true>(n, IA, JA, AA, P, Q, active, s);
+}
+
+// The fused product with its result in double-single (the Krylov basis of
+// the double-single Arnoldi).
+extern "C" int fg_csrmv64_fused_ds(int n, const int *IA, const int *JA, const double *AA, const double *P,
+                                   void *Q, const int *active, cudaStream_t s)
+{
+	return launch_csrmv<double, double, double, dsf, true>(n, IA, JA, AA, P, (dsf *)Q, active, s);
 }
 
 extern "C" int fg_csrmv64(int n, const int *IA, const int *JA, const double *AA, const double *P,
@@ -447,6 +462,87 @@ __global__ void __launch_bounds__(RED_TPB) k_cgs_update(const double *V, size_t 
 	if (last_block_total(part, partials, &st->ticket, &tot, sh)) *Hn = sqrt(tot);
 }
 
+// The same CGS kernels and the scaling with the basis in double-single (the
+// FGMRES basis on the FP32 pipes: a basis entry is a float pair of 8 bytes
+// like an FP64 one, each product and sum is a double-single operation, the
+// per-thread partial sums go to FP64 for the block and grid reductions).
+__global__ void __launch_bounds__(RED_TPB) k_mdot_ds(const dsf *V, size_t ldv, int n, int m, const dsf *w,
+                                                     double *partials, fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	__shared__ double sh[MD_J][RED_TPB / 32];
+	const int j0 = blockIdx.y * MD_J, G = gridDim.x;
+	dsf acc[MD_J];
+#pragma unroll
+	for (int q = 0; q < MD_J; q++) acc[q] = dsf{ 0.0f, 0.0f };
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += G * blockDim.x) {
+		const dsf wk = w[k];
+#pragma unroll
+		for (int q = 0; q < MD_J; q++)
+			if (j0 + q < m) acc[q] = ds_fma(V[(size_t)(j0 + q) * ldv + k], wk, acc[q]);
+	}
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+	for (int q = 0; q < MD_J; q++) {
+		double v = fg_warp_sum(ds_to_double(acc[q]));
+		if (lane == 0) sh[q][wid] = v;
+	}
+	__syncthreads();
+	if (threadIdx.x < MD_J && j0 + (int)threadIdx.x < m) {
+		double t = 0.0;
+		for (int q = 0; q < RED_TPB / 32; q++) t += sh[threadIdx.x][q];
+		partials[(size_t)(j0 + threadIdx.x) * G + blockIdx.x] = t;
+	}
+}
+
+// w -= sum_j h[j] v_j; norm != 0: Hn = ||w|| (last block).  Dynamic shared
+// memory: m double-single coefficients.
+__global__ void __launch_bounds__(RED_TPB) k_cgs_update_ds(const dsf *V, size_t ldv, int n, int m, dsf *w,
+                                                           const double *h, int norm, double *Hn,
+                                                           double *partials, fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	extern __shared__ dsf hneg[];
+	__shared__ double sh[32];
+	for (int j = threadIdx.x; j < m; j += blockDim.x) hneg[j] = ds_neg(ds_from(h[j]));
+	__syncthreads();
+	dsf part = dsf{ 0.0f, 0.0f };
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		dsf x = w[k];
+		for (int j = 0; j < m; j++) x = ds_fma(hneg[j], V[(size_t)j * ldv + k], x);
+		w[k] = x;
+		part = ds_fma(x, x, part);
+	}
+	if (!norm) return;
+	double p = block_sum(ds_to_double(part), sh);
+	double tot;
+	if (last_block_total(p, partials, &st->ticket, &tot, sh)) *Hn = sqrt(tot);
+}
+
+// u := u / h in double-single; from_double: u holds FP64 values (read, then
+// overwritten in place by their double-single quotients).
+__global__ void k_scale_ds(dsf *u, int n, const double *h, int from_double, fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	__shared__ dsf sc;
+	if (threadIdx.x == 0) sc = ds_from(1.0 / *h);
+	__syncthreads();
+	const dsf zero = dsf{ 0.0f, 0.0f };
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		const dsf x = from_double ? ds_from(((const double *)u)[k]) : u[k];
+		u[k] = ds_fma(x, sc, zero);
+	}
+}
+
+// FP64 values to double-single in place (an operator without a double-single
+// output).
+__global__ void k_to_ds(double *x, int n, const int *active)
+{
+	if (active && !*active) return;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+		((dsf *)x)[k] = ds_from(x[k]);
+}
+
 // Orthogonalisation of the Arnoldi steps of restart cycle `cycle': 0 MGS
 // (one fused kernel per basis vector), 1 CGS, 2 CGS with one
 // re-orthogonalisation (CGS2), 3 CGS in a solve's first cycle and CGS2 in
@@ -597,17 +693,25 @@ extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 	size_t ldv = k->ldv;
 	double *V = k->V;
 	int *active = &k->st->active;
+	// the double-single basis (FP64 arithmetic otherwise: the residual, the
+	// Hessenberg matrix, the Givens rotations, Z and X stay FP64)
+	const bool dsv = k->dsv && !mixed && op->precond_dsin && op->matvec_dsout;
 	if (mixed && (!op->precond32 || !op->matvec_xf || !k->Z32)) return FEMGPU_E_ARG;
 	if (!mixed && !k->Z) return FEMGPU_E_ARG;
 	if ((rc = op->matvec(op->ctx, X, V, nullptr))) return rc;
 	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, k->ge, k->partials, k->st, 0);
-	k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, k->ge, k->st);
+	if (dsv) k_scale_ds<<<fg_grid(n), FG_TPB, 0, s>>>((dsf *)V, n, k->ge, 1, k->st);
+	else k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, k->ge, k->st);
 	for (int i = 0; i < kmax; i++) {
 		double *v = V + (size_t)i * ldv, *w = V + (size_t)(i + 1) * ldv;
 		if (mixed) {
 			float *z = k->Z32 + (size_t)i * ldv;
 			if ((rc = op->precond32(op->ctx, v, z, active))) return rc;
 			if ((rc = op->matvec_xf(op->ctx, z, w, active, mixed == 2))) return rc;
+		} else if (dsv) {
+			double *z = k->Z + (size_t)i * ldv;
+			if ((rc = op->precond_dsin(op->ctx, v, z, active))) return rc;
+			if ((rc = op->matvec_dsout(op->ctx, z, w, active))) return rc;
 		} else {
 			double *z = k->Z + (size_t)i * ldv;
 			if (op->precond) {
@@ -617,7 +721,24 @@ extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 			}
 			if ((rc = op->matvec(op->ctx, z, w, active))) return rc;
 		}
-		const int gs = gs_mode(cycle);
+		int gs = gs_mode(cycle);
+		if (dsv && gs == 0) gs = 1;                        // MGS has no double-single form
+		if (dsv) {
+			const int m = i + 1;
+			double *h = k->partials + (size_t)G * (kmax + 1);
+			for (int pass = 0; pass < gs; pass++) {
+				const int last = pass == gs - 1;
+				k_mdot_ds<<<dim3(G, (m + MD_J - 1) / MD_J), RED_TPB, 0, s>>>((const dsf *)V, ldv, n, m, (const dsf *)w,
+				                                                           k->partials, k->st);
+				k_mdot_fin<<<m, 32, 0, s>>>(k->partials, G, m, h, k->H + i, ldh, pass, k->st);
+				k_cgs_update_ds<<<G, RED_TPB, sizeof(dsf) * (size_t)m, s>>>((const dsf *)V, ldv, n, m, (dsf *)w, h, last,
+				                                                         k->H + (i + 1) * ldh + i, k->partials,
+				                                                         k->st);
+			}
+			k_scale_ds<<<fg_grid(n), FG_TPB, 0, s>>>((dsf *)w, n, k->H + (i + 1) * ldh + i, 0, k->st);
+			k_givens<<<1, 1, 0, s>>>(k->H, ldh, k->cs, k->sn, k->ge, i, kmax, k->st);
+			continue;
+		}
 		if (gs == 0) {
 			for (int j = 0; j <= i + 1; j++)
 				k_mgs<<<G, RED_TPB, 0, s>>>(V, ldv, n, i, j, k->H, ldh, k->partials, k->st);
@@ -682,6 +803,34 @@ static int tr_precond(void *c, const double *p, double *z, const int *a)
 {
 	return fg_precond((femgpu_transport *)c, p, z, a);
 }
+extern "C" int fg_ilu0_apply64_dsin(femgpu_transport *t, const void *p, double *z, const int *active);
+extern "C" int fg_ilu0_ds_ready(const femgpu_transport *t);
+static int tr_precond_dsin(void *c, const void *p, double *z, const int *a)
+{
+	return fg_ilu0_apply64_dsin((femgpu_transport *)c, p, z, a);
+}
+static int tr_matvec_dsout(void *c, const double *p, void *q, const int *a)
+{
+	femgpu_transport *t = (femgpu_transport *)c;
+	if (t->o.scheme == FEMGPU_CSR) return fg_csrmv64_fused_ds(t->neq, t->IA, t->JA, t->A, p, q, a, t->stream);
+	int rc = fg_matvec(t, p, (double *)q, a);
+	if (rc) return rc;
+	k_to_ds<<<fg_grid(t->neq), FG_TPB, 0, t->stream>>>((double *)q, t->neq, a);
+	return (int)cudaGetLastError();
+}
+
+// The double-single basis for FP64 FGMRES with the double-single ILU(0)
+// sweeps (FEMGPU_KRYLOV_DS=0 keeps the FP64 basis).
+static int krylov_ds(const femgpu_transport *t)
+{
+	static int env = -1;
+	if (env < 0) {
+		const char *e = getenv("FEMGPU_KRYLOV_DS");
+		env = (e && e[0] == '0') ? 0 : 1;
+	}
+	return env && t->o.solver == FEMGPU_FGMRES && t->o.precision == FEMGPU_FP64 &&
+	       t->o.precond == FEMGPU_PREC_ILU0 && fg_ilu0_ds_ready(t);
+}
 static int tr_precond32(void *c, const double *p, float *z, const int *a)
 {
 	return fg_precond32((femgpu_transport *)c, p, z, a);
@@ -701,6 +850,9 @@ extern "C" void fg_transport_krylov(femgpu_transport *t, fg_krylov *k, fg_linop 
 	op->precond = tr_precond;
 	op->precond32 = tr_precond32;
 	op->matvec_xf = tr_matvec_xf;
+	op->precond_dsin = tr_precond_dsin;
+	op->matvec_dsout = tr_matvec_dsout;
+	k->dsv = krylov_ds(t);
 }
 
 extern "C" int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, int first)

@@ -41,6 +41,11 @@ int femgpu_transport_set_transient(femgpu_transport *t, const femgpu_transient_o
 		fgh_set_error("CAUDD shock capturing belongs to the DD build (setStabilizationForm.c:67)");
 		return FEMGPU_E_ARG;
 	}
+	if (o->method < FEMGPU_TI_PREDICTOR1 || o->method > FEMGPU_TI_PREDICTOR2 ||
+	    (o->method == FEMGPU_TI_PREDICTOR2 && o->stab != FEMGPU_STAB_DD)) {
+		fgh_set_error("time integration %d with stabilisation %d (setStabilizationForm.c:7-61)", o->method, o->stab);
+		return FEMGPU_E_ARG;
+	}
 	n1 = (size_t)t->neq + 1;
 	if (!t->du) {
 		if (fgh_dmalloc((void **)&t->du, sizeof(double) * n1) ||
@@ -51,6 +56,16 @@ int femgpu_transport_set_transient(femgpu_transport *t, const femgpu_transient_o
 			return FEMGPU_E_NOMEM;
 		if (t->o.scheme != FEMGPU_EBE && !t->ke && fgh_dmalloc((void **)&t->ke, sizeof(double) * 9 * (size_t)t->nel))
 			return FEMGPU_E_NOMEM;
+	}
+	if (o->method == FEMGPU_TI_PREDICTOR2 && !t->uB) {
+		if (fgh_dmalloc((void **)&t->uB, sizeof(double) * (size_t)t->nel) ||
+		    fgh_dmalloc((void **)&t->aB, sizeof(double) * (size_t)t->nel) ||
+		    fgh_dmalloc((void **)&t->bub, sizeof(double) * 5 * (size_t)t->nel))
+			return FEMGPU_E_NOMEM;
+	}
+	if (t->uB) {
+		CK(cudaMemsetAsync(t->uB, 0, sizeof(double) * (size_t)t->nel, t->stream));
+		CK(cudaMemsetAsync(t->aB, 0, sizeof(double) * (size_t)t->nel, t->stream));
 	}
 	CK(cudaMemsetAsync(t->du, 0, sizeof(double) * n1, t->stream));
 	CK(cudaMemsetAsync(t->Da, 0, sizeof(double) * n1, t->stream));
@@ -63,9 +78,20 @@ int femgpu_transport_set_transient(femgpu_transport *t, const femgpu_transient_o
 	return 0;
 }
 
+int femgpu_transport_set_bubbles(femgpu_transport *t, const double *uB_host, const double *aB_host)
+{
+	if (!t) return FEMGPU_E_ARG;
+	if (!t->transient || !t->uB) { fgh_set_error("set_bubbles: not a Predictor2 context"); return FEMGPU_E_NOT_BUILT; }
+	if (uB_host) CK(cudaMemcpyAsync(t->uB, uB_host, sizeof(double) * (size_t)t->nel, cudaMemcpyHostToDevice, t->stream));
+	if (aB_host) CK(cudaMemcpyAsync(t->aB, aB_host, sizeof(double) * (size_t)t->nel, cudaMemcpyHostToDevice, t->stream));
+	CK(cudaStreamSynchronize(t->stream));
+	return 0;
+}
+
 static int build_transient_dev(femgpu_transport *t)
 {
-	KR(fg_build_transient(t, t->tr.stab == FEMGPU_STAB_DD, t->tr.alpha * t->tr.dt));
+	if (t->tr.method == FEMGPU_TI_PREDICTOR2) KR(fg_build_mfdd(t, t->tr.alpha * t->tr.dt));
+	else KR(fg_build_transient(t, t->tr.stab == FEMGPU_STAB_DD, t->tr.alpha * t->tr.dt));
 	KR(fg_assemble_transient(t));
 	t->built = 1;
 	t->factored = 0;
@@ -110,7 +136,7 @@ static int stop_corr(const femgpu_transient_opts *o, double norm_a, double norm_
 typedef struct {
 	femgpu_transport *t;
 	double Alpha, DeltaT, AlphaB, DeltaTB;
-	int tag, stage;
+	int tag, stage, bubble;
 	double *u_hist;
 	int *ncorr, *iters, iters_cap;
 } tr_loop;
@@ -127,7 +153,8 @@ static int multicorrect(tr_loop *L, double c)
 	do {
 		int it = 0;
 		i++;
-		KR(fg_build_transient(t, dd, dd ? L->AlphaB * L->DeltaTB : L->Alpha * L->DeltaT));
+		if (L->bubble) KR(fg_build_mfdd(t, L->AlphaB * L->DeltaTB));
+		else KR(fg_build_transient(t, dd, dd ? L->AlphaB * L->DeltaTB : L->Alpha * L->DeltaT));
 		KR(fg_assemble_transient(t));
 		t->built = 1;
 		t->factored = 0;
@@ -135,6 +162,7 @@ static int multicorrect(tr_loop *L, double c)
 		rc = fgh_transport_gmres(t, t->F, t->Da, &it);
 		if (rc && rc != FEMGPU_E_NOT_CONVERGED) return rc;    /* gmres stops at lmax cycles, as pgmres */
 		if (L->iters && i <= L->iters_cap) L->iters[(size_t)L->stage * L->iters_cap + (i - 1)] = it;
+		if (L->bubble) KR(fg_bubble_correct(t, c));          /* calculate_DaB, aB, uB */
 		KR(fg_tr_correct(t, c));
 		KR(dnorm(t, t->du, &norm_a));
 		KR(dnorm(t, t->Da, &norm_Da));
@@ -192,7 +220,21 @@ int femgpu_transport_predictor(femgpu_transport *t, const double *u0_host, int m
 	L.t = t; L.tag = 1; L.u_hist = u_hist; L.ncorr = ncorr; L.iters = iters; L.iters_cap = iters_cap;
 	L.Alpha = alpha; L.DeltaT = dt; L.AlphaB = alpha; L.DeltaTB = dt;
 
-	if (o->method == FEMGPU_TI_PREDICTOR1) {
+	if (o->method == FEMGPU_TI_PREDICTOR2) {
+		/* Predictor_New.c:52-123 */
+		const double c1 = (1.0 - alpha) * dt, c2 = alpha * dt;
+		KR(fg_bubble_init(t));                                /* uB_InitialSolution, aB = 0 */
+		L.bubble = 1;
+		do {
+			step++;
+			time += dt;
+			KR(fg_tr_predict(t, c1));                         /* u_old = u, u += c1 a, a = 0 */
+			KR(fg_bubble_predict(t, c1));                     /* uB += c1 aB, aB = 0 */
+			KR(multicorrect(&L, c2));
+			if (t_hist) t_hist[step - 1] = time;
+			KR(stop_time(&L, t->uold, time, &done));
+		} while (!done && step < max_steps);
+	} else if (o->method == FEMGPU_TI_PREDICTOR1) {
 		/* Predictor_Old.c:62-136 */
 		const double c1 = (1.0 - alpha) * dt, c2 = alpha * dt;
 		do {

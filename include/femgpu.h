@@ -242,13 +242,22 @@ typedef struct femgpu_transient_opts {
  * Predictor1_TRBDF2 (Predictor_Old_TRBDF2.c:3-179: a trapezoidal stage of
  * (2 - sqrt 2) dt, then a BDF2 stage), each with the reference's own
  * Alpha / DeltaT bookkeeping for the builds. */
-enum femgpu_time_integration { FEMGPU_TI_PREDICTOR1 = 0, FEMGPU_TI_BDF = 1, FEMGPU_TI_TRBDF2 = 2 };
+enum femgpu_time_integration { FEMGPU_TI_PREDICTOR1 = 0, FEMGPU_TI_BDF = 1, FEMGPU_TI_TRBDF2 = 2,
+                               FEMGPU_TI_PREDICTOR2 = 3 };
+/* Predictor2 (Predictor_New.c:3-137, DD stabilisation only): the element
+ * bubbles are unknowns of the time loop -- uB starts at each element's mean
+ * nodal value (uB_InitialSolution.c), the build is Build_M_F_DD
+ * (Build_M_F_DD.c:6-218: the bubble row condensed into the element matrix),
+ * and after every solve calculate_DaB.c updates the bubbles. */
 int femgpu_transport_set_transient(femgpu_transport *ctx, const femgpu_transient_opts *o);
 /* One transient Build on the state (u, a) (host [neq+1]; NULL: the context's):
  * R_host [neq+1] the residual, A_host the storage values (as
  * femgpu_transport_build); each call advances the DD state. */
 int femgpu_transport_build_transient(femgpu_transport *ctx, const double *u_host, const double *a_host,
 		double *R_host, double *A_host);
+/* The bubble state (Predictor2) for the next femgpu_transport_build_transient:
+ * uB_host, aB_host [nel] (NULL: leave as is). */
+int femgpu_transport_set_bubbles(femgpu_transport *ctx, const double *uB_host, const double *aB_host);
 /* The time loop of opts.method from u0_host [neq+1] (the problem's
  * InitialSolution; a = 0, a fresh DD state).  Predictor1: per step
  * u += (1-alpha) dt a, a = 0, then corrections Build -> precond_setup ->

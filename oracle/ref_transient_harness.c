@@ -10,8 +10,9 @@
  * h_shock options, the assembly pointers, csrmv / ebemv / edemv, the NOT /
  * Diag / ILU(0) preconditioners, the CONE / CONE2 / CARTOLA / PUDIM
  * plug-ins, and the time loops themselves: 00_CommonFiles/Time_Integration/
- * Predictor_Old.c, Predictor_Old_BDF.c and Predictor_Old_TRBDF2.c with the
- * stop criteria of Criteria.c.
+ * Predictor_Old.c, Predictor_Old_BDF.c, Predictor_Old_TRBDF2.c and
+ * Predictor_New.c (with Build_M_F_DD.c, calculate_DaB.c, uB_InitialSolution.c)
+ * with the stop criteria of Criteria.c.
  *
  * One documented adapter: the driver's solver pointer takes (B, X)
  * (TranspEquation.h: solver(P, M, FS, FF, B, X)), while the shipped pgmres.c
@@ -107,13 +108,15 @@ static int solver_rec(ParametersType *P, MatrixDataType *M, FemStructsType *FS, 
  *   problem: 0 CONE, 1 CONE2, 2 CARTOLA, 3 PUDIM; ntype: Node Type (1 free, 0 prescribed)
  *   stab "SUPG" | "DD"; shock "CAU" | "CAUDD" | "YZBeta"; hshock "2sqrtArea" | "Option1" | "Option2"
  *   stopmc "ITERATION" | "NORM"; steady "YES" | "NOT"
- *   tint "Predictor1" | "Predictor1_BDF" | "Predictor1_TRBDF2" (setStabilizationForm.c:10-19)
+ *   tint "Predictor1" | "Predictor1_BDF" | "Predictor1_TRBDF2" | "Predictor2" (setStabilizationForm.c:10-58;
+ *   Predictor2 runs Predictor_New with Build_M_F_DD)
  * Outputs:
  *   info [5] = neq, nnzero, nedge, bandwidth after reordering, (out) time checks; node_id [nnodes]
  *   beta [2*nel], fsrc [3*nel], upresc [nnodes]: the plug-ins as Build evaluates them
  *   u0 [neq+1]: the plug-in's initial solution
  *   IA/JA/sbe (CSR) or lm2 (JA, 2*nedge) / EDGE_by_Element (sbe, 3*nel) / order (3*nel) (EDE)
- *   two consecutive Builds on (ub, dub) (the DD build keeps per-element state):
+ *   two consecutive Builds on (ub, dub) (the DD builds keep per-element state; Build_M_F_DD also
+ *   reads the element bubbles ubB, dubB [nel]):
  *   A1, R1 and A2, R2 (storage values EBE 9*nel / EDE 4*(nedge+1) / CSR nnz+1; R [neq+1])
  *   then the time loop from u0, stopped after maxsteps time checks: per stage (multicorrection
  *   loop) uhist [cap*(neq+1)], ncorr [cap], iters [cap*64] (GMRES iterations of each correction),
@@ -126,8 +129,9 @@ int ref_transient_run(int nnodes, const double *x, const double *y, const int *n
                       double dt, double final_time, double nonlin_tol, int max_corr, double time_tol, double stab_tol,
                       int kmax, int lmax, double tol, int *info, int *node_id, double *beta, double *fsrc,
                       double *upresc, double *u0, int *IA_out, int *JA_out, int *sbe_out, int *order_out,
-                      const double *ub, const double *dub, double *A1, double *R1, double *A2, double *R2,
-                      int maxsteps, double *uhist, double *thist, int *ncorr, int *iters)
+                      const double *ub, const double *dub, const double *ubB, const double *dubB, double *A1,
+                      double *R1, double *A2, double *R2, int maxsteps, double *uhist, double *thist, int *ncorr,
+                      int *iters)
 {
 	int I, J, neq;
 	ParametersType *P = mycalloc("P", 1, sizeof(ParametersType));
@@ -239,7 +243,8 @@ int ref_transient_run(int nnodes, const double *x, const double *y, const int *n
 	FF->precondR = NO_precond;
 	FF->scaling = noscale;
 	FF->unscaling = nounscale;
-	FOF->Build = strcasecmp(stab, "DD") == 0 ? Build_M_K_R_DD : Build_M_K_R_SUPG;
+	int predictor2 = strcasecmp(tint, "Predictor2") == 0;
+	FOF->Build = predictor2 ? Build_M_F_DD : strcasecmp(stab, "DD") == 0 ? Build_M_K_R_DD : Build_M_K_R_SUPG;
 	FF->ShockCapture = strcasecmp(shock, "YZBeta") == 0 ? YZBeta_ShockCapture
 	                 : strcasecmp(shock, "CAUDD") == 0 ? CAU_DD_ShockCapture : CAU_ShockCapture;
 	FF->h_shock = strcasecmp(hshock, "Option1") == 0 ? h_shock_Option1
@@ -262,11 +267,22 @@ int ref_transient_run(int nnodes, const double *x, const double *y, const int *n
 		FF->InitialSolution(P, Node, u0);
 	}
 
-	/* two Builds on (ub, dub), fresh per-element state */
+	/* two Builds on (ub, dub) (and the bubbles (ubB, dubB) for Build_M_F_DD),
+	 * fresh per-element state */
 	{
 		double *dold = mycalloc("delta_old", nel, sizeof(double));
 		AuxBuildStructuresType *aux = mycalloc("aux", 1, sizeof(AuxBuildStructuresType));
+		double **M2 = mycalloc("M2", nel, sizeof(double *)), *M2aux = mycalloc("M2aux", 3 * nel, sizeof(double));
+		double **R2b = mycalloc("R2", nel, sizeof(double *)), *R2aux = mycalloc("R2aux", nel, sizeof(double));
+		double *uBb = mycalloc("uB", nel, sizeof(double)), *duBb = mycalloc("duB", nel, sizeof(double));
+		for (I = 0; I < nel; I++) { M2[I] = M2aux + 3 * I; R2b[I] = R2aux + I; }
 		aux->tolerance = stab_tol;
+		aux->M2 = M2; aux->R2 = R2b; aux->invN2 = mycalloc("invN2", nel, sizeof(double));
+		if (predictor2) {
+			memcpy(uBb, ubB, sizeof(double) * nel);
+			memcpy(duBb, dubB, sizeof(double) * nel);
+		}
+		FS->uB = uBb; FS->duB = duBb;
 		FS->AuxBuild = aux;
 		FS->delta_old = dold;
 		P->Alpha_Build = alpha;
@@ -280,7 +296,8 @@ int ref_transient_run(int nnodes, const double *x, const double *y, const int *n
 		memcpy(A2, ebe || ede ? M->Aaux : M->AA, sizeof(double) * nA);
 		memcpy(R2, F, sizeof(double) * (neq + 1));
 		free(dold);
-		free(aux);
+		free(aux->invN2); free(aux);
+		free(M2); free(M2aux); free(R2b); free(R2aux); free(uBb); free(duBb);
 		memset(u, 0, sizeof(double) * (neq + 1));
 	}
 
@@ -294,6 +311,7 @@ int ref_transient_run(int nnodes, const double *x, const double *y, const int *n
 	FOF->solver = solver_rec;
 	if (strcasecmp(tint, "Predictor1_BDF") == 0) Predictor_Old_BDF(P, M, FS, FF, FOF);
 	else if (strcasecmp(tint, "Predictor1_TRBDF2") == 0) Predictor_Old_TRBDF2(P, M, FS, FF, FOF);
+	else if (predictor2) Predictor_New(P, M, FS, FF, FOF);
 	else Predictor_Old(P, M, FS, FF, FOF);
 	info[4] = g_tcheck;
 	return g_stage < g_cap ? g_stage : g_cap;

@@ -544,6 +544,11 @@ TT_CASES = {
                                            shock="CAUDD", tint="Predictor1_TRBDF2", dt=0.05, maxsteps=6),
     "tt_cartola16_ebe_diag_supg_trbdf2": dict(problem="CARTOLA", n=16, scheme="EBE", precond="Diag",
                                               tint="Predictor1_TRBDF2", dt=0.01, maxsteps=6),
+    "tt_cone16_csr_ilu0_dd_predictor2": dict(problem="CONE", n=16, scheme="CSR", reord="SYMRCM", precond="ILU0",
+                                             stab="DD", shock="CAUDD", tint="Predictor2"),
+    "tt_cone2_12_ebe_diag_dd_predictor2": dict(problem="CONE2", n=12, scheme="EBE", precond="Diag", stab="DD",
+                                               shock="CAU", hshock="Option1", tint="Predictor2", dt=0.05,
+                                               final=0.5, stopmc="NORM", max_corr=3),
 }
 
 
@@ -553,7 +558,7 @@ def transient_lib():
     f.restype = ctypes.c_int
     s, d, i = ctypes.c_char_p, ctypes.c_double, ctypes.c_int
     f.argtypes = [i, _dp, _dp, _ip, i, _ip, i, s, s, s, s, s, s, s, s, s, d, d, d, d, i, d, d, i, i, d,
-                  _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp,
+                  _ip, _ip, _dp, _dp, _dp, _dp, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                   i, _dp, _dp, _ip, _ip]
     return lib
 
@@ -585,6 +590,8 @@ def run_transient(lib, name, case):
     ub = rng.uniform(-0.5, 1.5, neq + 1)
     dub = rng.uniform(-1.0, 1.0, neq + 1)
     ub[neq] = dub[neq] = 0.0
+    ubB = rng.uniform(-0.5, 1.5, ne)
+    dubB = rng.uniform(-1.0, 1.0, ne)
     A1, A2 = np.zeros(cap), np.zeros(cap)
     R1, R2 = np.zeros(neq + 1), np.zeros(neq + 1)
     ms = c["maxsteps"]
@@ -597,12 +604,13 @@ def run_transient(lib, name, case):
         e(c["scheme"]), e(c["reord"]), e(c["precond"]), e(c["stab"]), e(c["shock"]), e(c["hshock"]),
         e(c["stopmc"]), e(c["steady"]), e(c["tint"]), c["alpha"], c["dt"], c["final"], c["nonlin_tol"], c["max_corr"],
         c["time_tol"], c["stab_tol"], c["kmax"], c["lmax"], c["tol"], info, node_id, beta, fsrc, upresc, u0,
-        IA, JA, sbe, order, ub, dub, A1, R1, A2, R2, ms, uh, th, nc, its)
+        IA, JA, sbe, order, ub, dub, ubB, dubB, A1, R1, A2, R2, ms, uh, th, nc, its)
     neq_r, nnz, nedge = int(info[0]), int(info[1]), int(info[2])
     assert neq_r == neq
     nA = {"CSR": nnz + 1, "EDE": 4 * (nedge + 1), "EBE": 9 * ne}[c["scheme"]]
     out = dict(x=m.x, y=m.y, vert=m.vert, node_type=ntype, neq=neq, nnz=nnz, nedge=nedge, node_id=node_id,
                beta=beta.reshape(ne, 2), fsrc=fsrc.reshape(ne, 3), upresc=upresc, u0=u0, ub=ub, dub=dub,
+               ubB=ubB, dubB=dubB,
                A1=A1[:nA], R1=R1, A2=A2[:nA], R2=R2, stages=stages, tchecks=int(info[4]),
                uhist=uh.reshape(cap, neq + 1)[:stages], thist=th[:int(info[4])], ncorr=nc[:stages],
                iters=its.reshape(cap, 64)[:stages], meta=np.array(repr(c)))

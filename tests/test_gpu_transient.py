@@ -3,9 +3,10 @@ the reference's own run (tests/golden/tt_*.npz, generated by
 oracle/ref_transient_harness.c from the reference's sources):
 
 * the storage pattern and node numbering (CSR with or without SYMRCM, EDE);
-* two consecutive Builds on a seeded state (u, a) -- Build_M_K_R_SUPG or
-  Build_M_K_R_DD, whose second build reads the first one's per-element shock
-  parameter -- matrix storage and residual bit-identical;
+* two consecutive Builds on a seeded state (u, a) -- Build_M_K_R_SUPG,
+  Build_M_K_R_DD or Build_M_F_DD (with seeded bubbles), the DD builds' second
+  build reading the first one's per-element shock parameter -- matrix storage
+  and residual bit-identical;
 * the reference's time loop (Predictor_Old, Predictor_Old_BDF or
   Predictor_Old_TRBDF2) from the problem's initial solution: u at the end of
   every multicorrection stage within 1e-8 relative, the same times and
@@ -20,7 +21,9 @@ the device and reference runs agree to 4e-15 after the first step, and that
 shock term amplifies the reductions' rounding differences about x3-5 per
 step, past 1e-8 after 11 steps); BDF2
 on CONE (CSR, SYMRCM, ILU(0)) and TR-BDF2 on CONE2 (DD + CAUDD) and CARTOLA
-(EBE, Diag)."""
+(EBE, Diag); Predictor_New with Build_M_F_DD (the element bubbles as unknowns
+of the time loop) on CONE (CSR, SYMRCM, ILU(0), CAUDD) and CONE2 (EBE, Diag,
+CAU, Option1, NORM)."""
 import ast
 import glob
 import os
@@ -63,6 +66,8 @@ def test_transient_builds_and_predictor(gpu_lib, name):
         if c["scheme"] == "CSR":
             assert np.array_equal(pat["IA"], g["IA"]) and np.array_equal(pat["JA"], g["JA"]), "CSR pattern"
             assert np.array_equal(pat["sbe"], g["sbe"]), "CSR_by_Element"
+        if c["tint"].upper() == "PREDICTOR2":
+            T.set_bubbles(g["ubB"], g["dubB"])
         R1, A1 = T.build_transient(g["ub"], g["dub"], want_matrix=True)
         assert np.array_equal(A1, g["A1"]), "first build: matrix"
         assert np.array_equal(R1[:neq], g["R1"][:neq]), "first build: residual"
