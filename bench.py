@@ -385,7 +385,7 @@ def run_ours(a):
     else:
         alg = nnz * 12 + (neq + 1) * 4 + 2 * neq * 8
         t_k = kern["spmv_f64_fused"]
-        name = "k_csrmv_tile<double, fused> (FP64 CSR, row tiles, coalesced slice staged in shared memory)"
+        name = "k_sellmv<double, fused> (FP64 CSR product over the SELL-32 copy, fused multiply-adds)"
     achieved = alg / (t_k * 1e-3) / 1e9
     traffic = read_traffic(dom)
     spmv_bytes = nnz * 12 + (neq + 1) * 4 + 2 * neq * 8
@@ -400,11 +400,12 @@ def run_ours(a):
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6.8 TB/s"},
-        "matvec": {"kernel": "k_csrmv_tile<double, fused> (FP64 CSR, the FGMRES operator: fused multiply-adds)",
+        "matvec": {"kernel": "k_sellmv<double, fused> (FP64 CSR over the SELL-32 copy, the FGMRES operator: fused "
+                             "multiply-adds)",
                    "GB/s": spmv_bytes / (kern["spmv_f64_fused"] * 1e-3) / 1e9,
                    "frac": spmv_bytes / (kern["spmv_f64_fused"] * 1e-3) / 1e9 / peak,
                    "us": kern["spmv_f64_fused"] * 1e3, "bytes": spmv_bytes,
-                   "exact_kernel": "k_csrmv_tile<double> (csrmv.c's rounding, bit-identical; FP64-pipe bound)",
+                   "exact_kernel": "k_sellmv<double> (csrmv.c's rounding, bit-identical; FP64-pipe bound)",
                    "exact_us": kern["spmv_f64"] * 1e3, "exact_GB/s": spmv_gbs, "exact_frac": spmv_gbs / peak,
                    "f32_us": kern["spmv_f32"] * 1e3,
                    "f32_GB/s": (nnz * 8 + (neq + 1) * 4 + 2 * neq * 4) / (kern["spmv_f32"] * 1e-3) / 1e9},
@@ -600,9 +601,8 @@ def kernel_times(T, s, a, reps=10):
     s.wait_stream(torch.cuda.current_stream())
     out["spmv_f64"] = timeit(lambda: L.femgpu_transport_matvec_dev(T.handle, vp(x.data_ptr()), vp(y.data_ptr())))
     # the FGMRES operator: the same product with fused multiply-adds
-    IAd, JAd, AAd = T.csr_dev()
-    out["spmv_f64_fused"] = timeit(lambda: L.femgpu_csrmv_f64_fused(T.neq, vp(IAd), vp(JAd), vp(AAd), vp(x.data_ptr()),
-                                                                     vp(y.data_ptr()), vp(s.cuda_stream)))
+    out["spmv_f64_fused"] = timeit(lambda: L.femgpu_transport_operator_dev(T.handle, vp(x.data_ptr()),
+                                                                           vp(y.data_ptr())))
     out["ilu0_apply_f64"] = timeit(lambda: L.femgpu_transport_precond_dev(T.handle, vp(x.data_ptr()),
                                                                           vp(y.data_ptr())))
     out["ilu0_apply_f32"] = timeit(lambda: L.femgpu_transport_precond32_dev(T.handle, vp(x.data_ptr()),

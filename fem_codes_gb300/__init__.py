@@ -154,6 +154,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_euler_set_slip": [_vp, _vp, _vp, _vp],
         "femgpu_transport_set_transient": [_vp, _vp],
         "femgpu_transport_set_bubbles": [_vp, _vp, _vp],
+        "femgpu_transport_operator_dev": [_vp, _vp, _vp],
         "femgpu_transport_build_transient": [_vp, _vp, _vp, _vp, _vp],
         "femgpu_transport_predictor": [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int],
         "femgpu_deck_transport_opts": [_vp, _vp],

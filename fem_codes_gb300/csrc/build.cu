@@ -710,7 +710,8 @@ extern "C" int fg_assemble_transient(femgpu_transport *t)
 		k_assemble_ede<<<fg_grid(t->nedge + 1LL), FG_TPB, 0, s>>>(t->nedge, t->ec_ptr, t->ec, t->order,
 			t->ke, t->A);
 	k_gather_R<<<fg_grid(neq + 1LL), FG_TPB, 0, s>>>(neq, t->ri_ptr, t->ri, t->re, t->F);
-	return (int)cudaGetLastError();
+	FG_TRY(cudaGetLastError());
+	return t->o.scheme == FEMGPU_CSR ? fg_sell_refresh(t) : 0;
 }
 
 extern "C" int fg_assemble(femgpu_transport *t)
@@ -720,6 +721,8 @@ extern "C" int fg_assemble(femgpu_transport *t)
 	if (t->o.scheme == FEMGPU_CSR) {
 		k_assemble_csr<<<fg_grid(neq, 128, 32), 128, 0, s>>>(neq, t->nnz, t->IA, t->sbe, t->ri_ptr,
 			t->ri, t->ke, t->fe, t->vert, t->node_type, t->upresc, t->A, t->F, &t->st->err);
+		FG_TRY(cudaGetLastError());
+		return fg_sell_refresh(t);
 	} else if (t->o.scheme == FEMGPU_EDE) {
 		k_assemble_ede<<<fg_grid(t->nedge + 1LL), FG_TPB, 0, s>>>(t->nedge, t->ec_ptr, t->ec, t->order,
 			t->ke, t->A);

@@ -175,6 +175,14 @@ struct femgpu_transport {
 	fg_ilu ilu;
 	fg_ilu_sweeps sweeps;
 	int sweep_wait1;                /* 1 + dependency-wait bound; 0: default */
+	/* the CSR matrix in 32-row slices (SELL-32) for the products: entry j of
+	 * row r at sell_base[r/32] + 32 j + r%32; sell_src maps a slot to its CSR
+	 * position (-1: padding) for the refresh after each assembly */
+	long long *sell_base;
+	int *sell_w, *sell_src, *sell_JA;
+	double *sell_A;
+	int nslice;
+	long long nslot;
 
 	/* transient driver (femgpu_transport_set_transient) */
 	int transient;
@@ -242,6 +250,8 @@ int fg_csrmv64_fused(int n, const int *IA, const int *JA, const double *AA, cons
                      double *Q, const int *active, cudaStream_t s);
 int fg_csrmv64_fused_ds(int n, const int *IA, const int *JA, const double *AA, const double *P,
                         void *Q, const int *active, cudaStream_t s);
+int fg_sell_refresh(femgpu_transport *t);                    /* sell_A from A */
+int fg_sellmv(femgpu_transport *t, const double *P, void *Q, int fused, int ds_out, const int *active);
 int fg_diag_setup(femgpu_transport *t);
 int fg_precond(femgpu_transport *t, const double *p, double *z, const int *active);
 /* One restart cycle of the reference's left-preconditioned GMRES

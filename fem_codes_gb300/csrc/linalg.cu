@@ -160,6 +160,74 @@ extern "C" int fg_csrmv32(int n, const int *IA, const int *JA, const float *AA, 
 	return launch_csrmv<float, float, float, float>(n, IA, JA, AA, P, Q, active, s);
 }
 
+// csrmv.c:15-20 over the SELL-32 copy of the matrix: one thread per row,
+// the row's entries in column order (separately rounded, as the reference,
+// or fused), each warp's loads of an entry index coalesced across its 32
+// rows (the slice is stored column by column).  Eight entries per round keep
+// eight independent loads in flight.
+#define SELL_UNR 8
+template <typename TO, bool FUSED>
+__global__ void __launch_bounds__(256) k_sellmv(int n, const long long *__restrict__ base, const int *__restrict__ width,
+                                                const int *__restrict__ IA, const int *__restrict__ JS,
+                                                const double *__restrict__ AS, const double *__restrict__ P,
+                                                TO *__restrict__ Q, const int *active)
+{
+	if (active && !*active) return;
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const int sl = i >> 5;
+	const long long b = __ldg(&base[sl]) + (i & 31);
+	const int w = __ldg(&width[sl]), len = __ldg(&IA[i + 1]) - __ldg(&IA[i]);
+	double q = 0.0;
+	for (int j = 0; j < w; j += SELL_UNR) {
+		double a[SELL_UNR], p[SELL_UNR];
+#pragma unroll
+		for (int u = 0; u < SELL_UNR; u++) {
+			const bool on = j + u < len;
+			a[u] = on ? __ldcs(&AS[b + 32LL * (j + u)]) : 0.0;
+			const int c = on ? __ldcs(&JS[b + 32LL * (j + u)]) : 0;
+			p[u] = on ? __ldg(&P[c]) : 0.0;
+		}
+#pragma unroll
+		for (int u = 0; u < SELL_UNR; u++)
+			if (j + u < len) q = FUSED ? fma(a[u], p[u], q) : __dadd_rn(q, __dmul_rn(a[u], p[u]));
+	}
+	Q[i] = mv_out<TO>(q);
+}
+
+__global__ void k_sell_refresh(long long nslot, const int *__restrict__ src, const double *__restrict__ AA,
+                               double *__restrict__ AS)
+{
+	for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nslot;
+	     k += (long long)gridDim.x * blockDim.x) {
+		const int q = src[k];
+		AS[k] = q >= 0 ? AA[q] : 0.0;
+	}
+}
+
+extern "C" int fg_sell_refresh(femgpu_transport *t)
+{
+	if (!t->sell_A) return 0;
+	k_sell_refresh<<<fg_grid(t->nslot), FG_TPB, 0, t->stream>>>(t->nslot, t->sell_src, t->A, t->sell_A);
+	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_sellmv(femgpu_transport *t, const double *P, void *Q, int fused, int ds_out, const int *active)
+{
+	const int n = t->neq, g = (n + 255) / 256;
+	cudaStream_t s = t->stream;
+	if (ds_out)
+		k_sellmv<dsf, true><<<g, 256, 0, s>>>(n, t->sell_base, t->sell_w, t->IA, t->sell_JA, t->sell_A, P, (dsf *)Q,
+		                                     active);
+	else if (fused)
+		k_sellmv<double, true><<<g, 256, 0, s>>>(n, t->sell_base, t->sell_w, t->IA, t->sell_JA, t->sell_A, P,
+		                                        (double *)Q, active);
+	else
+		k_sellmv<double, false><<<g, 256, 0, s>>>(n, t->sell_base, t->sell_w, t->IA, t->sell_JA, t->sell_A, P,
+		                                         (double *)Q, active);
+	return (int)cudaGetLastError();
+}
+
 // ebemv.c:42-63 gathered per row: for each incident element (ascending),
 // Q += A[3a]*p1 + A[3a+1]*p2 + A[3a+2]*p3 with P[neq] read as 0.
 __global__ void k_ebemv(int neq, const int *__restrict__ ri_ptr, const int *__restrict__ ri,
@@ -218,7 +286,10 @@ __global__ void k_edemv(int neq, const int *__restrict__ first, const int *__res
 extern "C" int fg_matvec(femgpu_transport *t, const double *P, double *Q, const int *active)
 {
 	cudaStream_t s = t->stream;
-	if (t->o.scheme == FEMGPU_CSR) return fg_csrmv64(t->neq, t->IA, t->JA, t->A, P, Q, active, s);
+	if (t->o.scheme == FEMGPU_CSR) {
+		if (t->sell_A) return fg_sellmv(t, P, Q, 0, 0, active);
+		return fg_csrmv64(t->neq, t->IA, t->JA, t->A, P, Q, active, s);
+	}
 	if (t->o.scheme == FEMGPU_EBE)
 		k_ebemv<<<fg_grid(t->neq + 1LL, 128, 32), 128, 0, s>>>(t->neq, t->ri_ptr, t->ri, t->lm, t->A, P, Q,
 		                                                      active);
@@ -795,14 +866,22 @@ extern "C" int fg_kry_true_rho(const fg_krylov *k, const fg_linop *op, const dou
 static int tr_matvec(void *c, const double *p, double *q, const int *a)
 {
 	femgpu_transport *t = (femgpu_transport *)c;
-	if (t->o.solver == FEMGPU_FGMRES && t->o.scheme == FEMGPU_CSR)
+	if (t->o.solver == FEMGPU_FGMRES && t->o.scheme == FEMGPU_CSR) {
+		if (t->sell_A) return fg_sellmv(t, p, q, 1, 0, a);
 		return fg_csrmv64_fused(t->neq, t->IA, t->JA, t->A, p, q, a, t->stream);
+	}
 	return fg_matvec(t, p, q, a);
 }
 static int tr_precond(void *c, const double *p, double *z, const int *a)
 {
 	return fg_precond((femgpu_transport *)c, p, z, a);
 }
+// The Krylov operator on its own (timing, tests).
+extern "C" int fg_operator(femgpu_transport *t, const double *p, double *q)
+{
+	return tr_matvec(t, p, q, nullptr);
+}
+
 extern "C" int fg_ilu0_apply64_dsin(femgpu_transport *t, const void *p, double *z, const int *active);
 extern "C" int fg_ilu0_ds_ready(const femgpu_transport *t);
 static int tr_precond_dsin(void *c, const void *p, double *z, const int *a)
@@ -812,7 +891,10 @@ static int tr_precond_dsin(void *c, const void *p, double *z, const int *a)
 static int tr_matvec_dsout(void *c, const double *p, void *q, const int *a)
 {
 	femgpu_transport *t = (femgpu_transport *)c;
-	if (t->o.scheme == FEMGPU_CSR) return fg_csrmv64_fused_ds(t->neq, t->IA, t->JA, t->A, p, q, a, t->stream);
+	if (t->o.scheme == FEMGPU_CSR) {
+		if (t->sell_A) return fg_sellmv(t, p, q, 1, 1, a);
+		return fg_csrmv64_fused_ds(t->neq, t->IA, t->JA, t->A, p, q, a, t->stream);
+	}
 	int rc = fg_matvec(t, p, (double *)q, a);
 	if (rc) return rc;
 	k_to_ds<<<fg_grid(t->neq), FG_TPB, 0, t->stream>>>((double *)q, t->neq, a);

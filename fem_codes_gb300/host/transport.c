@@ -81,6 +81,48 @@ static int sync_err(femgpu_transport *t)
 	return 0;
 }
 
+/* The SELL-32 layout of the CSR pattern (rows in slices of 32, each slice
+ * padded to its longest row and stored entry index by entry index): the
+ * slots' columns, their CSR positions and the slice offsets. */
+static int build_sell(femgpu_transport *t, const int *IA, const int *JA)
+{
+	const int n = t->neq, ns = (n + 31) / 32;
+	long long *base = malloc(sizeof(long long) * ((size_t)ns + 1)), nslot = 0;
+	int *w = malloc(sizeof(int) * (size_t)ns), *src = NULL, *col = NULL, s, r, j, rc = 0;
+	if (!base || !w) { free(base); free(w); return FEMGPU_E_NOMEM; }
+	for (s = 0; s < ns; s++) {
+		int wm = 0;
+		for (r = 32 * s; r < n && r < 32 * s + 32; r++) if (IA[r + 1] - IA[r] > wm) wm = IA[r + 1] - IA[r];
+		base[s] = nslot;
+		w[s] = wm;
+		nslot += 32LL * wm;
+	}
+	base[ns] = nslot;
+	src = malloc(sizeof(int) * ((size_t)nslot + 1));
+	col = malloc(sizeof(int) * ((size_t)nslot + 1));
+	if (!src || !col) rc = FEMGPU_E_NOMEM;
+	if (!rc) {
+		long long k;
+		for (k = 0; k < nslot; k++) { src[k] = -1; col[k] = 0; }
+		for (r = 0; r < n; r++)
+			for (j = 0; j < IA[r + 1] - IA[r]; j++) {
+				long long at = base[r / 32] + 32LL * j + (r & 31);
+				src[at] = IA[r] + j;
+				col[at] = JA[IA[r] + j];
+			}
+		t->nslice = ns;
+		t->nslot = nslot;
+		if (upload((void **)&t->sell_base, base, sizeof(long long) * ((size_t)ns + 1)) ||
+		    upload((void **)&t->sell_w, w, sizeof(int) * (size_t)ns) ||
+		    upload((void **)&t->sell_src, src, sizeof(int) * ((size_t)nslot + 1)) ||
+		    upload((void **)&t->sell_JA, col, sizeof(int) * ((size_t)nslot + 1)) ||
+		    fgh_dmalloc((void **)&t->sell_A, sizeof(double) * ((size_t)nslot + 1)))
+			rc = FEMGPU_E_NOMEM;
+	}
+	free(base); free(w); free(src); free(col);
+	return rc;
+}
+
 /* Download the CSR pattern and rebuild the device structures under a new
  * equation numbering (reverse Cuthill-McKee, csr_Initialization.c:144-179). */
 static int reorder_symrcm(femgpu_transport *t, int *hIA, int *hJA)
@@ -201,6 +243,8 @@ int femgpu_transport_create(femgpu_transport **out, const femgpu_transport_opts 
 			CK(cudaMemcpy(hJA, t->JA, sizeof(int) * (size_t)t->nnz, cudaMemcpyDeviceToHost));
 		}
 		t->bandwidth = fgh_bandwidth(neq, hIA, hJA);
+		rc = build_sell(t, hIA, hJA);
+		if (rc) return rc;
 		nA = (size_t)t->nnz + 1;
 		DM(t->ke, sizeof(double) * 9 * (size_t)nel);
 	} else if (t->o.scheme == FEMGPU_EDE) {
@@ -307,7 +351,7 @@ void femgpu_transport_destroy(femgpu_transport *t)
 		t->ec, t->e2_ptr, t->e2, t->A, t->ke, t->fe, t->A32, t->u, t->F, t->F0, t->invDiag,
 		t->invDiag32, t->ilu.LU, t->ilu.Dinv, t->V, t->H, t->cs, t->sn, t->ge, t->gy, t->w2,
 		t->Z, t->Z32, t->xr, t->dr, t->partials, t->st, t->du, t->uold, t->Da, t->re, t->dold,
-		t->u1, t->u2, t->uB, t->aB, t->bub };
+		t->u1, t->u2, t->uB, t->aB, t->bub, t->sell_base, t->sell_w, t->sell_src, t->sell_JA, t->sell_A };
 	for (i = 0; i < (int)(sizeof ptrs / sizeof ptrs[0]); i++) if (ptrs[i]) cudaFree(ptrs[i]);
 	if (t->o.precond == FEMGPU_PREC_ILU0 || t->o.precond == FEMGPU_PREC_LEARNED) fg_ilu_free(t);
 	if (t->st_host) cudaFreeHost(t->st_host);
@@ -769,6 +813,15 @@ int femgpu_transport_solve_bx(femgpu_transport *t, const double *B_host, double 
 
 double *femgpu_transport_u_dev(femgpu_transport *t) { return t ? t->u : NULL; }
 double *femgpu_transport_F_dev(femgpu_transport *t) { return t ? t->F : NULL; }
+
+int fg_operator(femgpu_transport *t, const double *p, double *q);
+
+int femgpu_transport_operator_dev(femgpu_transport *t, const double *P, double *Q)
+{
+	if (!t || !P || !Q) return FEMGPU_E_ARG;
+	KR(fg_operator(t, P, Q));
+	return 0;
+}
 
 /* -------------------------------------------------------------- Process */
 int femgpu_transport_process(femgpu_transport *t, int npicard, double *u_hist, int *iters)

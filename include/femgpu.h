@@ -284,6 +284,11 @@ int femgpu_transport_write_vtu(femgpu_transport *ctx, const char *path, const do
 int femgpu_transport_build_dev(femgpu_transport *ctx);
 int femgpu_transport_precond_setup_dev(femgpu_transport *ctx, int tag);
 int femgpu_transport_matvec_dev(femgpu_transport *ctx, const double *P, double *Q);
+/* Q = A P as the context's Krylov solver applies it (FGMRES with CSR
+ * storage: the fused product over the SELL-32 copy, within rounding of
+ * csrmv.c; otherwise femgpu_transport_matvec_dev's product), device
+ * pointers on the context's stream. */
+int femgpu_transport_operator_dev(femgpu_transport *ctx, const double *P, double *Q);
 int femgpu_transport_precond_dev(femgpu_transport *ctx, const double *p, double *z);
 /* The same preconditioner evaluated in FP32 (the mixed-precision solves'). */
 int femgpu_transport_precond32_dev(femgpu_transport *ctx, const double *p, float *z);

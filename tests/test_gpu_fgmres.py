@@ -93,3 +93,37 @@ def test_mixed_requires_csr_fgmres(gpu_lib):
         fg.SSTransport.from_problem(m, p, scheme="EBE", precond="DIAG", precision="MIXED", solver="FGMRES")
     with pytest.raises(fg.FemGpuError):
         fg.SSTransport.from_problem(m, p, precision="MIXED", solver="GMRES")
+
+
+def test_sell_operators_vs_csrmv(gpu_lib):
+    """The products over the SELL-32 copy of the matrix: the reference's
+    GMRES context applies csrmv.c's separately rounded sums (bit-identical to
+    the oracle's csrmv), the FGMRES context the fused form (each row within
+    2 nnz_row eps of sum |a_ij p_j|); the copy follows a second Build."""
+    import ctypes
+    import torch
+    import fem_codes_gb300 as fg
+    vp = ctypes.c_void_p
+    m = structured_mesh(200, 120, perturb=0.2, seed=9)
+    p = skew_problem(m)
+    P = np.random.default_rng(2).standard_normal(m.nnodes + 1)
+    for solver in ("GMRES", "FGMRES"):
+        with fg.SSTransport.from_problem(m, p, scheme="CSR", reorder="SYMRCM", precond="ILU0", solver=solver) as T:
+            for u in (np.zeros(T.neq + 1), 0.3 * np.ones(T.neq + 1)):
+                F, A = T.Build(u=u, want_matrix=True)
+                pat = T.pattern()
+                IA, JA = pat["IA"], pat["JA"]
+                x = np.ascontiguousarray(P[:T.neq + 1])
+                Qref = pyoracle.csrmv(IA, JA, A, x)[:T.neq]
+                xd = torch.from_numpy(x).cuda()
+                qd = torch.zeros_like(xd)
+                torch.cuda.synchronize()
+                assert T._L.femgpu_transport_operator_dev(T.handle, vp(xd.data_ptr()), vp(qd.data_ptr())) == 0
+                torch.cuda.synchronize()
+                q = qd.cpu().numpy()[:T.neq]
+                if solver == "GMRES":
+                    assert np.array_equal(q, Qref)
+                else:
+                    rows = np.repeat(np.arange(T.neq), np.diff(IA))
+                    mag = np.bincount(rows, weights=np.abs(A[:IA[-1]] * x[JA]), minlength=T.neq)
+                    assert np.all(np.abs(q - Qref) <= 2.0 * np.diff(IA) * np.finfo(np.float64).eps * mag)
