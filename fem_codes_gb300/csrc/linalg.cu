@@ -513,17 +513,34 @@ __global__ void k_mdot_fin(const double *partials, int G, int m, double *h, doub
 	}
 }
 
-// w -= sum_j h[j] v_j; norm != 0: Hn = ||w|| (last block).
+// w -= sum_j h[j] v_j; norm != 0: Hn = ||w|| (last block).  The basis
+// entries of a thread's element are loaded CGS_UNR at a time ahead of the
+// dependent subtractions (the same order of subtractions), so a warp keeps
+// CGS_UNR coalesced loads in flight; the kernel runs on CGS_GRID x the
+// reduction grid.  Dynamic shared memory: the m coefficients.
+#define CGS_UNR 8
+#define CGS_GRID 4
 __global__ void __launch_bounds__(RED_TPB) k_cgs_update(const double *V, size_t ldv, int n, int m, double *w,
                                                         const double *h, int norm, double *Hn, double *partials,
                                                         fg_status *st)
 {
 	if (!gmres_live(st)) return;
+	extern __shared__ double hsh[];
 	__shared__ double sh[32];
+	for (int j = threadIdx.x; j < m; j += blockDim.x) hsh[j] = h[j];
+	__syncthreads();
 	double part = 0.0;
 	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
 		double x = w[k];
-		for (int j = 0; j < m; j++) x -= h[j] * V[(size_t)j * ldv + k];
+		int j = 0;
+		for (; j + CGS_UNR <= m; j += CGS_UNR) {
+			double v[CGS_UNR];
+#pragma unroll
+			for (int u = 0; u < CGS_UNR; u++) v[u] = V[(size_t)(j + u) * ldv + k];
+#pragma unroll
+			for (int u = 0; u < CGS_UNR; u++) x -= hsh[j + u] * v[u];
+		}
+		for (; j < m; j++) x -= hsh[j] * V[(size_t)j * ldv + k];
 		w[k] = x;
 		part += x * x;
 	}
@@ -580,7 +597,15 @@ __global__ void __launch_bounds__(RED_TPB) k_cgs_update_ds(const dsf *V, size_t 
 	dsf part = dsf{ 0.0f, 0.0f };
 	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
 		dsf x = w[k];
-		for (int j = 0; j < m; j++) x = ds_fma(hneg[j], V[(size_t)j * ldv + k], x);
+		int j = 0;
+		for (; j + CGS_UNR <= m; j += CGS_UNR) {
+			dsf v[CGS_UNR];
+#pragma unroll
+			for (int u = 0; u < CGS_UNR; u++) v[u] = V[(size_t)(j + u) * ldv + k];
+#pragma unroll
+			for (int u = 0; u < CGS_UNR; u++) x = ds_fma(hneg[j + u], v[u], x);
+		}
+		for (; j < m; j++) x = ds_fma(hneg[j], V[(size_t)j * ldv + k], x);
 		w[k] = x;
 		part = ds_fma(x, x, part);
 	}
@@ -767,6 +792,9 @@ extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 	// the double-single basis (FP64 arithmetic otherwise: the residual, the
 	// Hessenberg matrix, the Givens rotations, Z and X stay FP64)
 	const bool dsv = k->dsv && !mixed && op->precond_dsin && op->matvec_dsout;
+	// the update's grid: its norm partials must stay below the coefficients,
+	// which the multi-dot finish stores at partials + G (kmax + 1)
+	const int cgs_grid = G * (CGS_GRID < kmax + 1 ? CGS_GRID : kmax + 1);
 	if (mixed && (!op->precond32 || !op->matvec_xf || !k->Z32)) return FEMGPU_E_ARG;
 	if (!mixed && !k->Z) return FEMGPU_E_ARG;
 	if ((rc = op->matvec(op->ctx, X, V, nullptr))) return rc;
@@ -802,7 +830,7 @@ extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 				k_mdot_ds<<<dim3(G, (m + MD_J - 1) / MD_J), RED_TPB, 0, s>>>((const dsf *)V, ldv, n, m, (const dsf *)w,
 				                                                           k->partials, k->st);
 				k_mdot_fin<<<m, 32, 0, s>>>(k->partials, G, m, h, k->H + i, ldh, pass, k->st);
-				k_cgs_update_ds<<<G, RED_TPB, sizeof(dsf) * (size_t)m, s>>>((const dsf *)V, ldv, n, m, (dsf *)w, h, last,
+				k_cgs_update_ds<<<cgs_grid, RED_TPB, sizeof(dsf) * (size_t)m, s>>>((const dsf *)V, ldv, n, m, (dsf *)w, h, last,
 				                                                         k->H + (i + 1) * ldh + i, k->partials,
 				                                                         k->st);
 			}
@@ -820,8 +848,9 @@ extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 				const int last = pass == gs - 1;
 				k_mdot<<<dim3(G, (m + MD_J - 1) / MD_J), RED_TPB, 0, s>>>(V, ldv, n, m, w, k->partials, k->st);
 				k_mdot_fin<<<m, 32, 0, s>>>(k->partials, G, m, h, k->H + i, ldh, pass, k->st);
-				k_cgs_update<<<G, RED_TPB, 0, s>>>(V, ldv, n, m, w, h, last, k->H + (i + 1) * ldh + i,
-				                                   k->partials, k->st);
+				k_cgs_update<<<cgs_grid, RED_TPB, sizeof(double) * (size_t)m, s>>>(V, ldv, n, m, w, h, last,
+				                                                                     k->H + (i + 1) * ldh + i,
+				                                                                     k->partials, k->st);
 			}
 		}
 		k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(w, n, k->H + (i + 1) * ldh + i, k->st);
