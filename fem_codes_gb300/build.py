@@ -54,6 +54,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for f in cu:
         o = os.path.join(BUILD, f + ".o")
         flags = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v" if verbose else "-O3"]
+        # build-time tuning macros (e.g. -DFG_SW2_CW=24: consumer warps of the ILU(0) sweeps)
+        flags += os.environ.get("FEMGPU_NVCC_EXTRA", "").split()
         if f in NO_FMA:
             flags += ["--fmad=false"]
         jobs.append([NVCC] + ARCH + flags + INC + ["-c", os.path.join(CSRC, f), "-o", o])

@@ -40,7 +40,10 @@
 #include <vector>
 #include <algorithm>
 
-#define SW_SUB 512                    // max rows of a sub-block
+#ifndef FG_SW2_CW
+#define FG_SW2_CW 16
+#endif
+#define SW_SUB (FG_SW2_CW * 32)       // max rows of a sub-block
 #define SW_MAXW 8                     // dependencies per row on the unrolled path
 #define SW_RPT 4                      // rows per consumer thread per pass
 #define FAC_THREADS 1024
@@ -380,7 +383,8 @@ __host__ __device__ constexpr int rec_bytes(int w, bool upper, int ts)
 	return (((rec_ib(w) + rec_vb(w, upper, ts)) / 16) & 1) ? rec_ib(w) + rec_vb(w, upper, ts)
 	                                                        : rec_ib(w) + rec_vb(w, upper, ts) + 16;
 }
-#define SW2_CW 16                     // consumer warps of the record-layout sweep (SW_SUB rows)
+#define SW2_CW FG_SW2_CW              // consumer warps of the record-layout sweep (SW_SUB rows)
+#define NEED_STRIDE (((SW2_CW) + 15) / 16 * 16)   // bytes of a warp's need table
 
 template <typename T, bool UPPER, bool FMA, int W>
 __global__ void __launch_bounds__((SW2_CW + 1) * 32, 1)
@@ -488,7 +492,7 @@ k_sweep_rec(SweepArgs a, const T *__restrict__ in, T *out)
 // back.  A warp releases a stage (mbarrier of CW arrivals) as soon as its
 // rows are in registers.  Header: {rows, sub-blocks of the level, first
 // position, far flag}, then CW need tables of 16 bytes, then the records.
-#define DF_HDR (16 + SW2_CW * 16)
+#define DF_HDR (16 + SW2_CW * NEED_STRIDE)
 
 template <typename T, bool UPPER, bool FMA, int W>
 __global__ void __launch_bounds__((SW2_CW + 1) * 32, 1)
@@ -497,7 +501,7 @@ k_sweep_df(SweepArgs a, const T *__restrict__ in, T *out)
 	constexpr int CW = SW2_CW;
 	constexpr int IB = rec_ib(W), VB = rec_vb(W, UPPER, (int)sizeof(T)), RB = rec_bytes(W, UPPER, (int)sizeof(T));
 	static_assert(SW_SUB == CW * 32, "one row per consumer thread and sub-block");
-	static_assert(CW <= 16, "one need byte per consumer warp in a 16-byte table");
+	static_assert(CW <= NEED_STRIDE && CW <= 32, "one need byte per consumer warp in a warp's table");
 	if (a.active && !*a.active) return;
 	extern __shared__ __align__(128) unsigned char sm[];
 	const unsigned ring_b = (unsigned)al16((SW_RING + 1) * sizeof(T));
@@ -550,7 +554,7 @@ k_sweep_df(SweepArgs a, const T *__restrict__ in, T *out)
 			for (int k = 0; k < VB / 16; k++) cv.q[k] = ((const int4 *)(st + roff + IB))[k];
 			const T x0 = *(const T *)(st + boff);
 			const int4 h = *(const int4 *)st;
-			const int need = lane < CW ? (int)st[16 + warp * 16 + lane] : 255;
+			const int need = lane < CW ? (int)st[16 + warp * NEED_STRIDE + lane] : 255;
 			if (j == 0) nsub = h.y;
 			__syncwarp();
 			if (lane == 0) mbar_arrive(&empty[s]);        // this warp's rows are in registers
@@ -688,7 +692,7 @@ k_sweep_cs(SweepArgs a, const T *__restrict__ in, T *out)
 			for (int k = 0; k < VB / 16; k++) cv.q[k] = ((const int4 *)(st + roff + IB))[k];
 			const T x0 = *(const T *)(st + boff);
 			const int4 h = *(const int4 *)st;
-			const int need = lane < CW ? (int)st[16 + warp * 16 + lane] : 255;
+			const int need = lane < CW ? (int)st[16 + warp * NEED_STRIDE + lane] : 255;
 			if (j == 0) nsub = h.y;
 			__syncwarp();
 			if (lane == 0) mbar_arrive(&empty[s]);        // this warp's slots are in registers
@@ -1336,7 +1340,7 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 				// need[w][pw]: smallest level distance of a dependency of warp w's rows
 				// produced by warp pw (255: none within skew + 1 levels)
 				unsigned char *need = b + 16;
-				memset(need, 255, (size_t)SW2_CW * 16);
+				memset(need, 255, (size_t)SW2_CW * NEED_STRIDE);
 				for (int j = 0; j < c; j++) {
 					int r = H.rows[start + j];
 					for (int q = IA[r]; q < IA[r + 1]; q++) {
@@ -1346,7 +1350,7 @@ static int build_prog(const int *IA, const int *JA, int n, const HostLevels &H, 
 						if (end - p > near_lim) dl--;      // read back from global memory: the next level's release
 						if (dl > skew + 1) continue;
 						int pw = ((p - H.start[lp]) % SW_SUB) / 32;
-						unsigned char &e = need[(j / 32) * 16 + pw];
+						unsigned char &e = need[(j / 32) * NEED_STRIDE + pw];
 						if (dl < (int)e) e = (unsigned char)dl;
 					}
 				}
@@ -1613,7 +1617,7 @@ static int build_prog_chain(const int *IA, const int *JA, int n, const ChainLeve
 		const int hh[4] = { c, nsub, start, hasfar };
 		memcpy(b, hh, sizeof hh);
 		unsigned char *need = b + 16;
-		memset(need, 255, (size_t)SW2_CW * 16);
+		memset(need, 255, (size_t)SW2_CW * NEED_STRIDE);
 		for (int j = 0; j < c; j++) {
 			const int r = H.slot_row[start + j];
 			int *ri = (int *)(b + DF_HDR + (size_t)j * RB), k = 0;
@@ -1635,7 +1639,7 @@ static int build_prog_chain(const int *IA, const int *JA, int n, const ChainLeve
 				if (!nearp) dl--;                     // read back from global memory: the next level's release
 				if (dl <= skew + 1) {
 					const int pw = ((p - H.lstart[lp]) % SW_SUB) / 32;
-					unsigned char &e = need[(j / 32) * 16 + pw];
+					unsigned char &e = need[(j / 32) * NEED_STRIDE + pw];
 					if (dl < (int)e) e = (unsigned char)dl;
 				}
 				val_off.push_back(vo + k * tsize);
