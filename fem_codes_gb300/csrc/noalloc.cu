@@ -60,18 +60,24 @@ k_resnorm_noalloc(int n, const int *__restrict__ IA, const int *__restrict__ JA,
 	}
 }
 
-// Device address of the scratch array, looked up once per device with that
-// device current (the host-side symbol is only a stand-in, not an address).
+// Device address of the scratch array, looked up with the device current
+// (the host-side symbol is only a stand-in, not an address): on a device's
+// first call, and again on every call whose stream is not being captured, so
+// that after a device reset, or with another context current on the device,
+// the call uses the address valid now; a call on a capturing stream reuses
+// the address its device's last lookup gave.
 static double *g_na_ptr[NA_MAX_DEVICES];
 static std::mutex g_na_mu;
 
-static int na_scratch(double **out)
+static int na_scratch(cudaStream_t s, double **out)
 {
 	int dev = 0;
+	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
 	FG_TRY(cudaGetDevice(&dev));
 	if (dev < 0 || dev >= NA_MAX_DEVICES) return FEMGPU_E_ARG;
+	FG_TRY(cudaStreamIsCapturing(s, &cap));
 	std::lock_guard<std::mutex> lk(g_na_mu);
-	if (!g_na_ptr[dev]) {
+	if (!g_na_ptr[dev] || cap == cudaStreamCaptureStatusNone) {
 		double *p = nullptr;
 		cudaError_t e = cudaGetSymbolAddress((void **)&p, g_na_scratch);
 		if (e != cudaSuccess || !p) return e != cudaSuccess ? (int)e : FEMGPU_E_CUDA;
@@ -87,9 +93,9 @@ extern "C" int femgpu_csr_resnorm_noalloc(int n, const int *IA, const int *JA, c
 	if (n <= 0 || !IA || !JA || !AA || !u || !F || !out2) return FEMGPU_E_ARG;
 	if (n > NA_MAX_ROWS) return FEMGPU_E_ARG;          // beyond the static scratch
 	double *scratch = nullptr;
-	int rc = na_scratch(&scratch);
-	if (rc) return rc > 0 ? FEMGPU_E_CUDA : rc;
 	cudaStream_t s = (cudaStream_t)stream;
+	int rc = na_scratch(s, &scratch);
+	if (rc) return rc > 0 ? FEMGPU_E_CUDA : rc;
 	int blocks = (n + NA_TPB * NA_ROWS_PER_THREAD - 1) / (NA_TPB * NA_ROWS_PER_THREAD);
 	if (blocks > NA_MAX_BLOCKS) return FEMGPU_E_ARG;
 	// the ticket must start at zero (a previous call may have been cut short)

@@ -614,10 +614,11 @@ int femgpu_csrmv_f64_fused(int n, const int *IA, const int *JA, const double *AA
  * partial sums live in a fixed static device array (32 KB, held by every GPU
  * that loads the library until exit), so n <= 4,194,304 rows; larger n returns
  * FEMGPU_E_ARG.  The first call on a device looks up that array's device
- * address with the device current and keeps it for the process (make that
- * first call before any stream capture; after cudaDeviceReset the kept address
- * is stale).  All calls share the array: calls that overlap on the GPU race,
- * so serialise them. */
+ * address with the device current (make that first call before any stream
+ * capture); later calls look it up again unless their stream is being
+ * captured, so a device reset or another current context is followed.  All
+ * calls share the array: calls that overlap on the GPU race, so serialise
+ * them. */
 int femgpu_csr_resnorm_noalloc(int n, const int *IA, const int *JA, const double *AA,
 		const double *u, const double *F, double *out2, void *stream);
 
