@@ -931,13 +931,17 @@ static int tr_matvec_dsout(void *c, const double *p, void *q, const int *a)
 }
 
 // The double-single basis for FP64 FGMRES with the double-single ILU(0)
-// sweeps (FEMGPU_KRYLOV_DS=0 keeps the FP64 basis).
+// sweeps, on request (FEMGPU_KRYLOV_DS=1): measured at 2048x1024 its
+// multi-dot and update kernels take about twice as long as the FP64 ones
+// (those are bound by memory latency, not by the FP64 pipe, and a
+// double-single product-sum costs a dozen FP32 instructions), so the FP64
+// basis is the default.
 static int krylov_ds(const femgpu_transport *t)
 {
 	static int env = -1;
 	if (env < 0) {
 		const char *e = getenv("FEMGPU_KRYLOV_DS");
-		env = (e && e[0] == '0') ? 0 : 1;
+		env = (e && e[0] == '1') ? 1 : 0;
 	}
 	return env && t->o.solver == FEMGPU_FGMRES && t->o.precision == FEMGPU_FP64 &&
 	       t->o.precond == FEMGPU_PREC_ILU0 && fg_ilu0_ds_ready(t);
