@@ -80,7 +80,8 @@ class EulerOpts(ctypes.Structure):
                 ("alpha", ctypes.c_double), ("dt", ctypes.c_double), ("stab_tol", ctypes.c_double),
                 ("precond", ctypes.c_int), ("solver", ctypes.c_int), ("kmax", ctypes.c_int),
                 ("lmax", ctypes.c_int), ("tol", ctypes.c_double), ("ncorr", ctypes.c_int),
-                ("precision", ctypes.c_int), ("scheme", ctypes.c_int), ("ilu_blocks", ctypes.c_int)]
+                ("precision", ctypes.c_int), ("scheme", ctypes.c_int), ("ilu_blocks", ctypes.c_int),
+                ("scaling", ctypes.c_int)]
 
 
 class NSOpts(ctypes.Structure):
@@ -152,6 +153,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_mesh_side_types": [ctypes.c_int, _vp, _vp, ctypes.c_int, _vp, _vp],
         "femgpu_transport_set_sweep_wait": [_vp, ctypes.c_int],
         "femgpu_euler_set_slip": [_vp, _vp, _vp, _vp],
+        "femgpu_euler_scale": [_vp, _vp, _vp],
         "femgpu_transport_set_transient": [_vp, _vp],
         "femgpu_transport_set_bubbles": [_vp, _vp, _vp],
         "femgpu_transport_operator_dev": [_vp, _vp, _vp],
@@ -808,12 +810,13 @@ class Euler:
 
     def __init__(self, x, y, vert, node_id, neq, upresc, gamma=1.4, mach=1.0, dimensionless=False,
                  alpha=0.5, dt=1e-3, stab_tol=1e-6, precond="BlockDiag", solver="GMRES", kmax=30,
-                 lmax=100, tol=1e-8, ncorr=2, precision="FP64", scheme="EBE", ilu_blocks=0):
+                 lmax=100, tol=1e-8, ncorr=2, precision="FP64", scheme="EBE", ilu_blocks=0, scaling="NOT"):
         L = load()
         o = EulerOpts()
         L.femgpu_euler_default_opts(ctypes.byref(o))
         o.scheme = OPTS["scheme"][scheme.upper()]
         o.ilu_blocks = int(ilu_blocks)
+        o.scaling = {"NOT": 0, "BLOCKSCALING": 1}[scaling.upper()]
         o.gamma, o.mach, o.dimensionless = float(gamma), float(mach), int(bool(dimensionless))
         o.alpha, o.dt, o.stab_tol = float(alpha), float(dt), float(stab_tol)
         o.precond = OPTS["precond"][precond.upper()]
@@ -888,6 +891,14 @@ class Euler:
         of a CSR context (hierarchy rebuilt at every precond_setup)."""
         self._amg = amg
         self._check(self._L.femgpu_euler_set_amg(self._h, amg.handle), "set_amg")
+
+    def scaling(self, want_matrix=False):
+        """FemFunctions->scaling = Block_scaling_EBE after a Build: returns
+        (R, Ae) scaled."""
+        R = np.zeros(self.neq + 1)
+        Ae = np.zeros(self.nel * 144) if want_matrix else None
+        self._check(self._L.femgpu_euler_scale(self._h, _ptr(R), _ptr(Ae)), "scaling")
+        return R, (Ae.reshape(self.nel, 144) if want_matrix else None)
 
     def set_slip(self, slip=None, cs=None, sn=None):
         """Slip walls: slip [nnodes] (the nodes with v1Type = -1) and the cosine

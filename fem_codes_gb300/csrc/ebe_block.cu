@@ -276,6 +276,47 @@ extern "C" int fg_ebe_matvec(femgpu_ebe *c, const double *P, double *Q, int offd
 	return (int)cudaGetLastError();
 }
 
+// Block_scaling.c:7-110 for the 4-dof element matrices, one thread per
+// element: every prescribed dof's row and column of Ae (12x12, row-major)
+// become zero with a one on the diagonal (matrix_Bondary_Conditions), then
+// each vertex's row block is replaced by invBD(vertex) times the adjusted
+// row block, each entry summed over j in order from zero (matrix_Scaling).
+__global__ void k_block_scale4(int nel, const int *__restrict__ vert, const int *__restrict__ node_id,
+                               const double *__restrict__ invBD, double *A)
+{
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nel; e += gridDim.x * blockDim.x) {
+		double *a = A + 144LL * e;
+		int v[3];
+		for (int b = 0; b < 3; b++) v[b] = vert[3 * e + b];
+		for (int b = 0; b < 3; b++)
+			for (int d = 0; d < 4; d++) {
+				if (node_id[4 * v[b] + d] >= 0) continue;
+				const int r = 4 * b + d;
+				for (int k = 0; k < 12; k++) { a[12 * r + k] = 0.0; a[12 * k + r] = 0.0; }
+				a[12 * r + r] = 1.0;
+			}
+		for (int b = 0; b < 3; b++) {
+			double m[4][12];
+			const double *D = invBD + 16LL * v[b];
+			for (int j = 0; j < 4; j++)
+				for (int k = 0; k < 12; k++) m[j][k] = a[12 * (4 * b + j) + k];
+			for (int i = 0; i < 4; i++)
+				for (int k = 0; k < 12; k++) {
+					double s = 0.0;
+					for (int j = 0; j < 4; j++) s += D[4 * i + j] * m[j][k];
+					a[12 * (4 * b + i) + k] = s;
+				}
+		}
+	}
+}
+
+extern "C" int fg_ebe_block_scale(femgpu_ebe *c)
+{
+	if (c->ndof != 4) return FEMGPU_E_ARG;
+	k_block_scale4<<<fg_grid(c->nel), FG_TPB, 0, c->stream>>>(c->nel, c->vert, c->node_id, c->invBD, c->A);
+	return (int)cudaGetLastError();
+}
+
 extern "C" int fg_ebe_blockdiag_setup(femgpu_ebe *c)
 {
 	int g = fg_grid(c->nnodes);

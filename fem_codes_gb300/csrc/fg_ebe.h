@@ -27,6 +27,9 @@ struct femgpu_ebe {
 int fg_ebe_lm(femgpu_ebe *c);
 int fg_ebe_matvec(femgpu_ebe *c, const double *P, double *Q, int offdiag);
 int fg_ebe_blockdiag_setup(femgpu_ebe *c);
+/* Block_scaling_EBE's element step (ndof 4): identity rows/columns for the
+ * prescribed dofs, each vertex's row block times its invBD. */
+int fg_ebe_block_scale(femgpu_ebe *c);
 int fg_ebe_blockdiag_apply(femgpu_ebe *c, const double *p, double *z, int mode);
 /* Mixed precision: A32 = (float) A; Q = A32 P with FP32 element rows and
  * FP64 row totals; z = D^-1 p in FP64 arithmetic, stored in FP32. */

@@ -162,7 +162,8 @@ int femgpu_euler_create(femgpu_euler **out, const femgpu_euler_opts *opts, int n
 	    (o.scheme == FEMGPU_CSR && o.precision != FEMGPU_FP64) ||
 	    (o.solver != FEMGPU_PGMRES && o.solver != FEMGPU_FGMRES) ||
 	    (o.precision != FEMGPU_FP64 && o.precision != FEMGPU_MIXED_IR) ||
-	    (o.precision == FEMGPU_MIXED_IR && o.solver != FEMGPU_FGMRES)) {
+	    (o.precision == FEMGPU_MIXED_IR && o.solver != FEMGPU_FGMRES) ||
+	    (o.scaling != 0 && (o.scaling != 1 || o.scheme != FEMGPU_EBE))) {
 		fgh_set_error("femgpu_euler_create: bad argument or option");
 		return FEMGPU_E_ARG;
 	}
@@ -303,6 +304,35 @@ int femgpu_euler_build(femgpu_euler *c, const double *u, const double *du, doubl
 	return 0;
 }
 
+/* FemFunctions->scaling = Block_scaling_EBE (Block_scaling.c:7-49): the
+ * block diagonal of the current matrix set up and R := D^-1 R
+ * (BlockDiag_precond_EBE_setup), then the element matrices scaled. */
+int femgpu_euler_scale_dev(femgpu_euler *c)
+{
+	if (!c) return FEMGPU_E_ARG;
+	if (!c->built) { fgh_set_error("scaling before build"); return FEMGPU_E_NOT_BUILT; }
+	if (c->o.scheme != FEMGPU_EBE) { fgh_set_error("BlockScaling needs EBE storage (setScaling.c)"); return FEMGPU_E_ARG; }
+	KR(fg_ebe_blockdiag_setup(c->ebe));
+	KR(fg_ebe_blockdiag_apply(c->ebe, c->R, c->R, 0));
+	KR(fg_ebe_block_scale(c->ebe));
+	c->ebe->have_bd = 0;
+	c->have_bd = 0;
+	return 0;
+}
+
+int femgpu_euler_scale(femgpu_euler *c, double *R_host, double *Ae_host)
+{
+	if (!c) return FEMGPU_E_ARG;
+	KR(femgpu_euler_scale_dev(c));
+	if (R_host)
+		CK(cudaMemcpyAsync(R_host, c->R, sizeof(double) * ((size_t)c->neq + 1), cudaMemcpyDeviceToHost, c->stream));
+	if (Ae_host)
+		CK(cudaMemcpyAsync(Ae_host, c->ebe->A, sizeof(double) * 144 * (size_t)c->nel, cudaMemcpyDeviceToHost,
+		                   c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	return 0;
+}
+
 int femgpu_euler_precond_setup_dev(femgpu_euler *c)
 {
 	if (!c) return FEMGPU_E_ARG;
@@ -405,6 +435,7 @@ static int predictor(femgpu_euler *c, int nsteps, double *uhist, int *iters)
 			int it = 0;
 			CK(cudaEventRecord(c->ev[0], c->stream));
 			KR(femgpu_euler_build_dev(c));                                  /* :71      */
+			if (c->o.scaling) KR(femgpu_euler_scale_dev(c));                /* :73      */
 			CK(cudaEventRecord(c->ev[1], c->stream));
 			KR(femgpu_euler_precond_setup_dev(c));                          /* :75      */
 			CK(cudaEventRecord(c->ev[2], c->stream));

@@ -374,6 +374,12 @@ typedef struct femgpu_euler_opts {
 	int ilu_blocks;      /* CSR + ILU0: 0 the whole matrix (the reference's), */
 	                     /* P > 1 block ILU(0) over P row blocks (as         */
 	                     /* femgpu_transport_opts.ilu_blocks)                */
+	int scaling;         /* Scaling: 0 NOT, 1 BlockScaling (EBE storage):    */
+	                     /* after every Build, Block_scaling_EBE              */
+	                     /* (Block_scaling.c:7-49): the nodal block diagonal  */
+	                     /* set up and R := D^-1 R, the prescribed rows and   */
+	                     /* columns of each element matrix made identity, and */
+	                     /* each node's row block multiplied by its D^-1      */
 } femgpu_euler_opts;
 
 void femgpu_euler_default_opts(femgpu_euler_opts *o);
@@ -404,6 +410,13 @@ int femgpu_euler_build_dev(femgpu_euler *ctx);
 /* precond_setup (BlockDiag_precond_EBE_setup.c:6-86 with PGMRES: R := D^-1 R;
  * FGMRES leaves R unpreconditioned).  R_host [neq+1] receives R (NULL skips). */
 int femgpu_euler_precond_setup(femgpu_euler *ctx, double *R_host);
+/* FemFunctions->scaling = Block_scaling_EBE (Block_scaling.c:7-49; Scaling
+ * "BlockScaling", EBE storage): after a Build, the block diagonal of the
+ * current matrix set up and R := D^-1 R, then the element matrices scaled
+ * (opts.scaling makes the predictor call it after every Build). R_host
+ * [neq+1] and Ae_host [nel*144] receive the results when non-NULL. */
+int femgpu_euler_scale_dev(femgpu_euler *eu);
+int femgpu_euler_scale(femgpu_euler *eu, double *R_host, double *Ae_host);
 int femgpu_euler_precond_setup_dev(femgpu_euler *ctx);
 /* solver (pgmres.c:4-211 with FemFunctions->mv = ebemvNDOF4): Da solves
  * A Da = R.  B_host [neq+1] replaces R when non-NULL; X_host receives Da. */

@@ -21,6 +21,7 @@ void myfree(void *);
 int ebemvNDOF4(ParametersType *, MatrixDataType *, FemStructsType *, double *, double *);
 int BlockDiag_precond_EBE_setup(ParametersType *, MatrixDataType *, FemStructsType *, int, double *);
 int BlockDiag_precond(ParametersType *, MatrixDataType *, FemStructsType *, double *, double *);
+int Block_scaling_EBE(ParametersType *, MatrixDataType *, FemStructsType *);
 int Build_M_K_F_SUPG(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *);
 double Delta_CAU(double, double *, double *, double *, double (*)[4], double (*)[4], double (*)[4],
                  double *, double, double, double, double, double, double, double, int, double *, double *);
@@ -111,6 +112,23 @@ int ref_euler_build(int nnodes, const double *x, const double *y, const int *nod
 	return 0;
 }
 
+/* One Build followed by the scaling Block_scaling_EBE (Block_scaling.c:7-49,
+ * the Scaling "BlockScaling" of setScaling.c): scaled Ae [nel*144] and R. */
+int ref_euler_build_scaled(int nnodes, const double *x, const double *y, const int *node_id, int nel,
+                           const int *vert, int neq, double alpha, double dt, double stab_tol, const double *u,
+                           const double *du, double *Ae, double *R)
+{
+	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF;
+	setup(0, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
+	memcpy(FS->u, u, sizeof(double) * (neq + 1));
+	memcpy(FS->du, du, sizeof(double) * (neq + 1));
+	Build_M_K_F_SUPG(P, M, FS, FF);
+	Block_scaling_EBE(P, M, FS);
+	memcpy(Ae, M->Aaux, sizeof(double) * nel * 144);
+	memcpy(R, FS->F, sizeof(double) * (neq + 1));
+	return 0;
+}
+
 /* A slip-wall angle with the shape of the reference's BC_theta plug-ins
  * (CYLINDER/CYLINDER_theta.c: atan(-x/y) about the cylinder's centre); here
  * about (2, -1), below the REFLETIDO domain, so it is defined on every wall
@@ -149,7 +167,7 @@ int ref_euler_build_slip(int nnodes, const double *x, const double *y, const int
 /* Predictor_Old.c:46-132 with ncorr correctors per step (StopByIterations,
  * Criteria.c:25-31) and nsteps steps, BlockDiag + EBE + the GMRES above.
  * u in/out; ahist [nsteps*(neq+1)], uhist likewise; iters [nsteps*ncorr]. */
-static int predictor(int csr, int nnodes, const double *x, const double *y, const int *node_id, int nel,
+static int predictor(int csr, int scaling, int nnodes, const double *x, const double *y, const int *node_id, int nel,
                      const int *vert, int neq, double alpha, double dt, double stab_tol, int kmax,
                      int lmax, double tol, int nsteps, int ncorr, double *u_io, double *uhist, int *iters)
 {
@@ -164,6 +182,7 @@ static int predictor(int csr, int nnodes, const double *x, const double *y, cons
 		for (i = 0; i < ncorr; i++) {
 			int before = P->iterations;
 			Build_M_K_F_SUPG(P, M, FS, FF);
+			if (scaling) Block_scaling_EBE(P, M, FS);       /* Predictor_Old.c:73 */
 			FF->precond_setup(P, M, FS, tag++, R);
 			gmres6(P, M, FS, FF, R, Da);
 			iters[step * ncorr + i] = P->iterations - before;
@@ -181,7 +200,16 @@ int ref_euler_predictor(int nnodes, const double *x, const double *y, const int 
                         const int *vert, int neq, double alpha, double dt, double stab_tol, int kmax,
                         int lmax, double tol, int nsteps, int ncorr, double *u_io, double *uhist, int *iters)
 {
-	return predictor(0, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, kmax, lmax, tol, nsteps, ncorr,
+	return predictor(0, 0, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, kmax, lmax, tol, nsteps, ncorr,
+	                 u_io, uhist, iters);
+}
+
+/* The same predictor with Block_scaling_EBE after every Build. */
+int ref_euler_predictor_scaled(int nnodes, const double *x, const double *y, const int *node_id, int nel,
+                               const int *vert, int neq, double alpha, double dt, double stab_tol, int kmax,
+                               int lmax, double tol, int nsteps, int ncorr, double *u_io, double *uhist, int *iters)
+{
+	return predictor(0, 1, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, kmax, lmax, tol, nsteps, ncorr,
 	                 u_io, uhist, iters);
 }
 
@@ -190,7 +218,7 @@ int ref_euler_predictor_csr(int nnodes, const double *x, const double *y, const 
                             const int *vert, int neq, double alpha, double dt, double stab_tol, int kmax,
                             int lmax, double tol, int nsteps, int ncorr, double *u_io, double *uhist, int *iters)
 {
-	return predictor(1, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, kmax, lmax, tol, nsteps, ncorr,
+	return predictor(1, 0, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, kmax, lmax, tol, nsteps, ncorr,
 	                 u_io, uhist, iters);
 }
 

@@ -230,6 +230,8 @@ def main_euler():
                                         ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _dp, _dp,
                                         _ip]
     lib.ref_euler_predictor_csr.argtypes = lib.ref_euler_predictor.argtypes
+    lib.ref_euler_build_scaled.argtypes = lib.ref_euler_build.argtypes
+    lib.ref_euler_predictor_scaled.argtypes = lib.ref_euler_predictor.argtypes
     lib.ref_euler_build_slip.argtypes = [ctypes.c_int, _dp, _dp, _ip, _ip, ctypes.c_int, _ip, ctypes.c_int,
                                          ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp,
                                          _dp, _dp]
@@ -286,9 +288,20 @@ def main_euler():
         cs, sn = np.zeros(mesh.nnodes), np.zeros(mesh.nnodes)
         lib.ref_euler_build_slip(mesh.nnodes, mesh.x, mesh.y, nid, slip, mesh.nel, vert, neq, alpha, dt, stol, u,
                                  du, Ae_s, R_s, cs, sn)
+        # Scaling "BlockScaling": Block_scaling_EBE after the Build, and the predictor with it
+        Ae_b, R_b = np.zeros(mesh.nel * 144), np.zeros(neq + 1)
+        lib.ref_euler_build_scaled(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol, u, du,
+                                   Ae_b, R_b)
+        ups = pb.u0.copy()
+        uhs = np.zeros(nsteps * (neq + 1))
+        its_s = np.zeros(nsteps * ncorr, np.int32)
+        lib.ref_euler_predictor_scaled(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol,
+                                       kmax, lmax, tol, nsteps, ncorr, ups, uhs, its_s)
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id,
             amg_spec=np.array(AMG_SYS_SPEC), amg_Fp=amg_Fp,
+            bs_Ae=Ae_b.reshape(mesh.nel, 144), bs_R=R_b, bs_uhist=uhs.reshape(nsteps, neq + 1),
+            bs_iters=its_s.reshape(nsteps, ncorr),
             slip=slip, slip_cs=cs, slip_sn=sn, slip_Ae=Ae_s.reshape(mesh.nel, 144), slip_R=R_s,
             neq=neq, upresc=pb.upresc, u0=pb.u0, gamma=pb.gamma, alpha=alpha, dt=dt, stab_tol=stol,
             u=u, du=du, Ae=Ae.reshape(mesh.nel, 144), R=R, kmax=kmax, lmax=lmax, tol=tol,

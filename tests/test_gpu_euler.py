@@ -89,6 +89,23 @@ def test_euler_predictor_vs_reference(gpu_lib, name):
     assert np.abs(its.astype(int) - g["iters"].astype(int)).max() <= 1
 
 
+@pytest.mark.parametrize("name", CASES)
+def test_euler_block_scaling_vs_reference(gpu_lib, name):
+    """Scaling "BlockScaling" (Block_scaling_EBE after every Build,
+    Predictor_Old.c:73): the scaled element matrices and R bit-identical to
+    the reference's, and its predictor-multicorrector run within 1e-8."""
+    g = _load(name)
+    with _euler(g) as eu:
+        eu.Build(g["u"], g["du"])
+        R, Ae = eu.scaling(want_matrix=True)
+    assert np.array_equal(Ae, g["bs_Ae"])
+    assert np.array_equal(R, g["bs_R"])
+    with _euler(g, scaling="BlockScaling") as eu:
+        uh, its = eu.Predictor(g["u0"], int(g["nsteps"]))
+    assert _rel(uh, g["bs_uhist"]) < SOL_RTOL
+    assert np.abs(its.astype(int) - g["bs_iters"].astype(int)).max() <= 1
+
+
 def test_euler_build_large_vs_oracle(gpu_lib):
     import fem_codes_gb300 as fg
     m = structured_mesh(96, 24, lx=4.0, ly=1.0, perturb=0.25, seed=11)
