@@ -302,6 +302,9 @@ int femgpu_deck_euler_opts(const femgpu_deck *d, femgpu_euler_opts *o)
 	if (block_precond(d->Preconditioner, o->scheme == FEMGPU_CSR, &o->precond)) return FEMGPU_E_ARG;
 	if (strcasecmp(d->StabilizationForm, "SUPG") != 0 || strcasecmp(d->ShockCapture, "CAU") != 0)
 		return FEMGPU_E_ARG;
+	/* setScaling.c:6-27: "NOT", or "BlockScaling" with EBE storage only */
+	if (!strcasecmp(d->Scaling, "BlockScaling") && o->scheme == FEMGPU_EBE) o->scaling = 1;
+	else if (strcasecmp(d->Scaling, "NOT") != 0) return FEMGPU_E_ARG;
 	o->dimensionless = !strcasecmp(d->Dimensionless, "YES");
 	o->mach = d->Mach;
 	o->alpha = d->Alpha;

@@ -207,6 +207,22 @@ int femgpu_shim_euler_precond(ParametersType *P, MatrixDataType *M, FemStructsTy
 	return rc ? fail("precond", rc) : 0;
 }
 
+/* FemFunctions->scaling = Block_scaling_EBE (Block_scaling.c:7-49, chosen by
+ * setScaling.c:10-13 for Scaling "BlockScaling"): the element matrices
+ * scaled by the inverse nodal blocks on the device and F := D^-1 F; with
+ * femgpu_shim_euler_copy_matrix the scaled matrices are copied to Aaux.
+ * Scaling "NOT" does nothing, as NO_scaling (scaling.c) does. */
+int femgpu_shim_euler_scaling(ParametersType *P, MatrixDataType *M, FemStructsType *FS)
+{
+	int rc;
+	if (!strcasecmp(P->Scaling, "NOT")) return 0;
+	if (strcasecmp(P->Scaling, "BlockScaling") != 0) return fail("scaling (unknown Scaling)", FEMGPU_E_ARG);
+	if (!g_eu) return fail("scaling", FEMGPU_E_NOT_BUILT);
+	if (strcasecmp(P->MatrixVectorProductScheme, "EBE") != 0) return fail("scaling (CSR storage)", FEMGPU_E_ARG);
+	rc = femgpu_euler_scale(g_eu, FS->F, g_copy_matrix ? M->Aaux : NULL);
+	return rc ? fail("scaling", rc) : 0;
+}
+
 /* FemOtherFunctions->solver (EulerEquations.h:168): A X = B by the
  * reference's pgmres (or FGMRES, femgpu_shim_euler_use_fgmres); the inner
  * iterations are added to Parameters->iterations. */
@@ -226,6 +242,7 @@ void femgpu_shim_euler_install(FemFunctionsType *FF, FemOtherFunctionsType *FOF)
 	FF->mv = femgpu_shim_euler_mv;
 	FF->precond = femgpu_shim_euler_precond;
 	FF->precond_setup = femgpu_shim_euler_precond_setup;
+	FF->scaling = femgpu_shim_euler_scaling;
 	FOF->solver = femgpu_shim_euler_solver;
 	FOF->Build = femgpu_shim_euler_Build;
 }

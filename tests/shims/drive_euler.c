@@ -1,7 +1,7 @@
 /*
  * Test infrastructure: drives femgpu_shim_euler.c the way Predictor_Old.c:
  * 46-126 does (predict u += (1 - alpha) dt a, a = 0; per corrector Build,
- * precond_setup, the 6-argument solver, a += Da, u += alpha dt Da) through the
+ * scaling, precond_setup, the 6-argument solver, a += Da, u += alpha dt Da) through the
  * reference's struct layout (shim_types_euler.h), with the REFLETIDO
  * plug-ins: inflow x = 0 (1, 2.9, 0, 5.990715), top (1.7, 4.452878,
  * -0.860744, 9.870181681), rho v = 0 on the bottom wall, gamma 1.4.
@@ -24,6 +24,11 @@ static double rhop(double x, double y) { (void)y; return left(x) ? 1.0 : 1.7; }
 static double v1p(double x, double y) { (void)y; return left(x) ? 2.9 : 4.452878; }
 static double v2p(double x, double y) { return (left(x) || fabs(y) <= 1e-15) ? 0.0 : -0.860744; }
 static double ep(double x, double y) { (void)y; return left(x) ? 5.990715 : 9.870181681; }
+
+static int g_scaling;
+/* on != 0: Scaling "BlockScaling", FemFunctions->scaling called after each
+ * Build as Predictor_Old.c:73 does */
+void drive_euler_set_scaling(int on) { g_scaling = on; }
 
 /* nsteps time steps of ncorr correctors from u0 [neq+1]; uhist
  * [nsteps*(neq+1)], iters [nsteps*ncorr].  Returns 0 or a negative code. */
@@ -49,7 +54,7 @@ int drive_euler(int nnodes, const double *x, const double *y, int nel, const int
 	strcpy(P.StabilizationForm, "SUPG");
 	strcpy(P.ShockCapture, "CAU");
 	strcpy(P.Preconditioner, "BlockDiag");
-	strcpy(P.Scaling, "NOT");
+	strcpy(P.Scaling, g_scaling ? "BlockScaling" : "NOT");
 	strcpy(P.StopMulticorrection, "ITERATION");
 	strcpy(P.reordering, "NOT");
 	strcpy(P.Dimensionless, "NO");
@@ -88,6 +93,7 @@ int drive_euler(int nnodes, const double *x, const double *y, int nel, const int
 		for (c = 0; c < ncorr && !rc; c++) {
 			int before = P.iterations;
 			rc = FOF.Build(&P, &M, &FS, &FF);
+			if (!rc) rc = FF.scaling(&P, &M, &FS);
 			if (!rc) rc = FF.precond_setup(&P, &M, &FS, 1, FS.F);
 			if (!rc) rc = FOF.solver(&P, &M, &FS, &FF, FS.F, Da);
 			iters[step * ncorr + c] = P.iterations - before;

@@ -40,6 +40,7 @@ int main(void)
 	}
 	strcpy(P.MatrixVectorProductScheme, "EBE"); strcpy(P.StabilizationForm, "SUPG");
 	strcpy(P.ShockCapture, "CAU"); strcpy(P.Preconditioner, "BlockDiag"); strcpy(P.Dimensionless, "NO");
+	strcpy(P.Scaling, "NOT");
 	P.SolverTolerance = 1e-8; P.StabilizationTolerance = 1e-6; P.Mach = 1.0; P.Alpha = 0.5; P.DeltaT = 1e-3;
 	P.KrylovBasisVectorsQuantity = 10; P.LinearMaxIter = 10; P.NonLinearMaxIter = 2;
 	P.nnodes = 4; P.nel = 2; P.neq = 4;

@@ -125,7 +125,19 @@ def test_euler_and_ns_decks(tmp_path):
     assert dd["Preconditioner"].startswith("AMG 2 3 -1 1.0 2") and dd["StopMulticorrection"] == "ITERATION"
     assert dd["DeltaT"] == 5e-3 and dd["NonLinearMaxIter"] == 2 and dd["nel"] == 162
     o = fg.deck_opts(d)
-    assert (o.scheme, o.precond, o.kmax, o.lmax, o.ncorr) == (2, 5, 50, 100, 2)
+    assert (o.scheme, o.precond, o.kmax, o.lmax, o.ncorr, o.scaling) == (2, 5, 50, 100, 2, 0)
+    # setScaling.c:6-27: BlockScaling with EBE storage, rejected with CSR
+    for scheme, pre, ok in (("EBE", "BlockDiag", True), ("CSR", "ILU0", False)):
+        t = text.replace("NOT\t:scaling", "BlockScaling\t:scaling").replace("CSR\t:scheme", f"{scheme}\t:scheme")
+        t = t.replace("AMG 2 3 -1 1.0 2\t:Preconditioner", f"{pre}\t:Preconditioner")
+        path.write_bytes(t.encode())
+        db = fg.read_deck(str(path), "euler")
+        assert db.as_dict()["Scaling"] == "BlockScaling"
+        if ok:
+            assert fg.deck_opts(db).scaling == 1
+        else:
+            with pytest.raises(fg.FemGpuError):
+                fg.deck_opts(db)
     ns = [("E", "e"), ("CAVITY", "t"), ("1000", "re"), ("1", "vmax"), ("0.1", "tol"), ("2", "case"),
           ("1e-8", "nl"), ("50", "maxit"), ("30", "krylov"), ("GMRES", "solver")]
     text = "".join(f"{v}\t:{lab}\r\n" for v, lab in ns) + "ILU0\t:Preconditioner\r\n"

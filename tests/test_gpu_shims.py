@@ -71,9 +71,15 @@ def test_transport_shim_reproduces_reference_picard_run(gpu_lib, tmp_path):
     assert np.all(np.abs(its - g["iters"]) <= 1), (its, g["iters"])
 
 
-def test_euler_shim_reproduces_reference_predictor_run(gpu_lib, tmp_path):
+@pytest.mark.parametrize("scaling", [False, True])
+def test_euler_shim_reproduces_reference_predictor_run(gpu_lib, tmp_path, scaling):
+    """The reference's predictor loop through the shim's function pointers;
+    with Scaling "BlockScaling" its scaling (Block_scaling_EBE) runs after
+    each Build and the run follows the reference's scaled one."""
     g = dict(np.load(os.path.join(ROOT, "tests", "golden", "eul_refletido_16x4.npz")))
     L = _driver("euler", tmp_path)
+    L.drive_euler_set_scaling(int(scaling))
+    pre = "bs_" if scaling else ""
     f = L.drive_euler
     f.restype = ctypes.c_int
     f.argtypes = [ctypes.c_int, _dp, _dp, ctypes.c_int, _ip, _ip, ctypes.c_int, _dp, ctypes.c_double,
@@ -95,6 +101,6 @@ def test_euler_shim_reproduces_reference_predictor_run(gpu_lib, tmp_path):
            int(g["lmax"]), float(g["tol"]), ns, nc, uh, its)
     assert rc == 0, rc
     uh = uh.reshape(ns, neq + 1)
-    ref = g["uhist"].reshape(ns, neq + 1)
+    ref = g[pre + "uhist"].reshape(ns, neq + 1)
     assert np.abs(uh - ref).max() / np.abs(ref).max() < SOL_RTOL
-    assert np.abs(its - g["iters"].reshape(-1)).max() <= 1, (its, g["iters"])
+    assert np.abs(its - g[pre + "iters"].reshape(-1)).max() <= 1, (its, g[pre + "iters"])
