@@ -642,15 +642,17 @@ class SSTransport:
                       nonlin_tol=1e-3, steady="NOT", time_tol=1e-6, method="Predictor1"):
         """Switch to the transient driver: Build_M_K_R_SUPG / Build_M_K_R_DD
         and the deck's TimeIntegration (Predictor1 | Predictor1_BDF |
-        Predictor1_TRBDF2) with its StopMulticorrection (ITERATION | NORM) and
-        StopAtSteadyState (YES | NOT)."""
+        Predictor1_TRBDF2, and with DD Predictor2 | Predictor2_BDF |
+        Predictor2_TRBDF2, which build with Build_M_F_DD) with its
+        StopMulticorrection (ITERATION | NORM) and StopAtSteadyState
+        (YES | NOT)."""
         o = TransientOpts(stab={"SUPG": 0, "DD": 1}[stab.upper()], alpha=alpha, dt=dt, final_time=final_time,
                           stop_norm={"ITERATION": 0, "NORM": 1}[stop.upper()], max_corr=int(max_corr),
                           nonlin_tol=nonlin_tol, steady_stop={"NOT": 0, "YES": 1}[steady.upper()],
                           time_tol=time_tol,
                           method={"PREDICTOR1": 0, "PREDICTOR1_BDF": 1, "PREDICTOR1_TRBDF2": 2,
-                                  "PREDICTOR2": 3}[method.upper()])
-        self._stages = 2 if method.upper() == "PREDICTOR1_TRBDF2" else 1
+                                  "PREDICTOR2": 3, "PREDICTOR2_BDF": 4, "PREDICTOR2_TRBDF2": 5}[method.upper()])
+        self._stages = 2 if method.upper().endswith("_TRBDF2") else 1
         self._check(self._L.femgpu_transport_set_transient(self._h, ctypes.byref(o)), "set_transient")
 
     def build_transient(self, u=None, a=None, want_matrix=False):

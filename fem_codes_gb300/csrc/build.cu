@@ -597,6 +597,14 @@ extern "C" int fg_tr_lin(femgpu_transport *t, const double *p, const double *q, 
 	return (int)cudaGetLastError();
 }
 
+// Predictor_New_BDF.c:144-147 / Predictor_New_TRBDF2.c:155-158 for the
+// bubbles: uB = cp p - cq q, aB = 0 (uB may be p).
+extern "C" int fg_bubble_lin(femgpu_transport *t, const double *p, const double *q, double cp, double cq)
+{
+	k_tr_lin<<<fg_grid(t->nel), FG_TPB, 0, t->stream>>>(t->uB, p, q, t->aB, t->nel, cp, cq);
+	return (int)cudaGetLastError();
+}
+
 // Criteria.c:52-53: diff = u - u_old (into Da, free between steps).
 __global__ void k_tr_diff(const double *u, const double *uold, double *d, int n)
 {

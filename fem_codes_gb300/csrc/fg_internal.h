@@ -193,6 +193,8 @@ struct femgpu_transport {
 	double *uold, *Da, *u1, *u2;    /* predictor vectors (neq+1)             */
 	double *uB, *aB, *bub;          /* Predictor_New: bubble unknowns, rate, and
 	                                   invN2, R2, M2[3] per element          */
+	double *uB1, *uB2;              /* Predictor_New_BDF / _TRBDF2: bubble
+	                                   history (nel each)                    */
 
 	/* Krylov workspace */
 	int kmax;
@@ -237,6 +239,7 @@ int fg_build_mfdd(femgpu_transport *t, double adt);          /* Me, re, bub   */
 int fg_bubble_correct(femgpu_transport *t, double c);        /* DaB, aB, uB   */
 int fg_bubble_predict(femgpu_transport *t, double c);
 int fg_bubble_init(femgpu_transport *t);
+int fg_bubble_lin(femgpu_transport *t, const double *p, const double *q, double cp, double cq);
 int fg_tr_axpy_zero(femgpu_transport *t, double c);          /* u += c a, a=0 */
 int fg_tr_lin(femgpu_transport *t, const double *p, const double *q, double cp, double cq); /* u=cp p-cq q */
 

@@ -1,8 +1,9 @@
 /*
  * The transient scalar transport driver (02_Transport_Equation/2D) on a
- * transport context: Build_M_K_R_SUPG / Build_M_K_R_DD on the device
- * (csrc/build.cu) and the predictor-multicorrector of
- * 00_CommonFiles/Time_Integration/Predictor_Old.c:3-148 with the stop
+ * transport context: Build_M_K_R_SUPG / Build_M_K_R_DD / Build_M_F_DD on the
+ * device (csrc/build.cu) and the predictor-multicorrectors of
+ * 00_CommonFiles/Time_Integration (Predictor_Old.c:3-148 and its BDF /
+ * TRBDF2 forms, Predictor_New.c and its BDF / TRBDF2 forms) with the stop
  * criteria of Criteria.c:22-79, every vector operation on the device and the
  * criteria's norms read back once per correction.  Plain C.
  */
@@ -41,8 +42,8 @@ int femgpu_transport_set_transient(femgpu_transport *t, const femgpu_transient_o
 		fgh_set_error("CAUDD shock capturing belongs to the DD build (setStabilizationForm.c:67)");
 		return FEMGPU_E_ARG;
 	}
-	if (o->method < FEMGPU_TI_PREDICTOR1 || o->method > FEMGPU_TI_PREDICTOR2 ||
-	    (o->method == FEMGPU_TI_PREDICTOR2 && o->stab != FEMGPU_STAB_DD)) {
+	if (o->method < FEMGPU_TI_PREDICTOR1 || o->method > FEMGPU_TI_PREDICTOR2_TRBDF2 ||
+	    (o->method >= FEMGPU_TI_PREDICTOR2 && o->stab != FEMGPU_STAB_DD)) {
 		fgh_set_error("time integration %d with stabilisation %d (setStabilizationForm.c:7-61)", o->method, o->stab);
 		return FEMGPU_E_ARG;
 	}
@@ -57,10 +58,15 @@ int femgpu_transport_set_transient(femgpu_transport *t, const femgpu_transient_o
 		if (t->o.scheme != FEMGPU_EBE && !t->ke && fgh_dmalloc((void **)&t->ke, sizeof(double) * 9 * (size_t)t->nel))
 			return FEMGPU_E_NOMEM;
 	}
-	if (o->method == FEMGPU_TI_PREDICTOR2 && !t->uB) {
+	if (o->method >= FEMGPU_TI_PREDICTOR2 && !t->uB) {
 		if (fgh_dmalloc((void **)&t->uB, sizeof(double) * (size_t)t->nel) ||
 		    fgh_dmalloc((void **)&t->aB, sizeof(double) * (size_t)t->nel) ||
 		    fgh_dmalloc((void **)&t->bub, sizeof(double) * 5 * (size_t)t->nel))
+			return FEMGPU_E_NOMEM;
+	}
+	if (o->method > FEMGPU_TI_PREDICTOR2 && !t->uB1) {
+		if (fgh_dmalloc((void **)&t->uB1, sizeof(double) * (size_t)t->nel) ||
+		    fgh_dmalloc((void **)&t->uB2, sizeof(double) * (size_t)t->nel))
 			return FEMGPU_E_NOMEM;
 	}
 	if (t->uB) {
@@ -90,7 +96,7 @@ int femgpu_transport_set_bubbles(femgpu_transport *t, const double *uB_host, con
 
 static int build_transient_dev(femgpu_transport *t)
 {
-	if (t->tr.method == FEMGPU_TI_PREDICTOR2) KR(fg_build_mfdd(t, t->tr.alpha * t->tr.dt));
+	if (t->tr.method >= FEMGPU_TI_PREDICTOR2) KR(fg_build_mfdd(t, t->tr.alpha * t->tr.dt));
 	else KR(fg_build_transient(t, t->tr.stab == FEMGPU_STAB_DD, t->tr.alpha * t->tr.dt));
 	KR(fg_assemble_transient(t));
 	t->built = 1;
@@ -233,6 +239,82 @@ int femgpu_transport_predictor(femgpu_transport *t, const double *u0_host, int m
 			KR(multicorrect(&L, c2));
 			if (t_hist) t_hist[step - 1] = time;
 			KR(stop_time(&L, t->uold, time, &done));
+		} while (!done && step < max_steps);
+	} else if (o->method == FEMGPU_TI_PREDICTOR2_BDF) {
+		/* Predictor_New_BDF.c:56-198: uB starts at zero (the file's
+		 * uB_InitialSolution call is commented out); one implicit step
+		 * built with Alpha_Build = 1, then BDF2 on u and uB with
+		 * Alpha_Build = 2/3; u_old is u before each BDF2 prediction */
+		const double four_thirds = 4.0/3.0, two_thirds = 2.0/3.0, one_third = 1.0/3.0;
+		const size_t nbB = sizeof(double) * (size_t)t->nel;
+		L.bubble = 1;
+		CK(cudaMemsetAsync(t->uB, 0, nbB, t->stream));
+		CK(cudaMemsetAsync(t->aB, 0, nbB, t->stream));
+		step = 1;
+		time += dt;
+		L.Alpha = 1.0;
+		L.AlphaB = 1.0;
+		CK(cudaMemcpyAsync(t->u1, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+		CK(cudaMemcpyAsync(t->uB1, t->uB, nbB, cudaMemcpyDeviceToDevice, t->stream));
+		KR(multicorrect(&L, dt));
+		CK(cudaMemcpyAsync(t->u2, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+		CK(cudaMemcpyAsync(t->uB2, t->uB, nbB, cudaMemcpyDeviceToDevice, t->stream));
+		if (t_hist) t_hist[0] = time;
+		L.Alpha = two_thirds;
+		L.AlphaB = two_thirds;
+		while (step < max_steps) {
+			step++;
+			time += dt;
+			CK(cudaMemcpyAsync(t->uold, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+			KR(fg_tr_lin(t, t->u2, t->u1, four_thirds, one_third));    /* u = 4/3 u2 - 1/3 u1, a = 0 */
+			KR(fg_bubble_lin(t, t->uB2, t->uB1, four_thirds, one_third));
+			KR(multicorrect(&L, two_thirds * dt));
+			CK(cudaMemcpyAsync(t->u1, t->u2, nb, cudaMemcpyDeviceToDevice, t->stream));
+			CK(cudaMemcpyAsync(t->u2, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+			CK(cudaMemcpyAsync(t->uB1, t->uB2, nbB, cudaMemcpyDeviceToDevice, t->stream));
+			CK(cudaMemcpyAsync(t->uB2, t->uB, nbB, cudaMemcpyDeviceToDevice, t->stream));
+			if (t_hist) t_hist[step - 1] = time;
+			KR(stop_time(&L, t->uold, time, &done));
+			if (done) break;
+		}
+	} else if (o->method == FEMGPU_TI_PREDICTOR2_TRBDF2) {
+		/* Predictor_New_TRBDF2.c:52-199: TR then BDF2 stages on u and uB,
+		 * DeltaT_Build and Alpha_Build set per stage; uB_old starts at zero
+		 * and u_old at the initial solution, both copied after each BDF2
+		 * stage */
+		const double lambda = 2.0 - sqrt(2.0);
+		const double A = 1.0/(lambda*(2.0 - lambda));
+		const double B = (1.0 - lambda)*(1.0 - lambda)/(lambda*(2.0 - lambda));
+		const double dtTR = lambda*dt, dtBDF2 = (1.0 - lambda)*dt;
+		const size_t nbB = sizeof(double) * (size_t)t->nel;
+		double *u_old = t->u1, *uB_old = t->uB1;
+		L.bubble = 1;
+		KR(fg_bubble_init(t));                                /* uB_InitialSolution, aB = 0 */
+		CK(cudaMemsetAsync(uB_old, 0, nbB, t->stream));
+		CK(cudaMemcpyAsync(u_old, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+		do {
+			const double a_tr = 0.5, a_bdf = 1.0/(2.0 - lambda);
+			L.DeltaT = dtTR;
+			L.DeltaTB = dtTR;
+			L.Alpha = a_tr;
+			L.AlphaB = a_tr;
+			step++;
+			time += dtTR;
+			KR(fg_tr_axpy_zero(t, a_tr*dtTR));                  /* u += alpha dtTR a, a = 0 */
+			KR(fg_bubble_predict(t, a_tr*dtTR));                /* uB += alpha dtTR aB, aB = 0 */
+			KR(multicorrect(&L, a_tr*dtTR));
+			L.Alpha = a_bdf;
+			L.AlphaB = a_bdf;
+			L.DeltaT = dtBDF2;
+			L.DeltaTB = dtBDF2;
+			time += dtBDF2;
+			KR(fg_tr_lin(t, t->u, u_old, A, B));                 /* u = A u - B u_old, a = 0 */
+			KR(fg_bubble_lin(t, t->uB, uB_old, A, B));           /* uB = A uB - B uB_old, aB = 0 */
+			KR(multicorrect(&L, a_bdf*dtBDF2));
+			CK(cudaMemcpyAsync(u_old, t->u, nb, cudaMemcpyDeviceToDevice, t->stream));
+			CK(cudaMemcpyAsync(uB_old, t->uB, nbB, cudaMemcpyDeviceToDevice, t->stream));
+			if (t_hist) t_hist[step - 1] = time;
+			KR(stop_time(&L, u_old, time, &done));
 		} while (!done && step < max_steps);
 	} else if (o->method == FEMGPU_TI_PREDICTOR1) {
 		/* Predictor_Old.c:62-136 */

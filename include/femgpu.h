@@ -243,12 +243,18 @@ typedef struct femgpu_transient_opts {
  * (2 - sqrt 2) dt, then a BDF2 stage), each with the reference's own
  * Alpha / DeltaT bookkeeping for the builds. */
 enum femgpu_time_integration { FEMGPU_TI_PREDICTOR1 = 0, FEMGPU_TI_BDF = 1, FEMGPU_TI_TRBDF2 = 2,
-                               FEMGPU_TI_PREDICTOR2 = 3 };
+                               FEMGPU_TI_PREDICTOR2 = 3, FEMGPU_TI_PREDICTOR2_BDF = 4,
+                               FEMGPU_TI_PREDICTOR2_TRBDF2 = 5 };
 /* Predictor2 (Predictor_New.c:3-137, DD stabilisation only): the element
  * bubbles are unknowns of the time loop -- uB starts at each element's mean
  * nodal value (uB_InitialSolution.c), the build is Build_M_F_DD
  * (Build_M_F_DD.c:6-218: the bubble row condensed into the element matrix),
- * and after every solve calculate_DaB.c updates the bubbles. */
+ * and after every solve calculate_DaB.c updates the bubbles.
+ * Predictor2_BDF (Predictor_New_BDF.c:3-216: uB starts at zero, one implicit
+ * step built with Alpha_Build = 1, then BDF2 on u and uB) and
+ * Predictor2_TRBDF2 (Predictor_New_TRBDF2.c:3-228: a trapezoidal and a BDF2
+ * stage per step on u and uB, DeltaT_Build set per stage) are the same with
+ * the two multistep forms (setStabilizationForm.c:54-61). */
 int femgpu_transport_set_transient(femgpu_transport *ctx, const femgpu_transient_opts *o);
 /* One transient Build on the state (u, a) (host [neq+1]; NULL: the context's):
  * R_host [neq+1] the residual, A_host the storage values (as

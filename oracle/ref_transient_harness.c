@@ -11,7 +11,8 @@
  * Diag / ILU(0) preconditioners, the CONE / CONE2 / CARTOLA / PUDIM
  * plug-ins, and the time loops themselves: 00_CommonFiles/Time_Integration/
  * Predictor_Old.c, Predictor_Old_BDF.c, Predictor_Old_TRBDF2.c and
- * Predictor_New.c (with Build_M_F_DD.c, calculate_DaB.c, uB_InitialSolution.c)
+ * Predictor_New.c, Predictor_New_BDF.c and Predictor_New_TRBDF2.c (with
+ * Build_M_F_DD.c, calculate_DaB.c, uB_InitialSolution.c)
  * with the stop criteria of Criteria.c.
  *
  * One documented adapter: the driver's solver pointer takes (B, X)
@@ -108,8 +109,9 @@ static int solver_rec(ParametersType *P, MatrixDataType *M, FemStructsType *FS, 
  *   problem: 0 CONE, 1 CONE2, 2 CARTOLA, 3 PUDIM; ntype: Node Type (1 free, 0 prescribed)
  *   stab "SUPG" | "DD"; shock "CAU" | "CAUDD" | "YZBeta"; hshock "2sqrtArea" | "Option1" | "Option2"
  *   stopmc "ITERATION" | "NORM"; steady "YES" | "NOT"
- *   tint "Predictor1" | "Predictor1_BDF" | "Predictor1_TRBDF2" | "Predictor2" (setStabilizationForm.c:10-58;
- *   Predictor2 runs Predictor_New with Build_M_F_DD)
+ *   tint "Predictor1" | "Predictor1_BDF" | "Predictor1_TRBDF2" | "Predictor2" | "Predictor2_BDF" |
+ *   "Predictor2_TRBDF2" (setStabilizationForm.c:10-62; the Predictor2 forms run Predictor_New* with
+ *   Build_M_F_DD)
  * Outputs:
  *   info [5] = neq, nnzero, nedge, bandwidth after reordering, (out) time checks; node_id [nnodes]
  *   beta [2*nel], fsrc [3*nel], upresc [nnodes]: the plug-ins as Build evaluates them
@@ -243,7 +245,7 @@ int ref_transient_run(int nnodes, const double *x, const double *y, const int *n
 	FF->precondR = NO_precond;
 	FF->scaling = noscale;
 	FF->unscaling = nounscale;
-	int predictor2 = strcasecmp(tint, "Predictor2") == 0;
+	int predictor2 = strncasecmp(tint, "Predictor2", 10) == 0;
 	FOF->Build = predictor2 ? Build_M_F_DD : strcasecmp(stab, "DD") == 0 ? Build_M_K_R_DD : Build_M_K_R_SUPG;
 	FF->ShockCapture = strcasecmp(shock, "YZBeta") == 0 ? YZBeta_ShockCapture
 	                 : strcasecmp(shock, "CAUDD") == 0 ? CAU_DD_ShockCapture : CAU_ShockCapture;
@@ -311,6 +313,8 @@ int ref_transient_run(int nnodes, const double *x, const double *y, const int *n
 	FOF->solver = solver_rec;
 	if (strcasecmp(tint, "Predictor1_BDF") == 0) Predictor_Old_BDF(P, M, FS, FF, FOF);
 	else if (strcasecmp(tint, "Predictor1_TRBDF2") == 0) Predictor_Old_TRBDF2(P, M, FS, FF, FOF);
+	else if (strcasecmp(tint, "Predictor2_BDF") == 0) Predictor_New_BDF(P, M, FS, FF, FOF);
+	else if (strcasecmp(tint, "Predictor2_TRBDF2") == 0) Predictor_New_TRBDF2(P, M, FS, FF, FOF);
 	else if (predictor2) Predictor_New(P, M, FS, FF, FOF);
 	else Predictor_Old(P, M, FS, FF, FOF);
 	info[4] = g_tcheck;

@@ -562,6 +562,12 @@ TT_CASES = {
     "tt_cone2_12_ebe_diag_dd_predictor2": dict(problem="CONE2", n=12, scheme="EBE", precond="Diag", stab="DD",
                                                shock="CAU", hshock="Option1", tint="Predictor2", dt=0.05,
                                                final=0.5, stopmc="NORM", max_corr=3),
+    "tt_cone16_csr_ilu0_dd_predictor2_bdf": dict(problem="CONE", n=16, scheme="CSR", reord="SYMRCM",
+                                                 precond="ILU0", stab="DD", shock="CAUDD", tint="Predictor2_BDF",
+                                                 maxsteps=8),
+    "tt_cone2_12_ebe_diag_dd_predictor2_trbdf2": dict(problem="CONE2", n=12, scheme="EBE", precond="Diag",
+                                                      stab="DD", shock="CAU", tint="Predictor2_TRBDF2", dt=0.05,
+                                                      maxsteps=6),
 }
 
 
@@ -637,10 +643,11 @@ def run_transient(lib, name, case):
           f"iters={its.reshape(cap, 64)[:stages, 0].tolist()}")
 
 
-def main_transient():
+def main_transient(names=()):
     lib = transient_lib()
     for name, case in TT_CASES.items():
-        run_transient(lib, name, case)
+        if not names or name in names:
+            run_transient(lib, name, case)
 
 
 def main(only=()):
@@ -657,6 +664,9 @@ def main(only=()):
         return
     if only == ("transient",):
         main_transient()
+        return
+    if only and all(n in TT_CASES for n in only):
+        main_transient(only)
         return
     if not only:
         main_transient()

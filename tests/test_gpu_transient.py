@@ -7,8 +7,9 @@ oracle/ref_transient_harness.c from the reference's sources):
   Build_M_K_R_DD or Build_M_F_DD (with seeded bubbles), the DD builds' second
   build reading the first one's per-element shock parameter -- matrix storage
   and residual bit-identical;
-* the reference's time loop (Predictor_Old, Predictor_Old_BDF or
-  Predictor_Old_TRBDF2) from the problem's initial solution: u at the end of
+* the reference's time loop (Predictor_Old, Predictor_Old_BDF,
+  Predictor_Old_TRBDF2, Predictor_New, Predictor_New_BDF or
+  Predictor_New_TRBDF2) from the problem's initial solution: u at the end of
   every multicorrection stage within 1e-8 relative, the same times and
   corrections per stage, GMRES iterations within 1 (the device reductions sum
   in another order).
@@ -23,7 +24,8 @@ step, past 1e-8 after 11 steps); BDF2
 on CONE (CSR, SYMRCM, ILU(0)) and TR-BDF2 on CONE2 (DD + CAUDD) and CARTOLA
 (EBE, Diag); Predictor_New with Build_M_F_DD (the element bubbles as unknowns
 of the time loop) on CONE (CSR, SYMRCM, ILU(0), CAUDD) and CONE2 (EBE, Diag,
-CAU, Option1, NORM)."""
+CAU, Option1, NORM); Predictor_New_BDF on CONE (CSR, SYMRCM, ILU(0), CAUDD)
+and Predictor_New_TRBDF2 on CONE2 (EBE, Diag, CAU)."""
 import ast
 import glob
 import os
@@ -66,7 +68,7 @@ def test_transient_builds_and_predictor(gpu_lib, name):
         if c["scheme"] == "CSR":
             assert np.array_equal(pat["IA"], g["IA"]) and np.array_equal(pat["JA"], g["JA"]), "CSR pattern"
             assert np.array_equal(pat["sbe"], g["sbe"]), "CSR_by_Element"
-        if c["tint"].upper() == "PREDICTOR2":
+        if c["tint"].upper().startswith("PREDICTOR2"):
             T.set_bubbles(g["ubB"], g["dubB"])
         R1, A1 = T.build_transient(g["ub"], g["dub"], want_matrix=True)
         assert np.array_equal(A1, g["A1"]), "first build: matrix"
@@ -75,7 +77,7 @@ def test_transient_builds_and_predictor(gpu_lib, name):
         assert np.array_equal(A2, g["A2"]), "second build: matrix"
         assert np.array_equal(R2[:neq], g["R2"][:neq]), "second build: residual"
         # the reference asks its time criterion after every step but BDF's first
-        bdf = c["tint"].upper() == "PREDICTOR1_BDF"
+        bdf = c["tint"].upper() in ("PREDICTOR1_BDF", "PREDICTOR2_BDF")
         steps = int(g["tchecks"]) + (1 if bdf else 0)
         out = T.predictor(g["u0"], steps, iters_cap=64)
     assert len(out["t"]) == steps and len(out["ncorr"]) == int(g["stages"])
