@@ -161,6 +161,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_transport_predictor": [_vp, _vp, ctypes.c_int, _vp, _vp, _vp, _vp, ctypes.c_int],
         "femgpu_deck_transport_opts": [_vp, _vp],
         "femgpu_deck_euler_opts": [_vp, _vp],
+        "femgpu_deck_transient_opts": [_vp, _vp, _vp],
         "femgpu_deck_ns_opts": [_vp, _vp],
         "femgpu_deck_amg": [_vp, _vp, _vp, _vp, _vp],
         "femgpu_ilu_chain_segments": [ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
@@ -311,8 +312,9 @@ def ilu_block_cut(IA, JA, P):
     return first[: rc + 1]
 
 
-EQUATIONS = {"transport": 0, "euler": 1, "ns": 2}
-NODE_TYPES = {"transport": 1, "euler": 4, "ns": 3}
+EQUATIONS = {"transport": 0, "euler": 1, "ns": 2, "transient": 3}
+NODE_TYPES = {"transport": 1, "euler": 4, "ns": 3, "transient": 1}
+MESH_NO_ELEM_TYPE = 0x100            # FEMGPU_MESH_NO_ELEM_TYPE: the transient driver's element lines
 
 
 def read_deck(path, equation="transport"):
@@ -340,19 +342,21 @@ def read_mesh(path, equation="transport"):
     """A mesh file in the drivers' format: dict(x, y, node_type [nnodes, k],
     vert [nel, 3], elem_type).  For transport the element types are the
     boundary sides its Preprocess sets (femgpu_mesh_side_types); Euler and
-    Navier-Stokes keep the file's column."""
+    Navier-Stokes keep the file's column; the transient transport files have
+    none (element types 0)."""
     L = load()
     k = NODE_TYPES[equation]
+    kf = k | (MESH_NO_ELEM_TYPE if equation == "transient" else 0)
     nn, ne = ctypes.c_int(0), ctypes.c_int(0)
     p = os.fsencode(path)
-    rc = L.femgpu_mesh_read(p, k, ctypes.byref(nn), ctypes.byref(ne), None, None, None, None, None)
+    rc = L.femgpu_mesh_read(p, kf, ctypes.byref(nn), ctypes.byref(ne), None, None, None, None, None)
     if rc:
         raise FemGpuError(rc, f"read_mesh {path}")
     x, y = np.zeros(nn.value), np.zeros(nn.value)
     nt = np.zeros((nn.value, k), np.int32)
     vert = np.zeros((ne.value, 3), np.int32)
     et = np.zeros(ne.value, np.int32)
-    rc = L.femgpu_mesh_read(p, k, ctypes.byref(nn), ctypes.byref(ne), _ptr(x), _ptr(y), _ptr(nt), _ptr(vert),
+    rc = L.femgpu_mesh_read(p, kf, ctypes.byref(nn), ctypes.byref(ne), _ptr(x), _ptr(y), _ptr(nt), _ptr(vert),
                             _ptr(et))
     if rc:
         raise FemGpuError(rc, f"read_mesh {path}")
@@ -364,9 +368,16 @@ def read_mesh(path, equation="transport"):
 
 
 def deck_opts(deck):
-    """The deck's strings as the library's options (Opts, EulerOpts or NSOpts)."""
+    """The deck's strings as the library's options (Opts, EulerOpts or NSOpts;
+    for a transient transport deck the pair (Opts, TransientOpts))."""
     L = load()
     eq = deck.equation
+    if eq == EQUATIONS["transient"]:
+        o, tr = Opts(), TransientOpts()
+        rc = L.femgpu_deck_transient_opts(ctypes.byref(deck), ctypes.byref(o), ctypes.byref(tr))
+        if rc:
+            raise FemGpuError(rc, "deck_opts")
+        return o, tr
     o = (Opts, EulerOpts, NSOpts)[eq]()
     f = (L.femgpu_deck_transport_opts, L.femgpu_deck_euler_opts, L.femgpu_deck_ns_opts)[eq]
     rc = f(ctypes.byref(deck), ctypes.byref(o))

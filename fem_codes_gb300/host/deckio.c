@@ -30,7 +30,7 @@ int femgpu_deck_read(const char *path, int equation, femgpu_deck *d)
 	char label[2048];
 	FILE *f;
 	int bad = 0;
-	if (!path || !d || equation < FEMGPU_EQ_TRANSPORT || equation > FEMGPU_EQ_NS) return FEMGPU_E_ARG;
+	if (!path || !d || equation < FEMGPU_EQ_TRANSPORT || equation > FEMGPU_EQ_TRANSIENT) return FEMGPU_E_ARG;
 	f = fopen(path, "r");
 	if (!f) { fgh_set_error("deck %s: cannot open", path); return FEMGPU_E_ARG; }
 	memset(d, 0, sizeof *d);
@@ -51,6 +51,31 @@ int femgpu_deck_read(const char *path, int equation, femgpu_deck *d)
 		RD("%199s\t:%2047[^\n]\n", d->ShockCapture, label);
 		RD("%199s\t:%2047[^\n]\n", d->h_Shock, label);
 		RD("%199s\t:%2047[^\n]\n", d->OutputFlow, label);
+		RD("%d\t:%2047[^\n]\n", &d->nnodes, label);
+		RD("%d\t:%2047[^\n]\n", &d->nel, label);
+	} else if (equation == FEMGPU_EQ_TRANSIENT) {     /* 02_Transport_Equation Preprocess.c:42-66 */
+		RD("%299s\t:%2047[^\n]\n", d->ProblemTitle, label);
+		RD("%lf\t:%2047[^\n]\n", &d->SolverTolerance, label);
+		RD("%lf\t:%2047[^\n]\n", &d->NonLinearTolerance, label);
+		RD("%lf\t:%2047[^\n]", &d->TimeIntegrationTolerance, label);
+		RD("%lf\t:%2047[^\n]", &d->StabilizationTolerance, label);
+		RD("%d\t:%2047[^\n]\n", &d->NonLinearMaxIter, label);
+		RD("%d\t:%2047[^\n]\n", &d->LinearMaxIter, label);
+		RD("%199s\t:%2047[^\n]\n", d->StopAtSteadyState, label);
+		RD("%d\t:%2047[^\n]\n", &d->KrylovBasisVectorsQuantity, label);
+		RD("%199s\t:%2047[^\n]\n", d->Solver, label);
+		RD("%999s\t:%2047[^\n]\n", d->Preconditioner, label);
+		RD("%199s\t:%2047[^\n]\n", d->Scaling, label);
+		RD("%199s\t:%2047[^\n]\n", d->reordering, label);
+		RD("%199s\t:%2047[^\n]\n", d->MatrixVectorProductScheme, label);
+		RD("%199s\t:%2047[^\n]\n", d->StabilizationForm, label);
+		RD("%199s\t:%2047[^\n]\n", d->ShockCapture, label);
+		RD("%199s\t:%2047[^\n]\n", d->h_Shock, label);
+		RD("%199s\t:%2047[^\n]\n", d->TimeIntegration, label);
+		RD("%lf\t:%2047[^\n]\n", &d->Alpha, label);
+		RD("%lf\t:%2047[^\n]\n", &d->DeltaT, label);
+		RD("%199s\t:%2047[^\n]", d->StopMulticorrection, label);
+		RD("%lf\t:%2047[^\n]\n", &d->FinalTime, label);
 		RD("%d\t:%2047[^\n]\n", &d->nnodes, label);
 		RD("%d\t:%2047[^\n]\n", &d->nel, label);
 	} else if (equation == FEMGPU_EQ_EULER) {         /* Preprocess.c:45-74 */
@@ -154,7 +179,8 @@ int femgpu_mesh_read(const char *path, int ntype, int *nnodes, int *nel, double 
 	FILE *f;
 	char *buf = NULL, *p, *end;
 	long len;
-	int nn = 0, ne = 0, i, k, v, rc = 0;
+	int nn = 0, ne = 0, i, k, v, rc = 0, etype_col = !(ntype & FEMGPU_MESH_NO_ELEM_TYPE);
+	ntype &= ~FEMGPU_MESH_NO_ELEM_TYPE;
 	if (!path || !nnodes || !nel || ntype < 1 || ntype > 4) return FEMGPU_E_ARG;
 	f = fopen(path, "rb");
 	if (!f) { fgh_set_error("mesh %s: cannot open", path); return FEMGPU_E_ARG; }
@@ -185,7 +211,8 @@ int femgpu_mesh_read(const char *path, int ntype, int *nnodes, int *nel, double 
 				if (!next_int(&p, end, &v) || v < 0 || v >= nn) { rc = FEMGPU_E_MESH; goto out; }
 				if (vert) vert[3 * (size_t)i + k] = v;
 			}
-			if (!next_int(&p, end, &v)) { rc = FEMGPU_E_MESH; goto out; }
+			v = 0;
+			if (etype_col && !next_int(&p, end, &v)) { rc = FEMGPU_E_MESH; goto out; }
 			if (elem_type) elem_type[i] = v;
 		}
 	}
@@ -260,6 +287,60 @@ int femgpu_deck_transport_opts(const femgpu_deck *d, femgpu_transport_opts *o)
 	o->lmax = d->SolverMaxIter;
 	o->tol = d->SolverTolerance;
 	o->nonlin_tol = d->NonLinearTolerance;
+	return 0;
+}
+
+int femgpu_deck_transient_opts(const femgpu_deck *d, femgpu_transport_opts *o, femgpu_transient_opts *tr)
+{
+	static const char *const methods[] = { "Predictor1", "Predictor1_BDF", "Predictor1_TRBDF2", "Predictor2",
+	                                       "Predictor2_BDF", "Predictor2_TRBDF2" };
+	int m;
+	if (!d || !o || !tr || d->equation != FEMGPU_EQ_TRANSIENT) return FEMGPU_E_ARG;
+	femgpu_transport_default_opts(o);
+	memset(tr, 0, sizeof *tr);
+	if (!strcasecmp(d->MatrixVectorProductScheme, "CSR")) o->scheme = FEMGPU_CSR;
+	else if (!strcasecmp(d->MatrixVectorProductScheme, "EDE")) o->scheme = FEMGPU_EDE;
+	else if (!strcasecmp(d->MatrixVectorProductScheme, "EBE")) o->scheme = FEMGPU_EBE;
+	else return FEMGPU_E_ARG;
+	o->reorder = !strcasecmp(d->reordering, "SYMRCM") ? FEMGPU_REORDER_SYMRCM : FEMGPU_REORDER_NOT;
+	if (strcasecmp(d->Scaling, "NOT") != 0 || strcasecmp(d->Solver, "GMRES") != 0) return FEMGPU_E_ARG;
+	/* setPreconditioner.c:6-30, 79-89 */
+	if (!strcasecmp(d->Preconditioner, "NOT")) o->precond = FEMGPU_PREC_NOT;
+	else if (!strcasecmp(d->Preconditioner, "Diag")) o->precond = FEMGPU_PREC_DIAG;
+	else if (ilu_level_of(d->Preconditioner) >= 0 && o->scheme == FEMGPU_CSR) {
+		o->precond = FEMGPU_PREC_ILU0;
+		o->ilu_level = ilu_level_of(d->Preconditioner);
+	} else return FEMGPU_E_ARG;
+	/* setStabilizationForm.c:6-98 */
+	if (!strcasecmp(d->StabilizationForm, "SUPG")) tr->stab = FEMGPU_STAB_SUPG;
+	else if (!strcasecmp(d->StabilizationForm, "DD")) tr->stab = FEMGPU_STAB_DD;
+	else return FEMGPU_E_ARG;
+	for (m = 0; m < 6 && strcasecmp(d->TimeIntegration, methods[m]) != 0; m++) {}
+	if (m == 6 || (m >= FEMGPU_TI_PREDICTOR2 && tr->stab != FEMGPU_STAB_DD)) return FEMGPU_E_ARG;
+	tr->method = m;
+	if (!strcasecmp(d->ShockCapture, "CAU")) o->shock = FEMGPU_SHOCK_CAU;
+	else if (!strcasecmp(d->ShockCapture, "YZBeta")) o->shock = FEMGPU_SHOCK_YZBETA;
+	else if (!strcasecmp(d->ShockCapture, "CAUDD") && tr->stab == FEMGPU_STAB_DD) o->shock = FEMGPU_SHOCK_CAUDD;
+	else return FEMGPU_E_ARG;
+	if (!strcasecmp(d->h_Shock, "2sqrtArea")) o->hshock = FEMGPU_H_2SQRTAREA;
+	else if (!strcasecmp(d->h_Shock, "Option1")) o->hshock = FEMGPU_H_OPTION1;
+	else if (!strcasecmp(d->h_Shock, "Option2")) o->hshock = FEMGPU_H_OPTION2;
+	else return FEMGPU_E_ARG;
+	/* Criteria.c:3-20 */
+	if (!strcasecmp(d->StopMulticorrection, "NORM")) tr->stop_norm = 1;
+	else if (strcasecmp(d->StopMulticorrection, "ITERATION") != 0) return FEMGPU_E_ARG;
+	if (!strcasecmp(d->StopAtSteadyState, "YES")) tr->steady_stop = 1;
+	else if (strcasecmp(d->StopAtSteadyState, "NOT") != 0) return FEMGPU_E_ARG;
+	o->kmax = d->KrylovBasisVectorsQuantity;
+	o->lmax = d->LinearMaxIter;
+	o->tol = d->SolverTolerance;
+	o->nonlin_tol = d->NonLinearTolerance;
+	tr->alpha = d->Alpha;
+	tr->dt = d->DeltaT;
+	tr->final_time = d->FinalTime;
+	tr->max_corr = d->NonLinearMaxIter;
+	tr->nonlin_tol = d->NonLinearTolerance;
+	tr->time_tol = d->TimeIntegrationTolerance;
 	return 0;
 }
 

@@ -649,7 +649,13 @@ int femgpu_csr_resnorm_noalloc(int n, const int *IA, const int *JA, const double
  * driver's node types -- 1 for transport (Type), 4 for Euler (rhoType,
  * v1Type, v2Type, eType), 3 for Navier-Stokes (v1Type, v2Type, pType); the
  * element count; per element three vertices and its type). */
-enum femgpu_equation { FEMGPU_EQ_TRANSPORT = 0, FEMGPU_EQ_EULER = 1, FEMGPU_EQ_NS = 2 };
+enum femgpu_equation { FEMGPU_EQ_TRANSPORT = 0, FEMGPU_EQ_EULER = 1, FEMGPU_EQ_NS = 2,
+                       FEMGPU_EQ_TRANSIENT = 3 };
+/* FEMGPU_EQ_TRANSIENT: the transient transport driver's deck
+ * (02_Transport_Equation/2D/01_CommonFiles/Preprocess.c:42-66); its mesh
+ * file has one node type and no element type column (Preprocess.c:94-97):
+ * read it with ntype = 1 | FEMGPU_MESH_NO_ELEM_TYPE. */
+#define FEMGPU_MESH_NO_ELEM_TYPE 0x100
 typedef struct femgpu_deck {
 	int equation;
 	char Experiments[200], ProblemTitle[300], Solver[200], Preconditioner[1000], Scaling[200],
@@ -666,7 +672,10 @@ int femgpu_deck_read(const char *path, int equation, femgpu_deck *deck);
 int femgpu_deck_mesh_file(const femgpu_deck *deck, const char *dir, char *path, int cap);
 /* Read a mesh file with ntype node types per node: sizes into nnodes, nel;
  * x, y [nnodes], node_type [ntype*nnodes], vert [3*nel], elem_type [nel]
- * filled when non-NULL (call once with NULL arrays for the sizes). */
+ * filled when non-NULL (call once with NULL arrays for the sizes).  With
+ * FEMGPU_MESH_NO_ELEM_TYPE or-ed into ntype the element lines hold three
+ * vertices only and elem_type is set to 0 (the calloc'd Type the transient
+ * driver leaves). */
 int femgpu_mesh_read(const char *path, int ntype, int *nnodes, int *nel, double *x, double *y, int *node_type,
 		int *vert, int *elem_type);
 /* The element types the transport drivers' Preprocess sets after reading
@@ -681,6 +690,13 @@ int femgpu_mesh_side_types(int nnodes, const double *x, const double *y, int nel
 int femgpu_deck_transport_opts(const femgpu_deck *deck, femgpu_transport_opts *o);
 int femgpu_deck_euler_opts(const femgpu_deck *deck, femgpu_euler_opts *o);
 int femgpu_deck_ns_opts(const femgpu_deck *deck, femgpu_ns_opts *o);
+/* A transient transport deck as a transport context's options and its
+ * transient options (02_Transport_Equation/2D/01_CommonFiles:
+ * setMatrixVectorProductType.c, setPreconditioner.c (NOT, Diag, ILU<p> with
+ * CSR), setStabilizationForm.c (SUPG or DD with the six TimeIntegration
+ * strings, the shock capture and h_Shock strings), Criteria.c (ITERATION |
+ * NORM, YES | NOT)); Scaling must be NOT. */
+int femgpu_deck_transient_opts(const femgpu_deck *deck, femgpu_transport_opts *o, femgpu_transient_opts *tr);
 int femgpu_deck_amg(const femgpu_deck *deck, int *ncl, double *beta, double *omega, int *nr);
 
 /* ---- host utilities (no GPU needed) ------------------------------------- */

@@ -320,3 +320,42 @@ int ref_transient_run(int nnodes, const double *x, const double *y, const int *n
 	info[4] = g_tcheck;
 	return g_stage < g_cap ? g_stage : g_cap;
 }
+
+/* The transient driver's own Preprocess (Preprocess.c:5-180) on a deck (the
+ * mesh file at ../../../../INPUT_DATA/<title>_<nnodes>_<nel>.dat from the
+ * working directory): iv [7] = nnodes, nel, neq, NonLinearMaxIter,
+ * LinearMaxIter, KrylovBasisVectorsQuantity, nnzero (CSR); dv [7] =
+ * SolverTolerance, NonLinearTolerance, TimeIntegrationTolerance,
+ * StabilizationTolerance, Alpha, DeltaT, FinalTime; sv [13 x 64] the
+ * strings in reading order; per node x, y, Type, id; per element the
+ * vertices and Type. */
+int Preprocess(int, char **, ParametersType **, MatrixDataType **, FemStructsType **, FemFunctionsType **,
+               FemOtherFunctionsType **);
+
+int ref_transient_preprocess(const char *deck, int *iv, double *dv, char *sv, double *x, double *y, int *type,
+                             int *id, int *vert, int *etype, int cap_nodes, int cap_el)
+{
+	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF; FemOtherFunctionsType *FOF;
+	char *argv[2] = { "harness", (char *)deck };
+	int I;
+	const char *str[13];
+	Preprocess(2, argv, &P, &M, &FS, &FF, &FOF);
+	iv[0] = P->nnodes; iv[1] = P->nel; iv[2] = P->neq; iv[3] = P->NonLinearMaxIter; iv[4] = P->LinearMaxIter;
+	iv[5] = P->KrylovBasisVectorsQuantity; iv[6] = P->nnzero;
+	dv[0] = P->SolverTolerance; dv[1] = P->NonLinearTolerance; dv[2] = P->TimeIntegrationTolerance;
+	dv[3] = P->StabilizationTolerance; dv[4] = P->Alpha; dv[5] = P->DeltaT; dv[6] = P->FinalTime;
+	str[0] = P->ProblemTitle; str[1] = P->StopAtSteadyState; str[2] = P->Solver; str[3] = P->Preconditioner;
+	str[4] = P->Scaling; str[5] = P->reordering; str[6] = P->MatrixVectorProductScheme;
+	str[7] = P->StabilizationForm; str[8] = P->ShockCapture; str[9] = P->h_Shock; str[10] = P->TimeIntegration;
+	str[11] = P->StopMulticorrection; str[12] = "";
+	for (I = 0; I < 13; I++) strncpy(sv + 64 * I, str[I], 63);
+	if (P->nnodes > cap_nodes || P->nel > cap_el) return -1;
+	for (I = 0; I < P->nnodes; I++) {
+		x[I] = FS->Node[I].x; y[I] = FS->Node[I].y; type[I] = FS->Node[I].Type; id[I] = FS->Node[I].id;
+	}
+	for (I = 0; I < P->nel; I++) {
+		vert[3 * I] = FS->Element[I].Vertex[0]; vert[3 * I + 1] = FS->Element[I].Vertex[1];
+		vert[3 * I + 2] = FS->Element[I].Vertex[2]; etype[I] = FS->Element[I].Type;
+	}
+	return 0;
+}

@@ -157,3 +157,108 @@ def test_bad_files_rejected(tmp_path):
         fg.read_mesh(str(p), "transport")
     with pytest.raises(fg.FemGpuError):
         fg.read_deck(str(tmp_path / "missing.dat"), "transport")
+
+
+TRANSIENT_REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libfemref_transient.so")
+TRANSIENT_DECK = [("CONE", "Problem title"), ("1e-8", "Solver tolerance"), ("1e-3", "Non linear tolerance"),
+                  ("1e-4", "Time integration tolerance"), ("1e-6", "Stabilization tolerance"),
+                  ("3", "Non linear max iterations"), ("200", "Linear max iterations"),
+                  ("YES", "Stop at steady state"), ("25", "Krylov basis vectors"), ("GMRES", "Solver"),
+                  ("ILU1", "Preconditioner"), ("NOT", "Scaling"), ("SYMRCM", "Reordering"),
+                  ("CSR", "Matrix vector product scheme"), ("DD", "Stabilization form"),
+                  ("CAUDD", "Shock capture"), ("Option1", "h shock"), ("Predictor2_TRBDF2", "Time integration"),
+                  ("0.5", "Alpha"), ("0.05", "Delta t"), ("NORM", "Stop multicorrection"), ("1.5", "Final time")]
+
+
+def write_transient_case(tmp, nx=10, ny=10, deck=TRANSIENT_DECK):
+    """A transient transport deck and its mesh file where the driver's
+    Preprocess looks for it: ../../../../INPUT_DATA from the run folder."""
+    m = structured_mesh(nx, ny, perturb=0.2, seed=5)
+    bnd = (m.x == 0.0) | (m.x == 1.0) | (m.y == 0.0) | (m.y == 1.0)
+    ntype = np.where(bnd, 0, 1).astype(np.int32)
+    run = tmp / "a" / "b" / "c" / "run"
+    mesh_dir = tmp / "INPUT_DATA"
+    run.mkdir(parents=True)
+    mesh_dir.mkdir()
+    lines = deck + [(str(m.nnodes), "nnodes"), (str(m.nel), "nel")]
+    path = run / "params.dat"
+    path.write_bytes("".join(f"{v}\t:{lab}\r\n" for v, lab in lines).encode())
+    with open(mesh_dir / f"CONE_{m.nnodes}_{m.nel}.dat", "w") as f:
+        f.write(f"{m.nnodes}\n")
+        for a, b, t in zip(m.x, m.y, ntype):
+            f.write(f"{a:.17g}\t{b:.17g}\t{t}\n")
+        f.write(f"{m.nel}\n")
+        for v in m.vert:
+            f.write(f"{v[0]}\t{v[1]}\t{v[2]}\n")
+    return m, ntype, path, mesh_dir
+
+
+def test_transient_deck_mesh_and_options(tmp_path):
+    """The transient driver's deck (02_Transport_Equation/2D Preprocess.c:
+    42-66) and its mesh file without element types (Preprocess.c:94-97), and
+    the deck strings as transport + transient options."""
+    m, ntype, deck, mesh_dir = write_transient_case(tmp_path)
+    d = fg.read_deck(str(deck), "transient")
+    dd = d.as_dict()
+    assert dd["ProblemTitle"] == "CONE" and dd["TimeIntegration"] == "Predictor2_TRBDF2"
+    assert (dd["SolverTolerance"], dd["NonLinearTolerance"], dd["TimeIntegrationTolerance"],
+            dd["StabilizationTolerance"], dd["Alpha"], dd["DeltaT"], dd["FinalTime"]) == \
+        (1e-8, 1e-3, 1e-4, 1e-6, 0.5, 0.05, 1.5)
+    assert (dd["NonLinearMaxIter"], dd["LinearMaxIter"], dd["KrylovBasisVectorsQuantity"]) == (3, 200, 25)
+    assert (dd["StopAtSteadyState"], dd["StopMulticorrection"], dd["h_Shock"]) == ("YES", "NORM", "Option1")
+    mesh = fg.read_mesh(fg.deck_mesh_file(d, str(mesh_dir)), "transient")
+    assert np.array_equal(mesh["x"], m.x) and np.array_equal(mesh["y"], m.y)
+    assert np.array_equal(mesh["node_type"], ntype) and np.array_equal(mesh["vert"], m.vert)
+    assert not mesh["elem_type"].any()
+    o, tr = fg.deck_opts(d)
+    assert (o.scheme, o.reorder, o.precond, o.ilu_level, o.shock, o.kmax, o.lmax, o.tol) == \
+        (2, 1, 1, 1, 2, 25, 200, 1e-8)
+    assert (tr.stab, tr.method, tr.stop_norm, tr.steady_stop, tr.max_corr) == (1, 5, 1, 1, 3)
+    assert (tr.alpha, tr.dt, tr.final_time, tr.nonlin_tol, tr.time_tol) == (0.5, 0.05, 1.5, 1e-3, 1e-4)
+    # setStabilizationForm.c / setPreconditioner.c reject these combinations
+    for key, val in (("Stabilization form", "SUPG"), ("Matrix vector product scheme", "EBE"),
+                     ("Time integration", "Predictor3"), ("Stop multicorrection", "SOMETIMES")):
+        bad = [(val if lab == key else v, lab) for v, lab in TRANSIENT_DECK]
+        sub = tmp_path / key.replace(" ", "_")
+        sub.mkdir()
+        _, _, p, _ = write_transient_case(sub, deck=bad)
+        with pytest.raises(fg.FemGpuError):
+            fg.deck_opts(fg.read_deck(str(p), "transient"))
+
+
+@pytest.mark.skipif(not os.path.exists(TRANSIENT_REF_LIB), reason="the reference library is not built here")
+def test_transient_reading_matches_reference_preprocess(tmp_path):
+    m, ntype, deck, mesh_dir = write_transient_case(tmp_path)
+    L = ctypes.CDLL(TRANSIENT_REF_LIB)
+    f = L.ref_transient_preprocess
+    f.restype = ctypes.c_int
+    nn, ne = m.nnodes, m.nel
+    iv, dv = np.zeros(7, np.int32), np.zeros(7)
+    sv = ctypes.create_string_buffer(64 * 13)
+    x, y = np.zeros(nn), np.zeros(nn)
+    t, ident = np.zeros(nn, np.int32), np.zeros(nn, np.int32)
+    vert, et = np.zeros(3 * ne, np.int32), np.full(ne, 7, np.int32)
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    cwd = os.getcwd()
+    os.chdir(deck.parent)
+    try:
+        rc = f(str(deck).encode(), vp(iv), vp(dv), sv, vp(x), vp(y), vp(t), vp(ident), vp(vert), vp(et), nn, ne)
+    finally:
+        os.chdir(cwd)
+    assert rc == 0
+    d = fg.read_deck(str(deck), "transient").as_dict()
+    strings = [sv.raw[64 * i:64 * (i + 1)].split(b"\0")[0].decode() for i in range(12)]
+    assert strings == [d[k] for k in ("ProblemTitle", "StopAtSteadyState", "Solver", "Preconditioner", "Scaling",
+                                      "reordering", "MatrixVectorProductScheme", "StabilizationForm",
+                                      "ShockCapture", "h_Shock", "TimeIntegration", "StopMulticorrection")]
+    assert list(iv[[0, 1, 3, 4, 5]]) == [d["nnodes"], d["nel"], d["NonLinearMaxIter"], d["LinearMaxIter"],
+                                         d["KrylovBasisVectorsQuantity"]]
+    assert list(dv) == [d[k] for k in ("SolverTolerance", "NonLinearTolerance", "TimeIntegrationTolerance",
+                                       "StabilizationTolerance", "Alpha", "DeltaT", "FinalTime")]
+    mesh = fg.read_mesh(fg.deck_mesh_file(fg.read_deck(str(deck), "transient"), str(mesh_dir)), "transient")
+    assert np.array_equal(mesh["x"], x) and np.array_equal(mesh["y"], y)
+    assert np.array_equal(mesh["node_type"], t)
+    assert np.array_equal(mesh["vert"].reshape(-1), vert) and np.array_equal(mesh["elem_type"], et)
+    free = mesh["node_type"] >= 1
+    assert iv[2] == free.sum() and np.all(ident[~free] == -1)
+    assert np.array_equal(np.sort(ident[free]), np.arange(iv[2]))
