@@ -127,6 +127,15 @@ typedef struct fg_krylov {
 	fg_status *st;                  /* device status                          */
 	fg_status *st_host;             /* pinned host mirror                     */
 	int dsv;                        /* FGMRES: Arnoldi basis in double-single */
+	/* FGMRES look-ahead (la_s != NULL): the preconditioner of the next step
+	 * runs on la_s, on the raw operator output la_w, while the Gram-Schmidt
+	 * of this step runs on stream; la_t [ldv] the combination of the stored
+	 * directions, la_eta the subdiagonal entry, la_flag [kmax+1] per-step
+	 * snapshots of the convergence flag for the la_s work */
+	cudaStream_t la_s;
+	cudaEvent_t la_ev_w, la_ev_y;
+	double *la_w, *la_t, *la_eta;
+	int *la_flag;
 } fg_krylov;
 
 /* Operator callbacks, stream-ordered, returning cudaError_t (> 0) or a
@@ -145,6 +154,8 @@ typedef struct fg_linop {
 	int (*precond_dsin)(void *ctx, const void *p, double *z, const int *active);
 	int (*matvec_dsout)(void *ctx, const double *p, void *q, const int *active);
 	int (*matvec_xf)(void *ctx, const float *p, double *q, const int *active, int op32);
+	/* z = M^-1 p on the given stream (the look-ahead FGMRES step) */
+	int (*precond_s)(void *ctx, const double *p, double *z, const int *active, cudaStream_t s);
 } fg_linop;
 
 struct femgpu_transport {
@@ -195,6 +206,12 @@ struct femgpu_transport {
 	                                   invN2, R2, M2[3] per element          */
 	double *uB1, *uB2;              /* Predictor_New_BDF / _TRBDF2: bubble
 	                                   history (nel each)                    */
+
+	/* FGMRES look-ahead resources (fg_krylov.la_*), made on first use */
+	cudaStream_t la_s;
+	cudaEvent_t la_ev[2];
+	double *la_buf;                 /* la_w [ldv], la_t [ldv], la_eta [1]    */
+	int *la_flag;                   /* [kmax + 1]                            */
 
 	/* Krylov workspace */
 	int kmax;

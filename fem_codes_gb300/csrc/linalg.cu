@@ -513,16 +513,16 @@ __global__ void k_mdot_fin(const double *partials, int G, int m, double *h, doub
 	}
 }
 
-// w -= sum_j h[j] v_j; norm != 0: Hn = ||w|| (last block).  The basis
-// entries of a thread's element are loaded CGS_UNR at a time ahead of the
-// dependent subtractions (the same order of subtractions), so a warp keeps
-// CGS_UNR coalesced loads in flight; the kernel runs on CGS_GRID x the
-// reduction grid.  Dynamic shared memory: the m coefficients.
+// w = win - sum_j h[j] v_j (win may be w); norm != 0: Hn = ||w|| (last
+// block).  The basis entries of a thread's element are loaded CGS_UNR at a
+// time ahead of the dependent subtractions (the same order of subtractions),
+// so a warp keeps CGS_UNR coalesced loads in flight; the kernel runs on
+// CGS_GRID x the reduction grid.  Dynamic shared memory: the m coefficients.
 #define CGS_UNR 8
 #define CGS_GRID 4
-__global__ void __launch_bounds__(RED_TPB) k_cgs_update(const double *V, size_t ldv, int n, int m, double *w,
-                                                        const double *h, int norm, double *Hn, double *partials,
-                                                        fg_status *st)
+__global__ void __launch_bounds__(RED_TPB) k_cgs_update(const double *V, size_t ldv, int n, int m, const double *win,
+                                                        double *w, const double *h, int norm, double *Hn,
+                                                        double *partials, fg_status *st)
 {
 	if (!gmres_live(st)) return;
 	extern __shared__ double hsh[];
@@ -531,7 +531,7 @@ __global__ void __launch_bounds__(RED_TPB) k_cgs_update(const double *V, size_t 
 	__syncthreads();
 	double part = 0.0;
 	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-		double x = w[k];
+		double x = win[k];
 		int j = 0;
 		for (; j + CGS_UNR <= m; j += CGS_UNR) {
 			double v[CGS_UNR];
@@ -777,6 +777,111 @@ extern "C" int fg_kry_pgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 	return (int)cudaGetLastError();
 }
 
+// ------------------------------------------------ look-ahead FGMRES ----
+// The step's directions combined with the Gram-Schmidt coefficients of
+// column i (read before the Givens rotations overwrite it): t = sum_j H(j,i)
+// z_j over m = i + 1 stored directions, and eta = H(i+1,i).  Loads as in
+// k_cgs_update.  Dynamic shared memory: the m coefficients.
+__global__ void __launch_bounds__(RED_TPB) k_zcombo(const double *Z, size_t ldv, int n, int m, const double *Hcol,
+                                                    int ldh, double *t, double *eta, fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	extern __shared__ double hsh[];
+	for (int j = threadIdx.x; j < m; j += blockDim.x) hsh[j] = Hcol[(size_t)j * ldh];
+	if (blockIdx.x == 0 && threadIdx.x == 0) *eta = Hcol[(size_t)m * ldh];
+	__syncthreads();
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		double x = 0.0;
+		int j = 0;
+		for (; j + CGS_UNR <= m; j += CGS_UNR) {
+			double v[CGS_UNR];
+#pragma unroll
+			for (int u = 0; u < CGS_UNR; u++) v[u] = Z[(size_t)(j + u) * ldv + k];
+#pragma unroll
+			for (int u = 0; u < CGS_UNR; u++) x += hsh[j + u] * v[u];
+		}
+		for (; j < m; j++) x += hsh[j] * Z[(size_t)j * ldv + k];
+		t[k] = x;
+	}
+}
+
+// z := (z - t) / eta: the next direction from y = M^-1 w (in z) and t.
+__global__ void k_la_fin(double *z, const double *t, int n, const double *eta, fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	const double r = 1.0 / *eta;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) z[k] = (z[k] - t[k]) * r;
+}
+
+// The convergence flag as the step starts, for the work on the look-ahead
+// stream: a copy that no later kernel changes, so every thread of a sweep
+// reads the same value while the Givens kernel of the step may clear the
+// flag itself concurrently.
+__global__ void k_la_snap(const fg_status *st, int *flag) { *flag = st->active; }
+
+// Dynamic shared memory the Gram-Schmidt kernels of a look-ahead step ask
+// for: more than an SM holding an ILU sweep CTA (about 215 KB of its 228 KB)
+// has left, so the FP64-heavy blocks run on the other SMs and do not take
+// issue slots from the latency-bound sweep.
+#define LA_SMEM (24 * 1024)
+
+// Look-ahead flexible GMRES cycle.  With w = A z_i and v_(i+1) =
+// (w - V h) / eta, linearity of M^-1 gives M^-1 v_(i+1) = (y - Z h) / eta
+// for y = M^-1 w and Z = [M^-1 v_0 .. M^-1 v_i].  So y is computed on la_s
+// from the raw operator output while the step's Gram-Schmidt runs on the main
+// stream (block ILU(0)'s sweeps hold one SM per matrix block, the multi-dot
+// and the update the others), t = Z h follows the coefficients, and the step
+// then waits only for y and forms z_(i+1) = (y - t) / eta.  The z_i equal
+// M^-1 v_i up to rounding; the Arnoldi relation A Z = V H holds for the
+// stored z_i whatever their rounding, and, as every FGMRES solve here, the
+// solve is accepted on the true residual.
+static int fgmres_cycle_la(const fg_krylov *k, const fg_linop *op, const double *B, double *X, int cycle)
+{
+	cudaStream_t s = k->stream, s2 = k->la_s;
+	int n = k->n, kmax = k->kmax, ldh = kmax + 1, G = k->nblk, rc;
+	size_t ldv = k->ldv;
+	double *V = k->V, *Z = k->Z;
+	int *active = &k->st->active;
+	const int cgs_grid = G * (CGS_GRID < kmax + 1 ? CGS_GRID : kmax + 1);
+	const int gs = gs_mode(cycle);
+	if ((rc = op->matvec(op->ctx, X, V, nullptr))) return rc;
+	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, k->ge, k->partials, k->st, 0);
+	k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, k->ge, k->st);
+	if ((rc = op->precond(op->ctx, V, Z, active))) return rc;
+	for (int i = 0; i < kmax; i++) {
+		const int m = i + 1, more = i + 1 < kmax;
+		const size_t hs = sizeof(double) * (size_t)m > LA_SMEM ? sizeof(double) * (size_t)m : LA_SMEM;
+		double *w = V + (size_t)(i + 1) * ldv, *znext = Z + (size_t)(i + 1) * ldv;
+		double *h = k->partials + (size_t)G * (kmax + 1);
+		if ((rc = op->matvec(op->ctx, Z + (size_t)i * ldv, k->la_w, active))) return rc;
+		if (more) {
+			k_la_snap<<<1, 1, 0, s>>>(k->st, k->la_flag + i);
+			FG_TRY(cudaEventRecord(k->la_ev_w, s));
+			FG_TRY(cudaStreamWaitEvent(s2, k->la_ev_w, 0));
+			if ((rc = op->precond_s(op->ctx, k->la_w, znext, k->la_flag + i, s2))) return rc;
+			FG_TRY(cudaEventRecord(k->la_ev_y, s2));
+		}
+		for (int pass = 0; pass < gs; pass++) {
+			const int last = pass == gs - 1;
+			const double *win = pass == 0 ? k->la_w : w;
+			k_mdot<<<dim3(G, (m + MD_J - 1) / MD_J), RED_TPB, LA_SMEM, s>>>(V, ldv, n, m, win, k->partials, k->st);
+			k_mdot_fin<<<m, 32, 0, s>>>(k->partials, G, m, h, k->H + i, ldh, pass, k->st);
+			k_cgs_update<<<cgs_grid, RED_TPB, hs, s>>>(V, ldv, n, m, win, w, h, last, k->H + (i + 1) * ldh + i,
+			                                           k->partials, k->st);
+		}
+		if (more) k_zcombo<<<cgs_grid, RED_TPB, hs, s>>>(Z, ldv, n, m, k->H + i, ldh, k->la_t, k->la_eta, k->st);
+		k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(w, n, k->H + (i + 1) * ldh + i, k->st);
+		k_givens<<<1, 1, 0, s>>>(k->H, ldh, k->cs, k->sn, k->ge, i, kmax, k->st);
+		if (more) {
+			FG_TRY(cudaStreamWaitEvent(s, k->la_ev_y, 0));
+			k_la_fin<<<fg_grid(n), FG_TPB, 0, s>>>(znext, k->la_t, n, k->la_eta, k->st);
+		}
+	}
+	k_backsolve<<<1, 1, 0, s>>>(k->H, ldh, k->ge, k->gy, k->st);
+	k_update_x<double><<<fg_grid(n), FG_TPB, 0, s>>>(X, Z, ldv, n, k->gy, k->st);
+	return (int)cudaGetLastError();
+}
+
 // One restart cycle of flexible GMRES with right preconditioning:
 // r0 = B - A X, z_i = M^-1 v_i, w = A z_i, MGS, Givens; X += Z y.  The
 // Arnoldi residual is the unpreconditioned one.  mixed: 0 FP64 throughout,
@@ -792,6 +897,8 @@ extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 	// the double-single basis (FP64 arithmetic otherwise: the residual, the
 	// Hessenberg matrix, the Givens rotations, Z and X stay FP64)
 	const bool dsv = k->dsv && !mixed && op->precond_dsin && op->matvec_dsout;
+	if (!mixed && !dsv && k->la_s && op->precond_s && k->Z && gs_mode(cycle) != 0)
+		return fgmres_cycle_la(k, op, B, X, cycle);
 	// the update's grid: its norm partials must stay below the coefficients,
 	// which the multi-dot finish stores at partials + G (kmax + 1)
 	const int cgs_grid = G * (CGS_GRID < kmax + 1 ? CGS_GRID : kmax + 1);
@@ -848,7 +955,7 @@ extern "C" int fg_kry_fgmres_cycle(const fg_krylov *k, const fg_linop *op, const
 				const int last = pass == gs - 1;
 				k_mdot<<<dim3(G, (m + MD_J - 1) / MD_J), RED_TPB, 0, s>>>(V, ldv, n, m, w, k->partials, k->st);
 				k_mdot_fin<<<m, 32, 0, s>>>(k->partials, G, m, h, k->H + i, ldh, pass, k->st);
-				k_cgs_update<<<cgs_grid, RED_TPB, sizeof(double) * (size_t)m, s>>>(V, ldv, n, m, w, h, last,
+				k_cgs_update<<<cgs_grid, RED_TPB, sizeof(double) * (size_t)m, s>>>(V, ldv, n, m, w, w, h, last,
 				                                                                     k->H + (i + 1) * ldh + i,
 				                                                                     k->partials, k->st);
 			}
@@ -946,6 +1053,51 @@ static int krylov_ds(const femgpu_transport *t)
 	return env && t->o.solver == FEMGPU_FGMRES && t->o.precision == FEMGPU_FP64 &&
 	       t->o.precond == FEMGPU_PREC_ILU0 && fg_ilu0_ds_ready(t);
 }
+// The preconditioner on another stream (the look-ahead step): the ILU(0)
+// apply launches everything on the context's stream, which is swapped for
+// the call.
+static int tr_precond_s(void *c, const double *p, double *z, const int *a, cudaStream_t s)
+{
+	femgpu_transport *t = (femgpu_transport *)c;
+	cudaStream_t keep = t->stream;
+	t->stream = s;
+	int rc = fg_precond(t, p, z, a);
+	t->stream = keep;
+	return rc;
+}
+
+// FGMRES with the look-ahead step (fgmres_cycle_la): FP64 block or global
+// ILU(p) contexts, unless FEMGPU_LOOKAHEAD=0 (read at every cycle).  Its stream (the highest
+// priority, so the sweep CTAs are placed before the Gram-Schmidt blocks
+// that become ready with them), events and vectors are made on first use;
+// without them the plain cycle runs.
+static int lookahead_on(femgpu_transport *t)
+{
+	const char *e = getenv("FEMGPU_LOOKAHEAD");
+	if ((e && e[0] == '0') || t->o.solver != FEMGPU_FGMRES || t->o.precision != FEMGPU_FP64 ||
+	    t->o.precond != FEMGPU_PREC_ILU0 || !t->Z)
+		return 0;
+	if (!t->la_s) {
+		int lo = 0, hi = 0;
+		cudaStream_t st = nullptr;
+		if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess ||
+		    cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, hi) != cudaSuccess) {
+			cudaGetLastError();
+			return 0;
+		}
+		if (cudaEventCreateWithFlags(&t->la_ev[0], cudaEventDisableTiming) != cudaSuccess ||
+		    cudaEventCreateWithFlags(&t->la_ev[1], cudaEventDisableTiming) != cudaSuccess ||
+		    cudaMalloc((void **)&t->la_buf, sizeof(double) * (2 * t->ldv + 1)) != cudaSuccess ||
+		    cudaMalloc((void **)&t->la_flag, sizeof(int) * ((size_t)t->kmax + 1)) != cudaSuccess) {
+			cudaGetLastError();
+			cudaStreamDestroy(st);
+			return 0;
+		}
+		t->la_s = st;
+	}
+	return 1;
+}
+
 static int tr_precond32(void *c, const double *p, float *z, const int *a)
 {
 	return fg_precond32((femgpu_transport *)c, p, z, a);
@@ -967,7 +1119,18 @@ extern "C" void fg_transport_krylov(femgpu_transport *t, fg_krylov *k, fg_linop 
 	op->matvec_xf = tr_matvec_xf;
 	op->precond_dsin = tr_precond_dsin;
 	op->matvec_dsout = tr_matvec_dsout;
+	op->precond_s = tr_precond_s;
 	k->dsv = krylov_ds(t);
+	k->la_s = nullptr;
+	if (!k->dsv && lookahead_on(t)) {
+		k->la_s = t->la_s;
+		k->la_ev_w = t->la_ev[0];
+		k->la_ev_y = t->la_ev[1];
+		k->la_w = t->la_buf;
+		k->la_t = t->la_buf + t->ldv;
+		k->la_eta = t->la_buf + 2 * t->ldv;
+		k->la_flag = t->la_flag;
+	}
 }
 
 extern "C" int fg_gmres_cycle(femgpu_transport *t, const double *B, double *X, int first)

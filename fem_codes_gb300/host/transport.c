@@ -351,8 +351,14 @@ void femgpu_transport_destroy(femgpu_transport *t)
 		t->ec, t->e2_ptr, t->e2, t->A, t->ke, t->fe, t->A32, t->u, t->F, t->F0, t->invDiag,
 		t->invDiag32, t->ilu.LU, t->ilu.Dinv, t->V, t->H, t->cs, t->sn, t->ge, t->gy, t->w2,
 		t->Z, t->Z32, t->xr, t->dr, t->partials, t->st, t->du, t->uold, t->Da, t->re, t->dold,
-		t->u1, t->u2, t->uB, t->aB, t->bub, t->uB1, t->uB2, t->sell_base, t->sell_w, t->sell_src, t->sell_JA, t->sell_A };
+		t->u1, t->u2, t->uB, t->aB, t->bub, t->uB1, t->uB2, t->la_buf, t->la_flag, t->sell_base, t->sell_w, t->sell_src, t->sell_JA, t->sell_A };
 	for (i = 0; i < (int)(sizeof ptrs / sizeof ptrs[0]); i++) if (ptrs[i]) cudaFree(ptrs[i]);
+	if (t->la_s) {
+		cudaStreamSynchronize(t->la_s);
+		cudaEventDestroy(t->la_ev[0]);
+		cudaEventDestroy(t->la_ev[1]);
+		cudaStreamDestroy(t->la_s);
+	}
 	if (t->o.precond == FEMGPU_PREC_ILU0 || t->o.precond == FEMGPU_PREC_LEARNED) fg_ilu_free(t);
 	if (t->st_host) cudaFreeHost(t->st_host);
 	for (i = 0; i < 4; i++) if (t->ev[i]) cudaEventDestroy(t->ev[i]);
