@@ -21,8 +21,11 @@ dependency levels, each factorised by its own thread-block cluster and swept
 by its own thread block (--ilu-blocks 0: ILU(0) of the whole matrix).  The
 sweeps solve rows chained along the SYMRCM fronts 32 at a time by a warp scan
 in double-single arithmetic (48-bit significands on the FP32 pipes, the
-residual and Arnoldi in FP64).  Steps continue the Picard sequence from the
-warm-up steps.
+residual and Arnoldi in FP64), forward and backward in one launch.  Each
+FGMRES step starts the next direction's sweeps on a second stream as soon as
+the operator product is done and runs the Gram-Schmidt on the other SMs
+meanwhile (the look-ahead step; FEMGPU_LOOKAHEAD=0 for the plain step).
+Steps continue the Picard sequence from the warm-up steps.
 
 The same line carries an "euler" object (REFLETIDO on 1024x256 cells, a step
 being one implicit time step: predictor + 2 correctors) and an "ns" object
@@ -372,7 +375,10 @@ def run_ours(a):
         t_k = kern[sweep_key]
         if chain:
             ds = a.precision == "FP64" and os.environ.get("FEMGPU_SWEEP_DS", "1") != "0"
-            name = ("k_sweep_cs (ILU(0) forward+backward, chain-scan: rows chained along the SYMRCM fronts solved "
+            fb = ds and os.environ.get("FEMGPU_SWEEP_FB", "1") != "0"
+            name = (("k_sweep_cs_fb (ILU(0) forward and backward sweeps in one launch" if fb else
+                     "k_sweep_cs (ILU(0) forward+backward")
+                    + ", chain-scan: rows chained along the SYMRCM fronts solved "
                     "32 at a time by a warp scan" + (" in double-single arithmetic" if ds else "")
                     + ", row records, dataflow between warps")
         elif os.environ.get("FEMGPU_SWEEP_LAYOUT") == "ell":

@@ -64,7 +64,16 @@ typedef struct fg_ilu_sweeps {
 	 * the fused FP64 sweeps run on the FP32 pipes, 48-bit significands) */
 	unsigned char *prog_lo_ds, *prog_up_ds;
 	int ds;
+	/* bit i: program i of lo64, up64, lo32, up32, lo64c, up64c, lo32c,
+	 * up32c still holds an earlier factor's values (refreshed by the first
+	 * application that uses it) */
+	int stale;
+	/* ds: dpos [n] the slot of natural row r in the sweeps' gathered input
+	 * (the inverse of the gather of the double-single apply) */
+	int *dpos;
 	double *bl64, *y64;
+	double *o64;                    /* ds: the double-single sweeps' output
+	                                   (natural order), apart from their input */
 	float *bl32, *y32;
 	int *fac_ptr, *fac_prog;   /* precompiled elimination of each row        */
 	/* the same elimination for the cluster kernel: per level-order position
@@ -156,6 +165,13 @@ typedef struct fg_linop {
 	int (*matvec_xf)(void *ctx, const float *p, double *q, const int *active, int op32);
 	/* z = M^-1 p on the given stream (the look-ahead FGMRES step) */
 	int (*precond_s)(void *ctx, const double *p, double *z, const int *active, cudaStream_t s);
+	/* the look-ahead step with the gather fused into the product (NULL when
+	 * the context has no such form): q = A p, also written as the
+	 * preconditioner's gathered input; the preconditioner on that input on
+	 * the given stream; and its output (double-single, natural order) */
+	int (*matvec_g)(void *ctx, const double *p, double *q, const int *active);
+	int (*precond_g)(void *ctx, const int *active, cudaStream_t s);
+	const void *(*precond_g_out)(void *ctx);
 } fg_linop;
 
 struct femgpu_transport {
@@ -306,6 +322,7 @@ int fg_add(double *x, const double *d, int n, cudaStream_t s);          /* x += 
 int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJA);
 int fg_ilu0_factor(femgpu_transport *t);
 int fg_ilu0_apply64(femgpu_transport *t, const double *p, double *z, const int *active);
+int fg_ilu0_sweeps_gathered(femgpu_transport *t, const int *active);
 int fg_ilu0_apply32(femgpu_transport *t, const double *p, float *z, const int *active);
 void fg_ilu_free(femgpu_transport *t);
 int fg_dot(femgpu_transport *t, const double *a, const double *b, int n, double *out_dev);

@@ -632,31 +632,29 @@ template <> __device__ __forceinline__ double fma_t(double a, double b, double c
 template <> __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 template <> __device__ __forceinline__ dsf fma_t(dsf a, dsf b, dsf c) { return ds_fma(a, b, c); }
 
+// One chain-scan sweep of this thread block's matrix block: the staging,
+// dataflow and scan of k_sweep_cs, on the barriers full/empty (D of them);
+// every thread returns after a block barrier, true when a wait gave up.
 template <typename T, bool UPPER, int W>
-__global__ void __launch_bounds__((SW2_CW + 1) * 32, 1)
-k_sweep_cs(SweepArgs a, const T *__restrict__ in, T *out)
+__device__ __forceinline__ bool cs_sweep(const SweepArgs &a, const T *__restrict__ in, T *out, unsigned char *sm,
+                                         unsigned long long *full, unsigned long long *empty, int *failed,
+                                         int *issued, int *pdone, int *prog)
 {
 	constexpr int CW = SW2_CW;
 	constexpr int IB = rec_ib(W), VB = rec_vb_cs(W, UPPER, (int)sizeof(T)), RB = rec_bytes_cs(W, UPPER, (int)sizeof(T));
 	constexpr int MO = W + (UPPER ? 1 : 0);              // first scan multiplier
 	static_assert(SW_SUB == CW * 32, "one slot per consumer thread and sub-block");
-	if (a.active && !*a.active) return;
-	extern __shared__ __align__(128) unsigned char sm[];
 	const unsigned ring_b = (unsigned)al16((SW_RING + 1) * sizeof(T));
 	T *ring = (T *)sm;
-	unsigned long long *full = (unsigned long long *)(sm + ring_b);
-	unsigned long long *empty = full + SW_MAXD;
 	unsigned char *stages = sm + ((ring_b + SW_BAR_BYTES + 127) & ~127u);
-	__shared__ int failed, issued, pdone;
-	__shared__ int prog[CW];
-	volatile int *vfailed = &failed;
+	volatile int *vfailed = failed;
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, D = a.D;
 	const unsigned sbytes = (unsigned)a.stage_bytes;
 	const int sb0 = a.chunk_sb ? a.chunk_sb[blockIdx.x] : 0, sb1 = a.chunk_sb ? a.chunk_sb[blockIdx.x + 1] : a.nsb;
 	const int l0 = a.chunk_lev ? a.chunk_lev[blockIdx.x] : 0, l1 = a.chunk_lev ? a.chunk_lev[blockIdx.x + 1] : a.nlev;
 
 	if (tid == 0) {
-		failed = 0; issued = 0; pdone = 0;
+		*failed = 0; *issued = 0; *pdone = 0;
 		ring[SW_RING] = zero_t<T>();
 		for (int s = 0; s < D; s++) { mbar_init(&full[s], 1); mbar_init(&empty[s], CW); }
 		fence_mbar_init();
@@ -665,81 +663,119 @@ k_sweep_cs(SweepArgs a, const T *__restrict__ in, T *out)
 	__syncthreads();
 
 	if (warp == CW) {                                     // ---- producer warp
-		sweep_producer(a, in, stages, sbytes, full, empty, D, sb0, sb1, lane, vfailed, &issued, &pdone, true);
-		return;
-	}
-
-	const int ctid = tid;                                 // ---- consumer warps
-	const unsigned roff = (unsigned)DF_HDR + (unsigned)(ctid < a.cmax ? ctid : a.cmax - 1) * RB;
-	const unsigned boff = (unsigned)a.bvo + (unsigned)(ctid < a.cmax ? ctid : a.cmax - 1) * sizeof(T);
-	int s = 0, waited = 0;
-	unsigned ph = 0;
-	bool fail = false;
-	T ydef = zero_t<T>();                                 // an output not yet stored to global memory
-	int odef = -1;
-	for (int l = l0; l < l1 && !fail; l++) {
-		const int ll = l - l0;
-		int nsub = 1;
-		for (int j = 0; j < nsub; j++) {
-			if (!mbar_wait_or_fail(&full[s], ph, vfailed)) { *vfailed = 1; fail = true; break; }
-			waited++;
-			const unsigned char *st = stages + (unsigned)s * sbytes;
-			union { int4 q[IB / 16]; int i[IB / 4]; } ci;
-			union { int4 q[VB / 16]; T v[VB / sizeof(T)]; } cv;
+		sweep_producer(a, in, stages, sbytes, full, empty, D, sb0, sb1, lane, vfailed, issued, pdone, true);
+	} else {                                              // ---- consumer warps
+		const int ctid = tid;
+		const unsigned roff = (unsigned)DF_HDR + (unsigned)(ctid < a.cmax ? ctid : a.cmax - 1) * RB;
+		const unsigned boff = (unsigned)a.bvo + (unsigned)(ctid < a.cmax ? ctid : a.cmax - 1) * sizeof(T);
+		int s = 0, waited = 0;
+		unsigned ph = 0;
+		bool fail = false;
+		T ydef = zero_t<T>();                             // an output not yet stored to global memory
+		int odef = -1;
+		for (int l = l0; l < l1 && !fail; l++) {
+			const int ll = l - l0;
+			int nsub = 1;
+			for (int j = 0; j < nsub; j++) {
+				if (!mbar_wait_or_fail(&full[s], ph, vfailed)) { *vfailed = 1; fail = true; break; }
+				waited++;
+				const unsigned char *st = stages + (unsigned)s * sbytes;
+				union { int4 q[IB / 16]; int i[IB / 4]; } ci;
+				union { int4 q[VB / 16]; T v[VB / sizeof(T)]; } cv;
 #pragma unroll
-			for (int k = 0; k < IB / 16; k++) ci.q[k] = ((const int4 *)(st + roff))[k];
+				for (int k = 0; k < IB / 16; k++) ci.q[k] = ((const int4 *)(st + roff))[k];
 #pragma unroll
-			for (int k = 0; k < VB / 16; k++) cv.q[k] = ((const int4 *)(st + roff + IB))[k];
-			const T x0 = *(const T *)(st + boff);
-			const int4 h = *(const int4 *)st;
-			const int need = lane < CW ? (int)st[16 + warp * NEED_STRIDE + lane] : 255;
-			if (j == 0) nsub = h.y;
+				for (int k = 0; k < VB / 16; k++) cv.q[k] = ((const int4 *)(st + roff + IB))[k];
+				const T x0 = *(const T *)(st + boff);
+				const int4 h = *(const int4 *)st;
+				const int need = lane < CW ? (int)st[16 + warp * NEED_STRIDE + lane] : 255;
+				if (j == 0) nsub = h.y;
+				__syncwarp();
+				if (lane == 0) mbar_arrive(&empty[s]);    // this warp's slots are in registers
+				if (++s == D) { s = 0; ph ^= 1u; }
+				if (32 * warp >= h.x) continue;           // no chunk of this warp here (uniform)
+				const int want = ll - (need == 255 ? a.skew + 1 : need);
+				bool ready = false;
+				for (int it = 0; it < a.wait; it++) {
+					const bool mine = lane >= CW || lane == warp || ld_acquire_cta(&prog[lane]) >= want;
+					if (__all_sync(0xffffffffu, mine)) { ready = true; break; }
+					if (__any_sync(0xffffffffu, *vfailed != 0)) break;
+				}
+				if (!ready) { *vfailed = 1; fail = true; break; }
+				__syncwarp();
+				T d[W];
+#pragma unroll
+				for (int k = 0; k < W; k++) {
+					unsigned c = (unsigned)ci.i[k] & ~SW_NEAR;
+					d[k] = ring[c < SW_RING ? c : SW_RING];
+				}
+				if (h.w) {
+#pragma unroll
+					for (int k = 0; k < W; k++)
+						if (!((unsigned)ci.i[k] & SW_NEAR)) d[k] = ld_cg(&out[ci.i[k]]);
+				}
+				T y = x0;
+#pragma unroll
+				for (int k = 0; k < W; k++) y = fmsub<T, true>(y, d[k], cv.v[k]);
+				if (UPPER) y = mul(y, cv.v[W]);
+				// the segments' recurrences across the warp's lanes
+#pragma unroll
+				for (int k = 0; k < 5; k++) {
+					const T up = shfl_up_t(y, 1 << k);
+					if (lane >= (1 << k)) y = fma_t(cv.v[MO + k], up, y);
+				}
+				ring[(h.z + ctid) & (SW_RING - 1)] = y;
+				if (odef >= 0) out[odef] = ydef;          // an earlier sub-block of this level
+				ydef = y;
+				odef = ci.i[W];
+			}
+			if (fail) break;
 			__syncwarp();
-			if (lane == 0) mbar_arrive(&empty[s]);        // this warp's slots are in registers
-			if (++s == D) { s = 0; ph ^= 1u; }
-			if (32 * warp >= h.x) continue;               // no chunk of this warp here (uniform)
-			const int want = ll - (need == 255 ? a.skew + 1 : need);
-			bool ready = false;
-			for (int it = 0; it < a.wait; it++) {
-				const bool mine = lane >= CW || lane == warp || ld_acquire_cta(&prog[lane]) >= want;
-				if (__all_sync(0xffffffffu, mine)) { ready = true; break; }
-				if (__any_sync(0xffffffffu, *vfailed != 0)) break;
-			}
-			if (!ready) { *vfailed = 1; fail = true; break; }
-			__syncwarp();
-			T d[W];
-#pragma unroll
-			for (int k = 0; k < W; k++) {
-				unsigned c = (unsigned)ci.i[k] & ~SW_NEAR;
-				d[k] = ring[c < SW_RING ? c : SW_RING];
-			}
-			if (h.w) {
-#pragma unroll
-				for (int k = 0; k < W; k++)
-					if (!((unsigned)ci.i[k] & SW_NEAR)) d[k] = ld_cg(&out[ci.i[k]]);
-			}
-			T y = x0;
-#pragma unroll
-			for (int k = 0; k < W; k++) y = fmsub<T, true>(y, d[k], cv.v[k]);
-			if (UPPER) y = mul(y, cv.v[W]);
-			// the segments' recurrences across the warp's lanes
-#pragma unroll
-			for (int k = 0; k < 5; k++) {
-				const T up = shfl_up_t(y, 1 << k);
-				if (lane >= (1 << k)) y = fma_t(cv.v[MO + k], up, y);
-			}
-			ring[(h.z + ctid) & (SW_RING - 1)] = y;
-			if (odef >= 0) out[odef] = ydef;              // an earlier sub-block of this level
-			ydef = y;
-			odef = ci.i[W];
+			if (lane == 0) st_release_cta(&prog[warp], ll);
+			if (odef >= 0) { out[odef] = ydef; odef = -1; }
 		}
-		if (fail) break;
-		__syncwarp();
-		if (lane == 0) st_release_cta(&prog[warp], ll);
-		if (odef >= 0) { out[odef] = ydef; odef = -1; }
+		consumer_sync<CW>();
+		if (*vfailed && ctid == 0) sweep_drain(a, full, D, waited, issued, pdone);
 	}
-	consumer_sync<CW>();
-	if (*vfailed && ctid == 0) sweep_drain(a, full, D, waited, &issued, &pdone);
+	__syncthreads();
+	return *vfailed != 0;
+}
+
+template <typename T, bool UPPER, int W>
+__global__ void __launch_bounds__((SW2_CW + 1) * 32, 1)
+k_sweep_cs(SweepArgs a, const T *__restrict__ in, T *out)
+{
+	if (a.active && !*a.active) return;
+	extern __shared__ __align__(128) unsigned char sm[];
+	const unsigned ring_b = (unsigned)al16((SW_RING + 1) * sizeof(T));
+	unsigned long long *full = (unsigned long long *)(sm + ring_b);
+	__shared__ int failed, issued, pdone;
+	__shared__ int prog[SW2_CW];
+	(void)cs_sweep<T, UPPER, W>(a, in, out, sm, full, full + SW_MAXD, &failed, &issued, &pdone, prog);
+}
+
+// Both sweeps of one preconditioner application in one launch: each thread
+// block sweeps its matrix block forward (in -> y) and then backward (y ->
+// out), keeping its SM between the two (block ILU(0): a block's backward
+// sweep reads only its own forward results).  The consumers' global stores
+// of y are ordered before the producer's bulk copies of y by an async-proxy
+// fence and the block barrier; the backward sweep runs on barriers of its
+// own.  Dynamic shared memory: the larger of the two sweeps' layouts.
+template <typename T, int WL, int WU>
+__global__ void __launch_bounds__((SW2_CW + 1) * 32, 1)
+k_sweep_cs_fb(SweepArgs al, SweepArgs au, const T *__restrict__ in, T *y, T *out)
+{
+	if (al.active && !*al.active) return;
+	extern __shared__ __align__(128) unsigned char sm[];
+	const unsigned ring_b = (unsigned)al16((SW_RING + 1) * sizeof(T));
+	unsigned long long *full = (unsigned long long *)(sm + ring_b);
+	__shared__ unsigned long long bar2[2 * SW_MAXD];
+	__shared__ int failed, issued, pdone;
+	__shared__ int prog[SW2_CW];
+	if (cs_sweep<T, false, WL>(al, in, y, sm, full, full + SW_MAXD, &failed, &issued, &pdone, prog)) return;
+	asm volatile("fence.proxy.async.global;" ::: "memory");
+	__syncthreads();
+	(void)cs_sweep<T, true, WU>(au, y, out, sm, bar2, bar2 + SW_MAXD, &failed, &issued, &pdone, prog);
 }
 
 // Scan multipliers of a chain-scan program from the factor, one warp per
@@ -798,6 +834,13 @@ __global__ void k_perm_in_dsds(const dsf *__restrict__ p, const int *__restrict_
 	if (active && !*active) return;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
 		in[ppos[i]] = p[rows[i]];
+}
+
+// dpos[rows[i]] = ppos[i]: where the gather of the double-single apply puts
+// natural row r, for a product that writes the gathered input itself.
+__global__ void k_inv_gather(const int *__restrict__ rows, const int *__restrict__ ppos, int n, int *dpos)
+{
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dpos[rows[i]] = ppos[i];
 }
 
 __global__ void k_ds_to_double(const dsf *__restrict__ x, int n, double *z, const int *active)
@@ -1867,8 +1910,15 @@ static int factor_cluster_size(int P)
 	SD_SET(double, false, false, W); SD_SET(double, true, false, W); \
 	SD_SET(double, false, true, W); SD_SET(double, true, true, W); \
 	SD_SET(float, false, false, W); SD_SET(float, true, false, W)
+#define SF_SET(W) FG_TRY(cudaFuncSetAttribute(k_sweep_cs_fb<dsf, W, W>, \
+	cudaFuncAttributeMaxDynamicSharedMemorySize, SW_SMEM_CAP))
 static int sweep_attrs(void)
 {
+	SF_SET(2);
+	SF_SET(3);
+	SF_SET(4);
+	SF_SET(6);
+	SF_SET(8);
 	SW_SET_CW(4);
 	SW_SET_CW(8);
 	SW_SET_CW(16);
@@ -1923,6 +1973,23 @@ static void launch_cs(const SweepArgs &a, int rw, int grid, int bytes, cudaStrea
 	case 8: k_sweep_cs<T, UPPER, 8><<<grid, nt, bytes, s>>>(a, in, out); break;
 	case 12: k_sweep_cs<T, UPPER, 12><<<grid, nt, bytes, s>>>(a, in, out); break;
 	default: k_sweep_cs<T, UPPER, 16><<<grid, nt, bytes, s>>>(a, in, out); break;
+	}
+}
+
+// Both double-single sweeps in one launch (k_sweep_cs_fb) when the two
+// programs have the same record width (one of 2, 3, 4, 6, 8) and blocks;
+// false: the caller launches them one by one.
+static bool launch_cs_fb(const SweepArgs &al, const SweepArgs &au, int rw, int grid, int bytes, cudaStream_t s,
+                         const dsf *in, dsf *y, dsf *out)
+{
+	const int nt = (SW2_CW + 1) * 32;
+	switch (rw) {
+	case 2: k_sweep_cs_fb<dsf, 2, 2><<<grid, nt, bytes, s>>>(al, au, in, y, out); return true;
+	case 3: k_sweep_cs_fb<dsf, 3, 3><<<grid, nt, bytes, s>>>(al, au, in, y, out); return true;
+	case 4: k_sweep_cs_fb<dsf, 4, 4><<<grid, nt, bytes, s>>>(al, au, in, y, out); return true;
+	case 6: k_sweep_cs_fb<dsf, 6, 6><<<grid, nt, bytes, s>>>(al, au, in, y, out); return true;
+	case 8: k_sweep_cs_fb<dsf, 8, 8><<<grid, nt, bytes, s>>>(al, au, in, y, out); return true;
+	default: return false;
 	}
 }
 
@@ -2090,6 +2157,9 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 				FG_TRY(cudaMalloc((void **)&S.prog_up_ds, bu));
 				FG_TRY(cudaMemcpy(S.prog_lo_ds, S.lo64c.prog, bl, cudaMemcpyDeviceToDevice));
 				FG_TRY(cudaMemcpy(S.prog_up_ds, S.up64c.prog, bu, cudaMemcpyDeviceToDevice));
+				FG_TRY(cudaMalloc((void **)&S.dpos, sizeof(int) * (size_t)n));
+				k_inv_gather<<<fg_grid(n), FG_TPB, 0, t->stream>>>(S.lo64c.rows, S.lo64c.ppos, n, S.dpos);
+				FG_TRY(cudaGetLastError());
 				S.ds = 1;
 			}
 		}
@@ -2100,6 +2170,10 @@ extern "C" int fg_ilu_prepare(femgpu_transport *t, const int *hIA, const int *hJ
 	FG_TRY(cudaMalloc((void **)&S.y32, sizeof(float) * nb));
 	FG_TRY(cudaMemset(S.bl64, 0, sizeof(double) * nb));
 	FG_TRY(cudaMemset(S.y64, 0, sizeof(double) * nb));
+	if (S.ds) {
+		FG_TRY(cudaMalloc((void **)&S.o64, sizeof(double) * nb));
+		FG_TRY(cudaMemset(S.o64, 0, sizeof(double) * nb));
+	}
 	FG_TRY(cudaMemset(S.bl32, 0, sizeof(float) * nb));
 	FG_TRY(cudaMemset(S.y32, 0, sizeof(float) * nb));
 	const fg_sweep *all[4] = { &S.lo64, &S.up64, &S.lo32, &S.up32 };
@@ -2145,15 +2219,9 @@ extern "C" int fg_ilu0_factor(femgpu_transport *t)
 		                                                       S.lo64.nlev, S.lo64.chunk_lev, S.fac_ptr,
 		                                                       S.fac_prog, t->ilu.LU, t->ilu.Dinv, &t->st->err);
 	}
-	fg_sweep *pr[8] = { &S.lo64, &S.up64, &S.lo32, &S.up32, &S.lo64c, &S.up64c, &S.lo32c, &S.up32c };
-	for (int i = 0; i < (S.chain ? 8 : 4); i++) {
-		int g = fg_grid(pr[i]->nval);
-		const bool f64 = (i & 2) == 0;
-		if (f64) k_refresh<double><<<g, FG_TPB, 0, s>>>(pr[i]->prog, pr[i]->val_off, pr[i]->val_src,
-		                                               pr[i]->nval, t->ilu.LU, t->ilu.Dinv);
-		else k_refresh<float><<<g, FG_TPB, 0, s>>>(pr[i]->prog, pr[i]->val_off, pr[i]->val_src,
-		                                          pr[i]->nval, t->ilu.LU, t->ilu.Dinv);
-	}
+	// the double-single chain programs (the FGMRES sweeps) take the new
+	// values now, the others when an application first uses them
+	S.stale = S.chain ? 0xFF : 0x0F;
 	if (S.ds) {
 		const fg_sweep &L = S.lo64c, &U = S.up64c;
 		k_refresh<dsf><<<fg_grid(L.nval), FG_TPB, 0, s>>>(S.prog_lo_ds, L.val_off, L.val_src, L.nval, t->ilu.LU,
@@ -2167,20 +2235,37 @@ extern "C" int fg_ilu0_factor(femgpu_transport *t)
 		                                                                     U.cs_row, U.nslot, t->ilu.LU,
 		                                                                     t->ilu.Dinv);
 	}
-	if (S.chain) {
-		for (int i = 4; i < 8; i++) {
-			const fg_sweep &c = *pr[i];
-			const int g = fg_grid((long long)c.nslot);
-			const bool f64 = (i & 2) == 0, up = (i & 1) != 0;
-			if (f64 && up) k_chain_mult<double, true><<<g, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
-			                                                              c.nslot, t->ilu.LU, t->ilu.Dinv);
-			else if (f64) k_chain_mult<double, false><<<g, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
-			                                                              c.nslot, t->ilu.LU, t->ilu.Dinv);
-			else if (up) k_chain_mult<float, true><<<g, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
-			                                                           c.nslot, t->ilu.LU, t->ilu.Dinv);
-			else k_chain_mult<float, false><<<g, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
-			                                                    c.nslot, t->ilu.LU, t->ilu.Dinv);
+	return (int)cudaGetLastError();
+}
+
+// Program pair i0, i0 + 1 (0: lo64/up64, 2: lo32/up32, 4: lo64c/up64c,
+// 6: lo32c/up32c) given the current factor's values (and, for the chain
+// programs, their scan multipliers) if the factorisation left it stale; on
+// the context's stream, ahead of the application that uses it.
+static int refresh_pair(femgpu_transport *t, int i0)
+{
+	fg_ilu_sweeps &S = t->sweeps;
+	cudaStream_t s = t->stream;
+	fg_sweep *pr[8] = { &S.lo64, &S.up64, &S.lo32, &S.up32, &S.lo64c, &S.up64c, &S.lo32c, &S.up32c };
+	for (int i = i0; i < i0 + 2; i++) {
+		if (!(S.stale & (1 << i))) continue;
+		const fg_sweep &c = *pr[i];
+		const bool f64 = (i & 2) == 0, up = (i & 1) != 0;
+		const int g = fg_grid(c.nval);
+		if (f64) k_refresh<double><<<g, FG_TPB, 0, s>>>(c.prog, c.val_off, c.val_src, c.nval, t->ilu.LU, t->ilu.Dinv);
+		else k_refresh<float><<<g, FG_TPB, 0, s>>>(c.prog, c.val_off, c.val_src, c.nval, t->ilu.LU, t->ilu.Dinv);
+		if (i >= 4) {
+			const int gc = fg_grid((long long)c.nslot);
+			if (f64 && up) k_chain_mult<double, true><<<gc, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
+			                                                               c.nslot, t->ilu.LU, t->ilu.Dinv);
+			else if (f64) k_chain_mult<double, false><<<gc, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
+			                                                               c.nslot, t->ilu.LU, t->ilu.Dinv);
+			else if (up) k_chain_mult<float, true><<<gc, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
+			                                                            c.nslot, t->ilu.LU, t->ilu.Dinv);
+			else k_chain_mult<float, false><<<gc, FG_TPB, 0, s>>>(c.prog, c.cs_voff, c.cs_src, c.cs_row,
+			                                                     c.nslot, t->ilu.LU, t->ilu.Dinv);
 		}
+		S.stale &= ~(1 << i);
 	}
 	return (int)cudaGetLastError();
 }
@@ -2225,16 +2310,33 @@ static int apply_t(femgpu_transport *t, const fg_sweep &lo, const fg_sweep &up, 
 // The double-single chain sweeps: gather into double-single slots, the
 // forward and backward chain-scan programs with double-single values, the
 // backward output (natural order, in the gather buffer) back to FP64.
+static int sweeps_ds(femgpu_transport *t, const int *active);
 static int apply_ds(femgpu_transport *t, const double *p, const dsf *p_ds, double *z, const int *active)
+{
+	fg_ilu_sweeps &S = t->sweeps;
+	const fg_sweep &lo = S.lo64c;
+	cudaStream_t s = t->stream;
+	const int n = t->neq;
+	dsf *bl = (dsf *)S.bl64;
+	if (p_ds) k_perm_in_dsds<<<fg_grid(n), FG_TPB, 0, s>>>(p_ds, lo.rows, lo.ppos, n, bl, active);
+	else k_perm_in_ds<<<fg_grid(n), FG_TPB, 0, s>>>(p, lo.rows, lo.ppos, n, bl);
+	const int rc = sweeps_ds(t, active);
+	if (rc) return rc;
+	k_ds_to_double<<<fg_grid(n), FG_TPB, 0, s>>>((const dsf *)S.o64, n, z, active);
+	return (int)cudaGetLastError();
+}
+
+// The two double-single chain sweeps on the gathered input in the gather
+// buffer; the backward sweep writes its output, in natural order, to o64 (not
+// back into the gather buffer: in the one-launch form a block's backward sweep
+// may run while another block's forward sweep still reads its input there).
+static int sweeps_ds(femgpu_transport *t, const int *active)
 {
 	fg_ilu_sweeps &S = t->sweeps;
 	const fg_sweep &lo = S.lo64c, &up = S.up64c;
 	cudaStream_t s = t->stream;
-	const int n = t->neq;
 	int D, sb, bytes;
-	dsf *bl = (dsf *)S.bl64, *y = (dsf *)S.y64;
-	if (p_ds) k_perm_in_dsds<<<fg_grid(n), FG_TPB, 0, s>>>(p_ds, lo.rows, lo.ppos, n, bl, active);
-	else k_perm_in_ds<<<fg_grid(n), FG_TPB, 0, s>>>(p, lo.rows, lo.ppos, n, bl);
+	dsf *bl = (dsf *)S.bl64, *y = (dsf *)S.y64, *o = (dsf *)S.o64;
 	SweepArgs a;
 	a.err = &t->st->err;
 	a.active = active;
@@ -2244,15 +2346,27 @@ static int apply_ds(femgpu_transport *t, const double *p, const dsf *p_ds, doubl
 	a.prog = S.prog_lo_ds; a.blk_off = lo.blk_off; a.sb_in = lo.sb_in; a.sb_inb = lo.sb_inb;
 	a.nlev = lo.nlev; a.nsb = lo.nsb; a.D = D; a.stage_bytes = sb;
 	a.chunk_sb = lo.chunk_sb; a.chunk_lev = lo.chunk_lev; a.bvo = lo.bvo; a.cmax = lo.cmax; a.skew = lo.skew;
-	launch_cs<dsf, false>(a, lo.rw, lo.nchunk, bytes, s, bl, y);
+	SweepArgs b = a;
+	const int bytes_lo = bytes;
 	bytes = sweep_smem(up, sizeof(dsf), &D, &sb);
 	if (bytes < 0) return bytes;
-	a.prog = S.prog_up_ds; a.blk_off = up.blk_off; a.sb_in = up.sb_in; a.sb_inb = up.sb_inb;
-	a.nlev = up.nlev; a.nsb = up.nsb; a.D = D; a.stage_bytes = sb;
-	a.chunk_sb = up.chunk_sb; a.chunk_lev = up.chunk_lev; a.bvo = up.bvo; a.cmax = up.cmax; a.skew = up.skew;
-	launch_cs<dsf, true>(a, up.rw, up.nchunk, bytes, s, y, bl);
-	k_ds_to_double<<<fg_grid(n), FG_TPB, 0, s>>>(bl, n, z, active);
+	b.prog = S.prog_up_ds; b.blk_off = up.blk_off; b.sb_in = up.sb_in; b.sb_inb = up.sb_inb;
+	b.nlev = up.nlev; b.nsb = up.nsb; b.D = D; b.stage_bytes = sb;
+	b.chunk_sb = up.chunk_sb; b.chunk_lev = up.chunk_lev; b.bvo = up.bvo; b.cmax = up.cmax; b.skew = up.skew;
+	// one launch for both sweeps unless FEMGPU_SWEEP_FB=0
+	const char *e = getenv("FEMGPU_SWEEP_FB");
+	if (!(e && e[0] == '0') && lo.rw == up.rw && lo.nchunk == up.nchunk &&
+	    launch_cs_fb(a, b, lo.rw, lo.nchunk, bytes_lo > bytes ? bytes_lo : bytes, s, bl, y, o))
+		return (int)cudaGetLastError();
+	launch_cs<dsf, false>(a, lo.rw, lo.nchunk, bytes_lo, s, bl, y);
+	launch_cs<dsf, true>(b, up.rw, up.nchunk, bytes, s, y, o);
 	return (int)cudaGetLastError();
+}
+
+extern "C" int fg_ilu0_sweeps_gathered(femgpu_transport *t, const int *active)
+{
+	if (!t->sweeps.ds) return FEMGPU_E_ARG;
+	return sweeps_ds(t, active);
 }
 
 extern "C" int fg_ilu0_apply64(femgpu_transport *t, const double *p, double *z, const int *active)
@@ -2260,8 +2374,10 @@ extern "C" int fg_ilu0_apply64(femgpu_transport *t, const double *p, double *z, 
 	fg_ilu_sweeps &S = t->sweeps;
 	const bool fma = t->o.solver == FEMGPU_FGMRES;
 	if (fma && S.ds) return apply_ds(t, p, NULL, z, active);
-	if (fma && S.chain)
-		return apply_t<double, double, double>(t, S.lo64c, S.up64c, S.bl64, S.y64, p, z, active, true);
+	const int pair = (fma && S.chain) ? 4 : 0;
+	const int rc = refresh_pair(t, pair);
+	if (rc) return rc;
+	if (pair) return apply_t<double, double, double>(t, S.lo64c, S.up64c, S.bl64, S.y64, p, z, active, true);
 	return apply_t<double, double, double>(t, S.lo64, S.up64, S.bl64, S.y64, p, z, active, fma);
 }
 
@@ -2281,6 +2397,8 @@ extern "C" int fg_ilu0_apply64_dsin(femgpu_transport *t, const void *p, double *
 extern "C" int fg_ilu0_apply32(femgpu_transport *t, const double *p, float *z, const int *active)
 {
 	fg_ilu_sweeps &S = t->sweeps;
+	const int rc = refresh_pair(t, S.chain ? 6 : 2);
+	if (rc) return rc;
 	if (S.chain) return apply_t<float, double, float>(t, S.lo32c, S.up32c, S.bl32, S.y32, p, z, active, false);
 	return apply_t<float, double, float>(t, S.lo32, S.up32, S.bl32, S.y32, p, z, active, false);
 }
@@ -2297,12 +2415,16 @@ extern "C" void fg_ilu_free(femgpu_transport *t)
 		memset(all[i], 0, sizeof(fg_sweep));
 	}
 	S.chain = 0;
-	void *v[] = { S.bl64, S.y64, S.bl32, S.y32, S.fac_ptr, S.fac_prog, S.fac2_hdr, S.fac2, S.fIA, S.fJA, S.fmap,
+	void *v[] = { S.bl64, S.y64, S.o64, S.bl32, S.y32, S.fac_ptr, S.fac_prog, S.fac2_hdr, S.fac2, S.fIA, S.fJA, S.fmap,
 	              S.fA };
 	for (void *q : v) if (q) cudaFree(q);
+	S.bl64 = S.y64 = S.o64 = nullptr;
+	S.bl32 = S.y32 = nullptr;
 	S.fIA = S.fJA = S.fmap = nullptr;
 	S.fA = nullptr;
 	S.fill = 0;
+	if (S.dpos) cudaFree(S.dpos);
+	S.dpos = nullptr;
 	if (S.prog_lo_ds) cudaFree(S.prog_lo_ds);
 	if (S.prog_up_ds) cudaFree(S.prog_up_ds);
 	S.prog_lo_ds = S.prog_up_ds = nullptr;

@@ -166,11 +166,15 @@ extern "C" int fg_csrmv32(int n, const int *IA, const int *JA, const float *AA, 
 // rows (the slice is stored column by column).  Eight entries per round keep
 // eight independent loads in flight.
 #define SELL_UNR 8
-template <typename TO, bool FUSED>
+// GATHER: each result also goes, as a double-single value, to slot dpos[i]
+// of G (the ILU sweeps' gathered input, so the look-ahead step's
+// preconditioner needs no gather of its own).
+template <typename TO, bool FUSED, bool GATHER = false>
 __global__ void __launch_bounds__(256) k_sellmv(int n, const long long *__restrict__ base, const int *__restrict__ width,
                                                 const int *__restrict__ IA, const int *__restrict__ JS,
                                                 const double *__restrict__ AS, const double *__restrict__ P,
-                                                TO *__restrict__ Q, const int *active)
+                                                TO *__restrict__ Q, const int *active,
+                                                const int *__restrict__ dpos = nullptr, dsf *__restrict__ G = nullptr)
 {
 	if (active && !*active) return;
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -193,6 +197,7 @@ __global__ void __launch_bounds__(256) k_sellmv(int n, const long long *__restri
 			if (j + u < len) q = FUSED ? fma(a[u], p[u], q) : __dadd_rn(q, __dmul_rn(a[u], p[u]));
 	}
 	Q[i] = mv_out<TO>(q);
+	if (GATHER) G[__ldg(&dpos[i])] = ds_from(q);
 }
 
 __global__ void k_sell_refresh(long long nslot, const int *__restrict__ src, const double *__restrict__ AA,
@@ -209,6 +214,16 @@ extern "C" int fg_sell_refresh(femgpu_transport *t)
 {
 	if (!t->sell_A) return 0;
 	k_sell_refresh<<<fg_grid(t->nslot), FG_TPB, 0, t->stream>>>(t->nslot, t->sell_src, t->A, t->sell_A);
+	return (int)cudaGetLastError();
+}
+
+// The FGMRES operator (fused form) that also writes the ILU sweeps' gathered
+// double-single input.
+static int sellmv_gather(femgpu_transport *t, const double *P, double *Q, const int *active)
+{
+	const int n = t->neq, g = (n + 255) / 256;
+	k_sellmv<double, true, true><<<g, 256, 0, t->stream>>>(n, t->sell_base, t->sell_w, t->IA, t->sell_JA, t->sell_A, P,
+	                                                      Q, active, t->sweeps.dpos, (dsf *)t->sweeps.bl64);
 	return (int)cudaGetLastError();
 }
 
@@ -813,6 +828,17 @@ __global__ void k_la_fin(double *z, const double *t, int n, const double *eta, f
 	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) z[k] = (z[k] - t[k]) * r;
 }
 
+// The same from the preconditioner's double-single output y (natural order).
+__global__ void k_la_fin_ds(double *z, const dsf *y, const double *t, int n, const double *eta, fg_status *st)
+{
+	if (!gmres_live(st)) return;
+	const double r = 1.0 / *eta;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+		const dsf v = y[k];
+		z[k] = (((double)v.hi + (double)v.lo) - t[k]) * r;
+	}
+}
+
 // The convergence flag as the step starts, for the work on the look-ahead
 // stream: a copy that no later kernel changes, so every thread of a sweep
 // reads the same value while the Givens kernel of the step may clear the
@@ -844,6 +870,8 @@ static int fgmres_cycle_la(const fg_krylov *k, const fg_linop *op, const double 
 	int *active = &k->st->active;
 	const int cgs_grid = G * (CGS_GRID < kmax + 1 ? CGS_GRID : kmax + 1);
 	const int gs = gs_mode(cycle);
+	// the product writes the preconditioner's gathered input itself
+	const bool fused = op->matvec_g && op->precond_g && op->precond_g_out;
 	if ((rc = op->matvec(op->ctx, X, V, nullptr))) return rc;
 	k_residual_start<<<G, RED_TPB, 0, s>>>(V, B, n, k->ge, k->partials, k->st, 0);
 	k_scale<<<fg_grid(n), FG_TPB, 0, s>>>(V, n, k->ge, k->st);
@@ -853,12 +881,16 @@ static int fgmres_cycle_la(const fg_krylov *k, const fg_linop *op, const double 
 		const size_t hs = sizeof(double) * (size_t)m > LA_SMEM ? sizeof(double) * (size_t)m : LA_SMEM;
 		double *w = V + (size_t)(i + 1) * ldv, *znext = Z + (size_t)(i + 1) * ldv;
 		double *h = k->partials + (size_t)G * (kmax + 1);
-		if ((rc = op->matvec(op->ctx, Z + (size_t)i * ldv, k->la_w, active))) return rc;
+		if (fused) rc = op->matvec_g(op->ctx, Z + (size_t)i * ldv, k->la_w, active);
+		else rc = op->matvec(op->ctx, Z + (size_t)i * ldv, k->la_w, active);
+		if (rc) return rc;
 		if (more) {
 			k_la_snap<<<1, 1, 0, s>>>(k->st, k->la_flag + i);
 			FG_TRY(cudaEventRecord(k->la_ev_w, s));
 			FG_TRY(cudaStreamWaitEvent(s2, k->la_ev_w, 0));
-			if ((rc = op->precond_s(op->ctx, k->la_w, znext, k->la_flag + i, s2))) return rc;
+			if (fused) rc = op->precond_g(op->ctx, k->la_flag + i, s2);
+			else rc = op->precond_s(op->ctx, k->la_w, znext, k->la_flag + i, s2);
+			if (rc) return rc;
 			FG_TRY(cudaEventRecord(k->la_ev_y, s2));
 		}
 		for (int pass = 0; pass < gs; pass++) {
@@ -874,7 +906,10 @@ static int fgmres_cycle_la(const fg_krylov *k, const fg_linop *op, const double 
 		k_givens<<<1, 1, 0, s>>>(k->H, ldh, k->cs, k->sn, k->ge, i, kmax, k->st);
 		if (more) {
 			FG_TRY(cudaStreamWaitEvent(s, k->la_ev_y, 0));
-			k_la_fin<<<fg_grid(n), FG_TPB, 0, s>>>(znext, k->la_t, n, k->la_eta, k->st);
+			if (fused)
+				k_la_fin_ds<<<fg_grid(n), FG_TPB, 0, s>>>(znext, (const dsf *)op->precond_g_out(op->ctx), k->la_t, n,
+				                                         k->la_eta, k->st);
+			else k_la_fin<<<fg_grid(n), FG_TPB, 0, s>>>(znext, k->la_t, n, k->la_eta, k->st);
 		}
 	}
 	k_backsolve<<<1, 1, 0, s>>>(k->H, ldh, k->ge, k->gy, k->st);
@@ -1066,6 +1101,21 @@ static int tr_precond_s(void *c, const double *p, double *z, const int *a, cudaS
 	return rc;
 }
 
+static int tr_matvec_g(void *c, const double *p, double *q, const int *a)
+{
+	return sellmv_gather((femgpu_transport *)c, p, q, a);
+}
+static int tr_precond_g(void *c, const int *a, cudaStream_t s)
+{
+	femgpu_transport *t = (femgpu_transport *)c;
+	cudaStream_t keep = t->stream;
+	t->stream = s;
+	int rc = fg_ilu0_sweeps_gathered(t, a);
+	t->stream = keep;
+	return rc;
+}
+static const void *tr_precond_g_out(void *c) { return ((femgpu_transport *)c)->sweeps.o64; }
+
 // FGMRES with the look-ahead step (fgmres_cycle_la): FP64 block or global
 // ILU(p) contexts, unless FEMGPU_LOOKAHEAD=0 (read at every cycle).  Its stream (the highest
 // priority, so the sweep CTAs are placed before the Gram-Schmidt blocks
@@ -1120,6 +1170,9 @@ extern "C" void fg_transport_krylov(femgpu_transport *t, fg_krylov *k, fg_linop 
 	op->precond_dsin = tr_precond_dsin;
 	op->matvec_dsout = tr_matvec_dsout;
 	op->precond_s = tr_precond_s;
+	op->matvec_g = nullptr;
+	op->precond_g = nullptr;
+	op->precond_g_out = nullptr;
 	k->dsv = krylov_ds(t);
 	k->la_s = nullptr;
 	if (!k->dsv && lookahead_on(t)) {
@@ -1130,6 +1183,14 @@ extern "C" void fg_transport_krylov(femgpu_transport *t, fg_krylov *k, fg_linop 
 		k->la_t = t->la_buf + t->ldv;
 		k->la_eta = t->la_buf + 2 * t->ldv;
 		k->la_flag = t->la_flag;
+		// the gather fused into the product: CSR over the SELL copy with the
+		// double-single sweeps (FEMGPU_LA_GATHER=0: the separate gather)
+		const char *e = getenv("FEMGPU_LA_GATHER");
+		if (t->o.scheme == FEMGPU_CSR && t->sell_A && t->sweeps.ds && t->sweeps.dpos && !(e && e[0] == '0')) {
+			op->matvec_g = tr_matvec_g;
+			op->precond_g = tr_precond_g;
+			op->precond_g_out = tr_precond_g_out;
+		}
 	}
 }
 

@@ -133,7 +133,8 @@ def test_sell_operators_vs_csrmv(gpu_lib):
 def test_lookahead_fgmres_matches_plain(gpu_lib, monkeypatch, kmax, blocks):
     """The look-ahead FGMRES step (the next direction's preconditioner applied
     to the raw operator output on a second stream while the Gram-Schmidt runs,
-    z = (M^-1 w - Z h) / eta) against the plain step (FEMGPU_LOOKAHEAD=0):
+    z = (M^-1 w - Z h) / eta), with the sweeps' gather as its own kernel and
+    written by the product, against the plain step (FEMGPU_LOOKAHEAD=0):
     both reach the true residual, within two iterations of each other, and
     agree with the direct solve; kmax 20 restarts (classical Gram-Schmidt
     with re-orthogonalisation in the later cycles), blocks 0 is the global
@@ -143,8 +144,10 @@ def test_lookahead_fgmres_matches_plain(gpu_lib, monkeypatch, kmax, blocks):
     p = skew_problem(m)
     x_ref, A, b = direct(m, p)
     out = {}
-    for la in ("0", "1"):
-        monkeypatch.setenv("FEMGPU_LOOKAHEAD", la)
+    for la in ("0", "1", "1g"):
+        monkeypatch.setenv("FEMGPU_LOOKAHEAD", la[0])
+        # "1": the sweeps' gather as a kernel of its own; "1g": written by the product
+        monkeypatch.setenv("FEMGPU_LA_GATHER", "1" if la == "1g" else "0")
         with fg.SSTransport.from_problem(m, p, scheme="CSR", reorder="SYMRCM", precond="ILU0", kmax=kmax,
                                          lmax=400, tol=TOL, solver="FGMRES", ilu_blocks=blocks) as T:
             T.Build(u=np.zeros(T.neq + 1))
@@ -156,3 +159,4 @@ def test_lookahead_fgmres_matches_plain(gpu_lib, monkeypatch, kmax, blocks):
         assert np.linalg.norm(b - A @ u[:-1]) / np.linalg.norm(b) <= TOL * 1.01
         assert np.linalg.norm(u[:-1] - x_ref) / np.linalg.norm(x_ref) < SOL_TOL
     assert abs(out["0"][1] - out["1"][1]) <= 2, (out["0"][1], out["1"][1])
+    assert abs(out["0"][1] - out["1g"][1]) <= 2, (out["0"][1], out["1g"][1])

@@ -40,7 +40,8 @@ CHAIN_TOL = 1e-11
 DS_TOL = 1e-9
 
 
-def apply_ilu(m, p, reorder, solver, layout=None, near=None, blocks=0, sync=None, chain="0", info=None, ds=None):
+def apply_ilu(m, p, reorder, solver, layout=None, near=None, blocks=0, sync=None, chain="0", info=None, ds=None,
+              fb=None):
     """Factor and apply the device ILU(0) of the transport system once; the
     layout, ring reach, level synchronisation (dataflow or one barrier per
     level), the chain-scan programs (chain "0": row-by-row only) and their
@@ -48,7 +49,7 @@ def apply_ilu(m, p, reorder, solver, layout=None, near=None, blocks=0, sync=None
     built."""
     import fem_codes_gb300 as fg
     env = {"FEMGPU_SWEEP_LAYOUT": layout, "FEMGPU_SWEEP_NEAR": near, "FEMGPU_SWEEP_SYNC": sync,
-           "FEMGPU_SWEEP_CHAIN": chain, "FEMGPU_SWEEP_DS": ds}
+           "FEMGPU_SWEEP_CHAIN": chain, "FEMGPU_SWEEP_DS": ds, "FEMGPU_SWEEP_FB": fb}
     saved = {k: os.environ.get(k) for k in env}
     try:
         for k, v in env.items():
@@ -185,6 +186,20 @@ def test_chain_sweeps_match_row_sweeps(gpu_lib, reorder, blocks, near, ds):
     assert info["chain"] == 1
     tol = CHAIN_TOL if ds == "0" else DS_TOL
     assert _rel_max(zc, z) <= tol, _rel_max(zc, z)
+
+
+@pytest.mark.parametrize("reorder,blocks,near", [("SYMRCM", 0, None), ("SYMRCM", 16, None), ("SYMRCM", 4, 8),
+                                                 ("NOT", 0, 8)])
+def test_fused_forward_backward_sweeps(gpu_lib, reorder, blocks, near):
+    """The double-single forward and backward sweeps in one launch (each
+    thread block keeps its SM from its block's forward sweep to its backward
+    sweep) give the two launches' result bit for bit."""
+    m = structured_mesh(160, 96, perturb=0.2, seed=21)
+    p = skew_problem(m)
+    z2, x2, _, _ = apply_ilu(m, p, reorder, "FGMRES", blocks=blocks, near=near, chain=None, fb="0")
+    z1, x1, _, _ = apply_ilu(m, p, reorder, "FGMRES", blocks=blocks, near=near, chain=None, fb="1")
+    assert np.array_equal(x1, x2)
+    assert np.array_equal(z1, z2)
 
 
 def test_chain_sweeps_wide_levels(gpu_lib):
