@@ -849,7 +849,9 @@ __global__ void k_la_snap(const fg_status *st, int *flag) { *flag = st->active; 
 // for: more than an SM holding an ILU sweep CTA (about 215 KB of its 228 KB)
 // has left, so the FP64-heavy blocks run on the other SMs and do not take
 // issue slots from the latency-bound sweep.
+#ifndef LA_SMEM
 #define LA_SMEM (24 * 1024)
+#endif
 
 // Look-ahead flexible GMRES cycle.  With w = A z_i and v_(i+1) =
 // (w - V h) / eta, linearity of M^-1 gives M^-1 v_(i+1) = (y - Z h) / eta
