@@ -658,16 +658,26 @@ def launches_estimate(a, iters):
     """Kernel launches of the timed steps (a FGMRES cycle enqueues all kmax
     steps; those past convergence are predicated off but launched): build 2
     (element build, CSR assembly with the RHS) + factor 5 (cluster elimination,
-    4 program refreshes) + per cycle 5 (residual start 3, back-substitution and
-    update 2) + per step (preconditioner 3: gather and two sweeps; matvec 1;
-    classical Gram-Schmidt 3, re-orthogonalised in restarted cycles 6; scale;
-    Givens) + the true-residual check 2."""
+    double-single program refresh and scan multipliers of both sweeps) + per
+    cycle 5 (product, residual start, scaling; back-substitution and update)
+    and in the look-ahead step 3 more for the first direction's preconditioner
+    (gather, both sweeps in one launch, conversion) + per step (look-ahead step: product with the
+    gather 1, flag copy 1, sweeps 1, classical Gram-Schmidt 3 per pass (one
+    pass in the first cycle, two in restarted ones), Z h 1, scaling 1, Givens
+    1, next direction 1; the last step of a cycle has no next direction; plain
+    step (FEMGPU_LOOKAHEAD=0): preconditioner 3, product 1, Gram-Schmidt,
+    scaling, Givens) + the true-residual check 2."""
     kmax = a.kmax
+    la = os.environ.get("FEMGPU_LOOKAHEAD", "1") != "0" and a.precision == "FP64"
     tot = 0
     for it in iters:
         cyc = max(1, (int(it) + kmax - 1) // kmax)
         for c in range(cyc):
-            tot += 5 + kmax * (3 + 1 + (3 if c == 0 else 6) + 2)
+            gs = 3 * (1 if c == 0 else 2)
+            if la:
+                tot += 8 + (kmax - 1) * (7 + gs) + (3 + gs)
+            else:
+                tot += 5 + kmax * (3 + 1 + gs + 2)
         tot += 2 + 5 + 2
     return tot
 
