@@ -1874,7 +1874,7 @@ static int factor_cluster_size(int P)
 		    cudaSuccess) { cudaGetLastError(); return 0; }
 		cudaFuncSetAttribute(k_ilu0_factor_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 		cudaGetLastError();
-		for (int c = 16; c >= 2; c /= 2) {
+		for (int c = 16; c >= 1; c /= 2) {
 			cudaLaunchConfig_t cfg = {};
 			cudaLaunchAttribute at[1];
 			at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1886,8 +1886,12 @@ static int factor_cluster_size(int P)
 			cudaGetLastError();
 		}
 	}
-	for (int c = 16; c >= 2; c /= 2)
-		if (fits[c] >= P) return c;
+	// FEMGPU_FACTOR_CLUSTER caps the cluster size (1 allowed: one CTA per
+	// block with the cluster kernel)
+	const char *e = getenv("FEMGPU_FACTOR_CLUSTER");
+	const int cap = e ? atoi(e) : 16;
+	for (int c = 16; c >= (cap == 1 ? 1 : 2); c /= 2)
+		if (c <= cap && fits[c] >= P) return c;
 	return 0;
 }
 
