@@ -81,7 +81,7 @@ class EulerOpts(ctypes.Structure):
                 ("precond", ctypes.c_int), ("solver", ctypes.c_int), ("kmax", ctypes.c_int),
                 ("lmax", ctypes.c_int), ("tol", ctypes.c_double), ("ncorr", ctypes.c_int),
                 ("precision", ctypes.c_int), ("scheme", ctypes.c_int), ("ilu_blocks", ctypes.c_int),
-                ("scaling", ctypes.c_int)]
+                ("scaling", ctypes.c_int), ("shock", ctypes.c_int), ("invY", ctypes.c_double * 4)]
 
 
 class NSOpts(ctypes.Structure):
@@ -823,10 +823,14 @@ class Euler:
 
     def __init__(self, x, y, vert, node_id, neq, upresc, gamma=1.4, mach=1.0, dimensionless=False,
                  alpha=0.5, dt=1e-3, stab_tol=1e-6, precond="BlockDiag", solver="GMRES", kmax=30,
-                 lmax=100, tol=1e-8, ncorr=2, precision="FP64", scheme="EBE", ilu_blocks=0, scaling="NOT"):
+                 lmax=100, tol=1e-8, ncorr=2, precision="FP64", scheme="EBE", ilu_blocks=0, scaling="NOT",
+                 shock="CAU", invY=(1.0, 1.0, 1.0, 1.0)):
         L = load()
         o = EulerOpts()
         L.femgpu_euler_default_opts(ctypes.byref(o))
+        o.shock = {"CAU": 0, "YZBETA": 1}[shock.upper()]
+        for k in range(4):
+            o.invY[k] = float(invY[k])
         o.scheme = OPTS["scheme"][scheme.upper()]
         o.ilu_blocks = int(ilu_blocks)
         o.scaling = {"NOT": 0, "BLOCKSCALING": 1}[scaling.upper()]

@@ -68,12 +68,14 @@ __device__ __forceinline__ double a0norm2(const double (&A0)[4][4], const double
 struct EulerCoef {
 	double gamma, mach, alpha, dt, stab_tol;
 	int dimensionless, neq;
+	int yzbeta;                 // shock capturing: 0 Delta_CAU, 1 Delta_YZBeta
+	double invY[4];             // YZBeta: the deck's Y^-1
 };
 
 __global__ void __launch_bounds__(128) k_euler_element(int nel, const int *__restrict__ vert,
 		const int *__restrict__ node_id, const double *__restrict__ xn, const double *__restrict__ yn,
 		const double *__restrict__ upresc, const double *__restrict__ u, const double *__restrict__ du,
-		EulerCoef cf, double *__restrict__ A, double *__restrict__ Re)
+		EulerCoef cf, double *__restrict__ A, double *__restrict__ Re, double *__restrict__ dold)
 {
 	const double third = 1.0 / 3.0, sixth = 1.0 / 6.0;
 	const double gamma = cf.gamma;
@@ -180,9 +182,36 @@ __global__ void __launch_bounds__(128) k_euler_element(int nel, const int *__res
 			A0[2][1] = A0[1][2]; A0[3][1] = A0[1][3]; A0[3][2] = A0[2][3];
 		}
 
-		// CAU delta (Delta_CAU.c:17-82).
+		// Shock-capturing delta: Delta_YZBeta.c:6-108 (stateful: blended with
+		// the element's previous delta, which it replaces) or Delta_CAU.c:17-82.
 		double delta;
-		{
+		if (cf.yzbeta) {
+			double Z[4];
+			#pragma unroll
+			for (int i = 0; i < 4; i++) Z[i] = dUb[i] + jvec<true>(Ax, gx, i) + jvec<false>(Ay, gy, i);
+			const double *iY = cf.invY;
+			double nYZ = sqrt(iY[0] * Z[0] * iY[0] * Z[0] + iY[1] * Z[1] * iY[1] * Z[1] +
+			                  iY[2] * Z[2] * iY[2] * Z[2] + iY[3] * Z[3] * iY[3] * Z[3]);
+			double nYx = iY[0] * gx[0] * iY[0] * gx[0] + iY[1] * gx[1] * iY[1] * gx[1] +
+			             iY[2] * gx[2] * iY[2] * gx[2] + iY[3] * gx[3] * iY[3] * gx[3];
+			double nYy = iY[0] * gy[0] * iY[0] * gy[0] + iY[1] * gy[1] * iY[1] * gy[1] +
+			             iY[2] * gy[2] * iY[2] * gy[2] + iY[3] * gy[3] * iY[3] * gy[3];
+			double sYdU = nYx + nYy;
+			double nYU = sqrt(iY[0] * Ub[0] * iY[0] * Ub[0] + iY[1] * Ub[1] * iY[1] * Ub[1] +
+			                  iY[2] * Ub[2] * iY[2] * Ub[2] + iY[3] * Ub[3] * iY[3] * Ub[3]);
+			double nrho = sqrt(gx[0] * gx[0] + gy[0] * gy[0]), J1 = 0.0, J2 = 0.0;
+			if (fabs(nrho) >= 1e-12) { J1 = gx[0] / nrho; J2 = gy[0] / nrho; }
+			double H = (fabs(J1 * yb[0] + J2 * xb[0]) + fabs(J1 * yb[1] + J2 * xb[1]) +
+			            fabs(J1 * yb[2] + J2 * xb[2])) / twoArea;
+			H = fabs(H) >= 1e-12 ? 2.0 * (1.0 / H) : 0.0;
+			const bool sok = fabs(sYdU) >= 1e-12, uok = fabs(nYU) >= 1e-12;
+			double d1 = nYZ * (sok ? 1.0 / sqrt(sYdU) : 0.0) * (uok ? 1.0 : 0.0) * (H * 0.5);
+			double d2 = nYZ * (sok ? 1.0 : 0.0) * (uok ? 1.0 / nYU : 0.0) * (H * 0.5 * H * 0.5);
+			const double w = 0.5;
+			double ad = w * (d1 + d2);
+			delta = w * (ad) + (1 - w) * dold[e];
+			dold[e] = delta;
+		} else {
 			double kx[4], ky[4], L[4];
 			#pragma unroll
 			for (int i = 0; i < 4; i++) {
@@ -375,10 +404,12 @@ extern "C" int fg_euler_build(femgpu_euler *c, const double *u, const double *du
 	EulerCoef cf;
 	cf.gamma = c->o.gamma; cf.mach = c->o.mach; cf.alpha = c->o.alpha; cf.dt = c->o.dt;
 	cf.stab_tol = c->o.stab_tol; cf.dimensionless = c->o.dimensionless; cf.neq = c->neq;
+	cf.yzbeta = c->o.shock == FEMGPU_SHOCK_YZBETA;
+	for (int k = 0; k < 4; k++) cf.invY[k] = c->o.invY[k];
 	femgpu_ebe *b = c->ebe;
 	int g = (int)((c->nel + 127LL) / 128);
 	k_euler_element<<<g, 128, 0, c->stream>>>(c->nel, b->vert, b->node_id, c->x, c->y, c->upresc, u, du, cf,
-	                                          b->A, c->Re);
+	                                          b->A, c->Re, c->dold);
 	FG_TRY(cudaGetLastError());
 	if (c->nslip_el > 0) {
 		k_euler_rotate<<<fg_grid(c->nslip_el), FG_TPB, 0, c->stream>>>(c->nslip_el, c->slip_el, b->vert,

@@ -29,6 +29,7 @@ struct femgpu_euler {
 	 * its wall angle, and the elements with a slip vertex */
 	int *slip_flag, *slip_el, nslip_el;
 	double *slip_cs, *slip_sn;
+	double *dold;                  /* YZBeta: each element's previous delta      */
 	cudaEvent_t ev[4];
 	double times[3];               /* build, precond setup, solve (s)            */
 };

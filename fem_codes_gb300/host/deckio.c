@@ -381,8 +381,11 @@ int femgpu_deck_euler_opts(const femgpu_deck *d, femgpu_euler_opts *o)
 		o->scheme = FEMGPU_CSR;
 	else return FEMGPU_E_ARG;
 	if (block_precond(d->Preconditioner, o->scheme == FEMGPU_CSR, &o->precond)) return FEMGPU_E_ARG;
-	if (strcasecmp(d->StabilizationForm, "SUPG") != 0 || strcasecmp(d->ShockCapture, "CAU") != 0)
-		return FEMGPU_E_ARG;
+	/* setStabilizationForm.c:6-32: SUPG with CAU or YZBeta (Y^-1 from the deck) */
+	if (strcasecmp(d->StabilizationForm, "SUPG") != 0) return FEMGPU_E_ARG;
+	if (!strcasecmp(d->ShockCapture, "YZBeta")) o->shock = FEMGPU_SHOCK_YZBETA;
+	else if (strcasecmp(d->ShockCapture, "CAU") != 0) return FEMGPU_E_ARG;
+	o->invY[0] = d->invY[0]; o->invY[1] = d->invY[1]; o->invY[2] = d->invY[2]; o->invY[3] = d->invY[3];
 	/* setScaling.c:6-27: "NOT", or "BlockScaling" with EBE storage only */
 	if (!strcasecmp(d->Scaling, "BlockScaling") && o->scheme == FEMGPU_EBE) o->scaling = 1;
 	else if (strcasecmp(d->Scaling, "NOT") != 0) return FEMGPU_E_ARG;

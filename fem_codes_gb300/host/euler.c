@@ -35,6 +35,8 @@ void femgpu_euler_default_opts(femgpu_euler_opts *o)
 	o->tol = 1e-8;
 	o->ncorr = 2;
 	o->scheme = FEMGPU_EBE;
+	o->shock = FEMGPU_SHOCK_CAU;
+	o->invY[0] = o->invY[1] = o->invY[2] = o->invY[3] = 1.0;
 }
 
 /* ---- operator callbacks of the Krylov solver ---------------------------- */
@@ -128,6 +130,8 @@ static int create(femgpu_euler *c, const femgpu_euler_opts *o, int nnodes, const
 	DM(c->R, sizeof(double) * n1);
 	DM(c->Da, sizeof(double) * n1);
 	DM(c->Re, sizeof(double) * 12 * (size_t)nel);
+	DM(c->dold, sizeof(double) * (size_t)nel);
+	CK(cudaMemsetAsync(c->dold, 0, sizeof(double) * (size_t)nel, c->stream));
 	CK(cudaMemsetAsync(c->u, 0, sizeof(double) * n1, c->stream));
 	CK(cudaMemsetAsync(c->a, 0, sizeof(double) * n1, c->stream));
 	CK(cudaMemsetAsync(c->R, 0, sizeof(double) * n1, c->stream));
@@ -163,7 +167,8 @@ int femgpu_euler_create(femgpu_euler **out, const femgpu_euler_opts *opts, int n
 	    (o.solver != FEMGPU_PGMRES && o.solver != FEMGPU_FGMRES) ||
 	    (o.precision != FEMGPU_FP64 && o.precision != FEMGPU_MIXED_IR) ||
 	    (o.precision == FEMGPU_MIXED_IR && o.solver != FEMGPU_FGMRES) ||
-	    (o.scaling != 0 && (o.scaling != 1 || o.scheme != FEMGPU_EBE))) {
+	    (o.scaling != 0 && (o.scaling != 1 || o.scheme != FEMGPU_EBE)) ||
+	    (o.shock != FEMGPU_SHOCK_CAU && o.shock != FEMGPU_SHOCK_YZBETA)) {
 		fgh_set_error("femgpu_euler_create: bad argument or option");
 		return FEMGPU_E_ARG;
 	}
@@ -184,7 +189,7 @@ void femgpu_euler_destroy(femgpu_euler *c)
 	if (c->ebe) femgpu_ebe_destroy(c->ebe);
 	{
 		void *p[] = { c->x, c->y, c->upresc, c->u, c->a, c->R, c->Da, c->Re, c->slip_flag, c->slip_el, c->slip_cs,
-		              c->slip_sn };
+		              c->slip_sn, c->dold };
 		for (i = 0; i < (int)(sizeof p / sizeof p[0]); i++) if (p[i]) cudaFree(p[i]);
 	}
 	fgh_kry_free(&c->kry);
@@ -471,6 +476,7 @@ int femgpu_euler_predictor(femgpu_euler *c, double *u, int nsteps, double *uhist
 	n1 = (size_t)c->neq + 1;
 	if (u) CK(cudaMemcpyAsync(c->u, u, sizeof(double) * n1, cudaMemcpyHostToDevice, c->stream));
 	CK(cudaMemsetAsync(c->a, 0, sizeof(double) * n1, c->stream));          /* a = 0 (mycalloc, :18) */
+	CK(cudaMemsetAsync(c->dold, 0, sizeof(double) * (size_t)c->nel, c->stream));   /* delta_old = 0 (:23) */
 	rc = predictor(c, nsteps, uhist, iters);
 	if (rc) return rc;
 	if (u) CK(cudaMemcpyAsync(u, c->u, sizeof(double) * n1, cudaMemcpyDeviceToHost, c->stream));

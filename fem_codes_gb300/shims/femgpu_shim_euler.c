@@ -85,9 +85,12 @@ static int eu_of(ParametersType *P, FemStructsType *FS, FemFunctionsType *FF)
 	double *x, *y, *up;
 	int *nid, *vert;
 	if (g_eu) return 0;
-	if (strcasecmp(P->StabilizationForm, "SUPG") != 0 || strcasecmp(P->ShockCapture, "CAU") != 0)
+	if (strcasecmp(P->StabilizationForm, "SUPG") != 0 ||
+	    (strcasecmp(P->ShockCapture, "CAU") != 0 && strcasecmp(P->ShockCapture, "YZBeta") != 0))
 		return FEMGPU_E_ARG;
 	femgpu_euler_default_opts(&o);
+	if (!strcasecmp(P->ShockCapture, "YZBeta")) o.shock = FEMGPU_SHOCK_YZBETA;
+	for (k = 0; k < 4; k++) o.invY[k] = P->invY[k];
 	if (!strcasecmp(P->MatrixVectorProductScheme, "EBE")) o.scheme = FEMGPU_EBE;
 	else if (!strcasecmp(P->MatrixVectorProductScheme, "CSR") && !strcasecmp(P->reordering, "NOT"))
 		o.scheme = FEMGPU_CSR;

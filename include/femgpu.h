@@ -386,6 +386,12 @@ typedef struct femgpu_euler_opts {
 	                     /* set up and R := D^-1 R, the prescribed rows and   */
 	                     /* columns of each element matrix made identity, and */
 	                     /* each node's row block multiplied by its D^-1      */
+	int shock;           /* ShockCapture: FEMGPU_SHOCK_CAU (Delta_CAU.c) or   */
+	                     /* FEMGPU_SHOCK_YZBETA (Delta_YZBeta.c:6-108: with   */
+	                     /* invY, blended with each element's previous delta, */
+	                     /* which starts at 0 when the context is made and    */
+	                     /* at every femgpu_euler_predictor call)             */
+	double invY[4];      /* the deck's Y^-1 (YZBeta)                          */
 } femgpu_euler_opts;
 
 void femgpu_euler_default_opts(femgpu_euler_opts *o);
@@ -437,7 +443,9 @@ int femgpu_euler_solve_dev(femgpu_euler *ctx, int *iters);
  * steps of ncorr correctors from u (host [neq+1], in/out; NULL = the device
  * state) with a = 0 at the start of every step.  uhist [nsteps*(neq+1)]
  * receives u after each step and iters [nsteps*ncorr] the GMRES iterations
- * of each corrector (NULL skips). */
+ * of each corrector (NULL skips).  The YZBeta shock parameters start at zero
+ * here (Predictor_Old.c:23); femgpu_euler_predictor_dev continues from the
+ * device state, theirs included. */
 int femgpu_euler_predictor(femgpu_euler *ctx, double *u, int nsteps, double *uhist, int *iters);
 int femgpu_euler_predictor_dev(femgpu_euler *ctx, int nsteps, int *iters);
 /* Device pointers of the state vectors u, a, R, Da [neq+1] and the block

@@ -25,6 +25,19 @@ int Block_scaling_EBE(ParametersType *, MatrixDataType *, FemStructsType *);
 int Build_M_K_F_SUPG(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *);
 double Delta_CAU(double, double *, double *, double *, double (*)[4], double (*)[4], double (*)[4],
                  double *, double, double, double, double, double, double, double, int, double *, double *);
+double Delta_YZBeta(double, double *, double *, double *, double (*)[4], double (*)[4], double (*)[4],
+                    double *, double, double, double, double, double, double, double, int, double *, double *);
+
+/* Shock capturing of the builds below: 0 Delta_CAU, 1 Delta_YZBeta with the
+ * deck's Y^-1 (the ShockCapture "YZBeta" of setStabilizationForm.c:27). */
+static int g_yz;
+static double g_invY[4];
+void ref_euler_set_shock(int yzbeta, const double *invY)
+{
+	int k;
+	g_yz = yzbeta;
+	for (k = 0; k < 4; k++) g_invY[k] = invY ? invY[k] : 1.0;
+}
 void dimensional_Ax_Ay_calculations(double, double, double *, double (*)[4], double (*)[4]);
 double REFLETIDO_gamma(double, double);
 double REFLETIDO_rhopresc(double, double);
@@ -88,13 +101,35 @@ static void setup(int csr, int nnodes, const double *x, const double *y, const i
 	FF->rhopresc = REFLETIDO_rhopresc; FF->v1presc = REFLETIDO_v1presc;
 	FF->v2presc = REFLETIDO_v2presc; FF->epresc = REFLETIDO_epresc;
 	FF->Ax_Ay_calculations = dimensional_Ax_Ay_calculations;
-	FF->ShockCapture = Delta_CAU;
+	FF->ShockCapture = g_yz ? Delta_YZBeta : Delta_CAU;
+	for (k = 0; k < 4; k++) P->invY[k] = g_invY[k];
 	FF->BC_theta = zero_theta;
 	FF->assembly = csr ? csr_assembly : ebe_assembly;
 	FF->mv = csr ? csrmv : ebemvNDOF4;
 	FF->precond = csr ? ILUp_precond : BlockDiag_precond;
 	FF->precond_setup = csr ? ILUp_precond_setup : BlockDiag_precond_EBE_setup;
 	*Po = P; *Mo = M; *FSo = FS; *FFo = FF;
+}
+
+/* Two consecutive Builds on the state (u, du) from a zero delta_old (the
+ * second reads the first's per-element shock parameter: Delta_YZBeta keeps
+ * one): Ae1, R1 and Ae2, R2, and delta_old after the second [nel]. */
+int ref_euler_build2(int nnodes, const double *x, const double *y, const int *node_id, int nel, const int *vert,
+                     int neq, double alpha, double dt, double stab_tol, const double *u, const double *du,
+                     double *Ae1, double *R1, double *Ae2, double *R2, double *dold)
+{
+	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF;
+	setup(0, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
+	memcpy(FS->u, u, sizeof(double) * (neq + 1));
+	memcpy(FS->du, du, sizeof(double) * (neq + 1));
+	Build_M_K_F_SUPG(P, M, FS, FF);
+	memcpy(Ae1, M->Aaux, sizeof(double) * nel * 144);
+	memcpy(R1, FS->F, sizeof(double) * (neq + 1));
+	Build_M_K_F_SUPG(P, M, FS, FF);
+	memcpy(Ae2, M->Aaux, sizeof(double) * nel * 144);
+	memcpy(R2, FS->F, sizeof(double) * (neq + 1));
+	memcpy(dold, FS->delta_old, sizeof(double) * nel);
+	return 0;
 }
 
 /* One Build on the state (u, du): element matrices Ae [nel*144] and R. */

@@ -217,6 +217,10 @@ EULER_CASES = {
 }
 
 
+# Y^-1 of the YZBeta cases: 1 / the REFLETIDO inflow state (1 for its zero v)
+YZ_INVY = np.array([1.0, 1.0 / 2.9, 1.0, 1.0 / 5.990715])
+
+
 def main_euler():
     """Euler SUPG+CAU Build on a perturbed state (element matrices and
     residual) and a short predictor-multicorrector run, through the
@@ -235,6 +239,9 @@ def main_euler():
     lib.ref_euler_build_slip.argtypes = [ctypes.c_int, _dp, _dp, _ip, _ip, ctypes.c_int, _ip, ctypes.c_int,
                                          ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp,
                                          _dp, _dp]
+    lib.ref_euler_set_shock.argtypes = [ctypes.c_int, _dp]
+    lib.ref_euler_build2.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
     lib.ref_euler_build_csr.restype = ctypes.c_int
     lib.ref_euler_build_csr.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp, ctypes.c_int,
@@ -297,11 +304,27 @@ def main_euler():
         its_s = np.zeros(nsteps * ncorr, np.int32)
         lib.ref_euler_predictor_scaled(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol,
                                        kmax, lmax, tol, nsteps, ncorr, ups, uhs, its_s)
+        # ShockCapture "YZBeta" (Delta_YZBeta.c) with Y^-1 from the inflow state: two consecutive
+        # Builds from a zero delta_old (the second blends the first's delta) and the predictor
+        lib.ref_euler_set_shock(1, YZ_INVY)
+        Ae_y1, R_y1, Ae_y2, R_y2 = (np.zeros(mesh.nel * 144), np.zeros(neq + 1), np.zeros(mesh.nel * 144),
+                                    np.zeros(neq + 1))
+        dold_y = np.zeros(mesh.nel)
+        lib.ref_euler_build2(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol, u, du,
+                             Ae_y1, R_y1, Ae_y2, R_y2, dold_y)
+        upy = pb.u0.copy()
+        uhy = np.zeros(nsteps * (neq + 1))
+        its_y = np.zeros(nsteps * ncorr, np.int32)
+        lib.ref_euler_predictor(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol,
+                                kmax, lmax, tol, nsteps, ncorr, upy, uhy, its_y)
+        lib.ref_euler_set_shock(0, np.ones(4))
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id,
             amg_spec=np.array(AMG_SYS_SPEC), amg_Fp=amg_Fp,
             bs_Ae=Ae_b.reshape(mesh.nel, 144), bs_R=R_b, bs_uhist=uhs.reshape(nsteps, neq + 1),
             bs_iters=its_s.reshape(nsteps, ncorr),
+            yz_invY=YZ_INVY, yz_Ae1=Ae_y1.reshape(mesh.nel, 144), yz_R1=R_y1, yz_Ae2=Ae_y2.reshape(mesh.nel, 144),
+            yz_R2=R_y2, yz_dold=dold_y, yz_uhist=uhy.reshape(nsteps, neq + 1), yz_iters=its_y.reshape(nsteps, ncorr),
             slip=slip, slip_cs=cs, slip_sn=sn, slip_Ae=Ae_s.reshape(mesh.nel, 144), slip_R=R_s,
             neq=neq, upresc=pb.upresc, u0=pb.u0, gamma=pb.gamma, alpha=alpha, dt=dt, stab_tol=stol,
             u=u, du=du, Ae=Ae.reshape(mesh.nel, 144), R=R, kmax=kmax, lmax=lmax, tol=tol,

@@ -126,6 +126,12 @@ def test_euler_and_ns_decks(tmp_path):
     assert dd["DeltaT"] == 5e-3 and dd["NonLinearMaxIter"] == 2 and dd["nel"] == 162
     o = fg.deck_opts(d)
     assert (o.scheme, o.precond, o.kmax, o.lmax, o.ncorr, o.scaling) == (2, 5, 50, 100, 2, 0)
+    assert (o.shock, list(o.invY)) == (0, [1.0, 1.0, 1.0, 1.0])
+    # setStabilizationForm.c:27: ShockCapture YZBeta takes the deck's Y^-1
+    t = text.replace("CAU\t:shock", "YZBeta\t:shock").replace("1\t:y1", "0.5\t:y1")
+    path.write_bytes(t.encode())
+    oy = fg.deck_opts(fg.read_deck(str(path), "euler"))
+    assert (oy.shock, list(oy.invY)) == (1, [1.0, 0.5, 1.0, 1.0])
     # setScaling.c:6-27: BlockScaling with EBE storage, rejected with CSR
     for scheme, pre, ok in (("EBE", "BlockDiag", True), ("CSR", "ILU0", False)):
         t = text.replace("NOT\t:scaling", "BlockScaling\t:scaling").replace("CSR\t:scheme", f"{scheme}\t:scheme")

@@ -273,3 +273,22 @@ def test_euler_csr_amg_setup_bitexact(gpu_lib, name):
     finally:
         amg.close()
     assert np.array_equal(Rp[:neq], g["amg_Fp"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_euler_yzbeta_vs_reference(gpu_lib, name):
+    """ShockCapture "YZBeta" (Delta_YZBeta.c:6-108, setStabilizationForm.c:27)
+    with the deck's Y^-1: two consecutive Builds from a zero delta_old, the
+    second blending the first's per-element delta, bit-identical Ae and R;
+    the predictor-multicorrector run (delta_old zeroed at its start, as
+    Predictor_Old.c:23 allocates it) within 1e-8."""
+    g = _load(name)
+    with _euler(g, shock="YZBeta", invY=g["yz_invY"]) as eu:
+        R1, Ae1 = eu.Build(g["u"], g["du"], want_matrix=True)
+        R2, Ae2 = eu.Build(g["u"], g["du"], want_matrix=True)
+    assert np.array_equal(Ae1, g["yz_Ae1"]) and np.array_equal(R1, g["yz_R1"])
+    assert np.array_equal(Ae2, g["yz_Ae2"]) and np.array_equal(R2, g["yz_R2"])
+    with _euler(g, shock="YZBeta", invY=g["yz_invY"]) as eu:
+        uh, its = eu.Predictor(g["u0"], int(g["nsteps"]))
+    assert _rel(uh, g["yz_uhist"]) < SOL_RTOL
+    assert np.abs(its.astype(int) - g["yz_iters"].astype(int)).max() <= 1
