@@ -81,7 +81,8 @@ class EulerOpts(ctypes.Structure):
                 ("precond", ctypes.c_int), ("solver", ctypes.c_int), ("kmax", ctypes.c_int),
                 ("lmax", ctypes.c_int), ("tol", ctypes.c_double), ("ncorr", ctypes.c_int),
                 ("precision", ctypes.c_int), ("scheme", ctypes.c_int), ("ilu_blocks", ctypes.c_int),
-                ("scaling", ctypes.c_int), ("shock", ctypes.c_int), ("invY", ctypes.c_double * 4)]
+                ("scaling", ctypes.c_int), ("shock", ctypes.c_int), ("invY", ctypes.c_double * 4),
+                ("method", ctypes.c_int)]
 
 
 class NSOpts(ctypes.Structure):
@@ -162,6 +163,7 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_deck_transport_opts": [_vp, _vp],
         "femgpu_deck_euler_opts": [_vp, _vp],
         "femgpu_deck_transient_opts": [_vp, _vp, _vp],
+        "femgpu_euler_set_build_params": [_vp, ctypes.c_double, ctypes.c_double],
         "femgpu_deck_ns_opts": [_vp, _vp],
         "femgpu_deck_amg": [_vp, _vp, _vp, _vp, _vp],
         "femgpu_ilu_chain_segments": [ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
@@ -824,11 +826,12 @@ class Euler:
     def __init__(self, x, y, vert, node_id, neq, upresc, gamma=1.4, mach=1.0, dimensionless=False,
                  alpha=0.5, dt=1e-3, stab_tol=1e-6, precond="BlockDiag", solver="GMRES", kmax=30,
                  lmax=100, tol=1e-8, ncorr=2, precision="FP64", scheme="EBE", ilu_blocks=0, scaling="NOT",
-                 shock="CAU", invY=(1.0, 1.0, 1.0, 1.0)):
+                 shock="CAU", invY=(1.0, 1.0, 1.0, 1.0), method="Predictor1"):
         L = load()
         o = EulerOpts()
         L.femgpu_euler_default_opts(ctypes.byref(o))
         o.shock = {"CAU": 0, "YZBETA": 1}[shock.upper()]
+        o.method = {"PREDICTOR1": 0, "PREDICTOR1_BDF": 1, "PREDICTOR1_TRBDF2": 2}[method.upper()]
         for k in range(4):
             o.invY[k] = float(invY[k])
         o.scheme = OPTS["scheme"][scheme.upper()]
@@ -949,11 +952,14 @@ class Euler:
         return X, it.value
 
     def Predictor(self, u0, nsteps):
-        """Predictor_Old for nsteps steps from u0. Returns (u after each step
-        [nsteps, neq+1], GMRES iterations [nsteps, ncorr])."""
+        """The time loop (Predictor_Old, or its BDF / TR-BDF2 form) for nsteps
+        steps from u0. Returns (u after each stage [stages, neq+1], GMRES
+        iterations [stages, ncorr]); a stage is a step, two per step for
+        TR-BDF2."""
         u = np.array(u0, dtype=np.float64, copy=True)
-        uh = np.zeros((nsteps, self.neq + 1))
-        its = np.zeros((nsteps, self.opts.ncorr), np.int32)
+        stages = nsteps * (2 if self.opts.method == 2 else 1)
+        uh = np.zeros((stages, self.neq + 1))
+        its = np.zeros((stages, self.opts.ncorr), np.int32)
         self._check(self._L.femgpu_euler_predictor(self._h, _ptr(u), int(nsteps), _ptr(uh), _ptr(its)),
                     "Predictor")
         return uh, its

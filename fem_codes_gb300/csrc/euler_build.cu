@@ -402,7 +402,7 @@ __global__ void k_euler_rotate(int nslip, const int *__restrict__ slip_el, const
 extern "C" int fg_euler_build(femgpu_euler *c, const double *u, const double *du)
 {
 	EulerCoef cf;
-	cf.gamma = c->o.gamma; cf.mach = c->o.mach; cf.alpha = c->o.alpha; cf.dt = c->o.dt;
+	cf.gamma = c->o.gamma; cf.mach = c->o.mach; cf.alpha = c->alpha_build; cf.dt = c->dt_build;
 	cf.stab_tol = c->o.stab_tol; cf.dimensionless = c->o.dimensionless; cf.neq = c->neq;
 	cf.yzbeta = c->o.shock == FEMGPU_SHOCK_YZBETA;
 	for (int k = 0; k < 4; k++) cf.invY[k] = c->o.invY[k];
@@ -424,6 +424,20 @@ extern "C" int fg_euler_build(femgpu_euler *c, const double *u, const double *du
 extern "C" int fg_euler_predict(femgpu_euler *c, double c_pred)
 {
 	k_euler_predict<<<fg_grid(c->neq), FG_TPB, 0, c->stream>>>(c->neq, c->u, c->a, c_pred);
+	return (int)cudaGetLastError();
+}
+
+__global__ void k_euler_lin(int n, double *u, const double *p, const double *q, double *a, double cp, double cq)
+{
+	for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < n; I += gridDim.x * blockDim.x) {
+		u[I] = cp*p[I] - cq*q[I];
+		a[I] = 0.0;
+	}
+}
+
+extern "C" int fg_euler_lin(femgpu_euler *c, const double *p, const double *q, double cp, double cq)
+{
+	k_euler_lin<<<fg_grid(c->neq), FG_TPB, 0, c->stream>>>(c->neq, c->u, p, q, c->a, cp, cq);
 	return (int)cudaGetLastError();
 }
 

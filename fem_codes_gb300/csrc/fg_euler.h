@@ -30,6 +30,8 @@ struct femgpu_euler {
 	int *slip_flag, *slip_el, nslip_el;
 	double *slip_cs, *slip_sn;
 	double *dold;                  /* YZBeta: each element's previous delta      */
+	double alpha_build, dt_build;  /* the builds' Alpha_Build, DeltaT_Build      */
+	double *u1, *u2, *uold;        /* BDF / TR-BDF2 history (neq+1 each)         */
 	cudaEvent_t ev[4];
 	double times[3];               /* build, precond setup, solve (s)            */
 };
@@ -41,6 +43,9 @@ int fg_euler_build(femgpu_euler *c, const double *u, const double *du);
 int fg_euler_predict(femgpu_euler *c, double c_pred);
 /* a += Da, u += c_corr Da (Predictor_Old.c:115-116). */
 int fg_euler_correct(femgpu_euler *c, double c_corr);
+/* u = cp p - cq q, a = 0 (u may be p): Predictor_Old_BDF.c:119-123,
+ * Predictor_Old_TRBDF2.c:118-122. */
+int fg_euler_lin(femgpu_euler *c, const double *p, const double *q, double cp, double cq);
 
 #ifdef __cplusplus
 }

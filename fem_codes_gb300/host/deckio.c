@@ -386,6 +386,10 @@ int femgpu_deck_euler_opts(const femgpu_deck *d, femgpu_euler_opts *o)
 	if (!strcasecmp(d->ShockCapture, "YZBeta")) o->shock = FEMGPU_SHOCK_YZBETA;
 	else if (strcasecmp(d->ShockCapture, "CAU") != 0) return FEMGPU_E_ARG;
 	o->invY[0] = d->invY[0]; o->invY[1] = d->invY[1]; o->invY[2] = d->invY[2]; o->invY[3] = d->invY[3];
+	/* setStabilizationForm.c:9-21: Predictor1, Predictor1_BDF, Predictor1_TRBDF2 */
+	if (!strcasecmp(d->TimeIntegration, "Predictor1_BDF")) o->method = FEMGPU_TI_BDF;
+	else if (!strcasecmp(d->TimeIntegration, "Predictor1_TRBDF2")) o->method = FEMGPU_TI_TRBDF2;
+	else if (strcasecmp(d->TimeIntegration, "Predictor1") != 0) return FEMGPU_E_ARG;
 	/* setScaling.c:6-27: "NOT", or "BlockScaling" with EBE storage only */
 	if (!strcasecmp(d->Scaling, "BlockScaling") && o->scheme == FEMGPU_EBE) o->scaling = 1;
 	else if (strcasecmp(d->Scaling, "NOT") != 0) return FEMGPU_E_ARG;

@@ -131,6 +131,8 @@ static int create(femgpu_euler *c, const femgpu_euler_opts *o, int nnodes, const
 	DM(c->Da, sizeof(double) * n1);
 	DM(c->Re, sizeof(double) * 12 * (size_t)nel);
 	DM(c->dold, sizeof(double) * (size_t)nel);
+	c->alpha_build = o->alpha;
+	c->dt_build = o->dt;
 	CK(cudaMemsetAsync(c->dold, 0, sizeof(double) * (size_t)nel, c->stream));
 	CK(cudaMemsetAsync(c->u, 0, sizeof(double) * n1, c->stream));
 	CK(cudaMemsetAsync(c->a, 0, sizeof(double) * n1, c->stream));
@@ -168,7 +170,8 @@ int femgpu_euler_create(femgpu_euler **out, const femgpu_euler_opts *opts, int n
 	    (o.precision != FEMGPU_FP64 && o.precision != FEMGPU_MIXED_IR) ||
 	    (o.precision == FEMGPU_MIXED_IR && o.solver != FEMGPU_FGMRES) ||
 	    (o.scaling != 0 && (o.scaling != 1 || o.scheme != FEMGPU_EBE)) ||
-	    (o.shock != FEMGPU_SHOCK_CAU && o.shock != FEMGPU_SHOCK_YZBETA)) {
+	    (o.shock != FEMGPU_SHOCK_CAU && o.shock != FEMGPU_SHOCK_YZBETA) ||
+	    (o.method != FEMGPU_TI_PREDICTOR1 && o.method != FEMGPU_TI_BDF && o.method != FEMGPU_TI_TRBDF2)) {
 		fgh_set_error("femgpu_euler_create: bad argument or option");
 		return FEMGPU_E_ARG;
 	}
@@ -189,7 +192,7 @@ void femgpu_euler_destroy(femgpu_euler *c)
 	if (c->ebe) femgpu_ebe_destroy(c->ebe);
 	{
 		void *p[] = { c->x, c->y, c->upresc, c->u, c->a, c->R, c->Da, c->Re, c->slip_flag, c->slip_el, c->slip_cs,
-		              c->slip_sn, c->dold };
+		              c->slip_sn, c->dold, c->u1, c->u2, c->uold };
 		for (i = 0; i < (int)(sizeof p / sizeof p[0]); i++) if (p[i]) cudaFree(p[i]);
 	}
 	fgh_kry_free(&c->kry);
@@ -428,37 +431,100 @@ static double elapsed(cudaEvent_t a, cudaEvent_t b)
 	return 1e-3 * ms;
 }
 
+/* One multicorrection stage (Predictor_Old.c:68-126): ncorr correctors of
+ * build, scaling, preconditioner set-up, solve and a += Da, u += coef Da;
+ * then u to uhist[stage] and the iterations to iters[stage*ncorr...]. */
+static int stage(femgpu_euler *c, double coef, int st, double *uhist, int *iters)
+{
+	size_t n1 = (size_t)c->neq + 1;
+	int i, rc;
+	for (i = 0; i < c->o.ncorr; i++) {
+		int it = 0;
+		CK(cudaEventRecord(c->ev[0], c->stream));
+		KR(femgpu_euler_build_dev(c));                                      /* :71      */
+		if (c->o.scaling) KR(femgpu_euler_scale_dev(c));                    /* :73      */
+		CK(cudaEventRecord(c->ev[1], c->stream));
+		KR(femgpu_euler_precond_setup_dev(c));                              /* :75      */
+		CK(cudaEventRecord(c->ev[2], c->stream));
+		rc = solve(c, c->R, c->Da, &it);                                    /* :111     */
+		if (rc) return rc;
+		CK(cudaEventRecord(c->ev[3], c->stream));
+		KR(fg_euler_correct(c, coef));                                      /* :115-116 */
+		CK(cudaEventSynchronize(c->ev[3]));
+		c->times[0] += elapsed(c->ev[0], c->ev[1]);
+		c->times[1] += elapsed(c->ev[1], c->ev[2]);
+		c->times[2] += elapsed(c->ev[2], c->ev[3]);
+		if (iters) iters[st * c->o.ncorr + i] = it;
+	}
+	if (uhist)
+		CK(cudaMemcpyAsync(uhist + (size_t)st * n1, c->u, sizeof(double) * n1, cudaMemcpyDeviceToHost, c->stream));
+	return 0;
+}
+
 static int predictor(femgpu_euler *c, int nsteps, double *uhist, int *iters)
 {
-	const double c_pred = (1.0 - c->o.alpha) * c->o.dt, c_corr = c->o.alpha * c->o.dt;
-	size_t n1 = (size_t)c->neq + 1;
-	int step, i, rc;
+	const double alpha = c->o.alpha, dt = c->o.dt;
+	const size_t n1 = (size_t)c->neq + 1, nb = sizeof(double) * (size_t)c->neq;
+	int step;
 	memset(c->times, 0, sizeof c->times);
-	for (step = 0; step < nsteps; step++) {
-		KR(fg_euler_predict(c, c_pred));                                    /* :57-62   */
-		for (i = 0; i < c->o.ncorr; i++) {                                  /* :68-126  */
-			int it = 0;
-			CK(cudaEventRecord(c->ev[0], c->stream));
-			KR(femgpu_euler_build_dev(c));                                  /* :71      */
-			if (c->o.scaling) KR(femgpu_euler_scale_dev(c));                /* :73      */
-			CK(cudaEventRecord(c->ev[1], c->stream));
-			KR(femgpu_euler_precond_setup_dev(c));                          /* :75      */
-			CK(cudaEventRecord(c->ev[2], c->stream));
-			rc = solve(c, c->R, c->Da, &it);                                /* :111     */
-			if (rc) return rc;
-			CK(cudaEventRecord(c->ev[3], c->stream));
-			KR(fg_euler_correct(c, c_corr));                                /* :115-116 */
-			CK(cudaEventSynchronize(c->ev[3]));
-			c->times[0] += elapsed(c->ev[0], c->ev[1]);
-			c->times[1] += elapsed(c->ev[1], c->ev[2]);
-			c->times[2] += elapsed(c->ev[2], c->ev[3]);
-			if (iters) iters[step * c->o.ncorr + i] = it;
+	c->alpha_build = alpha;                                  /* Alpha_Build = Alpha   */
+	c->dt_build = dt;                                        /* DeltaT_Build = DeltaT */
+	if (c->o.method != FEMGPU_TI_PREDICTOR1 && !c->u1) {
+		DM(c->u1, sizeof(double) * n1);
+		DM(c->u2, sizeof(double) * n1);
+		DM(c->uold, sizeof(double) * n1);
+	}
+	if (c->o.method == FEMGPU_TI_BDF && nsteps > 0) {
+		/* Predictor_Old_BDF.c:50-160: an implicit first step whose update
+		 * keeps the deck's alpha, then BDF2 u = 4/3 u_n - 1/3 u_(n-1) with
+		 * updates of 2/3 dt; the builds keep Alpha_Build and DeltaT_Build */
+		const double four_thirds = 4.0/3.0, two_thirds = 2.0/3.0, one_third = 1.0/3.0;
+		CK(cudaMemcpyAsync(c->u1, c->u, nb, cudaMemcpyDeviceToDevice, c->stream));
+		CK(cudaMemsetAsync(c->a, 0, nb, c->stream));
+		KR(stage(c, alpha*dt, 0, uhist, iters));
+		CK(cudaMemcpyAsync(c->u2, c->u, nb, cudaMemcpyDeviceToDevice, c->stream));
+		for (step = 1; step < nsteps; step++) {
+			KR(fg_euler_lin(c, c->u2, c->u1, four_thirds, one_third));
+			KR(stage(c, two_thirds*dt, step, uhist, iters));
+			CK(cudaMemcpyAsync(c->u1, c->u2, nb, cudaMemcpyDeviceToDevice, c->stream));
+			CK(cudaMemcpyAsync(c->u2, c->u, nb, cudaMemcpyDeviceToDevice, c->stream));
 		}
-		if (uhist)
-			CK(cudaMemcpyAsync(uhist + (size_t)step * n1, c->u, sizeof(double) * n1, cudaMemcpyDeviceToHost,
-			                   c->stream));
+	} else if (c->o.method == FEMGPU_TI_TRBDF2) {
+		/* Predictor_Old_TRBDF2.c:34-165: per step a trapezoidal stage of
+		 * lambda dt (alpha 1/2) and a BDF2 stage u = A u - B u_old (alpha
+		 * 1/(2 - lambda)) over the rest; DeltaT_Build is the TR sub-step
+		 * before the loop and the BDF2 sub-step from the first BDF2 stage on */
+		const double lambda = 2.0 - sqrt(2.0);
+		const double A = 1.0/(lambda*(2.0 - lambda));
+		const double B = (1.0 - lambda)*(1.0 - lambda)/(lambda*(2.0 - lambda));
+		const double dtTR = lambda*dt, dtBDF2 = (1.0 - lambda)*dt;
+		const double a_tr = 0.5, a_bdf = 1.0/(2.0 - lambda);
+		CK(cudaMemcpyAsync(c->uold, c->u, nb, cudaMemcpyDeviceToDevice, c->stream));
+		c->dt_build = dtTR;
+		for (step = 0; step < nsteps; step++) {
+			KR(fg_euler_predict(c, a_tr*dtTR));                    /* u += alpha dtTR a, a = 0 */
+			KR(stage(c, a_tr*dtTR, 2 * step, uhist, iters));
+			c->dt_build = dtBDF2;
+			KR(fg_euler_lin(c, c->u, c->uold, A, B));              /* u = A u - B u_old, a = 0 */
+			KR(stage(c, a_bdf*dtBDF2, 2 * step + 1, uhist, iters));
+			CK(cudaMemcpyAsync(c->uold, c->u, nb, cudaMemcpyDeviceToDevice, c->stream));
+		}
+	} else {
+		const double c_pred = (1.0 - alpha) * dt, c_corr = alpha * dt;
+		for (step = 0; step < nsteps; step++) {
+			KR(fg_euler_predict(c, c_pred));                       /* :57-62   */
+			KR(stage(c, c_corr, step, uhist, iters));
+		}
 	}
 	CK(cudaStreamSynchronize(c->stream));
+	return 0;
+}
+
+int femgpu_euler_set_build_params(femgpu_euler *c, double alpha_build, double dt_build)
+{
+	if (!c || !(dt_build > 0.0)) return FEMGPU_E_ARG;
+	c->alpha_build = alpha_build;
+	c->dt_build = dt_build;
 	return 0;
 }
 

@@ -168,7 +168,9 @@ int femgpu_shim_euler_Build(ParametersType *P, MatrixDataType *M, FemStructsType
 	const int csr = !strcasecmp(P->MatrixVectorProductScheme, "CSR");
 	int rc = eu_of(P, FS, FF);
 	if (rc) return fail("Build (context)", rc);
-	rc = femgpu_euler_build(g_eu, FS->u, FS->du, g_copy_matrix && !csr ? M->Aaux : NULL, FS->F);
+	/* the time loop's Alpha_Build / DeltaT_Build (Build_M_K_F_SUPG.c:19-20) */
+	if (P->DeltaT_Build > 0.0) rc = femgpu_euler_set_build_params(g_eu, P->Alpha_Build, P->DeltaT_Build);
+	if (!rc) rc = femgpu_euler_build(g_eu, FS->u, FS->du, g_copy_matrix && !csr ? M->Aaux : NULL, FS->F);
 	if (!rc && g_copy_matrix && csr) {
 		int nn[2];
 		rc = femgpu_euler_csr(g_eu, nn, NULL, NULL, NULL, M->AA);

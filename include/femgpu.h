@@ -392,6 +392,13 @@ typedef struct femgpu_euler_opts {
 	                     /* which starts at 0 when the context is made and    */
 	                     /* at every femgpu_euler_predictor call)             */
 	double invY[4];      /* the deck's Y^-1 (YZBeta)                          */
+	int method;          /* TimeIntegration: FEMGPU_TI_PREDICTOR1            */
+	                     /* (Predictor_Old.c), FEMGPU_TI_BDF                  */
+	                     /* (Predictor_Old_BDF.c: an implicit first step,     */
+	                     /* then BDF2) or FEMGPU_TI_TRBDF2                    */
+	                     /* (Predictor_Old_TRBDF2.c: a trapezoidal and a BDF2 */
+	                     /* stage per step, the build's DeltaT the TR sub-step */
+	                     /* for its first build only, the BDF2 one after)     */
 } femgpu_euler_opts;
 
 void femgpu_euler_default_opts(femgpu_euler_opts *o);
@@ -443,10 +450,17 @@ int femgpu_euler_solve_dev(femgpu_euler *ctx, int *iters);
  * steps of ncorr correctors from u (host [neq+1], in/out; NULL = the device
  * state) with a = 0 at the start of every step.  uhist [nsteps*(neq+1)]
  * receives u after each step and iters [nsteps*ncorr] the GMRES iterations
- * of each corrector (NULL skips).  The YZBeta shock parameters start at zero
+ * of each corrector (NULL skips); with FEMGPU_TI_TRBDF2 a step has two stages
+ * and uhist [2*nsteps*(neq+1)], iters [2*nsteps*ncorr] hold them, the TR
+ * stage first.  The YZBeta shock parameters start at zero
  * here (Predictor_Old.c:23); femgpu_euler_predictor_dev continues from the
  * device state, theirs included. */
 int femgpu_euler_predictor(femgpu_euler *ctx, double *u, int nsteps, double *uhist, int *iters);
+/* The Alpha_Build and DeltaT_Build the following builds use
+ * (Build_M_K_F_SUPG.c:19-20; the time loops set them: Predictor_Old_TRBDF2.c
+ * changes DeltaT_Build between its stages), for a driver that keeps its own
+ * time loop; femgpu_euler_predictor sets them itself. */
+int femgpu_euler_set_build_params(femgpu_euler *ctx, double alpha_build, double dt_build);
 int femgpu_euler_predictor_dev(femgpu_euler *ctx, int nsteps, int *iters);
 /* Device pointers of the state vectors u, a, R, Da [neq+1] and the block
  * EBE operator holding the element matrices. */

@@ -290,3 +290,71 @@ int ref_euler_build_csr(int nnodes, const double *x, const double *y, const int 
 	}
 	return nnz;
 }
+
+/* The reference's own Predictor_Old_BDF.c / Predictor_Old_TRBDF2.c
+ * (00_CommonFiles/Time_Integration, TimeIntegration "Predictor1_BDF" /
+ * "Predictor1_TRBDF2" of setStabilizationForm.c:12-17) on the EBE
+ * BlockDiag set-up above: ncorr correctors per stage (StopByIterations) and
+ * nsteps time checks (StopTimeIntegration).  Per stage (multicorrection
+ * loop): uhist [cap*(neq+1)] u at its end, iters [cap*ncorr] the GMRES
+ * iterations of its correctors.  Returns the number of stages. */
+int Predictor_Old_BDF(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *,
+                      FemOtherFunctionsType *);
+int Predictor_Old_TRBDF2(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *,
+                         FemOtherFunctionsType *);
+static const double *g_u0;
+static double *g_uh, *g_uc;
+static int *g_it, g_stage, g_cap, g_ncorr, g_nchk, g_maxchk, g_neq1, g_corr;
+static int tint_init(ParametersType *P, NodeType *N, double *u)
+{
+	(void)N;
+	memcpy(u, g_u0, sizeof(double) * (P->neq + 1));
+	return 0;
+}
+static int tint_stage(ParametersType *P, double na, double nda, int i)
+{
+	(void)na; (void)nda;
+	if (i < g_ncorr) return 0;
+	if (g_stage < g_cap) memcpy(g_uh + (size_t)g_stage * g_neq1, g_uc, sizeof(double) * g_neq1);
+	g_stage++;
+	g_corr = 0;
+	return 1;
+}
+static int tint_time(ParametersType *P, double *u, double *uo, double t)
+{
+	(void)P; (void)u; (void)uo; (void)t;
+	return ++g_nchk >= g_maxchk;
+}
+static int tint_solver(ParametersType *P, MatrixDataType *M, FemStructsType *FS, FemFunctionsType *FF, double *B,
+                       double *X)
+{
+	int before = P->iterations, rc = gmres6(P, M, FS, FF, B, X);
+	if (g_stage < g_cap && g_corr < g_ncorr) g_it[(size_t)g_stage * g_ncorr + g_corr] = P->iterations - before;
+	g_corr++;
+	return rc;
+}
+static int tint_noscale(ParametersType *P, MatrixDataType *M, FemStructsType *FS) { return 0; }
+static int tint_nounscale(ParametersType *P, MatrixDataType *M, FemStructsType *FS, double *x) { return 0; }
+
+int ref_euler_predictor_tint(int trbdf2, int nnodes, const double *x, const double *y, const int *node_id, int nel,
+                             const int *vert, int neq, double alpha, double dt, double stab_tol, int kmax, int lmax,
+                             double tol, int nsteps, int ncorr, const double *u0, int cap, double *uhist, int *iters)
+{
+	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF;
+	FemOtherFunctionsType *FOF = mycalloc("FOF", 1, sizeof(FemOtherFunctionsType));
+	setup(0, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
+	P->KrylovBasisVectorsQuantity = kmax; P->LinearMaxIter = lmax; P->SolverTolerance = tol;
+	P->NonLinearMaxIter = ncorr;
+	FOF->Build = Build_M_K_F_SUPG;
+	FOF->solver = tint_solver;
+	FF->InitialSolution = tint_init;
+	FF->StopCriteria = tint_stage;
+	FF->StopTimeIntegration = tint_time;
+	FF->scaling = tint_noscale;
+	FF->unscaling = tint_nounscale;
+	g_u0 = u0; g_uh = uhist; g_uc = FS->u; g_it = iters; g_stage = 0; g_cap = cap; g_ncorr = ncorr;
+	g_nchk = 0; g_maxchk = nsteps; g_neq1 = neq + 1; g_corr = 0;
+	if (trbdf2) Predictor_Old_TRBDF2(P, M, FS, FF, FOF);
+	else Predictor_Old_BDF(P, M, FS, FF, FOF);
+	return g_stage;
+}

@@ -240,6 +240,11 @@ def main_euler():
                                          ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp,
                                          _dp, _dp]
     lib.ref_euler_set_shock.argtypes = [ctypes.c_int, _dp]
+    lib.ref_euler_predictor_tint.restype = ctypes.c_int
+    lib.ref_euler_predictor_tint.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip,
+                                             ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                             ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                             ctypes.c_int, _dp, ctypes.c_int, _dp, _ip]
     lib.ref_euler_build2.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
     lib.ref_euler_build_csr.restype = ctypes.c_int
@@ -318,6 +323,17 @@ def main_euler():
         lib.ref_euler_predictor(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol,
                                 kmax, lmax, tol, nsteps, ncorr, upy, uhy, its_y)
         lib.ref_euler_set_shock(0, np.ones(4))
+        # TimeIntegration Predictor1_BDF (3 time checks: 4 stages) and Predictor1_TRBDF2 (2 checks:
+        # 4 stages) through the reference's own loops
+        tint = {}
+        for key, trbdf2, checks in (("bdf", 0, 3), ("tr", 1, 2)):
+            cap = 8
+            uht = np.zeros(cap * (neq + 1))
+            itt = np.zeros(cap * ncorr, np.int32)
+            st = lib.ref_euler_predictor_tint(trbdf2, mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha,
+                                              dt, stol, kmax, lmax, tol, checks, ncorr, pb.u0, cap, uht, itt)
+            tint[key + "_uhist"] = uht[:st * (neq + 1)].reshape(st, neq + 1)
+            tint[key + "_iters"] = itt[:st * ncorr].reshape(st, ncorr)
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id,
             amg_spec=np.array(AMG_SYS_SPEC), amg_Fp=amg_Fp,
@@ -325,6 +341,7 @@ def main_euler():
             bs_iters=its_s.reshape(nsteps, ncorr),
             yz_invY=YZ_INVY, yz_Ae1=Ae_y1.reshape(mesh.nel, 144), yz_R1=R_y1, yz_Ae2=Ae_y2.reshape(mesh.nel, 144),
             yz_R2=R_y2, yz_dold=dold_y, yz_uhist=uhy.reshape(nsteps, neq + 1), yz_iters=its_y.reshape(nsteps, ncorr),
+            **tint,
             slip=slip, slip_cs=cs, slip_sn=sn, slip_Ae=Ae_s.reshape(mesh.nel, 144), slip_R=R_s,
             neq=neq, upresc=pb.upresc, u0=pb.u0, gamma=pb.gamma, alpha=alpha, dt=dt, stab_tol=stol,
             u=u, du=du, Ae=Ae.reshape(mesh.nel, 144), R=R, kmax=kmax, lmax=lmax, tol=tol,

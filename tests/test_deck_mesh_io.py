@@ -132,6 +132,15 @@ def test_euler_and_ns_decks(tmp_path):
     path.write_bytes(t.encode())
     oy = fg.deck_opts(fg.read_deck(str(path), "euler"))
     assert (oy.shock, list(oy.invY)) == (1, [1.0, 0.5, 1.0, 1.0])
+    # setStabilizationForm.c:9-21: the SUPG time loops
+    for ti, method in (("PREDICTOR1_BDF", 1), ("Predictor1_TRBDF2", 2), ("Predictor2", None)):
+        path.write_bytes(text.replace("PREDICTOR1\t:ti", f"{ti}\t:ti").encode())
+        dt_ = fg.read_deck(str(path), "euler")
+        if method is None:
+            with pytest.raises(fg.FemGpuError):
+                fg.deck_opts(dt_)
+        else:
+            assert fg.deck_opts(dt_).method == method
     # setScaling.c:6-27: BlockScaling with EBE storage, rejected with CSR
     for scheme, pre, ok in (("EBE", "BlockDiag", True), ("CSR", "ILU0", False)):
         t = text.replace("NOT\t:scaling", "BlockScaling\t:scaling").replace("CSR\t:scheme", f"{scheme}\t:scheme")

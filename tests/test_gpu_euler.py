@@ -292,3 +292,21 @@ def test_euler_yzbeta_vs_reference(gpu_lib, name):
         uh, its = eu.Predictor(g["u0"], int(g["nsteps"]))
     assert _rel(uh, g["yz_uhist"]) < SOL_RTOL
     assert np.abs(its.astype(int) - g["yz_iters"].astype(int)).max() <= 1
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("method,key,nsteps", [("Predictor1_BDF", "bdf", 4), ("Predictor1_TRBDF2", "tr", 2)])
+def test_euler_bdf_trbdf2_vs_reference(gpu_lib, name, method, key, nsteps):
+    """TimeIntegration Predictor1_BDF (Predictor_Old_BDF.c: an implicit first
+    step, then BDF2) and Predictor1_TRBDF2 (Predictor_Old_TRBDF2.c: a TR and
+    a BDF2 stage per step, the build's DeltaT switching from the TR to the
+    BDF2 sub-step at the first BDF2 stage) against the reference's own loops
+    (oracle/ref_euler_harness.c): u after every stage within 1e-8, GMRES
+    iterations within 1."""
+    g = _load(name)
+    with _euler(g, method=method) as eu:
+        uh, its = eu.Predictor(g["u0"], nsteps)
+    ref = g[key + "_uhist"]
+    assert uh.shape == ref.shape
+    assert _rel(uh, ref) < SOL_RTOL, _rel(uh, ref)
+    assert np.abs(its.astype(int) - g[key + "_iters"].astype(int)).max() <= 1
