@@ -1,7 +1,9 @@
-// 2D Euler SUPG+CAU element build (03_Euler_Equations/2D/01_CommonFiles:
-// Build_M_K_F_SUPG.c:6-1072, Delta_CAU.c:4-84, Ax_Ay_calculations.c:3-98,
+// 2D Euler SUPG element build with CAU or YZBeta shock capturing
+// (03_Euler_Equations/2D/01_CommonFiles: Build_M_K_F_SUPG.c:6-1072,
+// Delta_CAU.c:4-84, Delta_YZBeta.c:6-108, Ax_Ay_calculations.c:3-98,
 // eval_U_dU.c:3-94) and the predictor-multicorrector vector updates
-// (00_CommonFiles/Time_Integration/Predictor_Old.c:57-62,115-116).
+// (00_CommonFiles/Time_Integration/Predictor_Old.c:57-62,115-116 and the
+// BDF / TR-BDF2 combinations of Predictor_Old_BDF.c, Predictor_Old_TRBDF2.c).
 //
 // One thread per element computes the 12x12 matrix Ae = Me + alpha dt Ke and
 // the 12 residual entries Re = -(Me dUe + Ke Ue) and writes Ae straight into
