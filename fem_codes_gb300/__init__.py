@@ -82,7 +82,7 @@ class EulerOpts(ctypes.Structure):
                 ("lmax", ctypes.c_int), ("tol", ctypes.c_double), ("ncorr", ctypes.c_int),
                 ("precision", ctypes.c_int), ("scheme", ctypes.c_int), ("ilu_blocks", ctypes.c_int),
                 ("scaling", ctypes.c_int), ("shock", ctypes.c_int), ("invY", ctypes.c_double * 4),
-                ("method", ctypes.c_int)]
+                ("stab", ctypes.c_int), ("method", ctypes.c_int)]
 
 
 class NSOpts(ctypes.Structure):
@@ -164,6 +164,8 @@ def load(build_if_needed: bool = True) -> ctypes.CDLL:
         "femgpu_deck_euler_opts": [_vp, _vp],
         "femgpu_deck_transient_opts": [_vp, _vp, _vp],
         "femgpu_euler_set_build_params": [_vp, ctypes.c_double, ctypes.c_double],
+        "femgpu_euler_set_bubbles": [_vp, _vp],
+        "femgpu_euler_state": [_vp, _vp, _vp],
         "femgpu_deck_ns_opts": [_vp, _vp],
         "femgpu_deck_amg": [_vp, _vp, _vp, _vp, _vp],
         "femgpu_ilu_chain_segments": [ctypes.c_int, _vp, _vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
@@ -826,11 +828,12 @@ class Euler:
     def __init__(self, x, y, vert, node_id, neq, upresc, gamma=1.4, mach=1.0, dimensionless=False,
                  alpha=0.5, dt=1e-3, stab_tol=1e-6, precond="BlockDiag", solver="GMRES", kmax=30,
                  lmax=100, tol=1e-8, ncorr=2, precision="FP64", scheme="EBE", ilu_blocks=0, scaling="NOT",
-                 shock="CAU", invY=(1.0, 1.0, 1.0, 1.0), method="Predictor1"):
+                 shock="CAU", invY=(1.0, 1.0, 1.0, 1.0), method="Predictor1", stab="SUPG"):
         L = load()
         o = EulerOpts()
         L.femgpu_euler_default_opts(ctypes.byref(o))
-        o.shock = {"CAU": 0, "YZBETA": 1}[shock.upper()]
+        o.shock = {"CAU": 0, "YZBETA": 1, "CAUDD": 2}[shock.upper()]
+        o.stab = {"SUPG": 0, "DD": 1}[stab.upper()]
         o.method = {"PREDICTOR1": 0, "PREDICTOR1_BDF": 1, "PREDICTOR1_TRBDF2": 2}[method.upper()]
         for k in range(4):
             o.invY[k] = float(invY[k])
@@ -963,6 +966,20 @@ class Euler:
         self._check(self._L.femgpu_euler_predictor(self._h, _ptr(u), int(nsteps), _ptr(uh), _ptr(its)),
                     "Predictor")
         return uh, its
+
+    def set_bubbles(self, uB=None):
+        """The DD build's element bubbles [nel, 4] for the following builds
+        (None: zero)."""
+        keep = None if uB is None else _f64(np.asarray(uB).reshape(-1))
+        self._check(self._L.femgpu_euler_set_bubbles(self._h, None if keep is None else _ptr(keep)), "set_bubbles")
+
+    def state(self):
+        """The DD build's element bubbles [nel, 4] and each element's previous
+        shock parameter delta_old [nel]."""
+        uB = np.zeros((self.nel, 4))
+        dold = np.zeros(self.nel)
+        self._check(self._L.femgpu_euler_state(self._h, _ptr(uB), _ptr(dold)), "state")
+        return uB, dold
 
     def predictor_dev(self, nsteps):
         """Predictor_Old continuing from the device state; returns the GMRES

@@ -16,6 +16,7 @@
 // element against 1.25 kB written).
 #include "fg_common.cuh"
 #include "fg_euler.h"
+#include "euler_elem.cuh"
 
 // Structure of the flux Jacobians: 0 structural zero, 1 unit entry, 2 general
 // (row 0 of Ax is e_1 and of Ay e_2; Ax[2][3] = Ay[1][3] = 0).  The
@@ -112,107 +113,20 @@ __global__ void __launch_bounds__(128) k_euler_element(int nel, const int *__res
 			gy[i] = (Ue[i] * xb[0] + Ue[i + 4] * xb[1] + Ue[i + 8] * xb[2]) / twoArea;
 		}
 		double v1 = Ub[1] / Ub[0], v2 = Ub[2] / Ub[0], E = Ub[3] / Ub[0];
-		double nU23 = (Ub[1] * Ub[1]) + (Ub[2] * Ub[2]);
 
-		// Flux Jacobians (Ax_Ay_calculations.c).
-		double Ax[4][4], Ay[4][4];
-		#pragma unroll
-		for (int i = 0; i < 4; i++)
-			#pragma unroll
-			for (int j = 0; j < 4; j++) { Ax[i][j] = 0.0; Ay[i][j] = 0.0; }
-		Ax[0][1] = 1.0;
-		Ay[0][2] = 1.0;
-		if (!cf.dimensionless) {
-			double rho = Ub[0], r2 = rho * rho;
-			Ax[1][0] = -(v1 * v1) + (((gamma - 1) * nU23 * 0.5) / r2);
-			Ax[1][1] = (3.0 - gamma) * v1;
-			Ax[1][2] = -(gamma - 1.0) * v2;
-			Ax[1][3] = gamma - 1.0;
-			Ax[2][0] = -v1 * v2;
-			Ax[2][1] = v2;
-			Ax[2][2] = v1;
-			Ax[3][0] = (-gamma * v1 * E) + ((gamma - 1.0) * v1 * (nU23 / r2));
-			Ax[3][1] = (gamma * E) - ((gamma - 1.0) * 0.5 * ((nU23 / r2) + (2.0 * v1 * v1)));
-			Ax[3][2] = -((gamma - 1.0) * v1 * v2);
-			Ax[3][3] = gamma * v1;
-			Ay[2][0] = -(v2 * v2) + (((gamma - 1.0) * nU23 * 0.5) / r2);
-			Ay[3][0] = (-gamma * v2 * E) + (((gamma - 1.0) * v2 * nU23) / r2);
-			Ay[3][2] = (gamma * E) - ((gamma - 1.0) * 0.5 * ((nU23 / r2) + (2.0 * v2 * v2)));
-		} else {
-			double nv = v1 * v1 + v2 * v2, eps2 = cf.mach * cf.mach;
-			Ax[1][0] = -(v1 * v1) + ((gamma - 1) * nv * 0.5);
-			Ax[1][1] = (3.0 - gamma) * v1;
-			Ax[1][2] = -(gamma - 1.0) * v2;
-			Ax[1][3] = (gamma - 1.0) / eps2;
-			Ax[2][0] = -v1 * v2;
-			Ax[2][1] = v2;
-			Ax[2][2] = v1;
-			Ax[3][0] = -v1 * (gamma * E - ((gamma - 1.0) * eps2 * nv));
-			Ax[3][1] = gamma * E - (gamma - 1.0) * eps2 * (0.5 * nv + v1 * v1);
-			Ax[3][2] = -(gamma - 1.0) * eps2 * v1 * v2;
-			Ax[3][3] = gamma * v1;
-			Ay[2][0] = -(v2 * v2) + (((gamma - 1.0) * nv * 0.5));
-			Ay[3][0] = -v2 * (gamma * E - (gamma - 1.0) * eps2 * nv);
-			Ay[3][2] = gamma * E - (gamma - 1.0) * eps2 * (0.5 * nv + v2 * v2);
-		}
-		Ay[1][0] = Ax[2][0];
-		Ay[1][1] = v2;
-		Ay[1][2] = v1;
-		Ay[2][1] = -(gamma - 1.0) * v1;
-		Ay[2][2] = (3.0 - gamma) * v2;
-		Ay[2][3] = Ax[1][3];
-		Ay[3][1] = Ax[3][2];
-		Ay[3][3] = gamma * v2;
-
-		// A0^-1 in entropy variables (:131-159).
-		double A0[4][4];
-		{
-			double rho_i = Ub[3] - ((nU23 * 0.5) / Ub[0]);
-			double V2 = Ub[1] / rho_i, V3 = Ub[2] / rho_i, V4 = (-Ub[0]) / rho_i;
-			double re = -1.0 / (rho_i * V4), k1 = (V2 * V2 + V3 * V3) * 0.5 / V4;
-			A0[0][0] = re * (k1 * k1 + gamma);
-			A0[0][1] = re * (k1 * V2);
-			A0[0][2] = re * (k1 * V3);
-			A0[0][3] = re * ((k1 + 1.0) * V4);
-			A0[1][1] = re * (V2 * V2 - V4);
-			A0[1][2] = re * (V2 * V3);
-			A0[1][3] = re * (V2 * V4);
-			A0[2][2] = re * (V3 * V3 - V4);
-			A0[2][3] = re * (V3 * V4);
-			A0[3][3] = re * V4 * V4;
-			A0[1][0] = A0[0][1]; A0[2][0] = A0[0][2]; A0[3][0] = A0[0][3];
-			A0[2][1] = A0[1][2]; A0[3][1] = A0[1][3]; A0[3][2] = A0[2][3];
-		}
+		// Flux Jacobians (Ax_Ay_calculations.c) and A0^-1 in entropy
+		// variables (:131-159).
+		double Ax[4][4], Ay[4][4], A0[4][4];
+		euler_jacobians(Ub, gamma, cf.mach, cf.dimensionless, Ax, Ay);
+		euler_a0(Ub, gamma, A0);
 
 		// Shock-capturing delta: Delta_YZBeta.c:6-108 (stateful: blended with
 		// the element's previous delta, which it replaces) or Delta_CAU.c:17-82.
 		double delta;
 		if (cf.yzbeta) {
 			double Z[4];
-			#pragma unroll
-			for (int i = 0; i < 4; i++) Z[i] = dUb[i] + jvec<true>(Ax, gx, i) + jvec<false>(Ay, gy, i);
-			const double *iY = cf.invY;
-			double nYZ = sqrt(iY[0] * Z[0] * iY[0] * Z[0] + iY[1] * Z[1] * iY[1] * Z[1] +
-			                  iY[2] * Z[2] * iY[2] * Z[2] + iY[3] * Z[3] * iY[3] * Z[3]);
-			double nYx = iY[0] * gx[0] * iY[0] * gx[0] + iY[1] * gx[1] * iY[1] * gx[1] +
-			             iY[2] * gx[2] * iY[2] * gx[2] + iY[3] * gx[3] * iY[3] * gx[3];
-			double nYy = iY[0] * gy[0] * iY[0] * gy[0] + iY[1] * gy[1] * iY[1] * gy[1] +
-			             iY[2] * gy[2] * iY[2] * gy[2] + iY[3] * gy[3] * iY[3] * gy[3];
-			double sYdU = nYx + nYy;
-			double nYU = sqrt(iY[0] * Ub[0] * iY[0] * Ub[0] + iY[1] * Ub[1] * iY[1] * Ub[1] +
-			                  iY[2] * Ub[2] * iY[2] * Ub[2] + iY[3] * Ub[3] * iY[3] * Ub[3]);
-			double nrho = sqrt(gx[0] * gx[0] + gy[0] * gy[0]), J1 = 0.0, J2 = 0.0;
-			if (fabs(nrho) >= 1e-12) { J1 = gx[0] / nrho; J2 = gy[0] / nrho; }
-			double H = (fabs(J1 * yb[0] + J2 * xb[0]) + fabs(J1 * yb[1] + J2 * xb[1]) +
-			            fabs(J1 * yb[2] + J2 * xb[2])) / twoArea;
-			H = fabs(H) >= 1e-12 ? 2.0 * (1.0 / H) : 0.0;
-			const bool sok = fabs(sYdU) >= 1e-12, uok = fabs(nYU) >= 1e-12;
-			double d1 = nYZ * (sok ? 1.0 / sqrt(sYdU) : 0.0) * (uok ? 1.0 : 0.0) * (H * 0.5);
-			double d2 = nYZ * (sok ? 1.0 : 0.0) * (uok ? 1.0 / nYU : 0.0) * (H * 0.5 * H * 0.5);
-			const double w = 0.5;
-			double ad = w * (d1 + d2);
-			delta = w * (ad) + (1 - w) * dold[e];
-			dold[e] = delta;
+			euler_residual4(Ax, Ay, gx, gy, dUb, Z);
+			delta = euler_delta_yzbeta(Z, gx, gy, Ub, cf.invY, yb, xb, twoArea, &dold[e]);
 		} else {
 			double kx[4], ky[4], L[4];
 			#pragma unroll
@@ -401,6 +315,34 @@ __global__ void k_euler_rotate(int nslip, const int *__restrict__ slip_el, const
 	}
 }
 
+// Build_M_K_F_DD_Transiente.c:37-911 (StabilizationForm "DD"): one thread
+// per element through euler_dd_element; the element's bubble uB [4] and
+// delta_old advance in place.
+__global__ void __launch_bounds__(128) k_euler_element_dd(int nel, const int *__restrict__ vert,
+		const int *__restrict__ node_id, const double *__restrict__ xn, const double *__restrict__ yn,
+		const double *__restrict__ upresc, const double *__restrict__ u, const double *__restrict__ du,
+		EulerCoef cf, double *__restrict__ A, double *__restrict__ Re, double *__restrict__ dold,
+		double *__restrict__ uB)
+{
+	for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nel; e += gridDim.x * blockDim.x) {
+		double X[3], Y[3], Ue[12], dUe[12];
+		#pragma unroll
+		for (int a = 0; a < 3; a++) {
+			int J = __ldg(&vert[3 * e + a]);
+			X[a] = __ldg(&xn[J]);
+			Y[a] = __ldg(&yn[J]);
+			#pragma unroll
+			for (int k = 0; k < 4; k++) {                          // eval_U_dU.c:22-91
+				int id = __ldg(&node_id[4 * J + k]);
+				Ue[4 * a + k] = id >= 0 ? __ldg(&u[id]) : __ldg(&upresc[4 * J + k]);
+				dUe[4 * a + k] = id >= 0 ? __ldg(&du[id]) : 0.0;
+			}
+		}
+		euler_dd_element(X, Y, Ue, dUe, cf.gamma, cf.mach, cf.dimensionless, cf.alpha, cf.dt, cf.stab_tol,
+		                 cf.yzbeta, cf.invY, &dold[e], uB + 4LL * e, A + 144LL * e, Re + 12LL * e);
+	}
+}
+
 extern "C" int fg_euler_build(femgpu_euler *c, const double *u, const double *du)
 {
 	EulerCoef cf;
@@ -410,10 +352,14 @@ extern "C" int fg_euler_build(femgpu_euler *c, const double *u, const double *du
 	for (int k = 0; k < 4; k++) cf.invY[k] = c->o.invY[k];
 	femgpu_ebe *b = c->ebe;
 	int g = (int)((c->nel + 127LL) / 128);
-	k_euler_element<<<g, 128, 0, c->stream>>>(c->nel, b->vert, b->node_id, c->x, c->y, c->upresc, u, du, cf,
-	                                          b->A, c->Re, c->dold);
+	if (c->o.stab == FEMGPU_STAB_DD)
+		k_euler_element_dd<<<g, 128, 0, c->stream>>>(c->nel, b->vert, b->node_id, c->x, c->y, c->upresc, u, du,
+		                                             cf, b->A, c->Re, c->dold, c->uB);
+	else
+		k_euler_element<<<g, 128, 0, c->stream>>>(c->nel, b->vert, b->node_id, c->x, c->y, c->upresc, u, du,
+		                                          cf, b->A, c->Re, c->dold);
 	FG_TRY(cudaGetLastError());
-	if (c->nslip_el > 0) {
+	if (c->nslip_el > 0 && c->o.stab != FEMGPU_STAB_DD) {
 		k_euler_rotate<<<fg_grid(c->nslip_el), FG_TPB, 0, c->stream>>>(c->nslip_el, c->slip_el, b->vert,
 		                                                              c->slip_flag, c->slip_cs, c->slip_sn,
 		                                                              b->A, c->Re);

@@ -29,7 +29,8 @@ struct femgpu_euler {
 	 * its wall angle, and the elements with a slip vertex */
 	int *slip_flag, *slip_el, nslip_el;
 	double *slip_cs, *slip_sn;
-	double *dold;                  /* YZBeta: each element's previous delta      */
+	double *dold;                  /* YZBeta, DD: each element's previous delta  */
+	double *uB;                    /* DD: the element bubbles (4 per element)    */
 	double alpha_build, dt_build;  /* the builds' Alpha_Build, DeltaT_Build      */
 	double *u1, *u2, *uold;        /* BDF / TR-BDF2 history (neq+1 each)         */
 	cudaEvent_t ev[4];

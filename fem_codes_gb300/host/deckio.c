@@ -381,10 +381,14 @@ int femgpu_deck_euler_opts(const femgpu_deck *d, femgpu_euler_opts *o)
 		o->scheme = FEMGPU_CSR;
 	else return FEMGPU_E_ARG;
 	if (block_precond(d->Preconditioner, o->scheme == FEMGPU_CSR, &o->precond)) return FEMGPU_E_ARG;
-	/* setStabilizationForm.c:6-32: SUPG with CAU or YZBeta (Y^-1 from the deck) */
-	if (strcasecmp(d->StabilizationForm, "SUPG") != 0) return FEMGPU_E_ARG;
+	/* setStabilizationForm.c:6-75: SUPG with CAU or YZBeta, DD (with the
+	 * Predictor1 loops: Build_M_K_F_DD_Transiente) with CAUDD or YZBeta;
+	 * Y^-1 from the deck */
+	if (!strcasecmp(d->StabilizationForm, "DD")) o->stab = FEMGPU_STAB_DD;
+	else if (strcasecmp(d->StabilizationForm, "SUPG") != 0) return FEMGPU_E_ARG;
 	if (!strcasecmp(d->ShockCapture, "YZBeta")) o->shock = FEMGPU_SHOCK_YZBETA;
-	else if (strcasecmp(d->ShockCapture, "CAU") != 0) return FEMGPU_E_ARG;
+	else if (o->stab == FEMGPU_STAB_DD && !strcasecmp(d->ShockCapture, "CAUDD")) o->shock = FEMGPU_SHOCK_CAUDD;
+	else if (o->stab != FEMGPU_STAB_SUPG || strcasecmp(d->ShockCapture, "CAU") != 0) return FEMGPU_E_ARG;
 	o->invY[0] = d->invY[0]; o->invY[1] = d->invY[1]; o->invY[2] = d->invY[2]; o->invY[3] = d->invY[3];
 	/* setStabilizationForm.c:9-21: Predictor1, Predictor1_BDF, Predictor1_TRBDF2 */
 	if (!strcasecmp(d->TimeIntegration, "Predictor1_BDF")) o->method = FEMGPU_TI_BDF;

@@ -131,6 +131,8 @@ static int create(femgpu_euler *c, const femgpu_euler_opts *o, int nnodes, const
 	DM(c->Da, sizeof(double) * n1);
 	DM(c->Re, sizeof(double) * 12 * (size_t)nel);
 	DM(c->dold, sizeof(double) * (size_t)nel);
+	DM(c->uB, sizeof(double) * 4 * (size_t)nel);
+	CK(cudaMemsetAsync(c->uB, 0, sizeof(double) * 4 * (size_t)nel, c->stream));
 	c->alpha_build = o->alpha;
 	c->dt_build = o->dt;
 	CK(cudaMemsetAsync(c->dold, 0, sizeof(double) * (size_t)nel, c->stream));
@@ -170,7 +172,9 @@ int femgpu_euler_create(femgpu_euler **out, const femgpu_euler_opts *opts, int n
 	    (o.precision != FEMGPU_FP64 && o.precision != FEMGPU_MIXED_IR) ||
 	    (o.precision == FEMGPU_MIXED_IR && o.solver != FEMGPU_FGMRES) ||
 	    (o.scaling != 0 && (o.scaling != 1 || o.scheme != FEMGPU_EBE)) ||
-	    (o.shock != FEMGPU_SHOCK_CAU && o.shock != FEMGPU_SHOCK_YZBETA) ||
+	    (o.stab != FEMGPU_STAB_SUPG && o.stab != FEMGPU_STAB_DD) ||
+	    (o.stab == FEMGPU_STAB_SUPG && o.shock != FEMGPU_SHOCK_CAU && o.shock != FEMGPU_SHOCK_YZBETA) ||
+	    (o.stab == FEMGPU_STAB_DD && o.shock != FEMGPU_SHOCK_CAUDD && o.shock != FEMGPU_SHOCK_YZBETA) ||
 	    (o.method != FEMGPU_TI_PREDICTOR1 && o.method != FEMGPU_TI_BDF && o.method != FEMGPU_TI_TRBDF2)) {
 		fgh_set_error("femgpu_euler_create: bad argument or option");
 		return FEMGPU_E_ARG;
@@ -192,7 +196,7 @@ void femgpu_euler_destroy(femgpu_euler *c)
 	if (c->ebe) femgpu_ebe_destroy(c->ebe);
 	{
 		void *p[] = { c->x, c->y, c->upresc, c->u, c->a, c->R, c->Da, c->Re, c->slip_flag, c->slip_el, c->slip_cs,
-		              c->slip_sn, c->dold, c->u1, c->u2, c->uold };
+		              c->slip_sn, c->dold, c->uB, c->u1, c->u2, c->uold };
 		for (i = 0; i < (int)(sizeof p / sizeof p[0]); i++) if (p[i]) cudaFree(p[i]);
 	}
 	fgh_kry_free(&c->kry);
@@ -528,6 +532,26 @@ int femgpu_euler_set_build_params(femgpu_euler *c, double alpha_build, double dt
 	return 0;
 }
 
+int femgpu_euler_set_bubbles(femgpu_euler *c, const double *uB)
+{
+	const size_t nb = sizeof(double) * 4 * (size_t)(c ? c->nel : 0);
+	if (!c) return FEMGPU_E_ARG;
+	if (uB) CK(cudaMemcpyAsync(c->uB, uB, nb, cudaMemcpyHostToDevice, c->stream));
+	else CK(cudaMemsetAsync(c->uB, 0, nb, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	return 0;
+}
+
+int femgpu_euler_state(femgpu_euler *c, double *uB, double *delta_old)
+{
+	if (!c) return FEMGPU_E_ARG;
+	if (uB) CK(cudaMemcpyAsync(uB, c->uB, sizeof(double) * 4 * (size_t)c->nel, cudaMemcpyDeviceToHost, c->stream));
+	if (delta_old)
+		CK(cudaMemcpyAsync(delta_old, c->dold, sizeof(double) * (size_t)c->nel, cudaMemcpyDeviceToHost, c->stream));
+	CK(cudaStreamSynchronize(c->stream));
+	return 0;
+}
+
 int femgpu_euler_predictor_dev(femgpu_euler *c, int nsteps, int *iters)
 {
 	if (!c || nsteps < 0) return FEMGPU_E_ARG;
@@ -543,6 +567,7 @@ int femgpu_euler_predictor(femgpu_euler *c, double *u, int nsteps, double *uhist
 	if (u) CK(cudaMemcpyAsync(c->u, u, sizeof(double) * n1, cudaMemcpyHostToDevice, c->stream));
 	CK(cudaMemsetAsync(c->a, 0, sizeof(double) * n1, c->stream));          /* a = 0 (mycalloc, :18) */
 	CK(cudaMemsetAsync(c->dold, 0, sizeof(double) * (size_t)c->nel, c->stream));   /* delta_old = 0 (:23) */
+	CK(cudaMemsetAsync(c->uB, 0, sizeof(double) * 4 * (size_t)c->nel, c->stream));  /* uB_old = 0 (:22)   */
 	rc = predictor(c, nsteps, uhist, iters);
 	if (rc) return rc;
 	if (u) CK(cudaMemcpyAsync(u, c->u, sizeof(double) * n1, cudaMemcpyDeviceToHost, c->stream));

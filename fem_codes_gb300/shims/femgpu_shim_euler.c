@@ -85,11 +85,13 @@ static int eu_of(ParametersType *P, FemStructsType *FS, FemFunctionsType *FF)
 	double *x, *y, *up;
 	int *nid, *vert;
 	if (g_eu) return 0;
-	if (strcasecmp(P->StabilizationForm, "SUPG") != 0 ||
-	    (strcasecmp(P->ShockCapture, "CAU") != 0 && strcasecmp(P->ShockCapture, "YZBeta") != 0))
-		return FEMGPU_E_ARG;
 	femgpu_euler_default_opts(&o);
+	/* setStabilizationForm.c:6-75: SUPG (CAU, YZBeta) or DD (CAUDD, YZBeta) */
+	if (!strcasecmp(P->StabilizationForm, "DD")) o.stab = FEMGPU_STAB_DD;
+	else if (strcasecmp(P->StabilizationForm, "SUPG") != 0) return FEMGPU_E_ARG;
 	if (!strcasecmp(P->ShockCapture, "YZBeta")) o.shock = FEMGPU_SHOCK_YZBETA;
+	else if (o.stab == FEMGPU_STAB_DD && !strcasecmp(P->ShockCapture, "CAUDD")) o.shock = FEMGPU_SHOCK_CAUDD;
+	else if (o.stab != FEMGPU_STAB_SUPG || strcasecmp(P->ShockCapture, "CAU") != 0) return FEMGPU_E_ARG;
 	for (k = 0; k < 4; k++) o.invY[k] = P->invY[k];
 	if (!strcasecmp(P->MatrixVectorProductScheme, "EBE")) o.scheme = FEMGPU_EBE;
 	else if (!strcasecmp(P->MatrixVectorProductScheme, "CSR") && !strcasecmp(P->reordering, "NOT"))

@@ -392,6 +392,12 @@ typedef struct femgpu_euler_opts {
 	                     /* which starts at 0 when the context is made and    */
 	                     /* at every femgpu_euler_predictor call)             */
 	double invY[4];      /* the deck's Y^-1 (YZBeta)                          */
+	int stab;            /* StabilizationForm: FEMGPU_STAB_SUPG              */
+	                     /* (Build_M_K_F_SUPG.c; shock CAU or YZBETA) or      */
+	                     /* FEMGPU_STAB_DD (Build_M_K_F_DD_Transiente.c: the  */
+	                     /* element bubbles condensed out, updated by every   */
+	                     /* build; shock CAUDD (Delta_DD.c) or YZBETA; no     */
+	                     /* slip-wall rotation, as the reference's)           */
 	int method;          /* TimeIntegration: FEMGPU_TI_PREDICTOR1            */
 	                     /* (Predictor_Old.c), FEMGPU_TI_BDF                  */
 	                     /* (Predictor_Old_BDF.c: an implicit first step,     */
@@ -461,6 +467,10 @@ int femgpu_euler_predictor(femgpu_euler *ctx, double *u, int nsteps, double *uhi
  * changes DeltaT_Build between its stages), for a driver that keeps its own
  * time loop; femgpu_euler_predictor sets them itself. */
 int femgpu_euler_set_build_params(femgpu_euler *ctx, double alpha_build, double dt_build);
+/* DD state: the element bubbles uB [4*nel] for the following builds (NULL:
+ * zero), and the current bubbles and delta_old [nel] (either may be NULL). */
+int femgpu_euler_set_bubbles(femgpu_euler *ctx, const double *uB);
+int femgpu_euler_state(femgpu_euler *ctx, double *uB, double *delta_old);
 int femgpu_euler_predictor_dev(femgpu_euler *ctx, int nsteps, int *iters);
 /* Device pointers of the state vectors u, a, R, Da [neq+1] and the block
  * EBE operator holding the element matrices. */

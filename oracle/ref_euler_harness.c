@@ -30,8 +30,12 @@ double Delta_YZBeta(double, double *, double *, double *, double (*)[4], double 
 
 /* Shock capturing of the builds below: 0 Delta_CAU, 1 Delta_YZBeta with the
  * deck's Y^-1 (the ShockCapture "YZBeta" of setStabilizationForm.c:27). */
-static int g_yz;
+static int g_yz, g_dd;
 static double g_invY[4];
+/* The element build of the predictor below: 0 Build_M_K_F_SUPG, 1 the DD
+ * build Build_M_K_F_DD_Transiente (StabilizationForm "DD"; shock capturing
+ * Delta_DD, or Delta_YZBeta after ref_euler_set_shock(1, ...)). */
+void ref_euler_set_dd(int dd) { g_dd = dd; }
 void ref_euler_set_shock(int yzbeta, const double *invY)
 {
 	int k;
@@ -39,6 +43,9 @@ void ref_euler_set_shock(int yzbeta, const double *invY)
 	for (k = 0; k < 4; k++) g_invY[k] = invY ? invY[k] : 1.0;
 }
 void dimensional_Ax_Ay_calculations(double, double, double *, double (*)[4], double (*)[4]);
+int Build_M_K_F_DD_Transiente(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *);
+double Delta_DD(double, double *, double *, double *, double (*)[4], double (*)[4], double (*)[4],
+                double *, double, double, double, double, double, double, double, int, double *, double *);
 double REFLETIDO_gamma(double, double);
 double REFLETIDO_rhopresc(double, double);
 double REFLETIDO_v1presc(double, double);
@@ -97,11 +104,12 @@ static void setup(int csr, int nnodes, const double *x, const double *y, const i
 	FS->u = mycalloc("u", neq + 1, sizeof(double));
 	FS->du = mycalloc("du", neq + 1, sizeof(double));
 	FS->delta_old = mycalloc("delta_old", nel, sizeof(double));
+	FS->uB = mycalloc("uB", 4 * nel, sizeof(double));
 	FF->gamma = REFLETIDO_gamma;
 	FF->rhopresc = REFLETIDO_rhopresc; FF->v1presc = REFLETIDO_v1presc;
 	FF->v2presc = REFLETIDO_v2presc; FF->epresc = REFLETIDO_epresc;
 	FF->Ax_Ay_calculations = dimensional_Ax_Ay_calculations;
-	FF->ShockCapture = g_yz ? Delta_YZBeta : Delta_CAU;
+	FF->ShockCapture = g_yz ? Delta_YZBeta : g_dd ? Delta_DD : Delta_CAU;
 	for (k = 0; k < 4; k++) P->invY[k] = g_invY[k];
 	FF->BC_theta = zero_theta;
 	FF->assembly = csr ? csr_assembly : ebe_assembly;
@@ -216,7 +224,8 @@ static int predictor(int csr, int scaling, int nnodes, const double *x, const do
 		for (I = 0; I < neq; I++) { u[I] += (1.0 - alpha)*dt*a[I]; a[I] = 0.0; }
 		for (i = 0; i < ncorr; i++) {
 			int before = P->iterations;
-			Build_M_K_F_SUPG(P, M, FS, FF);
+			if (g_dd) Build_M_K_F_DD_Transiente(P, M, FS, FF);
+			else Build_M_K_F_SUPG(P, M, FS, FF);
 			if (scaling) Block_scaling_EBE(P, M, FS);       /* Predictor_Old.c:73 */
 			FF->precond_setup(P, M, FS, tag++, R);
 			gmres6(P, M, FS, FF, R, Da);
@@ -357,4 +366,31 @@ int ref_euler_predictor_tint(int trbdf2, int nnodes, const double *x, const doub
 	if (trbdf2) Predictor_Old_TRBDF2(P, M, FS, FF, FOF);
 	else Predictor_Old_BDF(P, M, FS, FF, FOF);
 	return g_stage;
+}
+
+/* Two consecutive DD builds (Build_M_K_F_DD_Transiente.c:6-915, the
+ * StabilizationForm "DD" of setStabilizationForm.c:33-46) on (u, du) from a
+ * zero delta_old and the element bubbles uB0 [4*nel]: shock capturing Delta_DD
+ * ("CAUDD"), or Delta_YZBeta after ref_euler_set_shock(1, ...).  Ae1, R1,
+ * Ae2, R2 as ref_euler_build2; uB [4*nel] and delta_old [nel] after the
+ * second build. */
+int ref_euler_build_dd(int nnodes, const double *x, const double *y, const int *node_id, int nel, const int *vert,
+                       int neq, double alpha, double dt, double stab_tol, const double *u, const double *du,
+                       const double *uB0, double *Ae1, double *R1, double *Ae2, double *R2, double *uB, double *dold)
+{
+	ParametersType *P; MatrixDataType *M; FemStructsType *FS; FemFunctionsType *FF;
+	setup(0, nnodes, x, y, node_id, nel, vert, neq, alpha, dt, stab_tol, &P, &M, &FS, &FF);
+	if (!g_yz) FF->ShockCapture = Delta_DD;
+	memcpy(FS->uB, uB0, sizeof(double) * 4 * nel);
+	memcpy(FS->u, u, sizeof(double) * (neq + 1));
+	memcpy(FS->du, du, sizeof(double) * (neq + 1));
+	Build_M_K_F_DD_Transiente(P, M, FS, FF);
+	memcpy(Ae1, M->Aaux, sizeof(double) * nel * 144);
+	memcpy(R1, FS->F, sizeof(double) * (neq + 1));
+	Build_M_K_F_DD_Transiente(P, M, FS, FF);
+	memcpy(Ae2, M->Aaux, sizeof(double) * nel * 144);
+	memcpy(R2, FS->F, sizeof(double) * (neq + 1));
+	memcpy(uB, FS->uB, sizeof(double) * 4 * nel);
+	memcpy(dold, FS->delta_old, sizeof(double) * nel);
+	return 0;
 }

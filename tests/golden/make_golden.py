@@ -240,6 +240,9 @@ def main_euler():
                                          ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp,
                                          _dp, _dp]
     lib.ref_euler_set_shock.argtypes = [ctypes.c_int, _dp]
+    lib.ref_euler_set_dd.argtypes = [ctypes.c_int]
+    lib.ref_euler_build_dd.argtypes = [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
     lib.ref_euler_predictor_tint.restype = ctypes.c_int
     lib.ref_euler_predictor_tint.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, _ip,
                                              ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -334,9 +337,36 @@ def main_euler():
                                               dt, stol, kmax, lmax, tol, checks, ncorr, pb.u0, cap, uht, itt)
             tint[key + "_uhist"] = uht[:st * (neq + 1)].reshape(st, neq + 1)
             tint[key + "_iters"] = itt[:st * ncorr].reshape(st, ncorr)
+        # StabilizationForm "DD" (Build_M_K_F_DD_Transiente): two consecutive builds from seeded element
+        # bubbles and a zero delta_old, with Delta_DD ("dd") and with Delta_YZBeta ("ddyz"), and the
+        # Predictor_Old run with the DD build and Delta_DD
+        dd = {}
+        uB0 = rng.uniform(0.5, 1.5, 4 * mesh.nel)
+        for key, yz in (("dd", 0), ("ddyz", 1)):
+            lib.ref_euler_set_shock(yz, YZ_INVY if yz else np.ones(4))
+            outs = [np.zeros(mesh.nel * 144), np.zeros(neq + 1), np.zeros(mesh.nel * 144), np.zeros(neq + 1),
+                    np.zeros(4 * mesh.nel), np.zeros(mesh.nel)]
+            lib.ref_euler_build_dd(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol, u, du,
+                                   uB0, *outs)
+            for k, v in zip(("Ae1", "R1", "Ae2", "R2", "uB", "dold"), outs):
+                dd[f"{key}_{k}"] = v.reshape(mesh.nel, 144) if k.startswith("Ae") else v
+        lib.ref_euler_set_shock(0, np.ones(4))
+        dd["dd_uB0"] = uB0
+        # (at CFL 1: at the cases' CFL of 2-5 the DD system's GMRES stagnates in the reference too)
+        dd_dt = euler_cfl_dt(mesh, 1.0)
+        lib.ref_euler_set_dd(1)
+        upd = pb.u0.copy()
+        uhd = np.zeros(nsteps * (neq + 1))
+        its_d = np.zeros(nsteps * ncorr, np.int32)
+        lib.ref_euler_predictor(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dd_dt, stol,
+                                kmax, lmax, tol, nsteps, ncorr, upd, uhd, its_d)
+        lib.ref_euler_set_dd(0)
+        dd["dd_dt"] = dd_dt
+        dd["dd_uhist"] = uhd.reshape(nsteps, neq + 1)
+        dd["dd_iters"] = its_d.reshape(nsteps, ncorr)
         np.savez_compressed(
             os.path.join(HERE, f"{name}.npz"), x=mesh.x, y=mesh.y, vert=mesh.vert, node_id=pb.node_id,
-            amg_spec=np.array(AMG_SYS_SPEC), amg_Fp=amg_Fp,
+            amg_spec=np.array(AMG_SYS_SPEC), amg_Fp=amg_Fp, **dd,
             bs_Ae=Ae_b.reshape(mesh.nel, 144), bs_R=R_b, bs_uhist=uhs.reshape(nsteps, neq + 1),
             bs_iters=its_s.reshape(nsteps, ncorr),
             yz_invY=YZ_INVY, yz_Ae1=Ae_y1.reshape(mesh.nel, 144), yz_R1=R_y1, yz_Ae2=Ae_y2.reshape(mesh.nel, 144),
