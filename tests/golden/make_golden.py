@@ -352,16 +352,13 @@ def main_euler():
                 dd[f"{key}_{k}"] = v.reshape(mesh.nel, 144) if k.startswith("Ae") else v
         lib.ref_euler_set_shock(0, np.ones(4))
         dd["dd_uB0"] = uB0
-        # (at CFL 1: at the cases' CFL of 2-5 the DD system's GMRES stagnates in the reference too)
-        dd_dt = euler_cfl_dt(mesh, 1.0)
         lib.ref_euler_set_dd(1)
         upd = pb.u0.copy()
         uhd = np.zeros(nsteps * (neq + 1))
         its_d = np.zeros(nsteps * ncorr, np.int32)
-        lib.ref_euler_predictor(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dd_dt, stol,
+        lib.ref_euler_predictor(mesh.nnodes, mesh.x, mesh.y, nid, mesh.nel, vert, neq, alpha, dt, stol,
                                 kmax, lmax, tol, nsteps, ncorr, upd, uhd, its_d)
         lib.ref_euler_set_dd(0)
-        dd["dd_dt"] = dd_dt
         dd["dd_uhist"] = uhd.reshape(nsteps, neq + 1)
         dd["dd_iters"] = its_d.reshape(nsteps, ncorr)
         np.savez_compressed(

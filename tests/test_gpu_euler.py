@@ -312,15 +312,6 @@ def test_euler_bdf_trbdf2_vs_reference(gpu_lib, name, method, key, nsteps):
     assert np.abs(its.astype(int) - g[key + "_iters"].astype(int)).max() <= 1
 
 
-def _ae_match(ours, ref):
-    """Element matrices equal, except at the entries where the reference
-    reads an uninitialised value: the dimensional Ax_Ay_calculations of the
-    DD build (Build_M_K_F_DD_Transiente.c) assigns Ay[0][0] twice and never
-    Ay[0][3], so those entries hold run-dependent denormals (|v| < 1e-290)
-    in the reference and the structural 0 contribution here."""
-    garbage = np.abs(ref) < 1e-290
-    return np.array_equal(ours[~garbage], ref[~garbage]) and np.abs(ours[garbage]).max(initial=0) < 1e-290
-
 
 @pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("shock,key", [("CAUDD", "dd"), ("YZBeta", "ddyz")])
@@ -330,8 +321,10 @@ def test_euler_dd_build_vs_reference(gpu_lib, name, shock, key):
     element bubble updated in the build) with Delta_DD (CAUDD) or
     Delta_YZBeta: two consecutive Builds from the same seeded bubbles and a
     zero delta_old as the reference's own; R, the bubbles and delta_old
-    bit-identical, Ae bit-identical outside the reference's uninitialised
-    Ay[0][3] entries."""
+    and Ae bit-identical.  (The reference's Ax_Ay_calculations never sets
+    Ay[0][3], which this build reads; the reference library is compiled
+    with zero-filled locals, so it reads the Jacobian's structural 0 there,
+    as the device build does.)"""
     g = _load(name)
     invY = g["yz_invY"] if shock == "YZBeta" else (1.0, 1.0, 1.0, 1.0)
     with _euler(g, stab="DD", shock=shock, invY=invY) as eu:
@@ -340,7 +333,7 @@ def test_euler_dd_build_vs_reference(gpu_lib, name, shock, key):
         R2, Ae2 = eu.Build(g["u"], g["du"], want_matrix=True)
         uB, dold = eu.state()
     assert np.array_equal(R1, g[key + "_R1"]) and np.array_equal(R2, g[key + "_R2"])
-    assert _ae_match(Ae1, g[key + "_Ae1"]) and _ae_match(Ae2, g[key + "_Ae2"])
+    assert np.array_equal(Ae1, g[key + "_Ae1"]) and np.array_equal(Ae2, g[key + "_Ae2"])
     assert np.array_equal(uB.reshape(-1), g[key + "_uB"])
     assert np.array_equal(dold, g[key + "_dold"])
 
@@ -348,10 +341,10 @@ def test_euler_dd_build_vs_reference(gpu_lib, name, shock, key):
 @pytest.mark.parametrize("name", CASES)
 def test_euler_dd_predictor_vs_reference(gpu_lib, name):
     """Predictor_Old with the DD build and Delta_DD (bubbles and delta_old
-    zero at the start) at a CFL-1 time step against the reference's own
-    run: u after every step within 1e-8, GMRES iterations within 1."""
+    zero at the start) against the reference's own run: u after every step
+    within 1e-8, GMRES iterations within 1."""
     g = _load(name)
-    with _euler(g, stab="DD", shock="CAUDD", dt=float(g["dd_dt"])) as eu:
+    with _euler(g, stab="DD", shock="CAUDD") as eu:
         uh, its = eu.Predictor(g["u0"], int(g["nsteps"]))
     assert _rel(uh, g["dd_uhist"]) < SOL_RTOL, _rel(uh, g["dd_uhist"])
     assert np.abs(its.astype(int) - g["dd_iters"].astype(int)).max() <= 1
