@@ -272,6 +272,101 @@ __global__ void __launch_bounds__(UPD_TPB) k_gnn_update(int n, const float *__re
 	}
 }
 
+// The same update for bf16 activations on the tensor cores (mma.sync
+// m16n8k16, bf16 operands, FP32 accumulation).  Each FP32 weight is split
+// into bf16 parts w = hi + lo (|w - hi - lo| <= 2^-16 |w|) and both parts
+// are multiplied, so the product keeps the FP32 weights; the activations are
+// bf16 already.  A 128-node tile is staged as bf16 rows of MPAD in shared
+// memory (16-byte loads, no conversion); warp w of 8 takes nodes 16w..16w+15
+// and all 32 outputs (4 fragments of 8 columns) over K = 96 in 6 steps.  The
+// row stride of 104 elements (52 words) puts the 8 rows a fragment load
+// touches in 8 distinct groups of 4 banks.
+#define MPAD (3 * W + 8)
+#define MMA_SMEM ((2 * W * MPAD + UTILE * MPAD) * (int)sizeof(__nv_bfloat16) + W * (int)sizeof(float))
+__device__ __forceinline__ unsigned ld_pair(const __nv_bfloat16 *p)
+{
+	return *reinterpret_cast<const unsigned *>(p);
+}
+__device__ __forceinline__ void mma_bf16(float (&d)[4], unsigned a0, unsigned a1, unsigned a2, unsigned a3,
+                                         unsigned b0, unsigned b1)
+{
+	asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+	             "{%0,%1,%2,%3};"
+	             : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+	             : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+__global__ void __launch_bounds__(UPD_TPB) k_gnn_update_mma(int n, const float *__restrict__ th,
+		const __nv_bfloat16 *h, const __nv_bfloat16 *m1, const __nv_bfloat16 *m2, __nv_bfloat16 *hout,
+		unsigned *mask, const int *active)
+{
+	if (active && !*active) return;
+	extern __shared__ __align__(16) unsigned char dynb[];
+	__nv_bfloat16 *sWh = reinterpret_cast<__nv_bfloat16 *>(dynb);   // [W][MPAD]: W^T, row = output
+	__nv_bfloat16 *sWl = sWh + W * MPAD;
+	__nv_bfloat16 *sA = sWl + W * MPAD;                              // [UTILE][MPAD]: [h, m1, m2]
+	float *sB = reinterpret_cast<float *>(sA + UTILE * MPAD);       // bias [W]
+	for (int e = threadIdx.x; e < 3 * W * W; e += blockDim.x) {
+		int k = e / W, o = e - k * W;
+		float w = th[e];
+		__nv_bfloat16 hi = __float2bfloat16_rn(w);
+		sWh[o * MPAD + k] = hi;
+		sWl[o * MPAD + k] = __float2bfloat16_rn(w - __bfloat162float(hi));
+	}
+	if (threadIdx.x < W) sB[threadIdx.x] = th[3 * W * W + threadIdx.x];
+	const int t = threadIdx.x, lane = t & 31, warp = t >> 5, g = lane >> 2, c = (lane & 3) * 2;
+	int ntile = (n + UTILE - 1) / UTILE;
+	for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+		int base = tile * UTILE;
+		__syncthreads();
+		for (int e = t; e < UTILE * 12; e += blockDim.x) {          // 3 sources x 4 16-byte parts per node
+			int nd = e / 12, q = e - nd * 12, src = q >> 2, part = q & 3, i = base + nd;
+			const __nv_bfloat16 *sp = src == 0 ? h : (src == 1 ? m1 : m2);
+			uint4 v = make_uint4(0u, 0u, 0u, 0u);
+			if (i < n) v = *reinterpret_cast<const uint4 *>(&sp[(size_t)i * W + part * 8]);
+			*reinterpret_cast<uint4 *>(&sA[nd * MPAD + src * W + part * 8]) = v;
+		}
+		__syncthreads();
+		float acc[4][4];
+		#pragma unroll
+		for (int nt = 0; nt < 4; nt++) {
+			acc[nt][0] = acc[nt][2] = sB[nt * 8 + c];
+			acc[nt][1] = acc[nt][3] = sB[nt * 8 + c + 1];
+		}
+		const __nv_bfloat16 *r0 = sA + (warp * 16 + g) * MPAD, *r1 = r0 + 8 * MPAD;
+		#pragma unroll
+		for (int ks = 0; ks < 3 * W / 16; ks++) {
+			const int k0 = ks * 16 + c;
+			unsigned a0 = ld_pair(r0 + k0), a1 = ld_pair(r1 + k0), a2 = ld_pair(r0 + k0 + 8), a3 = ld_pair(r1 + k0 + 8);
+			#pragma unroll
+			for (int nt = 0; nt < 4; nt++) {
+				const __nv_bfloat16 *bh = sWh + (nt * 8 + g) * MPAD + k0, *bl = sWl + (nt * 8 + g) * MPAD + k0;
+				mma_bf16(acc[nt], a0, a1, a2, a3, ld_pair(bh), ld_pair(bh + 8));
+				mma_bf16(acc[nt], a0, a1, a2, a3, ld_pair(bl), ld_pair(bl + 8));
+			}
+		}
+		#pragma unroll
+		for (int rr = 0; rr < 2; rr++) {
+			int nd = warp * 16 + g + 8 * rr, i = base + nd;
+			const __nv_bfloat16 *in = sA + nd * MPAD;
+			unsigned bits = 0;
+			#pragma unroll
+			for (int nt = 0; nt < 4; nt++) {
+				int col = nt * 8 + c;
+				float u0 = acc[nt][2 * rr], u1 = acc[nt][2 * rr + 1];
+				bits |= (u0 > 0.0f ? 1u : 0u) << col;
+				bits |= (u1 > 0.0f ? 1u : 0u) << (col + 1);
+				__nv_bfloat162 o;
+				o.x = __float2bfloat16_rn(__bfloat162float(in[col]) + (u0 > 0.0f ? u0 : 0.0f));
+				o.y = __float2bfloat16_rn(__bfloat162float(in[col + 1]) + (u1 > 0.0f ? u1 : 0.0f));
+				if (i < n) *reinterpret_cast<__nv_bfloat162 *>(&hout[(size_t)i * W + col]) = o;
+			}
+			bits |= __shfl_xor_sync(0xffffffffu, bits, 1);
+			bits |= __shfl_xor_sync(0xffffffffu, bits, 2);
+			if (mask && i < n && (lane & 3) == 0) mask[i] = bits;
+		}
+	}
+}
+
 // z_i = s (Wd . h_i + bd) dbar / d_i: a warp reduces the rows of 32
 // consecutive nodes (lane = feature), lane q keeps node q's sum and does its
 // FP64 scaling (once per node).
@@ -549,9 +644,17 @@ static int update_attrs()
 		FG_TRY(cudaFuncSetAttribute(k_gnn_update<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, UPD_SMEM));
 		FG_TRY(cudaFuncSetAttribute(k_gnn_update<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                            UPD_SMEM));
+		FG_TRY(cudaFuncSetAttribute(k_gnn_update_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, MMA_SMEM));
 		done = 1;
 	}
 	return 0;
+}
+// bf16 activations take the tensor-core update unless FEMGPU_GNN_MMA=0
+// (read at every launch: the FP32-core form stays available for comparison)
+static bool update_mma()
+{
+	const char *e = getenv("FEMGPU_GNN_MMA");
+	return !(e && e[0] == '0');
 }
 static int nb(long long n, int tpb, int cap)
 {
@@ -592,9 +695,20 @@ static int forward_t(fg_gnn *g, const double *r, double *z, int train, const int
 		int ml = train ? l : 0;
 		k_gnn_agg<TA><<<nb(8LL * n, 256, 32 * FG_SMS), 256, 0, s>>>(n, g->gptr, g->gcol, g->wA, g->wT, H[cur],
 		                                                            M1[ml], M2[ml], active);
-		k_gnn_update<TA><<<nb(n, UTILE, 4 * FG_SMS), UPD_TPB, UPD_SMEM, s>>>(n, g->theta + GNN_OFF_L(l), H[cur], M1[ml],
-		                                                             M2[ml], H[nxt],
-		                                                             train ? g->mask[l + 1] : nullptr, active);
+		if constexpr (std::is_same<TA, __nv_bfloat16>::value) {
+			if (update_mma())
+				k_gnn_update_mma<<<nb(n, UTILE, 4 * FG_SMS), UPD_TPB, MMA_SMEM, s>>>(
+					n, g->theta + GNN_OFF_L(l), H[cur], M1[ml], M2[ml], H[nxt],
+					train ? g->mask[l + 1] : nullptr, active);
+			else
+				k_gnn_update<TA><<<nb(n, UTILE, 4 * FG_SMS), UPD_TPB, UPD_SMEM, s>>>(
+					n, g->theta + GNN_OFF_L(l), H[cur], M1[ml], M2[ml], H[nxt],
+					train ? g->mask[l + 1] : nullptr, active);
+		} else {
+			k_gnn_update<TA><<<nb(n, UTILE, 4 * FG_SMS), UPD_TPB, UPD_SMEM, s>>>(n, g->theta + GNN_OFF_L(l), H[cur],
+			                                                             M1[ml], M2[ml], H[nxt],
+			                                                             train ? g->mask[l + 1] : nullptr, active);
+		}
 	}
 	int last = train ? GNN_LAYERS : (GNN_LAYERS & 1);
 	k_gnn_decode<TA><<<nb(n, 256, 16 * FG_SMS), 256, 0, s>>>(n, H[last], g->theta, g->stats, g->d, z,

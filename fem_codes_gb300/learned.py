@@ -122,6 +122,10 @@ class MeshGNN:
         self._check(self._L.femgpu_gnn_apply(self._h, r.ctypes.data_as(_vp), z.ctypes.data_as(_vp)), "apply")
         return z
 
+    def apply_dev(self, r_ptr, z_ptr):
+        """z = N(r) on device buffers (FP64, n entries each), on the context's stream."""
+        self._check(self._L.femgpu_gnn_apply_dev(self._h, _vp(r_ptr), _vp(z_ptr)), "apply_dev")
+
     def loss_grad(self, r, t):
         """Host-buffer forward + backward: (loss, grad, z)."""
         r = np.ascontiguousarray(r[: self.n], np.float64)
@@ -276,3 +280,56 @@ def evaluate(spec, gnn=None, kmax=50, tol=1e-8, lmax=400, stall_ratio=0.9, preco
     fell = pc == "LEARNED" and T.fell_back()
     T.close()
     return dict(iters=it, seconds=dt, rel=rel, converged=rel <= tol * 1.0001, fell_back=fell)
+
+
+def grid_csr(nx, seed=0):
+    """A 5-point upwinded advection-diffusion pattern on an nx x nx grid
+    (CSR, columns ascending in each row)."""
+    n = nx * nx
+    i = np.arange(n)
+    x, y = i % nx, i // nx
+    cols = [i, i - 1, i + 1, i - nx, i + nx]
+    ok = [x >= 0, x > 0, x < nx - 1, y > 0, y < nx - 1]
+    vals = [np.full(n, 4.4), np.full(n, -1.3), np.full(n, -0.7), np.full(n, -1.2), np.full(n, -0.8)]
+    nnz_row = np.sum(ok, axis=0)
+    IA = np.zeros(n + 1, np.int64)
+    IA[1:] = np.cumsum(nnz_row)
+    JA = np.concatenate([c[m] for c, m in zip(cols, ok)])
+    AA = np.concatenate([v[m] for v, m in zip(vals, ok)])
+    order = np.lexsort((JA, np.concatenate([i[m] for m in ok])))
+    return IA.astype(np.int32), JA[order].astype(np.int32), AA[order]
+
+
+def time_apply(nx, reps=20, warmup=3):
+    """CUDA-event time of one network application (bf16 activations) on the
+    nx x nx grid graph, inputs resident on the device; returns ms."""
+    import torch
+    IA, JA, AA = grid_csr(nx)
+    net = MeshGNN(init_params(7), bf16=True)
+    stream = torch.cuda.Stream()            # a stream of its own: the context keeps its stream when given NULL
+    net.set_stream(stream.cuda_stream)
+    net.attach_csr(IA, JA, AA)
+    r = torch.randn(net.n, dtype=torch.float64, device="cuda")
+    z = torch.empty_like(r)
+    torch.cuda.synchronize()
+    for _ in range(warmup):
+        net.apply_dev(r.data_ptr(), z.data_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        net.apply_dev(r.data_ptr(), z.data_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    net.close()
+    return e0.elapsed_time(e1) / reps
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="time one learned-preconditioner application on a grid graph")
+    ap.add_argument("--nx", type=int, default=1024)
+    ap.add_argument("--reps", type=int, default=20)
+    a = ap.parse_args()
+    print(json.dumps({"nodes": a.nx * a.nx, "ms_per_apply": time_apply(a.nx, a.reps)}))

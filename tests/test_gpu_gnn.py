@@ -132,3 +132,26 @@ def test_learned_falls_back_to_ilu_on_stall(gpu_lib):
         out = Ld.evaluate(spec, net, kmax=30, lmax=400, stall_ratio=1e-3)
         assert out["fell_back"] and out["converged"]
     net.close()
+
+
+def test_update_tensor_cores_match_fp32_cores(gpu_lib, system, monkeypatch):
+    """bf16 activations: the tensor-core update (mma.sync m16n8k16, weights
+    split into two bf16 parts, FP32 accumulation) against the FP32-core
+    update of the same network (FEMGPU_GNN_MMA=0).  The two differ only in
+    the accumulation order, so a stored bf16 activation can flip by one
+    rounding step: z within relative 1e-2 of each other, and both within
+    the oracle's bf16 bar."""
+    from fem_codes_gb300.learned import MeshGNN
+    IA, JA, AA, r, t = system
+    th = G.init(7)
+    _, _, zo = G.loss_and_grad(th, G.graph(IA, JA, AA), r, t, act_bf16=True, kind=MeshGNN.LOSSES["supervised"])
+    zs = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("FEMGPU_GNN_MMA", mode)
+        net = MeshGNN(th, bf16=True)
+        net.attach_csr(IA, JA, AA[: len(JA)])
+        zs[mode] = net.apply(r)
+        assert np.array_equal(zs[mode], net.apply(r))
+        net.close()
+    assert _rel(zs["1"], zs["0"]) < 1e-2
+    assert _rel(zs["1"], zo) < 2e-2 and _rel(zs["0"], zo) < 2e-2
